@@ -1,0 +1,250 @@
+/*
+ * posidonius_gb300.h -- C ABI of the GB300-native WHFast + tidal-effects path.
+ *
+ * The reference (Posidonius, Rust) has no C FFI: its surface is the JSON case
+ * format, the `posidonius start|resume` flow and the Rust entry points
+ * `Universe::new`, `WHFast::new`, the `Integrator` trait and the `Universe`
+ * methods.  Every entry point below replaces one of those; the comment of each
+ * cites the reference item it stands for (paths inside the posidonius project).
+ *
+ * Conventions
+ *  - Plain pointers and sizes only; no C++ or torch types cross this boundary.
+ *  - Every function returns a POSI_* status code (0 = success); physics events
+ *    that make the reference `panic!` are reported as codes instead.
+ *  - The library owns all device memory; the caller owns handles and must
+ *    release them with the matching destroy call.  One CUDA stream per handle;
+ *    calls on one handle are not thread-safe.
+ *  - All arithmetic is IEEE FP64.
+ */
+#ifndef POSIDONIUS_GB300_H
+#define POSIDONIUS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum posi_status {
+    POSI_OK = 0,
+    POSI_COMPLETED = 1,          /* src/integrator/whfast.rs:300-301 Err("Simulation completed") */
+    POSI_ERR_ARG = -1,           /* bad argument / null pointer */
+    POSI_ERR_IO = -2,            /* file missing or unreadable (src/integrator/output.rs:178-203) */
+    POSI_ERR_PARSE = -3,         /* malformed JSON case */
+    POSI_ERR_UNSUPPORTED = -4,   /* case uses an effect outside this path (Kaula, creep, disk, wind,
+                                    dynamic tides, Anderson/Newhall GR, non-WHFast integrator, ...) */
+    POSI_ERR_CUDA = -5,          /* CUDA runtime error or no device */
+    POSI_ERR_PHYSICS = -6,       /* a system hit a reference panic (see posi_system_status) */
+    POSI_ERR_STATE = -7          /* call not valid in this state (e.g. initialise a resumed run) */
+};
+
+/* Per-system status word (sys_i64[POSI_SI_STATUS]).  The low byte holds the
+ * fatal event that froze the system; higher bits are sticky warnings. */
+enum posi_system_status {
+    POSI_SYS_OK = 0,
+    POSI_SYS_ROCHE = 1,          /* src/particles/universe.rs:225-228 destroyed by close encounter */
+    POSI_SYS_COLLISION = 2,      /* src/particles/universe.rs:230-233 radii overlap */
+    POSI_SYS_EJECTED = 3,        /* src/particles/universe.rs:234-237 beyond MAX_DISTANCE */
+    POSI_SYS_ZERO_INERTIA = 4,   /* src/particles/common.rs:5-7 moment of inertia is zero */
+    POSI_SYS_BISECTION_LIMIT = 5,/* Kepler bisection did not close (src/integrator/whfast.rs:792-805) */
+    POSI_SYS_COMPLETED = 6,      /* time limit reached; the system is frozen */
+    POSI_SYS_FATAL_MASK = 0xff,
+    POSI_SYS_WARN_NONCONVERGED = 1 << 8,  /* src/integrator/whfast.rs:389-391 */
+    POSI_SYS_WARN_TIMESTEP = 1 << 9       /* src/integrator/whfast.rs:702-707 */
+};
+
+/* ---- flat system layout ---------------------------------------------------
+ * One system = sys_i64[POSI_SI_COUNT] + sys_f64[POSI_SF_COUNT]
+ *            + nmax bodies of body_i64[POSI_BI_COUNT] + body_f64[POSI_BF_COUNT].
+ * Host arrays are row-major: system s, body b, field f lives at
+ * body_f64[(s*nmax + b)*POSI_BF_COUNT + f].  Bodies keep the reference's
+ * particle order (the host may sit at any index).
+ */
+enum posi_coords { POSI_JACOBI = 0, POSI_DEMOCRATIC_HELIOCENTRIC = 1, POSI_WHDS = 2 };
+enum posi_effect_kind { POSI_EFFECT_DISABLED = 0, POSI_EFFECT_CENTRAL = 1, POSI_EFFECT_ORBITING = 2 };
+enum posi_evolution {
+    POSI_EVO_NON_EVOLVING = 0,
+    POSI_EVO_LECONTE2011 = 1,
+    POSI_EVO_BARAFFE1998 = 2,
+    POSI_EVO_BARAFFE2015 = 3,
+    POSI_EVO_LECONTE_CHABRIER2013 = 4     /* LeconteChabrier2013(false) */
+};
+
+enum posi_sys_i64_field {
+    POSI_SI_N = 0,               /* Universe::n_particles */
+    POSI_SI_HOST,                /* Hosts.index.most_massive (also tides/flattening/GR host) */
+    POSI_SI_COORDS,              /* WHFast.alternative_coordinates_type */
+    POSI_SI_TIDES,               /* ConsiderEffects.tides */
+    POSI_SI_FLAT,                /* ConsiderEffects.rotational_flattening */
+    POSI_SI_GR,                  /* ConsiderEffects.general_relativity (Kidder1995) */
+    POSI_SI_EVOLUTION,           /* ConsiderEffects.evolution */
+    POSI_SI_ITERATION,           /* WHFast.current_iteration */
+    POSI_SI_N_HIST,              /* WHFast.n_historic_snapshots */
+    POSI_SI_TIMESTEP_WARNING,    /* WHFast.timestep_warning */
+    POSI_SI_STATUS,              /* posi_system_status word */
+    POSI_SI_FAIL_STEP,           /* iteration at which a fatal event froze the system */
+    POSI_SI_FAIL_PAIR,           /* i*1024 + j of the offending pair */
+    POSI_SI_LAST_MIDPOINT_ITERS, /* midpoint iterations of the last half kick */
+    POSI_SI_COUNT
+};
+
+enum posi_sys_f64_field {
+    POSI_SF_DT = 0,              /* WHFast.time_step */
+    POSI_SF_HALF_DT,             /* WHFast.half_time_step */
+    POSI_SF_TIME,                /* WHFast.current_time */
+    POSI_SF_TIME_LIMIT,          /* Universe.time_limit */
+    POSI_SF_LAST_HIST,           /* WHFast.last_historic_snapshot_time */
+    POSI_SF_HIST_PERIOD,         /* WHFast.historic_snapshot_period */
+    POSI_SF_LAST_REC,            /* WHFast.last_recovery_snapshot_time */
+    POSI_SF_REC_PERIOD,          /* WHFast.recovery_snapshot_period */
+    POSI_SF_INITIAL_TIME,        /* Universe.initial_time */
+    POSI_SF_COUNT
+};
+
+enum posi_body_i64_field {
+    POSI_BI_TIDES_KIND = 0,      /* TidesEffect: posi_effect_kind (ConstantTimeLag model) */
+    POSI_BI_FLAT_KIND,           /* RotationalFlatteningEffect: posi_effect_kind (OblateSpheroid) */
+    POSI_BI_GR_KIND,             /* GeneralRelativityEffect: posi_effect_kind (Kidder1995) */
+    POSI_BI_EVO_TYPE,            /* posi_evolution */
+    POSI_BI_EVO_OFFSET,          /* offset of this body's tables in `tables` */
+    POSI_BI_EVO_LEN,             /* rows per table (time, radius, rg2, love: 4*len doubles) */
+    POSI_BI_EVO_LEFT,            /* Evolver.left_index */
+    POSI_BI_COUNT
+};
+
+enum posi_body_f64_field {
+    POSI_BF_MASS = 0, POSI_BF_MASS_G, POSI_BF_RADIUS, POSI_BF_RG2, POSI_BF_MOI,
+    POSI_BF_PX, POSI_BF_PY, POSI_BF_PZ,          /* inertial_position */
+    POSI_BF_VX, POSI_BF_VY, POSI_BF_VZ,          /* inertial_velocity */
+    POSI_BF_AX, POSI_BF_AY, POSI_BF_AZ,          /* inertial_acceleration (Newtonian) */
+    POSI_BF_LX, POSI_BF_LY, POSI_BF_LZ,          /* angular_momentum */
+    POSI_BF_SX, POSI_BF_SY, POSI_BF_SZ,          /* spin */
+    POSI_BF_NSV2,                                /* norm_spin_vector_2 */
+    POSI_BF_EVX, POSI_BF_EVY, POSI_BF_EVZ,       /* WHFast.inertial_velocity_errors */
+    POSI_BF_ELX, POSI_BF_ELY, POSI_BF_ELZ,       /* WHFast.particle_angular_momentum_errors */
+    POSI_BF_SIGMA,                               /* tides scaled_dissipation_factor */
+    POSI_BF_K2,                                  /* tides (ConstantTimeLag) love_number */
+    POSI_BF_K2F,                                 /* flattening (OblateSpheroid) love_number */
+    POSI_BF_ADDAX, POSI_BF_ADDAY, POSI_BF_ADDAZ, /* inertial_additional_acceleration */
+    POSI_BF_DLX, POSI_BF_DLY, POSI_BF_DLZ,       /* dangular_momentum_dt */
+    POSI_BF_DENERGY_DT,                          /* tides denergy_dt (history output) */
+    POSI_BF_LAG_ANGLE,                           /* tides lag_angle (history output) */
+    POSI_BF_COUNT
+};
+
+/* Largest body count of the batched kernels. */
+#define POSI_MAX_BODIES 32
+
+/* Arithmetic modes.  EXACT keeps the reference's operation order with no FMA
+ * contraction and reproduces the Rust FP64 results bit for bit; FAST lets the
+ * compiler contract FMAs and shares reciprocals (<= 1e-12 relative per step). */
+enum posi_mode { POSI_MODE_EXACT = 0, POSI_MODE_FAST = 1 };
+
+/* Thread mappings of the batched kernel (bodies per lane group). */
+enum posi_mapping {
+    POSI_MAP_AUTO = 0,           /* autotuned per body-count bucket */
+    POSI_MAP_THREAD = 1,         /* one thread per system */
+    POSI_MAP_LANES4 = 4,         /* 4 lanes per system, lane-strided bodies */
+    POSI_MAP_LANES8 = 8,
+    POSI_MAP_LANES16 = 16,
+    POSI_MAP_WARP = 32           /* one warp per system */
+};
+
+typedef struct posi_handle posi_handle;
+typedef struct posi_batch posi_batch;
+
+/* ---- library ----------------------------------------------------------- */
+const char* posi_version(void);
+const char* posi_status_string(int status);
+/* Number of CUDA devices visible (0 when none); never allocates. */
+int posi_device_count(void);
+
+/* ---- single system (the drop-in path: one system, one launch per step) -- */
+
+/* src/integrator/output.rs:178-241 restore_snapshot + deserialize_json_snapshot:
+ * read a WHFast JSON case (or JSON recovery snapshot). */
+posi_handle* posi_universe_from_json(const char* path, int mode, int* status);
+
+/* src/particles/universe.rs:73-175 Universe::new + src/integrator/whfast.rs:143-165
+ * WHFast::new, from one system in the flat layout (nmax = n). */
+posi_handle* posi_universe_from_arrays(const int64_t* sys_i64, const double* sys_f64,
+                                       const int64_t* body_i64, const double* body_f64,
+                                       const double* tables, int64_t n_tables,
+                                       int mode, int* status);
+
+void posi_destroy(posi_handle* h);
+
+/* src/integrator/mod.rs:16-27 Integrator::get_n_particles / get_current_time /
+ * get_n_historic_snapshots. */
+int posi_get_n_particles(const posi_handle* h, int64_t* n);
+int posi_get_current_time(const posi_handle* h, double* t);
+int posi_get_n_historic_snapshots(const posi_handle* h, int64_t* n);
+
+/* src/integrator/whfast.rs:187-224 set_time_limit / set_snapshot_periods
+ * (non-positive values keep the current setting). */
+int posi_set_time_limit(posi_handle* h, double time_limit);
+int posi_set_snapshot_periods(posi_handle* h, double historic_period, double recovery_period);
+
+/* src/integrator/whfast.rs:226-233 initialize_physical_values
+ * (+ src/particles/universe.rs:177-196 calculate_roche_radiuses). */
+int posi_initialize_physical_values(posi_handle* h);
+
+/* src/integrator/whfast.rs:235-305 Integrator::iterate, n_steps times (one
+ * kernel launch per step).  Returns POSI_COMPLETED after the step that makes
+ * current_time + time_step exceed time_limit, like Err("Simulation completed").
+ * *steps_done receives the steps performed; *recovery_trigger is set when the
+ * last step reported a recovery-snapshot trigger (Ok(true)). */
+int posi_iterate(posi_handle* h, int64_t n_steps, int64_t* steps_done, int* recovery_trigger);
+
+/* src/particles/universe.rs:198-303 gravity_calculate_acceleration
+ * (ignore_terms: 0 None, 1 WHFastOne, 2 WHFastTwo). */
+int posi_gravity_calculate_acceleration(posi_handle* h, int ignore_terms);
+
+/* src/particles/universe.rs:318-351 inertial_to_heliocentric followed by
+ * src/particles/universe.rs:428-538 calculate_additional_effects. */
+int posi_calculate_additional_effects(posi_handle* h, double current_time, int evolution,
+                                      int dangular_momentum_dt, int accelerations);
+
+/* Copy the state to/from the host in the flat layout (nmax = n). */
+int posi_get_state(const posi_handle* h, int64_t* sys_i64, double* sys_f64,
+                   int64_t* body_i64, double* body_f64);
+int posi_set_state(posi_handle* h, const int64_t* sys_i64, const double* sys_f64,
+                   const int64_t* body_i64, const double* body_f64);
+
+/* ---- batched ensembles (many independent systems, one persistent kernel) -- */
+
+/* nmax >= every system's n, nmax <= POSI_MAX_BODIES.  The arrays are copied to
+ * the device; mapping selects the thread layout (POSI_MAP_AUTO = autotuned). */
+posi_batch* posi_batch_create(int64_t n_systems, int64_t nmax,
+                              const int64_t* sys_i64, const double* sys_f64,
+                              const int64_t* body_i64, const double* body_f64,
+                              const double* tables, int64_t n_tables,
+                              int mode, int mapping, int* status);
+void posi_batch_destroy(posi_batch* b);
+
+/* initialize_physical_values for every system (whfast.rs:226-233). */
+int posi_batch_initialize_physical_values(posi_batch* b);
+
+/* Advance every live system by n_steps WHFast steps, steps_per_launch steps per
+ * persistent-kernel launch; the launches are captured once in a CUDA graph and
+ * replayed.  Systems that complete or hit a fatal event are frozen. */
+int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch);
+
+/* Host <-> device copies of the whole ensemble (flat layout). */
+int posi_batch_get_state(const posi_batch* b, int64_t* sys_i64, double* sys_f64,
+                         int64_t* body_i64, double* body_f64);
+int posi_batch_set_state(posi_batch* b, const int64_t* sys_i64, const double* sys_f64,
+                         const int64_t* body_i64, const double* body_f64);
+
+/* Mapping chosen for systems with n bodies (after autotuning), or -1. */
+int posi_batch_mapping_for(const posi_batch* b, int64_t n);
+
+/* Device time of the last posi_batch_iterate in milliseconds (CUDA events on
+ * the batch's stream) and the number of kernel launches it made. */
+int posi_batch_last_timing(const posi_batch* b, double* ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* POSIDONIUS_GB300_H */

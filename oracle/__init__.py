@@ -1,0 +1,93 @@
+"""CPU oracle for the WHFast + tidal-effects path (test infrastructure only).
+
+``whfast_oracle.cpp`` restates the reference's Rust FP64 functions in C++ in
+the same operation order; ``case_json.py`` reads the reference's JSON cases.
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py``
+load this package -- as the checker and the CPU baseline, never as the
+measured product path.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from posidonius_gb300 import layout as L
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+LIB_FLOPS = os.path.join(BUILD, "liboracle_flops.so")
+
+ITERATE, GRAVITY, ADDITIONAL_EFFECTS, INITIALIZE = 0, 1, 2, 3
+
+
+def build(force=False):
+    """Compile the oracle with make (g++, -ffp-contract=off)."""
+    if force or not (os.path.exists(LIB) and os.path.exists(LIB_FLOPS)):
+        subprocess.check_call(["make", "-s", "-C", HERE, "-j2"])
+    else:
+        subprocess.check_call(["make", "-s", "-C", HERE, "-j2"])
+
+
+_libs = {}
+
+
+def _lib(flops=False):
+    path = LIB_FLOPS if flops else LIB
+    if path not in _libs:
+        if not os.path.exists(path):
+            build()
+        lib = ctypes.CDLL(path)
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        f64p = ctypes.POINTER(ctypes.c_double)
+        lib.oracle_run.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, i64p, f64p, i64p, f64p, f64p,
+                                   f64p, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                   i64p, i64p]
+        lib.oracle_run.restype = ctypes.c_int
+        lib.oracle_constant.argtypes = [ctypes.c_int]
+        lib.oracle_constant.restype = ctypes.c_double
+        if flops:
+            lib.oracle_flops.argtypes = [i64p, ctypes.c_int]
+        _libs[path] = lib
+    return _libs[path]
+
+
+def _p(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def as_ensemble(case):
+    """Accept a single-system dict (case_json.load_case) or a stacked ensemble."""
+    if "n_sys" in case:
+        return case
+    from .case_json import stack
+    return stack([case])
+
+
+def run(ens, op=ITERATE, max_steps=0, init_physical=False, arg=0, t_arg=0.0, nthreads=1, flops=False):
+    """Run `op` in place on a copy of the ensemble; returns (ensemble, steps_done, result[, flops])."""
+    ens = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in as_ensemble(ens).items()}
+    lib = _lib(flops)
+    ns, nmax = ens["n_sys"], ens["nmax"]
+    for k, dt in (("sys_i64", np.int64), ("sys_f64", np.float64), ("body_i64", np.int64),
+                  ("body_f64", np.float64), ("tables", np.float64), ("roche", np.float64)):
+        ens[k] = np.ascontiguousarray(ens[k], dtype=dt)
+    steps = np.zeros(ns, dtype=np.int64)
+    result = np.zeros(ns, dtype=np.int64)
+    if flops:
+        cnt = np.zeros(3, dtype=np.int64)
+        lib.oracle_flops(_p(cnt, ctypes.c_int64), 1)
+    lib.oracle_run(op, ns, nmax, _p(ens["sys_i64"], ctypes.c_int64), _p(ens["sys_f64"], ctypes.c_double),
+                   _p(ens["body_i64"], ctypes.c_int64), _p(ens["body_f64"], ctypes.c_double),
+                   _p(ens["tables"], ctypes.c_double), _p(ens["roche"], ctypes.c_double), int(max_steps),
+                   int(init_physical), int(arg), float(t_arg), 1 if flops else int(nthreads),
+                   _p(steps, ctypes.c_int64), _p(result, ctypes.c_int64))
+    if flops:
+        lib.oracle_flops(_p(cnt, ctypes.c_int64), 1)
+        return ens, steps, result, cnt
+    return ens, steps, result
+
+
+def constant(which):
+    return _lib().oracle_constant(which)

@@ -1,0 +1,214 @@
+"""Reference JSON case -> flat system layout (test infrastructure).
+
+Reads a Posidonius WHFast case / recovery snapshot written by serde
+(``src/integrator/output.rs:28-54`` write, ``:205-241`` read; the layout is
+the serde form of ``WHFast`` in ``src/integrator/whfast.rs:99-120``) with
+Python's ``json`` module (correctly rounded float parsing) and packs it into
+the flat layout declared in ``include/posidonius_gb300.h``.
+
+This is the checker's own reader: the product parses JSON in C++
+(``posi_universe_from_json``); tests compare the two.
+"""
+import json
+
+import numpy as np
+
+from posidonius_gb300 import layout as L
+
+EVOLUTION_CODES = {
+    "NonEvolving": L.EVO_NON_EVOLVING,
+    "Leconte2011": L.EVO_LECONTE2011,
+    "Baraffe1998": L.EVO_BARAFFE1998,
+    "Baraffe2015": L.EVO_BARAFFE2015,
+}
+
+
+class Unsupported(ValueError):
+    """The case uses a part of Posidonius outside the WHFast/CTL/oblate/Kidder path."""
+
+
+def _evolution_code(evo):
+    if isinstance(evo, str):
+        if evo in EVOLUTION_CODES:
+            return EVOLUTION_CODES[evo]
+        raise Unsupported(f"evolution {evo}")
+    (name, arg), = evo.items()
+    if name == "LeconteChabrier2013":
+        if arg:
+            raise Unsupported("LeconteChabrier2013(true) dynamical tides")
+        return L.EVO_LECONTE_CHABRIER2013
+    if name in EVOLUTION_CODES:
+        return EVOLUTION_CODES[name]
+    raise Unsupported(f"evolution {name}")
+
+
+def _effect(effect, model_key):
+    """(kind, params) of a serde externally-tagged effect enum."""
+    if effect == "Disabled":
+        return L.EFFECT_DISABLED, None
+    if effect == "OrbitingBody" or effect == {"OrbitingBody": None}:
+        return L.EFFECT_ORBITING, None
+    (tag, inner), = effect.items()
+    kind = {"CentralBody": L.EFFECT_CENTRAL, "OrbitingBody": L.EFFECT_ORBITING}[tag]
+    if model_key is None:
+        return kind, inner
+    if not isinstance(inner, dict) or model_key not in inner:
+        raise Unsupported(f"model {inner}")
+    return kind, inner[model_key]
+
+
+def load_case(path_or_dict):
+    """Return a dict of flat arrays for one system (nmax = n)."""
+    d = path_or_dict
+    if not isinstance(d, dict):
+        with open(d) as f:
+            d = json.load(f)
+    if "alternative_coordinates_type" not in d:
+        raise Unsupported("not a WHFast case")
+    u = d["universe"]
+    n = int(u["n_particles"])
+    ce = u["consider_effects"]
+    if ce["disk"] or ce["wind"]:
+        raise Unsupported("disk/wind effects")
+    gr_impl = u["general_relativity_implementation"]
+    if ce["general_relativity"] and gr_impl != "Kidder1995":
+        raise Unsupported(f"general relativity {gr_impl}")
+    hosts = u["hosts"]
+    host = int(hosts["index"]["most_massive"])
+    for eff in ("tides", "rotational_flattening"):
+        if ce[eff] and int(hosts["index"][eff]) != host:
+            raise Unsupported(f"{eff} host is not the most massive body")
+
+    si = np.zeros(L.SI_COUNT, dtype=np.int64)
+    sf = np.zeros(L.SF_COUNT, dtype=np.float64)
+    bi = np.zeros((n, L.BI_COUNT), dtype=np.int64)
+    bf = np.zeros((n, L.BF_COUNT), dtype=np.float64)
+    si[L.SI_N] = n
+    si[L.SI_HOST] = host
+    si[L.SI_COORDS] = {"Jacobi": L.JACOBI, "DemocraticHeliocentric": L.DEMOCRATIC_HELIOCENTRIC,
+                       "WHDS": L.WHDS}[d["alternative_coordinates_type"]]
+    si[L.SI_TIDES] = int(ce["tides"])
+    si[L.SI_FLAT] = int(ce["rotational_flattening"])
+    si[L.SI_GR] = int(ce["general_relativity"])
+    si[L.SI_EVOLUTION] = int(ce["evolution"])
+    si[L.SI_ITERATION] = int(d["current_iteration"])
+    si[L.SI_N_HIST] = int(d["n_historic_snapshots"])
+    si[L.SI_TIMESTEP_WARNING] = int(d["timestep_warning"])
+    sf[L.SF_DT] = d["time_step"]
+    sf[L.SF_HALF_DT] = d["half_time_step"]
+    sf[L.SF_TIME] = d["current_time"]
+    sf[L.SF_TIME_LIMIT] = u["time_limit"]
+    sf[L.SF_LAST_HIST] = d["last_historic_snapshot_time"]
+    sf[L.SF_HIST_PERIOD] = d["historic_snapshot_period"]
+    sf[L.SF_LAST_REC] = d["last_recovery_snapshot_time"]
+    sf[L.SF_REC_PERIOD] = d["recovery_snapshot_period"]
+    sf[L.SF_INITIAL_TIME] = u["initial_time"]
+
+    tables = []
+    off = 0
+    for b in range(n):
+        p = u["particles"][b]
+        ev = u["particles_evolvers"][b]
+        tk, tparams = _effect(p["tides"]["effect"], "ConstantTimeLag")
+        fk, fparams = _effect(p["rotational_flattening"]["effect"], "OblateSpheroid")
+        gk, gimpl = _effect(p["general_relativity"]["effect"], None)
+        if p["wind"]["effect"] != "Disabled" or p["disk"]["effect"] != "Disabled":
+            if ce["wind"] or ce["disk"]:
+                raise Unsupported("wind/disk body")
+        if gk == L.EFFECT_CENTRAL and gimpl != "Kidder1995" and ce["general_relativity"]:
+            raise Unsupported(f"general relativity {gimpl}")
+        if ce["tides"] and b != host and tk != L.EFFECT_ORBITING:
+            # The reference's host torque loop visits every body and divides
+            # by the stale distance 0 of a non-orbiting one (NaN spin).
+            raise Unsupported("tides on with a non-orbiting body")
+        # Outputs of disabled effects are summed into dL/dt by the reference
+        # (src/particles/universe.rs:589-591); they must be zero here.
+        for eff, on in (("tides", ce["tides"]), ("rotational_flattening", ce["rotational_flattening"]),
+                        ("general_relativity", ce["general_relativity"])):
+            if not on:
+                o = p[eff]["parameters"]["output"]["dangular_momentum_dt"]
+                if o["x"] != 0.0 or o["y"] != 0.0 or o["z"] != 0.0:
+                    raise Unsupported(f"stale {eff} torque output")
+        if b == host:
+            hv = p["heliocentric_velocity"]
+            if hv["x"] != 0.0 or hv["y"] != 0.0 or hv["z"] != 0.0:
+                raise Unsupported("host with non-zero heliocentric velocity")
+        bi[b, L.BI_TIDES_KIND] = tk
+        bi[b, L.BI_FLAT_KIND] = fk
+        bi[b, L.BI_GR_KIND] = gk
+        evo_code = _evolution_code(p["evolution"])
+        evo_ev = _evolution_code(ev["evolution"])
+        if evo_code != evo_ev:
+            raise Unsupported("particle and evolver evolution types differ")
+        bi[b, L.BI_EVO_TYPE] = evo_code
+        bi[b, L.BI_EVO_LEFT] = int(ev["left_index"])
+        nrow = len(ev["time"])
+        if evo_code != L.EVO_NON_EVOLVING and nrow > 0:
+            block = np.zeros(4 * nrow)
+            block[0:nrow] = ev["time"]
+            block[nrow:2 * nrow] = ev["radius"]
+            if len(ev["radius_of_gyration_2"]) == nrow:
+                block[2 * nrow:3 * nrow] = ev["radius_of_gyration_2"]
+            if len(ev["love_number"]) == nrow:
+                block[3 * nrow:4 * nrow] = ev["love_number"]
+            bi[b, L.BI_EVO_OFFSET] = off
+            bi[b, L.BI_EVO_LEN] = nrow
+            tables.append(block)
+            off += 4 * nrow
+        F = bf[b]
+        F[L.BF_MASS] = p["mass"]
+        F[L.BF_MASS_G] = p["mass_g"]
+        F[L.BF_RADIUS] = p["radius"]
+        F[L.BF_RG2] = p["radius_of_gyration_2"]
+        F[L.BF_MOI] = p["moment_of_inertia"]
+        for k, key in enumerate(("x", "y", "z")):
+            F[L.BF_PX + k] = p["inertial_position"][key]
+            F[L.BF_VX + k] = p["inertial_velocity"][key]
+            F[L.BF_AX + k] = p["inertial_acceleration"][key]
+            F[L.BF_LX + k] = p["angular_momentum"][key]
+            F[L.BF_SX + k] = p["spin"][key]
+            F[L.BF_EVX + k] = d["inertial_velocity_errors"][b][key]
+            F[L.BF_ELX + k] = d["particle_angular_momentum_errors"][b][key]
+            F[L.BF_ADDAX + k] = p["inertial_additional_acceleration"][key]
+            F[L.BF_DLX + k] = p["dangular_momentum_dt"][key]
+        F[L.BF_NSV2] = p["norm_spin_vector_2"]
+        F[L.BF_SIGMA] = p["tides"]["parameters"]["internal"]["scaled_dissipation_factor"]
+        F[L.BF_K2] = tparams["love_number"] if tparams else 0.0
+        F[L.BF_K2F] = fparams["love_number"] if fparams else 0.0
+        F[L.BF_DENERGY_DT] = p["tides"]["parameters"]["internal"]["denergy_dt"]
+        F[L.BF_LAG_ANGLE] = p["tides"]["parameters"]["internal"]["lag_angle"]
+    # calculate_roche_radiuses fills the first n*n entries in rows of n
+    # (src/particles/universe.rs:177-196)
+    rr = u["roche_radiuses"]
+    roche = np.zeros((n, n), dtype=np.float64)
+    if len(rr) >= n * n:
+        roche = np.array(rr[: n * n], dtype=np.float64).reshape(n, n)
+    tab = np.concatenate(tables) if tables else np.zeros(1)
+    return {"sys_i64": si, "sys_f64": sf, "body_i64": bi, "body_f64": bf, "tables": tab,
+            "roche": roche, "n": n}
+
+
+def stack(cases, nmax=None):
+    """Stack single-system dicts into one padded ensemble (nmax bodies)."""
+    nmax = nmax or max(c["n"] for c in cases)
+    ns = len(cases)
+    si = np.zeros((ns, L.SI_COUNT), dtype=np.int64)
+    sf = np.zeros((ns, L.SF_COUNT), dtype=np.float64)
+    bi = np.zeros((ns, nmax, L.BI_COUNT), dtype=np.int64)
+    bf = np.zeros((ns, nmax, L.BF_COUNT), dtype=np.float64)
+    roche = np.zeros((ns, nmax, nmax), dtype=np.float64)
+    tabs = []
+    off = 0
+    for k, c in enumerate(cases):
+        n = c["n"]
+        si[k] = c["sys_i64"]
+        sf[k] = c["sys_f64"]
+        bi[k, :n] = c["body_i64"]
+        bf[k, :n] = c["body_f64"]
+        roche[k, :n, :n] = c["roche"]
+        evolving = bi[k, :n, L.BI_EVO_LEN] > 0
+        bi[k, :n, L.BI_EVO_OFFSET] = np.where(evolving, bi[k, :n, L.BI_EVO_OFFSET] + off, 0)
+        tabs.append(c["tables"])
+        off += len(c["tables"])
+    return {"sys_i64": si, "sys_f64": sf, "body_i64": bi, "body_f64": bf,
+            "tables": np.concatenate(tabs), "roche": roche, "nmax": nmax, "n_sys": ns}

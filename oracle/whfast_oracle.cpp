@@ -1,0 +1,1693 @@
+// whfast_oracle.cpp -- CPU restatement of Posidonius's WHFast + additional
+// effects path in FP64.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker: tests/, the smoke test
+// and the CPU-baseline / reference legs of bench.py load it to produce the
+// expected results and the CPU timing.  The product library never links,
+// loads or calls it.
+//
+// It restates, function by function and in the same floating-point operation
+// order, the reference functions cited beside each routine below (paths are
+// inside the posidonius project).  It must be compiled without FMA
+// contraction (-ffp-contract=off), which is Rust's default, so that every
+// +, -, *, / and sqrt rounds exactly as in the Rust binary.  `powi` follows
+// LLVM's expansion of llvm.powi (binary exponentiation, the same product
+// order as compiler-rt's __powidf2).
+//
+// Parity pin: tests/test_oracle_golden.py runs this restatement on the
+// reference's own golden cases (tests/data/<case>/case.json of the reference)
+// and checks the final inertial positions, velocities and accelerations
+// against tests/data/<case>/particle_*.json at the reference's 1e-14 absolute
+// tolerance (tests/common/universe.rs:47-72 of the reference).
+//
+// Built with -DORACLE_COUNT_FLOPS the same code counts every FP64 operation
+// (+ - * / sqrt each count 1), which gives the algorithmic flops per step.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "../include/posidonius_gb300.h"
+
+namespace orc {
+
+// ---------------------------------------------------------------------------
+// Arithmetic type: plain double, or a counting wrapper.
+// ---------------------------------------------------------------------------
+#ifdef ORACLE_COUNT_FLOPS
+static thread_local int64_t g_flops = 0, g_divs = 0, g_sqrts = 0;
+struct real {
+    double v;
+    real() : v(0.) {}
+    real(double x) : v(x) {}
+    explicit operator double() const { return v; }
+};
+static inline real operator+(real a, real b) { ++g_flops; return real(a.v + b.v); }
+static inline real operator-(real a, real b) { ++g_flops; return real(a.v - b.v); }
+static inline real operator*(real a, real b) { ++g_flops; return real(a.v * b.v); }
+static inline real operator/(real a, real b) { ++g_flops; ++g_divs; return real(a.v / b.v); }
+static inline real operator-(real a) { return real(-a.v); }
+static inline real& operator+=(real& a, real b) { a = a + b; return a; }
+static inline real& operator-=(real& a, real b) { a = a - b; return a; }
+static inline real& operator*=(real& a, real b) { a = a * b; return a; }
+static inline real& operator/=(real& a, real b) { a = a / b; return a; }
+static inline bool operator<(real a, real b) { return a.v < b.v; }
+static inline bool operator>(real a, real b) { return a.v > b.v; }
+static inline bool operator<=(real a, real b) { return a.v <= b.v; }
+static inline bool operator>=(real a, real b) { return a.v >= b.v; }
+static inline bool operator==(real a, real b) { return a.v == b.v; }
+static inline bool operator!=(real a, real b) { return a.v != b.v; }
+static inline real rsqrt_(real a) { ++g_flops; ++g_sqrts; return real(std::sqrt(a.v)); }
+static inline real rabs(real a) { return real(std::fabs(a.v)); }
+static inline real rfloor(real a) { return real(std::floor(a.v)); }
+static inline bool risnan(real a) { return std::isnan(a.v); }
+static inline double dv(real a) { return a.v; }
+#else
+typedef double real;
+static inline real rsqrt_(real a) { return std::sqrt(a); }
+static inline real rabs(real a) { return std::fabs(a); }
+static inline real rfloor(real a) { return std::floor(a); }
+static inline bool risnan(real a) { return std::isnan(a); }
+static inline double dv(real a) { return a; }
+#endif
+
+// LLVM's llvm.powi expansion for a constant exponent (SelectionDAG ExpandPowI,
+// identical product order to compiler-rt __powidf2): square-and-multiply from
+// the low bit, the first factor taken without multiplying by 1.
+static inline real powi(real x, int n) {
+    real res = 0.;
+    bool have = false;
+    real cur = x;
+    unsigned v = (unsigned)n;
+    while (v) {
+        if (v & 1u) {
+            if (have) res = res * cur; else { res = cur; have = true; }
+        }
+        v >>= 1;
+        if (v) cur = cur * cur;
+    }
+    return res;
+}
+
+// src/constants.rs:20-61
+static const int WHFAST_NMAX_QUART = 64;
+static const int WHFAST_NMAX_NEWT = 32;
+static const double DBL_EPSILON_ = 2.2204460492503131e-16;
+static const double DBL_EPSILON_2 = DBL_EPSILON_ * DBL_EPSILON_;
+static const int IMPLICIT_MIDPOINT_MIN_ITER = 3;
+static const int IMPLICIT_MIDPOINT_MAX_ITER = 10;
+static const double PI = 3.141592653589793;
+static const double DAY = 24. * 3600.;
+static const double M_SUN = 1.9818e30;
+static const double G_SI = 6.67428e-11;
+static const double AU = 1.49597870700e11;
+static const double SPEED_OF_LIGHT = (2.99792458e8 / AU) * DAY;
+static const double SPEED_OF_LIGHT_2 = SPEED_OF_LIGHT * SPEED_OF_LIGHT;
+static const double G = G_SI / (AU * AU * AU) * M_SUN * (DAY * DAY);
+static const double K2 = G;
+static const double MAX_DISTANCE = 100.;
+static const double MAX_DISTANCE_2 = MAX_DISTANCE * MAX_DISTANCE;
+
+struct V3 { real x, y, z; };
+
+// src/effects/tides/common.rs:35-79 (ConstantTimeLag subset)
+struct Tides {
+    int kind = POSI_EFFECT_DISABLED;
+    real love_number = 0.;           // ConstantTimeLagParameters.love_number
+    real distance = 0., radial_velocity = 0., scaled_dissipation_factor = 0.;
+    real rscal_star = 0., rscal_planet = 0.;
+    real ortho_star = 0., ortho_planet = 0., radial = 0., radial_diss_pm = 0.;
+    real denergy_dt = 0., lag_angle = 0.;
+    V3 out_acc{0., 0., 0.}, out_dldt{0., 0., 0.};
+    V3 pos{0., 0., 0.}, vel{0., 0., 0.};
+};
+// src/effects/rotational_flattening/common.rs:8-62 (OblateSpheroid subset)
+struct Flat {
+    int kind = POSI_EFFECT_DISABLED;
+    real love_number = 0.;
+    real distance = 0., rscal_star = 0., rscal_planet = 0., radial = 0.;
+    real factor_star = 0., factor_planet = 0., ortho_star = 0., ortho_planet = 0.;
+    V3 out_acc{0., 0., 0.}, out_dldt{0., 0., 0.};
+    V3 pos{0., 0., 0.}, vel{0., 0., 0.};
+};
+// src/effects/general_relativity.rs:10-59 (Kidder1995 subset)
+struct GR {
+    int kind = POSI_EFFECT_DISABLED;
+    real distance = 0., radial_velocity = 0., norm_v = 0., norm_v2 = 0., factor = 0.;
+    V3 out_acc{0., 0., 0.}, out_dldt{0., 0., 0.};
+    V3 pos{0., 0., 0.}, vel{0., 0., 0.};
+};
+// src/particles/particle.rs:16-52
+struct Particle {
+    int id = 0;
+    real mass = 0., mass_g = 0., radius = 0.;
+    V3 r{0., 0., 0.}, v{0., 0., 0.}, a{0., 0., 0.}, a_add{0., 0., 0.};
+    V3 hr{0., 0., 0.}, hv{0., 0., 0.};
+    real hd = 0., hvr = 0., hnv = 0., hnv2 = 0.;
+    V3 spin{0., 0., 0.};
+    real nsv2 = 0.;
+    V3 L{0., 0., 0.}, dLdt{0., 0., 0.};
+    real rg2 = 0., moi = 0.;
+    Tides tides;
+    Flat flat;
+    GR gr;
+    V3 wind_dldt{0., 0., 0.};   // wind is disabled on this path: always zero
+    int evolution = POSI_EVO_NON_EVOLVING;
+};
+// src/effects/evolution.rs:20-28
+struct Evolver {
+    int type = POSI_EVO_NON_EVOLVING;
+    const double *time = nullptr, *radius = nullptr, *rg2 = nullptr, *love = nullptr;
+    int64_t len = 0;
+    int64_t left_index = 0;
+};
+// src/integrator/whfast.rs:123-130
+struct AltCoords {
+    real mass = 0., mass_g = 0.;
+    V3 pos{0., 0., 0.}, vel{0., 0., 0.}, acc{0., 0., 0.};
+};
+
+// src/integrator/whfast.rs:99-120 + src/particles/universe.rs:50-63
+struct Sim {
+    int n = 0, host = 0, coords = POSI_JACOBI;
+    bool tides = false, flat = false, gr = false, evolution = false;
+    real dt = 0., half_dt = 0., t = 0., time_limit = 0.;
+    real last_hist = -1., hist_period = 0., last_rec = -1., rec_period = 0.;
+    int64_t iteration = 0, n_hist = 0, timestep_warning = 0, status = 0, fail_step = 0, fail_pair = 0;
+    int64_t last_midpoint_iters = 0;
+    std::vector<Particle> p;
+    std::vector<Evolver> ev;
+    std::vector<AltCoords> alt;
+    std::vector<V3> errv, errL;
+    std::vector<real> roche;
+    bool fatal() const { return (status & POSI_SYS_FATAL_MASK) != 0; }
+};
+
+// ---------------------------------------------------------------------------
+// src/particles/common.rs:3-14 calculate_spin
+// ---------------------------------------------------------------------------
+static void calculate_spin(Sim& s) {
+    for (int i = 0; i < s.n; ++i) {
+        Particle& q = s.p[i];
+        if (q.moi == 0.) {
+            s.status = (s.status & ~int64_t(POSI_SYS_FATAL_MASK)) | POSI_SYS_ZERO_INERTIA;
+            return;
+        }
+        q.spin.x = q.L.x / q.moi;
+        q.spin.y = q.L.y / q.moi;
+        q.spin.z = q.L.z / q.moi;
+        q.nsv2 = powi(q.spin.x, 2) + powi(q.spin.y, 2) + powi(q.spin.z, 2);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// src/tools.rs:884-907 find_indices_around_target_value and
+// src/tools.rs:840-860 linear_interpolation
+// ---------------------------------------------------------------------------
+static void find_indices_around_target_value(const double* data, int64_t ndata, double target,
+                                             int64_t* left, int64_t* right) {
+    int64_t last = ndata - 1;
+    int64_t pos = -1;
+    for (int64_t k = 0; k < ndata; ++k) {
+        if (data[k] > target) { pos = k; break; }
+    }
+    if (pos < 0) {
+        if (data[last] > target) { *left = 0; *right = 0; } else { *left = last; *right = last; }
+    } else if (pos == 0) {
+        *left = 0; *right = 0;
+    } else {
+        *left = pos - 1; *right = pos;
+    }
+}
+
+static real linear_interpolation(real target_x, const double* x, const double* y, int64_t n, int64_t* left_out) {
+    int64_t left, right;
+    find_indices_around_target_value(x, n, dv(target_x), &left, &right);
+    real target_y;
+    if (left == right) {
+        target_y = y[left];
+    } else {
+        real x_left = x[left];
+        real target_percent = (target_x - x_left) / (real(x[right]) - x_left);
+        target_y = real(y[left]) * (real(1.) - target_percent) + real(y[right]) * target_percent;
+    }
+    *left_out = left;
+    return target_y;
+}
+
+// src/effects/evolution.rs:446-513 Evolver::idx / radius / radius_of_gyration_2 / love_number
+static int64_t evolver_idx(const Evolver& e) {
+    const int64_t security_shift = 10;
+    return e.left_index > security_shift ? e.left_index - security_shift : 0;
+}
+static real evolver_radius(Evolver& e, real t, real current) {
+    if (e.type == POSI_EVO_NON_EVOLVING) return current;
+    int64_t i0 = evolver_idx(e), left = 0;
+    real r = linear_interpolation(t, e.time + i0, e.radius + i0, e.len - i0, &left);
+    e.left_index += left;
+    return r;
+}
+static real evolver_rg2(Evolver& e, real t, real current) {
+    if (e.type == POSI_EVO_BARAFFE2015 || e.type == POSI_EVO_LECONTE2011 || e.type == POSI_EVO_LECONTE_CHABRIER2013) {
+        int64_t i0 = evolver_idx(e), left = 0;
+        real r = linear_interpolation(t, e.time + i0, e.rg2 + i0, e.len - i0, &left);
+        e.left_index += left;
+        return r;
+    }
+    return current;
+}
+static real evolver_love(Evolver& e, real t, real current) {
+    if (e.type == POSI_EVO_LECONTE_CHABRIER2013) {
+        int64_t i0 = evolver_idx(e), left = 0;
+        real r = linear_interpolation(t, e.time + i0, e.love + i0, e.len - i0, &left);
+        e.left_index += left;
+        return r;
+    }
+    return current;
+}
+
+// src/effects/evolution.rs:516-546 (the love number update writes to a copy
+// of the parameters in the reference, so only the index bookkeeping remains)
+static void non_spin_dependent_evolving_quantities(Sim& s, real t) {
+    for (int i = 0; i < s.n; ++i) {
+        Particle& q = s.p[i];
+        Evolver& e = s.ev[i];
+        real new_radius = evolver_radius(e, t, q.radius);
+        real new_rg2 = evolver_rg2(e, t, q.rg2);
+        if (new_radius != q.radius || new_rg2 != q.rg2) {
+            q.radius = new_radius;
+            q.rg2 = new_rg2;
+            q.moi = q.mass * q.rg2 * powi(q.radius, 2);
+        }
+        if (q.tides.kind != POSI_EFFECT_DISABLED) {
+            (void)evolver_love(e, t, q.tides.love_number);
+        }
+    }
+}
+
+// src/effects/evolution.rs:548-567: only the dynamical-tide evolutions set a
+// non-zero lag angle, and those are outside this path.
+static void spin_dependent_evolving_quantities(Sim& s, real) {
+    for (int i = 0; i < s.n; ++i) s.p[i].tides.lag_angle = 0.;
+}
+
+// src/particles/universe.rs:305-316
+static void calculate_spin_and_evolving_quantities(Sim& s, real t, bool evolution) {
+    if (evolution && s.evolution) non_spin_dependent_evolving_quantities(s, t);
+    calculate_spin(s);
+    if (evolution && s.evolution) spin_dependent_evolving_quantities(s, t);
+}
+
+// src/particles/universe.rs:177-196
+static void calculate_roche_radiuses(Sim& s) {
+    const int n = s.n;
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) {
+            if (i == j) continue;
+            const Particle& a = s.p[i];
+            const Particle& b = s.p[j];
+            if (a.mass > b.mass) {
+                s.roche[i * n + j] = (b.radius / 0.462) * real(std::pow(dv(a.mass / b.mass), 1. / 3.));
+            } else {
+                s.roche[i * n + j] = (a.radius / 0.462) * real(std::pow(dv(b.mass / a.mass), 1. / 3.));
+            }
+        }
+    }
+}
+
+static void set_fatal(Sim& s, int code, int i, int j) {
+    if (s.fatal()) return;
+    s.status = (s.status & ~int64_t(POSI_SYS_FATAL_MASK)) | code;
+    s.fail_step = s.iteration;
+    s.fail_pair = int64_t(i) * 1024 + j;
+}
+
+// src/particles/universe.rs:198-303 (ignore_terms: 0 None, 1 WHFastOne, 2 WHFastTwo)
+static void gravity_calculate_acceleration(Sim& s, int ignore_terms) {
+    const int n = s.n, mm = s.host;
+    std::vector<V3> acc(n, V3{0., 0., 0.});
+    for (int i = 0; i < n; ++i) {
+        const Particle& a = s.p[i];
+        for (int j = 0; j < n; ++j) {
+            if (i == j) continue;
+            const Particle& b = s.p[j];
+            real dx = a.r.x - b.r.x;
+            real dy = a.r.y - b.r.y;
+            real dz = a.r.z - b.r.z;
+            real distance_2 = dx * dx + dy * dy + dz * dz;
+            if (i < j) {
+                if (distance_2 <= powi(s.roche[i * n + j], 2)) { set_fatal(s, POSI_SYS_ROCHE, i, j); return; }
+                if (distance_2 <= powi(a.radius + b.radius, 2)) { set_fatal(s, POSI_SYS_COLLISION, i, j); return; }
+                if (MAX_DISTANCE_2 > 0. && i == mm && distance_2 > MAX_DISTANCE_2) { set_fatal(s, POSI_SYS_EJECTED, i, j); return; }
+            }
+            if (ignore_terms == 1 &&
+                ((i == mm && mm == 0 && j == 1) || (i == mm && mm > 0 && j == 0) ||
+                 (j == mm && mm == 0 && i == 1) || (j == mm && mm > 0 && i == 0))) {
+                continue;
+            }
+            if (ignore_terms == 2 && (i == mm || j == mm)) continue;
+            real distance = rsqrt_(distance_2);
+            real prefact = -G / (distance * distance * distance) * b.mass;
+            acc[i].x += prefact * dx;
+            acc[i].y += prefact * dy;
+            acc[i].z += prefact * dz;
+        }
+    }
+    for (int i = 0; i < n; ++i) s.p[i].a = acc[i];
+}
+
+// src/particles/universe.rs:318-351
+static void inertial_to_heliocentric(Sim& s) {
+    Particle& h = s.p[s.host];
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        q.hr.x = q.r.x - h.r.x;
+        q.hr.y = q.r.y - h.r.y;
+        q.hr.z = q.r.z - h.r.z;
+        q.hv.x = q.v.x - h.v.x;
+        q.hv.y = q.v.y - h.v.y;
+        q.hv.z = q.v.z - h.v.z;
+        q.hd = rsqrt_(powi(q.hr.x, 2) + powi(q.hr.y, 2) + powi(q.hr.z, 2));
+        q.hvr = (q.hr.x * q.hv.x + q.hr.y * q.hv.y + q.hr.z * q.hv.z) / q.hd;
+        q.hnv2 = powi(q.hv.x - h.hv.x, 2) + powi(q.hv.y - h.hv.y, 2) + powi(q.hv.z - h.hv.z, 2);
+        q.hnv = rsqrt_(q.hnv2);
+    }
+    h.hr = V3{0., 0., 0.};
+    h.hv = V3{0., 0., 0.};
+    h.hd = 0.; h.hvr = 0.; h.hnv2 = 0.; h.hnv = 0.;
+}
+
+// src/particles/universe.rs:353-426 with
+// src/effects/tides/common.rs:143-170,202-217,
+// src/effects/rotational_flattening/common.rs:93-120,148-161,
+// src/effects/general_relativity.rs:86-109,153-174
+static void initialize(Sim& s, bool dl, bool acc) {
+    const bool it = (dl && s.tides) || (acc && s.tides);
+    const bool ifl = (dl && s.flat) || (acc && s.flat);
+    const bool igr = (dl && s.gr) || (acc && s.gr);
+    if (it || ifl || igr) {
+        Particle& h = s.p[s.host];
+        if (it && h.tides.kind == POSI_EFFECT_CENTRAL) {
+            // tides::copy_heliocentric_coordinates
+            h.tides.pos = h.hr; h.tides.vel = h.hv; h.tides.distance = h.hd; h.tides.radial_velocity = h.hvr;
+            for (int i = 0; i < s.n; ++i) {
+                if (i == s.host) continue;
+                Particle& q = s.p[i];
+                if (q.tides.kind == POSI_EFFECT_ORBITING) {
+                    q.tides.pos = q.hr; q.tides.vel = q.hv; q.tides.distance = q.hd; q.tides.radial_velocity = q.hvr;
+                }
+            }
+            // tides::initialize
+            h.tides.rscal_star = 0.; h.tides.rscal_planet = 0.;
+            h.tides.out_acc = V3{0., 0., 0.}; h.tides.out_dldt = V3{0., 0., 0.};
+            for (int i = 0; i < s.n; ++i) {
+                if (i == s.host) continue;
+                Particle& q = s.p[i];
+                if (q.tides.kind == POSI_EFFECT_ORBITING) {
+                    q.tides.rscal_star = q.tides.pos.x * h.spin.x + q.tides.pos.y * h.spin.y + q.tides.pos.z * h.spin.z;
+                    q.tides.rscal_planet = q.tides.pos.x * q.spin.x + q.tides.pos.y * q.spin.y + q.tides.pos.z * q.spin.z;
+                    q.tides.out_acc = V3{0., 0., 0.}; q.tides.out_dldt = V3{0., 0., 0.};
+                }
+            }
+        }
+        if (ifl && h.flat.kind == POSI_EFFECT_CENTRAL) {
+            h.flat.pos = h.hr; h.flat.vel = h.hv; h.flat.distance = h.hd;
+            for (int i = 0; i < s.n; ++i) {
+                if (i == s.host) continue;
+                Particle& q = s.p[i];
+                if (q.flat.kind == POSI_EFFECT_ORBITING) { q.flat.pos = q.hr; q.flat.vel = q.hv; q.flat.distance = q.hd; }
+            }
+            h.flat.rscal_star = 0.; h.flat.rscal_planet = 0.;
+            h.flat.out_acc = V3{0., 0., 0.}; h.flat.out_dldt = V3{0., 0., 0.};
+            for (int i = 0; i < s.n; ++i) {
+                if (i == s.host) continue;
+                Particle& q = s.p[i];
+                if (q.flat.kind == POSI_EFFECT_ORBITING) {
+                    q.flat.rscal_star = q.flat.pos.x * h.spin.x + q.flat.pos.y * h.spin.y + q.flat.pos.z * h.spin.z;
+                    q.flat.rscal_planet = q.flat.pos.x * q.spin.x + q.flat.pos.y * q.spin.y + q.flat.pos.z * q.spin.z;
+                    q.flat.out_acc = V3{0., 0., 0.}; q.flat.out_dldt = V3{0., 0., 0.};
+                }
+            }
+        }
+        if (igr && h.gr.kind == POSI_EFFECT_CENTRAL) {
+            h.gr.pos = h.hr; h.gr.vel = h.hv; h.gr.distance = h.hd; h.gr.radial_velocity = h.hvr;
+            h.gr.norm_v = h.hnv; h.gr.norm_v2 = h.hnv2;
+            for (int i = 0; i < s.n; ++i) {
+                if (i == s.host) continue;
+                Particle& q = s.p[i];
+                if (q.gr.kind == POSI_EFFECT_ORBITING) {
+                    q.gr.pos = q.hr; q.gr.vel = q.hv; q.gr.distance = q.hd; q.gr.radial_velocity = q.hvr;
+                    q.gr.norm_v = q.hnv; q.gr.norm_v2 = q.hnv2;
+                }
+            }
+            h.gr.factor = 0.;
+            h.gr.out_acc = V3{0., 0., 0.}; h.gr.out_dldt = V3{0., 0., 0.};
+            for (int i = 0; i < s.n; ++i) {
+                if (i == s.host) continue;
+                Particle& q = s.p[i];
+                if (q.gr.kind == POSI_EFFECT_ORBITING) {
+                    q.gr.factor = h.mass_g * q.mass_g / powi(h.mass_g + q.mass_g, 2);
+                    q.gr.out_acc = V3{0., 0., 0.}; q.gr.out_dldt = V3{0., 0., 0.};
+                }
+            }
+        }
+    }
+    if (acc) {
+        for (int i = 0; i < s.n; ++i) s.p[i].a_add = V3{0., 0., 0.};
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Constant-time-lag tides: src/effects/tides/constant_time_lag.rs
+// ---------------------------------------------------------------------------
+// :206-264 (the pair-dependent dissipation factor is the particle's own for
+// every non-dynamical evolution, :144-165)
+static void tides_orthogonal(Sim& s) {
+    Particle& h = s.p[s.host];
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool central_body = (pass == 0);
+        for (int i = 0; i < s.n; ++i) {
+            if (i == s.host) continue;
+            Particle& q = s.p[i];
+            if (q.tides.kind != POSI_EFFECT_ORBITING) continue;
+            real distance_7 = powi(q.tides.distance, 7);
+            if (central_body) {
+                q.tides.ortho_star = real(4.5) * powi(q.mass, 2) * powi(h.radius, 10) * h.tides.scaled_dissipation_factor / distance_7;
+            } else {
+                q.tides.ortho_planet = real(4.5) * powi(h.mass, 2) * powi(q.radius, 10) * q.tides.scaled_dissipation_factor / distance_7;
+            }
+        }
+    }
+}
+
+// :266-307
+static void tides_radial(Sim& s) {
+    Particle& h = s.p[s.host];
+    real host_mass_2 = h.mass * h.mass;
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.tides.kind != POSI_EFFECT_ORBITING) continue;
+        real host_love = (h.tides.kind == POSI_EFFECT_CENTRAL) ? h.tides.love_number : real(0.);
+        real particle_mass_2 = q.mass * q.mass;
+        real conservative = real(-3.0) * K2 / powi(q.tides.distance, 7)
+            * (particle_mass_2 * powi(h.radius, 5) * host_love + host_mass_2 * powi(q.radius, 5) * q.tides.love_number);
+        real factor1 = real(-13.5) * q.tides.radial_velocity / powi(q.tides.distance, 8);
+        real term1 = particle_mass_2 * powi(h.radius, 10) * h.tides.scaled_dissipation_factor;
+        real term2 = host_mass_2 * powi(q.radius, 10) * q.tides.scaled_dissipation_factor;
+        q.tides.radial_diss_pm = factor1 * term2;
+        real dissipative = q.tides.radial_diss_pm + factor1 * term1;
+        q.tides.radial = conservative + dissipative;
+    }
+}
+
+// :309-332
+static V3 tidal_force(const Particle& h, const Particle& q) {
+    const Tides& t = q.tides;
+    real factor3 = t.radial + (t.ortho_star + t.ortho_planet) * t.radial_velocity / t.distance;
+    V3 f;
+    f.x = factor3 * t.pos.x / t.distance
+        + t.ortho_star / t.distance * (h.spin.y * t.pos.z - h.spin.z * t.pos.y - t.vel.x)
+        + t.ortho_planet / t.distance * (q.spin.y * t.pos.z - q.spin.z * t.pos.y - t.vel.x);
+    f.y = factor3 * t.pos.y / t.distance
+        + t.ortho_star / t.distance * (h.spin.z * t.pos.x - h.spin.x * t.pos.z - t.vel.y)
+        + t.ortho_planet / t.distance * (q.spin.z * t.pos.x - q.spin.x * t.pos.z - t.vel.y);
+    f.z = factor3 * t.pos.z / t.distance
+        + t.ortho_star / t.distance * (h.spin.x * t.pos.y - h.spin.y * t.pos.x - t.vel.z)
+        + t.ortho_planet / t.distance * (q.spin.x * t.pos.y - q.spin.y * t.pos.x - t.vel.z);
+    return f;
+}
+
+// :171-204
+static V3 tides_torque(const Particle& h, const Particle& q, bool central_body) {
+    V3 rs;
+    real orth, rscal;
+    if (!central_body) { rs = q.spin; rscal = q.tides.rscal_planet; orth = q.tides.ortho_planet; }
+    else { rs = h.spin; rscal = q.tides.rscal_star; orth = q.tides.ortho_star; }
+    const Tides& t = q.tides;
+    real d = t.distance;
+    V3 r;
+    r.x = orth * (d * rs.x - rscal * t.pos.x / d - real(1.0) / d * (t.pos.y * t.vel.z - t.pos.z * t.vel.y));
+    r.y = orth * (d * rs.y - rscal * t.pos.y / d - real(1.0) / d * (t.pos.z * t.vel.x - t.pos.x * t.vel.z));
+    r.z = orth * (d * rs.z - rscal * t.pos.z / d - real(1.0) / d * (t.pos.x * t.vel.y - t.pos.y * t.vel.x));
+    return r;
+}
+
+// src/effects/tides/common.rs:312-370 (ConstantTimeLag branch)
+static void tidal_acceleration(Sim& s) {
+    Particle& h = s.p[s.host];
+    real factor2 = real(1.) / h.mass;
+    V3 sum{0., 0., 0.};
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.tides.kind != POSI_EFFECT_ORBITING) continue;
+        V3 f = tidal_force(h, q);
+        real factor1 = real(1.) / q.mass;
+        sum.x += f.x; sum.y += f.y; sum.z += f.z;
+        q.tides.out_acc.x = factor1 * f.x;
+        q.tides.out_acc.y = factor1 * f.y;
+        q.tides.out_acc.z = factor1 * f.z;
+    }
+    h.tides.out_acc.x = real(-1.0) * factor2 * sum.x;
+    h.tides.out_acc.y = real(-1.0) * factor2 * sum.y;
+    h.tides.out_acc.z = real(-1.0) * factor2 * sum.z;
+}
+
+// src/effects/tides/common.rs:223-261 (every non-host body is an orbiting
+// body here; the loader rejects cases where it is not)
+static void tides_dangular_momentum_dt(Sim& s) {
+    Particle& h = s.p[s.host];
+    const real factor = -1.0;
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.tides.kind != POSI_EFFECT_ORBITING) continue;
+        V3 t = tides_torque(h, q, false);
+        q.tides.out_dldt.x = factor * t.x;
+        q.tides.out_dldt.y = factor * t.y;
+        q.tides.out_dldt.z = factor * t.z;
+    }
+    V3 sum{0., 0., 0.};
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        if (h.tides.kind != POSI_EFFECT_CENTRAL) continue;
+        V3 t = tides_torque(h, s.p[i], true);
+        sum.x += factor * t.x; sum.y += factor * t.y; sum.z += factor * t.z;
+    }
+    h.tides.out_dldt = sum;
+}
+
+// src/effects/tides/common.rs:263-279
+static void tides_denergy_dt(Sim& s) {
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.tides.kind != POSI_EFFECT_ORBITING) continue;
+        Tides& t = q.tides;
+        real factor2 = t.ortho_planet / t.distance;
+        t.denergy_dt = -((real(1.0) / t.distance * (t.radial_diss_pm + factor2 * t.radial_velocity))
+                    * (t.pos.x * t.vel.x + t.pos.y * t.vel.y + t.pos.z * t.vel.z)
+                    + factor2
+                    * ((q.spin.y * t.pos.z - q.spin.z * t.pos.y - t.vel.x) * t.vel.x
+                    + (q.spin.z * t.pos.x - q.spin.x * t.pos.z - t.vel.y) * t.vel.y
+                    + (q.spin.x * t.pos.y - q.spin.y * t.pos.x - t.vel.z) * t.vel.z))
+                    - (t.out_dldt.x * q.spin.x + t.out_dldt.y * q.spin.y + t.out_dldt.z * q.spin.z);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Rotational flattening (oblate spheroid):
+// src/effects/rotational_flattening/oblate_spheroid.rs, common.rs
+// ---------------------------------------------------------------------------
+// oblate_spheroid.rs:12-49
+static void flat_orthogonal(Sim& s) {
+    Particle& h = s.p[s.host];
+    real host_love = (h.flat.kind == POSI_EFFECT_CENTRAL) ? h.flat.love_number : real(0.);
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool central_body = (pass == 0);
+        for (int i = 0; i < s.n; ++i) {
+            if (i == s.host) continue;
+            Particle& q = s.p[i];
+            if (q.flat.kind != POSI_EFFECT_ORBITING) continue;
+            Flat& f = q.flat;
+            if (central_body) {
+                f.factor_star = q.mass * host_love * h.nsv2 * powi(h.radius, 5) / real(6.);
+                f.ortho_star = real(-6.) * f.factor_star * f.rscal_star / (h.nsv2 * powi(f.distance, 5));
+            } else {
+                f.factor_planet = h.mass * f.love_number * q.nsv2 * powi(q.radius, 5) / real(6.);
+                f.ortho_planet = real(-6.) * f.factor_planet * f.rscal_planet / (q.nsv2 * powi(f.distance, 5));
+            }
+        }
+    }
+}
+
+// oblate_spheroid.rs:51-60
+static void flat_radial(Sim& s) {
+    Particle& h = s.p[s.host];
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.flat.kind != POSI_EFFECT_ORBITING) continue;
+        Flat& f = q.flat;
+        f.radial = real(-3.) / powi(f.distance, 5) * (f.factor_planet + f.factor_star)
+            + real(15.) / powi(f.distance, 7) * (f.factor_star * f.rscal_star * f.rscal_star / h.nsv2
+                + f.factor_planet * f.rscal_planet * f.rscal_planet / q.nsv2);
+    }
+}
+
+// oblate_spheroid.rs:83-97 via common.rs:203-237
+static void flat_acceleration(Sim& s) {
+    Particle& h = s.p[s.host];
+    real factor2 = real(1.) / h.mass;
+    V3 sum{0., 0., 0.};
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.flat.kind != POSI_EFFECT_ORBITING) continue;
+        Flat& f = q.flat;
+        V3 F;
+        F.x = f.radial * f.pos.x + f.ortho_planet * q.spin.x + f.ortho_star * h.spin.x;
+        F.y = f.radial * f.pos.y + f.ortho_planet * q.spin.y + f.ortho_star * h.spin.y;
+        F.z = f.radial * f.pos.z + f.ortho_planet * q.spin.z + f.ortho_star * h.spin.z;
+        sum.x += F.x; sum.y += F.y; sum.z += F.z;
+        real factor1 = real(1.) / q.mass;
+        f.out_acc.x = factor1 * F.x;
+        f.out_acc.y = factor1 * F.y;
+        f.out_acc.z = factor1 * F.z;
+    }
+    h.flat.out_acc.x = real(-1.0) * factor2 * sum.x;
+    h.flat.out_acc.y = real(-1.0) * factor2 * sum.y;
+    h.flat.out_acc.z = real(-1.0) * factor2 * sum.z;
+}
+
+// oblate_spheroid.rs:62-81
+static V3 flat_torque(const Particle& h, const Particle& q, bool central_body) {
+    V3 rs = h.spin;
+    real orth;
+    if (!central_body) { rs = q.spin; orth = q.flat.ortho_planet; }
+    else { orth = q.flat.ortho_star; }
+    const V3& p = q.flat.pos;
+    V3 t;
+    t.x = orth * (p.y * rs.z - p.z * rs.y);
+    t.y = orth * (p.z * rs.x - p.x * rs.z);
+    t.z = orth * (p.x * rs.y - p.y * rs.x);
+    return t;
+}
+
+// common.rs:165-201
+static void flat_dangular_momentum_dt(Sim& s) {
+    Particle& h = s.p[s.host];
+    const real factor = -1.0;
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.flat.kind != POSI_EFFECT_ORBITING) continue;
+        V3 t = flat_torque(h, q, false);
+        q.flat.out_dldt.x = factor * t.x;
+        q.flat.out_dldt.y = factor * t.y;
+        q.flat.out_dldt.z = factor * t.z;
+    }
+    V3 sum{0., 0., 0.};
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        if (h.flat.kind != POSI_EFFECT_CENTRAL) continue;
+        V3 t = flat_torque(h, s.p[i], true);
+        sum.x += factor * t.x; sum.y += factor * t.y; sum.z += factor * t.z;
+    }
+    h.flat.out_dldt = sum;
+}
+
+// ---------------------------------------------------------------------------
+// General relativity, Kidder (1995): src/effects/general_relativity.rs
+// ---------------------------------------------------------------------------
+// :187-239
+static void gr_first_order(Sim& s) {
+    Particle& h = s.p[s.host];
+    V3 sum{0., 0., 0.};
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.gr.kind != POSI_EFFECT_ORBITING) continue;
+        GR& g = q.gr;
+        real mg = h.mass_g + q.mass_g;
+        real distance_2 = powi(g.distance, 2);
+        real radial_velocity_2 = powi(g.radial_velocity, 2);
+        real radial = -mg / (distance_2 * SPEED_OF_LIGHT_2)
+            * ((real(1.0) + real(3.0) * g.factor) * g.norm_v2
+               - real(2.0) * (real(2.0) + g.factor) * mg / g.distance
+               - real(1.5) * g.factor * radial_velocity_2);
+        real ortho = mg / (distance_2 * SPEED_OF_LIGHT_2)
+            * real(2.0) * (real(2.0) - g.factor) * g.radial_velocity * g.norm_v;
+        V3 a;
+        a.x = radial * g.pos.x / g.distance + ortho * g.vel.x / g.norm_v;
+        a.y = radial * g.pos.y / g.distance + ortho * g.vel.y / g.norm_v;
+        a.z = radial * g.pos.z / g.distance + ortho * g.vel.z / g.norm_v;
+        sum.x += q.mass / h.mass * a.x;
+        sum.y += q.mass / h.mass * a.y;
+        sum.z += q.mass / h.mass * a.z;
+        g.out_acc = a;
+    }
+    h.gr.out_acc.x = real(-1.0) * sum.x;
+    h.gr.out_acc.y = real(-1.0) * sum.y;
+    h.gr.out_acc.z = real(-1.0) * sum.z;
+}
+
+// :241-298
+static void gr_second_order(Sim& s) {
+    Particle& h = s.p[s.host];
+    V3 sum{0., 0., 0.};
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.gr.kind != POSI_EFFECT_ORBITING) continue;
+        GR& g = q.gr;
+        const real f = g.factor;
+        real mg = h.mass_g + q.mass_g;
+        real distance_2 = powi(g.distance, 2);
+        real nv2 = g.norm_v2;
+        real nv4 = powi(nv2, 2);
+        real vr2 = powi(g.radial_velocity, 2);
+        real vr4 = powi(vr2, 2);
+        real f2 = powi(f, 2);
+        real radial = -mg / (distance_2 * SPEED_OF_LIGHT_2)
+            * (real(3.0 / 4.0) * (real(12.0) + real(29.0) * f) * (powi(mg, 2) / distance_2)
+               + f * (real(3.0) - real(4.0) * f) * nv4
+               + real(15.0 / 8.0) * f * (real(1.0) - real(3.0) * f) * vr4
+               - real(3.0 / 2.0) * f * (real(3.0) - real(4.0) * f) * vr2 * nv2
+               - real(0.5) * f * (real(13.0) - real(4.0) * f) * (mg / g.distance) * nv2
+               - (real(2.0) + real(25.0) * f + real(2.0) * f2) * (mg / g.distance) * vr2);
+        real ortho = -mg / (distance_2 * SPEED_OF_LIGHT_2)
+            * real(-0.5) * g.radial_velocity
+            * (f * (real(15.0) + real(4.0) * f) * nv2
+               - (real(4.0) + real(41.0) * f + real(8.0) * f2) * (mg / g.distance)
+               - real(3.0) * f * (real(3.0) + real(2.0) * f) * vr2);
+        V3 a;
+        a.x = radial * g.pos.x / g.distance + ortho * g.vel.x;
+        a.y = radial * g.pos.y / g.distance + ortho * g.vel.y;
+        a.z = radial * g.pos.z / g.distance + ortho * g.vel.z;
+        sum.x += q.mass / h.mass * a.x;
+        sum.y += q.mass / h.mass * a.y;
+        sum.z += q.mass / h.mass * a.z;
+        g.out_acc.x += a.x; g.out_acc.y += a.y; g.out_acc.z += a.z;
+    }
+    h.gr.out_acc.x += real(-1.0) * sum.x;
+    h.gr.out_acc.y += real(-1.0) * sum.y;
+    h.gr.out_acc.z += real(-1.0) * sum.z;
+}
+
+// :300-456
+static void gr_spin_orbit(Sim& s) {
+    Particle& h = s.p[s.host];
+    V3 sL{h.moi * h.spin.x, h.moi * h.spin.y, h.moi * h.spin.z};
+    V3 sum{0., 0., 0.};
+    h.gr.out_dldt = V3{0., 0., 0.};
+    const real fa = G / SPEED_OF_LIGHT_2;
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.gr.kind != POSI_EFFECT_ORBITING) continue;
+        GR& g = q.gr;
+        real M = h.mass + q.mass;
+        real dM = h.mass - q.mass;
+        real mass_factor = dM / M;
+        V3 pL{q.moi * q.spin.x, q.moi * q.spin.y, q.moi * q.spin.z};
+        V3 nn{g.pos.x / g.distance, g.pos.y / g.distance, g.pos.z / g.distance};
+        real msx = mass_factor * M * (pL.x / q.mass - sL.x / h.mass);
+        real msy = mass_factor * M * (pL.y / q.mass - sL.y / h.mass);
+        real msz = mass_factor * M * (pL.z / q.mass - sL.z / h.mass);
+        real e1x = real(6.) * nn.x * ((nn.y * g.vel.z - nn.z * g.vel.y) * (real(2.) * (sL.x + pL.x) + msx));
+        real e1y = real(6.) * nn.y * ((nn.z * g.vel.x - nn.x * g.vel.z) * (real(2.) * (sL.y + pL.y) + msy));
+        real e1z = real(6.) * nn.z * ((nn.x * g.vel.y - nn.y * g.vel.x) * (real(2.) * (sL.z + pL.z) + msz));
+        V3 e7{real(7.) * (sL.x + pL.x) + real(3.) * msx,
+              real(7.) * (sL.y + pL.y) + real(3.) * msy,
+              real(7.) * (sL.z + pL.z) + real(3.) * msz};
+        real e2x = g.vel.y * e7.z - g.vel.z * e7.y;
+        real e2y = g.vel.z * e7.x - g.vel.x * e7.z;
+        real e2z = g.vel.x * e7.y - g.vel.y * e7.x;
+        V3 e3s{real(3.) * (sL.x + pL.x) + msx, real(3.) * (sL.y + pL.y) + msy, real(3.) * (sL.z + pL.z) + msz};
+        real e3x = real(3.) * g.radial_velocity * (nn.y * e3s.z - nn.z * e3s.y);
+        real e3y = real(3.) * g.radial_velocity * (nn.z * e3s.x - nn.x * e3s.z);
+        real e3z = real(3.) * g.radial_velocity * (nn.x * e3s.y - nn.y * e3s.x);
+        real ax = fa * (e1x - e2x + e3x);
+        real ay = fa * (e1y - e2y + e3y);
+        real az = fa * (e1z - e2z + e3z);
+        sum.x += q.mass / h.mass * ax;
+        sum.y += q.mass / h.mass * ay;
+        sum.z += q.mass / h.mass * az;
+        g.out_acc.x += ax; g.out_acc.y += ay; g.out_acc.z += az;
+        // Kidder 1995 eq. 2.4a
+        real mu = (h.mass * q.mass) / M;
+        V3 lo{mu * (g.pos.y * g.vel.z - g.pos.z * g.vel.y),
+              mu * (g.pos.z * g.vel.x - g.pos.x * g.vel.z),
+              mu * (g.pos.x * g.vel.y - g.pos.y * g.vel.x)};
+        real fm = real(2.) + real(3. / 2.) * q.mass / h.mass;
+        real h1x = fm * (lo.y * sL.z - lo.z * sL.y);
+        real h1y = fm * (lo.z * sL.x - lo.x * sL.z);
+        real h1z = fm * (lo.x * sL.y - lo.y * sL.x);
+        real h2x = pL.y * sL.z - pL.z * sL.y;
+        real h2y = pL.z * sL.x - pL.x * sL.z;
+        real h2z = pL.x * sL.y - pL.y * sL.x;
+        real sp = nn.x * pL.x + nn.y * pL.y + nn.z * pL.z;
+        real h3x = real(3.) * sp * (nn.y * sL.z - nn.z * sL.y);
+        real h3y = real(3.) * sp * (nn.z * sL.x - nn.x * sL.z);
+        real h3z = real(3.) * sp * (nn.x * sL.y - nn.y * sL.x);
+        h.gr.out_dldt.x += fa * (h1x - h2x + h3x);
+        h.gr.out_dldt.y += fa * (h1y - h2y + h3y);
+        h.gr.out_dldt.z += fa * (h1z - h2z + h3z);
+        // Kidder 1995 eq. 2.4b
+        real fm2 = real(2.) + real(3. / 2.) * h.mass / q.mass;
+        real q1x = fm2 * (lo.y * pL.z - lo.z * pL.y);
+        real q1y = fm2 * (lo.z * pL.x - lo.x * pL.z);
+        real q1z = fm2 * (lo.x * pL.y - lo.y * pL.x);
+        real q2x = sL.y * pL.z - sL.z * pL.y;
+        real q2y = sL.z * pL.x - sL.x * pL.z;
+        real q2z = sL.x * pL.y - sL.y * pL.x;
+        real ss = nn.x * sL.x + nn.y * sL.y + nn.z * sL.z;
+        real q3x = real(3.) * ss * (nn.y * pL.z - nn.z * pL.y);
+        real q3y = real(3.) * ss * (nn.z * pL.x - nn.x * pL.z);
+        real q3z = real(3.) * ss * (nn.x * pL.y - nn.y * pL.x);
+        g.out_dldt.x = fa * (q1x - q2x + q3x);
+        g.out_dldt.y = fa * (q1y - q2y + q3y);
+        g.out_dldt.z = fa * (q1z - q2z + q3z);
+    }
+    h.gr.out_acc.x += real(-1.0) * sum.x;
+    h.gr.out_acc.y += real(-1.0) * sum.y;
+    h.gr.out_acc.z += real(-1.0) * sum.z;
+}
+
+// src/particles/universe.rs:580-614
+static void calculate_dangular_momentum_dt(Sim& s) {
+    for (int i = 0; i < s.n; ++i) {
+        Particle& q = s.p[i];
+        q.dLdt.x = q.tides.out_dldt.x + q.flat.out_dldt.x + q.gr.out_dldt.x + q.wind_dldt.x;
+        q.dLdt.y = q.tides.out_dldt.y + q.flat.out_dldt.y + q.gr.out_dldt.y + q.wind_dldt.y;
+        q.dLdt.z = q.tides.out_dldt.z + q.flat.out_dldt.z + q.gr.out_dldt.z + q.wind_dldt.z;
+    }
+}
+
+// src/particles/universe.rs:540-567
+static void add_additional_acceleration_corrections(Sim& s) {
+    for (int i = 0; i < s.n; ++i) {
+        Particle& q = s.p[i];
+        if (s.tides) { q.a_add.x += q.tides.out_acc.x; q.a_add.y += q.tides.out_acc.y; q.a_add.z += q.tides.out_acc.z; }
+        if (s.flat) { q.a_add.x += q.flat.out_acc.x; q.a_add.y += q.flat.out_acc.y; q.a_add.z += q.flat.out_acc.z; }
+        if (s.gr) { q.a_add.x += q.gr.out_acc.x; q.a_add.y += q.gr.out_acc.y; q.a_add.z += q.gr.out_acc.z; }
+    }
+}
+
+// src/particles/universe.rs:428-538
+static void calculate_additional_effects(Sim& s, real t, bool evolution, bool dl, bool acc) {
+    initialize(s, dl, acc);
+    calculate_spin_and_evolving_quantities(s, t, evolution);
+    if (s.fatal()) return;
+    if (s.tides || s.flat) {
+        if ((dl && (s.tides || s.flat)) || (acc && (s.tides || s.flat || s.gr))) {
+            if (s.tides) tides_orthogonal(s);
+            if (s.flat) flat_orthogonal(s);
+            if (acc && (s.tides || s.flat)) {
+                if (s.tides) { tides_radial(s); tidal_acceleration(s); }
+                if (s.flat) { flat_radial(s); flat_acceleration(s); }
+            }
+            if (dl && (s.tides || s.flat)) {
+                if (s.tides) tides_dangular_momentum_dt(s);
+                if (s.flat) flat_dangular_momentum_dt(s);
+            }
+        }
+    }
+    if (acc && s.gr) {
+        if (s.p[s.host].gr.kind == POSI_EFFECT_CENTRAL) {
+            gr_first_order(s);
+            gr_second_order(s);
+            gr_spin_orbit(s);
+        }
+    }
+    if (dl) {
+        if (s.tides || s.flat || s.gr) calculate_dangular_momentum_dt(s);
+    }
+    if (acc) add_additional_acceleration_corrections(s);
+}
+
+// ---------------------------------------------------------------------------
+// WHFast: src/integrator/whfast.rs
+// ---------------------------------------------------------------------------
+// :424-451
+static bool converged_velocity_dependent_forces_integration(const Sim& s, const std::vector<V3>& fv,
+                                                            const std::vector<V3>& fL,
+                                                            const std::vector<V3>& pv,
+                                                            const std::vector<V3>& pL, bool spin) {
+    real fv2 = 0., dv2 = 0., fL2 = 0., dL2 = 0.;
+    for (int i = 0; i < s.n; ++i) {
+        real dvx = fv[i].x - pv[i].x, dvy = fv[i].y - pv[i].y, dvz = fv[i].z - pv[i].z;
+        dv2 += powi(dvx, 2) + powi(dvy, 2) + powi(dvz, 2);
+        fv2 += powi(fv[i].x, 2) + powi(fv[i].y, 2) + powi(fv[i].z, 2);
+        if (spin) {
+            real dsx = fL[i].x - pL[i].x, dsy = fL[i].y - pL[i].y, dsz = fL[i].z - pL[i].z;
+            dL2 += powi(dsx, 2) + powi(dsy, 2) + powi(dsz, 2);
+            fL2 += powi(fL[i].x, 2) + powi(fL[i].y, 2) + powi(fL[i].z, 2);
+        }
+    }
+    return (spin && dv2 / fv2 < real(DBL_EPSILON_2) && dL2 / fL2 < real(DBL_EPSILON_2)) ||
+           (!spin && dv2 / fv2 < real(DBL_EPSILON_2));
+}
+
+// :322-422
+static void integrate_velocity_dependent_forces(Sim& s, real dt, bool spin, bool evolution) {
+    const int n = s.n;
+    std::vector<V3> ov(n), oL(n), fv(n), fL(n), pv(n), pL(n), dvc(n, V3{0., 0., 0.}), dLc(n, V3{0., 0., 0.});
+    for (int i = 0; i < n; ++i) { ov[i] = s.p[i].v; oL[i] = s.p[i].L; fv[i] = ov[i]; fL[i] = oL[i]; }
+    bool converged = false;
+    int iters = 0;
+    for (int it = 0; it < IMPLICIT_MIDPOINT_MAX_ITER; ++it) {
+        iters = it + 1;
+        pv = fv; pL = fL;
+        inertial_to_heliocentric(s);
+        calculate_additional_effects(s, s.t, evolution && it == 0, spin, true);
+        if (s.fatal()) return;
+        for (int i = 0; i < n; ++i) {
+            const Particle& q = s.p[i];
+            dvc[i].x = dt * q.a_add.x - s.errv[i].x;
+            dvc[i].y = dt * q.a_add.y - s.errv[i].y;
+            dvc[i].z = dt * q.a_add.z - s.errv[i].z;
+            fv[i].x = ov[i].x + dvc[i].x;
+            fv[i].y = ov[i].y + dvc[i].y;
+            fv[i].z = ov[i].z + dvc[i].z;
+            if (spin) {
+                dLc[i].x = dt * q.dLdt.x - s.errL[i].x;
+                dLc[i].y = dt * q.dLdt.y - s.errL[i].y;
+                dLc[i].z = dt * q.dLdt.z - s.errL[i].z;
+                fL[i].x = oL[i].x + dLc[i].x;
+                fL[i].y = oL[i].y + dLc[i].y;
+                fL[i].z = oL[i].z + dLc[i].z;
+            }
+        }
+        if (it >= IMPLICIT_MIDPOINT_MIN_ITER - 1 && converged_velocity_dependent_forces_integration(s, fv, fL, pv, pL, spin)) {
+            converged = true;
+            break;
+        }
+        for (int i = 0; i < n; ++i) {
+            Particle& q = s.p[i];
+            q.v.x = real(0.5) * (ov[i].x + fv[i].x);
+            q.v.y = real(0.5) * (ov[i].y + fv[i].y);
+            q.v.z = real(0.5) * (ov[i].z + fv[i].z);
+            if (spin) {
+                q.L.x = real(0.5) * (oL[i].x + fL[i].x);
+                q.L.y = real(0.5) * (oL[i].y + fL[i].y);
+                q.L.z = real(0.5) * (oL[i].z + fL[i].z);
+            }
+        }
+    }
+    s.last_midpoint_iters = iters;
+    if (!converged) s.status |= POSI_SYS_WARN_NONCONVERGED;
+    for (int i = 0; i < n; ++i) {
+        Particle& q = s.p[i];
+        q.v = fv[i];
+        s.errv[i].x = (q.v.x - ov[i].x) - dvc[i].x;
+        s.errv[i].y = (q.v.y - ov[i].y) - dvc[i].y;
+        s.errv[i].z = (q.v.z - ov[i].z) - dvc[i].z;
+        if (spin) {
+            q.L = fL[i];
+            s.errL[i].x = (q.L.x - oL[i].x) - dLc[i].x;
+            s.errL[i].y = (q.L.y - oL[i].y) - dLc[i].y;
+            s.errL[i].z = (q.L.z - oL[i].z) - dLc[i].z;
+        }
+    }
+}
+
+// :844-876
+static void stumpff_cs3(real z_in, real cs[4]) {
+    static const double invfactorial[14] = {1., 1., 1. / 2., 1. / 6., 1. / 24., 1. / 120., 1. / 720., 1. / 5040.,
+                                            1. / 40320., 1. / 362880., 1. / 3628800., 1. / 39916800.,
+                                            1. / 479001600., 1. / 6227020800.};
+    real z = z_in;
+    int n = 0;
+    while (rabs(z) > real(0.1)) { z = z / real(4.); n += 1; }
+    const int nmax = 13;
+    real c_odd = invfactorial[nmax];
+    real c_even = invfactorial[nmax - 1];
+    int np = nmax - 2;
+    while (np >= 3) {
+        c_odd = real(invfactorial[np]) - z * c_odd;
+        c_even = real(invfactorial[np - 1]) - z * c_even;
+        np -= 2;
+    }
+    cs[3] = c_odd;
+    cs[2] = c_even;
+    cs[1] = real(invfactorial[1]) - z * c_odd;
+    cs[0] = real(invfactorial[0]) - z * c_even;
+    while (n > 0) {
+        cs[3] = (cs[2] + cs[0] * cs[3]) * real(0.25);
+        cs[2] = cs[1] * cs[1] * real(0.5);
+        cs[1] = cs[0] * cs[1];
+        cs[0] = real(2.) * cs[0] * cs[0] - real(1.);
+        n -= 1;
+    }
+}
+
+// :835-842
+static void stiefel_gs3(real beta, real x, real gs[4]) {
+    real x2 = powi(x, 2);
+    stumpff_cs3(beta * x2, gs);
+    gs[1] = gs[1] * x;
+    gs[2] = gs[2] * x2;
+    gs[3] = gs[3] * (x2 * x);
+}
+
+// :676-833
+static void kepler_individual_step(Sim& s, int i, real mass_g, real dt) {
+    V3 p1p = s.alt[i].pos, p1v = s.alt[i].vel;
+    real r0 = rsqrt_(powi(p1p.x, 2) + powi(p1p.y, 2) + powi(p1p.z, 2));
+    real r0i = real(1.) / r0;
+    real v2 = powi(p1v.x, 2) + powi(p1v.y, 2) + powi(p1v.z, 2);
+    real beta = real(2.) * mass_g * r0i - v2;
+    real eta0 = p1p.x * p1v.x + p1p.y * p1v.y + p1p.z * p1v.z;
+    real zeta0 = mass_g - beta * r0;
+    real x;
+    real gs[4];
+    real invperiod = 0.;
+    real x_per_period;
+    bool x_per_period_nan;
+    if (beta > real(0.)) {
+        real sqrt_beta = rsqrt_(beta);
+        invperiod = sqrt_beta * beta / (real(2.) * real(PI) * mass_g);
+        x_per_period = real(2.) * real(PI) / sqrt_beta;
+        x_per_period_nan = risnan(x_per_period);
+        if (rabs(dt) * invperiod > real(1.) && s.timestep_warning == 0) {
+            s.status |= POSI_SYS_WARN_TIMESTEP;
+            s.timestep_warning += 1;
+        }
+        real dtr0i = dt * r0i;
+        x = dtr0i * (real(1.) - dtr0i * eta0 * real(0.5) * r0i);
+    } else {
+        x = 0.;
+        x_per_period = 0.;
+        x_per_period_nan = true;
+    }
+    int converged = 0;
+    real old_x = x;
+    stiefel_gs3(beta, x, gs);
+    real eta0_gs1_zeta0_gs2 = eta0 * gs[1] + zeta0 * gs[2];
+    real ri = real(1.) / (r0 + eta0_gs1_zeta0_gs2);
+    x = ri * (x * eta0_gs1_zeta0_gs2 - eta0 * gs[2] - zeta0 * gs[3] + dt);
+    if (!x_per_period_nan && rabs(x - old_x) > real(0.01) * x_per_period) {
+        x = beta * dt / mass_g;
+        real prev_x[WHFAST_NMAX_QUART + 1];
+        for (int k = 0; k <= WHFAST_NMAX_QUART; ++k) prev_x[k] = 0.;
+        bool done = false;
+        for (int n_lag = 1; n_lag < WHFAST_NMAX_QUART && !done; ++n_lag) {
+            stiefel_gs3(beta, x, gs);
+            real f = r0 * x + eta0 * gs[2] + zeta0 * gs[3] - dt;
+            real fp = r0 + eta0 * gs[1] + zeta0 * gs[2];
+            real fpp = eta0 * gs[0] + zeta0 * gs[1];
+            real denom = fp + rsqrt_(rabs(real(16.) * fp * fp - real(20.) * f * fpp));
+            x = (x * denom - real(5.) * f) / denom;
+            for (int k = 1; k < n_lag; ++k) {
+                if (x == prev_x[k]) { converged = 1; done = true; break; }
+            }
+            if (!done) prev_x[n_lag] = x;
+        }
+        real e = eta0 * gs[1] + zeta0 * gs[2];
+        ri = real(1.) / (r0 + e);
+    } else {
+        real old_x2;
+        for (int k = 1; k < WHFAST_NMAX_NEWT; ++k) {
+            old_x2 = old_x;
+            old_x = x;
+            stiefel_gs3(beta, x, gs);
+            real e = eta0 * gs[1] + zeta0 * gs[2];
+            ri = real(1.) / (r0 + e);
+            x = ri * (x * e - eta0 * gs[2] - zeta0 * gs[3] + dt);
+            if (x == old_x || x == old_x2) { converged = 1; break; }
+        }
+    }
+    if (converged == 0) {
+        real x_min, x_max;
+        if (beta > real(0.)) {
+            x_min = x_per_period * rfloor(dt * invperiod);
+            x_max = x_min + x_per_period;
+        } else {
+            real h2 = r0 * r0 * v2 - eta0 * eta0;
+            real q = h2 / mass_g / (real(1.) + rsqrt_(real(1.) - h2 * beta / (mass_g * mass_g)));
+            real vq = rsqrt_(h2) / q;
+            x_min = real(1.) / (vq + r0 / dt);
+            x_max = dt / q;
+        }
+        x = (x_max + x_min) / real(2.);
+        int guard = 0;
+        for (;;) {
+            stiefel_gs3(beta, x, gs);
+            real sres = r0 * x + eta0 * gs[2] + zeta0 * gs[3] - dt;
+            if (sres >= real(0.)) x_max = x; else x_min = x;
+            x = (x_max + x_min) / real(2.);
+            if (rabs(x_max - x_min) / x_max <= real(1e-15)) break;
+            if (++guard > 4096) { set_fatal(s, POSI_SYS_BISECTION_LIMIT, i, i); break; }
+        }
+        real e = eta0 * gs[1] + zeta0 * gs[2];
+        ri = real(1.) / (r0 + e);
+    }
+    if (risnan(ri)) {
+        ri = 0.; gs[1] = 0.; gs[2] = 0.; gs[3] = 0.;
+    }
+    real f = -mass_g * gs[2] * r0i;
+    real g = dt - mass_g * gs[3];
+    real fd = -mass_g * gs[1] * r0i * ri;
+    real gd = -mass_g * gs[2] * ri;
+    AltCoords& pj = s.alt[i];
+    pj.pos.x += f * p1p.x + g * p1v.x;
+    pj.pos.y += f * p1p.y + g * p1v.y;
+    pj.pos.z += f * p1p.z + g * p1v.z;
+    pj.vel.x += fd * p1p.x + gd * p1v.x;
+    pj.vel.y += fd * p1p.y + gd * p1v.y;
+    pj.vel.z += fd * p1p.z + gd * p1v.z;
+}
+
+// :628-672
+static void kepler_steps(Sim& s, real dt) {
+    const int mm = s.host;
+    if (s.coords == POSI_JACOBI) {
+        real gm = s.p[mm].mass_g;
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            gm += s.alt[i].mass_g;
+            kepler_individual_step(s, i, gm, dt);
+        }
+    } else if (s.coords == POSI_DEMOCRATIC_HELIOCENTRIC) {
+        real gm = s.p[mm].mass_g;
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            kepler_individual_step(s, i, gm, dt);
+        }
+    } else {
+        real gm0 = s.p[mm].mass_g;
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            kepler_individual_step(s, i, gm0 + s.alt[i].mass_g, dt);
+        }
+    }
+    AltCoords& st = s.alt[mm];
+    st.pos.x += dt * st.vel.x;
+    st.pos.y += dt * st.vel.y;
+    st.pos.z += dt * st.vel.z;
+}
+
+// :889-933
+static void inertial_to_jacobi_posvel(Sim& s) {
+    const int mm = s.host;
+    const Particle& star = s.p[mm];
+    real m0 = star.mass;
+    real eta = m0;
+    real sx = eta * star.r.x, sy = eta * star.r.y, sz = eta * star.r.z;
+    real svx = eta * star.v.x, svy = eta * star.v.y, svz = eta * star.v.z;
+    for (int i = 0; i < s.n; ++i) {
+        if (i == mm) continue;
+        const Particle& q = s.p[i];
+        AltCoords& a = s.alt[i];
+        real ei = real(1.) / eta;
+        eta += q.mass;
+        real pme = eta * ei;
+        a.mass = q.mass;
+        a.mass_g = q.mass_g;
+        a.pos.x = q.r.x - sx * ei;
+        a.pos.y = q.r.y - sy * ei;
+        a.pos.z = q.r.z - sz * ei;
+        a.vel.x = q.v.x - svx * ei;
+        a.vel.y = q.v.y - svy * ei;
+        a.vel.z = q.v.z - svz * ei;
+        sx = sx * pme + q.mass * a.pos.x;
+        sy = sy * pme + q.mass * a.pos.y;
+        sz = sz * pme + q.mass * a.pos.z;
+        svx = svx * pme + q.mass * a.vel.x;
+        svy = svy * pme + q.mass * a.vel.y;
+        svz = svz * pme + q.mass * a.vel.z;
+    }
+    real mtot = eta;
+    real mtot_i = real(1.) / mtot;
+    AltCoords& st = s.alt[mm];
+    st.mass = mtot;
+    st.pos.x = sx * mtot_i; st.pos.y = sy * mtot_i; st.pos.z = sz * mtot_i;
+    st.vel.x = svx * mtot_i; st.vel.y = svy * mtot_i; st.vel.z = svz * mtot_i;
+}
+
+// :935-963
+static void inertial_to_jacobi_acc(Sim& s) {
+    const int mm = s.host;
+    const Particle& star = s.p[mm];
+    real eta = star.mass;
+    real sax = eta * star.a.x, say = eta * star.a.y, saz = eta * star.a.z;
+    for (int i = 0; i < s.n; ++i) {
+        if (i == mm) continue;
+        const Particle& q = s.p[i];
+        AltCoords& a = s.alt[i];
+        real ei = real(1.) / eta;
+        eta += q.mass;
+        real pme = eta * ei;
+        a.acc.x = q.a.x - sax * ei;
+        a.acc.y = q.a.y - say * ei;
+        a.acc.z = q.a.z - saz * ei;
+        sax = sax * pme + q.mass * a.acc.x;
+        say = say * pme + q.mass * a.acc.y;
+        saz = saz * pme + q.mass * a.acc.z;
+    }
+    real mtot_i = real(1.) / eta;
+    AltCoords& st = s.alt[mm];
+    st.acc.x = sax * mtot_i; st.acc.y = say * mtot_i; st.acc.z = saz * mtot_i;
+}
+
+// :973-1023
+static void inertial_to_whds_and_dh_posvel(Sim& s) {
+    const int mm = s.host;
+    const Particle& star = s.p[mm];
+    AltCoords& st = s.alt[mm];
+    st.pos = V3{0., 0., 0.}; st.vel = V3{0., 0., 0.}; st.mass = 0.; st.mass_g = 0.;
+    for (int k = -1; k < s.n; ++k) {
+        if (k == mm) continue;
+        const Particle& q = (k < 0) ? star : s.p[k];
+        st.pos.x += q.r.x * q.mass; st.pos.y += q.r.y * q.mass; st.pos.z += q.r.z * q.mass;
+        st.vel.x += q.v.x * q.mass; st.vel.y += q.v.y * q.mass; st.vel.z += q.v.z * q.mass;
+        st.mass += q.mass;
+        st.mass_g += q.mass_g;
+    }
+    real mtot = st.mass;
+    st.pos.x /= mtot; st.pos.y /= mtot; st.pos.z /= mtot;
+    st.vel.x /= mtot; st.vel.y /= mtot; st.vel.z /= mtot;
+    for (int i = 0; i < s.n; ++i) {
+        if (i == mm) continue;
+        const Particle& q = s.p[i];
+        AltCoords& a = s.alt[i];
+        a.pos.x = q.r.x - star.r.x; a.pos.y = q.r.y - star.r.y; a.pos.z = q.r.z - star.r.z;
+        a.vel.x = q.v.x - st.vel.x; a.vel.y = q.v.y - st.vel.y; a.vel.z = q.v.z - st.vel.z;
+        a.mass = q.mass;
+        a.mass_g = q.mass_g;
+        if (s.coords == POSI_WHDS) {
+            real factor = (star.mass + q.mass) / star.mass;
+            a.vel.x *= factor; a.vel.y *= factor; a.vel.z *= factor;
+        }
+    }
+}
+
+// :1034-1080
+static void jacobi_to_inertial_posvel(Sim& s) {
+    const int mm = s.host;
+    AltCoords& st = s.alt[mm];
+    real m0 = st.mass;
+    real eta = m0;
+    real sx = eta * st.pos.x, sy = eta * st.pos.y, sz = eta * st.pos.z;
+    real svx = eta * st.vel.x, svy = eta * st.vel.y, svz = eta * st.vel.z;
+    for (int i = s.n - 1; i >= 0; --i) {
+        if (i == mm) continue;
+        Particle& q = s.p[i];
+        const AltCoords& a = s.alt[i];
+        real ei = real(1.) / eta;
+        sx = (sx - q.mass * a.pos.x) * ei;
+        sy = (sy - q.mass * a.pos.y) * ei;
+        sz = (sz - q.mass * a.pos.z) * ei;
+        svx = (svx - q.mass * a.vel.x) * ei;
+        svy = (svy - q.mass * a.vel.y) * ei;
+        svz = (svz - q.mass * a.vel.z) * ei;
+        q.r.x = a.pos.x + sx; q.r.y = a.pos.y + sy; q.r.z = a.pos.z + sz;
+        q.v.x = a.vel.x + svx; q.v.y = a.vel.y + svy; q.v.z = a.vel.z + svz;
+        eta -= q.mass;
+        sx *= eta; sy *= eta; sz *= eta;
+        svx *= eta; svy *= eta; svz *= eta;
+    }
+    real mtot_i = real(1.) / eta;
+    Particle& star = s.p[mm];
+    star.r.x = sx * mtot_i; star.r.y = sy * mtot_i; star.r.z = sz * mtot_i;
+    star.v.x = svx * mtot_i; star.v.y = svy * mtot_i; star.v.z = svz * mtot_i;
+}
+
+// :1090-1155
+static void whds_and_dh_to_inertial_posvel(Sim& s) {
+    const int mm = s.host;
+    AltCoords& st = s.alt[mm];
+    Particle& star = s.p[mm];
+    {
+        real mtot = st.mass;
+        V3 nsp = st.pos;
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            const AltCoords& a = s.alt[i];
+            const Particle& q = s.p[i];
+            nsp.x -= a.pos.x * q.mass / mtot;
+            nsp.y -= a.pos.y * q.mass / mtot;
+            nsp.z -= a.pos.z * q.mass / mtot;
+        }
+        star.r = nsp;
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            const AltCoords& a = s.alt[i];
+            Particle& q = s.p[i];
+            q.r.x = a.pos.x + star.r.x; q.r.y = a.pos.y + star.r.y; q.r.z = a.pos.z + star.r.z;
+        }
+    }
+    real m0 = star.mass;
+    V3 nsv = st.vel;
+    for (int i = 0; i < s.n; ++i) {
+        if (i == mm) continue;
+        const AltCoords& a = s.alt[i];
+        Particle& q = s.p[i];
+        if (s.coords == POSI_WHDS) {
+            real factor = (m0 + q.mass) / m0;
+            q.v.x = a.vel.x / factor + st.vel.x;
+            q.v.y = a.vel.y / factor + st.vel.y;
+            q.v.z = a.vel.z / factor + st.vel.z;
+        } else {
+            q.v.x = a.vel.x + st.vel.x;
+            q.v.y = a.vel.y + st.vel.y;
+            q.v.z = a.vel.z + st.vel.z;
+        }
+        real factor = (s.coords == POSI_WHDS) ? q.mass / (m0 + q.mass) : q.mass / m0;
+        nsv.x -= a.vel.x * factor;
+        nsv.y -= a.vel.y * factor;
+        nsv.z -= a.vel.z * factor;
+    }
+    star.v = nsv;
+}
+
+static void inertial_to_alternative_posvel(Sim& s) {
+    if (s.coords == POSI_JACOBI) inertial_to_jacobi_posvel(s); else inertial_to_whds_and_dh_posvel(s);
+}
+static void alternative_to_inertial_posvel(Sim& s) {
+    if (s.coords == POSI_JACOBI) jacobi_to_inertial_posvel(s); else whds_and_dh_to_inertial_posvel(s);
+}
+
+// :495-556
+static void jump_step(Sim& s, real dt) {
+    const int mm = s.host;
+    if (s.coords == POSI_JACOBI) return;
+    real m0 = s.p[mm].mass;
+    real px = 0., py = 0., pz = 0.;
+    if (s.coords == POSI_DEMOCRATIC_HELIOCENTRIC) {
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            const AltCoords& a = s.alt[i];
+            const Particle& q = s.p[i];
+            px += q.mass * a.vel.x; py += q.mass * a.vel.y; pz += q.mass * a.vel.z;
+        }
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            AltCoords& a = s.alt[i];
+            a.pos.x += dt * px / m0;
+            a.pos.y += dt * py / m0;
+            a.pos.z += dt * pz / m0;
+        }
+    } else {
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            const AltCoords& a = s.alt[i];
+            const Particle& q = s.p[i];
+            real factor = m0 + q.mass;
+            px += q.mass * a.vel.x / factor; py += q.mass * a.vel.y / factor; pz += q.mass * a.vel.z / factor;
+        }
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            AltCoords& a = s.alt[i];
+            const Particle& q = s.p[i];
+            real factor = m0 + q.mass;
+            a.pos.x += dt * (px - (q.mass * a.vel.x / factor));
+            a.pos.y += dt * (py - (q.mass * a.vel.y / factor));
+            a.pos.z += dt * (pz - (q.mass * a.vel.z / factor));
+        }
+    }
+}
+
+// :558-625
+static void interaction_step(Sim& s, real dt) {
+    const int mm = s.host;
+    if (s.coords == POSI_JACOBI) {
+        inertial_to_jacobi_acc(s);
+        const real softening = 1e-12;
+        real eta = s.p[mm].mass;
+        int k = 0;
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            AltCoords& a = s.alt[i];
+            eta += a.mass;
+            a.vel.x += dt * a.acc.x;
+            a.vel.y += dt * a.acc.y;
+            a.vel.z += dt * a.acc.z;
+            if (k > 0) {
+                real rj2i = real(1.) / (powi(a.pos.x, 2) + powi(a.pos.y, 2) + powi(a.pos.z, 2) + softening);
+                real rji = rsqrt_(rj2i);
+                real rj3im = rji * rj2i * G * eta;
+                real prefac = dt * rj3im;
+                a.vel.x += prefac * a.pos.x;
+                a.vel.y += prefac * a.pos.y;
+                a.vel.z += prefac * a.pos.z;
+            }
+            ++k;
+        }
+    } else if (s.coords == POSI_DEMOCRATIC_HELIOCENTRIC) {
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            AltCoords& a = s.alt[i];
+            const Particle& q = s.p[i];
+            a.vel.x += dt * q.a.x; a.vel.y += dt * q.a.y; a.vel.z += dt * q.a.z;
+        }
+    } else {
+        real m0 = s.p[mm].mass;
+        for (int i = 0; i < s.n; ++i) {
+            if (i == mm) continue;
+            AltCoords& a = s.alt[i];
+            const Particle& q = s.p[i];
+            real factor = m0 + q.mass;
+            a.vel.x += dt * factor * q.a.x / m0;
+            a.vel.y += dt * factor * q.a.y / m0;
+            a.vel.z += dt * factor * q.a.z / m0;
+        }
+    }
+}
+
+// :226-233
+static int initialize_physical_values(Sim& s) {
+    if (s.t != real(0.)) return POSI_ERR_STATE;
+    calculate_spin_and_evolving_quantities(s, s.t, true);
+    calculate_roche_radiuses(s);
+    return POSI_OK;
+}
+
+// :235-305 (the historic snapshot itself is not written; its side effects on
+// the state -- the evolution update and the spin refresh -- are reproduced)
+static int iterate(Sim& s, bool* recovery_trigger) {
+    bool first = s.last_hist < real(0.);
+    bool hist_trig = s.last_hist + s.hist_period <= s.t;
+    bool rec_trig = s.last_rec + s.rec_period <= s.t;
+    if (first || hist_trig) {
+        inertial_to_heliocentric(s);
+        calculate_spin_and_evolving_quantities(s, s.t, true);
+        if (s.fatal()) return POSI_ERR_PHYSICS;
+        if (s.tides) tides_denergy_dt(s);
+        if (!first) s.last_hist += s.hist_period; else s.last_hist = 0.;
+        s.n_hist += 1;
+    }
+    const int ignore = (s.coords == POSI_JACOBI) ? 1 : 2;
+    const bool spin = s.tides || s.flat || s.evolution || s.gr;
+    integrate_velocity_dependent_forces(s, s.half_dt, spin, true);
+    if (s.fatal()) return POSI_ERR_PHYSICS;
+    // part 1: :469-479
+    inertial_to_alternative_posvel(s);
+    kepler_steps(s, s.half_dt);
+    jump_step(s, s.half_dt);
+    alternative_to_inertial_posvel(s);
+    if (s.fatal()) return POSI_ERR_PHYSICS;
+    gravity_calculate_acceleration(s, ignore);
+    if (s.fatal()) return POSI_ERR_PHYSICS;
+    // part 2: :482-491
+    interaction_step(s, s.dt);
+    jump_step(s, s.half_dt);
+    kepler_steps(s, s.half_dt);
+    alternative_to_inertial_posvel(s);
+    if (s.fatal()) return POSI_ERR_PHYSICS;
+    integrate_velocity_dependent_forces(s, s.half_dt, spin, false);
+    if (s.fatal()) return POSI_ERR_PHYSICS;
+    s.t += s.dt;
+    s.iteration += 1;
+    if (s.t + s.dt > s.time_limit) return POSI_COMPLETED;
+    *recovery_trigger = first || rec_trig;
+    return POSI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Flat layout <-> Sim
+// ---------------------------------------------------------------------------
+static void load(Sim& s, int64_t nmax, const int64_t* si, const double* sf, const int64_t* bi, const double* bf,
+                 const double* tables, const double* roche) {
+    s.n = (int)si[POSI_SI_N];
+    s.host = (int)si[POSI_SI_HOST];
+    s.coords = (int)si[POSI_SI_COORDS];
+    s.tides = si[POSI_SI_TIDES] != 0;
+    s.flat = si[POSI_SI_FLAT] != 0;
+    s.gr = si[POSI_SI_GR] != 0;
+    s.evolution = si[POSI_SI_EVOLUTION] != 0;
+    s.iteration = si[POSI_SI_ITERATION];
+    s.n_hist = si[POSI_SI_N_HIST];
+    s.timestep_warning = si[POSI_SI_TIMESTEP_WARNING];
+    s.status = si[POSI_SI_STATUS];
+    s.fail_step = si[POSI_SI_FAIL_STEP];
+    s.fail_pair = si[POSI_SI_FAIL_PAIR];
+    s.last_midpoint_iters = si[POSI_SI_LAST_MIDPOINT_ITERS];
+    s.dt = sf[POSI_SF_DT];
+    s.half_dt = sf[POSI_SF_HALF_DT];
+    s.t = sf[POSI_SF_TIME];
+    s.time_limit = sf[POSI_SF_TIME_LIMIT];
+    s.last_hist = sf[POSI_SF_LAST_HIST];
+    s.hist_period = sf[POSI_SF_HIST_PERIOD];
+    s.last_rec = sf[POSI_SF_LAST_REC];
+    s.rec_period = sf[POSI_SF_REC_PERIOD];
+    const int n = s.n;
+    s.p.assign(n, Particle());
+    s.ev.assign(n, Evolver());
+    s.alt.assign(n, AltCoords());
+    s.errv.assign(n, V3{0., 0., 0.});
+    s.errL.assign(n, V3{0., 0., 0.});
+    s.roche.assign((size_t)n * n, real(0.));
+    for (int b = 0; b < n; ++b) {
+        const int64_t* I = bi + (size_t)b * POSI_BI_COUNT;
+        const double* F = bf + (size_t)b * POSI_BF_COUNT;
+        Particle& q = s.p[b];
+        q.id = b;
+        q.mass = F[POSI_BF_MASS]; q.mass_g = F[POSI_BF_MASS_G]; q.radius = F[POSI_BF_RADIUS];
+        q.rg2 = F[POSI_BF_RG2]; q.moi = F[POSI_BF_MOI];
+        q.r = V3{F[POSI_BF_PX], F[POSI_BF_PY], F[POSI_BF_PZ]};
+        q.v = V3{F[POSI_BF_VX], F[POSI_BF_VY], F[POSI_BF_VZ]};
+        q.a = V3{F[POSI_BF_AX], F[POSI_BF_AY], F[POSI_BF_AZ]};
+        q.L = V3{F[POSI_BF_LX], F[POSI_BF_LY], F[POSI_BF_LZ]};
+        q.spin = V3{F[POSI_BF_SX], F[POSI_BF_SY], F[POSI_BF_SZ]};
+        q.nsv2 = F[POSI_BF_NSV2];
+        q.a_add = V3{F[POSI_BF_ADDAX], F[POSI_BF_ADDAY], F[POSI_BF_ADDAZ]};
+        q.dLdt = V3{F[POSI_BF_DLX], F[POSI_BF_DLY], F[POSI_BF_DLZ]};
+        s.errv[b] = V3{F[POSI_BF_EVX], F[POSI_BF_EVY], F[POSI_BF_EVZ]};
+        s.errL[b] = V3{F[POSI_BF_ELX], F[POSI_BF_ELY], F[POSI_BF_ELZ]};
+        q.tides.kind = (int)I[POSI_BI_TIDES_KIND];
+        q.tides.scaled_dissipation_factor = F[POSI_BF_SIGMA];
+        q.tides.love_number = F[POSI_BF_K2];
+        q.tides.denergy_dt = F[POSI_BF_DENERGY_DT];
+        q.tides.lag_angle = F[POSI_BF_LAG_ANGLE];
+        q.flat.kind = (int)I[POSI_BI_FLAT_KIND];
+        q.flat.love_number = F[POSI_BF_K2F];
+        q.gr.kind = (int)I[POSI_BI_GR_KIND];
+        q.evolution = (int)I[POSI_BI_EVO_TYPE];
+        Evolver& e = s.ev[b];
+        e.type = q.evolution;
+        e.len = I[POSI_BI_EVO_LEN];
+        e.left_index = I[POSI_BI_EVO_LEFT];
+        if (e.type != POSI_EVO_NON_EVOLVING && e.len > 0) {
+            const double* base = tables + I[POSI_BI_EVO_OFFSET];
+            e.time = base; e.radius = base + e.len; e.rg2 = base + 2 * e.len; e.love = base + 3 * e.len;
+        } else {
+            e.type = POSI_EVO_NON_EVOLVING;
+        }
+    }
+    if (roche) {
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) s.roche[(size_t)i * n + j] = roche[(size_t)i * nmax + j];
+    }
+}
+
+static void store(const Sim& s, int64_t nmax, int64_t* si, double* sf, int64_t* bi, double* bf, double* roche) {
+    si[POSI_SI_ITERATION] = s.iteration;
+    si[POSI_SI_N_HIST] = s.n_hist;
+    si[POSI_SI_TIMESTEP_WARNING] = s.timestep_warning;
+    si[POSI_SI_STATUS] = s.status;
+    si[POSI_SI_FAIL_STEP] = s.fail_step;
+    si[POSI_SI_FAIL_PAIR] = s.fail_pair;
+    si[POSI_SI_LAST_MIDPOINT_ITERS] = s.last_midpoint_iters;
+    sf[POSI_SF_TIME] = dv(s.t);
+    sf[POSI_SF_LAST_HIST] = dv(s.last_hist);
+    sf[POSI_SF_LAST_REC] = dv(s.last_rec);
+    for (int b = 0; b < s.n; ++b) {
+        int64_t* I = bi + (size_t)b * POSI_BI_COUNT;
+        double* F = bf + (size_t)b * POSI_BF_COUNT;
+        const Particle& q = s.p[b];
+        F[POSI_BF_RADIUS] = dv(q.radius); F[POSI_BF_RG2] = dv(q.rg2); F[POSI_BF_MOI] = dv(q.moi);
+        F[POSI_BF_PX] = dv(q.r.x); F[POSI_BF_PY] = dv(q.r.y); F[POSI_BF_PZ] = dv(q.r.z);
+        F[POSI_BF_VX] = dv(q.v.x); F[POSI_BF_VY] = dv(q.v.y); F[POSI_BF_VZ] = dv(q.v.z);
+        F[POSI_BF_AX] = dv(q.a.x); F[POSI_BF_AY] = dv(q.a.y); F[POSI_BF_AZ] = dv(q.a.z);
+        F[POSI_BF_LX] = dv(q.L.x); F[POSI_BF_LY] = dv(q.L.y); F[POSI_BF_LZ] = dv(q.L.z);
+        F[POSI_BF_SX] = dv(q.spin.x); F[POSI_BF_SY] = dv(q.spin.y); F[POSI_BF_SZ] = dv(q.spin.z);
+        F[POSI_BF_NSV2] = dv(q.nsv2);
+        F[POSI_BF_EVX] = dv(s.errv[b].x); F[POSI_BF_EVY] = dv(s.errv[b].y); F[POSI_BF_EVZ] = dv(s.errv[b].z);
+        F[POSI_BF_ELX] = dv(s.errL[b].x); F[POSI_BF_ELY] = dv(s.errL[b].y); F[POSI_BF_ELZ] = dv(s.errL[b].z);
+        F[POSI_BF_ADDAX] = dv(q.a_add.x); F[POSI_BF_ADDAY] = dv(q.a_add.y); F[POSI_BF_ADDAZ] = dv(q.a_add.z);
+        F[POSI_BF_DLX] = dv(q.dLdt.x); F[POSI_BF_DLY] = dv(q.dLdt.y); F[POSI_BF_DLZ] = dv(q.dLdt.z);
+        F[POSI_BF_DENERGY_DT] = dv(q.tides.denergy_dt);
+        F[POSI_BF_LAG_ANGLE] = dv(q.tides.lag_angle);
+        I[POSI_BI_EVO_LEFT] = s.ev[b].left_index;
+    }
+    if (roche) {
+        for (int i = 0; i < s.n; ++i)
+            for (int j = 0; j < s.n; ++j) roche[(size_t)i * nmax + j] = dv(s.roche[(size_t)i * s.n + j]);
+    }
+}
+
+}  // namespace orc
+
+// ---------------------------------------------------------------------------
+// C entry points (ctypes)
+// ---------------------------------------------------------------------------
+enum oracle_op {
+    ORACLE_ITERATE = 0,            // initialise if asked, then up to max_steps WHFast steps
+    ORACLE_GRAVITY = 1,            // gravity_calculate_acceleration(arg)
+    ORACLE_ADDITIONAL_EFFECTS = 2, // inertial_to_heliocentric + calculate_additional_effects
+    ORACLE_INITIALIZE = 3          // initialize_physical_values
+};
+
+extern "C" {
+
+// Runs `op` on every system of the flat-layout ensemble, in place.
+// roche: n_sys*nmax*nmax doubles (in/out) or NULL.
+// For ORACLE_ITERATE: steps_done[s] receives the steps performed and
+// result[s] the last iterate() code.  nthreads <= 0 uses the hardware count.
+int oracle_run(int op, int64_t n_sys, int64_t nmax, int64_t* sys_i64, double* sys_f64, int64_t* body_i64,
+               double* body_f64, const double* tables, double* roche, int64_t max_steps, int init_physical,
+               int arg, double t_arg, int nthreads, int64_t* steps_done, int64_t* result) {
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    if (nthreads > n_sys) nthreads = (int)std::max<int64_t>(1, n_sys);
+    std::atomic<int64_t> next{0};
+    auto worker = [&]() {
+        orc::Sim s;
+        for (;;) {
+            int64_t k = next.fetch_add(1);
+            if (k >= n_sys) break;
+            int64_t* si = sys_i64 + k * POSI_SI_COUNT;
+            double* sf = sys_f64 + k * POSI_SF_COUNT;
+            int64_t* bi = body_i64 + k * nmax * POSI_BI_COUNT;
+            double* bf = body_f64 + k * nmax * POSI_BF_COUNT;
+            double* ro = roche ? roche + k * nmax * nmax : nullptr;
+            orc::load(s, nmax, si, sf, bi, bf, tables, ro);
+            int64_t done = 0, rc = POSI_OK;
+            if (op == ORACLE_ITERATE) {
+                if (init_physical) rc = orc::initialize_physical_values(s);
+                while (rc == POSI_OK && done < max_steps && !s.fatal()) {
+                    bool rec = false;
+                    rc = orc::iterate(s, &rec);
+                    if (rc == POSI_OK || rc == POSI_COMPLETED) ++done;
+                }
+                if (rc == POSI_COMPLETED) s.status = (s.status & ~int64_t(POSI_SYS_FATAL_MASK)) | POSI_SYS_COMPLETED;
+            } else if (op == ORACLE_GRAVITY) {
+                orc::gravity_calculate_acceleration(s, arg);
+            } else if (op == ORACLE_ADDITIONAL_EFFECTS) {
+                orc::inertial_to_heliocentric(s);
+                orc::calculate_additional_effects(s, t_arg, (arg & 1) != 0, (arg & 2) != 0, (arg & 4) != 0);
+            } else if (op == ORACLE_INITIALIZE) {
+                rc = orc::initialize_physical_values(s);
+            }
+            orc::store(s, nmax, si, sf, bi, bf, ro);
+            if (steps_done) steps_done[k] = done;
+            if (result) result[k] = rc;
+        }
+    };
+    if (nthreads == 1) {
+        worker();
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nthreads; ++t) th.emplace_back(worker);
+        for (auto& t : th) t.join();
+    }
+    return 0;
+}
+
+#ifdef ORACLE_COUNT_FLOPS
+// Flop counters of the calling thread since the last reset: {all, divisions, square roots}.
+void oracle_flops(int64_t* out, int reset) {
+    out[0] = orc::g_flops; out[1] = orc::g_divs; out[2] = orc::g_sqrts;
+    if (reset) { orc::g_flops = 0; orc::g_divs = 0; orc::g_sqrts = 0; }
+}
+#endif
+
+double oracle_constant(int which) {
+    switch (which) {
+        case 0: return orc::G;
+        case 1: return orc::SPEED_OF_LIGHT_2;
+        case 2: return orc::DBL_EPSILON_2;
+        default: return 0.;
+    }
+}
+
+}  // extern "C"
