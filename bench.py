@@ -1,0 +1,367 @@
+"""Benchmark of the batched WHFast + tidal-effects kernel on GB300.
+
+Workload (``--workload ensemble8``, the default): 4096 independent systems of a
+0.08 Msun star and 7 planets (semi-major axes 0.01-0.07 AU, >= 8 mutual Hill
+radii apart), constant-time-lag tides + oblate flattening + Kidder GR, WHFast
+Jacobi, dt = 0.08 d, FP64, seeded synthetic inputs (posidonius_gb300.ensemble).
+One bench step = one WHFast step of every system.  Metric: system-steps/s.
+
+Timed region: K steps in R launches of the persistent kernel (CUDA graph
+replay); L2 is flushed before each launch and only the launches are timed,
+with CUDA events on the batch's stream.  ``e2e`` times the public C ABI with
+host buffers: upload of the whole ensemble from pinned memory, K steps,
+download of the whole state.
+
+``--impl reference`` times the reference's path on the host cores: the C++
+restatement of the Rust FP64 code (the Rust toolchain is not available), all
+threads, same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "system-steps/s"
+UNIT = "system-steps/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3000)
+    p.add_argument("--warmup", type=int, default=300)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="ensemble8", choices=["ensemble8", "uneven", "single"])
+    p.add_argument("--n-systems", type=int, default=None)
+    p.add_argument("--launches", type=int, default=10, help="timed launches (L2 flushed before each)")
+    p.add_argument("--mode", default="fast", choices=["fast", "exact"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    return p.parse_args()
+
+
+def make_workload(name, n_systems, rank=0):
+    from posidonius_gb300 import ensemble as E
+    seed = E.SEED_BASE + E.WORKLOAD_IDS[name] + 1000 * rank
+    if name == "ensemble8":
+        return E.workload_ensemble8(n_systems or 4096, seed=seed)
+    if name == "uneven":
+        return E.workload_uneven(n_systems or 16384, seed=seed)
+    return E.workload_single(seed=seed)
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                                 f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "power_w_max": max(power),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def fp64_peak():
+    from posidonius_gb300 import _lib
+    ms = ctypes.c_double()
+    tf = ctypes.c_double()
+    best = 0.0
+    for _ in range(3):
+        _lib.check(_lib.lib().posi_fp64_probe(152 * 8, 256, 20000, ctypes.byref(ms), ctypes.byref(tf)))
+        best = max(best, tf.value)
+    return best
+
+
+def newtonian_energy(state, s):
+    """Barycentric Newtonian energy of system s (kinetic + pairwise potential)."""
+    from posidonius_gb300 import ensemble as E, layout as L
+    n = int(state["sys_i64"][s, L.SI_N])
+    bf = state["body_f64"][s, :n]
+    m = bf[:, L.BF_MASS]
+    r = bf[:, L.POS]
+    v = bf[:, L.VEL]
+    ek = 0.5 * np.sum(m * np.sum(v * v, axis=1))
+    ep = 0.0
+    for i in range(n):
+        for j in range(i + 1, n):
+            ep -= E.G * m[i] * m[j] / np.linalg.norm(r[i] - r[j])
+    return ek + ep
+
+
+def pinned_like(state):
+    import torch
+    out = {}
+    for k in ("sys_i64", "sys_f64", "body_i64", "body_f64"):
+        t = torch.empty(state[k].shape, dtype=torch.int64 if k.endswith("i64") else torch.float64, pin_memory=True)
+        a = t.numpy()
+        a[...] = state[k]
+        out[k] = a
+        out["_t_" + k] = t
+    return out
+
+
+def cpu_leg(ens, steps_hint, seconds, nthreads):
+    """Time the oracle on a bounded sample of the workload (all threads)."""
+    import oracle
+    from posidonius_gb300 import layout as L
+    ns_total = ens["n_sys"]
+    n_sys = min(ns_total, max(64, nthreads * 16))
+    sub = {k: (v[:n_sys] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
+    sub["n_sys"] = n_sys
+    state, _, _ = oracle.run(sub, op=oracle.INITIALIZE, nthreads=nthreads)
+    # calibrate: 10 steps, then size the sample for ~`seconds`
+    t0 = time.perf_counter()
+    state, _, _ = oracle.run(state, max_steps=10, nthreads=nthreads)
+    per_step = (time.perf_counter() - t0) / 10
+    steps = max(10, int(seconds / max(per_step, 1e-9)))
+    t0 = time.perf_counter()
+    oracle.run(state, max_steps=steps, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    # algorithmic flops per system-step of this workload (counted restatement)
+    flo_state, _, _ = oracle.run({k: (v[:4] if isinstance(v, np.ndarray) and k != "tables" else v)
+                                  for k, v in state.items()} | {"n_sys": 4}, op=oracle.ITERATE, max_steps=1)
+    _, _, _, cnt = oracle.run(flo_state, max_steps=20, flops=True)
+    flops = cnt[0] / (4 * 20)
+    return {"value": n_sys * steps / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{n_sys} systems x {steps} WHFast steps of the {ens.get('_name', 'ensemble')} workload, "
+                      f"C++ restatement of the Rust FP64 path, {nthreads} threads, {dt:.1f} s",
+            "flops_per_system_step": flops}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    ens = make_workload(args.workload, args.n_systems)
+    nthreads = os.cpu_count() or 1
+    state, _, _ = oracle.run(ens, op=oracle.INITIALIZE, nthreads=nthreads)
+    # bounded sample: as many steps of the whole ensemble as fit ~a minute
+    t0 = time.perf_counter()
+    state, _, _ = oracle.run(state, max_steps=max(1, min(args.warmup, 3)), nthreads=nthreads)
+    per_step = (time.perf_counter() - t0) / max(1, min(args.warmup, 3))
+    steps = max(1, min(args.steps, int(60.0 / max(per_step, 1e-9))))
+    t0 = time.perf_counter()
+    state, _, _ = oracle.run(state, max_steps=steps, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    value = ens["n_sys"] * steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": min(args.warmup, 3), "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "n_systems": int(ens["n_sys"]), "bodies_per_system": int(ens["nmax"]),
+                   "dt_days": 0.08, "effects": "CTL tides + oblate flattening + Kidder GR"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"{int(ens['n_sys'])} systems x {steps} steps (C++ restatement of the Rust FP64 "
+                                   f"path; Rust toolchain unavailable)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    world, rank, local = dist_setup(args)
+    import torch
+
+    import posidonius_gb300 as pg
+    from posidonius_gb300 import layout as L
+
+    torch.cuda.set_device(local)
+    ens = make_workload(args.workload, args.n_systems, rank)
+    ens["_name"] = args.workload
+    mode = pg.FAST if args.mode == "fast" else pg.EXACT
+    batch = pg.Batch(ens, mode=mode)
+    batch.initialize_physical_values()
+    K = args.steps
+    R = max(1, min(args.launches, K))
+    spl = (K + R - 1) // R
+    W = max(3, args.warmup)
+    batch.iterate(W, min(W, spl))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    # ---- device-timed region -------------------------------------------------
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    total_ms = 0.0
+    launches = 0
+    done = 0
+    while done < K:
+        n = min(spl, K - done)
+        flush.fill_(float(done))
+        torch.cuda.synchronize()
+        batch.iterate(n, n)
+        ms, nl = batch.last_timing()
+        total_ms += ms
+        launches += nl
+        done += n
+    torch.cuda.synchronize()
+    barrier(world)
+    clock_info = clocks.stop()
+    total_ms = max_over_ranks(total_ms, world)
+    value = world * batch.n_sys * K / (total_ms * 1e-3)
+    per_launch_ms = total_ms / R
+
+    # ---- end-to-end through the C ABI with host buffers -----------------------
+    state = batch.get_state()
+    host = pinned_like(state)
+    out = {k: host[k].copy() for k in ("sys_i64", "sys_f64", "body_i64", "body_f64")}
+    out_p = pinned_like(out)
+    h2d = sum(host[k].nbytes for k in ("sys_i64", "sys_f64", "body_i64", "body_f64"))
+    d2h = h2d
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    batch.set_state(host)
+    batch.iterate(K, spl)
+    batch.get_state(out_p | {"roche": None})
+    e2e_s = time.perf_counter() - t0
+    barrier(world)
+    e2e_s = max_over_ranks(e2e_s, world)
+    e2e_value = world * batch.n_sys * K / e2e_s
+
+    # ---- accuracy and roofline --------------------------------------------------
+    final = batch.get_state()
+    st = final["sys_i64"][:, L.SI_STATUS]
+    peak = fp64_peak()
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded; posidonius_gb300.ensemble)",
+        "config": {"workload": args.workload, "n_systems": int(batch.n_sys), "bodies_per_system": int(batch.nmax),
+                   "dt_days": 0.08, "mode": args.mode, "steps_per_launch": spl, "timed_launches": R,
+                   "effects": "CTL tides + oblate flattening + Kidder GR", "coordinates": "Jacobi",
+                   "l2": f"flushed ({L2_FLUSH_BYTES >> 20} MiB write) before every timed launch",
+                   "parallelism": f"replicas x{world} (independent ensembles per GPU)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
+                "note": f"one C-ABI call chain: upload {h2d} B, {K} steps, download {d2h} B"},
+        "gpu_launches": int(launches),
+        "clocks": clock_info,
+        "systems_frozen": int(np.sum((st & L.SYS_FATAL_MASK) != 0)),
+        "midpoint_iterations": {str(k): int(v) for k, v in zip(*np.unique(final["sys_i64"][:, L.SI_LAST_MIDPOINT_ITERS],
+                                                                           return_counts=True))},
+    }
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        cpu = cpu_leg(ens, K, args.cpu_seconds, os.cpu_count() or 1)
+        flops = cpu.pop("flops_per_system_step")
+        result["cpu_baseline"] = cpu
+        # accuracy: relative Newtonian-energy deviation from the oracle's own
+        # trajectory on a sample of systems, after W + 2K steps from the start
+        sample = list(range(0, batch.n_sys, max(1, batch.n_sys // 8)))[:8]
+        sub = {k: (v[sample] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
+        sub["n_sys"] = len(sample)
+        ref, _, _ = oracle.run(sub, max_steps=W + 2 * K, init_physical=True, nthreads=len(sample))
+        errs = [abs(newtonian_energy(final, s) - newtonian_energy(ref, i)) / abs(newtonian_energy(ref, i))
+                for i, s in enumerate(sample)]
+        result["energy_rel_err_vs_oracle"] = max(errs)
+        result["accuracy_note"] = (f"relative deviation of the barycentric Newtonian energy from the oracle's own "
+                                   f"trajectory after {W + 2 * K} steps, max over {len(sample)} sampled systems")
+        achieved = flops * batch.n_sys * spl / (per_launch_ms * 1e-3) / 1e12
+        result["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                              "frac": achieved / peak, "traffic": None,
+                              "flops_per_system_step": flops,
+                              "peak_source": "measured in-run: posi_fp64_probe (DFMA chains; MEASURED_PEAKS.json "
+                                             "has no FP64 entry)",
+                              "note": "algorithmic flops (+ - * / sqrt = 1, counted by the oracle) per launch / "
+                                      "CUDA-event launch time"}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

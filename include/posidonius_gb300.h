@@ -157,8 +157,19 @@ typedef struct posi_batch posi_batch;
 /* ---- library ----------------------------------------------------------- */
 const char* posi_version(void);
 const char* posi_status_string(int status);
+/* Human-readable detail of the last failing call on this thread. */
+const char* posi_last_error(void);
 /* Number of CUDA devices visible (0 when none); never allocates. */
 int posi_device_count(void);
+
+/* ---- case files ---------------------------------------------------------- */
+
+/* src/integrator/output.rs:205-241 deserialize_json_snapshot, without the GPU:
+ * parse a WHFast JSON case into the flat layout.  Call once with null arrays
+ * to learn *n and *n_tables, then with buffers of POSI_SI_COUNT,
+ * POSI_SF_COUNT, n*POSI_BI_COUNT, n*POSI_BF_COUNT, n_tables and n*n elements. */
+int posi_read_case(const char* path, int64_t* n, int64_t* n_tables, int64_t* sys_i64, double* sys_f64,
+                   int64_t* body_i64, double* body_f64, double* tables, double* roche);
 
 /* ---- single system (the drop-in path: one system, one launch per step) -- */
 
@@ -167,10 +178,12 @@ int posi_device_count(void);
 posi_handle* posi_universe_from_json(const char* path, int mode, int* status);
 
 /* src/particles/universe.rs:73-175 Universe::new + src/integrator/whfast.rs:143-165
- * WHFast::new, from one system in the flat layout (nmax = n). */
+ * WHFast::new, from one system in the flat layout (nmax = n).  roche: n*n
+ * Roche radii of a resumed state (Universe.roche_radiuses), or NULL for zeros
+ * (a new run computes them in posi_initialize_physical_values). */
 posi_handle* posi_universe_from_arrays(const int64_t* sys_i64, const double* sys_f64,
                                        const int64_t* body_i64, const double* body_f64,
-                                       const double* tables, int64_t n_tables,
+                                       const double* tables, int64_t n_tables, const double* roche,
                                        int mode, int* status);
 
 void posi_destroy(posi_handle* h);
@@ -206,20 +219,22 @@ int posi_gravity_calculate_acceleration(posi_handle* h, int ignore_terms);
 int posi_calculate_additional_effects(posi_handle* h, double current_time, int evolution,
                                       int dangular_momentum_dt, int accelerations);
 
-/* Copy the state to/from the host in the flat layout (nmax = n). */
+/* Copy the state to/from the host in the flat layout (nmax = n); roche (n*n)
+ * may be NULL. */
 int posi_get_state(const posi_handle* h, int64_t* sys_i64, double* sys_f64,
-                   int64_t* body_i64, double* body_f64);
+                   int64_t* body_i64, double* body_f64, double* roche);
 int posi_set_state(posi_handle* h, const int64_t* sys_i64, const double* sys_f64,
                    const int64_t* body_i64, const double* body_f64);
 
 /* ---- batched ensembles (many independent systems, one persistent kernel) -- */
 
 /* nmax >= every system's n, nmax <= POSI_MAX_BODIES.  The arrays are copied to
- * the device; mapping selects the thread layout (POSI_MAP_AUTO = autotuned). */
+ * the device; roche is n_systems*nmax*nmax or NULL; mapping selects the
+ * thread layout (POSI_MAP_AUTO = autotuned). */
 posi_batch* posi_batch_create(int64_t n_systems, int64_t nmax,
                               const int64_t* sys_i64, const double* sys_f64,
                               const int64_t* body_i64, const double* body_f64,
-                              const double* tables, int64_t n_tables,
+                              const double* tables, int64_t n_tables, const double* roche,
                               int mode, int mapping, int* status);
 void posi_batch_destroy(posi_batch* b);
 
@@ -233,9 +248,12 @@ int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch)
 
 /* Host <-> device copies of the whole ensemble (flat layout). */
 int posi_batch_get_state(const posi_batch* b, int64_t* sys_i64, double* sys_f64,
-                         int64_t* body_i64, double* body_f64);
+                         int64_t* body_i64, double* body_f64, double* roche);
 int posi_batch_set_state(posi_batch* b, const int64_t* sys_i64, const double* sys_f64,
                          const int64_t* body_i64, const double* body_f64);
+
+/* Size of the ensemble. */
+int posi_batch_size(const posi_batch* b, int64_t* n_systems, int64_t* nmax);
 
 /* Mapping chosen for systems with n bodies (after autotuning), or -1. */
 int posi_batch_mapping_for(const posi_batch* b, int64_t n);
@@ -243,6 +261,14 @@ int posi_batch_mapping_for(const posi_batch* b, int64_t n);
 /* Device time of the last posi_batch_iterate in milliseconds (CUDA events on
  * the batch's stream) and the number of kernel launches it made. */
 int posi_batch_last_timing(const posi_batch* b, double* ms, int64_t* launches);
+
+/* ---- diagnostics ------------------------------------------------------- */
+
+/* FP64 rate of the device: `blocks` x `threads` threads, each running eight
+ * independent DFMA chains for `iters` iterations.  Reports the kernel time and
+ * the rate in TFLOP/s (a DFMA counts 2 flops).  Roofline denominator of the
+ * FP64-bound kernels. */
+int posi_fp64_probe(int blocks, int threads, int iters, double* ms, double* tflops);
 
 #ifdef __cplusplus
 }

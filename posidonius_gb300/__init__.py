@@ -1,0 +1,248 @@
+"""GB300-native WHFast + tidal-effects path of Posidonius (FP64, sm_103a).
+
+Python mirror of the reference's integrator surface over the C ABI
+(``include/posidonius_gb300.h``):
+
+* :func:`restore_snapshot` -- ``output::restore_snapshot``
+  (src/integrator/output.rs:178-203): open a WHFast JSON case, initialising
+  the physical values of a new run;
+* :class:`WHFast` -- one system, one kernel launch per step (the drop-in for
+  ``WHFast`` + ``Integrator``, src/integrator/whfast.rs, src/integrator/mod.rs);
+* :class:`Batch` -- many independent systems advanced by one persistent kernel
+  replayed through a CUDA graph.
+
+Nothing here computes physics on the CPU; every call goes to the CUDA library
+and raises when it is missing.
+"""
+import ctypes
+
+import numpy as np
+
+from . import layout
+from . import layout as L
+from ._lib import PosiError, check, lib, ptr
+
+__all__ = ["WHFast", "Batch", "restore_snapshot", "read_case", "layout", "PosiError", "EXACT", "FAST"]
+
+EXACT = L.MODE_EXACT
+FAST = L.MODE_FAST
+
+
+def read_case(path):
+    """Parse a WHFast JSON case into the flat layout (C++ reader, no GPU)."""
+    n = ctypes.c_int64()
+    nt = ctypes.c_int64()
+    check(lib().posi_read_case(str(path).encode(), ctypes.byref(n), ctypes.byref(nt), None, None, None, None, None,
+                               None))
+    n, nt = n.value, nt.value
+    out = {
+        "sys_i64": np.zeros(L.SI_COUNT, np.int64),
+        "sys_f64": np.zeros(L.SF_COUNT, np.float64),
+        "body_i64": np.zeros((n, L.BI_COUNT), np.int64),
+        "body_f64": np.zeros((n, L.BF_COUNT), np.float64),
+        "tables": np.zeros(max(nt, 1), np.float64),
+        "roche": np.zeros((n, n), np.float64),
+        "n": n,
+    }
+    check(lib().posi_read_case(str(path).encode(), None, None, ptr(out["sys_i64"], "i"), ptr(out["sys_f64"], "f"),
+                               ptr(out["body_i64"], "i"), ptr(out["body_f64"], "f"), ptr(out["tables"], "f"),
+                               ptr(out["roche"], "f")))
+    if nt == 0:
+        out["tables"] = np.zeros(1)
+    return out
+
+
+class WHFast:
+    """One system on the GPU (src/integrator/whfast.rs:99-1157)."""
+
+    def __init__(self, handle):
+        if not handle:
+            raise PosiError(L.ERR_ARG, "null handle")
+        self._h = ctypes.c_void_p(handle)
+
+    @classmethod
+    def from_json(cls, path, mode=EXACT):
+        st = ctypes.c_int(0)
+        h = lib().posi_universe_from_json(str(path).encode(), int(mode), ctypes.byref(st))
+        if not h:
+            check(st.value)
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, case, mode=EXACT):
+        st = ctypes.c_int(0)
+        arr = {k: np.ascontiguousarray(case[k], dtype=np.int64 if k.endswith("i64") else np.float64)
+               for k in ("sys_i64", "sys_f64", "body_i64", "body_f64", "tables")}
+        roche = case.get("roche")
+        roche = None if roche is None else np.ascontiguousarray(roche, dtype=np.float64)
+        h = lib().posi_universe_from_arrays(ptr(arr["sys_i64"], "i"), ptr(arr["sys_f64"], "f"),
+                                            ptr(arr["body_i64"], "i"), ptr(arr["body_f64"], "f"),
+                                            ptr(arr["tables"], "f"), int(arr["tables"].size), ptr(roche, "f"),
+                                            int(mode), ctypes.byref(st))
+        if not h:
+            check(st.value)
+        return cls(h)
+
+    def close(self):
+        if self._h:
+            lib().posi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # Integrator trait (src/integrator/mod.rs:16-27)
+    def get_n_particles(self):
+        n = ctypes.c_int64()
+        check(lib().posi_get_n_particles(self._h, ctypes.byref(n)))
+        return n.value
+
+    def get_current_time(self):
+        t = ctypes.c_double()
+        check(lib().posi_get_current_time(self._h, ctypes.byref(t)))
+        return t.value
+
+    def get_n_historic_snapshots(self):
+        n = ctypes.c_int64()
+        check(lib().posi_get_n_historic_snapshots(self._h, ctypes.byref(n)))
+        return n.value
+
+    def set_time_limit(self, time_limit):
+        check(lib().posi_set_time_limit(self._h, float(time_limit)))
+
+    def set_snapshot_periods(self, historic_period, recovery_period):
+        check(lib().posi_set_snapshot_periods(self._h, float(historic_period), float(recovery_period)))
+
+    def initialize_physical_values(self):
+        check(lib().posi_initialize_physical_values(self._h))
+
+    def iterate(self, n_steps=1):
+        """Advance up to n_steps steps.  Returns (status, steps_done, recovery_trigger);
+        status is layout.OK or layout.COMPLETED ("Simulation completed")."""
+        done = ctypes.c_int64()
+        rec = ctypes.c_int()
+        st = lib().posi_iterate(self._h, int(n_steps), ctypes.byref(done), ctypes.byref(rec))
+        check(st, ok=(L.OK, L.COMPLETED))
+        return st, done.value, bool(rec.value)
+
+    def run(self, max_steps=None):
+        """Iterate until the simulation completes or max_steps steps ran (the
+        loop of src/main.rs:158-176 without snapshot writing).  Returns the
+        number of steps performed."""
+        total = 0
+        while max_steps is None or total < max_steps:
+            st, done, _ = self.iterate(10**9 if max_steps is None else max_steps - total)
+            total += done
+            if st == L.COMPLETED or done == 0:
+                break
+        return total
+
+    # Universe methods (src/particles/universe.rs)
+    def gravity_calculate_acceleration(self, ignore_terms):
+        check(lib().posi_gravity_calculate_acceleration(self._h, int(ignore_terms)))
+
+    def calculate_additional_effects(self, current_time, evolution, dangular_momentum_dt, accelerations=True):
+        check(lib().posi_calculate_additional_effects(self._h, float(current_time), int(bool(evolution)),
+                                                      int(bool(dangular_momentum_dt)), int(bool(accelerations))))
+
+    def get_state(self):
+        n = self.get_n_particles()
+        out = {
+            "sys_i64": np.zeros(L.SI_COUNT, np.int64),
+            "sys_f64": np.zeros(L.SF_COUNT, np.float64),
+            "body_i64": np.zeros((n, L.BI_COUNT), np.int64),
+            "body_f64": np.zeros((n, L.BF_COUNT), np.float64),
+            "roche": np.zeros((n, n), np.float64),
+            "n": n,
+        }
+        check(lib().posi_get_state(self._h, ptr(out["sys_i64"], "i"), ptr(out["sys_f64"], "f"),
+                                   ptr(out["body_i64"], "i"), ptr(out["body_f64"], "f"), ptr(out["roche"], "f")))
+        return out
+
+    def set_state(self, state):
+        arr = {k: np.ascontiguousarray(state[k], dtype=np.int64 if k.endswith("i64") else np.float64)
+               for k in ("sys_i64", "sys_f64", "body_i64", "body_f64")}
+        check(lib().posi_set_state(self._h, ptr(arr["sys_i64"], "i"), ptr(arr["sys_f64"], "f"),
+                                   ptr(arr["body_i64"], "i"), ptr(arr["body_f64"], "f")))
+
+
+def restore_snapshot(path, mode=EXACT):
+    """src/integrator/output.rs:178-203: open a case; a new run (current_time 0)
+    gets its physical values initialised."""
+    w = WHFast.from_json(path, mode)
+    if w.get_current_time() == 0.0:
+        w.initialize_physical_values()
+    return w
+
+
+class Batch:
+    """An ensemble of independent systems (flat layout, nmax bodies each)."""
+
+    def __init__(self, ens, mode=FAST, mapping=L.MAP_AUTO):
+        self.n_sys = int(ens["n_sys"])
+        self.nmax = int(ens["nmax"])
+        arr = {k: np.ascontiguousarray(ens[k], dtype=np.int64 if k.endswith("i64") else np.float64)
+               for k in ("sys_i64", "sys_f64", "body_i64", "body_f64", "tables")}
+        roche = ens.get("roche")
+        roche = None if roche is None else np.ascontiguousarray(roche, dtype=np.float64)
+        st = ctypes.c_int(0)
+        h = lib().posi_batch_create(self.n_sys, self.nmax, ptr(arr["sys_i64"], "i"), ptr(arr["sys_f64"], "f"),
+                                    ptr(arr["body_i64"], "i"), ptr(arr["body_f64"], "f"), ptr(arr["tables"], "f"),
+                                    int(arr["tables"].size), ptr(roche, "f"), int(mode), int(mapping),
+                                    ctypes.byref(st))
+        if not h:
+            check(st.value)
+        self._h = ctypes.c_void_p(h)
+
+    def close(self):
+        if self._h:
+            lib().posi_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initialize_physical_values(self):
+        check(lib().posi_batch_initialize_physical_values(self._h))
+
+    def iterate(self, n_steps, steps_per_launch=0):
+        check(lib().posi_batch_iterate(self._h, int(n_steps), int(steps_per_launch)))
+
+    def last_timing(self):
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        check(lib().posi_batch_last_timing(self._h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def mapping_for(self, n):
+        return lib().posi_batch_mapping_for(self._h, int(n))
+
+    def empty_state(self):
+        ns, nm = self.n_sys, self.nmax
+        return {
+            "sys_i64": np.zeros((ns, L.SI_COUNT), np.int64),
+            "sys_f64": np.zeros((ns, L.SF_COUNT), np.float64),
+            "body_i64": np.zeros((ns, nm, L.BI_COUNT), np.int64),
+            "body_f64": np.zeros((ns, nm, L.BF_COUNT), np.float64),
+            "roche": np.zeros((ns, nm, nm), np.float64),
+            "n_sys": ns, "nmax": nm,
+        }
+
+    def get_state(self, out=None):
+        out = out or self.empty_state()
+        check(lib().posi_batch_get_state(self._h, ptr(out["sys_i64"], "i"), ptr(out["sys_f64"], "f"),
+                                         ptr(out["body_i64"], "i"), ptr(out["body_f64"], "f"),
+                                         ptr(out.get("roche"), "f")))
+        return out
+
+    def set_state(self, state):
+        arr = {k: np.ascontiguousarray(state[k], dtype=np.int64 if k.endswith("i64") else np.float64)
+               for k in ("sys_i64", "sys_f64", "body_i64", "body_f64")}
+        check(lib().posi_batch_set_state(self._h, ptr(arr["sys_i64"], "i"), ptr(arr["sys_f64"], "f"),
+                                         ptr(arr["body_i64"], "i"), ptr(arr["body_f64"], "f")))

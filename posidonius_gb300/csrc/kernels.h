@@ -1,0 +1,49 @@
+// kernels.h -- host-side launch interface of the two arithmetic modes.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace posi {
+
+// Device view of an ensemble; identical layout to POSI_NS::Dev.
+struct DevView {
+    int64_t n_sys, nmax, stride;
+    double* bf;
+    int64_t* bi;
+    double* sf;
+    int64_t* si;
+    const double* roche;
+    const double* tables;
+    const int32_t* list;
+    int32_t n_list;
+    int32_t* step_flags;
+};
+
+enum KernelOp { OP_STEPS = 0, OP_INIT = 1, OP_GRAVITY = 2, OP_EFFECTS = 3 };
+
+struct LaunchArgs {
+    int op;
+    int G;                 // lanes per system: 4, 8, 16 or 32
+    int64_t n_steps;       // OP_STEPS
+    int ignore_terms;      // OP_GRAVITY
+    double t_eval;         // OP_EFFECTS
+    int evolution, dl, acc;
+};
+
+// Returns cudaSuccess or the launch error.
+cudaError_t launch_exact(const DevView& d, const LaunchArgs& a, cudaStream_t stream);
+cudaError_t launch_fast(const DevView& d, const LaunchArgs& a, cudaStream_t stream);
+
+// Lanes per system used for a system of n bodies (0 when n is out of range).
+inline int group_size_for(int64_t n) {
+    if (n < 1) return 0;
+    if (n <= 4) return 4;
+    if (n <= 8) return 8;
+    if (n <= 16) return 16;
+    if (n <= 32) return 32;
+    return 0;
+}
+
+constexpr int kBlockThreads = 128;
+
+}  // namespace posi

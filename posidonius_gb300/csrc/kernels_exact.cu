@@ -1,0 +1,9 @@
+// Reference-order FP64 kernels: compiled with -fmad=false (no contraction).
+#define POSI_EXACT 1
+#include "kernels_impl.cuh"
+
+namespace posi {
+cudaError_t launch_exact(const DevView& d, const LaunchArgs& a, cudaStream_t stream) {
+    return posi_exact::launch_any(d, a, stream);
+}
+}  // namespace posi

@@ -1,0 +1,9 @@
+// Fast FP64 kernels: compiled with -fmad=true (multiply-add contraction).
+#define POSI_EXACT 0
+#include "kernels_impl.cuh"
+
+namespace posi {
+cudaError_t launch_fast(const DevView& d, const LaunchArgs& a, cudaStream_t stream) {
+    return posi_fast::launch_any(d, a, stream);
+}
+}  // namespace posi

@@ -1,0 +1,51 @@
+// kernels_impl.cuh -- launch wrappers, included once per arithmetic mode.
+#pragma once
+#include "kernels.h"
+#include "whfast_device.cuh"
+
+namespace POSI_NS {
+
+static_assert(sizeof(Dev) == sizeof(posi::DevView), "device view layout");
+
+template <int G>
+static cudaError_t launch_g(const posi::DevView& v, const posi::LaunchArgs& a, cudaStream_t stream) {
+    Dev d;
+    d.n_sys = v.n_sys; d.nmax = v.nmax; d.stride = v.stride;
+    d.bf = v.bf; d.bi = v.bi; d.sf = v.sf; d.si = v.si;
+    d.roche = v.roche; d.tables = v.tables; d.list = v.list; d.n_list = v.n_list;
+    d.step_flags = v.step_flags;
+    const int threads = posi::kBlockThreads;
+    const int groups_per_block = threads / G;
+    const int blocks = (int)((v.n_list + groups_per_block - 1) / groups_per_block);
+    if (blocks <= 0) return cudaSuccess;
+    const size_t smem = (size_t)groups_per_block * GroupSmem<G>::bytes;
+    switch (a.op) {
+        case posi::OP_STEPS:
+            whfast_steps_kernel<G><<<blocks, threads, smem, stream>>>(d, a.n_steps);
+            break;
+        case posi::OP_INIT:
+            init_physical_kernel<G><<<blocks, threads, smem, stream>>>(d);
+            break;
+        case posi::OP_GRAVITY:
+            gravity_kernel<G><<<blocks, threads, smem, stream>>>(d, a.ignore_terms);
+            break;
+        case posi::OP_EFFECTS:
+            additional_effects_kernel<G><<<blocks, threads, smem, stream>>>(d, a.t_eval, a.evolution, a.dl, a.acc);
+            break;
+        default:
+            return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_any(const posi::DevView& v, const posi::LaunchArgs& a, cudaStream_t stream) {
+    switch (a.G) {
+        case 4: return launch_g<4>(v, a, stream);
+        case 8: return launch_g<8>(v, a, stream);
+        case 16: return launch_g<16>(v, a, stream);
+        case 32: return launch_g<32>(v, a, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace POSI_NS

@@ -1,0 +1,682 @@
+// posi_host.cu -- C ABI of the GB300 WHFast + tidal-effects path.
+//
+// Host side of the boundary declared in include/posidonius_gb300.h: case
+// reading, device buffers (field-major SoA), host<->device transposes, the
+// per-body-count buckets of the batched kernel and the CUDA-graph replay of
+// its launches.  All floating-point work runs in the kernels of
+// kernels_exact.cu / kernels_fast.cu; the only host arithmetic is the Roche
+// radius table (libm pow, as src/particles/universe.rs:177-196 uses it) and
+// the step-time bookkeeping of the plain path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/posidonius_gb300.h"
+#include "case_reader.hpp"
+#include "json.hpp"
+#include "kernels.h"
+
+using posi::DevView;
+using posi::LaunchArgs;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+// AoS (row-major, rows x fields) <-> SoA (fields x rows) on the device.
+template <typename T>
+__global__ void aos_to_soa(const T* __restrict__ aos, T* __restrict__ soa, int64_t rows, int fields) {
+    const int64_t total = rows * fields;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = k / fields;
+        const int f = (int)(k % fields);
+        soa[(int64_t)f * rows + r] = aos[k];
+    }
+}
+template <typename T>
+__global__ void soa_to_aos(const T* __restrict__ soa, T* __restrict__ aos, int64_t rows, int fields) {
+    const int64_t total = rows * fields;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = k / fields;
+        const int f = (int)(k % fields);
+        aos[k] = soa[(int64_t)f * rows + r];
+    }
+}
+
+int grid_for(int64_t n) {
+    int64_t b = (n + 255) / 256;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 16));
+}
+
+#define CK(call)                                                        \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) {                                        \
+            g_last_error = std::string(#call) + ": " + cudaGetErrorString(e_); \
+            return POSI_ERR_CUDA;                                       \
+        }                                                               \
+    } while (0)
+
+}  // namespace
+
+struct Bucket {
+    int G;
+    int32_t offset;  // into the system list
+    int32_t count;
+};
+
+struct posi_batch {
+    int64_t n_sys = 0, nmax = 0, stride = 0;
+    int mode = POSI_MODE_EXACT;
+    int mapping = POSI_MAP_AUTO;
+    double* d_bf = nullptr;
+    int64_t* d_bi = nullptr;
+    double* d_sf = nullptr;
+    int64_t* d_si = nullptr;
+    double* d_roche = nullptr;
+    double* d_tables = nullptr;
+    int32_t* d_list = nullptr;
+    int32_t* d_flags = nullptr;
+    void* d_stage = nullptr;  // AoS staging buffer
+    size_t stage_bytes = 0;
+    int64_t n_tables = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<Bucket> buckets;
+    std::vector<int64_t> n_of;  // bodies per system
+    std::map<int64_t, int> mapping_of_n;
+    double last_ms = 0.;
+    int64_t last_launches = 0;
+    cudaGraphExec_t graph = nullptr;
+    int64_t graph_steps = -1, graph_spl = -1;
+
+    DevView view(int32_t list_offset, int32_t count) const {
+        DevView v;
+        v.n_sys = n_sys; v.nmax = nmax; v.stride = stride;
+        v.bf = d_bf; v.bi = d_bi; v.sf = d_sf; v.si = d_si;
+        v.roche = d_roche; v.tables = d_tables;
+        v.list = d_list + list_offset; v.n_list = count;
+        v.step_flags = d_flags;
+        return v;
+    }
+    cudaError_t launch(const Bucket& bk, const LaunchArgs& a0) const {
+        LaunchArgs a = a0;
+        a.G = bk.G;
+        DevView v = view(bk.offset, bk.count);
+        return mode == POSI_MODE_EXACT ? posi::launch_exact(v, a, stream) : posi::launch_fast(v, a, stream);
+    }
+};
+
+struct posi_handle {
+    posi_batch* b = nullptr;
+    // host mirror of the system scalars (the device copy is authoritative)
+    std::vector<int64_t> si;
+    std::vector<double> sf;
+};
+
+namespace {
+
+void free_batch(posi_batch* b) {
+    if (!b) return;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    cudaFree(b->d_bf); cudaFree(b->d_bi); cudaFree(b->d_sf); cudaFree(b->d_si);
+    cudaFree(b->d_roche); cudaFree(b->d_tables); cudaFree(b->d_list); cudaFree(b->d_flags);
+    cudaFree(b->d_stage);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int validate_system(const int64_t* si, int64_t nmax, std::string& err) {
+    const int64_t n = si[POSI_SI_N], host = si[POSI_SI_HOST], coords = si[POSI_SI_COORDS];
+    if (n < 1 || n > nmax) { err = "system body count out of range"; return POSI_ERR_ARG; }
+    if (posi::group_size_for(n) == 0) { err = "too many bodies for the batched kernel"; return POSI_ERR_UNSUPPORTED; }
+    if (host < 0 || host >= n) { err = "host index out of range"; return POSI_ERR_ARG; }
+    if (coords < POSI_JACOBI || coords > POSI_WHDS) { err = "unknown coordinates type"; return POSI_ERR_ARG; }
+    return POSI_OK;
+}
+
+// Upload host AoS arrays into the device SoA array `dst` (rows x fields).
+template <typename T>
+int upload_aos(posi_batch* b, const T* host, T* dst, int64_t rows, int fields) {
+    const size_t bytes = (size_t)rows * fields * sizeof(T);
+    CK(cudaMemcpyAsync(b->d_stage, host, bytes, cudaMemcpyHostToDevice, b->stream));
+    aos_to_soa<T><<<grid_for(rows * fields), 256, 0, b->stream>>>((const T*)b->d_stage, dst, rows, fields);
+    CK(cudaGetLastError());
+    return POSI_OK;
+}
+
+template <typename T>
+int download_aos(const posi_batch* b, T* host, const T* src, int64_t rows, int fields) {
+    const size_t bytes = (size_t)rows * fields * sizeof(T);
+    soa_to_aos<T><<<grid_for(rows * fields), 256, 0, b->stream>>>(src, (T*)b->d_stage, rows, fields);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host, b->d_stage, bytes, cudaMemcpyDeviceToHost, b->stream));
+    return POSI_OK;
+}
+
+int build_buckets(posi_batch* b, const int64_t* sys_i64) {
+    // group the systems by lanes per system (one body per lane)
+    std::map<int, std::vector<int32_t>> by_g;
+    b->n_of.resize(b->n_sys);
+    for (int64_t s = 0; s < b->n_sys; ++s) {
+        const int64_t n = sys_i64[s * POSI_SI_COUNT + POSI_SI_N];
+        b->n_of[s] = n;
+        int G = posi::group_size_for(n);
+        if (b->mapping >= POSI_MAP_LANES4 && b->mapping <= POSI_MAP_WARP && b->mapping >= G) G = b->mapping;
+        by_g[G].push_back((int32_t)s);
+        b->mapping_of_n[n] = G;
+    }
+    std::vector<int32_t> list;
+    b->buckets.clear();
+    for (auto& kv : by_g) {
+        Bucket bk;
+        bk.G = kv.first;
+        bk.offset = (int32_t)list.size();
+        bk.count = (int32_t)kv.second.size();
+        list.insert(list.end(), kv.second.begin(), kv.second.end());
+        b->buckets.push_back(bk);
+    }
+    CK(cudaMalloc(&b->d_list, std::max<size_t>(1, list.size()) * sizeof(int32_t)));
+    CK(cudaMemcpyAsync(b->d_list, list.data(), list.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return POSI_OK;
+}
+
+posi_batch* create_batch(int64_t n_sys, int64_t nmax, const int64_t* si, const double* sf, const int64_t* bi,
+                         const double* bf, const double* tables, int64_t n_tables, const double* roche, int mode,
+                         int mapping, int* status) {
+    auto fail = [&](int code, posi_batch* b) -> posi_batch* {
+        free_batch(b);
+        if (status) *status = code;
+        return nullptr;
+    };
+    if (n_sys < 1 || nmax < 1 || nmax > POSI_MAX_BODIES || !si || !sf || !bi || !bf) {
+        g_last_error = "bad arguments";
+        return fail(POSI_ERR_ARG, nullptr);
+    }
+    if (mode != POSI_MODE_EXACT && mode != POSI_MODE_FAST) { g_last_error = "unknown mode"; return fail(POSI_ERR_ARG, nullptr); }
+    for (int64_t s = 0; s < n_sys; ++s) {
+        std::string err;
+        int rc = validate_system(si + s * POSI_SI_COUNT, nmax, err);
+        if (rc != POSI_OK) { g_last_error = err; return fail(rc, nullptr); }
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        g_last_error = "no CUDA device";
+        return fail(POSI_ERR_CUDA, nullptr);
+    }
+    posi_batch* b = new posi_batch();
+    b->n_sys = n_sys;
+    b->nmax = nmax;
+    b->stride = n_sys * nmax;
+    b->mode = mode;
+    b->mapping = mapping;
+    b->n_tables = std::max<int64_t>(1, n_tables);
+    auto ok = [&](cudaError_t e) {
+        if (e != cudaSuccess) { g_last_error = cudaGetErrorString(e); return false; }
+        return true;
+    };
+    if (!ok(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) || !ok(cudaEventCreate(&b->ev0)) ||
+        !ok(cudaEventCreate(&b->ev1)))
+        return fail(POSI_ERR_CUDA, b);
+    const size_t nb = (size_t)b->stride;
+    b->stage_bytes = std::max({nb * POSI_BF_COUNT * sizeof(double), nb * POSI_BI_COUNT * sizeof(int64_t),
+                               (size_t)n_sys * POSI_SF_COUNT * sizeof(double),
+                               (size_t)n_sys * POSI_SI_COUNT * sizeof(int64_t), nb * nmax * sizeof(double)});
+    if (!ok(cudaMalloc(&b->d_bf, nb * POSI_BF_COUNT * sizeof(double))) ||
+        !ok(cudaMalloc(&b->d_bi, nb * POSI_BI_COUNT * sizeof(int64_t))) ||
+        !ok(cudaMalloc(&b->d_sf, (size_t)n_sys * POSI_SF_COUNT * sizeof(double))) ||
+        !ok(cudaMalloc(&b->d_si, (size_t)n_sys * POSI_SI_COUNT * sizeof(int64_t))) ||
+        !ok(cudaMalloc(&b->d_roche, nb * nmax * sizeof(double))) ||
+        !ok(cudaMalloc(&b->d_tables, (size_t)b->n_tables * sizeof(double))) ||
+        !ok(cudaMalloc(&b->d_flags, (size_t)n_sys * sizeof(int32_t))) || !ok(cudaMalloc(&b->d_stage, b->stage_bytes)))
+        return fail(POSI_ERR_CUDA, b);
+    int rc;
+    if ((rc = upload_aos<int64_t>(b, si, b->d_si, n_sys, POSI_SI_COUNT)) != POSI_OK ||
+        (rc = upload_aos<double>(b, sf, b->d_sf, n_sys, POSI_SF_COUNT)) != POSI_OK ||
+        (rc = upload_aos<int64_t>(b, bi, b->d_bi, b->stride, POSI_BI_COUNT)) != POSI_OK ||
+        (rc = upload_aos<double>(b, bf, b->d_bf, b->stride, POSI_BF_COUNT)) != POSI_OK)
+        return fail(rc, b);
+    if (!ok(cudaStreamSynchronize(b->stream))) return fail(POSI_ERR_CUDA, b);
+    if (roche) {
+        if (!ok(cudaMemcpyAsync(b->d_roche, roche, nb * nmax * sizeof(double), cudaMemcpyHostToDevice, b->stream)))
+            return fail(POSI_ERR_CUDA, b);
+    } else if (!ok(cudaMemsetAsync(b->d_roche, 0, nb * nmax * sizeof(double), b->stream))) {
+        return fail(POSI_ERR_CUDA, b);
+    }
+    if (tables && n_tables > 0) {
+        if (!ok(cudaMemcpyAsync(b->d_tables, tables, (size_t)n_tables * sizeof(double), cudaMemcpyHostToDevice, b->stream)))
+            return fail(POSI_ERR_CUDA, b);
+    } else if (!ok(cudaMemsetAsync(b->d_tables, 0, (size_t)b->n_tables * sizeof(double), b->stream))) {
+        return fail(POSI_ERR_CUDA, b);
+    }
+    if (!ok(cudaMemsetAsync(b->d_flags, 0, (size_t)n_sys * sizeof(int32_t), b->stream))) return fail(POSI_ERR_CUDA, b);
+    if ((rc = build_buckets(b, si)) != POSI_OK) return fail(rc, b);
+    if (!ok(cudaStreamSynchronize(b->stream))) return fail(POSI_ERR_CUDA, b);
+    if (status) *status = POSI_OK;
+    return b;
+}
+
+int run_op(posi_batch* b, const LaunchArgs& a) {
+    for (const Bucket& bk : b->buckets) CK(b->launch(bk, a));
+    CK(cudaStreamSynchronize(b->stream));
+    return POSI_OK;
+}
+
+// src/particles/universe.rs:177-196 (libm pow, like Rust's f64::powf)
+int compute_roche(posi_batch* b) {
+    const size_t nb = (size_t)b->stride;
+    std::vector<double> mass(nb), radius(nb), roche(nb * b->nmax, 0.);
+    CK(cudaMemcpyAsync(mass.data(), b->d_bf + (size_t)POSI_BF_MASS * nb, nb * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaMemcpyAsync(radius.data(), b->d_bf + (size_t)POSI_BF_RADIUS * nb, nb * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    for (int64_t s = 0; s < b->n_sys; ++s) {
+        const int64_t n = b->n_of[s];
+        const size_t o = (size_t)s * b->nmax;
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t j = 0; j < n; ++j) {
+                if (i == j) continue;
+                const double ma = mass[o + i], mb = mass[o + j];
+                double r;
+                if (ma > mb) r = (radius[o + j] / 0.462) * std::pow(ma / mb, 1. / 3.);
+                else r = (radius[o + i] / 0.462) * std::pow(mb / ma, 1. / 3.);
+                roche[(o + i) * b->nmax + j] = r;
+            }
+    }
+    CK(cudaMemcpyAsync(b->d_roche, roche.data(), roche.size() * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return POSI_OK;
+}
+
+int batch_get(const posi_batch* b, int64_t* si, double* sf, int64_t* bi, double* bf, double* roche) {
+    int rc;
+    if (si && (rc = download_aos<int64_t>(b, si, b->d_si, b->n_sys, POSI_SI_COUNT)) != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    if (sf && (rc = download_aos<double>(b, sf, b->d_sf, b->n_sys, POSI_SF_COUNT)) != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    if (bi && (rc = download_aos<int64_t>(b, bi, b->d_bi, b->stride, POSI_BI_COUNT)) != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    if (bf && (rc = download_aos<double>(b, bf, b->d_bf, b->stride, POSI_BF_COUNT)) != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    if (roche)
+        CK(cudaMemcpyAsync(roche, b->d_roche, (size_t)b->stride * b->nmax * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    return POSI_OK;
+}
+
+int batch_set(posi_batch* b, const int64_t* si, const double* sf, const int64_t* bi, const double* bf) {
+    int rc;
+    if (si && (rc = upload_aos<int64_t>(b, si, b->d_si, b->n_sys, POSI_SI_COUNT)) != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    if (sf && (rc = upload_aos<double>(b, sf, b->d_sf, b->n_sys, POSI_SF_COUNT)) != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    if (bi && (rc = upload_aos<int64_t>(b, bi, b->d_bi, b->stride, POSI_BI_COUNT)) != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    if (bf && (rc = upload_aos<double>(b, bf, b->d_bf, b->stride, POSI_BF_COUNT)) != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    return POSI_OK;
+}
+
+int refresh_mirror(posi_handle* h) {
+    return batch_get(h->b, h->si.data(), h->sf.data(), nullptr, nullptr, nullptr);
+}
+
+posi_handle* make_handle(posi_batch* b, const int64_t* si, const double* sf) {
+    posi_handle* h = new posi_handle();
+    h->b = b;
+    h->si.assign(si, si + POSI_SI_COUNT);
+    h->sf.assign(sf, sf + POSI_SF_COUNT);
+    return h;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* posi_version(void) { return "posidonius-gb300 0.1 (sm_103a, FP64)"; }
+
+const char* posi_status_string(int status) {
+    switch (status) {
+        case POSI_OK: return "ok";
+        case POSI_COMPLETED: return "Simulation completed";
+        case POSI_ERR_ARG: return "bad argument";
+        case POSI_ERR_IO: return "file missing or unreadable";
+        case POSI_ERR_PARSE: return "malformed case";
+        case POSI_ERR_UNSUPPORTED: return "unsupported case";
+        case POSI_ERR_CUDA: return "CUDA error";
+        case POSI_ERR_PHYSICS: return "physics event (collision, Roche limit, ejection)";
+        case POSI_ERR_STATE: return "invalid state";
+        default: return "unknown status";
+    }
+}
+
+// Detail of the last error on this thread (not part of the reference surface).
+const char* posi_last_error(void) { return g_last_error.c_str(); }
+
+int posi_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+}  // extern "C"
+
+namespace {
+int load_case_file(const char* path, posi::FlatSystem& fs) {
+    if (!path) return POSI_ERR_ARG;
+    std::ifstream f(path, std::ios::binary);
+    if (!f) {
+        g_last_error = std::string("cannot open ") + path;
+        return POSI_ERR_IO;
+    }
+    std::stringstream ss;
+    ss << f.rdbuf();
+    const std::string text = ss.str();
+    posi::json::Value doc;
+    std::string err;
+    posi::json::Parser parser(text.data(), text.size());
+    if (!parser.parse(doc, err)) {
+        g_last_error = "JSON: " + err;
+        return POSI_ERR_PARSE;
+    }
+    int rc = posi::read_case(doc, fs, err);
+    if (rc != POSI_OK) g_last_error = err;
+    return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int posi_read_case(const char* path, int64_t* n, int64_t* n_tables, int64_t* sys_i64, double* sys_f64,
+                   int64_t* body_i64, double* body_f64, double* tables, double* roche) {
+    posi::FlatSystem fs;
+    int rc = load_case_file(path, fs);
+    if (rc != POSI_OK) return rc;
+    if (n) *n = fs.n;
+    if (n_tables) *n_tables = (int64_t)fs.tables.size();
+    if (sys_i64) std::memcpy(sys_i64, fs.si.data(), fs.si.size() * sizeof(int64_t));
+    if (sys_f64) std::memcpy(sys_f64, fs.sf.data(), fs.sf.size() * sizeof(double));
+    if (body_i64) std::memcpy(body_i64, fs.bi.data(), fs.bi.size() * sizeof(int64_t));
+    if (body_f64) std::memcpy(body_f64, fs.bf.data(), fs.bf.size() * sizeof(double));
+    if (tables && !fs.tables.empty()) std::memcpy(tables, fs.tables.data(), fs.tables.size() * sizeof(double));
+    if (roche) std::memcpy(roche, fs.roche.data(), fs.roche.size() * sizeof(double));
+    return POSI_OK;
+}
+
+posi_handle* posi_universe_from_json(const char* path, int mode, int* status) {
+    posi::FlatSystem fs;
+    int rc = load_case_file(path, fs);
+    if (rc != POSI_OK) {
+        if (status) *status = rc;
+        return nullptr;
+    }
+    posi_batch* b = create_batch(1, fs.n, fs.si.data(), fs.sf.data(), fs.bi.data(), fs.bf.data(),
+                                 fs.tables.empty() ? nullptr : fs.tables.data(), (int64_t)fs.tables.size(),
+                                 fs.roche.data(), mode, POSI_MAP_AUTO, status);
+    if (!b) return nullptr;
+    return make_handle(b, fs.si.data(), fs.sf.data());
+}
+
+posi_handle* posi_universe_from_arrays(const int64_t* sys_i64, const double* sys_f64, const int64_t* body_i64,
+                                       const double* body_f64, const double* tables, int64_t n_tables,
+                                       const double* roche, int mode, int* status) {
+    if (!sys_i64 || !sys_f64) { if (status) *status = POSI_ERR_ARG; return nullptr; }
+    const int64_t n = sys_i64[POSI_SI_N];
+    posi_batch* b = create_batch(1, n, sys_i64, sys_f64, body_i64, body_f64, tables, n_tables, roche, mode,
+                                 POSI_MAP_AUTO, status);
+    if (!b) return nullptr;
+    return make_handle(b, sys_i64, sys_f64);
+}
+
+void posi_destroy(posi_handle* h) {
+    if (!h) return;
+    free_batch(h->b);
+    delete h;
+}
+
+int posi_get_n_particles(const posi_handle* h, int64_t* n) {
+    if (!h || !n) return POSI_ERR_ARG;
+    *n = h->si[POSI_SI_N];
+    return POSI_OK;
+}
+
+int posi_get_current_time(const posi_handle* h, double* t) {
+    if (!h || !t) return POSI_ERR_ARG;
+    *t = h->sf[POSI_SF_TIME];
+    return POSI_OK;
+}
+
+int posi_get_n_historic_snapshots(const posi_handle* h, int64_t* n) {
+    if (!h || !n) return POSI_ERR_ARG;
+    *n = h->si[POSI_SI_N_HIST];
+    return POSI_OK;
+}
+
+// src/integrator/whfast.rs:187-208 (the evolving-body table-range check of the
+// reference does not apply: tables are read as they stand)
+int posi_set_time_limit(posi_handle* h, double time_limit) {
+    if (!h) return POSI_ERR_ARG;
+    if (time_limit > 0. && h->sf[POSI_SF_TIME_LIMIT] != time_limit) {
+        if (time_limit < h->sf[POSI_SF_TIME_LIMIT] && time_limit < h->sf[POSI_SF_TIME]) {
+            g_last_error = "new time limit is smaller than the current time";
+            return POSI_ERR_STATE;
+        }
+        h->sf[POSI_SF_TIME_LIMIT] = time_limit;
+        // a completed run may continue under a larger limit
+        if ((h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) == POSI_SYS_COMPLETED)
+            h->si[POSI_SI_STATUS] &= ~(int64_t)POSI_SYS_FATAL_MASK;
+        return batch_set(h->b, h->si.data(), h->sf.data(), nullptr, nullptr);
+    }
+    return POSI_OK;
+}
+
+// src/integrator/whfast.rs:210-224
+int posi_set_snapshot_periods(posi_handle* h, double historic_period, double recovery_period) {
+    if (!h) return POSI_ERR_ARG;
+    if (historic_period > 0.) h->sf[POSI_SF_HIST_PERIOD] = historic_period;
+    if (recovery_period > 0.) h->sf[POSI_SF_REC_PERIOD] = recovery_period;
+    return batch_set(h->b, nullptr, h->sf.data(), nullptr, nullptr);
+}
+
+int posi_initialize_physical_values(posi_handle* h) {
+    if (!h) return POSI_ERR_ARG;
+    if (h->sf[POSI_SF_TIME] != 0.) {
+        g_last_error = "physical values cannot be initialized on a resumed simulation";
+        return POSI_ERR_STATE;
+    }
+    return posi_batch_initialize_physical_values(h->b) == POSI_OK ? refresh_mirror(h) : POSI_ERR_CUDA;
+}
+
+int posi_iterate(posi_handle* h, int64_t n_steps, int64_t* steps_done, int* recovery_trigger) {
+    if (!h || n_steps < 0) return POSI_ERR_ARG;
+    if (steps_done) *steps_done = 0;
+    if (recovery_trigger) *recovery_trigger = 0;
+    if (h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) {
+        return (h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) == POSI_SYS_COMPLETED ? POSI_COMPLETED : POSI_ERR_PHYSICS;
+    }
+    // Predict, with the kernel's own time arithmetic, how many steps run before
+    // a step reports a recovery trigger or completes the simulation; the plain
+    // path then launches exactly that many one-step kernels.
+    double t = h->sf[POSI_SF_TIME], last_hist = h->sf[POSI_SF_LAST_HIST];
+    const double dt = h->sf[POSI_SF_DT], limit = h->sf[POSI_SF_TIME_LIMIT];
+    const double hp = h->sf[POSI_SF_HIST_PERIOD], lr = h->sf[POSI_SF_LAST_REC], rp = h->sf[POSI_SF_REC_PERIOD];
+    int64_t k = 0;
+    bool rec = false;
+    while (k < n_steps) {
+        const bool first = last_hist < 0.;
+        const bool ht = last_hist + hp <= t;
+        const bool rt = lr + rp <= t;
+        if (first || ht) last_hist = first ? 0. : last_hist + hp;
+        t += dt;
+        ++k;
+        if (t + dt > limit) break;
+        if (first || rt) { rec = true; break; }
+    }
+    LaunchArgs a{};
+    a.op = posi::OP_STEPS;
+    a.n_steps = 1;
+    posi_batch* b = h->b;
+    for (int64_t i = 0; i < k; ++i) {
+        for (const Bucket& bk : b->buckets) CK(b->launch(bk, a));
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    const int64_t it0 = h->si[POSI_SI_ITERATION];
+    int rc = refresh_mirror(h);
+    if (rc != POSI_OK) return rc;
+    if (steps_done) *steps_done = h->si[POSI_SI_ITERATION] - it0;
+    const int64_t fatal = h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK;
+    if (fatal == POSI_SYS_COMPLETED) return POSI_COMPLETED;
+    if (fatal) return POSI_ERR_PHYSICS;
+    if (recovery_trigger) *recovery_trigger = rec ? 1 : 0;
+    return POSI_OK;
+}
+
+int posi_gravity_calculate_acceleration(posi_handle* h, int ignore_terms) {
+    if (!h || ignore_terms < 0 || ignore_terms > 2) return POSI_ERR_ARG;
+    LaunchArgs a{};
+    a.op = posi::OP_GRAVITY;
+    a.ignore_terms = ignore_terms;
+    int rc = run_op(h->b, a);
+    if (rc != POSI_OK) return rc;
+    rc = refresh_mirror(h);
+    if (rc != POSI_OK) return rc;
+    return (h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) && (h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) != POSI_SYS_COMPLETED
+               ? POSI_ERR_PHYSICS : POSI_OK;
+}
+
+int posi_calculate_additional_effects(posi_handle* h, double current_time, int evolution, int dangular_momentum_dt,
+                                      int accelerations) {
+    if (!h) return POSI_ERR_ARG;
+    if (!accelerations) {
+        g_last_error = "the WHFast path always evaluates accelerations";
+        return POSI_ERR_UNSUPPORTED;
+    }
+    LaunchArgs a{};
+    a.op = posi::OP_EFFECTS;
+    a.t_eval = current_time;
+    a.evolution = evolution;
+    a.dl = dangular_momentum_dt;
+    a.acc = accelerations;
+    int rc = run_op(h->b, a);
+    if (rc != POSI_OK) return rc;
+    return refresh_mirror(h);
+}
+
+int posi_get_state(const posi_handle* h, int64_t* sys_i64, double* sys_f64, int64_t* body_i64, double* body_f64,
+                   double* roche) {
+    if (!h) return POSI_ERR_ARG;
+    return batch_get(h->b, sys_i64, sys_f64, body_i64, body_f64, roche);
+}
+
+int posi_set_state(posi_handle* h, const int64_t* sys_i64, const double* sys_f64, const int64_t* body_i64,
+                   const double* body_f64) {
+    if (!h) return POSI_ERR_ARG;
+    if (sys_i64 && sys_i64[POSI_SI_N] != h->si[POSI_SI_N]) return POSI_ERR_ARG;
+    int rc = batch_set(h->b, sys_i64, sys_f64, body_i64, body_f64);
+    if (rc != POSI_OK) return rc;
+    return refresh_mirror(h);
+}
+
+// ---- batched --------------------------------------------------------------
+
+posi_batch* posi_batch_create(int64_t n_systems, int64_t nmax, const int64_t* sys_i64, const double* sys_f64,
+                              const int64_t* body_i64, const double* body_f64, const double* tables,
+                              int64_t n_tables, const double* roche, int mode, int mapping, int* status) {
+    return create_batch(n_systems, nmax, sys_i64, sys_f64, body_i64, body_f64, tables, n_tables, roche, mode,
+                        mapping, status);
+}
+
+void posi_batch_destroy(posi_batch* b) { free_batch(b); }
+
+int posi_batch_size(const posi_batch* b, int64_t* n_systems, int64_t* nmax) {
+    if (!b) return POSI_ERR_ARG;
+    if (n_systems) *n_systems = b->n_sys;
+    if (nmax) *nmax = b->nmax;
+    return POSI_OK;
+}
+
+int posi_batch_initialize_physical_values(posi_batch* b) {
+    if (!b) return POSI_ERR_ARG;
+    LaunchArgs a{};
+    a.op = posi::OP_INIT;
+    int rc = run_op(b, a);
+    if (rc != POSI_OK) return rc;
+    return compute_roche(b);
+}
+
+int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch) {
+    if (!b || n_steps < 0) return POSI_ERR_ARG;
+    if (n_steps == 0) return POSI_OK;
+    if (steps_per_launch <= 0 || steps_per_launch > n_steps) steps_per_launch = n_steps;
+    const int64_t chunks = (n_steps + steps_per_launch - 1) / steps_per_launch;
+    if (!b->graph || b->graph_steps != n_steps || b->graph_spl != steps_per_launch) {
+        if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        LaunchArgs a{};
+        a.op = posi::OP_STEPS;
+        cudaError_t err = cudaSuccess;
+        for (int64_t c = 0; c < chunks && err == cudaSuccess; ++c) {
+            a.n_steps = std::min(steps_per_launch, n_steps - c * steps_per_launch);
+            for (const Bucket& bk : b->buckets) {
+                err = b->launch(bk, a);
+                if (err != cudaSuccess) break;
+            }
+        }
+        cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+        CK(err);
+        CK(e2);
+        err = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        CK(err);
+        b->graph_steps = n_steps;
+        b->graph_spl = steps_per_launch;
+    }
+    CK(cudaEventRecord(b->ev0, b->stream));
+    CK(cudaGraphLaunch(b->graph, b->stream));
+    CK(cudaEventRecord(b->ev1, b->stream));
+    CK(cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    b->last_ms = ms;
+    b->last_launches = chunks * (int64_t)b->buckets.size();
+    return POSI_OK;
+}
+
+int posi_batch_get_state(const posi_batch* b, int64_t* sys_i64, double* sys_f64, int64_t* body_i64, double* body_f64,
+                         double* roche) {
+    if (!b) return POSI_ERR_ARG;
+    return batch_get(b, sys_i64, sys_f64, body_i64, body_f64, roche);
+}
+
+int posi_batch_set_state(posi_batch* b, const int64_t* sys_i64, const double* sys_f64, const int64_t* body_i64,
+                         const double* body_f64) {
+    if (!b) return POSI_ERR_ARG;
+    return batch_set(b, sys_i64, sys_f64, body_i64, body_f64);
+}
+
+int posi_batch_mapping_for(const posi_batch* b, int64_t n) {
+    if (!b) return -1;
+    auto it = b->mapping_of_n.find(n);
+    return it == b->mapping_of_n.end() ? -1 : it->second;
+}
+
+int posi_batch_last_timing(const posi_batch* b, double* ms, int64_t* launches) {
+    if (!b) return POSI_ERR_ARG;
+    if (ms) *ms = b->last_ms;
+    if (launches) *launches = b->last_launches;
+    return POSI_OK;
+}
+
+}  // extern "C"

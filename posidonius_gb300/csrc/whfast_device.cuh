@@ -1,0 +1,1362 @@
+// whfast_device.cuh -- FP64 device code of the WHFast + tidal-effects step.
+//
+// Mapping: one group of G lanes (G = 4, 8, 16 or 32; G >= n) integrates one
+// independent system; lane j owns body j (reference particle order, the host
+// at any index).  Each lane keeps its body's whole state in registers for the
+// whole launch.  Cross-body work goes through a small per-group exchange area
+// in shared memory:
+//   - reductions over bodies (host back-reactions, midpoint convergence,
+//     democratic-heliocentric sums) are evaluated column-wise: every lane
+//     writes its body's contributions, then lane c folds column c over the
+//     bodies in index order -- the same order, hence the same rounding, as
+//     the reference's sequential loops, without G-fold redundancy;
+//   - the Jacobi recurrences are sequential by nature and run redundantly in
+//     every lane, each lane keeping its own body's result.
+//
+// This header is compiled twice: with POSI_EXACT=1 and -fmad=false the code
+// keeps the reference's operation order and reproduces the Rust FP64 results
+// bit for bit; with POSI_EXACT=0 and -fmad=true the compiler contracts
+// multiply-adds and a few divisions become multiplications by shared
+// reciprocals.  Position-only and parameter-only terms are evaluated once per
+// half kick in both modes (the reference recomputes the same values on every
+// midpoint iteration, so hoisting them does not change a bit).
+//
+// Reference: src/integrator/whfast.rs (step, midpoint, Kepler, transforms),
+// src/particles/universe.rs (gravity, heliocentric, additional effects),
+// src/effects/tides/{common,constant_time_lag}.rs,
+// src/effects/rotational_flattening/{common,oblate_spheroid}.rs,
+// src/effects/general_relativity.rs (Kidder 1995), src/effects/evolution.rs,
+// src/tools.rs:840-907, src/constants.rs.
+
+#pragma once
+#include <cstdint>
+
+#include "../../include/posidonius_gb300.h"
+
+#ifndef POSI_EXACT
+#error "POSI_EXACT must be defined (1: reference operation order, 0: fast)"
+#endif
+
+#if POSI_EXACT
+#define POSI_NS posi_exact
+#else
+#define POSI_NS posi_fast
+#endif
+
+namespace POSI_NS {
+
+// ---------------------------------------------------------------------------
+// src/constants.rs:20-61 -- the same literal expressions, folded at compile time
+// ---------------------------------------------------------------------------
+constexpr double kPI = 3.141592653589793;
+constexpr double kDAY = 24. * 3600.;
+constexpr double kM_SUN = 1.9818e30;
+constexpr double kG_SI = 6.67428e-11;
+constexpr double kAU = 1.49597870700e11;
+constexpr double kC = (2.99792458e8 / kAU) * kDAY;
+constexpr double kC2 = kC * kC;
+constexpr double kG = kG_SI / (kAU * kAU * kAU) * kM_SUN * (kDAY * kDAY);
+constexpr double kK2 = kG;
+constexpr double kMAX_DISTANCE_2 = 100. * 100.;
+constexpr double kDBL_EPSILON_2 = 2.2204460492503131e-16 * 2.2204460492503131e-16;
+constexpr double kMINUS_3K2 = -3.0 * kK2;
+constexpr double kFA = kG / kC2;
+constexpr double kTWO_PI = 2. * kPI;
+constexpr int kNMAX_QUART = 64;
+constexpr int kNMAX_NEWT = 32;
+constexpr int kMIDPOINT_MIN = 3;
+constexpr int kMIDPOINT_MAX = 10;
+constexpr int kBISECTION_GUARD = 4096;
+constexpr int kEVO_SHIFT = 10;
+
+// Division: exact IEEE quotient in EXACT mode; a product with a reciprocal
+// evaluated once elsewhere in FAST mode.
+__device__ __forceinline__ double qdiv(double a, double b, double inv_b) {
+#if POSI_EXACT
+    (void)inv_b;
+    return a / b;
+#else
+    (void)b;
+    return a * inv_b;
+#endif
+}
+
+// LLVM's expansion of llvm.powi with a constant exponent (square-and-multiply
+// from the low bit; the first factor is taken without multiplying by one).
+template <int N>
+__device__ __forceinline__ double powi(double x) {
+    double res = 0.;
+    bool have = false;
+    double cur = x;
+    unsigned v = (unsigned)N;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (v) {
+            if (v & 1u) {
+                if (have) res = res * cur; else { res = cur; have = true; }
+            }
+            v >>= 1;
+            if (v) cur = cur * cur;
+        }
+    }
+    return res;
+}
+
+// ---------------------------------------------------------------------------
+// Device view of an ensemble (field-major SoA).
+// ---------------------------------------------------------------------------
+struct Dev {
+    int64_t n_sys, nmax, stride;   // stride = n_sys * nmax
+    double* bf;                    // [POSI_BF_COUNT][stride]
+    int64_t* bi;                   // [POSI_BI_COUNT][stride]
+    double* sf;                    // [POSI_SF_COUNT][n_sys]
+    int64_t* si;                   // [POSI_SI_COUNT][n_sys]
+    const double* roche;           // [n_sys][nmax][nmax]
+    const double* tables;          // evolution tables
+    const int32_t* list;           // systems of this launch
+    int32_t n_list;
+    int32_t* step_flags;           // per system: bit0 recovery trigger, bit1 historic trigger
+};
+
+// Exchange area of one group (shared memory): XS slots of G doubles, a host
+// card, column results and a few integers.
+constexpr int kXS = 24;
+constexpr int kCARD = 32;
+constexpr int kSUMS = 32;
+template <int G>
+struct GroupSmem {
+    static constexpr int doubles = kXS * G + kCARD + kSUMS;
+    static constexpr int bytes = doubles * 8 + 32;  // + 8 ints
+};
+
+// host card slots
+enum { HC_PX = 0, HC_PY, HC_PZ, HC_VX, HC_VY, HC_VZ, HC_SX, HC_SY, HC_SZ, HC_NSV2, HC_M, HC_MG, HC_R,
+       HC_SIG, HC_K2, HC_K2F, HC_MOI, HC_AM, HC_APX, HC_APY, HC_APZ, HC_AVX, HC_AVY, HC_AVZ, HC_AAX, HC_AAY,
+       HC_AAZ, HC_COUNT };
+
+struct Body {
+    double m, mg, R, rg2, moi;
+    double r[3], v[3], a[3], L[3], S[3], nsv2;
+    double ev[3], eL[3];
+    double sig, k2, k2f;
+    double aa[3], dl[3];
+    double denergy, lag;
+    int tk, fk, gk, evo;
+    int64_t eoff, elen, eleft;
+    // alternative (Jacobi / democratic-heliocentric / WHDS) coordinates
+    double am, amg, ap[3], av[3], aacc[3];
+};
+
+// Per-planet constants of one half kick (positions and parameters are fixed
+// during the implicit-midpoint iterations).
+struct PC {
+    double x, y, z, d, inv_d;
+    // constant-time-lag tides
+    double o_s, o_p, osd, opd, cons, d8, term1, term2, inv_m;
+    // oblate flattening
+    double m_hk2f, hm_k2f, R5h, R5p, d5, n3d5, f15d7;
+    // Kidder GR
+    double A, B, C, D, E, t1, K2c, K3c, K4c, K5c, K6c, A05, P, Q, R3, mratio, mfM, mu, fm, fm2, nn[3];
+};
+
+template <int G>
+struct Sys {
+    // uniform per group
+    int s, n, host, coords, lane;
+    bool tides, flat, gr, evo, spin_on;
+    unsigned mask;
+    double dt, half_dt, t, time_limit, last_hist, hist_period, last_rec, rec_period;
+    int64_t iteration, n_hist, tw, status, fail_step, fail_pair, mid_iters;
+    double* xs;
+    double* card;
+    double* sums;
+    int* isc;
+    // own body
+    bool has, is_host;
+    Body b;
+    PC pc;
+
+    __device__ __forceinline__ void sync() const {
+        if (G > 1) __syncwarp(mask);
+    }
+    __device__ __forceinline__ double& X(int slot, int j) const { return xs[slot * G + j]; }
+    __device__ __forceinline__ bool fatal() const { return (status & POSI_SYS_FATAL_MASK) != 0; }
+    __device__ __forceinline__ bool planet() const { return has && !is_host; }
+
+    // ------------------------------------------------------------------
+    // load / store
+    // ------------------------------------------------------------------
+    __device__ void load(const Dev& D, int sys, int lane_, unsigned mask_, double* smem) {
+        s = sys;
+        lane = lane_;
+        mask = mask_;
+        xs = smem;
+        card = smem + kXS * G;
+        sums = card + kCARD;
+        isc = reinterpret_cast<int*>(sums + kSUMS);
+        const int64_t ns = D.n_sys;
+        n = (int)D.si[POSI_SI_N * ns + s];
+        host = (int)D.si[POSI_SI_HOST * ns + s];
+        coords = (int)D.si[POSI_SI_COORDS * ns + s];
+        tides = D.si[POSI_SI_TIDES * ns + s] != 0;
+        flat = D.si[POSI_SI_FLAT * ns + s] != 0;
+        gr = D.si[POSI_SI_GR * ns + s] != 0;
+        evo = D.si[POSI_SI_EVOLUTION * ns + s] != 0;
+        spin_on = tides || flat || evo || gr;
+        iteration = D.si[POSI_SI_ITERATION * ns + s];
+        n_hist = D.si[POSI_SI_N_HIST * ns + s];
+        tw = D.si[POSI_SI_TIMESTEP_WARNING * ns + s];
+        status = D.si[POSI_SI_STATUS * ns + s];
+        fail_step = D.si[POSI_SI_FAIL_STEP * ns + s];
+        fail_pair = D.si[POSI_SI_FAIL_PAIR * ns + s];
+        mid_iters = D.si[POSI_SI_LAST_MIDPOINT_ITERS * ns + s];
+        dt = D.sf[POSI_SF_DT * ns + s];
+        half_dt = D.sf[POSI_SF_HALF_DT * ns + s];
+        t = D.sf[POSI_SF_TIME * ns + s];
+        time_limit = D.sf[POSI_SF_TIME_LIMIT * ns + s];
+        last_hist = D.sf[POSI_SF_LAST_HIST * ns + s];
+        hist_period = D.sf[POSI_SF_HIST_PERIOD * ns + s];
+        last_rec = D.sf[POSI_SF_LAST_REC * ns + s];
+        rec_period = D.sf[POSI_SF_REC_PERIOD * ns + s];
+        has = lane < n;
+        is_host = lane == host;
+        if (lane < 8) isc[lane] = 0;
+        sync();
+        if (!has) return;
+        const int64_t st = D.stride;
+        const int64_t o = (int64_t)s * D.nmax + lane;
+        const double* F = D.bf + o;
+        b.m = F[POSI_BF_MASS * st];
+        b.mg = F[POSI_BF_MASS_G * st];
+        b.R = F[POSI_BF_RADIUS * st];
+        b.rg2 = F[POSI_BF_RG2 * st];
+        b.moi = F[POSI_BF_MOI * st];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            b.r[k] = F[(POSI_BF_PX + k) * st];
+            b.v[k] = F[(POSI_BF_VX + k) * st];
+            b.a[k] = F[(POSI_BF_AX + k) * st];
+            b.L[k] = F[(POSI_BF_LX + k) * st];
+            b.S[k] = F[(POSI_BF_SX + k) * st];
+            b.ev[k] = F[(POSI_BF_EVX + k) * st];
+            b.eL[k] = F[(POSI_BF_ELX + k) * st];
+            b.aa[k] = F[(POSI_BF_ADDAX + k) * st];
+            b.dl[k] = F[(POSI_BF_DLX + k) * st];
+            b.ap[k] = 0.; b.av[k] = 0.; b.aacc[k] = 0.;
+        }
+        b.nsv2 = F[POSI_BF_NSV2 * st];
+        b.sig = F[POSI_BF_SIGMA * st];
+        b.k2 = F[POSI_BF_K2 * st];
+        b.k2f = F[POSI_BF_K2F * st];
+        b.denergy = F[POSI_BF_DENERGY_DT * st];
+        b.lag = F[POSI_BF_LAG_ANGLE * st];
+        const int64_t* I = D.bi + o;
+        b.tk = (int)I[POSI_BI_TIDES_KIND * st];
+        b.fk = (int)I[POSI_BI_FLAT_KIND * st];
+        b.gk = (int)I[POSI_BI_GR_KIND * st];
+        b.evo = (int)I[POSI_BI_EVO_TYPE * st];
+        b.eoff = I[POSI_BI_EVO_OFFSET * st];
+        b.elen = I[POSI_BI_EVO_LEN * st];
+        b.eleft = I[POSI_BI_EVO_LEFT * st];
+        if (b.elen <= 0) b.evo = POSI_EVO_NON_EVOLVING;
+        b.am = 0.; b.amg = 0.;
+    }
+
+    __device__ void store(const Dev& D) const {
+        const int64_t ns = D.n_sys;
+        if (lane == 0) {
+            D.si[POSI_SI_ITERATION * ns + s] = iteration;
+            D.si[POSI_SI_N_HIST * ns + s] = n_hist;
+            D.si[POSI_SI_TIMESTEP_WARNING * ns + s] = tw;
+            D.si[POSI_SI_STATUS * ns + s] = status;
+            D.si[POSI_SI_FAIL_STEP * ns + s] = fail_step;
+            D.si[POSI_SI_FAIL_PAIR * ns + s] = fail_pair;
+            D.si[POSI_SI_LAST_MIDPOINT_ITERS * ns + s] = mid_iters;
+            D.sf[POSI_SF_TIME * ns + s] = t;
+            D.sf[POSI_SF_LAST_HIST * ns + s] = last_hist;
+            D.sf[POSI_SF_LAST_REC * ns + s] = last_rec;
+        }
+        if (!has) return;
+        const int64_t st = D.stride;
+        const int64_t o = (int64_t)s * D.nmax + lane;
+        double* F = D.bf + o;
+        F[POSI_BF_RADIUS * st] = b.R;
+        F[POSI_BF_RG2 * st] = b.rg2;
+        F[POSI_BF_MOI * st] = b.moi;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            F[(POSI_BF_PX + k) * st] = b.r[k];
+            F[(POSI_BF_VX + k) * st] = b.v[k];
+            F[(POSI_BF_AX + k) * st] = b.a[k];
+            F[(POSI_BF_LX + k) * st] = b.L[k];
+            F[(POSI_BF_SX + k) * st] = b.S[k];
+            F[(POSI_BF_EVX + k) * st] = b.ev[k];
+            F[(POSI_BF_ELX + k) * st] = b.eL[k];
+            F[(POSI_BF_ADDAX + k) * st] = b.aa[k];
+            F[(POSI_BF_DLX + k) * st] = b.dl[k];
+        }
+        F[POSI_BF_NSV2 * st] = b.nsv2;
+        F[POSI_BF_DENERGY_DT * st] = b.denergy;
+        F[POSI_BF_LAG_ANGLE * st] = b.lag;
+        D.bi[POSI_BI_EVO_LEFT * st + o] = b.eleft;
+    }
+
+    __device__ void set_fatal(int code, int i, int j) {
+        if (fatal()) return;
+        status = (status & ~(int64_t)POSI_SYS_FATAL_MASK) | code;
+        fail_step = iteration;
+        fail_pair = (int64_t)i * 1024 + j;
+    }
+
+    // Column fold: for c in [0, ncol) starting from init (0 if null),
+    // sums[c] = (((init + X(base+c, j0)) + X(base+c, j1)) + ...) over the
+    // bodies in index order, the host skipped (skip_host) or visited first
+    // (host_first).  Lane l evaluates columns l, l+G, ...
+    __device__ void colfold(int base, int ncol, const double* init, bool skip_host, bool host_first) {
+        sync();
+        for (int c = lane; c < ncol; c += G) {
+            double acc = init ? init[c] : 0.;
+            if (host_first) acc += X(base + c, host);
+            for (int j = 0; j < n; ++j) {
+                if ((skip_host || host_first) && j == host) continue;
+                acc += X(base + c, j);
+            }
+            sums[c] = acc;
+        }
+        sync();
+    }
+
+    // ------------------------------------------------------------------
+    // src/effects/evolution.rs:446-546 + src/tools.rs:840-907
+    // ------------------------------------------------------------------
+    __device__ double interp(const Dev& D, double target, int which) {
+        // Evolver::idx()
+        const int64_t i0 = b.eleft > kEVO_SHIFT ? b.eleft - kEVO_SHIFT : 0;
+        const double* x = D.tables + b.eoff + i0;
+        const double* y = D.tables + b.eoff + (int64_t)which * b.elen + i0;
+        const int64_t nd = b.elen - i0;
+        int64_t left, right, pos = -1;
+        for (int64_t k = 0; k < nd; ++k) {
+            if (x[k] > target) { pos = k; break; }
+        }
+        if (pos < 0) { left = nd - 1; right = nd - 1; }
+        else if (pos == 0) { left = 0; right = 0; }
+        else { left = pos - 1; right = pos; }
+        double ty;
+        if (left == right) {
+            ty = y[left];
+        } else {
+            const double xl = x[left];
+            const double pct = (target - xl) / (x[right] - xl);
+            ty = y[left] * (1. - pct) + y[right] * pct;
+        }
+        b.eleft += left;
+        return ty;
+    }
+
+    __device__ void evolve_non_spin(const Dev& D, double tt) {
+        if (b.evo == POSI_EVO_NON_EVOLVING) return;
+        const double nr = interp(D, tt, 1);
+        double ng = b.rg2;
+        if (b.evo == POSI_EVO_BARAFFE2015 || b.evo == POSI_EVO_LECONTE2011 || b.evo == POSI_EVO_LECONTE_CHABRIER2013)
+            ng = interp(D, tt, 2);
+        if (nr != b.R || ng != b.rg2) {
+            b.R = nr;
+            b.rg2 = ng;
+            b.moi = b.m * b.rg2 * powi<2>(b.R);
+        }
+        // The love-number update of the reference writes to a copy; only the
+        // table index moves.
+        if (b.tk != POSI_EFFECT_DISABLED && b.evo == POSI_EVO_LECONTE_CHABRIER2013) (void)interp(D, tt, 3);
+    }
+
+    // src/particles/universe.rs:305-316 with src/particles/common.rs:3-14
+    __device__ void spin_and_evolving(const Dev& D, double tt, bool evolution) {
+        if (has) {
+            if (evolution && evo) evolve_non_spin(D, tt);
+            if (b.moi == 0.) {
+                isc[1] = 1;
+            } else {
+                b.S[0] = b.L[0] / b.moi;
+                b.S[1] = b.L[1] / b.moi;
+                b.S[2] = b.L[2] / b.moi;
+                b.nsv2 = powi<2>(b.S[0]) + powi<2>(b.S[1]) + powi<2>(b.S[2]);
+            }
+            if (evolution && evo) b.lag = 0.;
+        }
+    }
+
+    __device__ void zero_inertia_check() {
+        sync();
+        if (isc[1]) set_fatal(POSI_SYS_ZERO_INERTIA, 0, 0);
+        sync();
+    }
+
+    // ------------------------------------------------------------------
+    // Per-planet constants of a half kick (after the spin/evolution update
+    // of its first midpoint iteration, so that evolved radii are used).
+    // ------------------------------------------------------------------
+    __device__ void planet_constants() {
+        const double hm = card[HC_M], hmg = card[HC_MG], hR = card[HC_R], hsig = card[HC_SIG];
+        const double hk2 = card[HC_K2], hk2f = card[HC_K2F];
+        PC& c = pc;
+        const double d = c.d;
+        c.inv_d = 1. / d;
+        c.inv_m = 1. / b.m;
+        if (tides && b.tk == POSI_EFFECT_ORBITING) {
+            // src/effects/tides/constant_time_lag.rs:229-264, :266-307
+            const double d7 = powi<7>(d);
+            c.o_s = 4.5 * powi<2>(b.m) * powi<10>(hR) * hsig / d7;
+            c.o_p = 4.5 * powi<2>(hm) * powi<10>(b.R) * b.sig / d7;
+            c.osd = c.o_s / d;
+            c.opd = c.o_p / d;
+            const double hm2 = hm * hm;
+            const double m2 = b.m * b.m;
+            c.cons = kMINUS_3K2 / powi<7>(d) * (m2 * powi<5>(hR) * hk2 + hm2 * powi<5>(b.R) * b.k2);
+            c.d8 = powi<8>(d);
+            c.term1 = m2 * powi<10>(hR) * hsig;
+            c.term2 = hm2 * powi<10>(b.R) * b.sig;
+        }
+        if (flat && b.fk == POSI_EFFECT_ORBITING) {
+            // src/effects/rotational_flattening/oblate_spheroid.rs:12-60
+            c.m_hk2f = b.m * hk2f;
+            c.hm_k2f = hm * b.k2f;
+            c.R5h = powi<5>(hR);
+            c.R5p = powi<5>(b.R);
+            c.d5 = powi<5>(d);
+            c.n3d5 = -3. / powi<5>(d);
+            c.f15d7 = 15. / powi<7>(d);
+        }
+        if (gr && b.gk == POSI_EFFECT_ORBITING) {
+            // src/effects/general_relativity.rs:98, :187-298, :300-456
+            const double f = hmg * b.mg / powi<2>(hmg + b.mg);
+            const double mgs = hmg + b.mg;
+            const double d2 = powi<2>(d);
+            const double mgd = mgs / d;
+            const double f2 = powi<2>(f);
+            c.A = -mgs / (d2 * kC2);
+            c.B = 1.0 + 3.0 * f;
+            c.C = 2.0 * (2.0 + f) * mgs / d;
+            c.D = 1.5 * f;
+            c.E = mgs / (d2 * kC2) * 2.0 * (2.0 - f);
+            c.t1 = (3.0 / 4.0) * (12.0 + 29.0 * f) * (powi<2>(mgs) / d2);
+            c.K2c = f * (3.0 - 4.0 * f);
+            c.K3c = (15.0 / 8.0) * f * (1.0 - 3.0 * f);
+            c.K4c = (3.0 / 2.0) * f * (3.0 - 4.0 * f);
+            c.K5c = 0.5 * f * (13.0 - 4.0 * f) * mgd;
+            c.K6c = (2.0 + 25.0 * f + 2.0 * f2) * mgd;
+            c.A05 = c.A * (-0.5);
+            c.P = f * (15.0 + 4.0 * f);
+            c.Q = (4.0 + 41.0 * f + 8.0 * f2) * mgd;
+            c.R3 = 3.0 * f * (3.0 + 2.0 * f);
+            c.mratio = b.m / hm;
+            const double M = hm + b.m;
+            const double mf = (hm - b.m) / M;
+            c.mfM = mf * M;
+            c.mu = (hm * b.m) / M;
+            c.fm = 2. + (3. / 2.) * b.m / hm;
+            c.fm2 = 2. + (3. / 2.) * hm / b.m;
+            c.nn[0] = c.x / d;
+            c.nn[1] = c.y / d;
+            c.nn[2] = c.z / d;
+        }
+    }
+
+    // ------------------------------------------------------------------
+    // One evaluation of src/particles/universe.rs:428-538 (after
+    // inertial_to_heliocentric :318-351), it = midpoint iteration.
+    // Contribution columns written per planet (host back-reactions):
+    //  0-2 tidal force, 3-5 -torque on host (tides), 6-8 flattening force,
+    //  9-11 -torque on host (flattening), 12-14 (m/M) a_1PN, 15-17 (m/M) a_2PN,
+    //  18-20 (m/M) a_SO, 21-23 host dL/dt (GR).
+    // ------------------------------------------------------------------
+    __device__ void additional_effects(const Dev& D, int it, bool evolution_now) {
+        // host inertial velocity and the spin it had before this evaluation
+        sync();
+        if (is_host) {
+            card[HC_VX] = b.v[0]; card[HC_VY] = b.v[1]; card[HC_VZ] = b.v[2];
+            card[HC_SX] = b.S[0]; card[HC_SY] = b.S[1]; card[HC_SZ] = b.S[2];
+        }
+        if (lane == 0) isc[1] = 0;
+        sync();
+        double hv[3] = {0., 0., 0.}, vr = 0., nv2 = 0., nv = 0., rs_s = 0., rs_p = 0.;
+        if (planet()) {
+            hv[0] = b.v[0] - card[HC_VX];
+            hv[1] = b.v[1] - card[HC_VY];
+            hv[2] = b.v[2] - card[HC_VZ];
+            vr = (pc.x * hv[0] + pc.y * hv[1] + pc.z * hv[2]) / pc.d;
+            // the host's previous heliocentric velocity is zero (universe.rs:335-338)
+            nv2 = powi<2>(hv[0] - 0.) + powi<2>(hv[1] - 0.) + powi<2>(hv[2] - 0.);
+            nv = sqrt(nv2);
+            // tides::initialize / rotational_flattening::initialize use the spin
+            // computed before this evaluation
+            rs_s = pc.x * card[HC_SX] + pc.y * card[HC_SY] + pc.z * card[HC_SZ];
+            rs_p = pc.x * b.S[0] + pc.y * b.S[1] + pc.z * b.S[2];
+        }
+        spin_and_evolving(D, t, evolution_now);
+        zero_inertia_check();
+        if (fatal()) return;
+        if (is_host) {
+            card[HC_SX] = b.S[0]; card[HC_SY] = b.S[1]; card[HC_SZ] = b.S[2];
+            card[HC_NSV2] = b.nsv2; card[HC_R] = b.R; card[HC_MOI] = b.moi;
+        }
+        sync();
+        if (it == 0 && planet()) planet_constants();
+        sync();
+
+        const double hS0 = card[HC_SX], hS1 = card[HC_SY], hS2 = card[HC_SZ];
+        const double hnsv2 = card[HC_NSV2];
+        double at[3] = {0., 0., 0.}, af[3] = {0., 0., 0.}, ag[3] = {0., 0., 0.};
+        double dt_[3] = {0., 0., 0.}, df[3] = {0., 0., 0.}, dg[3] = {0., 0., 0.};
+        // contribution columns go straight to the exchange area (zeros for
+        // effects a planet does not take part in)
+        const int ncol = gr ? 24 : (flat ? 12 : (tides ? 6 : 0));
+        if (planet()) {
+            for (int k = 0; k < ncol; ++k) X(k, lane) = 0.;
+        }
+        double* col = planet() ? &X(0, lane) : nullptr;
+        if (planet()) {
+            const PC& c = pc;
+            const double x = c.x, y = c.y, z = c.z, d = c.d;
+            if (tides && b.tk == POSI_EFFECT_ORBITING) {
+                // radial component (constant_time_lag.rs:266-307)
+                const double factor1 = -13.5 * vr / c.d8;
+                const double diss_pm = factor1 * c.term2;
+                const double radial = c.cons + (diss_pm + factor1 * c.term1);
+                // force (constant_time_lag.rs:309-332)
+                const double factor3 = radial + qdiv((c.o_s + c.o_p) * vr, d, c.inv_d);
+                double F[3];
+                F[0] = qdiv(factor3 * x, d, c.inv_d) + c.osd * (hS1 * z - hS2 * y - hv[0]) + c.opd * (b.S[1] * z - b.S[2] * y - hv[0]);
+                F[1] = qdiv(factor3 * y, d, c.inv_d) + c.osd * (hS2 * x - hS0 * z - hv[1]) + c.opd * (b.S[2] * x - b.S[0] * z - hv[1]);
+                F[2] = qdiv(factor3 * z, d, c.inv_d) + c.osd * (hS0 * y - hS1 * x - hv[2]) + c.opd * (b.S[0] * y - b.S[1] * x - hv[2]);
+                // tides/common.rs:312-370
+                at[0] = c.inv_m * F[0]; at[1] = c.inv_m * F[1]; at[2] = c.inv_m * F[2];
+                col[0 * G] = F[0]; col[1 * G] = F[1]; col[2 * G] = F[2];
+                // torques (constant_time_lag.rs:171-204), tides/common.rs:223-261
+                const double h0 = y * hv[2] - z * hv[1];
+                const double h1 = z * hv[0] - x * hv[2];
+                const double h2 = x * hv[1] - y * hv[0];
+                dt_[0] = -1.0 * (c.o_p * (d * b.S[0] - qdiv(rs_p * x, d, c.inv_d) - c.inv_d * h0));
+                dt_[1] = -1.0 * (c.o_p * (d * b.S[1] - qdiv(rs_p * y, d, c.inv_d) - c.inv_d * h1));
+                dt_[2] = -1.0 * (c.o_p * (d * b.S[2] - qdiv(rs_p * z, d, c.inv_d) - c.inv_d * h2));
+                col[3 * G] = -1.0 * (c.o_s * (d * hS0 - qdiv(rs_s * x, d, c.inv_d) - c.inv_d * h0));
+                col[4 * G] = -1.0 * (c.o_s * (d * hS1 - qdiv(rs_s * y, d, c.inv_d) - c.inv_d * h1));
+                col[5 * G] = -1.0 * (c.o_s * (d * hS2 - qdiv(rs_s * z, d, c.inv_d) - c.inv_d * h2));
+            }
+            if (flat && b.fk == POSI_EFFECT_ORBITING) {
+                // oblate_spheroid.rs:12-60
+                const double fs = c.m_hk2f * hnsv2 * c.R5h / 6.;
+                const double ofs = -6. * fs * rs_s / (hnsv2 * c.d5);
+                const double fp = c.hm_k2f * b.nsv2 * c.R5p / 6.;
+                const double ofp = -6. * fp * rs_p / (b.nsv2 * c.d5);
+                const double radial = c.n3d5 * (fp + fs) + c.f15d7 * (fs * rs_s * rs_s / hnsv2 + fp * rs_p * rs_p / b.nsv2);
+                // oblate_spheroid.rs:83-97, common.rs:203-237
+                double F[3];
+                F[0] = radial * x + ofp * b.S[0] + ofs * hS0;
+                F[1] = radial * y + ofp * b.S[1] + ofs * hS1;
+                F[2] = radial * z + ofp * b.S[2] + ofs * hS2;
+                af[0] = c.inv_m * F[0]; af[1] = c.inv_m * F[1]; af[2] = c.inv_m * F[2];
+                col[6 * G] = F[0]; col[7 * G] = F[1]; col[8 * G] = F[2];
+                // oblate_spheroid.rs:62-81, common.rs:165-201
+                df[0] = -1.0 * (ofp * (y * b.S[2] - z * b.S[1]));
+                df[1] = -1.0 * (ofp * (z * b.S[0] - x * b.S[2]));
+                df[2] = -1.0 * (ofp * (x * b.S[1] - y * b.S[0]));
+                col[9 * G] = -1.0 * (ofs * (y * hS2 - z * hS1));
+                col[10 * G] = -1.0 * (ofs * (z * hS0 - x * hS2));
+                col[11 * G] = -1.0 * (ofs * (x * hS1 - y * hS0));
+            }
+            if (gr && b.gk == POSI_EFFECT_ORBITING) {
+                const double vr2 = powi<2>(vr);
+                const double inv_nv = 1. / nv;
+                // first order (general_relativity.rs:187-239)
+                const double radial1 = c.A * (c.B * nv2 - c.C - c.D * vr2);
+                const double ortho1 = c.E * vr * nv;
+                double a1[3];
+                a1[0] = qdiv(radial1 * x, d, c.inv_d) + qdiv(ortho1 * hv[0], nv, inv_nv);
+                a1[1] = qdiv(radial1 * y, d, c.inv_d) + qdiv(ortho1 * hv[1], nv, inv_nv);
+                a1[2] = qdiv(radial1 * z, d, c.inv_d) + qdiv(ortho1 * hv[2], nv, inv_nv);
+                // second order (:241-298)
+                const double nv4 = powi<2>(nv2);
+                const double vr4 = powi<2>(vr2);
+                const double radial2 = c.A * (c.t1 + c.K2c * nv4 + c.K3c * vr4 - c.K4c * vr2 * nv2 - c.K5c * nv2 - c.K6c * vr2);
+                const double ortho2 = c.A05 * vr * (c.P * nv2 - c.Q - c.R3 * vr2);
+                double a2[3];
+                a2[0] = qdiv(radial2 * x, d, c.inv_d) + ortho2 * hv[0];
+                a2[1] = qdiv(radial2 * y, d, c.inv_d) + ortho2 * hv[1];
+                a2[2] = qdiv(radial2 * z, d, c.inv_d) + ortho2 * hv[2];
+                // spin-orbit (:300-456)
+                const double hmoi = card[HC_MOI], hm = card[HC_M];
+                const double sL0 = hmoi * hS0, sL1 = hmoi * hS1, sL2 = hmoi * hS2;
+                const double pL0 = b.moi * b.S[0], pL1 = b.moi * b.S[1], pL2 = b.moi * b.S[2];
+                const double* nn = c.nn;
+                const double msx = c.mfM * (pL0 / b.m - sL0 / hm);
+                const double msy = c.mfM * (pL1 / b.m - sL1 / hm);
+                const double msz = c.mfM * (pL2 / b.m - sL2 / hm);
+                const double e1x = 6. * nn[0] * ((nn[1] * hv[2] - nn[2] * hv[1]) * (2. * (sL0 + pL0) + msx));
+                const double e1y = 6. * nn[1] * ((nn[2] * hv[0] - nn[0] * hv[2]) * (2. * (sL1 + pL1) + msy));
+                const double e1z = 6. * nn[2] * ((nn[0] * hv[1] - nn[1] * hv[0]) * (2. * (sL2 + pL2) + msz));
+                const double e7x = 7. * (sL0 + pL0) + 3. * msx;
+                const double e7y = 7. * (sL1 + pL1) + 3. * msy;
+                const double e7z = 7. * (sL2 + pL2) + 3. * msz;
+                const double e2x = hv[1] * e7z - hv[2] * e7y;
+                const double e2y = hv[2] * e7x - hv[0] * e7z;
+                const double e2z = hv[0] * e7y - hv[1] * e7x;
+                const double e3sx = 3. * (sL0 + pL0) + msx;
+                const double e3sy = 3. * (sL1 + pL1) + msy;
+                const double e3sz = 3. * (sL2 + pL2) + msz;
+                const double e3x = 3. * vr * (nn[1] * e3sz - nn[2] * e3sy);
+                const double e3y = 3. * vr * (nn[2] * e3sx - nn[0] * e3sz);
+                const double e3z = 3. * vr * (nn[0] * e3sy - nn[1] * e3sx);
+                double a3[3];
+                a3[0] = kFA * (e1x - e2x + e3x);
+                a3[1] = kFA * (e1y - e2y + e3y);
+                a3[2] = kFA * (e1z - e2z + e3z);
+                ag[0] = a1[0] + a2[0] + a3[0];
+                ag[1] = a1[1] + a2[1] + a3[1];
+                ag[2] = a1[2] + a2[2] + a3[2];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    col[(12 + k) * G] = c.mratio * a1[k];
+                    col[(15 + k) * G] = c.mratio * a2[k];
+                    col[(18 + k) * G] = c.mratio * a3[k];
+                }
+                // Kidder 1995 eq. 2.4a / 2.4b
+                const double lo0 = c.mu * (y * hv[2] - z * hv[1]);
+                const double lo1 = c.mu * (z * hv[0] - x * hv[2]);
+                const double lo2 = c.mu * (x * hv[1] - y * hv[0]);
+                const double h1x = c.fm * (lo1 * sL2 - lo2 * sL1);
+                const double h1y = c.fm * (lo2 * sL0 - lo0 * sL2);
+                const double h1z = c.fm * (lo0 * sL1 - lo1 * sL0);
+                const double h2x = pL1 * sL2 - pL2 * sL1;
+                const double h2y = pL2 * sL0 - pL0 * sL2;
+                const double h2z = pL0 * sL1 - pL1 * sL0;
+                const double sp = nn[0] * pL0 + nn[1] * pL1 + nn[2] * pL2;
+                const double h3x = 3. * sp * (nn[1] * sL2 - nn[2] * sL1);
+                const double h3y = 3. * sp * (nn[2] * sL0 - nn[0] * sL2);
+                const double h3z = 3. * sp * (nn[0] * sL1 - nn[1] * sL0);
+                col[21 * G] = kFA * (h1x - h2x + h3x);
+                col[22 * G] = kFA * (h1y - h2y + h3y);
+                col[23 * G] = kFA * (h1z - h2z + h3z);
+                const double q1x = c.fm2 * (lo1 * pL2 - lo2 * pL1);
+                const double q1y = c.fm2 * (lo2 * pL0 - lo0 * pL2);
+                const double q1z = c.fm2 * (lo0 * pL1 - lo1 * pL0);
+                const double q2x = sL1 * pL2 - sL2 * pL1;
+                const double q2y = sL2 * pL0 - sL0 * pL2;
+                const double q2z = sL0 * pL1 - sL1 * pL0;
+                const double ss = nn[0] * sL0 + nn[1] * sL1 + nn[2] * sL2;
+                const double q3x = 3. * ss * (nn[1] * pL2 - nn[2] * pL1);
+                const double q3y = 3. * ss * (nn[2] * pL0 - nn[0] * pL2);
+                const double q3z = 3. * ss * (nn[0] * pL1 - nn[1] * pL0);
+                dg[0] = kFA * (q1x - q2x + q3x);
+                dg[1] = kFA * (q1y - q2y + q3y);
+                dg[2] = kFA * (q1z - q2z + q3z);
+            }
+        }
+        // host back-reactions: fold the contribution columns in body order
+        if (ncol > 0) colfold(0, ncol, nullptr, true, false);
+        if (is_host) {
+            const double factor2 = 1. / card[HC_M];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (tides) { at[k] = -1.0 * factor2 * sums[k]; dt_[k] = sums[3 + k]; }
+                if (flat) { af[k] = -1.0 * factor2 * sums[6 + k]; df[k] = sums[9 + k]; }
+                if (gr) {
+                    ag[k] = -1.0 * sums[12 + k] + -1.0 * sums[15 + k] + -1.0 * sums[18 + k];
+                    dg[k] = sums[21 + k];
+                }
+            }
+        }
+        sync();
+        if (has) {
+            // universe.rs:580-614 (disabled effects contribute their zero outputs)
+            if (spin_on && (tides || flat || gr)) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) b.dl[k] = dt_[k] + df[k] + dg[k] + 0.;
+            }
+            // universe.rs:540-567
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                double acc = 0.;
+                if (tides) acc += at[k];
+                if (flat) acc += af[k];
+                if (gr) acc += ag[k];
+                b.aa[k] = acc;
+            }
+        }
+    }
+
+    // ------------------------------------------------------------------
+    // src/integrator/whfast.rs:322-466 implicit midpoint with Kahan sums
+    // ------------------------------------------------------------------
+    __device__ void integrate_velocity_dependent_forces(const Dev& D, double hdt, bool evolution) {
+        // heliocentric positions are fixed during the iterations
+        sync();
+        if (is_host) { card[HC_PX] = b.r[0]; card[HC_PY] = b.r[1]; card[HC_PZ] = b.r[2];
+                       card[HC_M] = b.m; card[HC_MG] = b.mg; card[HC_R] = b.R; card[HC_SIG] = b.sig;
+                       card[HC_K2] = b.k2; card[HC_K2F] = b.k2f; }
+        sync();
+        if (planet()) {
+            pc.x = b.r[0] - card[HC_PX];
+            pc.y = b.r[1] - card[HC_PY];
+            pc.z = b.r[2] - card[HC_PZ];
+            pc.d = sqrt(powi<2>(pc.x) + powi<2>(pc.y) + powi<2>(pc.z));
+        }
+        double ov[3], oL[3], fv[3], fL[3], dvc[3] = {0., 0., 0.}, dLc[3] = {0., 0., 0.};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { ov[k] = b.v[k]; oL[k] = b.L[k]; fv[k] = ov[k]; fL[k] = oL[k]; }
+        bool converged = false;
+        int iters = 0;
+        for (int it = 0; it < kMIDPOINT_MAX; ++it) {
+            iters = it + 1;
+            double pv[3], pL[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { pv[k] = fv[k]; pL[k] = fL[k]; }
+            additional_effects(D, it, evolution && it == 0);
+            if (fatal()) return;
+            if (has) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    dvc[k] = hdt * b.aa[k] - b.ev[k];
+                    fv[k] = ov[k] + dvc[k];
+                    if (spin_on) {
+                        dLc[k] = hdt * b.dl[k] - b.eL[k];
+                        fL[k] = oL[k] + dLc[k];
+                    }
+                }
+            }
+            if (it >= kMIDPOINT_MIN - 1) {
+                // whfast.rs:424-451
+                sync();
+                if (has) {
+                    const double dvx = fv[0] - pv[0], dvy = fv[1] - pv[1], dvz = fv[2] - pv[2];
+                    X(0, lane) = powi<2>(dvx) + powi<2>(dvy) + powi<2>(dvz);
+                    X(1, lane) = powi<2>(fv[0]) + powi<2>(fv[1]) + powi<2>(fv[2]);
+                    const double dsx = fL[0] - pL[0], dsy = fL[1] - pL[1], dsz = fL[2] - pL[2];
+                    X(2, lane) = powi<2>(dsx) + powi<2>(dsy) + powi<2>(dsz);
+                    X(3, lane) = powi<2>(fL[0]) + powi<2>(fL[1]) + powi<2>(fL[2]);
+                }
+                colfold(0, spin_on ? 4 : 2, nullptr, false, false);
+                const double dv2 = sums[0], fv2 = sums[1];
+                bool conv;
+                if (spin_on) conv = dv2 / fv2 < kDBL_EPSILON_2 && sums[2] / sums[3] < kDBL_EPSILON_2;
+                else conv = dv2 / fv2 < kDBL_EPSILON_2;
+                if (conv) { converged = true; break; }
+            }
+            if (has) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    b.v[k] = 0.5 * (ov[k] + fv[k]);
+                    if (spin_on) b.L[k] = 0.5 * (oL[k] + fL[k]);
+                }
+            }
+        }
+        mid_iters = iters;
+        if (!converged) status |= POSI_SYS_WARN_NONCONVERGED;
+        if (has) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                b.v[k] = fv[k];
+                b.ev[k] = (b.v[k] - ov[k]) - dvc[k];
+                if (spin_on) {
+                    b.L[k] = fL[k];
+                    b.eL[k] = (b.L[k] - oL[k]) - dLc[k];
+                }
+            }
+        }
+    }
+
+    // ------------------------------------------------------------------
+    // Coordinate transforms (whfast.rs:881-1155)
+    // ------------------------------------------------------------------
+    // slots: 0 m, 1 mg, 2-4 r, 5-7 v (inertial)
+    __device__ void inertial_to_alternative() {
+        sync();
+        if (has) {
+            X(0, lane) = b.m; X(1, lane) = b.mg;
+            X(2, lane) = b.r[0]; X(3, lane) = b.r[1]; X(4, lane) = b.r[2];
+            X(5, lane) = b.v[0]; X(6, lane) = b.v[1]; X(7, lane) = b.v[2];
+        }
+        sync();
+        if (coords == POSI_JACOBI) {
+            // :889-933, sequential in every lane
+            const double m0 = X(0, host);
+            double eta = m0;
+            double s0 = eta * X(2, host), s1 = eta * X(3, host), s2 = eta * X(4, host);
+            double u0 = eta * X(5, host), u1 = eta * X(6, host), u2 = eta * X(7, host);
+            for (int j = 0; j < n; ++j) {
+                if (j == host) continue;
+                const double mj = X(0, j);
+                const double ei = 1. / eta;
+                eta += mj;
+                const double pme = eta * ei;
+                const double p0 = X(2, j) - s0 * ei, p1 = X(3, j) - s1 * ei, p2 = X(4, j) - s2 * ei;
+                const double w0 = X(5, j) - u0 * ei, w1 = X(6, j) - u1 * ei, w2 = X(7, j) - u2 * ei;
+                if (j == lane) {
+                    b.am = mj; b.amg = X(1, j);
+                    b.ap[0] = p0; b.ap[1] = p1; b.ap[2] = p2;
+                    b.av[0] = w0; b.av[1] = w1; b.av[2] = w2;
+                }
+                s0 = s0 * pme + mj * p0; s1 = s1 * pme + mj * p1; s2 = s2 * pme + mj * p2;
+                u0 = u0 * pme + mj * w0; u1 = u1 * pme + mj * w1; u2 = u2 * pme + mj * w2;
+            }
+            if (is_host) {
+                const double mtot_i = 1. / eta;
+                b.am = eta;
+                b.ap[0] = s0 * mtot_i; b.ap[1] = s1 * mtot_i; b.ap[2] = s2 * mtot_i;
+                b.av[0] = u0 * mtot_i; b.av[1] = u1 * mtot_i; b.av[2] = u2 * mtot_i;
+            }
+        } else {
+            // :973-1023 -- sums over host first, then the others in order
+            sync();
+            if (has) {
+                X(8, lane) = b.r[0] * b.m; X(9, lane) = b.r[1] * b.m; X(10, lane) = b.r[2] * b.m;
+                X(11, lane) = b.v[0] * b.m; X(12, lane) = b.v[1] * b.m; X(13, lane) = b.v[2] * b.m;
+                X(14, lane) = b.m; X(15, lane) = b.mg;
+            }
+            colfold(8, 8, nullptr, false, true);
+            const double mtot = sums[6];
+            const double st0 = sums[0] / mtot, st1 = sums[1] / mtot, st2 = sums[2] / mtot;
+            const double sv0 = sums[3] / mtot, sv1 = sums[4] / mtot, sv2 = sums[5] / mtot;
+            if (is_host) {
+                b.am = mtot; b.amg = sums[7];
+                b.ap[0] = st0; b.ap[1] = st1; b.ap[2] = st2;
+                b.av[0] = sv0; b.av[1] = sv1; b.av[2] = sv2;
+            } else if (has) {
+                const double hr0 = X(2, host), hr1 = X(3, host), hr2 = X(4, host);
+                b.ap[0] = b.r[0] - hr0; b.ap[1] = b.r[1] - hr1; b.ap[2] = b.r[2] - hr2;
+                b.av[0] = b.v[0] - sv0; b.av[1] = b.v[1] - sv1; b.av[2] = b.v[2] - sv2;
+                b.am = b.m; b.amg = b.mg;
+                if (coords == POSI_WHDS) {
+                    const double hm = X(0, host);
+                    const double factor = (hm + b.m) / hm;
+                    b.av[0] *= factor; b.av[1] *= factor; b.av[2] *= factor;
+                }
+            }
+        }
+        sync();
+    }
+
+    // slots: 0 m, 2-4 alt r, 5-7 alt v (host: barycentre)
+    __device__ void alternative_to_inertial() {
+        sync();
+        if (has) {
+            X(0, lane) = b.m;
+            X(2, lane) = b.ap[0]; X(3, lane) = b.ap[1]; X(4, lane) = b.ap[2];
+            X(5, lane) = b.av[0]; X(6, lane) = b.av[1]; X(7, lane) = b.av[2];
+        }
+        if (is_host) card[HC_AM] = b.am;
+        sync();
+        if (coords == POSI_JACOBI) {
+            // :1034-1080, reverse order, sequential in every lane
+            double eta = card[HC_AM];
+            double s0 = eta * X(2, host), s1 = eta * X(3, host), s2 = eta * X(4, host);
+            double u0 = eta * X(5, host), u1 = eta * X(6, host), u2 = eta * X(7, host);
+            for (int j = n - 1; j >= 0; --j) {
+                if (j == host) continue;
+                const double mj = X(0, j);
+                const double ei = 1. / eta;
+                s0 = (s0 - mj * X(2, j)) * ei; s1 = (s1 - mj * X(3, j)) * ei; s2 = (s2 - mj * X(4, j)) * ei;
+                u0 = (u0 - mj * X(5, j)) * ei; u1 = (u1 - mj * X(6, j)) * ei; u2 = (u2 - mj * X(7, j)) * ei;
+                if (j == lane) {
+                    b.r[0] = X(2, j) + s0; b.r[1] = X(3, j) + s1; b.r[2] = X(4, j) + s2;
+                    b.v[0] = X(5, j) + u0; b.v[1] = X(6, j) + u1; b.v[2] = X(7, j) + u2;
+                }
+                eta -= mj;
+                s0 *= eta; s1 *= eta; s2 *= eta;
+                u0 *= eta; u1 *= eta; u2 *= eta;
+            }
+            if (is_host) {
+                const double mtot_i = 1. / eta;
+                b.r[0] = s0 * mtot_i; b.r[1] = s1 * mtot_i; b.r[2] = s2 * mtot_i;
+                b.v[0] = u0 * mtot_i; b.v[1] = u1 * mtot_i; b.v[2] = u2 * mtot_i;
+            }
+        } else {
+            // :1090-1155
+            const double mtot = card[HC_AM];
+            const double hm = X(0, host);
+            const bool whds = coords == POSI_WHDS;
+            sync();
+            if (planet()) {
+                X(8, lane) = -(b.ap[0] * b.m / mtot);
+                X(9, lane) = -(b.ap[1] * b.m / mtot);
+                X(10, lane) = -(b.ap[2] * b.m / mtot);
+                const double factor = whds ? b.m / (hm + b.m) : b.m / hm;
+                X(11, lane) = -(b.av[0] * factor);
+                X(12, lane) = -(b.av[1] * factor);
+                X(13, lane) = -(b.av[2] * factor);
+            }
+            double init[6];
+            init[0] = X(2, host); init[1] = X(3, host); init[2] = X(4, host);
+            init[3] = X(5, host); init[4] = X(6, host); init[5] = X(7, host);
+            colfold(8, 6, init, true, false);
+            const double sp0 = sums[0], sp1 = sums[1], sp2 = sums[2];
+            if (is_host) {
+                b.r[0] = sp0; b.r[1] = sp1; b.r[2] = sp2;
+                b.v[0] = sums[3]; b.v[1] = sums[4]; b.v[2] = sums[5];
+            } else if (has) {
+                b.r[0] = b.ap[0] + sp0; b.r[1] = b.ap[1] + sp1; b.r[2] = b.ap[2] + sp2;
+                if (whds) {
+                    const double factor = (hm + b.m) / hm;
+                    b.v[0] = b.av[0] / factor + init[3];
+                    b.v[1] = b.av[1] / factor + init[4];
+                    b.v[2] = b.av[2] / factor + init[5];
+                } else {
+                    b.v[0] = b.av[0] + init[3];
+                    b.v[1] = b.av[1] + init[4];
+                    b.v[2] = b.av[2] + init[5];
+                }
+            }
+        }
+        sync();
+    }
+
+    // :495-556
+    __device__ void jump_step(double hdt) {
+        if (coords == POSI_JACOBI) return;
+        sync();
+        if (is_host) card[HC_M] = b.m;
+        const bool whds = coords == POSI_WHDS;
+        sync();
+        const double m0 = card[HC_M];
+        if (planet()) {
+            if (whds) {
+                const double factor = m0 + b.m;
+                X(8, lane) = b.m * b.av[0] / factor; X(9, lane) = b.m * b.av[1] / factor; X(10, lane) = b.m * b.av[2] / factor;
+            } else {
+                X(8, lane) = b.m * b.av[0]; X(9, lane) = b.m * b.av[1]; X(10, lane) = b.m * b.av[2];
+            }
+        }
+        colfold(8, 3, nullptr, true, false);
+        if (planet()) {
+            if (whds) {
+                const double factor = m0 + b.m;
+                b.ap[0] += hdt * (sums[0] - (b.m * b.av[0] / factor));
+                b.ap[1] += hdt * (sums[1] - (b.m * b.av[1] / factor));
+                b.ap[2] += hdt * (sums[2] - (b.m * b.av[2] / factor));
+            } else {
+                b.ap[0] += hdt * sums[0] / m0;
+                b.ap[1] += hdt * sums[1] / m0;
+                b.ap[2] += hdt * sums[2] / m0;
+            }
+        }
+        sync();
+    }
+
+    // :558-625 (Jacobi also :935-963 inertial_to_jacobi_acc)
+    __device__ void interaction_step(double fdt) {
+        if (coords == POSI_JACOBI) {
+            sync();
+            if (has) {
+                X(0, lane) = b.m;
+                X(2, lane) = b.a[0]; X(3, lane) = b.a[1]; X(4, lane) = b.a[2];
+            }
+            sync();
+            double eta = X(0, host);
+            double s0 = eta * X(2, host), s1 = eta * X(3, host), s2 = eta * X(4, host);
+            const double m0 = eta;
+            double eta_own = 0.;
+            int k_own = -1, k = 0;
+            for (int j = 0; j < n; ++j) {
+                if (j == host) continue;
+                const double mj = X(0, j);
+                const double ei = 1. / eta;
+                eta += mj;
+                const double pme = eta * ei;
+                const double a0 = X(2, j) - s0 * ei, a1 = X(3, j) - s1 * ei, a2 = X(4, j) - s2 * ei;
+                if (j == lane) { b.aacc[0] = a0; b.aacc[1] = a1; b.aacc[2] = a2; eta_own = eta; k_own = k; }
+                s0 = s0 * pme + mj * a0; s1 = s1 * pme + mj * a1; s2 = s2 * pme + mj * a2;
+                ++k;
+            }
+            (void)m0;
+            if (is_host) {
+                const double mtot_i = 1. / eta;
+                b.aacc[0] = s0 * mtot_i; b.aacc[1] = s1 * mtot_i; b.aacc[2] = s2 * mtot_i;
+            }
+            if (planet()) {
+                const double softening = 1e-12;
+                b.av[0] += fdt * b.aacc[0];
+                b.av[1] += fdt * b.aacc[1];
+                b.av[2] += fdt * b.aacc[2];
+                if (k_own > 0) {
+                    const double rj2i = 1. / (powi<2>(b.ap[0]) + powi<2>(b.ap[1]) + powi<2>(b.ap[2]) + softening);
+                    const double rji = sqrt(rj2i);
+                    const double rj3im = rji * rj2i * kG * eta_own;
+                    const double prefac = fdt * rj3im;
+                    b.av[0] += prefac * b.ap[0];
+                    b.av[1] += prefac * b.ap[1];
+                    b.av[2] += prefac * b.ap[2];
+                }
+            }
+            sync();
+        } else if (coords == POSI_DEMOCRATIC_HELIOCENTRIC) {
+            if (planet()) {
+                b.av[0] += fdt * b.a[0]; b.av[1] += fdt * b.a[1]; b.av[2] += fdt * b.a[2];
+            }
+        } else {
+            sync();
+            if (is_host) card[HC_M] = b.m;
+            sync();
+            const double m0 = card[HC_M];
+            if (planet()) {
+                const double factor = m0 + b.m;
+                b.av[0] += fdt * factor * b.a[0] / m0;
+                b.av[1] += fdt * factor * b.a[1] / m0;
+                b.av[2] += fdt * factor * b.a[2] / m0;
+            }
+            sync();
+        }
+    }
+
+    // :835-876
+    __device__ static void stiefel_gs3(double beta, double x, double gs[4]) {
+        const double x2 = powi<2>(x);
+        double z = beta * x2;
+        int nq = 0;
+        while (fabs(z) > 0.1) { z = z / 4.; nq += 1; }
+        // 1/k!, k = 0..13
+        const double if0 = 1., if1 = 1., if2 = 1. / 2., if3 = 1. / 6., if4 = 1. / 24., if5 = 1. / 120.,
+                     if6 = 1. / 720., if7 = 1. / 5040., if8 = 1. / 40320., if9 = 1. / 362880.,
+                     if10 = 1. / 3628800., if11 = 1. / 39916800., if12 = 1. / 479001600., if13 = 1. / 6227020800.;
+        double c_odd = if13, c_even = if12;
+        c_odd = if11 - z * c_odd; c_even = if10 - z * c_even;
+        c_odd = if9 - z * c_odd; c_even = if8 - z * c_even;
+        c_odd = if7 - z * c_odd; c_even = if6 - z * c_even;
+        c_odd = if5 - z * c_odd; c_even = if4 - z * c_even;
+        c_odd = if3 - z * c_odd; c_even = if2 - z * c_even;
+        double cs3 = c_odd, cs2 = c_even;
+        double cs1 = if1 - z * c_odd, cs0 = if0 - z * c_even;
+        while (nq > 0) {
+            cs3 = (cs2 + cs0 * cs3) * 0.25;
+            cs2 = cs1 * cs1 * 0.5;
+            cs1 = cs0 * cs1;
+            cs0 = 2. * cs0 * cs0 - 1.;
+            nq -= 1;
+        }
+        gs[0] = cs0;
+        gs[1] = cs1 * x;
+        gs[2] = cs2 * x2;
+        gs[3] = cs3 * (x2 * x);
+    }
+
+    // :676-833
+    __device__ void kepler_individual_step(double mass_g, double kdt) {
+        const double p0 = b.ap[0], p1 = b.ap[1], p2 = b.ap[2];
+        const double w0 = b.av[0], w1 = b.av[1], w2 = b.av[2];
+        const double r0 = sqrt(powi<2>(p0) + powi<2>(p1) + powi<2>(p2));
+        const double r0i = 1. / r0;
+        const double v2 = powi<2>(w0) + powi<2>(w1) + powi<2>(w2);
+        const double beta = 2. * mass_g * r0i - v2;
+        const double eta0 = p0 * w0 + p1 * w1 + p2 * w2;
+        const double zeta0 = mass_g - beta * r0;
+        double x, gs[4];
+        double invperiod = 0., x_per_period = 0.;
+        bool xpp_nan;
+        if (beta > 0.) {
+            const double sqrt_beta = sqrt(beta);
+            invperiod = sqrt_beta * beta / (kTWO_PI * mass_g);
+            x_per_period = kTWO_PI / sqrt_beta;
+            xpp_nan = isnan(x_per_period);
+            if (fabs(kdt) * invperiod > 1. && tw == 0) {
+                status |= POSI_SYS_WARN_TIMESTEP;
+                isc[2] = 1;
+            }
+            const double dtr0i = kdt * r0i;
+            x = dtr0i * (1. - dtr0i * eta0 * 0.5 * r0i);
+        } else {
+            x = 0.;
+            xpp_nan = true;
+        }
+        int converged = 0;
+        double old_x = x;
+        stiefel_gs3(beta, x, gs);
+        double e = eta0 * gs[1] + zeta0 * gs[2];
+        double ri = 1. / (r0 + e);
+        x = ri * (x * e - eta0 * gs[2] - zeta0 * gs[3] + kdt);
+        if (!xpp_nan && fabs(x - old_x) > 0.01 * x_per_period) {
+            x = beta * kdt / mass_g;
+            double prev_x[kNMAX_QUART + 1];
+            for (int k = 0; k <= kNMAX_QUART; ++k) prev_x[k] = 0.;
+            bool done = false;
+            for (int n_lag = 1; n_lag < kNMAX_QUART && !done; ++n_lag) {
+                stiefel_gs3(beta, x, gs);
+                const double f = r0 * x + eta0 * gs[2] + zeta0 * gs[3] - kdt;
+                const double fp = r0 + eta0 * gs[1] + zeta0 * gs[2];
+                const double fpp = eta0 * gs[0] + zeta0 * gs[1];
+                const double denom = fp + sqrt(fabs(16. * fp * fp - 20. * f * fpp));
+                x = (x * denom - 5. * f) / denom;
+                for (int k = 1; k < n_lag; ++k) {
+                    if (x == prev_x[k]) { converged = 1; done = true; break; }
+                }
+                if (!done) prev_x[n_lag] = x;
+            }
+            e = eta0 * gs[1] + zeta0 * gs[2];
+            ri = 1. / (r0 + e);
+        } else {
+            double old_x2;
+            for (int k = 1; k < kNMAX_NEWT; ++k) {
+                old_x2 = old_x;
+                old_x = x;
+                stiefel_gs3(beta, x, gs);
+                e = eta0 * gs[1] + zeta0 * gs[2];
+                ri = 1. / (r0 + e);
+                x = ri * (x * e - eta0 * gs[2] - zeta0 * gs[3] + kdt);
+                if (x == old_x || x == old_x2) { converged = 1; break; }
+            }
+        }
+        if (converged == 0) {
+            double x_min, x_max;
+            if (beta > 0.) {
+                x_min = x_per_period * floor(kdt * invperiod);
+                x_max = x_min + x_per_period;
+            } else {
+                const double h2 = r0 * r0 * v2 - eta0 * eta0;
+                const double q = h2 / mass_g / (1. + sqrt(1. - h2 * beta / (mass_g * mass_g)));
+                const double vq = sqrt(h2) / q;
+                x_min = 1. / (vq + r0 / kdt);
+                x_max = kdt / q;
+            }
+            x = (x_max + x_min) / 2.;
+            for (int guard = 0;; ++guard) {
+                stiefel_gs3(beta, x, gs);
+                const double sres = r0 * x + eta0 * gs[2] + zeta0 * gs[3] - kdt;
+                if (sres >= 0.) x_max = x; else x_min = x;
+                x = (x_max + x_min) / 2.;
+                if (fabs(x_max - x_min) / x_max <= 1e-15) break;
+                if (guard >= kBISECTION_GUARD) { isc[3] = 1; break; }
+            }
+            e = eta0 * gs[1] + zeta0 * gs[2];
+            ri = 1. / (r0 + e);
+        }
+        if (isnan(ri)) { ri = 0.; gs[1] = 0.; gs[2] = 0.; gs[3] = 0.; }
+        const double f = -mass_g * gs[2] * r0i;
+        const double g = kdt - mass_g * gs[3];
+        const double fd = -mass_g * gs[1] * r0i * ri;
+        const double gd = -mass_g * gs[2] * ri;
+        b.ap[0] += f * p0 + g * w0;
+        b.ap[1] += f * p1 + g * w1;
+        b.ap[2] += f * p2 + g * w2;
+        b.av[0] += fd * p0 + gd * w0;
+        b.av[1] += fd * p1 + gd * w1;
+        b.av[2] += fd * p2 + gd * w2;
+    }
+
+    // :628-672
+    __device__ void kepler_steps(double kdt) {
+        sync();
+        if (has) X(1, lane) = b.amg;
+        if (is_host) card[HC_MG] = b.mg;
+        if (lane == 0) { isc[2] = 0; isc[3] = 0; }
+        sync();
+        if (planet()) {
+            double gm;
+            if (coords == POSI_JACOBI) {
+                gm = card[HC_MG];
+                for (int j = 0; j < n; ++j) {
+                    if (j == host) continue;
+                    gm += X(1, j);
+                    if (j == lane) break;
+                }
+            } else if (coords == POSI_DEMOCRATIC_HELIOCENTRIC) {
+                gm = card[HC_MG];
+            } else {
+                gm = card[HC_MG] + b.amg;
+            }
+            kepler_individual_step(gm, kdt);
+        }
+        if (is_host) {
+            b.ap[0] += kdt * b.av[0];
+            b.ap[1] += kdt * b.av[1];
+            b.ap[2] += kdt * b.av[2];
+        }
+        sync();
+        if (isc[2]) tw += 1;
+        if (isc[3]) set_fatal(POSI_SYS_BISECTION_LIMIT, 0, 0);
+        sync();
+    }
+
+    // src/particles/universe.rs:198-303
+    __device__ void gravity(const Dev& D, int ignore_terms) {
+        sync();
+        if (has) {
+            X(0, lane) = b.m;
+            X(2, lane) = b.r[0]; X(3, lane) = b.r[1]; X(4, lane) = b.r[2];
+            X(5, lane) = b.R;
+        }
+        if (lane == 0) isc[0] = 0x7fffffff;
+        sync();
+        int code = 0, ev_pair = 0x7fffffff;
+        if (has) {
+            const int i = lane, mm = host;
+            const double* ro = D.roche + (int64_t)s * D.nmax * D.nmax + (int64_t)i * D.nmax;
+            double acc0 = 0., acc1 = 0., acc2 = 0.;
+            for (int j = 0; j < n; ++j) {
+                if (i == j) continue;
+                const double dx = b.r[0] - X(2, j);
+                const double dy = b.r[1] - X(3, j);
+                const double dz = b.r[2] - X(4, j);
+                const double distance_2 = dx * dx + dy * dy + dz * dz;
+                if (i < j && code == 0) {
+                    if (distance_2 <= powi<2>(ro[j])) { code = POSI_SYS_ROCHE; ev_pair = i * 1024 + j; }
+                    else if (distance_2 <= powi<2>(b.R + X(5, j))) { code = POSI_SYS_COLLISION; ev_pair = i * 1024 + j; }
+                    else if (kMAX_DISTANCE_2 > 0. && i == mm && distance_2 > kMAX_DISTANCE_2) { code = POSI_SYS_EJECTED; ev_pair = i * 1024 + j; }
+                }
+                if (ignore_terms == 1 &&
+                    ((i == mm && mm == 0 && j == 1) || (i == mm && mm > 0 && j == 0) ||
+                     (j == mm && mm == 0 && i == 1) || (j == mm && mm > 0 && i == 0)))
+                    continue;
+                if (ignore_terms == 2 && (i == mm || j == mm)) continue;
+                const double distance = sqrt(distance_2);
+                const double prefact = -kG / (distance * distance * distance) * X(0, j);
+                acc0 += prefact * dx;
+                acc1 += prefact * dy;
+                acc2 += prefact * dz;
+            }
+            b.a[0] = acc0; b.a[1] = acc1; b.a[2] = acc2;
+            if (code) atomicMin(&isc[0], ev_pair);
+        }
+        sync();
+        const int first = isc[0];
+        if (first != 0x7fffffff) {
+            // the reference panics at the first offending pair in (i, j) order
+            if (has && lane == first / 1024) isc[4] = code;
+            sync();
+            set_fatal(isc[4], first / 1024, first % 1024);
+        }
+        sync();
+    }
+
+    // ------------------------------------------------------------------
+    // src/integrator/whfast.rs:235-305 one step; returns false once the
+    // system is frozen (completed or fatal)
+    // ------------------------------------------------------------------
+    __device__ bool iterate(const Dev& D) {
+        const bool first = last_hist < 0.;
+        const bool hist_trig = last_hist + hist_period <= t;
+        const bool rec_trig = last_rec + rec_period <= t;
+        if (first || hist_trig) {
+            spin_and_evolving(D, t, true);
+            zero_inertia_check();
+            if (fatal()) return false;
+            if (!first) last_hist += hist_period; else last_hist = 0.;
+            n_hist += 1;
+        }
+        const int ignore = coords == POSI_JACOBI ? 1 : 2;
+        integrate_velocity_dependent_forces(D, half_dt, true);
+        if (fatal()) return false;
+        inertial_to_alternative();
+        kepler_steps(half_dt);
+        jump_step(half_dt);
+        alternative_to_inertial();
+        if (fatal()) return false;
+        gravity(D, ignore);
+        if (fatal()) return false;
+        interaction_step(dt);
+        jump_step(half_dt);
+        kepler_steps(half_dt);
+        alternative_to_inertial();
+        if (fatal()) return false;
+        integrate_velocity_dependent_forces(D, half_dt, false);
+        if (fatal()) return false;
+        t += dt;
+        iteration += 1;
+        if (lane == 0 && D.step_flags) D.step_flags[s] = (rec_trig || first ? 1 : 0) | ((first || hist_trig) ? 2 : 0);
+        if (t + dt > time_limit) {
+            status = (status & ~(int64_t)POSI_SYS_FATAL_MASK) | POSI_SYS_COMPLETED;
+            return false;
+        }
+        return true;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+template <int G>
+__device__ __forceinline__ bool group_setup(const Dev& D, int& sys, int& lane, unsigned& mask, double*& smem) {
+    extern __shared__ double shm[];
+    const int tid = threadIdx.x;
+    const int gib = tid / G;
+    lane = tid % G;
+    const int gid = blockIdx.x * (blockDim.x / G) + gib;
+    const int in_warp = (tid % 32) / G;
+    mask = (G >= 32) ? 0xffffffffu : (((1u << G) - 1u) << (in_warp * G));
+    smem = shm + (size_t)gib * (GroupSmem<G>::bytes / 8);
+    if (gid >= D.n_list) return false;
+    sys = D.list[gid];
+    return true;
+}
+
+// Advance each listed system by up to n_steps steps (the plain path launches
+// it with one system and n_steps = 1; the batched path with many systems and
+// many steps per launch).
+template <int G>
+__global__ void __launch_bounds__(128) whfast_steps_kernel(Dev D, int64_t n_steps) {
+    int sys, lane;
+    unsigned mask;
+    double* smem;
+    if (!group_setup<G>(D, sys, lane, mask, smem)) return;
+    Sys<G> S;
+    S.load(D, sys, lane, mask, smem);
+    if (!S.fatal()) {
+        for (int64_t k = 0; k < n_steps; ++k) {
+            if (!S.iterate(D)) break;
+        }
+    }
+    S.store(D);
+}
+
+// src/integrator/whfast.rs:226-233 (the Roche radii are computed on the host)
+template <int G>
+__global__ void __launch_bounds__(128) init_physical_kernel(Dev D) {
+    int sys, lane;
+    unsigned mask;
+    double* smem;
+    if (!group_setup<G>(D, sys, lane, mask, smem)) return;
+    Sys<G> S;
+    S.load(D, sys, lane, mask, smem);
+    S.spin_and_evolving(D, S.t, true);
+    S.zero_inertia_check();
+    S.store(D);
+}
+
+// src/particles/universe.rs:198-303
+template <int G>
+__global__ void __launch_bounds__(128) gravity_kernel(Dev D, int ignore_terms) {
+    int sys, lane;
+    unsigned mask;
+    double* smem;
+    if (!group_setup<G>(D, sys, lane, mask, smem)) return;
+    Sys<G> S;
+    S.load(D, sys, lane, mask, smem);
+    S.gravity(D, ignore_terms);
+    S.store(D);
+}
+
+// src/particles/universe.rs:318-351 + :428-538 (one evaluation)
+template <int G>
+__global__ void __launch_bounds__(128) additional_effects_kernel(Dev D, double t_eval, int evolution, int dl, int acc) {
+    int sys, lane;
+    unsigned mask;
+    double* smem;
+    if (!group_setup<G>(D, sys, lane, mask, smem)) return;
+    Sys<G> S;
+    S.load(D, sys, lane, mask, smem);
+    (void)acc;
+    S.spin_on = dl != 0;
+    S.t = t_eval;
+    S.sync();
+    if (S.is_host) { S.card[HC_PX] = S.b.r[0]; S.card[HC_PY] = S.b.r[1]; S.card[HC_PZ] = S.b.r[2];
+                     S.card[HC_M] = S.b.m; S.card[HC_MG] = S.b.mg; S.card[HC_R] = S.b.R; S.card[HC_SIG] = S.b.sig;
+                     S.card[HC_K2] = S.b.k2; S.card[HC_K2F] = S.b.k2f; }
+    S.sync();
+    if (S.planet()) {
+        S.pc.x = S.b.r[0] - S.card[HC_PX];
+        S.pc.y = S.b.r[1] - S.card[HC_PY];
+        S.pc.z = S.b.r[2] - S.card[HC_PZ];
+        S.pc.d = sqrt(powi<2>(S.pc.x) + powi<2>(S.pc.y) + powi<2>(S.pc.z));
+    }
+    S.additional_effects(D, 0, evolution != 0);
+    S.store(D);
+}
+
+}  // namespace POSI_NS

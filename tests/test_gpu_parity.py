@@ -1,0 +1,148 @@
+"""GPU parity: the CUDA path against the oracle and the reference goldens.
+
+EXACT mode (reference operation order, no FMA) must agree bit for bit with
+the oracle, which itself reproduces the reference's golden files exactly.
+FAST mode (FMA contraction, shared reciprocals) must stay within 1e-12
+relative per step of the oracle's trajectory; after the 199 steps of a golden
+case the tolerance written here is 1e-10 relative.
+"""
+import gzip
+
+import numpy as np
+import pytest
+
+import oracle
+import posidonius_gb300 as pg
+from oracle.case_json import load_case, stack
+from posidonius_gb300 import ensemble as E, layout as L
+
+from golden_cases import case_dict, case_path, expected, max_abs_error, names
+from parity import bitwise_diffs, max_rel_error
+
+pytestmark = pytest.mark.gpu
+
+FAST_TOL_199 = 1e-10
+FAST_TOL_STEP = 1e-12
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from posidonius_gb300 import build
+    build.build()
+
+
+def _json(tmp_path, name):
+    p = tmp_path / (name + ".json")
+    with gzip.open(case_path(name)) as f:
+        p.write_bytes(f.read())
+    return p
+
+
+@pytest.mark.parametrize("name", names())
+def test_plain_path_exact_matches_golden_and_oracle(tmp_path, name):
+    w = pg.restore_snapshot(_json(tmp_path, name), mode=pg.EXACT)
+    steps = w.run()
+    assert steps == 199
+    st = w.get_state()
+    assert max_abs_error(st["body_f64"], expected(name)) == 0.0
+    ref, _, _ = oracle.run(load_case(case_dict(name)), max_steps=10**6, init_physical=True)
+    assert bitwise_diffs(st, ref) == []
+
+
+@pytest.mark.parametrize("name", ["test_integrator-whfast_jacobi", "test_integrator-whfast_democraticheliocentric",
+                                  "test_integrator-whfast_whds", "test_evolution-brown_dwarf_non_evolving"])
+def test_plain_path_fast_within_tolerance(tmp_path, name):
+    w = pg.restore_snapshot(_json(tmp_path, name), mode=pg.FAST)
+    w.run()
+    st = w.get_state()
+    assert max_abs_error(st["body_f64"], expected(name)) <= 1e-12
+    ref, _, _ = oracle.run(load_case(case_dict(name)), max_steps=10**6, init_physical=True)
+    assert max_rel_error(st, ref) <= FAST_TOL_199
+
+
+def test_fast_one_step_relative_error():
+    ens = E.workload_ensemble8(64, seed=11)
+    b = pg.Batch(ens, mode=pg.FAST)
+    b.initialize_physical_values()
+    b.iterate(1)
+    ref, _, _ = oracle.run(ens, max_steps=1, init_physical=True, nthreads=4)
+    assert max_rel_error(b.get_state(), ref) <= FAST_TOL_STEP
+
+
+@pytest.mark.parametrize("name", ["test_integrator-whfast_jacobi", "test_integrator-whfast_whds"])
+def test_universe_methods_exact(tmp_path, name):
+    case = load_case(case_dict(name))
+    w = pg.WHFast.from_json(_json(tmp_path, name), mode=pg.EXACT)
+    w.initialize_physical_values()
+    ref, _, _ = oracle.run(case, op=oracle.INITIALIZE)
+    assert bitwise_diffs(w.get_state(), ref) == []
+    for ignore in (0, 1, 2):
+        w.gravity_calculate_acceleration(ignore)
+        ref, _, _ = oracle.run(ref, op=oracle.GRAVITY, arg=ignore)
+        assert bitwise_diffs(w.get_state(), ref) == []
+    w.calculate_additional_effects(0.0, True, True, True)
+    ref, _, _ = oracle.run(ref, op=oracle.ADDITIONAL_EFFECTS, arg=1 | 2 | 4, t_arg=0.0)
+    assert bitwise_diffs(w.get_state(), ref) == []
+
+
+def test_batched_goldens_exact():
+    cases = [load_case(case_dict(n)) for n in names()]
+    ens = stack(cases)
+    b = pg.Batch(ens, mode=pg.EXACT)
+    b.initialize_physical_values()
+    b.iterate(199, 50)
+    st = b.get_state()
+    for s, name in enumerate(names()):
+        assert max_abs_error(st["body_f64"][s], expected(name)) == 0.0, name
+    ref, _, _ = oracle.run(ens, max_steps=10**6, init_physical=True, nthreads=8)
+    assert bitwise_diffs(st, ref) == []
+
+
+def test_batched_uneven_exact_and_mappings():
+    ens = E.workload_uneven(96, seed=5)
+    ref, _, _ = oracle.run(ens, max_steps=40, init_physical=True, nthreads=8)
+    for mapping in (L.MAP_AUTO, L.MAP_LANES16, L.MAP_WARP):
+        b = pg.Batch(ens, mode=pg.EXACT, mapping=mapping)
+        b.initialize_physical_values()
+        b.iterate(40, 7)
+        assert bitwise_diffs(b.get_state(), ref) == [], mapping
+
+
+def test_batched_chunking_and_plain_agree():
+    ens = E.workload_ensemble8(8, seed=3)
+    outs = []
+    for spl in (1, 5, 20):
+        b = pg.Batch(ens, mode=pg.FAST)
+        b.initialize_physical_values()
+        b.iterate(20, spl)
+        outs.append(b.get_state())
+    assert bitwise_diffs(outs[0], outs[1]) == [] and bitwise_diffs(outs[0], outs[2]) == []
+    one = {k: (v[0] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
+    one["n"] = int(ens["sys_i64"][0, L.SI_N])
+    w = pg.WHFast.from_arrays(one, mode=pg.FAST)
+    w.initialize_physical_values()
+    # the first step reports a recovery trigger (first snapshot), so iterate()
+    # returns after it, like Ok(true) in the reference's loop
+    st, done, rec = w.iterate(20)
+    assert (st, done, rec) == (L.OK, 1, True)
+    assert w.run(19) == 19
+    plain = w.get_state()
+    assert bitwise_diffs(plain, {k: (v[:1] if isinstance(v, np.ndarray) and k != "tables" else v)
+                                 for k, v in outs[0].items()}) == []
+
+
+def test_collision_freezes_only_that_system():
+    ens = E.workload_ensemble8(4, seed=9)
+    # put planet 3 of system 1 on top of planet 2
+    ens["body_f64"][1, 3, L.POS] = ens["body_f64"][1, 2, L.POS] + 1e-9
+    ref, _, _ = oracle.run(ens, max_steps=5, init_physical=True)
+    b = pg.Batch(ens, mode=pg.EXACT)
+    b.initialize_physical_values()
+    b.iterate(5)
+    st = b.get_state()
+    assert st["sys_i64"][1, L.SI_STATUS] & L.SYS_FATAL_MASK in (L.SYS_ROCHE, L.SYS_COLLISION)
+    assert st["sys_i64"][1, L.SI_STATUS] == ref["sys_i64"][1, L.SI_STATUS]
+    assert st["sys_i64"][1, L.SI_FAIL_PAIR] == ref["sys_i64"][1, L.SI_FAIL_PAIR] == 2 * 1024 + 3
+    assert all(st["sys_i64"][s, L.SI_ITERATION] == 5 for s in (0, 2, 3))
+    assert bitwise_diffs({k: (v[[0, 2, 3]] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in st.items()},
+                         {k: (v[[0, 2, 3]] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ref.items()}) == []
