@@ -133,8 +133,9 @@ def test_batched_chunking_and_plain_agree():
 
 def test_collision_freezes_only_that_system():
     ens = E.workload_ensemble8(4, seed=9)
-    # put planet 3 of system 1 on top of planet 2
+    # put planet 3 of system 1 on top of planet 2, moving with it
     ens["body_f64"][1, 3, L.POS] = ens["body_f64"][1, 2, L.POS] + 1e-9
+    ens["body_f64"][1, 3, L.VEL] = ens["body_f64"][1, 2, L.VEL]
     ref, _, _ = oracle.run(ens, max_steps=5, init_physical=True)
     b = pg.Batch(ens, mode=pg.EXACT)
     b.initialize_physical_values()
