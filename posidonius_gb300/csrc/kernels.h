@@ -33,6 +33,9 @@ struct LaunchArgs {
 // Returns cudaSuccess or the launch error.
 cudaError_t launch_exact(const DevView& d, const LaunchArgs& a, cudaStream_t stream);
 cudaError_t launch_fast(const DevView& d, const LaunchArgs& a, cudaStream_t stream);
+// Kernel attributes (dynamic shared memory); call before the first launch.
+cudaError_t prepare_exact();
+cudaError_t prepare_fast();
 
 // Lanes per system used for a system of n bodies (0 when n is out of range).
 inline int group_size_for(int64_t n) {

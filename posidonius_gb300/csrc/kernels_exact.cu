@@ -6,4 +6,5 @@ namespace posi {
 cudaError_t launch_exact(const DevView& d, const LaunchArgs& a, cudaStream_t stream) {
     return posi_exact::launch_any(d, a, stream);
 }
+cudaError_t prepare_exact() { return posi_exact::prepare_all(); }
 }  // namespace posi

@@ -6,4 +6,5 @@ namespace posi {
 cudaError_t launch_fast(const DevView& d, const LaunchArgs& a, cudaStream_t stream) {
     return posi_fast::launch_any(d, a, stream);
 }
+cudaError_t prepare_fast() { return posi_fast::prepare_all(); }
 }  // namespace posi

@@ -38,6 +38,26 @@ static cudaError_t launch_g(const posi::DevView& v, const posi::LaunchArgs& a, c
     return cudaGetLastError();
 }
 
+template <int G>
+static cudaError_t prepare_g() {
+    const int smem = (posi::kBlockThreads / G) * GroupSmem<G>::bytes;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(whfast_steps_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(init_physical_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(gravity_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
+    return cudaFuncSetAttribute(additional_effects_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+// Dynamic shared memory above 48 KB must be allowed per kernel, outside any
+// stream capture.
+static cudaError_t prepare_all() {
+    cudaError_t e;
+    if ((e = prepare_g<4>()) != cudaSuccess) return e;
+    if ((e = prepare_g<8>()) != cudaSuccess) return e;
+    if ((e = prepare_g<16>()) != cudaSuccess) return e;
+    return prepare_g<32>();
+}
+
 static cudaError_t launch_any(const posi::DevView& v, const posi::LaunchArgs& a, cudaStream_t stream) {
     switch (a.G) {
         case 4: return launch_g<4>(v, a, stream);

@@ -230,6 +230,7 @@ posi_batch* create_batch(int64_t n_sys, int64_t nmax, const int64_t* si, const d
     if (!ok(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) || !ok(cudaEventCreate(&b->ev0)) ||
         !ok(cudaEventCreate(&b->ev1)))
         return fail(POSI_ERR_CUDA, b);
+    if (!ok(mode == POSI_MODE_EXACT ? posi::prepare_exact() : posi::prepare_fast())) return fail(POSI_ERR_CUDA, b);
     const size_t nb = (size_t)b->stride;
     b->stage_bytes = std::max({nb * POSI_BF_COUNT * sizeof(double), nb * POSI_BI_COUNT * sizeof(int64_t),
                                (size_t)n_sys * POSI_SF_COUNT * sizeof(double),

@@ -2,24 +2,32 @@
 //
 // Mapping: one group of G lanes (G = 4, 8, 16 or 32; G >= n) integrates one
 // independent system; lane j owns body j (reference particle order, the host
-// at any index).  Each lane keeps its body's whole state in registers for the
-// whole launch.  Cross-body work goes through a small per-group exchange area
-// in shared memory:
-//   - reductions over bodies (host back-reactions, midpoint convergence,
-//     democratic-heliocentric sums) are evaluated column-wise: every lane
-//     writes its body's contributions, then lane c folds column c over the
-//     bodies in index order -- the same order, hence the same rounding, as
-//     the reference's sequential loops, without G-fold redundancy;
-//   - the Jacobi recurrences are sequential by nature and run redundantly in
-//     every lane, each lane keeping its own body's result.
+// at any index).  Each lane keeps its body's state in registers for the whole
+// launch; the per-planet constants of a half kick live in shared memory.
 //
-// This header is compiled twice: with POSI_EXACT=1 and -fmad=false the code
-// keeps the reference's operation order and reproduces the Rust FP64 results
-// bit for bit; with POSI_EXACT=0 and -fmad=true the compiler contracts
-// multiply-adds and a few divisions become multiplications by shared
-// reciprocals.  Position-only and parameter-only terms are evaluated once per
-// half kick in both modes (the reference recomputes the same values on every
-// midpoint iteration, so hoisting them does not change a bit).
+// This header is compiled twice.
+//
+// POSI_EXACT=1 (with -fmad=false) keeps the reference's operation order and
+// reproduces the Rust FP64 results bit for bit.  Cross-body work goes through
+// a small per-group exchange area in shared memory: reductions over bodies
+// (host back-reactions, midpoint convergence, democratic-heliocentric sums)
+// are folded column-wise -- every lane writes its body's contributions, then
+// lane c folds column c over the bodies in index order, the reference's own
+// order -- and the Jacobi recurrences, sequential by nature, run in every lane.
+//
+// POSI_EXACT=0 (with -fmad=true) is the throughput build.  A 32-lane FP64
+// instruction holds an SMSP's FP64 pipe for the same time whatever its active
+// mask, so it minimises FP64 instructions per lane: divisions become products
+// with reciprocals computed once per launch or per half kick, the Jacobi
+// transforms are shuffle prefix / suffix scans over mass constants of the
+// launch, gravity uses rsqrt, and the host back-reactions collapse to
+// momentum sums (the host's tidal, flattening and GR acceleration is
+// -sum_p (m_p/m_host) a_p).  Results stay within 1e-12 relative per step of the
+// reference order.
+//
+// In both builds, position-only and parameter-only terms are evaluated once
+// per half kick instead of once per midpoint iteration (the reference
+// recomputes the same values, so this changes no bit).
 //
 // Reference: src/integrator/whfast.rs (step, midpoint, Kepler, transforms),
 // src/particles/universe.rs (gravity, heliocentric, additional effects),
@@ -69,18 +77,6 @@ constexpr int kMIDPOINT_MAX = 10;
 constexpr int kBISECTION_GUARD = 4096;
 constexpr int kEVO_SHIFT = 10;
 
-// Division: exact IEEE quotient in EXACT mode; a product with a reciprocal
-// evaluated once elsewhere in FAST mode.
-__device__ __forceinline__ double qdiv(double a, double b, double inv_b) {
-#if POSI_EXACT
-    (void)inv_b;
-    return a / b;
-#else
-    (void)b;
-    return a * inv_b;
-#endif
-}
-
 // LLVM's expansion of llvm.powi with a constant exponent (square-and-multiply
 // from the low bit; the first factor is taken without multiplying by one).
 template <int N>
@@ -118,21 +114,34 @@ struct Dev {
     int32_t* step_flags;           // per system: bit0 recovery trigger, bit1 historic trigger
 };
 
-// Exchange area of one group (shared memory): XS slots of G doubles, a host
-// card, column results and a few integers.
+// Per-planet constants of one half kick, slot k of lane j at P[k * G + j].
+enum {
+    PC_X = 0, PC_Y, PC_Z, PC_D, PC_INV_D, PC_XD, PC_YD, PC_ZD,
+    // constant-time-lag tides
+    PC_OS, PC_OP, PC_OSD, PC_OPD, PC_OSPD, PC_OSDD, PC_OPDD, PC_C13, PC_CONS, PC_D8, PC_TERM1, PC_TERM2, PC_T12,
+    // oblate flattening
+    PC_MHK2F, PC_HMK2F, PC_R5H, PC_R5P, PC_D5, PC_N3D5, PC_F15D7, PC_CFS, PC_CFP, PC_COFS, PC_COFP,
+    // Kidder GR
+    PC_A, PC_B, PC_C, PC_DD, PC_E, PC_T1, PC_K2C, PC_K3C, PC_K4C, PC_K5C, PC_K6C, PC_A05, PC_P, PC_Q, PC_R3,
+    PC_MRATIO, PC_MFM, PC_MU, PC_FM, PC_FM2, PC_NN0, PC_NN1, PC_NN2, PC_C6NN0, PC_C6NN1, PC_C6NN2,
+    PC_COUNT
+};
+
+// Shared memory of one group: XS exchange slots of G doubles, the per-planet
+// constants, a host card, column results and a few integers.
 constexpr int kXS = 24;
 constexpr int kCARD = 32;
 constexpr int kSUMS = 32;
 template <int G>
 struct GroupSmem {
-    static constexpr int doubles = kXS * G + kCARD + kSUMS;
+    static constexpr int doubles = kXS * G + PC_COUNT * G + kCARD + kSUMS;
     static constexpr int bytes = doubles * 8 + 32;  // + 8 ints
 };
 
 // host card slots
 enum { HC_PX = 0, HC_PY, HC_PZ, HC_VX, HC_VY, HC_VZ, HC_SX, HC_SY, HC_SZ, HC_NSV2, HC_M, HC_MG, HC_R,
-       HC_SIG, HC_K2, HC_K2F, HC_MOI, HC_AM, HC_APX, HC_APY, HC_APZ, HC_AVX, HC_AVY, HC_AVZ, HC_AAX, HC_AAY,
-       HC_AAZ, HC_COUNT };
+       HC_SIG, HC_K2, HC_K2F, HC_MOI, HC_AM, HC_SLX, HC_SLY, HC_SLZ, HC_COUNT };
+static_assert(HC_COUNT <= kCARD, "host card");
 
 struct Body {
     double m, mg, R, rg2, moi;
@@ -147,18 +156,6 @@ struct Body {
     double am, amg, ap[3], av[3], aacc[3];
 };
 
-// Per-planet constants of one half kick (positions and parameters are fixed
-// during the implicit-midpoint iterations).
-struct PC {
-    double x, y, z, d, inv_d;
-    // constant-time-lag tides
-    double o_s, o_p, osd, opd, cons, d8, term1, term2, inv_m;
-    // oblate flattening
-    double m_hk2f, hm_k2f, R5h, R5p, d5, n3d5, f15d7;
-    // Kidder GR
-    double A, B, C, D, E, t1, K2c, K3c, K4c, K5c, K6c, A05, P, Q, R3, mratio, mfM, mu, fm, fm2, nn[3];
-};
-
 template <int G>
 struct Sys {
     // uniform per group
@@ -168,20 +165,47 @@ struct Sys {
     double dt, half_dt, t, time_limit, last_hist, hist_period, last_rec, rec_period;
     int64_t iteration, n_hist, tw, status, fail_step, fail_pair, mid_iters;
     double* xs;
+    double* pcs;
     double* card;
     double* sums;
     int* isc;
     // own body
     bool has, is_host;
     Body b;
-    PC pc;
+#if !POSI_EXACT
+    // mass-only constants of the launch
+    double inv_m, inv_moi, inv_eta_excl, jac_c, eta_incl, kep_gm, gm_neg, whds_f, whds_w, dh_w;
+    double inv_mtot, inv_hm;
+    bool first_planet;
+#endif
 
     __device__ __forceinline__ void sync() const {
         if (G > 1) __syncwarp(mask);
     }
     __device__ __forceinline__ double& X(int slot, int j) const { return xs[slot * G + j]; }
+    __device__ __forceinline__ double& P(int slot) const { return pcs[slot * G + lane]; }
     __device__ __forceinline__ bool fatal() const { return (status & POSI_SYS_FATAL_MASK) != 0; }
     __device__ __forceinline__ bool planet() const { return has && !is_host; }
+
+#if !POSI_EXACT
+    // group collectives over the G lanes of this system
+    __device__ __forceinline__ double gbcast(double v, int src) const {
+        return G > 1 ? __shfl_sync(mask, v, src, G) : v;
+    }
+    __device__ __forceinline__ double gscan(double v) const {  // inclusive prefix in lane order
+#pragma unroll
+        for (int off = 1; off < G; off <<= 1) {
+            const double y = __shfl_up_sync(mask, v, off, G);
+            if (lane >= off) v += y;
+        }
+        return v;
+    }
+    __device__ __forceinline__ double gsum(double v) const {
+#pragma unroll
+        for (int off = G / 2; off > 0; off >>= 1) v += __shfl_xor_sync(mask, v, off, G);
+        return v;
+    }
+#endif
 
     // ------------------------------------------------------------------
     // load / store
@@ -191,7 +215,8 @@ struct Sys {
         lane = lane_;
         mask = mask_;
         xs = smem;
-        card = smem + kXS * G;
+        pcs = smem + kXS * G;
+        card = pcs + PC_COUNT * G;
         sums = card + kCARD;
         isc = reinterpret_cast<int*>(sums + kSUMS);
         const int64_t ns = D.n_sys;
@@ -221,45 +246,54 @@ struct Sys {
         has = lane < n;
         is_host = lane == host;
         if (lane < 8) isc[lane] = 0;
-        sync();
-        if (!has) return;
-        const int64_t st = D.stride;
-        const int64_t o = (int64_t)s * D.nmax + lane;
-        const double* F = D.bf + o;
-        b.m = F[POSI_BF_MASS * st];
-        b.mg = F[POSI_BF_MASS_G * st];
-        b.R = F[POSI_BF_RADIUS * st];
-        b.rg2 = F[POSI_BF_RG2 * st];
-        b.moi = F[POSI_BF_MOI * st];
+        b.m = 0.; b.mg = 0.; b.R = 0.; b.moi = 0.;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            b.r[k] = F[(POSI_BF_PX + k) * st];
-            b.v[k] = F[(POSI_BF_VX + k) * st];
-            b.a[k] = F[(POSI_BF_AX + k) * st];
-            b.L[k] = F[(POSI_BF_LX + k) * st];
-            b.S[k] = F[(POSI_BF_SX + k) * st];
-            b.ev[k] = F[(POSI_BF_EVX + k) * st];
-            b.eL[k] = F[(POSI_BF_ELX + k) * st];
-            b.aa[k] = F[(POSI_BF_ADDAX + k) * st];
-            b.dl[k] = F[(POSI_BF_DLX + k) * st];
+            b.r[k] = 0.; b.v[k] = 0.; b.a[k] = 0.; b.L[k] = 0.; b.S[k] = 0.;
             b.ap[k] = 0.; b.av[k] = 0.; b.aacc[k] = 0.;
         }
-        b.nsv2 = F[POSI_BF_NSV2 * st];
-        b.sig = F[POSI_BF_SIGMA * st];
-        b.k2 = F[POSI_BF_K2 * st];
-        b.k2f = F[POSI_BF_K2F * st];
-        b.denergy = F[POSI_BF_DENERGY_DT * st];
-        b.lag = F[POSI_BF_LAG_ANGLE * st];
-        const int64_t* I = D.bi + o;
-        b.tk = (int)I[POSI_BI_TIDES_KIND * st];
-        b.fk = (int)I[POSI_BI_FLAT_KIND * st];
-        b.gk = (int)I[POSI_BI_GR_KIND * st];
-        b.evo = (int)I[POSI_BI_EVO_TYPE * st];
-        b.eoff = I[POSI_BI_EVO_OFFSET * st];
-        b.elen = I[POSI_BI_EVO_LEN * st];
-        b.eleft = I[POSI_BI_EVO_LEFT * st];
-        if (b.elen <= 0) b.evo = POSI_EVO_NON_EVOLVING;
         b.am = 0.; b.amg = 0.;
+        if (has) {
+            const int64_t st = D.stride;
+            const int64_t o = (int64_t)s * D.nmax + lane;
+            const double* F = D.bf + o;
+            b.m = F[POSI_BF_MASS * st];
+            b.mg = F[POSI_BF_MASS_G * st];
+            b.R = F[POSI_BF_RADIUS * st];
+            b.rg2 = F[POSI_BF_RG2 * st];
+            b.moi = F[POSI_BF_MOI * st];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                b.r[k] = F[(POSI_BF_PX + k) * st];
+                b.v[k] = F[(POSI_BF_VX + k) * st];
+                b.a[k] = F[(POSI_BF_AX + k) * st];
+                b.L[k] = F[(POSI_BF_LX + k) * st];
+                b.S[k] = F[(POSI_BF_SX + k) * st];
+                b.ev[k] = F[(POSI_BF_EVX + k) * st];
+                b.eL[k] = F[(POSI_BF_ELX + k) * st];
+                b.aa[k] = F[(POSI_BF_ADDAX + k) * st];
+                b.dl[k] = F[(POSI_BF_DLX + k) * st];
+            }
+            b.nsv2 = F[POSI_BF_NSV2 * st];
+            b.sig = F[POSI_BF_SIGMA * st];
+            b.k2 = F[POSI_BF_K2 * st];
+            b.k2f = F[POSI_BF_K2F * st];
+            b.denergy = F[POSI_BF_DENERGY_DT * st];
+            b.lag = F[POSI_BF_LAG_ANGLE * st];
+            const int64_t* I = D.bi + o;
+            b.tk = (int)I[POSI_BI_TIDES_KIND * st];
+            b.fk = (int)I[POSI_BI_FLAT_KIND * st];
+            b.gk = (int)I[POSI_BI_GR_KIND * st];
+            b.evo = (int)I[POSI_BI_EVO_TYPE * st];
+            b.eoff = I[POSI_BI_EVO_OFFSET * st];
+            b.elen = I[POSI_BI_EVO_LEN * st];
+            b.eleft = I[POSI_BI_EVO_LEFT * st];
+            if (b.elen <= 0) b.evo = POSI_EVO_NON_EVOLVING;
+        }
+        sync();
+#if !POSI_EXACT
+        mass_constants();
+#endif
     }
 
     __device__ void store(const Dev& D) const {
@@ -326,6 +360,35 @@ struct Sys {
         sync();
     }
 
+#if !POSI_EXACT
+    // Mass-only constants of the launch: Jacobi prefix masses (host first,
+    // then the other bodies in index order), reciprocals, Kepler GM.
+    __device__ void mass_constants() {
+        const double own_m = planet() ? b.m : 0.;
+        const double own_mg = planet() ? b.mg : 0.;
+        const double hm = gbcast(has ? b.m : 0., host);
+        const double hmg = gbcast(has ? b.mg : 0., host);
+        const double incl_m = gscan(own_m);
+        const double incl_mg = gscan(own_mg);
+        const double tot_m = gbcast(incl_m, G - 1);
+        const double eta_excl = hm + (incl_m - own_m);
+        eta_incl = hm + incl_m;
+        inv_eta_excl = planet() ? 1. / eta_excl : 0.;
+        jac_c = planet() ? b.m / eta_incl : 0.;
+        kep_gm = hmg + incl_mg;
+        inv_mtot = 1. / (hm + tot_m);
+        inv_hm = 1. / hm;
+        inv_m = has ? 1. / b.m : 0.;
+        inv_moi = (has && b.moi != 0.) ? 1. / b.moi : 0.;
+        gm_neg = -kG * b.m;
+        whds_f = (hm + b.m) * inv_hm;             // (m0 + m) / m0
+        whds_w = planet() ? b.m / (hm + b.m) : 0.;
+        dh_w = planet() ? b.m * inv_hm : 0.;
+        const int p0 = host == 0 ? 1 : 0;
+        first_planet = lane == p0;
+    }
+#endif
+
     // ------------------------------------------------------------------
     // src/effects/evolution.rs:446-546 + src/tools.rs:840-907
     // ------------------------------------------------------------------
@@ -364,6 +427,9 @@ struct Sys {
             b.R = nr;
             b.rg2 = ng;
             b.moi = b.m * b.rg2 * powi<2>(b.R);
+#if !POSI_EXACT
+            inv_moi = b.moi != 0. ? 1. / b.moi : 0.;
+#endif
         }
         // The love-number update of the reference writes to a copy; only the
         // table index moves.
@@ -377,9 +443,15 @@ struct Sys {
             if (b.moi == 0.) {
                 isc[1] = 1;
             } else {
+#if POSI_EXACT
                 b.S[0] = b.L[0] / b.moi;
                 b.S[1] = b.L[1] / b.moi;
                 b.S[2] = b.L[2] / b.moi;
+#else
+                b.S[0] = b.L[0] * inv_moi;
+                b.S[1] = b.L[1] * inv_moi;
+                b.S[2] = b.L[2] * inv_moi;
+#endif
                 b.nsv2 = powi<2>(b.S[0]) + powi<2>(b.S[1]) + powi<2>(b.S[2]);
             }
             if (evolution && evo) b.lag = 0.;
@@ -396,36 +468,71 @@ struct Sys {
     // Per-planet constants of a half kick (after the spin/evolution update
     // of its first midpoint iteration, so that evolved radii are used).
     // ------------------------------------------------------------------
+    // Heliocentric position of a planet, its distance and unit vector: fixed
+    // for a whole half kick, needed from the first evaluation on.
+    __device__ void set_geometry(double x, double y, double z) {
+        P(PC_X) = x;
+        P(PC_Y) = y;
+        P(PC_Z) = z;
+        const double d = sqrt(powi<2>(x) + powi<2>(y) + powi<2>(z));
+        const double inv_d = 1. / d;
+        P(PC_D) = d;
+        P(PC_INV_D) = inv_d;
+        P(PC_XD) = x * inv_d;
+        P(PC_YD) = y * inv_d;
+        P(PC_ZD) = z * inv_d;
+    }
+
     __device__ void planet_constants() {
         const double hm = card[HC_M], hmg = card[HC_MG], hR = card[HC_R], hsig = card[HC_SIG];
         const double hk2 = card[HC_K2], hk2f = card[HC_K2F];
-        PC& c = pc;
-        const double d = c.d;
-        c.inv_d = 1. / d;
-        c.inv_m = 1. / b.m;
+        const double d = P(PC_D);
+        const double inv_d = P(PC_INV_D);
         if (tides && b.tk == POSI_EFFECT_ORBITING) {
             // src/effects/tides/constant_time_lag.rs:229-264, :266-307
             const double d7 = powi<7>(d);
-            c.o_s = 4.5 * powi<2>(b.m) * powi<10>(hR) * hsig / d7;
-            c.o_p = 4.5 * powi<2>(hm) * powi<10>(b.R) * b.sig / d7;
-            c.osd = c.o_s / d;
-            c.opd = c.o_p / d;
+            const double o_s = 4.5 * powi<2>(b.m) * powi<10>(hR) * hsig / d7;
+            const double o_p = 4.5 * powi<2>(hm) * powi<10>(b.R) * b.sig / d7;
+            P(PC_OS) = o_s;
+            P(PC_OP) = o_p;
+            P(PC_OSD) = o_s / d;
+            P(PC_OPD) = o_p / d;
             const double hm2 = hm * hm;
             const double m2 = b.m * b.m;
-            c.cons = kMINUS_3K2 / powi<7>(d) * (m2 * powi<5>(hR) * hk2 + hm2 * powi<5>(b.R) * b.k2);
-            c.d8 = powi<8>(d);
-            c.term1 = m2 * powi<10>(hR) * hsig;
-            c.term2 = hm2 * powi<10>(b.R) * b.sig;
+            P(PC_CONS) = kMINUS_3K2 / powi<7>(d) * (m2 * powi<5>(hR) * hk2 + hm2 * powi<5>(b.R) * b.k2);
+            const double d8 = powi<8>(d);
+            P(PC_D8) = d8;
+            const double term1 = m2 * powi<10>(hR) * hsig;
+            const double term2 = hm2 * powi<10>(b.R) * b.sig;
+            P(PC_TERM1) = term1;
+            P(PC_TERM2) = term2;
+#if !POSI_EXACT
+            P(PC_OSPD) = (o_s + o_p) * inv_d;
+            P(PC_OSDD) = o_s * d;
+            P(PC_OPDD) = o_p * d;
+            P(PC_C13) = -13.5 / d8;
+            P(PC_T12) = term1 + term2;
+#endif
         }
         if (flat && b.fk == POSI_EFFECT_ORBITING) {
             // src/effects/rotational_flattening/oblate_spheroid.rs:12-60
-            c.m_hk2f = b.m * hk2f;
-            c.hm_k2f = hm * b.k2f;
-            c.R5h = powi<5>(hR);
-            c.R5p = powi<5>(b.R);
-            c.d5 = powi<5>(d);
-            c.n3d5 = -3. / powi<5>(d);
-            c.f15d7 = 15. / powi<7>(d);
+            P(PC_MHK2F) = b.m * hk2f;
+            P(PC_HMK2F) = hm * b.k2f;
+            P(PC_R5H) = powi<5>(hR);
+            P(PC_R5P) = powi<5>(b.R);
+            P(PC_D5) = powi<5>(d);
+            P(PC_N3D5) = -3. / powi<5>(d);
+            P(PC_F15D7) = 15. / powi<7>(d);
+#if !POSI_EXACT
+            // factor_star = cfs |Omega_host|^2, ortho_star = cofs (r . Omega_host(previous))
+            const double cfs = b.m * hk2f * powi<5>(hR) * (1. / 6.);
+            const double cfp = hm * b.k2f * powi<5>(b.R) * (1. / 6.);
+            const double inv_d5 = 1. / powi<5>(d);
+            P(PC_CFS) = cfs;
+            P(PC_CFP) = cfp;
+            P(PC_COFS) = -6. * cfs * inv_d5;
+            P(PC_COFP) = -6. * cfp * inv_d5;
+#endif
         }
         if (gr && b.gk == POSI_EFFECT_ORBITING) {
             // src/effects/general_relativity.rs:98, :187-298, :300-456
@@ -434,42 +541,51 @@ struct Sys {
             const double d2 = powi<2>(d);
             const double mgd = mgs / d;
             const double f2 = powi<2>(f);
-            c.A = -mgs / (d2 * kC2);
-            c.B = 1.0 + 3.0 * f;
-            c.C = 2.0 * (2.0 + f) * mgs / d;
-            c.D = 1.5 * f;
-            c.E = mgs / (d2 * kC2) * 2.0 * (2.0 - f);
-            c.t1 = (3.0 / 4.0) * (12.0 + 29.0 * f) * (powi<2>(mgs) / d2);
-            c.K2c = f * (3.0 - 4.0 * f);
-            c.K3c = (15.0 / 8.0) * f * (1.0 - 3.0 * f);
-            c.K4c = (3.0 / 2.0) * f * (3.0 - 4.0 * f);
-            c.K5c = 0.5 * f * (13.0 - 4.0 * f) * mgd;
-            c.K6c = (2.0 + 25.0 * f + 2.0 * f2) * mgd;
-            c.A05 = c.A * (-0.5);
-            c.P = f * (15.0 + 4.0 * f);
-            c.Q = (4.0 + 41.0 * f + 8.0 * f2) * mgd;
-            c.R3 = 3.0 * f * (3.0 + 2.0 * f);
-            c.mratio = b.m / hm;
+            const double A = -mgs / (d2 * kC2);
+            P(PC_A) = A;
+            P(PC_B) = 1.0 + 3.0 * f;
+            P(PC_C) = 2.0 * (2.0 + f) * mgs / d;
+            P(PC_DD) = 1.5 * f;
+            P(PC_E) = mgs / (d2 * kC2) * 2.0 * (2.0 - f);
+            P(PC_T1) = (3.0 / 4.0) * (12.0 + 29.0 * f) * (powi<2>(mgs) / d2);
+            P(PC_K2C) = f * (3.0 - 4.0 * f);
+            P(PC_K3C) = (15.0 / 8.0) * f * (1.0 - 3.0 * f);
+            P(PC_K4C) = (3.0 / 2.0) * f * (3.0 - 4.0 * f);
+            P(PC_K5C) = 0.5 * f * (13.0 - 4.0 * f) * mgd;
+            P(PC_K6C) = (2.0 + 25.0 * f + 2.0 * f2) * mgd;
+            P(PC_A05) = A * (-0.5);
+            P(PC_P) = f * (15.0 + 4.0 * f);
+            P(PC_Q) = (4.0 + 41.0 * f + 8.0 * f2) * mgd;
+            P(PC_R3) = 3.0 * f * (3.0 + 2.0 * f);
+            P(PC_MRATIO) = b.m / hm;
             const double M = hm + b.m;
             const double mf = (hm - b.m) / M;
-            c.mfM = mf * M;
-            c.mu = (hm * b.m) / M;
-            c.fm = 2. + (3. / 2.) * b.m / hm;
-            c.fm2 = 2. + (3. / 2.) * hm / b.m;
-            c.nn[0] = c.x / d;
-            c.nn[1] = c.y / d;
-            c.nn[2] = c.z / d;
+            P(PC_MFM) = mf * M;
+            P(PC_MU) = (hm * b.m) / M;
+            P(PC_FM) = 2. + (3. / 2.) * b.m / hm;
+            P(PC_FM2) = 2. + (3. / 2.) * hm / b.m;
+            const double n0 = P(PC_X) / d, n1 = P(PC_Y) / d, n2 = P(PC_Z) / d;
+            P(PC_NN0) = n0;
+            P(PC_NN1) = n1;
+            P(PC_NN2) = n2;
+            P(PC_C6NN0) = 6. * n0;
+            P(PC_C6NN1) = 6. * n1;
+            P(PC_C6NN2) = 6. * n2;
         }
+#if !POSI_EXACT
+        if (!(gr && b.gk == POSI_EFFECT_ORBITING)) P(PC_MRATIO) = b.m * card[HC_M] == 0. ? 0. : b.m / hm;
+#endif
     }
 
     // ------------------------------------------------------------------
     // One evaluation of src/particles/universe.rs:428-538 (after
     // inertial_to_heliocentric :318-351), it = midpoint iteration.
+    // ------------------------------------------------------------------
+#if POSI_EXACT
     // Contribution columns written per planet (host back-reactions):
     //  0-2 tidal force, 3-5 -torque on host (tides), 6-8 flattening force,
     //  9-11 -torque on host (flattening), 12-14 (m/M) a_1PN, 15-17 (m/M) a_2PN,
     //  18-20 (m/M) a_SO, 21-23 host dL/dt (GR).
-    // ------------------------------------------------------------------
     __device__ void additional_effects(const Dev& D, int it, bool evolution_now) {
         // host inertial velocity and the spin it had before this evaluation
         sync();
@@ -480,18 +596,19 @@ struct Sys {
         if (lane == 0) isc[1] = 0;
         sync();
         double hv[3] = {0., 0., 0.}, vr = 0., nv2 = 0., nv = 0., rs_s = 0., rs_p = 0.;
+        const double x = P(PC_X), y = P(PC_Y), z = P(PC_Z), d = P(PC_D);
         if (planet()) {
             hv[0] = b.v[0] - card[HC_VX];
             hv[1] = b.v[1] - card[HC_VY];
             hv[2] = b.v[2] - card[HC_VZ];
-            vr = (pc.x * hv[0] + pc.y * hv[1] + pc.z * hv[2]) / pc.d;
+            vr = (x * hv[0] + y * hv[1] + z * hv[2]) / d;
             // the host's previous heliocentric velocity is zero (universe.rs:335-338)
             nv2 = powi<2>(hv[0] - 0.) + powi<2>(hv[1] - 0.) + powi<2>(hv[2] - 0.);
             nv = sqrt(nv2);
             // tides::initialize / rotational_flattening::initialize use the spin
             // computed before this evaluation
-            rs_s = pc.x * card[HC_SX] + pc.y * card[HC_SY] + pc.z * card[HC_SZ];
-            rs_p = pc.x * b.S[0] + pc.y * b.S[1] + pc.z * b.S[2];
+            rs_s = x * card[HC_SX] + y * card[HC_SY] + z * card[HC_SZ];
+            rs_p = x * b.S[0] + y * b.S[1] + z * b.S[2];
         }
         spin_and_evolving(D, t, evolution_now);
         zero_inertia_check();
@@ -508,54 +625,54 @@ struct Sys {
         const double hnsv2 = card[HC_NSV2];
         double at[3] = {0., 0., 0.}, af[3] = {0., 0., 0.}, ag[3] = {0., 0., 0.};
         double dt_[3] = {0., 0., 0.}, df[3] = {0., 0., 0.}, dg[3] = {0., 0., 0.};
-        // contribution columns go straight to the exchange area (zeros for
-        // effects a planet does not take part in)
         const int ncol = gr ? 24 : (flat ? 12 : (tides ? 6 : 0));
         if (planet()) {
             for (int k = 0; k < ncol; ++k) X(k, lane) = 0.;
         }
         double* col = planet() ? &X(0, lane) : nullptr;
         if (planet()) {
-            const PC& c = pc;
-            const double x = c.x, y = c.y, z = c.z, d = c.d;
+            const double inv_m = 1. / b.m;
             if (tides && b.tk == POSI_EFFECT_ORBITING) {
+                const double o_s = P(PC_OS), o_p = P(PC_OP), osd = P(PC_OSD), opd = P(PC_OPD);
                 // radial component (constant_time_lag.rs:266-307)
-                const double factor1 = -13.5 * vr / c.d8;
-                const double diss_pm = factor1 * c.term2;
-                const double radial = c.cons + (diss_pm + factor1 * c.term1);
+                const double factor1 = -13.5 * vr / P(PC_D8);
+                const double diss_pm = factor1 * P(PC_TERM2);
+                const double radial = P(PC_CONS) + (diss_pm + factor1 * P(PC_TERM1));
                 // force (constant_time_lag.rs:309-332)
-                const double factor3 = radial + qdiv((c.o_s + c.o_p) * vr, d, c.inv_d);
+                const double factor3 = radial + (o_s + o_p) * vr / d;
                 double F[3];
-                F[0] = qdiv(factor3 * x, d, c.inv_d) + c.osd * (hS1 * z - hS2 * y - hv[0]) + c.opd * (b.S[1] * z - b.S[2] * y - hv[0]);
-                F[1] = qdiv(factor3 * y, d, c.inv_d) + c.osd * (hS2 * x - hS0 * z - hv[1]) + c.opd * (b.S[2] * x - b.S[0] * z - hv[1]);
-                F[2] = qdiv(factor3 * z, d, c.inv_d) + c.osd * (hS0 * y - hS1 * x - hv[2]) + c.opd * (b.S[0] * y - b.S[1] * x - hv[2]);
+                F[0] = factor3 * x / d + osd * (hS1 * z - hS2 * y - hv[0]) + opd * (b.S[1] * z - b.S[2] * y - hv[0]);
+                F[1] = factor3 * y / d + osd * (hS2 * x - hS0 * z - hv[1]) + opd * (b.S[2] * x - b.S[0] * z - hv[1]);
+                F[2] = factor3 * z / d + osd * (hS0 * y - hS1 * x - hv[2]) + opd * (b.S[0] * y - b.S[1] * x - hv[2]);
                 // tides/common.rs:312-370
-                at[0] = c.inv_m * F[0]; at[1] = c.inv_m * F[1]; at[2] = c.inv_m * F[2];
+                at[0] = inv_m * F[0]; at[1] = inv_m * F[1]; at[2] = inv_m * F[2];
                 col[0 * G] = F[0]; col[1 * G] = F[1]; col[2 * G] = F[2];
                 // torques (constant_time_lag.rs:171-204), tides/common.rs:223-261
                 const double h0 = y * hv[2] - z * hv[1];
                 const double h1 = z * hv[0] - x * hv[2];
                 const double h2 = x * hv[1] - y * hv[0];
-                dt_[0] = -1.0 * (c.o_p * (d * b.S[0] - qdiv(rs_p * x, d, c.inv_d) - c.inv_d * h0));
-                dt_[1] = -1.0 * (c.o_p * (d * b.S[1] - qdiv(rs_p * y, d, c.inv_d) - c.inv_d * h1));
-                dt_[2] = -1.0 * (c.o_p * (d * b.S[2] - qdiv(rs_p * z, d, c.inv_d) - c.inv_d * h2));
-                col[3 * G] = -1.0 * (c.o_s * (d * hS0 - qdiv(rs_s * x, d, c.inv_d) - c.inv_d * h0));
-                col[4 * G] = -1.0 * (c.o_s * (d * hS1 - qdiv(rs_s * y, d, c.inv_d) - c.inv_d * h1));
-                col[5 * G] = -1.0 * (c.o_s * (d * hS2 - qdiv(rs_s * z, d, c.inv_d) - c.inv_d * h2));
+                const double inv_d = P(PC_INV_D);
+                dt_[0] = -1.0 * (o_p * (d * b.S[0] - rs_p * x / d - inv_d * h0));
+                dt_[1] = -1.0 * (o_p * (d * b.S[1] - rs_p * y / d - inv_d * h1));
+                dt_[2] = -1.0 * (o_p * (d * b.S[2] - rs_p * z / d - inv_d * h2));
+                col[3 * G] = -1.0 * (o_s * (d * hS0 - rs_s * x / d - inv_d * h0));
+                col[4 * G] = -1.0 * (o_s * (d * hS1 - rs_s * y / d - inv_d * h1));
+                col[5 * G] = -1.0 * (o_s * (d * hS2 - rs_s * z / d - inv_d * h2));
             }
             if (flat && b.fk == POSI_EFFECT_ORBITING) {
                 // oblate_spheroid.rs:12-60
-                const double fs = c.m_hk2f * hnsv2 * c.R5h / 6.;
-                const double ofs = -6. * fs * rs_s / (hnsv2 * c.d5);
-                const double fp = c.hm_k2f * b.nsv2 * c.R5p / 6.;
-                const double ofp = -6. * fp * rs_p / (b.nsv2 * c.d5);
-                const double radial = c.n3d5 * (fp + fs) + c.f15d7 * (fs * rs_s * rs_s / hnsv2 + fp * rs_p * rs_p / b.nsv2);
+                const double d5 = P(PC_D5);
+                const double fs = P(PC_MHK2F) * hnsv2 * P(PC_R5H) / 6.;
+                const double ofs = -6. * fs * rs_s / (hnsv2 * d5);
+                const double fp = P(PC_HMK2F) * b.nsv2 * P(PC_R5P) / 6.;
+                const double ofp = -6. * fp * rs_p / (b.nsv2 * d5);
+                const double radial = P(PC_N3D5) * (fp + fs) + P(PC_F15D7) * (fs * rs_s * rs_s / hnsv2 + fp * rs_p * rs_p / b.nsv2);
                 // oblate_spheroid.rs:83-97, common.rs:203-237
                 double F[3];
                 F[0] = radial * x + ofp * b.S[0] + ofs * hS0;
                 F[1] = radial * y + ofp * b.S[1] + ofs * hS1;
                 F[2] = radial * z + ofp * b.S[2] + ofs * hS2;
-                af[0] = c.inv_m * F[0]; af[1] = c.inv_m * F[1]; af[2] = c.inv_m * F[2];
+                af[0] = inv_m * F[0]; af[1] = inv_m * F[1]; af[2] = inv_m * F[2];
                 col[6 * G] = F[0]; col[7 * G] = F[1]; col[8 * G] = F[2];
                 // oblate_spheroid.rs:62-81, common.rs:165-201
                 df[0] = -1.0 * (ofp * (y * b.S[2] - z * b.S[1]));
@@ -567,34 +684,35 @@ struct Sys {
             }
             if (gr && b.gk == POSI_EFFECT_ORBITING) {
                 const double vr2 = powi<2>(vr);
-                const double inv_nv = 1. / nv;
                 // first order (general_relativity.rs:187-239)
-                const double radial1 = c.A * (c.B * nv2 - c.C - c.D * vr2);
-                const double ortho1 = c.E * vr * nv;
+                const double radial1 = P(PC_A) * (P(PC_B) * nv2 - P(PC_C) - P(PC_DD) * vr2);
+                const double ortho1 = P(PC_E) * vr * nv;
                 double a1[3];
-                a1[0] = qdiv(radial1 * x, d, c.inv_d) + qdiv(ortho1 * hv[0], nv, inv_nv);
-                a1[1] = qdiv(radial1 * y, d, c.inv_d) + qdiv(ortho1 * hv[1], nv, inv_nv);
-                a1[2] = qdiv(radial1 * z, d, c.inv_d) + qdiv(ortho1 * hv[2], nv, inv_nv);
+                a1[0] = radial1 * x / d + ortho1 * hv[0] / nv;
+                a1[1] = radial1 * y / d + ortho1 * hv[1] / nv;
+                a1[2] = radial1 * z / d + ortho1 * hv[2] / nv;
                 // second order (:241-298)
                 const double nv4 = powi<2>(nv2);
                 const double vr4 = powi<2>(vr2);
-                const double radial2 = c.A * (c.t1 + c.K2c * nv4 + c.K3c * vr4 - c.K4c * vr2 * nv2 - c.K5c * nv2 - c.K6c * vr2);
-                const double ortho2 = c.A05 * vr * (c.P * nv2 - c.Q - c.R3 * vr2);
+                const double radial2 = P(PC_A) * (P(PC_T1) + P(PC_K2C) * nv4 + P(PC_K3C) * vr4 - P(PC_K4C) * vr2 * nv2 -
+                                                  P(PC_K5C) * nv2 - P(PC_K6C) * vr2);
+                const double ortho2 = P(PC_A05) * vr * (P(PC_P) * nv2 - P(PC_Q) - P(PC_R3) * vr2);
                 double a2[3];
-                a2[0] = qdiv(radial2 * x, d, c.inv_d) + ortho2 * hv[0];
-                a2[1] = qdiv(radial2 * y, d, c.inv_d) + ortho2 * hv[1];
-                a2[2] = qdiv(radial2 * z, d, c.inv_d) + ortho2 * hv[2];
+                a2[0] = radial2 * x / d + ortho2 * hv[0];
+                a2[1] = radial2 * y / d + ortho2 * hv[1];
+                a2[2] = radial2 * z / d + ortho2 * hv[2];
                 // spin-orbit (:300-456)
                 const double hmoi = card[HC_MOI], hm = card[HC_M];
                 const double sL0 = hmoi * hS0, sL1 = hmoi * hS1, sL2 = hmoi * hS2;
                 const double pL0 = b.moi * b.S[0], pL1 = b.moi * b.S[1], pL2 = b.moi * b.S[2];
-                const double* nn = c.nn;
-                const double msx = c.mfM * (pL0 / b.m - sL0 / hm);
-                const double msy = c.mfM * (pL1 / b.m - sL1 / hm);
-                const double msz = c.mfM * (pL2 / b.m - sL2 / hm);
-                const double e1x = 6. * nn[0] * ((nn[1] * hv[2] - nn[2] * hv[1]) * (2. * (sL0 + pL0) + msx));
-                const double e1y = 6. * nn[1] * ((nn[2] * hv[0] - nn[0] * hv[2]) * (2. * (sL1 + pL1) + msy));
-                const double e1z = 6. * nn[2] * ((nn[0] * hv[1] - nn[1] * hv[0]) * (2. * (sL2 + pL2) + msz));
+                const double nn0 = P(PC_NN0), nn1 = P(PC_NN1), nn2 = P(PC_NN2);
+                const double mfM = P(PC_MFM);
+                const double msx = mfM * (pL0 / b.m - sL0 / hm);
+                const double msy = mfM * (pL1 / b.m - sL1 / hm);
+                const double msz = mfM * (pL2 / b.m - sL2 / hm);
+                const double e1x = 6. * nn0 * ((nn1 * hv[2] - nn2 * hv[1]) * (2. * (sL0 + pL0) + msx));
+                const double e1y = 6. * nn1 * ((nn2 * hv[0] - nn0 * hv[2]) * (2. * (sL1 + pL1) + msy));
+                const double e1z = 6. * nn2 * ((nn0 * hv[1] - nn1 * hv[0]) * (2. * (sL2 + pL2) + msz));
                 const double e7x = 7. * (sL0 + pL0) + 3. * msx;
                 const double e7y = 7. * (sL1 + pL1) + 3. * msy;
                 const double e7z = 7. * (sL2 + pL2) + 3. * msz;
@@ -604,9 +722,9 @@ struct Sys {
                 const double e3sx = 3. * (sL0 + pL0) + msx;
                 const double e3sy = 3. * (sL1 + pL1) + msy;
                 const double e3sz = 3. * (sL2 + pL2) + msz;
-                const double e3x = 3. * vr * (nn[1] * e3sz - nn[2] * e3sy);
-                const double e3y = 3. * vr * (nn[2] * e3sx - nn[0] * e3sz);
-                const double e3z = 3. * vr * (nn[0] * e3sy - nn[1] * e3sx);
+                const double e3x = 3. * vr * (nn1 * e3sz - nn2 * e3sy);
+                const double e3y = 3. * vr * (nn2 * e3sx - nn0 * e3sz);
+                const double e3z = 3. * vr * (nn0 * e3sy - nn1 * e3sx);
                 double a3[3];
                 a3[0] = kFA * (e1x - e2x + e3x);
                 a3[1] = kFA * (e1y - e2y + e3y);
@@ -614,39 +732,41 @@ struct Sys {
                 ag[0] = a1[0] + a2[0] + a3[0];
                 ag[1] = a1[1] + a2[1] + a3[1];
                 ag[2] = a1[2] + a2[2] + a3[2];
+                const double mratio = P(PC_MRATIO);
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    col[(12 + k) * G] = c.mratio * a1[k];
-                    col[(15 + k) * G] = c.mratio * a2[k];
-                    col[(18 + k) * G] = c.mratio * a3[k];
+                    col[(12 + k) * G] = mratio * a1[k];
+                    col[(15 + k) * G] = mratio * a2[k];
+                    col[(18 + k) * G] = mratio * a3[k];
                 }
                 // Kidder 1995 eq. 2.4a / 2.4b
-                const double lo0 = c.mu * (y * hv[2] - z * hv[1]);
-                const double lo1 = c.mu * (z * hv[0] - x * hv[2]);
-                const double lo2 = c.mu * (x * hv[1] - y * hv[0]);
-                const double h1x = c.fm * (lo1 * sL2 - lo2 * sL1);
-                const double h1y = c.fm * (lo2 * sL0 - lo0 * sL2);
-                const double h1z = c.fm * (lo0 * sL1 - lo1 * sL0);
+                const double mu = P(PC_MU), fm = P(PC_FM), fm2 = P(PC_FM2);
+                const double lo0 = mu * (y * hv[2] - z * hv[1]);
+                const double lo1 = mu * (z * hv[0] - x * hv[2]);
+                const double lo2 = mu * (x * hv[1] - y * hv[0]);
+                const double h1x = fm * (lo1 * sL2 - lo2 * sL1);
+                const double h1y = fm * (lo2 * sL0 - lo0 * sL2);
+                const double h1z = fm * (lo0 * sL1 - lo1 * sL0);
                 const double h2x = pL1 * sL2 - pL2 * sL1;
                 const double h2y = pL2 * sL0 - pL0 * sL2;
                 const double h2z = pL0 * sL1 - pL1 * sL0;
-                const double sp = nn[0] * pL0 + nn[1] * pL1 + nn[2] * pL2;
-                const double h3x = 3. * sp * (nn[1] * sL2 - nn[2] * sL1);
-                const double h3y = 3. * sp * (nn[2] * sL0 - nn[0] * sL2);
-                const double h3z = 3. * sp * (nn[0] * sL1 - nn[1] * sL0);
+                const double sp = nn0 * pL0 + nn1 * pL1 + nn2 * pL2;
+                const double h3x = 3. * sp * (nn1 * sL2 - nn2 * sL1);
+                const double h3y = 3. * sp * (nn2 * sL0 - nn0 * sL2);
+                const double h3z = 3. * sp * (nn0 * sL1 - nn1 * sL0);
                 col[21 * G] = kFA * (h1x - h2x + h3x);
                 col[22 * G] = kFA * (h1y - h2y + h3y);
                 col[23 * G] = kFA * (h1z - h2z + h3z);
-                const double q1x = c.fm2 * (lo1 * pL2 - lo2 * pL1);
-                const double q1y = c.fm2 * (lo2 * pL0 - lo0 * pL2);
-                const double q1z = c.fm2 * (lo0 * pL1 - lo1 * pL0);
+                const double q1x = fm2 * (lo1 * pL2 - lo2 * pL1);
+                const double q1y = fm2 * (lo2 * pL0 - lo0 * pL2);
+                const double q1z = fm2 * (lo0 * pL1 - lo1 * pL0);
                 const double q2x = sL1 * pL2 - sL2 * pL1;
                 const double q2y = sL2 * pL0 - sL0 * pL2;
                 const double q2z = sL0 * pL1 - sL1 * pL0;
-                const double ss = nn[0] * sL0 + nn[1] * sL1 + nn[2] * sL2;
-                const double q3x = 3. * ss * (nn[1] * pL2 - nn[2] * pL1);
-                const double q3y = 3. * ss * (nn[2] * pL0 - nn[0] * pL2);
-                const double q3z = 3. * ss * (nn[0] * pL1 - nn[1] * pL0);
+                const double ss = nn0 * sL0 + nn1 * sL1 + nn2 * sL2;
+                const double q3x = 3. * ss * (nn1 * pL2 - nn2 * pL1);
+                const double q3y = 3. * ss * (nn2 * pL0 - nn0 * pL2);
+                const double q3z = 3. * ss * (nn0 * pL1 - nn1 * pL0);
                 dg[0] = kFA * (q1x - q2x + q3x);
                 dg[1] = kFA * (q1y - q2y + q3y);
                 dg[2] = kFA * (q1z - q2z + q3z);
@@ -684,6 +804,148 @@ struct Sys {
             }
         }
     }
+#else
+    // FAST: six contribution columns per planet -- (m/M) a_add (the host's
+    // additional acceleration is minus their sum) and the torque the planet
+    // exerts on the host's spin (tides + flattening + GR).
+    __device__ void additional_effects(const Dev& D, int it, bool evolution_now) {
+        sync();
+        if (is_host) {
+            card[HC_VX] = b.v[0]; card[HC_VY] = b.v[1]; card[HC_VZ] = b.v[2];
+            card[HC_SX] = b.S[0]; card[HC_SY] = b.S[1]; card[HC_SZ] = b.S[2];
+        }
+        if (lane == 0) isc[1] = 0;
+        sync();
+        double hv0 = 0., hv1 = 0., hv2 = 0., vr = 0., nv2 = 0., rs_s = 0., rs_p = 0.;
+        const double x = P(PC_X), y = P(PC_Y), z = P(PC_Z);
+        if (planet()) {
+            hv0 = b.v[0] - card[HC_VX];
+            hv1 = b.v[1] - card[HC_VY];
+            hv2 = b.v[2] - card[HC_VZ];
+            vr = (x * hv0 + y * hv1 + z * hv2) * P(PC_INV_D);
+            nv2 = hv0 * hv0 + hv1 * hv1 + hv2 * hv2;
+            rs_s = x * card[HC_SX] + y * card[HC_SY] + z * card[HC_SZ];
+            rs_p = x * b.S[0] + y * b.S[1] + z * b.S[2];
+        }
+        spin_and_evolving(D, t, evolution_now);
+        zero_inertia_check();
+        if (fatal()) return;
+        if (is_host) {
+            card[HC_SX] = b.S[0]; card[HC_SY] = b.S[1]; card[HC_SZ] = b.S[2];
+            card[HC_NSV2] = b.nsv2; card[HC_R] = b.R; card[HC_MOI] = b.moi;
+            card[HC_SLX] = b.moi * b.S[0]; card[HC_SLY] = b.moi * b.S[1]; card[HC_SLZ] = b.moi * b.S[2];
+        }
+        sync();
+        if (it == 0 && planet()) planet_constants();
+        sync();
+        const double hS0 = card[HC_SX], hS1 = card[HC_SY], hS2 = card[HC_SZ];
+        double aa0 = 0., aa1 = 0., aa2 = 0., dl0 = 0., dl1 = 0., dl2 = 0.;  // own outputs
+        double th0 = 0., th1 = 0., th2 = 0.;                               // torque on the host
+        if (planet()) {
+            const double xd = P(PC_XD), yd = P(PC_YD), zd = P(PC_ZD);
+            const double S0 = b.S[0], S1 = b.S[1], S2 = b.S[2];
+            // r x v_rel (tidal torques, GR orbital angular momentum)
+            const double h0 = y * hv2 - z * hv1;
+            const double h1 = z * hv0 - x * hv2;
+            const double h2 = x * hv1 - y * hv0;
+            if (tides && b.tk == POSI_EFFECT_ORBITING) {
+                const double osd = P(PC_OSD), opd = P(PC_OPD);
+                const double factor1 = vr * P(PC_C13);
+                const double radial = P(PC_CONS) + factor1 * P(PC_T12);
+                const double factor3 = radial + P(PC_OSPD) * vr;
+                const double F0 = factor3 * xd + osd * (hS1 * z - hS2 * y - hv0) + opd * (S1 * z - S2 * y - hv0);
+                const double F1 = factor3 * yd + osd * (hS2 * x - hS0 * z - hv1) + opd * (S2 * x - S0 * z - hv1);
+                const double F2 = factor3 * zd + osd * (hS0 * y - hS1 * x - hv2) + opd * (S0 * y - S1 * x - hv2);
+                aa0 += inv_m * F0; aa1 += inv_m * F1; aa2 += inv_m * F2;
+                const double qp = P(PC_OP) * rs_p, qs = P(PC_OS) * rs_s;
+                const double opdd = P(PC_OPDD), osdd = P(PC_OSDD);
+                dl0 -= opdd * S0 - qp * xd - opd * h0;
+                dl1 -= opdd * S1 - qp * yd - opd * h1;
+                dl2 -= opdd * S2 - qp * zd - opd * h2;
+                th0 -= osdd * hS0 - qs * xd - osd * h0;
+                th1 -= osdd * hS1 - qs * yd - osd * h1;
+                th2 -= osdd * hS2 - qs * zd - osd * h2;
+            }
+            if (flat && b.fk == POSI_EFFECT_ORBITING) {
+                const double cfs = P(PC_CFS), cfp = P(PC_CFP);
+                const double ofs = P(PC_COFS) * rs_s, ofp = P(PC_COFP) * rs_p;
+                const double radial = P(PC_N3D5) * (cfp * b.nsv2 + cfs * card[HC_NSV2]) +
+                                      P(PC_F15D7) * (cfs * rs_s * rs_s + cfp * rs_p * rs_p);
+                const double F0 = radial * x + ofp * S0 + ofs * hS0;
+                const double F1 = radial * y + ofp * S1 + ofs * hS1;
+                const double F2 = radial * z + ofp * S2 + ofs * hS2;
+                aa0 += inv_m * F0; aa1 += inv_m * F1; aa2 += inv_m * F2;
+                dl0 -= ofp * (y * S2 - z * S1);
+                dl1 -= ofp * (z * S0 - x * S2);
+                dl2 -= ofp * (x * S1 - y * S0);
+                th0 -= ofs * (y * hS2 - z * hS1);
+                th1 -= ofs * (z * hS0 - x * hS2);
+                th2 -= ofs * (x * hS1 - y * hS0);
+            }
+            if (gr && b.gk == POSI_EFFECT_ORBITING) {
+                const double vr2 = vr * vr;
+                // first order: ortho / |v| = E v_r
+                const double radial1 = P(PC_A) * (P(PC_B) * nv2 - P(PC_C) - P(PC_DD) * vr2);
+                const double o1 = P(PC_E) * vr;
+                // second order
+                const double nv4 = nv2 * nv2;
+                const double vr4 = vr2 * vr2;
+                const double radial2 = P(PC_A) * (P(PC_T1) + P(PC_K2C) * nv4 + P(PC_K3C) * vr4 - P(PC_K4C) * vr2 * nv2 -
+                                                  P(PC_K5C) * nv2 - P(PC_K6C) * vr2);
+                const double ortho2 = P(PC_A05) * vr * (P(PC_P) * nv2 - P(PC_Q) - P(PC_R3) * vr2);
+                const double rad = radial1 + radial2, ort = o1 + ortho2;
+                double g0 = rad * xd + ort * hv0;
+                double g1 = rad * yd + ort * hv1;
+                double g2 = rad * zd + ort * hv2;
+                // spin-orbit
+                const double sL0 = card[HC_SLX], sL1 = card[HC_SLY], sL2 = card[HC_SLZ];
+                const double pL0 = b.moi * S0, pL1 = b.moi * S1, pL2 = b.moi * S2;
+                const double nn0 = P(PC_NN0), nn1 = P(PC_NN1), nn2 = P(PC_NN2);
+                const double mfM = P(PC_MFM);
+                const double msx = mfM * (pL0 * inv_m - sL0 * inv_hm);
+                const double msy = mfM * (pL1 * inv_m - sL1 * inv_hm);
+                const double msz = mfM * (pL2 * inv_m - sL2 * inv_hm);
+                const double t0 = sL0 + pL0, t1 = sL1 + pL1, t2 = sL2 + pL2;
+                const double e1x = P(PC_C6NN0) * ((nn1 * hv2 - nn2 * hv1) * (2. * t0 + msx));
+                const double e1y = P(PC_C6NN1) * ((nn2 * hv0 - nn0 * hv2) * (2. * t1 + msy));
+                const double e1z = P(PC_C6NN2) * ((nn0 * hv1 - nn1 * hv0) * (2. * t2 + msz));
+                const double e7x = 7. * t0 + 3. * msx, e7y = 7. * t1 + 3. * msy, e7z = 7. * t2 + 3. * msz;
+                const double e3sx = 3. * t0 + msx, e3sy = 3. * t1 + msy, e3sz = 3. * t2 + msz;
+                const double v3 = 3. * vr;
+                g0 += kFA * (e1x - (hv1 * e7z - hv2 * e7y) + v3 * (nn1 * e3sz - nn2 * e3sy));
+                g1 += kFA * (e1y - (hv2 * e7x - hv0 * e7z) + v3 * (nn2 * e3sx - nn0 * e3sz));
+                g2 += kFA * (e1z - (hv0 * e7y - hv1 * e7x) + v3 * (nn0 * e3sy - nn1 * e3sx));
+                aa0 += g0; aa1 += g1; aa2 += g2;
+                // Kidder 1995 eq. 2.4a / 2.4b
+                const double mu = P(PC_MU), fm = P(PC_FM), fm2 = P(PC_FM2);
+                const double lo0 = mu * h0, lo1 = mu * h1, lo2 = mu * h2;
+                const double h2x = pL1 * sL2 - pL2 * sL1;
+                const double h2y = pL2 * sL0 - pL0 * sL2;
+                const double h2z = pL0 * sL1 - pL1 * sL0;
+                const double sp3 = 3. * (nn0 * pL0 + nn1 * pL1 + nn2 * pL2);
+                const double ss3 = 3. * (nn0 * sL0 + nn1 * sL1 + nn2 * sL2);
+                th0 += kFA * (fm * (lo1 * sL2 - lo2 * sL1) - h2x + sp3 * (nn1 * sL2 - nn2 * sL1));
+                th1 += kFA * (fm * (lo2 * sL0 - lo0 * sL2) - h2y + sp3 * (nn2 * sL0 - nn0 * sL2));
+                th2 += kFA * (fm * (lo0 * sL1 - lo1 * sL0) - h2z + sp3 * (nn0 * sL1 - nn1 * sL0));
+                dl0 += kFA * (fm2 * (lo1 * pL2 - lo2 * pL1) + h2x + ss3 * (nn1 * pL2 - nn2 * pL1));
+                dl1 += kFA * (fm2 * (lo2 * pL0 - lo0 * pL2) + h2y + ss3 * (nn2 * pL0 - nn0 * pL2));
+                dl2 += kFA * (fm2 * (lo0 * pL1 - lo1 * pL0) + h2z + ss3 * (nn0 * pL1 - nn1 * pL0));
+            }
+            const double mr = P(PC_MRATIO);
+            X(0, lane) = mr * aa0; X(1, lane) = mr * aa1; X(2, lane) = mr * aa2;
+            X(3, lane) = th0; X(4, lane) = th1; X(5, lane) = th2;
+        }
+        if (tides || flat || gr) colfold(0, 6, nullptr, true, false);
+        if (is_host && (tides || flat || gr)) {
+            aa0 = -sums[0]; aa1 = -sums[1]; aa2 = -sums[2];
+            dl0 = sums[3]; dl1 = sums[4]; dl2 = sums[5];
+        }
+        if (has) {
+            if (spin_on && (tides || flat || gr)) { b.dl[0] = dl0; b.dl[1] = dl1; b.dl[2] = dl2; }
+            b.aa[0] = aa0; b.aa[1] = aa1; b.aa[2] = aa2;
+        }
+    }
+#endif
 
     // ------------------------------------------------------------------
     // src/integrator/whfast.rs:322-466 implicit midpoint with Kahan sums
@@ -695,12 +957,7 @@ struct Sys {
                        card[HC_M] = b.m; card[HC_MG] = b.mg; card[HC_R] = b.R; card[HC_SIG] = b.sig;
                        card[HC_K2] = b.k2; card[HC_K2F] = b.k2f; }
         sync();
-        if (planet()) {
-            pc.x = b.r[0] - card[HC_PX];
-            pc.y = b.r[1] - card[HC_PY];
-            pc.z = b.r[2] - card[HC_PZ];
-            pc.d = sqrt(powi<2>(pc.x) + powi<2>(pc.y) + powi<2>(pc.z));
-        }
+        if (planet()) set_geometry(b.r[0] - card[HC_PX], b.r[1] - card[HC_PY], b.r[2] - card[HC_PZ]);
         double ov[3], oL[3], fv[3], fL[3], dvc[3] = {0., 0., 0.}, dLc[3] = {0., 0., 0.};
 #pragma unroll
         for (int k = 0; k < 3; ++k) { ov[k] = b.v[k]; oL[k] = b.L[k]; fv[k] = ov[k]; fL[k] = oL[k]; }
@@ -768,6 +1025,7 @@ struct Sys {
     // ------------------------------------------------------------------
     // Coordinate transforms (whfast.rs:881-1155)
     // ------------------------------------------------------------------
+#if POSI_EXACT
     // slots: 0 m, 1 mg, 2-4 r, 5-7 v (inertial)
     __device__ void inertial_to_alternative() {
         sync();
@@ -953,7 +1211,6 @@ struct Sys {
             sync();
             double eta = X(0, host);
             double s0 = eta * X(2, host), s1 = eta * X(3, host), s2 = eta * X(4, host);
-            const double m0 = eta;
             double eta_own = 0.;
             int k_own = -1, k = 0;
             for (int j = 0; j < n; ++j) {
@@ -967,7 +1224,6 @@ struct Sys {
                 s0 = s0 * pme + mj * a0; s1 = s1 * pme + mj * a1; s2 = s2 * pme + mj * a2;
                 ++k;
             }
-            (void)m0;
             if (is_host) {
                 const double mtot_i = 1. / eta;
                 b.aacc[0] = s0 * mtot_i; b.aacc[1] = s1 * mtot_i; b.aacc[2] = s2 * mtot_i;
@@ -1006,6 +1262,118 @@ struct Sys {
             sync();
         }
     }
+#else
+    // FAST transforms: prefix / suffix scans over the lanes (bodies in index
+    // order; the host, first in the Jacobi order, is added separately).
+    __device__ void inertial_to_alternative() {
+        if (coords == POSI_JACOBI) {
+            const double own[6] = {planet() ? b.m * b.r[0] : 0., planet() ? b.m * b.r[1] : 0., planet() ? b.m * b.r[2] : 0.,
+                                   planet() ? b.m * b.v[0] : 0., planet() ? b.m * b.v[1] : 0., planet() ? b.m * b.v[2] : 0.};
+            const double hmv[6] = {b.m * b.r[0], b.m * b.r[1], b.m * b.r[2], b.m * b.v[0], b.m * b.v[1], b.m * b.v[2]};
+            double res[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const double hk = gbcast(hmv[k], host);
+                const double incl = gscan(own[k]);
+                const double tot = hk + gbcast(incl, G - 1);
+                if (is_host) res[k] = tot * inv_mtot;
+                else res[k] = (k < 3 ? b.r[k] : b.v[k - 3]) - (hk + (incl - own[k])) * inv_eta_excl;
+            }
+            b.ap[0] = res[0]; b.ap[1] = res[1]; b.ap[2] = res[2];
+            b.av[0] = res[3]; b.av[1] = res[4]; b.av[2] = res[5];
+            b.am = is_host ? 1. / inv_mtot : b.m;
+            b.amg = b.mg;
+        } else {
+            double bar[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) bar[k] = gsum(b.m * (k < 3 ? b.r[k] : b.v[k - 3])) * inv_mtot;
+            const double hr0 = gbcast(b.r[0], host), hr1 = gbcast(b.r[1], host), hr2 = gbcast(b.r[2], host);
+            if (is_host) {
+                b.ap[0] = bar[0]; b.ap[1] = bar[1]; b.ap[2] = bar[2];
+                b.av[0] = bar[3]; b.av[1] = bar[4]; b.av[2] = bar[5];
+            } else {
+                const double f = coords == POSI_WHDS ? whds_f : 1.;
+                b.ap[0] = b.r[0] - hr0; b.ap[1] = b.r[1] - hr1; b.ap[2] = b.r[2] - hr2;
+                b.av[0] = (b.v[0] - bar[3]) * f; b.av[1] = (b.v[1] - bar[4]) * f; b.av[2] = (b.v[2] - bar[5]) * f;
+            }
+            b.am = b.m;
+            b.amg = b.mg;
+        }
+    }
+
+    __device__ void alternative_to_inertial() {
+        if (coords == POSI_JACOBI) {
+            // R_(k-1) = R_total - sum_(i >= k) (m_i / eta_i) r'_i
+            double res[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const double a = k < 3 ? b.ap[k] : b.av[k - 3];
+                const double own = jac_c * a;
+                const double incl = gscan(own);
+                const double tot = gbcast(incl, G - 1);
+                const double R = gbcast(a, host);
+                res[k] = is_host ? R - tot : a + (R - (tot - incl + own));
+            }
+            b.r[0] = res[0]; b.r[1] = res[1]; b.r[2] = res[2];
+            b.v[0] = res[3]; b.v[1] = res[4]; b.v[2] = res[5];
+        } else {
+            const bool whds = coords == POSI_WHDS;
+            const double w = whds ? whds_w : dh_w;
+            double res[6];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double sp = gsum(planet() ? b.ap[k] * b.m : 0.) * inv_mtot;
+                const double sv = gsum(planet() ? b.av[k] * w : 0.);
+                const double R = gbcast(b.ap[k], host), V = gbcast(b.av[k], host);
+                const double rh = R - sp;
+                res[k] = is_host ? rh : b.ap[k] + rh;
+                res[3 + k] = is_host ? V - sv : (whds ? b.av[k] / whds_f : b.av[k]) + V;
+            }
+            b.r[0] = res[0]; b.r[1] = res[1]; b.r[2] = res[2];
+            b.v[0] = res[3]; b.v[1] = res[4]; b.v[2] = res[5];
+        }
+    }
+
+    __device__ void jump_step(double hdt) {
+        if (coords == POSI_JACOBI) return;
+        const bool whds = coords == POSI_WHDS;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double own = planet() ? b.av[k] * (whds ? whds_w : b.m) : 0.;
+            const double p = gsum(own);
+            if (planet()) b.ap[k] += whds ? hdt * (p - own) : hdt * p * inv_hm;
+        }
+    }
+
+    __device__ void interaction_step(double fdt) {
+        if (coords == POSI_JACOBI) {
+            const double hmA[3] = {b.m * b.a[0], b.m * b.a[1], b.m * b.a[2]};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double own = planet() ? b.m * b.a[k] : 0.;
+                const double hk = gbcast(hmA[k], host);
+                const double incl = gscan(own);
+                b.aacc[k] = b.a[k] - (hk + (incl - own)) * inv_eta_excl;
+            }
+            if (planet()) {
+                b.av[0] += fdt * b.aacc[0];
+                b.av[1] += fdt * b.aacc[1];
+                b.av[2] += fdt * b.aacc[2];
+                if (!first_planet) {
+                    const double r2 = b.ap[0] * b.ap[0] + b.ap[1] * b.ap[1] + b.ap[2] * b.ap[2] + 1e-12;
+                    const double ri = rsqrt(r2);
+                    const double prefac = fdt * (ri * ri * ri) * kG * eta_incl;
+                    b.av[0] += prefac * b.ap[0];
+                    b.av[1] += prefac * b.ap[1];
+                    b.av[2] += prefac * b.ap[2];
+                }
+            }
+        } else if (planet()) {
+            const double f = coords == POSI_WHDS ? fdt * whds_f : fdt;
+            b.av[0] += f * b.a[0]; b.av[1] += f * b.a[1]; b.av[2] += f * b.a[2];
+        }
+    }
+#endif
 
     // :835-876
     __device__ static void stiefel_gs3(double beta, double x, double gs[4]) {
@@ -1143,19 +1511,25 @@ struct Sys {
     // :628-672
     __device__ void kepler_steps(double kdt) {
         sync();
+#if POSI_EXACT
         if (has) X(1, lane) = b.amg;
+#endif
         if (is_host) card[HC_MG] = b.mg;
         if (lane == 0) { isc[2] = 0; isc[3] = 0; }
         sync();
         if (planet()) {
             double gm;
             if (coords == POSI_JACOBI) {
+#if POSI_EXACT
                 gm = card[HC_MG];
                 for (int j = 0; j < n; ++j) {
                     if (j == host) continue;
                     gm += X(1, j);
                     if (j == lane) break;
                 }
+#else
+                gm = kep_gm;
+#endif
             } else if (coords == POSI_DEMOCRATIC_HELIOCENTRIC) {
                 gm = card[HC_MG];
             } else {
@@ -1178,7 +1552,11 @@ struct Sys {
     __device__ void gravity(const Dev& D, int ignore_terms) {
         sync();
         if (has) {
+#if POSI_EXACT
             X(0, lane) = b.m;
+#else
+            X(0, lane) = gm_neg;
+#endif
             X(2, lane) = b.r[0]; X(3, lane) = b.r[1]; X(4, lane) = b.r[2];
             X(5, lane) = b.R;
         }
@@ -1205,8 +1583,13 @@ struct Sys {
                      (j == mm && mm == 0 && i == 1) || (j == mm && mm > 0 && i == 0)))
                     continue;
                 if (ignore_terms == 2 && (i == mm || j == mm)) continue;
+#if POSI_EXACT
                 const double distance = sqrt(distance_2);
                 const double prefact = -kG / (distance * distance * distance) * X(0, j);
+#else
+                const double ri = rsqrt(distance_2);
+                const double prefact = (ri * ri * ri) * X(0, j);
+#endif
                 acc0 += prefact * dx;
                 acc1 += prefact * dy;
                 acc2 += prefact * dz;
@@ -1349,12 +1732,7 @@ __global__ void __launch_bounds__(128) additional_effects_kernel(Dev D, double t
                      S.card[HC_M] = S.b.m; S.card[HC_MG] = S.b.mg; S.card[HC_R] = S.b.R; S.card[HC_SIG] = S.b.sig;
                      S.card[HC_K2] = S.b.k2; S.card[HC_K2F] = S.b.k2f; }
     S.sync();
-    if (S.planet()) {
-        S.pc.x = S.b.r[0] - S.card[HC_PX];
-        S.pc.y = S.b.r[1] - S.card[HC_PY];
-        S.pc.z = S.b.r[2] - S.card[HC_PZ];
-        S.pc.d = sqrt(powi<2>(S.pc.x) + powi<2>(S.pc.y) + powi<2>(S.pc.z));
-    }
+    if (S.planet()) S.set_geometry(S.b.r[0] - S.card[HC_PX], S.b.r[1] - S.card[HC_PY], S.b.r[2] - S.card[HC_PZ]);
     S.additional_effects(D, 0, evolution != 0);
     S.store(D);
 }

@@ -60,6 +60,20 @@ def test_plain_path_fast_within_tolerance(tmp_path, name):
     assert max_rel_error(st, ref) <= FAST_TOL_199
 
 
+def test_fast_long_run_within_tolerance():
+    """FAST build after 1e4 steps in 10 launches: <= 1e-9 relative in positions,
+    velocities and angular momenta against the oracle, no frozen system."""
+    ens = E.workload_ensemble8(32, seed=21)
+    b = pg.Batch(ens, mode=pg.FAST)
+    b.initialize_physical_values()
+    b.iterate(10000, 1000)
+    st = b.get_state()
+    assert np.all(st["sys_i64"][:, L.SI_STATUS] & L.SYS_FATAL_MASK == 0)
+    assert np.all(st["sys_i64"][:, L.SI_LAST_MIDPOINT_ITERS] < 10)
+    ref, _, _ = oracle.run(ens, max_steps=10000, init_physical=True, nthreads=8)
+    assert max_rel_error(st, ref) <= 1e-9
+
+
 def test_fast_one_step_relative_error():
     ens = E.workload_ensemble8(64, seed=11)
     b = pg.Batch(ens, mode=pg.FAST)
