@@ -100,7 +100,9 @@ class ClockSampler:
         self.proc = None
         self.lines = []
 
-    def start(self):
+    def start(self, wait_s=15.0):
+        """Start sampling and wait for the first sample, so that nvidia-smi's
+        start-up does not overlap the timed region."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.QUERY}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -109,6 +111,15 @@ class ClockSampler:
             self.t.start()
         except OSError:
             self.proc = None
+            return
+        t0 = time.time()
+        while not self.lines and time.time() - t0 < wait_s and self.proc.poll() is None:
+            time.sleep(0.05)
+        self.skip = len(self.lines)
+
+    def discard(self):
+        """Forget the samples taken so far (before the timed region)."""
+        self.skip = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -123,7 +134,7 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         sm, smax, power, reasons = [], [], [], set()
-        for line in self.lines:
+        for line in self.lines[getattr(self, "skip", 0):]:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -210,6 +221,25 @@ def cpu_leg(ens, steps_hint, seconds, nthreads):
             "flops_per_system_step": flops}
 
 
+def plain_path(mode, steps=400):
+    """Single-system drop-in path (posi_iterate, one kernel launch per step)
+    on the star + 3 planets workload, wall clock."""
+    import posidonius_gb300 as pg
+    from posidonius_gb300 import layout as L
+    one = make_workload("single", 1)
+    case = {k: (v[0] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in one.items()}
+    case["n"] = int(one["sys_i64"][0, L.SI_N])
+    w = pg.WHFast.from_arrays(case, mode=mode)
+    w.initialize_physical_values()
+    w.run(20)
+    t0 = time.perf_counter()
+    done = w.run(steps)
+    dt = time.perf_counter() - t0
+    w.close()
+    return {"value": done / dt, "unit": UNIT, "workload": "single (star + 3 planets)", "steps": done,
+            "note": "posi_iterate, one kernel launch per WHFast step, wall clock"}
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -275,7 +305,8 @@ def main():
         batch.iterate(spl, spl)
         done += spl
     W = done
-    time.sleep(0.5)
+    torch.cuda.synchronize()
+    clocks.discard()
 
     # ---- device-timed region -------------------------------------------------
     barrier(world)
@@ -318,6 +349,9 @@ def main():
     e2e_s = max_over_ranks(e2e_s, world)
     e2e_value = world * batch.n_sys * K / e2e_s
 
+    # ---- the plain path: one system (star + 3 planets), one launch per step ----
+    plain = plain_path(mode)
+
     # ---- accuracy and roofline --------------------------------------------------
     final = batch.get_state()
     st = final["sys_i64"][:, L.SI_STATUS]
@@ -334,6 +368,8 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
                 "note": f"one C-ABI call chain: upload {h2d} B, {K} steps, download {d2h} B"},
         "gpu_launches": int(launches),
+        "plain_path": plain,
+        "batched_over_plain": value / world / plain["value"],
         "clocks": clock_info,
         "systems_frozen": int(np.sum((st & L.SYS_FATAL_MASK) != 0)),
         "midpoint_iterations": {str(k): int(v) for k, v in zip(*np.unique(final["sys_i64"][:, L.SI_LAST_MIDPOINT_ITERS],

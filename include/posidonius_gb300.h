@@ -130,6 +130,13 @@ enum posi_body_f64_field {
     POSI_BF_DLX, POSI_BF_DLY, POSI_BF_DLZ,       /* dangular_momentum_dt */
     POSI_BF_DENERGY_DT,                          /* tides denergy_dt (history output) */
     POSI_BF_LAG_ANGLE,                           /* tides lag_angle (history output) */
+    /* tidal internals of the last evaluation (TidesParticleInternalParameters and
+     * coordinates, src/effects/tides/common.rs:35-79), read by the historic
+     * snapshot's dE/dt (src/effects/tides/common.rs:263-279) */
+    POSI_BF_TD_DIST, POSI_BF_TD_VR, POSI_BF_TD_ORTHO, POSI_BF_TD_DPM,
+    POSI_BF_TD_PX, POSI_BF_TD_PY, POSI_BF_TD_PZ,
+    POSI_BF_TD_VX, POSI_BF_TD_VY, POSI_BF_TD_VZ,
+    POSI_BF_TD_LX, POSI_BF_TD_LY, POSI_BF_TD_LZ,
     POSI_BF_COUNT
 };
 
@@ -145,7 +152,8 @@ enum posi_mode { POSI_MODE_EXACT = 0, POSI_MODE_FAST = 1 };
 enum posi_mapping {
     POSI_MAP_AUTO = 0,           /* autotuned per body-count bucket */
     POSI_MAP_THREAD = 1,         /* one thread per system */
-    POSI_MAP_LANES4 = 4,         /* 4 lanes per system, lane-strided bodies */
+    POSI_MAP_LANES2 = 2,         /* 2 lanes per system (one body per lane) */
+    POSI_MAP_LANES4 = 4,         /* 4 lanes per system */
     POSI_MAP_LANES8 = 8,
     POSI_MAP_LANES16 = 16,
     POSI_MAP_WARP = 32           /* one warp per system */
@@ -225,6 +233,22 @@ int posi_get_state(const posi_handle* h, int64_t* sys_i64, double* sys_f64,
                    int64_t* body_i64, double* body_f64, double* roche);
 int posi_set_state(posi_handle* h, const int64_t* sys_i64, const double* sys_f64,
                    const int64_t* body_i64, const double* body_f64);
+
+/* src/integrator/output.rs:63-89 get_universe_history_writer: open the
+ * historic-snapshot file (created if absent), fail with POSI_ERR_STATE when it
+ * is shorter than expected_bytes (n_historic_snapshots * 156 * n_particles),
+ * and truncate it to expected_bytes.  From then on posi_iterate appends one
+ * 156-byte bincode record per body at every historic trigger
+ * (src/integrator/output.rs:91-135). */
+int posi_open_history(posi_handle* h, const char* path, int64_t expected_bytes);
+int posi_close_history(posi_handle* h);
+
+/* src/integrator/whfast.rs:307-316 + src/integrator/output.rs:28-54
+ * write_recovery_snapshot: set last_recovery_snapshot_time, flush the history,
+ * rename an existing file to <stem>.<YYYYMMDD>T<AM|PM>.bin and write the
+ * WHFast case document with the current state (JSON paths; the handle must
+ * come from posi_universe_from_json). */
+int posi_write_recovery_snapshot(posi_handle* h, const char* path);
 
 /* ---- batched ensembles (many independent systems, one persistent kernel) -- */
 

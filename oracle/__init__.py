@@ -45,6 +45,8 @@ def _lib(flops=False):
                                    f64p, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                    i64p, i64p]
         lib.oracle_run.restype = ctypes.c_int
+        lib.oracle_history.argtypes = [f64p, ctypes.c_int64, i64p]
+        lib.oracle_history.restype = None
         lib.oracle_constant.argtypes = [ctypes.c_int]
         lib.oracle_constant.restype = ctypes.c_double
         if flops:
@@ -63,6 +65,29 @@ def as_ensemble(case):
         return case
     from .case_json import stack
     return stack([case])
+
+
+def run_with_history(case, max_steps, init_physical=False, max_records=100000):
+    """ITERATE one system single-threaded, collecting its historic records.
+
+    Returns (ensemble, steps_done, result, records) with records an array of
+    shape (n_triggers, n_bodies, 20) in the kernel's record layout.
+    """
+    lib = _lib()
+    ens = as_ensemble(case)
+    if ens["n_sys"] != 1:
+        raise ValueError("run_with_history takes one system")
+    n = int(ens["sys_i64"][0, L.SI_N])
+    buf = np.zeros((max_records, 20), dtype=np.float64)
+    length = np.zeros(1, dtype=np.int64)
+    lib.oracle_history(_p(buf, ctypes.c_double), max_records, None)
+    try:
+        out = run(ens, max_steps=max_steps, init_physical=init_physical, nthreads=1)
+        lib.oracle_history(_p(buf, ctypes.c_double), max_records, _p(length, ctypes.c_int64))
+    finally:
+        lib.oracle_history(None, 0, None)
+    k = int(length[0])
+    return out + (buf[:k].reshape(k // n, n, 20),)
 
 
 def run(ens, op=ITERATE, max_steps=0, init_physical=False, arg=0, t_arg=0.0, nthreads=1, flops=False):

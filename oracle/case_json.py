@@ -175,8 +175,17 @@ def load_case(path_or_dict):
         F[L.BF_SIGMA] = p["tides"]["parameters"]["internal"]["scaled_dissipation_factor"]
         F[L.BF_K2] = tparams["love_number"] if tparams else 0.0
         F[L.BF_K2F] = fparams["love_number"] if fparams else 0.0
-        F[L.BF_DENERGY_DT] = p["tides"]["parameters"]["internal"]["denergy_dt"]
-        F[L.BF_LAG_ANGLE] = p["tides"]["parameters"]["internal"]["lag_angle"]
+        tint = p["tides"]["parameters"]["internal"]
+        F[L.BF_DENERGY_DT] = tint["denergy_dt"]
+        F[L.BF_LAG_ANGLE] = tint["lag_angle"]
+        F[L.BF_TD_DIST] = tint["distance"]
+        F[L.BF_TD_VR] = tint["radial_velocity"]
+        F[L.BF_TD_ORTHO] = tint["orthogonal_component_of_the_tidal_force_due_to_planetary_tide"]
+        F[L.BF_TD_DPM] = tint["radial_component_of_the_tidal_force_dissipative_part_when_star_as_point_mass"]
+        for k, key in enumerate(("x", "y", "z")):
+            F[L.BF_TD_PX + k] = p["tides"]["coordinates"]["position"][key]
+            F[L.BF_TD_VX + k] = p["tides"]["coordinates"]["velocity"][key]
+            F[L.BF_TD_LX + k] = p["tides"]["parameters"]["output"]["dangular_momentum_dt"][key]
     # calculate_roche_radiuses fills the first n*n entries in rows of n
     # (src/particles/universe.rs:177-196)
     rr = u["roche_radiuses"]

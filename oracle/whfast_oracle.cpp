@@ -1452,8 +1452,31 @@ static int initialize_physical_values(Sim& s) {
     return POSI_OK;
 }
 
-// :235-305 (the historic snapshot itself is not written; its side effects on
-// the state -- the evolution update and the spin refresh -- are reproduced)
+// Historic records (src/integrator/output.rs:91-135), as 20 doubles per body:
+// t, dt, id, position, spin, velocity, mass, radius, rg2, love number,
+// scaled dissipation factor, lag angle, denergy_dt, migration timescale (the
+// disk is not on this path: 0).  Collected only when a buffer is attached.
+thread_local double* g_hist = nullptr;
+thread_local int64_t g_hist_cap = 0, g_hist_len = 0;
+
+static void write_historic_snapshot(const Sim& s) {
+    if (!g_hist) return;
+    for (int i = 0; i < s.n; ++i) {
+        if (g_hist_len >= g_hist_cap) return;
+        const Particle& q = s.p[i];
+        double* R = g_hist + g_hist_len * 20;
+        const real rec[20] = {s.t, s.dt, real((double)q.id), q.r.x, q.r.y, q.r.z, q.spin.x, q.spin.y, q.spin.z,
+                              q.v.x, q.v.y, q.v.z, q.mass, q.radius, q.rg2,
+                              q.tides.kind != POSI_EFFECT_DISABLED ? q.tides.love_number : real(0.),
+                              q.tides.scaled_dissipation_factor, q.tides.lag_angle, q.tides.denergy_dt, real(0.)};
+        for (int k = 0; k < 20; ++k) R[k] = static_cast<double>(rec[k]);
+        ++g_hist_len;
+    }
+}
+
+// :235-305 (the historic snapshot goes to the attached record buffer; its
+// side effects on the state -- the evolution update and the spin refresh --
+// are reproduced)
 static int iterate(Sim& s, bool* recovery_trigger) {
     bool first = s.last_hist < real(0.);
     bool hist_trig = s.last_hist + s.hist_period <= s.t;
@@ -1463,6 +1486,7 @@ static int iterate(Sim& s, bool* recovery_trigger) {
         calculate_spin_and_evolving_quantities(s, s.t, true);
         if (s.fatal()) return POSI_ERR_PHYSICS;
         if (s.tides) tides_denergy_dt(s);
+        write_historic_snapshot(s);
         if (!first) s.last_hist += s.hist_period; else s.last_hist = 0.;
         s.n_hist += 1;
     }
@@ -1549,6 +1573,13 @@ static void load(Sim& s, int64_t nmax, const int64_t* si, const double* sf, cons
         q.tides.love_number = F[POSI_BF_K2];
         q.tides.denergy_dt = F[POSI_BF_DENERGY_DT];
         q.tides.lag_angle = F[POSI_BF_LAG_ANGLE];
+        q.tides.distance = F[POSI_BF_TD_DIST];
+        q.tides.radial_velocity = F[POSI_BF_TD_VR];
+        q.tides.ortho_planet = F[POSI_BF_TD_ORTHO];
+        q.tides.radial_diss_pm = F[POSI_BF_TD_DPM];
+        q.tides.pos = V3{F[POSI_BF_TD_PX], F[POSI_BF_TD_PY], F[POSI_BF_TD_PZ]};
+        q.tides.vel = V3{F[POSI_BF_TD_VX], F[POSI_BF_TD_VY], F[POSI_BF_TD_VZ]};
+        q.tides.out_dldt = V3{F[POSI_BF_TD_LX], F[POSI_BF_TD_LY], F[POSI_BF_TD_LZ]};
         q.flat.kind = (int)I[POSI_BI_FLAT_KIND];
         q.flat.love_number = F[POSI_BF_K2F];
         q.gr.kind = (int)I[POSI_BI_GR_KIND];
@@ -1598,6 +1629,13 @@ static void store(const Sim& s, int64_t nmax, int64_t* si, double* sf, int64_t* 
         F[POSI_BF_DLX] = dv(q.dLdt.x); F[POSI_BF_DLY] = dv(q.dLdt.y); F[POSI_BF_DLZ] = dv(q.dLdt.z);
         F[POSI_BF_DENERGY_DT] = dv(q.tides.denergy_dt);
         F[POSI_BF_LAG_ANGLE] = dv(q.tides.lag_angle);
+        F[POSI_BF_TD_DIST] = dv(q.tides.distance);
+        F[POSI_BF_TD_VR] = dv(q.tides.radial_velocity);
+        F[POSI_BF_TD_ORTHO] = dv(q.tides.ortho_planet);
+        F[POSI_BF_TD_DPM] = dv(q.tides.radial_diss_pm);
+        F[POSI_BF_TD_PX] = dv(q.tides.pos.x); F[POSI_BF_TD_PY] = dv(q.tides.pos.y); F[POSI_BF_TD_PZ] = dv(q.tides.pos.z);
+        F[POSI_BF_TD_VX] = dv(q.tides.vel.x); F[POSI_BF_TD_VY] = dv(q.tides.vel.y); F[POSI_BF_TD_VZ] = dv(q.tides.vel.z);
+        F[POSI_BF_TD_LX] = dv(q.tides.out_dldt.x); F[POSI_BF_TD_LY] = dv(q.tides.out_dldt.y); F[POSI_BF_TD_LZ] = dv(q.tides.out_dldt.z);
         I[POSI_BI_EVO_LEFT] = s.ev[b].left_index;
     }
     if (roche) {
@@ -1671,6 +1709,18 @@ int oracle_run(int op, int64_t n_sys, int64_t nmax, int64_t* sys_i64, double* sy
         for (auto& t : th) t.join();
     }
     return 0;
+}
+
+// Attach (buf != NULL) or detach the historic-record buffer of the calling
+// thread: room for `capacity` body records of 20 doubles; *len receives the
+// count written so far on each call with len != NULL.
+void oracle_history(double* buf, int64_t capacity, int64_t* len) {
+    if (len) *len = orc::g_hist_len;
+    if (buf != orc::g_hist || !buf) {
+        orc::g_hist = buf;
+        orc::g_hist_cap = buf ? capacity : 0;
+        orc::g_hist_len = 0;
+    }
 }
 
 #ifdef ORACLE_COUNT_FLOPS

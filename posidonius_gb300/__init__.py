@@ -27,6 +27,9 @@ __all__ = ["WHFast", "Batch", "restore_snapshot", "read_case", "layout", "PosiEr
 EXACT = L.MODE_EXACT
 FAST = L.MODE_FAST
 
+# output.rs:56-61 n_bytes_per_particle_in_historic_snapshot
+HISTORY_BYTES_PER_PARTICLE = 8 + 8 + 4 + 8 * (20 - 3)
+
 
 def read_case(path):
     """Parse a WHFast JSON case into the flat layout (C++ reader, no GPU)."""
@@ -139,6 +142,23 @@ class WHFast:
             if st == L.COMPLETED or done == 0:
                 break
         return total
+
+    # Snapshot output (src/integrator/output.rs)
+    def open_history(self, path, expected_bytes=None):
+        """get_universe_history_writer (output.rs:63-89): from now on every
+        historic trigger appends its record to `path`.  expected_bytes
+        defaults to n_historic_snapshots x 156 x n_particles."""
+        if expected_bytes is None:
+            expected_bytes = self.get_n_historic_snapshots() * HISTORY_BYTES_PER_PARTICLE * self.get_n_particles()
+        check(lib().posi_open_history(self._h, str(path).encode(), int(expected_bytes)))
+
+    def close_history(self):
+        check(lib().posi_close_history(self._h))
+
+    def write_recovery_snapshot(self, path):
+        """WHFast::write_recovery_snapshot (whfast.rs:307-316): JSON snapshot
+        of the current state; an existing file is kept as a dated backup."""
+        check(lib().posi_write_recovery_snapshot(self._h, str(path).encode()))
 
     # Universe methods (src/particles/universe.rs)
     def gravity_calculate_acceleration(self, ignore_terms):

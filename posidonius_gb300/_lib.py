@@ -50,6 +50,9 @@ SIGNATURES = {
     "posi_batch_mapping_for": (ctypes.c_int, [_vp, ctypes.c_int64]),
     "posi_batch_last_timing": (ctypes.c_int, [_vp, _f64p, _i64p]),
     "posi_fp64_probe": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p, _f64p]),
+    "posi_open_history": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int64]),
+    "posi_close_history": (ctypes.c_int, [_vp]),
+    "posi_write_recovery_snapshot": (ctypes.c_int, [_vp, ctypes.c_char_p]),
 }
 
 _lib = None

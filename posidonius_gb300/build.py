@@ -1,7 +1,7 @@
 """Build recipe of the CUDA library (sm_103a, in-tree).
 
 Produces ``posidonius_gb300/_lib/libposidonius_gb300.so`` from the sources in
-``posidonius_gb300/csrc``.  The two kernel translation units are compiled
+``posidonius_gb300/csrc`` and the ``posidonius`` command beside it.  The two kernel translation units are compiled
 with different contraction settings: ``kernels_exact.cu`` with
 ``-fmad=false`` (the reference's operation order, no FMA) and
 ``kernels_fast.cu`` with ``-fmad=true``.
@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libposidonius_gb300.so")
+CLI = os.path.join(OUT_DIR, "posidonius")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 
@@ -25,6 +26,7 @@ UNITS = [
     ("posi_host.cu", ["-fmad=false"]),
     ("case_reader.cpp", ["-x", "cu", "-fmad=false"]),
     ("diagnostics.cu", ["-fmad=true"]),
+    ("snapshot.cpp", ["-x", "cu", "-fmad=false"]),
 ]
 
 
@@ -69,6 +71,11 @@ def build(force=False, verbose=False, extra_flags=()):
     if jobs or not os.path.exists(LIB):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         run(cmd)
+    # the `posidonius` command, linked against the library beside it
+    cli_src = os.path.join(CSRC, "posi_cli.cpp")
+    if force or _sources_newer(CLI, [cli_src, LIB] + headers):
+        run([nvcc()] + ARCH + ["-O2", "-std=c++17", "-x", "cu", cli_src, "-o", CLI, "-L" + OUT_DIR,
+                               "-lposidonius_gb300", "-lcudart", "-Xlinker", "-rpath,$ORIGIN"])
     return LIB
 
 

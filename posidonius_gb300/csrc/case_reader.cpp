@@ -1,6 +1,7 @@
 // case_reader.cpp -- see case_reader.hpp.
 #include "case_reader.hpp"
 
+#include <cmath>
 #include <cstring>
 
 namespace posi {
@@ -25,6 +26,7 @@ const json::Value* req(Ctx& c, const json::Value* v, const char* key) {
 double num(Ctx& c, const json::Value* v, const char* key) {
     const json::Value* r = req(c, v, key);
     if (!r) return 0.;
+    if (r->kind == json::Value::Null) return std::nan("");  // serde_json writes non-finite floats as null
     if (!r->is_number()) { c.fail(POSI_ERR_PARSE, std::string("field '") + key + "' is not a number"); return 0.; }
     return r->num();
 }
@@ -271,6 +273,16 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
         F[POSI_BF_SIGMA] = num(c, tint, "scaled_dissipation_factor");
         F[POSI_BF_DENERGY_DT] = num(c, tint, "denergy_dt");
         F[POSI_BF_LAG_ANGLE] = num(c, tint, "lag_angle");
+        F[POSI_BF_TD_DIST] = num(c, tint, "distance");
+        F[POSI_BF_TD_VR] = num(c, tint, "radial_velocity");
+        F[POSI_BF_TD_ORTHO] = num(c, tint, "orthogonal_component_of_the_tidal_force_due_to_planetary_tide");
+        F[POSI_BF_TD_DPM] = num(c, tint, "radial_component_of_the_tidal_force_dissipative_part_when_star_as_point_mass");
+        {
+            const json::Value* tco = req(c, tides_v, "coordinates");
+            axes(c, tco, "position", &F[POSI_BF_TD_PX]);
+            axes(c, tco, "velocity", &F[POSI_BF_TD_VX]);
+            axes(c, tout, "dangular_momentum_dt", &F[POSI_BF_TD_LX]);
+        }
         F[POSI_BF_K2] = tparams ? num(c, tparams, "love_number") : 0.;
         F[POSI_BF_K2F] = fparams ? num(c, fparams, "love_number") : 0.;
         if (c.code != POSI_OK) { err = c.err; return c.code; }

@@ -17,13 +17,14 @@ struct DevView {
     const int32_t* list;
     int32_t n_list;
     int32_t* step_flags;
+    double* hist;
 };
 
 enum KernelOp { OP_STEPS = 0, OP_INIT = 1, OP_GRAVITY = 2, OP_EFFECTS = 3 };
 
 struct LaunchArgs {
     int op;
-    int G;                 // lanes per system: 4, 8, 16 or 32
+    int G;                 // lanes per system: 2, 4, 8, 16 or 32
     int64_t n_steps;       // OP_STEPS
     int ignore_terms;      // OP_GRAVITY
     double t_eval;         // OP_EFFECTS
@@ -40,6 +41,7 @@ cudaError_t prepare_fast();
 // Lanes per system used for a system of n bodies (0 when n is out of range).
 inline int group_size_for(int64_t n) {
     if (n < 1) return 0;
+    if (n <= 2) return 2;
     if (n <= 4) return 4;
     if (n <= 8) return 8;
     if (n <= 16) return 16;

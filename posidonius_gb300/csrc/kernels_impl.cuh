@@ -14,6 +14,7 @@ static cudaError_t launch_g(const posi::DevView& v, const posi::LaunchArgs& a, c
     d.bf = v.bf; d.bi = v.bi; d.sf = v.sf; d.si = v.si;
     d.roche = v.roche; d.tables = v.tables; d.list = v.list; d.n_list = v.n_list;
     d.step_flags = v.step_flags;
+    d.hist = v.hist;
     const int threads = posi::kBlockThreads;
     const int groups_per_block = threads / G;
     const int blocks = (int)((v.n_list + groups_per_block - 1) / groups_per_block);
@@ -52,6 +53,7 @@ static cudaError_t prepare_g() {
 // stream capture.
 static cudaError_t prepare_all() {
     cudaError_t e;
+    if ((e = prepare_g<2>()) != cudaSuccess) return e;
     if ((e = prepare_g<4>()) != cudaSuccess) return e;
     if ((e = prepare_g<8>()) != cudaSuccess) return e;
     if ((e = prepare_g<16>()) != cudaSuccess) return e;
@@ -60,6 +62,7 @@ static cudaError_t prepare_all() {
 
 static cudaError_t launch_any(const posi::DevView& v, const posi::LaunchArgs& a, cudaStream_t stream) {
     switch (a.G) {
+        case 2: return launch_g<2>(v, a, stream);
         case 4: return launch_g<4>(v, a, stream);
         case 8: return launch_g<8>(v, a, stream);
         case 16: return launch_g<16>(v, a, stream);

@@ -24,6 +24,10 @@
 #include "case_reader.hpp"
 #include "json.hpp"
 #include "kernels.h"
+#include "snapshot.hpp"
+
+#include <ctime>
+#include <unistd.h>
 
 using posi::DevView;
 using posi::LaunchArgs;
@@ -86,6 +90,7 @@ struct posi_batch {
     double* d_tables = nullptr;
     int32_t* d_list = nullptr;
     int32_t* d_flags = nullptr;
+    double* d_hist = nullptr;  // historic records (attached by the snapshot writer)
     void* d_stage = nullptr;  // AoS staging buffer
     size_t stage_bytes = 0;
     int64_t n_tables = 0;
@@ -106,6 +111,7 @@ struct posi_batch {
         v.roche = d_roche; v.tables = d_tables;
         v.list = d_list + list_offset; v.n_list = count;
         v.step_flags = d_flags;
+        v.hist = d_hist;
         return v;
     }
     cudaError_t launch(const Bucket& bk, const LaunchArgs& a0) const {
@@ -121,6 +127,10 @@ struct posi_handle {
     // host mirror of the system scalars (the device copy is authoritative)
     std::vector<int64_t> si;
     std::vector<double> sf;
+    // the case document the run started from (recovery snapshots rewrite it)
+    std::shared_ptr<posi::json::Value> doc;
+    // historic snapshot file (src/integrator/output.rs:57-89)
+    std::FILE* hist = nullptr;
 };
 
 namespace {
@@ -131,6 +141,7 @@ void free_batch(posi_batch* b) {
     cudaFree(b->d_bf); cudaFree(b->d_bi); cudaFree(b->d_sf); cudaFree(b->d_si);
     cudaFree(b->d_roche); cudaFree(b->d_tables); cudaFree(b->d_list); cudaFree(b->d_flags);
     cudaFree(b->d_stage);
+    cudaFree(b->d_hist);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -173,7 +184,7 @@ int build_buckets(posi_batch* b, const int64_t* sys_i64) {
         const int64_t n = sys_i64[s * POSI_SI_COUNT + POSI_SI_N];
         b->n_of[s] = n;
         int G = posi::group_size_for(n);
-        if (b->mapping >= POSI_MAP_LANES4 && b->mapping <= POSI_MAP_WARP && b->mapping >= G) G = b->mapping;
+        if (b->mapping >= POSI_MAP_LANES2 && b->mapping <= POSI_MAP_WARP && b->mapping >= G) G = b->mapping;
         by_g[G].push_back((int32_t)s);
         b->mapping_of_n[n] = G;
     }
@@ -374,7 +385,7 @@ int posi_device_count(void) {
 }  // extern "C"
 
 namespace {
-int load_case_file(const char* path, posi::FlatSystem& fs) {
+int load_case_file(const char* path, posi::FlatSystem& fs, posi::json::Value* doc_out = nullptr) {
     if (!path) return POSI_ERR_ARG;
     std::ifstream f(path, std::ios::binary);
     if (!f) {
@@ -393,6 +404,7 @@ int load_case_file(const char* path, posi::FlatSystem& fs) {
     }
     int rc = posi::read_case(doc, fs, err);
     if (rc != POSI_OK) g_last_error = err;
+    if (rc == POSI_OK && doc_out) *doc_out = std::move(doc);
     return rc;
 }
 }  // namespace
@@ -417,7 +429,8 @@ int posi_read_case(const char* path, int64_t* n, int64_t* n_tables, int64_t* sys
 
 posi_handle* posi_universe_from_json(const char* path, int mode, int* status) {
     posi::FlatSystem fs;
-    int rc = load_case_file(path, fs);
+    posi::json::Value doc;
+    int rc = load_case_file(path, fs, &doc);
     if (rc != POSI_OK) {
         if (status) *status = rc;
         return nullptr;
@@ -426,7 +439,9 @@ posi_handle* posi_universe_from_json(const char* path, int mode, int* status) {
                                  fs.tables.empty() ? nullptr : fs.tables.data(), (int64_t)fs.tables.size(),
                                  fs.roche.data(), mode, POSI_MAP_AUTO, status);
     if (!b) return nullptr;
-    return make_handle(b, fs.si.data(), fs.sf.data());
+    posi_handle* h = make_handle(b, fs.si.data(), fs.sf.data());
+    h->doc = std::make_shared<posi::json::Value>(std::move(doc));
+    return h;
 }
 
 posi_handle* posi_universe_from_arrays(const int64_t* sys_i64, const double* sys_f64, const int64_t* body_i64,
@@ -442,6 +457,7 @@ posi_handle* posi_universe_from_arrays(const int64_t* sys_i64, const double* sys
 
 void posi_destroy(posi_handle* h) {
     if (!h) return;
+    if (h->hist) std::fclose(h->hist);
     free_batch(h->b);
     delete h;
 }
@@ -499,16 +515,37 @@ int posi_initialize_physical_values(posi_handle* h) {
     return posi_batch_initialize_physical_values(h->b) == POSI_OK ? refresh_mirror(h) : POSI_ERR_CUDA;
 }
 
+namespace {
+// The reference's panic text for a frozen system (src/particles/universe.rs:224-237,
+// src/particles/common.rs:5-7, src/integrator/whfast.rs:792-805).
+std::string fatal_message(const int64_t* si) {
+    const int64_t pair = si[POSI_SI_FAIL_PAIR], i = pair / 1024, j = pair % 1024;
+    switch (si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) {
+        case POSI_SYS_ROCHE:
+            return "Particle " + std::to_string(i) + " was destroyed by particle " + std::to_string(j) +
+                   " due to close encounter!";
+        case POSI_SYS_COLLISION:
+            return "Collision between particle " + std::to_string(i) + " and " + std::to_string(j) + "!";
+        case POSI_SYS_EJECTED: return "Particle " + std::to_string(j) + " has been ejected!";
+        case POSI_SYS_ZERO_INERTIA: return "Moment of inertia is zero";
+        case POSI_SYS_BISECTION_LIMIT: return "Kepler solver bisection did not converge";
+        default: return "fatal system status " + std::to_string(si[POSI_SI_STATUS]);
+    }
+}
+}  // namespace
+
 int posi_iterate(posi_handle* h, int64_t n_steps, int64_t* steps_done, int* recovery_trigger) {
     if (!h || n_steps < 0) return POSI_ERR_ARG;
     if (steps_done) *steps_done = 0;
     if (recovery_trigger) *recovery_trigger = 0;
     if (h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) {
-        return (h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) == POSI_SYS_COMPLETED ? POSI_COMPLETED : POSI_ERR_PHYSICS;
+        if ((h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) == POSI_SYS_COMPLETED) return POSI_COMPLETED;
+        g_last_error = fatal_message(h->si.data());
+        return POSI_ERR_PHYSICS;
     }
     // Predict, with the kernel's own time arithmetic, how many steps run before
     // a step reports a recovery trigger or completes the simulation; the plain
-    // path then launches exactly that many one-step kernels.
+    // path then runs exactly that many steps.
     double t = h->sf[POSI_SF_TIME], last_hist = h->sf[POSI_SF_LAST_HIST];
     const double dt = h->sf[POSI_SF_DT], limit = h->sf[POSI_SF_TIME_LIMIT];
     const double hp = h->sf[POSI_SF_HIST_PERIOD], lr = h->sf[POSI_SF_LAST_REC], rp = h->sf[POSI_SF_REC_PERIOD];
@@ -524,12 +561,57 @@ int posi_iterate(posi_handle* h, int64_t n_steps, int64_t* steps_done, int* reco
         if (t + dt > limit) break;
         if (first || rt) { rec = true; break; }
     }
+    // The k steps run as few multi-step launches: one when no history file is
+    // attached, else one per historic record (a launch opens with the
+    // trigger step, whose record the kernel leaves in the device buffer; the
+    // buffer is filled with NaN first, so a system that stopped earlier
+    // leaves it untouched and nothing is appended).
     LaunchArgs a{};
     a.op = posi::OP_STEPS;
-    a.n_steps = 1;
     posi_batch* b = h->b;
-    for (int64_t i = 0; i < k; ++i) {
+    const int64_t n = h->si[POSI_SI_N];
+    std::vector<double> record;
+    std::vector<unsigned char> bytes;
+    if (h->hist) record.resize((size_t)n * posi::kHistoryFields);
+    auto run_segment = [&](int64_t len, bool with_record) -> int {
+        if (len == 0) return POSI_OK;
+        if (with_record) CK(cudaMemsetAsync(b->d_hist, 0xff, record.size() * sizeof(double), b->stream));
+        a.n_steps = len;
         for (const Bucket& bk : b->buckets) CK(b->launch(bk, a));
+        if (!with_record) return POSI_OK;
+        CK(cudaMemcpyAsync(record.data(), b->d_hist, record.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                           b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+        if (std::isnan(record[0])) return POSI_OK;
+        bytes.clear();
+        posi::encode_history_record(record.data(), n, bytes);
+        if (std::fwrite(bytes.data(), 1, bytes.size(), h->hist) != bytes.size()) {
+            g_last_error = "cannot write the history file";
+            return POSI_ERR_IO;
+        }
+        return POSI_OK;
+    };
+    if (!h->hist) {
+        int rc = run_segment(k, false);
+        if (rc != POSI_OK) return rc;
+    } else {
+        double lh = h->sf[POSI_SF_LAST_HIST], tt = h->sf[POSI_SF_TIME];
+        int64_t seg = 0;
+        bool seg_record = false;
+        for (int64_t i = 0; i < k; ++i) {
+            const bool trig = lh < 0. || lh + hp <= tt;
+            if (trig) {
+                lh = lh < 0. ? 0. : lh + hp;
+                int rc = run_segment(seg, seg_record);
+                if (rc != POSI_OK) return rc;
+                seg = 0;
+                seg_record = true;
+            }
+            tt += dt;
+            ++seg;
+        }
+        int rc = run_segment(seg, seg_record);
+        if (rc != POSI_OK) return rc;
     }
     CK(cudaStreamSynchronize(b->stream));
     const int64_t it0 = h->si[POSI_SI_ITERATION];
@@ -538,7 +620,10 @@ int posi_iterate(posi_handle* h, int64_t n_steps, int64_t* steps_done, int* reco
     if (steps_done) *steps_done = h->si[POSI_SI_ITERATION] - it0;
     const int64_t fatal = h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK;
     if (fatal == POSI_SYS_COMPLETED) return POSI_COMPLETED;
-    if (fatal) return POSI_ERR_PHYSICS;
+    if (fatal) {
+        g_last_error = fatal_message(h->si.data());
+        return POSI_ERR_PHYSICS;
+    }
     if (recovery_trigger) *recovery_trigger = rec ? 1 : 0;
     return POSI_OK;
 }
@@ -587,6 +672,90 @@ int posi_set_state(posi_handle* h, const int64_t* sys_i64, const double* sys_f64
     int rc = batch_set(h->b, sys_i64, sys_f64, body_i64, body_f64);
     if (rc != POSI_OK) return rc;
     return refresh_mirror(h);
+}
+
+// src/integrator/output.rs:63-89 get_universe_history_writer: open (create or
+// append), refuse a file shorter than the history the snapshot accounts for,
+// and drop anything beyond it.
+int posi_open_history(posi_handle* h, const char* path, int64_t expected_bytes) {
+    if (!h || !path || expected_bytes < 0) return POSI_ERR_ARG;
+    if (h->hist) { std::fclose(h->hist); h->hist = nullptr; }
+    std::FILE* f = std::fopen(path, "ab");
+    if (!f) { g_last_error = std::string("cannot open ") + path; return POSI_ERR_IO; }
+    std::fseek(f, 0, SEEK_END);
+    const long size = std::ftell(f);
+    std::fclose(f);
+    if (size < expected_bytes) {
+        g_last_error = "historic snapshots do not contain all the expected history (" + std::to_string(size) +
+                       " bytes) as indicated by the recovery snapshot (" + std::to_string(expected_bytes) + " bytes)";
+        return POSI_ERR_STATE;
+    }
+    if (truncate(path, (off_t)expected_bytes) != 0) { g_last_error = "cannot truncate the history file"; return POSI_ERR_IO; }
+    h->hist = std::fopen(path, "ab");
+    if (!h->hist) { g_last_error = std::string("cannot open ") + path; return POSI_ERR_IO; }
+    posi_batch* b = h->b;
+    if (!b->d_hist) CK(cudaMalloc(&b->d_hist, (size_t)b->stride * posi::kHistoryFields * sizeof(double)));
+    return POSI_OK;
+}
+
+int posi_close_history(posi_handle* h) {
+    if (!h) return POSI_ERR_ARG;
+    if (h->hist) {
+        std::fclose(h->hist);
+        h->hist = nullptr;
+    }
+    return POSI_OK;
+}
+
+// src/integrator/whfast.rs:307-316 + src/integrator/output.rs:28-54
+int posi_write_recovery_snapshot(posi_handle* h, const char* path) {
+    if (!h || !path) return POSI_ERR_ARG;
+    if (!h->doc) {
+        g_last_error = "recovery snapshots need a handle opened from a JSON case";
+        return POSI_ERR_UNSUPPORTED;
+    }
+    std::string p(path);
+    const size_t dot = p.find_last_of('.');
+    const size_t slash = p.find_last_of('/');
+    const bool has_ext = dot != std::string::npos && (slash == std::string::npos || dot > slash);
+    const std::string ext = has_ext ? p.substr(dot + 1) : "";
+    if (ext != "json") {
+        g_last_error = "only JSON recovery snapshots are written (bincode snapshots are not supported)";
+        return POSI_ERR_UNSUPPORTED;
+    }
+    h->sf[POSI_SF_LAST_REC] = h->sf[POSI_SF_TIME];
+    int rc = batch_set(h->b, nullptr, h->sf.data(), nullptr, nullptr);
+    if (rc != POSI_OK) return rc;
+    if (h->hist) std::fflush(h->hist);
+    const int64_t n = h->si[POSI_SI_N];
+    std::vector<int64_t> si(POSI_SI_COUNT), bi((size_t)n * POSI_BI_COUNT);
+    std::vector<double> sf(POSI_SF_COUNT), bf((size_t)n * POSI_BF_COUNT), roche((size_t)n * n);
+    rc = batch_get(h->b, si.data(), sf.data(), bi.data(), bf.data(), roche.data());
+    if (rc != POSI_OK) return rc;
+    std::string err;
+    if (!posi::update_case_document(*h->doc, n, si.data(), sf.data(), bi.data(), bf.data(), roche.data(), err)) {
+        g_last_error = err;
+        return POSI_ERR_PARSE;
+    }
+    // keep one backup every 12 hours (the file name collides within a period)
+    std::FILE* probe = std::fopen(path, "rb");
+    if (probe) {
+        std::fclose(probe);
+        std::time_t now = std::time(nullptr);
+        std::tm g;
+        gmtime_r(&now, &g);
+        char stamp[32];
+        std::strftime(stamp, sizeof stamp, "%Y%m%dT", &g);
+        const std::string backup = (has_ext ? p.substr(0, dot) : p) + "." + stamp + (g.tm_hour < 12 ? "AM" : "PM") + ".bin";
+        std::rename(path, backup.c_str());
+    }
+    std::string text;
+    posi::write_json(*h->doc, text);
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) { g_last_error = std::string("cannot write ") + path; return POSI_ERR_IO; }
+    const size_t w = std::fwrite(text.data(), 1, text.size(), f);
+    std::fclose(f);
+    return w == text.size() ? POSI_OK : POSI_ERR_IO;
 }
 
 // ---- batched --------------------------------------------------------------

@@ -112,6 +112,7 @@ struct Dev {
     const int32_t* list;           // systems of this launch
     int32_t n_list;
     int32_t* step_flags;           // per system: bit0 recovery trigger, bit1 historic trigger
+    double* hist;                  // optional: [n_sys][nmax][HR_COUNT], last historic record
 };
 
 // Per-planet constants of one half kick, slot k of lane j at P[k * G + j].
@@ -124,8 +125,15 @@ enum {
     // Kidder GR
     PC_A, PC_B, PC_C, PC_DD, PC_E, PC_T1, PC_K2C, PC_K3C, PC_K4C, PC_K5C, PC_K6C, PC_A05, PC_P, PC_Q, PC_R3,
     PC_MRATIO, PC_MFM, PC_MU, PC_FM, PC_FM2, PC_NN0, PC_NN1, PC_NN2, PC_C6NN0, PC_C6NN1, PC_C6NN2,
+    // tidal internals of the last evaluation (state: read by the historic dE/dt)
+    PC_TD_DIST, PC_TD_VR, PC_TD_ORTHO, PC_TD_DPM, PC_TD_P0, PC_TD_P1, PC_TD_P2, PC_TD_V0, PC_TD_V1, PC_TD_V2,
+    PC_TD_L0, PC_TD_L1, PC_TD_L2,
     PC_COUNT
 };
+
+// Fields of one historic-snapshot record (src/integrator/output.rs:91-135).
+enum { HR_T = 0, HR_DT, HR_ID, HR_PX, HR_PY, HR_PZ, HR_SX, HR_SY, HR_SZ, HR_VX, HR_VY, HR_VZ, HR_M, HR_R, HR_RG2,
+       HR_K2, HR_SIGMA, HR_LAG, HR_DENERGY, HR_MIGRATION, HR_COUNT };
 
 // Shared memory of one group: XS exchange slots of G doubles, the per-planet
 // constants, a host card, column results and a few integers.
@@ -280,6 +288,8 @@ struct Sys {
             b.k2f = F[POSI_BF_K2F * st];
             b.denergy = F[POSI_BF_DENERGY_DT * st];
             b.lag = F[POSI_BF_LAG_ANGLE * st];
+#pragma unroll
+            for (int k = 0; k < 13; ++k) P(PC_TD_DIST + k) = F[(POSI_BF_TD_DIST + k) * st];
             const int64_t* I = D.bi + o;
             b.tk = (int)I[POSI_BI_TIDES_KIND * st];
             b.fk = (int)I[POSI_BI_FLAT_KIND * st];
@@ -332,6 +342,8 @@ struct Sys {
         F[POSI_BF_NSV2 * st] = b.nsv2;
         F[POSI_BF_DENERGY_DT * st] = b.denergy;
         F[POSI_BF_LAG_ANGLE * st] = b.lag;
+#pragma unroll
+        for (int k = 0; k < 13; ++k) F[(POSI_BF_TD_DIST + k) * st] = P(PC_TD_DIST + k);
         D.bi[POSI_BI_EVO_LEFT * st + o] = b.eleft;
     }
 
@@ -468,6 +480,42 @@ struct Sys {
     // Per-planet constants of a half kick (after the spin/evolution update
     // of its first midpoint iteration, so that evolved radii are used).
     // ------------------------------------------------------------------
+    __device__ __forceinline__ void record_tidal_internals(double d, double vr, double ortho, double dpm, double x,
+                                                           double y, double z, double vx, double vy, double vz,
+                                                           double lx, double ly, double lz) {
+        P(PC_TD_DIST) = d; P(PC_TD_VR) = vr; P(PC_TD_ORTHO) = ortho; P(PC_TD_DPM) = dpm;
+        P(PC_TD_P0) = x; P(PC_TD_P1) = y; P(PC_TD_P2) = z;
+        P(PC_TD_V0) = vx; P(PC_TD_V1) = vy; P(PC_TD_V2) = vz;
+        P(PC_TD_L0) = lx; P(PC_TD_L1) = ly; P(PC_TD_L2) = lz;
+    }
+
+    // src/effects/tides/common.rs:263-279, in the reference's operation order,
+    // from the tidal internals of the last evaluation and the current spin.
+    __device__ void tides_denergy_dt() {
+        if (!(planet() && b.tk == POSI_EFFECT_ORBITING)) return;
+        const double d = P(PC_TD_DIST), vr = P(PC_TD_VR);
+        const double x = P(PC_TD_P0), y = P(PC_TD_P1), z = P(PC_TD_P2);
+        const double vx = P(PC_TD_V0), vy = P(PC_TD_V1), vz = P(PC_TD_V2);
+        const double sx = b.S[0], sy = b.S[1], sz = b.S[2];
+        const double factor2 = P(PC_TD_ORTHO) / d;
+        b.denergy = -((1.0 / d * (P(PC_TD_DPM) + factor2 * vr)) * (x * vx + y * vy + z * vz)
+                      + factor2 * ((sy * z - sz * y - vx) * vx + (sz * x - sx * z - vy) * vy + (sx * y - sy * x - vz) * vz))
+                    - (P(PC_TD_L0) * sx + P(PC_TD_L1) * sy + P(PC_TD_L2) * sz);
+    }
+
+    // src/integrator/output.rs:91-135: the record of one historic snapshot.
+    __device__ void write_history_record(const Dev& D) const {
+        if (!D.hist || !has) return;
+        double* R = D.hist + ((int64_t)s * D.nmax + lane) * HR_COUNT;
+        R[HR_T] = t; R[HR_DT] = dt; R[HR_ID] = (double)lane;
+        R[HR_PX] = b.r[0]; R[HR_PY] = b.r[1]; R[HR_PZ] = b.r[2];
+        R[HR_SX] = b.S[0]; R[HR_SY] = b.S[1]; R[HR_SZ] = b.S[2];
+        R[HR_VX] = b.v[0]; R[HR_VY] = b.v[1]; R[HR_VZ] = b.v[2];
+        R[HR_M] = b.m; R[HR_R] = b.R; R[HR_RG2] = b.rg2;
+        R[HR_K2] = b.tk != POSI_EFFECT_DISABLED ? b.k2 : 0.;
+        R[HR_SIGMA] = b.sig; R[HR_LAG] = b.lag; R[HR_DENERGY] = b.denergy; R[HR_MIGRATION] = 0.;
+    }
+
     // Heliocentric position of a planet, its distance and unit vector: fixed
     // for a whole half kick, needed from the first evaluation on.
     __device__ void set_geometry(double x, double y, double z) {
@@ -658,6 +706,7 @@ struct Sys {
                 col[3 * G] = -1.0 * (o_s * (d * hS0 - rs_s * x / d - inv_d * h0));
                 col[4 * G] = -1.0 * (o_s * (d * hS1 - rs_s * y / d - inv_d * h1));
                 col[5 * G] = -1.0 * (o_s * (d * hS2 - rs_s * z / d - inv_d * h2));
+                record_tidal_internals(d, vr, o_p, diss_pm, x, y, z, hv[0], hv[1], hv[2], dt_[0], dt_[1], dt_[2]);
             }
             if (flat && b.fk == POSI_EFFECT_ORBITING) {
                 // oblate_spheroid.rs:12-60
@@ -778,7 +827,17 @@ struct Sys {
             const double factor2 = 1. / card[HC_M];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                if (tides) { at[k] = -1.0 * factor2 * sums[k]; dt_[k] = sums[3 + k]; }
+                if (tides) {
+                    at[k] = -1.0 * factor2 * sums[k];
+                    dt_[k] = sums[3 + k];
+                    // the host's tides output and its (zero) heliocentric
+                    // copies (tides/common.rs:202-261)
+                    P(PC_TD_L0 + k) = sums[3 + k];
+                    P(PC_TD_P0 + k) = 0.;
+                    P(PC_TD_V0 + k) = 0.;
+                    P(PC_TD_DIST) = 0.;
+                    P(PC_TD_VR) = 0.;
+                }
                 if (flat) { af[k] = -1.0 * factor2 * sums[6 + k]; df[k] = sums[9 + k]; }
                 if (gr) {
                     ag[k] = -1.0 * sums[12 + k] + -1.0 * sums[15 + k] + -1.0 * sums[18 + k];
@@ -865,6 +924,8 @@ struct Sys {
                 th0 -= osdd * hS0 - qs * xd - osd * h0;
                 th1 -= osdd * hS1 - qs * yd - osd * h1;
                 th2 -= osdd * hS2 - qs * zd - osd * h2;
+                record_tidal_internals(P(PC_D), vr, P(PC_OP), factor1 * P(PC_TERM2), x, y, z, hv0, hv1, hv2, dl0, dl1,
+                                       dl2);
             }
             if (flat && b.fk == POSI_EFFECT_ORBITING) {
                 const double cfs = P(PC_CFS), cfp = P(PC_CFP);
@@ -1620,6 +1681,8 @@ struct Sys {
             spin_and_evolving(D, t, true);
             zero_inertia_check();
             if (fatal()) return false;
+            if (tides) tides_denergy_dt();
+            write_history_record(D);
             if (!first) last_hist += hist_period; else last_hist = 0.;
             n_hist += 1;
         }

@@ -3,9 +3,9 @@ import numpy as np
 
 from posidonius_gb300 import layout as L
 
-# body fields the kernels maintain (the tidal dE/dt is only refreshed for the
-# historic snapshot record)
-STATE_FIELDS = [f for f in range(L.BF_COUNT) if f not in (L.BF_DENERGY_DT,)]
+# every body field is state the kernels maintain (the tidal dE/dt is refreshed
+# at historic-snapshot steps and is NaN after the first one, 0/0)
+STATE_FIELDS = list(range(L.BF_COUNT))
 SYS_I64_FIELDS = [L.SI_ITERATION, L.SI_N_HIST, L.SI_TIMESTEP_WARNING, L.SI_STATUS, L.SI_FAIL_STEP, L.SI_FAIL_PAIR,
                   L.SI_LAST_MIDPOINT_ITERS]
 SYS_F64_FIELDS = [L.SF_TIME, L.SF_LAST_HIST, L.SF_LAST_REC]
@@ -22,16 +22,24 @@ def as_batch_view(state):
     return state
 
 
+def same_bits(fa, fb):
+    """Element-wise: identical bits, or both NaN (the NaN payload of 0/0
+    differs between host architectures and the GPU)."""
+    fa, fb = np.asarray(fa, dtype=np.float64), np.asarray(fb, dtype=np.float64)
+    return (fa.view(np.int64) == fb.view(np.int64)) | (np.isnan(fa) & np.isnan(fb))
+
+
 def bitwise_diffs(a, b):
-    """Fields whose values differ in any bit; [] when identical."""
+    """Fields whose values differ in any bit (NaN matching NaN); [] when identical."""
     a, b = as_batch_view(a), as_batch_view(b)
     out = []
     ns = a["sys_i64"].shape[0]
     for s in range(ns):
         n = nbodies(a, s)
         fa, fb = a["body_f64"][s, :n][:, STATE_FIELDS], b["body_f64"][s, :n][:, STATE_FIELDS]
-        if not np.array_equal(fa.view(np.int64), fb.view(np.int64)):
-            bad = np.nonzero((fa.view(np.int64) != fb.view(np.int64)).any(axis=0))[0]
+        same = same_bits(fa, fb)
+        if not same.all():
+            bad = np.nonzero((~same).any(axis=0))[0]
             out.append((s, "body_f64", [STATE_FIELDS[i] for i in bad]))
         if not np.array_equal(a["body_i64"][s, :n, L.BI_EVO_LEFT], b["body_i64"][s, :n, L.BI_EVO_LEFT]):
             out.append((s, "evo_left", None))
@@ -39,7 +47,7 @@ def bitwise_diffs(a, b):
             if a["sys_i64"][s, f] != b["sys_i64"][s, f]:
                 out.append((s, "sys_i64", f))
         for f in SYS_F64_FIELDS:
-            if np.float64(a["sys_f64"][s, f]).view(np.int64) != np.float64(b["sys_f64"][s, f]).view(np.int64):
+            if not same_bits(a["sys_f64"][s, f], b["sys_f64"][s, f]):
                 out.append((s, "sys_f64", f))
     return out
 

@@ -97,3 +97,17 @@ def test_product_fails_loudly_without_a_device(built, tmp_path):
     with pytest.raises(pg.PosiError) as e:
         pg.WHFast.from_json(_unzip(tmp_path, "test_integrator-whfast_jacobi"))
     assert e.value.status == L.ERR_CUDA
+
+
+def test_cli_usage_without_gpu():
+    """The `posidonius` command is built beside the library and rejects a
+    malformed command line before touching a device."""
+    import subprocess
+    from posidonius_gb300 import build as B
+    B.build()
+    r = subprocess.run([B.CLI], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "posidonius start" in r.stderr
+    r = subprocess.run([B.CLI, "start", "only_one_arg.json"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2
+    r = subprocess.run([B.CLI, "resume", "a.json", "b.bin", "--bogus"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2
