@@ -43,12 +43,20 @@ def parse():
     p.add_argument("--warmup", type=int, default=300)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="ensemble8", choices=["ensemble8", "uneven", "single"])
+    p.add_argument("--no-autotune", action="store_true", help="smallest lane group per system, no tuning")
     p.add_argument("--n-systems", type=int, default=None)
     p.add_argument("--launches", type=int, default=10, help="timed launches (L2 flushed before each)")
     p.add_argument("--mode", default="fast", choices=["fast", "exact"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     return p.parse_args()
+
+
+EFFECTS = {
+    "ensemble8": "CTL tides + oblate flattening + Kidder GR",
+    "single": "CTL tides + oblate flattening + Kidder GR",
+    "uneven": "each of CTL tides / oblate flattening / Kidder GR on with p = 0.7; 20% circumbinary binaries",
+}
 
 
 def make_workload(name, n_systems, rank=0):
@@ -199,7 +207,9 @@ def cpu_leg(ens, steps_hint, seconds, nthreads):
     from posidonius_gb300 import layout as L
     ns_total = ens["n_sys"]
     n_sys = min(ns_total, max(64, nthreads * 16))
-    sub = {k: (v[:n_sys] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
+    # a strided sample, so that uneven workloads are represented
+    idx = np.linspace(0, ns_total - 1, n_sys).astype(np.int64)
+    sub = {k: (v[idx] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
     sub["n_sys"] = n_sys
     state, _, _ = oracle.run(sub, op=oracle.INITIALIZE, nthreads=nthreads)
     # calibrate: 10 steps, then size the sample for ~`seconds`
@@ -211,10 +221,12 @@ def cpu_leg(ens, steps_hint, seconds, nthreads):
     oracle.run(state, max_steps=steps, nthreads=nthreads)
     dt = time.perf_counter() - t0
     # algorithmic flops per system-step of this workload (counted restatement)
-    flo_state, _, _ = oracle.run({k: (v[:4] if isinstance(v, np.ndarray) and k != "tables" else v)
-                                  for k, v in state.items()} | {"n_sys": 4}, op=oracle.ITERATE, max_steps=1)
+    nf = min(n_sys, 64)
+    fidx = np.linspace(0, n_sys - 1, nf).astype(np.int64)
+    flo_state, _, _ = oracle.run({k: (v[fidx] if isinstance(v, np.ndarray) and k != "tables" else v)
+                                  for k, v in state.items()} | {"n_sys": nf}, op=oracle.ITERATE, max_steps=1)
     _, _, _, cnt = oracle.run(flo_state, max_steps=20, flops=True)
-    flops = cnt[0] / (4 * 20)
+    flops = cnt[0] / (nf * 20)
     return {"value": n_sys * steps / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
             "sample": f"{n_sys} systems x {steps} WHFast steps of the {ens.get('_name', 'ensemble')} workload, "
                       f"C++ restatement of the Rust FP64 path, {nthreads} threads, {dt:.1f} s",
@@ -222,8 +234,9 @@ def cpu_leg(ens, steps_hint, seconds, nthreads):
 
 
 def plain_path(mode, steps=400):
-    """Single-system drop-in path (posi_iterate, one kernel launch per step)
-    on the star + 3 planets workload, wall clock."""
+    """Single-system drop-in path on the star + 3 planets workload: one
+    posi_iterate(h, 1) call per WHFast step -- the granularity of the
+    reference's Integrator::iterate loop (src/main.rs:158-176) -- wall clock."""
     import posidonius_gb300 as pg
     from posidonius_gb300 import layout as L
     one = make_workload("single", 1)
@@ -233,11 +246,13 @@ def plain_path(mode, steps=400):
     w.initialize_physical_values()
     w.run(20)
     t0 = time.perf_counter()
-    done = w.run(steps)
+    done = 0
+    for _ in range(steps):
+        done += w.iterate(1)[1]
     dt = time.perf_counter() - t0
     w.close()
     return {"value": done / dt, "unit": UNIT, "workload": "single (star + 3 planets)", "steps": done,
-            "note": "posi_iterate, one kernel launch per WHFast step, wall clock"}
+            "note": "posi_iterate(h, 1) per WHFast step (one kernel launch + state readback each), wall clock"}
 
 
 def run_reference(args):
@@ -290,6 +305,9 @@ def main():
     mode = pg.FAST if args.mode == "fast" else pg.EXACT
     batch = pg.Batch(ens, mode=mode)
     batch.initialize_physical_values()
+    # lane mapping per body count: picked by the autotuner (state unchanged)
+    lanes = batch.autotune(probe_steps=20) if not args.no_autotune else {
+        int(n): batch.mapping_for(int(n)) for n in np.unique(ens["sys_i64"][:, L.SI_N])}
     K = args.steps
     R = max(1, min(args.launches, K))
     spl = (K + R - 1) // R
@@ -362,7 +380,9 @@ def main():
         "dtype": "f64", "data": "synthetic (seeded; posidonius_gb300.ensemble)",
         "config": {"workload": args.workload, "n_systems": int(batch.n_sys), "bodies_per_system": int(batch.nmax),
                    "dt_days": 0.08, "mode": args.mode, "steps_per_launch": spl, "timed_launches": R,
-                   "effects": "CTL tides + oblate flattening + Kidder GR", "coordinates": "Jacobi",
+                   "effects": EFFECTS[args.workload], "coordinates": "Jacobi",
+                   "lanes_per_system": {str(k): v for k, v in sorted(lanes.items())},
+                   "mapping": "autotuned" if not args.no_autotune else "smallest group",
                    "l2": f"flushed ({L2_FLUSH_BYTES >> 20} MiB write) before every timed launch",
                    "parallelism": f"replicas x{world} (independent ensembles per GPU)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,

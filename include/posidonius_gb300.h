@@ -282,6 +282,16 @@ int posi_batch_size(const posi_batch* b, int64_t* n_systems, int64_t* nmax);
 /* Mapping chosen for systems with n bodies (after autotuning), or -1. */
 int posi_batch_mapping_for(const posi_batch* b, int64_t n);
 
+/* Autotuner of the batched kernel (no reference counterpart: the reference
+ * integrates one system per process).  For every body count present, each
+ * admissible lane mapping (2..32 lanes per system, one body per lane) runs
+ * probe_steps steps on the systems of that count, timed with CUDA events; the
+ * state is restored after every trial and the fastest mapping is kept.
+ * lanes_by_n (optional, POSI_MAX_BODIES + 1 entries) receives the choice per
+ * body count (0 where no system has that count).  Results do not depend on
+ * the mapping: every mapping computes the same bits. */
+int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n);
+
 /* Device time of the last posi_batch_iterate in milliseconds (CUDA events on
  * the batch's stream) and the number of kernel launches it made. */
 int posi_batch_last_timing(const posi_batch* b, double* ms, int64_t* launches);

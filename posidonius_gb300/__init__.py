@@ -243,6 +243,13 @@ class Batch:
     def mapping_for(self, n):
         return lib().posi_batch_mapping_for(self._h, int(n))
 
+    def autotune(self, probe_steps=20):
+        """Pick the fastest lane mapping per body count (state unchanged).
+        Returns {body count: lanes per system}."""
+        out = (ctypes.c_int32 * (L.MAX_BODIES + 1))()
+        check(lib().posi_batch_autotune(self._h, int(probe_steps), out))
+        return {n: int(out[n]) for n in range(L.MAX_BODIES + 1) if out[n]}
+
     def empty_state(self):
         ns, nm = self.n_sys, self.nmax
         return {

@@ -97,8 +97,11 @@ struct posi_batch {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<Bucket> buckets;
-    std::vector<int64_t> n_of;  // bodies per system
+    std::vector<int64_t> n_of;    // bodies per system
+    std::vector<int64_t> key_of;  // ordering key: bodies, effect flags, coordinates
+    std::vector<int32_t> host_list;
     std::map<int64_t, int> mapping_of_n;
+    std::map<int64_t, double> tuned_ms_of_n;  // autotuner: best probe time per body count
     double last_ms = 0.;
     int64_t last_launches = 0;
     cudaGraphExec_t graph = nullptr;
@@ -176,21 +179,36 @@ int download_aos(const posi_batch* b, T* host, const T* src, int64_t rows, int f
     return POSI_OK;
 }
 
-int build_buckets(posi_batch* b, const int64_t* sys_i64) {
-    // group the systems by lanes per system (one body per lane)
+// Systems are grouped by lanes per system (one body per lane); within a
+// group they are ordered by body count, then effect flags and coordinates,
+// so that the groups sharing a warp take the same branches.  `chosen` maps a
+// body count to its lanes per system (the autotuner's choice); otherwise the
+// smallest group that holds the system, or the caller's fixed mapping.
+int build_buckets(posi_batch* b, const int64_t* sys_i64, const std::map<int64_t, int>* chosen = nullptr) {
     std::map<int, std::vector<int32_t>> by_g;
     b->n_of.resize(b->n_sys);
+    b->key_of.resize(b->n_sys);
     for (int64_t s = 0; s < b->n_sys; ++s) {
-        const int64_t n = sys_i64[s * POSI_SI_COUNT + POSI_SI_N];
+        const int64_t* si = sys_i64 + s * POSI_SI_COUNT;
+        const int64_t n = si[POSI_SI_N];
         b->n_of[s] = n;
+        b->key_of[s] = (((n * 2 + si[POSI_SI_TIDES]) * 2 + si[POSI_SI_FLAT]) * 2 + si[POSI_SI_GR]) * 4 +
+                       si[POSI_SI_COORDS];
+        b->key_of[s] = b->key_of[s] * 2 + si[POSI_SI_EVOLUTION];
         int G = posi::group_size_for(n);
-        if (b->mapping >= POSI_MAP_LANES2 && b->mapping <= POSI_MAP_WARP && b->mapping >= G) G = b->mapping;
+        if (chosen && chosen->count(n)) {
+            G = chosen->at(n);
+        } else if (b->mapping >= POSI_MAP_LANES2 && b->mapping <= POSI_MAP_WARP && b->mapping >= G) {
+            G = b->mapping;
+        }
         by_g[G].push_back((int32_t)s);
         b->mapping_of_n[n] = G;
     }
     std::vector<int32_t> list;
     b->buckets.clear();
     for (auto& kv : by_g) {
+        std::stable_sort(kv.second.begin(), kv.second.end(),
+                         [&](int32_t x, int32_t y) { return b->key_of[x] < b->key_of[y]; });
         Bucket bk;
         bk.G = kv.first;
         bk.offset = (int32_t)list.size();
@@ -198,9 +216,15 @@ int build_buckets(posi_batch* b, const int64_t* sys_i64) {
         list.insert(list.end(), kv.second.begin(), kv.second.end());
         b->buckets.push_back(bk);
     }
-    CK(cudaMalloc(&b->d_list, std::max<size_t>(1, list.size()) * sizeof(int32_t)));
+    if (!b->d_list) CK(cudaMalloc(&b->d_list, (size_t)std::max<int64_t>(1, b->n_sys) * sizeof(int32_t)));
     CK(cudaMemcpyAsync(b->d_list, list.data(), list.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));
     CK(cudaStreamSynchronize(b->stream));
+    b->host_list = list;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        b->graph_steps = -1;
+    }
     return POSI_OK;
 }
 
@@ -834,6 +858,92 @@ int posi_batch_set_state(posi_batch* b, const int64_t* sys_i64, const double* sy
                          const double* body_f64) {
     if (!b) return POSI_ERR_ARG;
     return batch_set(b, sys_i64, sys_f64, body_i64, body_f64);
+}
+
+// Autotuner: for every body count present, run each admissible lane mapping
+// (2..32 lanes per system, at least one lane per body) on the systems of that
+// count for probe_steps steps -- once to warm up, once timed with CUDA events
+// -- restoring their state after every trial, and keep the fastest.  The
+// buckets are then rebuilt with the chosen mappings.
+int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n) {
+    if (!b || probe_steps < 1) return POSI_ERR_ARG;
+    const size_t nb = (size_t)b->stride;
+    const size_t bytes_bf = nb * POSI_BF_COUNT * sizeof(double), bytes_bi = nb * POSI_BI_COUNT * sizeof(int64_t);
+    const size_t bytes_sf = (size_t)b->n_sys * POSI_SF_COUNT * sizeof(double);
+    const size_t bytes_si = (size_t)b->n_sys * POSI_SI_COUNT * sizeof(int64_t);
+    const size_t bytes_fl = (size_t)b->n_sys * sizeof(int32_t);
+    char* save = nullptr;
+    CK(cudaMalloc(&save, bytes_bf + bytes_bi + bytes_sf + bytes_si + bytes_fl));
+    struct Saved {
+        char* p;
+        ~Saved() { cudaFree(p); }
+    } guard{save};
+    char* p_bf = save;
+    char* p_bi = p_bf + bytes_bf;
+    char* p_sf = p_bi + bytes_bi;
+    char* p_si = p_sf + bytes_sf;
+    char* p_fl = p_si + bytes_si;
+    auto copy_all = [&](bool to_save) -> int {
+        auto cp = [&](void* dst, const void* src, size_t n) {
+            return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, b->stream);
+        };
+        if (to_save) {
+            CK(cp(p_bf, b->d_bf, bytes_bf)); CK(cp(p_bi, b->d_bi, bytes_bi)); CK(cp(p_sf, b->d_sf, bytes_sf));
+            CK(cp(p_si, b->d_si, bytes_si)); CK(cp(p_fl, b->d_flags, bytes_fl));
+        } else {
+            CK(cp(b->d_bf, p_bf, bytes_bf)); CK(cp(b->d_bi, p_bi, bytes_bi)); CK(cp(b->d_sf, p_sf, bytes_sf));
+            CK(cp(b->d_si, p_si, bytes_si)); CK(cp(b->d_flags, p_fl, bytes_fl));
+        }
+        return POSI_OK;
+    };
+    int rc = copy_all(true);
+    if (rc != POSI_OK) return rc;
+    // systems of each body count, in bucket order
+    std::map<int64_t, std::vector<int32_t>> by_n;
+    for (int32_t s : b->host_list) by_n[b->n_of[s]].push_back(s);
+    int32_t* d_probe = nullptr;
+    CK(cudaMalloc(&d_probe, (size_t)b->n_sys * sizeof(int32_t)));
+    struct ListGuard {
+        int32_t* p;
+        ~ListGuard() { cudaFree(p); }
+    } lguard{d_probe};
+    std::map<int64_t, int> chosen;
+    b->tuned_ms_of_n.clear();
+    LaunchArgs a{};
+    a.op = posi::OP_STEPS;
+    a.n_steps = probe_steps;
+    for (auto& kv : by_n) {
+        const int64_t n = kv.first;
+        const std::vector<int32_t>& sys = kv.second;
+        CK(cudaMemcpyAsync(d_probe, sys.data(), sys.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));
+        double best = 1e300;
+        int best_g = posi::group_size_for(n);
+        for (int G = posi::group_size_for(n); G <= 32; G *= 2) {
+            a.G = G;
+            DevView v = b->view(0, (int32_t)sys.size());
+            v.list = d_probe;
+            float ms = 0.f;
+            for (int trial = 0; trial < 2; ++trial) {
+                CK(cudaEventRecord(b->ev0, b->stream));
+                CK(b->mode == POSI_MODE_EXACT ? posi::launch_exact(v, a, b->stream) : posi::launch_fast(v, a, b->stream));
+                CK(cudaEventRecord(b->ev1, b->stream));
+                CK(cudaEventSynchronize(b->ev1));
+                CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+                if ((rc = copy_all(false)) != POSI_OK) return rc;
+            }
+            if (ms < best) { best = ms; best_g = G; }
+        }
+        chosen[n] = best_g;
+        b->tuned_ms_of_n[n] = best;
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    std::vector<int64_t> si((size_t)b->n_sys * POSI_SI_COUNT);
+    if ((rc = batch_get(b, si.data(), nullptr, nullptr, nullptr, nullptr)) != POSI_OK) return rc;
+    if ((rc = build_buckets(b, si.data(), &chosen)) != POSI_OK) return rc;
+    if (lanes_by_n) {
+        for (int k = 0; k <= POSI_MAX_BODIES; ++k) lanes_by_n[k] = chosen.count(k) ? chosen[k] : 0;
+    }
+    return POSI_OK;
 }
 
 int posi_batch_mapping_for(const posi_batch* b, int64_t n) {

@@ -122,6 +122,30 @@ def test_batched_uneven_exact_and_mappings():
         assert bitwise_diffs(b.get_state(), ref) == [], mapping
 
 
+@pytest.mark.parametrize("mode", [pg.EXACT, pg.FAST])
+def test_autotune_keeps_state_and_results(mode):
+    """The autotuner's trial runs leave the state untouched, its choices are
+    admissible, and a tuned batch computes the same bits as an untuned one."""
+    ens = E.workload_uneven(256, seed=11)
+    tuned = pg.Batch(ens, mode=mode)
+    tuned.initialize_physical_values()
+    before = tuned.get_state()
+    choice = tuned.autotune(probe_steps=5)
+    assert bitwise_diffs(tuned.get_state(), before) == []
+    ns = set(int(n) for n in ens["sys_i64"][:, L.SI_N])
+    assert set(choice) == ns
+    for n, g in choice.items():
+        assert g in (2, 4, 8, 16, 32) and g >= n and tuned.mapping_for(n) == g
+    plain = pg.Batch(ens, mode=mode)
+    plain.initialize_physical_values()
+    tuned.iterate(30, 10)
+    plain.iterate(30, 10)
+    assert bitwise_diffs(tuned.get_state(), plain.get_state()) == []
+    if mode == pg.EXACT:
+        ref, _, _ = oracle.run(ens, max_steps=30, init_physical=True, nthreads=8)
+        assert bitwise_diffs(tuned.get_state(), ref) == []
+
+
 def test_batched_chunking_and_plain_agree():
     ens = E.workload_ensemble8(8, seed=3)
     outs = []
