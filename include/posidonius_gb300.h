@@ -304,6 +304,39 @@ int posi_batch_last_timing(const posi_batch* b, double* ms, int64_t* launches);
  * FP64-bound kernels. */
 int posi_fp64_probe(int blocks, int threads, int iters, double* ms, double* tflops);
 
+/* ---- adjoint (reverse mode) of the batched WHFast step ----------------------
+ * No reference counterpart: the reference has no derivatives.  Gradients of a
+ * function of the state after n_steps steps with respect to the state at the
+ * start (positions, velocities, spin angular momenta, spins) and to every
+ * body's tidal dissipation factor (scaled_dissipation_factor) and Love number.
+ * Supported: Jacobi coordinates, non-evolving bodies, up to 8 bodies per system.
+ * The forward run stores the batch state every checkpoint_every steps; the
+ * backward run re-integrates each chunk (recording its steps) and sweeps it in
+ * reverse.  Derivatives are those of the computed map (the midpoint loop is
+ * reversed with its iteration counts, the Kepler root is differentiated
+ * implicitly). */
+typedef struct posi_adjoint posi_adjoint;
+posi_adjoint* posi_adjoint_create(posi_batch* b, int64_t n_steps, int64_t checkpoint_every, int* status);
+void posi_adjoint_destroy(posi_adjoint* a);
+/* Run the n_steps forward steps of the batch from its current state, keeping
+ * the checkpoints; the batch ends at the final state. */
+int posi_adjoint_forward(posi_adjoint* a);
+/* Per-system flags of posi_adjoint_backward: the system's gradients are not
+ * meaningful when any is set. */
+enum posi_adjoint_flag {
+    POSI_ADJ_KEPLER = 1,        /* a Kepler root did not converge */
+    POSI_ADJ_ZERO_INERTIA = 2,  /* a body has no moment of inertia */
+    POSI_ADJ_FROZEN = 4         /* the forward run froze the system (collision, Roche limit, ejection) */
+};
+/* lam_final: [n_systems][nmax][12] adjoints of the final (r, v, L, S); out:
+ * lam_initial (same layout, may be NULL), grad [n_systems][nmax][2] (d/d
+ * sigma, d/d k2; may be NULL) and system_flags [n_systems] (may be NULL).
+ * Host or device pointers (unified addressing). */
+int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_initial, double* grad,
+                          int32_t* system_flags);
+/* CUDA-event times of the last forward and backward runs. */
+int posi_adjoint_last_timing(const posi_adjoint* a, double* forward_ms, double* backward_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,6 +54,11 @@ SIGNATURES = {
     "posi_open_history": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int64]),
     "posi_close_history": (ctypes.c_int, [_vp]),
     "posi_write_recovery_snapshot": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "posi_adjoint_create": (_vp, [_vp, ctypes.c_int64, ctypes.c_int64, _intp]),
+    "posi_adjoint_destroy": (None, [_vp]),
+    "posi_adjoint_forward": (ctypes.c_int, [_vp]),
+    "posi_adjoint_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "posi_adjoint_last_timing": (ctypes.c_int, [_vp, _f64p, _f64p]),
 }
 
 _lib = None

@@ -1,0 +1,428 @@
+"""Gradients of WHFast trajectories: the adjoint behind ``torch.autograd``.
+
+:class:`Adjoint` drives the C ABI's checkpointed reverse mode
+(``posi_adjoint_*``): a forward run of a :class:`~posidonius_gb300.Batch` that
+keeps its state every ``checkpoint_every`` steps, then a backward run that
+re-integrates each chunk on the GPU, records its steps and sweeps them in
+reverse with the hand-derived vector-Jacobian products of the step.
+
+:class:`WHFastTrajectory` wraps it as a ``torch.autograd.Function``: initial
+positions, velocities and spin angular momenta, plus every body's tidal
+dissipation factor and Love number, in; the state after ``n_steps`` out.
+PyTorch is the gradient binding only: the trajectory and its adjoint run in
+the CUDA library; torch differentiates what the caller builds around it
+(orbital elements -> Cartesian state, final state -> loss).
+
+:func:`elements_to_state` and :func:`orbital_elements` are those torch-side
+maps for star + planets systems (the reference's
+``calculate_cartesian_coordinates`` / ``calculate_keplerian_orbital_elements``
+in src/tools.rs, and the pseudo-synchronous spin of src/tools.rs:909-927),
+and :func:`tidal_loss` is the objective of the differentiation workload: the
+sum of squared final eccentricities, squared relative semi-major-axis drifts
+and squared relative planetary spin-rate changes.
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from . import layout as L
+from ._lib import check, lib
+
+LAM_FIELDS = 12   # adjoint of (r, v, L, S) per body
+GRAD_FIELDS = 2   # d/d dissipation factor, d/d Love number
+FLAG_KEPLER = L.ADJ_KEPLER
+FLAG_ZERO_INERTIA = L.ADJ_ZERO_INERTIA
+FLAG_FROZEN = L.ADJ_FROZEN
+
+
+class Adjoint:
+    """Checkpointed reverse mode over a Batch (posi_adjoint_*)."""
+
+    def __init__(self, batch, n_steps, checkpoint_every=100):
+        st = ctypes.c_int(0)
+        h = lib().posi_adjoint_create(batch._h, int(n_steps), int(checkpoint_every), ctypes.byref(st))
+        if not h:
+            check(st.value)
+        self._h = ctypes.c_void_p(h)
+        self.batch = batch
+        self.n_steps = int(n_steps)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().posi_adjoint_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self):
+        check(lib().posi_adjoint_forward(self._h))
+
+    def backward(self, lam_final, lam_initial=None, grad=None):
+        """lam_final: [n_sys, nmax, 12] (numpy, or a contiguous CUDA float64
+        tensor); returns (lam_initial, grad) of the same kind.  Per-system
+        flags (FLAG_* bits; gradients of a flagged system are not meaningful)
+        are kept in ``self.flags``."""
+        ns, nm = self.batch.n_sys, self.batch.nmax
+        if isinstance(lam_final, np.ndarray):
+            lam_final = np.ascontiguousarray(lam_final, dtype=np.float64).reshape(ns, nm, LAM_FIELDS)
+            if lam_initial is None:
+                lam_initial = np.zeros((ns, nm, LAM_FIELDS))
+            if grad is None:
+                grad = np.zeros((ns, nm, GRAD_FIELDS))
+            ptrs = [a.ctypes.data for a in (lam_final, lam_initial, grad)]
+        else:  # torch tensors on the batch's device
+            import torch
+            lam_final = lam_final.contiguous().to(torch.float64)
+            if lam_initial is None:
+                lam_initial = torch.zeros((ns, nm, LAM_FIELDS), dtype=torch.float64, device=lam_final.device)
+            if grad is None:
+                grad = torch.zeros((ns, nm, GRAD_FIELDS), dtype=torch.float64, device=lam_final.device)
+            torch.cuda.synchronize(lam_final.device)
+            ptrs = [t.data_ptr() for t in (lam_final, lam_initial, grad)]
+        self.flags = np.zeros(ns, dtype=np.int32)
+        check(lib().posi_adjoint_backward(self._h, ctypes.c_void_p(ptrs[0]), ctypes.c_void_p(ptrs[1]),
+                                          ctypes.c_void_p(ptrs[2]), ctypes.c_void_p(self.flags.ctypes.data)))
+        return lam_initial, grad
+
+    def last_timing(self):
+        f, b = ctypes.c_double(), ctypes.c_double()
+        check(lib().posi_adjoint_last_timing(self._h, ctypes.byref(f), ctypes.byref(b)))
+        return f.value, b.value
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class WHFastTrajectory:
+    """``apply(r0, v0, L0, sigma, k2)`` -> ``(r, v, L)`` after n_steps.
+
+    Shapes [n_sys, nmax, 3] and [n_sys, nmax]; float64.  The batch supplies
+    everything else (masses, radii, effect flags, time step); spins start at
+    L / I (the reference's initialize_physical_values)."""
+
+    def __init__(self, batch, n_steps, checkpoint_every=100):
+        self.batch = batch
+        self.adjoint = Adjoint(batch, n_steps, checkpoint_every)
+        self.base = batch.get_state()
+        torch = _torch()
+
+        engine = self
+
+        class Fn(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, r0, v0, L0, sigma, k2):
+                final = engine.run(r0, v0, L0, sigma, k2)
+                out = [torch.as_tensor(final["body_f64"][..., sl], dtype=torch.float64, device=r0.device)
+                       for sl in (L.POS, L.VEL, L.ANG)]
+                return tuple(out)
+
+            @staticmethod
+            def backward(ctx, gr, gv, gL):
+                ns, nm = engine.batch.n_sys, engine.batch.nmax
+                lam = torch.zeros((ns, nm, 12), dtype=torch.float64, device=gr.device)
+                if gr is not None:
+                    lam[..., 0:3] = gr
+                if gv is not None:
+                    lam[..., 3:6] = gv
+                if gL is not None:
+                    lam[..., 6:9] = gL
+                lam_init, grad = engine.adjoint.backward(lam.contiguous())
+                moi = torch.as_tensor(engine.base["body_f64"][..., L.BF_MOI], dtype=torch.float64, device=gr.device)
+                inv = torch.where(moi != 0, 1.0 / torch.where(moi != 0, moi, torch.ones_like(moi)), torch.zeros_like(moi))
+                # initial spins are L0 / I
+                gL0 = lam_init[..., 6:9] + lam_init[..., 9:12] * inv[..., None]
+                return lam_init[..., 0:3], lam_init[..., 3:6], gL0, grad[..., 0], grad[..., 1]
+
+        self.Fn = Fn
+
+    def run(self, r0, v0, L0, sigma, k2):
+        st = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in self.base.items()}
+        bf = st["body_f64"]
+        bf[..., L.POS] = r0.detach().cpu().numpy()
+        bf[..., L.VEL] = v0.detach().cpu().numpy()
+        Lh = L0.detach().cpu().numpy()
+        bf[..., L.ANG] = Lh
+        moi = bf[..., L.BF_MOI]
+        safe = np.where(moi != 0, moi, 1.0)
+        bf[..., L.SPIN] = np.where((moi != 0)[..., None], Lh / safe[..., None], 0.0)
+        bf[..., L.BF_NSV2] = np.sum(bf[..., L.SPIN] ** 2, axis=-1)
+        bf[..., L.BF_SIGMA] = sigma.detach().cpu().numpy()
+        bf[..., L.BF_K2] = k2.detach().cpu().numpy()
+        self.batch.set_state(st)
+        self.adjoint.forward()
+        return self.batch.get_state()
+
+    def __call__(self, r0, v0, L0, sigma, k2):
+        return self.Fn.apply(r0, v0, L0, sigma, k2)
+
+
+# ---------------------------------------------------------------------------
+# torch-side maps of the differentiation workload (star + planets systems)
+# ---------------------------------------------------------------------------
+def kepler_to_cartesian(gm, a, e, inc, omega, node, mean_anomaly, iters=40):
+    """Elliptic orbital elements -> position, velocity relative to the central
+    body (Kepler's equation by Newton's method); torch, broadcasting."""
+    torch = _torch()
+    E = mean_anomaly + e * torch.sin(mean_anomaly)
+    for _ in range(iters):
+        E = E - (E - e * torch.sin(E) - mean_anomaly) / (1.0 - e * torch.cos(E))
+    cE, sE = torch.cos(E), torch.sin(E)
+    b = a * torch.sqrt(1.0 - e * e)
+    xo, yo = a * (cE - e), b * sE
+    n = torch.sqrt(gm / a ** 3)
+    edot = n / (1.0 - e * cE)
+    vxo, vyo = -a * sE * edot, b * cE * edot
+    co, so = torch.cos(omega), torch.sin(omega)
+    cn, sn = torch.cos(node), torch.sin(node)
+    ci, si = torch.cos(inc), torch.sin(inc)
+    r11, r12 = cn * co - sn * so * ci, -cn * so - sn * co * ci
+    r21, r22 = sn * co + cn * so * ci, -sn * so + cn * co * ci
+    r31, r32 = so * si, co * si
+    pos = torch.stack([r11 * xo + r12 * yo, r21 * xo + r22 * yo, r31 * xo + r32 * yo], dim=-1)
+    vel = torch.stack([r11 * vxo + r12 * vyo, r21 * vxo + r22 * vyo, r31 * vxo + r32 * vyo], dim=-1)
+    return pos, vel
+
+
+def pseudo_synchronous_spin(a, e, inc, node, star_mass, planet_mass):
+    """src/tools.rs:909-927: pseudo-synchronous rotation, zero obliquity."""
+    from .ensemble import G_SI, M_SUN, AU, HOUR
+    torch = _torch()
+    alpha = ((1.0 + 7.5 * e ** 2 + 45.0 / 8.0 * e ** 4 + 5.0 / 16.0 * e ** 6) / (1.0 + 3.0 * e ** 2 + 3.0 / 8.0 * e ** 4)
+             / (1.0 - e ** 2) ** 1.5)
+    w = alpha * torch.sqrt(G_SI * M_SUN * (star_mass + planet_mass)) * (a * AU) ** (-1.5) * HOUR * 24.0
+    return torch.stack([w * torch.sin(inc) * torch.sin(node), -w * torch.sin(inc) * torch.cos(node),
+                        w * torch.cos(inc)], dim=-1)
+
+
+def elements_to_state(elements, masses, moi, star_spin):
+    """elements [S, P, 6] (a, e, i, argument of pericentre, node, mean
+    anomaly) of P planets around body 0 -> barycentric r, v [S, P+1, 3] and
+    spin angular momenta L [S, P+1, 3]; masses [S, P+1], moi [S, P+1],
+    star_spin [S, 3] (fixed)."""
+    from .ensemble import G
+    torch = _torch()
+    a, e, inc, om, no, M = elements.unbind(-1)
+    ms, mp = masses[:, :1], masses[:, 1:]
+    pos, vel = kepler_to_cartesian(G * (ms + mp), a, e, inc, om, no, M)
+    zeros = torch.zeros_like(pos[:, :1])
+    hpos = torch.cat([zeros, pos], dim=1)
+    hvel = torch.cat([zeros, vel], dim=1)
+    mt = masses.sum(dim=1, keepdim=True)
+    cmp = (masses[..., None] * hpos).sum(dim=1, keepdim=True) / mt[..., None]
+    cmv = (masses[..., None] * hvel).sum(dim=1, keepdim=True) / mt[..., None]
+    spin_p = pseudo_synchronous_spin(a, e, inc, no, ms, mp)
+    spin = torch.cat([star_spin[:, None, :], spin_p], dim=1)
+    return hpos - cmp, hvel - cmv, moi[..., None] * spin
+
+
+def orbital_elements(r, v, masses):
+    """Semi-major axis and eccentricity of every planet relative to body 0."""
+    from .ensemble import G
+    torch = _torch()
+    rr = r[:, 1:] - r[:, :1]
+    vv = v[:, 1:] - v[:, :1]
+    mu = G * (masses[:, :1] + masses[:, 1:])
+    d = torch.linalg.norm(rr, dim=-1)
+    v2 = (vv * vv).sum(-1)
+    a = 1.0 / (2.0 / d - v2 / mu)
+    h = torch.linalg.cross(rr, vv)
+    evec = torch.linalg.cross(vv, h) / mu[..., None] - rr / d[..., None]
+    e = torch.linalg.norm(evec, dim=-1)
+    return a, e
+
+
+def tidal_loss(r, v, Lspin, masses, moi, a0, spin0):
+    """Per-system loss: sum_p e_p^2 + ((a_p - a0_p) / a0_p)^2 +
+    ((|Omega_p| - |Omega0_p|) / |Omega0_p|)^2."""
+    torch = _torch()
+    a, e = orbital_elements(r, v, masses)
+    w = torch.linalg.norm(Lspin[:, 1:], dim=-1) / moi[:, 1:]
+    return (e ** 2 + ((a - a0) / a0) ** 2 + ((w - spin0) / spin0) ** 2).sum(dim=1)
+
+
+def gradient_workload(n_systems=1024, seed=None, dt=0.08):
+    """Systems of the differentiation workload: the 0.08 Msun star + 3 planets
+    of the single-system workload (elements drawn the same way), returned as
+    (case ensemble, elements [S, 3, 6], masses [S, 4], moi [S, 4],
+    star_spin [S, 3])."""
+    from . import ensemble as E
+    rng = np.random.default_rng(E.SEED_BASE + E.WORKLOAD_IDS["gradient"] if seed is None else seed)
+    cases, els, ms, mois, sspin = [], [], [], [], []
+    for _ in range(n_systems):
+        star = E._star()
+        masses = np.exp(rng.uniform(np.log(0.3), np.log(3.0), size=3)) * E.M_EARTH
+        a = np.sort(rng.uniform(0.01, 0.05, size=3))
+        bodies, el = [star], []
+        for k in range(3):
+            b = E._planet(rng, star.mass, a[k], mass=masses[k])
+            bodies.append(b)
+        # recover the drawn elements from the generator's relative state
+        for b in bodies[1:]:
+            el.append(_elements_of(E.G * (star.mass + b.mass), b.pos, b.vel))
+        case = E.make_system(bodies, dt=dt)
+        cases.append(case)
+        els.append(el)
+        ms.append([b.mass for b in bodies])
+        mois.append(case["body_f64"][:, L.BF_MOI])
+        sspin.append(star.spin)
+    return (E.stack_systems(cases), np.array(els), np.array(ms), np.array(mois), np.array(sspin))
+
+
+def _elements_of(mu, r, v):
+    """(a, e, i, argument of pericentre, node, mean anomaly) of a bound orbit."""
+    r, v = np.asarray(r, float), np.asarray(v, float)
+    d = np.linalg.norm(r)
+    h = np.cross(r, v)
+    inc = math.acos(h[2] / np.linalg.norm(h))
+    node = math.atan2(h[0], -h[1])
+    evec = np.cross(v, h) / mu - r / d
+    e = np.linalg.norm(evec)
+    a = 1.0 / (2.0 / d - v @ v / mu)
+    nvec = np.array([math.cos(node), math.sin(node), 0.0])
+    # argument of pericentre and true anomaly in the orbital plane
+    hz = h / np.linalg.norm(h)
+    def ang(x, y):
+        return math.atan2(np.cross(x, y) @ hz, x @ y)
+    om = ang(nvec, evec)
+    f = ang(evec, r)
+    E_ = 2.0 * math.atan2(math.sqrt(1 - e) * math.sin(f / 2), math.sqrt(1 + e) * math.cos(f / 2))
+    M = E_ - e * math.sin(E_)
+    return [a, e, inc, om, node, M]
+
+
+def _state_arrays(elements, sigma, k2, masses, moi, star_spin):
+    """numpy initial state (r, v, L, S) of the workload's systems."""
+    torch = _torch()
+    t = lambda x: torch.as_tensor(np.asarray(x), dtype=torch.float64)
+    with torch.no_grad():
+        r0, v0, L0 = elements_to_state(t(elements), t(masses), t(moi), t(star_spin))
+    r0, v0, L0 = r0.numpy(), v0.numpy(), L0.numpy()
+    moi = np.asarray(moi)
+    S0 = L0 / np.where(moi != 0, moi, 1.0)[..., None]
+    return r0, v0, L0, S0
+
+
+def loss_of_parameters(ens, elements, sigma, k2, masses, moi, star_spin, n_steps, mode=None):
+    """Per-system loss after n_steps for parameter sets given per system (no
+    gradient): one batched GPU run of all of them."""
+    import posidonius_gb300 as pg
+    torch = _torch()
+    batch = pg.Batch(ens, mode=pg.FAST if mode is None else mode)
+    batch.initialize_physical_values()
+    st = batch.get_state()
+    r0, v0, L0, S0 = _state_arrays(elements, sigma, k2, masses, moi, star_spin)
+    n = r0.shape[1]
+    bf = st["body_f64"]
+    bf[:, :n, L.POS] = r0
+    bf[:, :n, L.VEL] = v0
+    bf[:, :n, L.ANG] = L0
+    bf[:, :n, L.SPIN] = S0
+    bf[:, :n, L.BF_NSV2] = np.sum(S0 ** 2, axis=-1)
+    bf[:, :n, L.BF_SIGMA] = sigma
+    bf[:, :n, L.BF_K2] = k2
+    batch.set_state(st)
+    batch.iterate(n_steps, min(n_steps, 1000))
+    fin = batch.get_state()["body_f64"][:, :n]
+    t = lambda x: torch.as_tensor(np.asarray(x), dtype=torch.float64)
+    with torch.no_grad():
+        el = t(elements)
+        a0 = el[..., 0]
+        spin0 = torch.linalg.norm(pseudo_synchronous_spin(el[..., 0], el[..., 1], el[..., 2], el[..., 4],
+                                                          t(masses)[:, :1], t(masses)[:, 1:]), dim=-1)
+        out = tidal_loss(t(fin[..., L.POS]), t(fin[..., L.VEL]), t(fin[..., L.ANG]), t(masses), t(moi), a0, spin0)
+    batch.close()
+    return out.numpy()
+
+
+def finite_difference_gradient(ens, elements, sigma, k2, masses, moi, star_spin, n_steps, rel_step=1e-6,
+                               rel_step_tidal=None, mode=None):
+    """Central finite differences of the per-system loss with respect to
+    (sigma [nb], k2 [nb], elements [np, 6]) of every system, all perturbed
+    copies integrated in one batch.  Returns (d/dsigma, d/dk2, d/delements).
+    The step is rel_step x |parameter| (angles: x max(|angle|, 1), e:
+    x max(e, 0.05)); sigma and k2 use rel_step_tidal when given (the loss is
+    nearly linear in them and their effect over a short run is close to the
+    loss's rounding level, so a larger relative step resolves it)."""
+    rel_tidal = rel_step if rel_step_tidal is None else rel_step_tidal
+    elements = np.asarray(elements, float)
+    sigma, k2 = np.asarray(sigma, float), np.asarray(k2, float)
+    S, nb = sigma.shape
+    npl = elements.shape[1]
+    params = [("sigma", b, None) for b in range(nb)] + [("k2", b, None) for b in range(nb)] + \
+             [("el", p, c) for p in range(npl) for c in range(6)]
+    P = len(params)
+    reps = 2 * P
+    idx = np.repeat(np.arange(S), reps)
+    E2 = {k: (v[idx] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
+    E2["n_sys"] = S * reps
+    el2 = np.repeat(elements, reps, axis=0)
+    sg2 = np.repeat(sigma, reps, axis=0)
+    k22 = np.repeat(k2, reps, axis=0)
+    steps = np.zeros((S, P))
+    for s in range(S):
+        for j, (kind, b, c) in enumerate(params):
+            for sgn, off in ((1.0, 0), (-1.0, 1)):
+                row = s * reps + 2 * j + off
+                if kind == "sigma":
+                    h = rel_tidal * abs(sigma[s, b])
+                    sg2[row, b] += sgn * h
+                elif kind == "k2":
+                    h = rel_tidal * abs(k2[s, b])
+                    k22[row, b] += sgn * h
+                else:
+                    x = elements[s, b, c]
+                    h = rel_step * (abs(x) if c == 0 else max(abs(x), 1.0 if c >= 2 else 0.05))
+                    el2[row, b, c] += sgn * h
+                steps[s, j] = h
+    loss = loss_of_parameters(E2, el2, sg2, k22, np.repeat(masses, reps, axis=0), np.repeat(moi, reps, axis=0),
+                              np.repeat(star_spin, reps, axis=0), n_steps, mode=mode).reshape(S, P, 2)
+    g = (loss[..., 0] - loss[..., 1]) / (2.0 * steps)
+    g = np.where(steps > 0, g, 0.0)
+    return g[:, :nb], g[:, nb:2 * nb], g[:, 2 * nb:].reshape(S, npl, 6)
+
+
+def adjoint_gradient(ens, elements, sigma, k2, masses, moi, star_spin, n_steps, checkpoint_every=100,
+                     device="cuda", mode=None):
+    """Per-system loss and its gradient with respect to (sigma, k2, elements)
+    by the adjoint (torch autograd around WHFastTrajectory).  Returns
+    (loss [S], d/dsigma, d/dk2, d/delements, (forward_ms, backward_ms),
+    flags [S]) -- gradients of systems with flags != 0 are not meaningful."""
+    import posidonius_gb300 as pg
+    torch = _torch()
+    batch = pg.Batch(ens, mode=pg.FAST if mode is None else mode)
+    batch.initialize_physical_values()
+    traj = WHFastTrajectory(batch, n_steps, checkpoint_every)
+    t = lambda x, g=False: torch.tensor(np.asarray(x), dtype=torch.float64, device=device, requires_grad=g)
+    el = t(elements, True)
+    sg = t(sigma, True)
+    kk = t(k2, True)
+    ms, mi, ss = t(masses), t(moi), t(star_spin)
+    r0, v0, L0 = elements_to_state(el, ms, mi, ss)
+    n = r0.shape[1]
+    nm = batch.nmax
+    if nm > n:  # pad to the batch's body slots
+        pad = lambda x: torch.cat([x, torch.zeros(x.shape[0], nm - n, *x.shape[2:], dtype=x.dtype, device=x.device)],
+                                  dim=1)
+        r0, v0, L0, sgp, kkp = pad(r0), pad(v0), pad(L0), pad(sg), pad(kk)
+    else:
+        sgp, kkp = sg, kk
+    r, v, Ls = traj(r0, v0, L0, sgp, kkp)
+    r, v, Ls = r[:, :n], v[:, :n], Ls[:, :n]
+    a0 = el[..., 0]
+    spin0 = torch.linalg.norm(pseudo_synchronous_spin(el[..., 0], el[..., 1], el[..., 2], el[..., 4], ms[:, :1],
+                                                      ms[:, 1:]), dim=-1)
+    loss = tidal_loss(r, v, Ls, ms, mi, a0, spin0)
+    loss.sum().backward()
+    timing = traj.adjoint.last_timing()
+    out = (loss.detach().cpu().numpy(), sg.grad.cpu().numpy(), kk.grad.cpu().numpy(), el.grad.cpu().numpy(), timing,
+           traj.adjoint.flags.copy())
+    traj.adjoint.close()
+    batch.close()
+    return out

@@ -1,0 +1,482 @@
+"""Generator of the reverse-mode sweeps of the per-planet effect blocks.
+
+The three additional-effect blocks of one planet -- constant-time-lag tides,
+oblate rotational flattening, Kidder (1995) general relativity -- are
+straight-line FP64 code.  This script restates them once (below, in the
+FAST build's formulation of ``csrc/whfast_device.cuh``, which follows
+src/effects/tides/constant_time_lag.rs:171-332, src/effects/tides/common.rs:
+223-370, src/effects/rotational_flattening/oblate_spheroid.rs:12-97 and
+src/effects/general_relativity.rs:177-456) by tracing them on a small
+expression graph, and emits ``csrc/adjoint_effects.cuh``: for every block a
+forward function and a vector-Jacobian product that recomputes the forward
+values it needs and then runs the reverse sweep, adjoint by adjoint, in
+registers.  Common subexpressions are merged and adjoints that nothing reads
+are never formed.
+
+Run ``python -m posidonius_gb300.adjoint_codegen`` after changing a block;
+the generated header is committed.
+"""
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "csrc", "adjoint_effects.cuh")
+
+
+class Node:
+    __slots__ = ("op", "args", "val", "id", "name")
+
+    def __init__(self, g, op, args=(), val=None, name=None):
+        self.op, self.args, self.val, self.name = op, tuple(args), val, name
+        self.id = None
+        g._add(self)
+
+    # arithmetic builds graph nodes
+    def _g(self):
+        return GRAPH
+
+    def __add__(self, o):
+        return GRAPH.op("add", self, o)
+
+    def __radd__(self, o):
+        return GRAPH.op("add", o, self)
+
+    def __sub__(self, o):
+        return GRAPH.op("sub", self, o)
+
+    def __rsub__(self, o):
+        return GRAPH.op("sub", o, self)
+
+    def __mul__(self, o):
+        return GRAPH.op("mul", self, o)
+
+    def __rmul__(self, o):
+        return GRAPH.op("mul", o, self)
+
+    def __truediv__(self, o):
+        return GRAPH.op("div", self, o)
+
+    def __rtruediv__(self, o):
+        return GRAPH.op("div", o, self)
+
+    def __neg__(self):
+        return GRAPH.op("neg", self)
+
+
+class Graph:
+    def __init__(self):
+        self.nodes = []
+        self.memo = {}
+        self.inputs = []     # differentiable inputs (name)
+        self.consts = []     # runtime constants (name), no adjoint
+
+    def _add(self, n):
+        n.id = len(self.nodes)
+        self.nodes.append(n)
+
+    def lit(self, v):
+        key = ("lit", float(v))
+        if key not in self.memo:
+            self.memo[key] = Node(self, "lit", val=float(v))
+        return self.memo[key]
+
+    def inp(self, name):
+        n = Node(self, "in", name=name)
+        self.inputs.append(n)
+        return n
+
+    def const(self, name):
+        n = Node(self, "cst", name=name)
+        self.consts.append(n)
+        return n
+
+    def op(self, op, a, b=None):
+        a = a if isinstance(a, Node) else self.lit(a)
+        if b is not None:
+            b = b if isinstance(b, Node) else self.lit(b)
+        # constant folding of literal operands
+        if a.op == "lit" and (b is None or b.op == "lit"):
+            x, y = a.val, (b.val if b is not None else None)
+            v = {"add": lambda: x + y, "sub": lambda: x - y, "mul": lambda: x * y, "div": lambda: x / y,
+                 "neg": lambda: -x, "sqrt": lambda: x ** 0.5}[op]()
+            return self.lit(v)
+        if op == "mul" and b is not None:
+            if a.op == "lit" and a.val == 1.0:
+                return b
+            if b.op == "lit" and b.val == 1.0:
+                return a
+        args = (a,) if b is None else (a, b)
+        if op in ("add", "mul"):  # commutative: canonical order for CSE
+            args = tuple(sorted(args, key=lambda n: n.id))
+        key = (op,) + tuple(n.id for n in args)
+        if key not in self.memo:
+            self.memo[key] = Node(self, op, args)
+        return self.memo[key]
+
+
+GRAPH = None
+
+
+def sqrt(a):
+    return GRAPH.op("sqrt", a)
+
+
+def cross(a, b):
+    return [a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]]
+
+
+def dot(a, b):
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]
+
+
+def powi(x, n):
+    """x**n by square-and-multiply (n >= 1)."""
+    result, base = None, x
+    while n:
+        if n & 1:
+            result = base if result is None else result * base
+        n >>= 1
+        if n:
+            base = base * base
+    return result
+
+
+# ---------------------------------------------------------------------------
+# The blocks.  Inputs common to all: heliocentric position r = (x, y, z),
+# heliocentric velocity hv, current spins S (planet) / H (host), previous
+# spins P (planet) / Q (host) -- the r.Omega products of an evaluation use
+# the spin of the previous evaluation.
+# ---------------------------------------------------------------------------
+K2 = "kK2"
+C2 = "kC2"
+FA = "kFA"
+GLOBALS = {K2, C2, FA}  # compile-time constants of the device code
+
+COMMON_INPUTS = ["x", "y", "z", "hv0", "hv1", "hv2", "S0", "S1", "S2", "H0", "H1", "H2",
+                 "P0", "P1", "P2", "Q0", "Q1", "Q2"]
+
+
+def _common(g):
+    v = {n: g.inp(n) for n in COMMON_INPUTS}
+    r = [v["x"], v["y"], v["z"]]
+    hv = [v["hv0"], v["hv1"], v["hv2"]]
+    S = [v["S0"], v["S1"], v["S2"]]
+    H = [v["H0"], v["H1"], v["H2"]]
+    P = [v["P0"], v["P1"], v["P2"]]
+    Q = [v["Q0"], v["Q1"], v["Q2"]]
+    d2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2]
+    d = sqrt(d2)
+    return r, hv, S, H, P, Q, d
+
+
+def block_tides(g):
+    r, hv, S, H, P, Q, d = _common(g)
+    sig_p, sig_h, k2_p, k2_h = g.inp("sig_p"), g.inp("sig_h"), g.inp("k2_p"), g.inp("k2_h")
+    m, hm, R, hR = g.const("m"), g.const("hm"), g.const("R"), g.const("hR")
+    inv_d = 1.0 / d
+    rd = [c * inv_d for c in r]
+    vr = dot(r, hv) * inv_d
+    rs_s = dot(r, Q)
+    rs_p = dot(r, P)
+    h = cross(r, hv)
+    d7 = powi(d, 7)
+    d8 = d7 * d
+    m2, hm2 = m * m, hm * hm
+    term1 = m2 * powi(hR, 10) * sig_h
+    term2 = hm2 * powi(R, 10) * sig_p
+    o_s = 4.5 * term1 / d7
+    o_p = 4.5 * term2 / d7
+    cons = g.const(K2) * -3.0 / d7 * (m2 * powi(hR, 5) * k2_h + hm2 * powi(R, 5) * k2_p)
+    osd, opd = o_s * inv_d, o_p * inv_d
+    factor1 = vr * (-13.5 / d8)
+    radial = cons + factor1 * (term1 + term2)
+    factor3 = radial + (o_s + o_p) * inv_d * vr
+    Hr, Sr = cross(H, r), cross(S, r)
+    F = [factor3 * rd[k] + osd * (Hr[k] - hv[k]) + opd * (Sr[k] - hv[k]) for k in range(3)]
+    inv_m = 1.0 / m
+    a = [inv_m * F[k] for k in range(3)]
+    opdd, osdd = o_p * d, o_s * d
+    qp, qs = o_p * rs_p, o_s * rs_s
+    dl = [-(opdd * S[k] - qp * rd[k] - opd * h[k]) for k in range(3)]
+    th = [-(osdd * H[k] - qs * rd[k] - osd * h[k]) for k in range(3)]
+    return a + dl + th
+
+
+def block_flat(g):
+    r, hv, S, H, P, Q, d = _common(g)
+    m, hm, R, hR = g.const("m"), g.const("hm"), g.const("R"), g.const("hR")
+    k2f, hk2f = g.const("k2f"), g.const("hk2f")
+    rs_s = dot(r, Q)
+    rs_p = dot(r, P)
+    cfs = m * hk2f * powi(hR, 5) * (1.0 / 6.0)
+    cfp = hm * k2f * powi(R, 5) * (1.0 / 6.0)
+    d5 = powi(d, 5)
+    d7 = d5 * d * d
+    inv_d5 = 1.0 / d5
+    ofs = -6.0 * cfs * inv_d5 * rs_s
+    ofp = -6.0 * cfp * inv_d5 * rs_p
+    nsv2_p = dot(S, S)
+    nsv2_h = dot(H, H)
+    radial = (-3.0 / d5) * (cfp * nsv2_p + cfs * nsv2_h) + (15.0 / d7) * (cfs * rs_s * rs_s + cfp * rs_p * rs_p)
+    F = [radial * r[k] + ofp * S[k] + ofs * H[k] for k in range(3)]
+    inv_m = 1.0 / m
+    a = [inv_m * F[k] for k in range(3)]
+    rS, rH = cross(r, S), cross(r, H)
+    dl = [-(ofp * rS[k]) for k in range(3)]
+    th = [-(ofs * rH[k]) for k in range(3)]
+    return a + dl + th
+
+
+def block_gr(g):
+    r, hv, S, H, P, Q, d = _common(g)
+    m, hm, mg, hmg = g.const("m"), g.const("hm"), g.const("mg"), g.const("hmg")
+    moi, hmoi = g.const("moi"), g.const("hmoi")
+    c2 = g.const(C2)
+    fa = g.const(FA)
+    inv_d = 1.0 / d
+    nn = [c * inv_d for c in r]
+    vr = dot(r, hv) * inv_d
+    nv2 = dot(hv, hv)
+    mgs = hmg + mg
+    f = hmg * mg / (mgs * mgs)
+    d2 = d * d
+    mgd = mgs * inv_d
+    A = -mgs / (d2 * c2)
+    B = 1.0 + 3.0 * f
+    C = 2.0 * (2.0 + f) * mgd
+    DD = 1.5 * f
+    E = mgs / (d2 * c2) * 2.0 * (2.0 - f)
+    T1 = 0.75 * (12.0 + 29.0 * f) * (mgs * mgs / d2)
+    K2C = f * (3.0 - 4.0 * f)
+    K3C = (15.0 / 8.0) * f * (1.0 - 3.0 * f)
+    K4C = 1.5 * f * (3.0 - 4.0 * f)
+    K5C = 0.5 * f * (13.0 - 4.0 * f) * mgd
+    K6C = (2.0 + 25.0 * f + 2.0 * f * f) * mgd
+    A05 = A * -0.5
+    Pc = f * (15.0 + 4.0 * f)
+    Qc = (4.0 + 41.0 * f + 8.0 * f * f) * mgd
+    R3 = 3.0 * f * (3.0 + 2.0 * f)
+    vr2 = vr * vr
+    radial1 = A * (B * nv2 - C - DD * vr2)
+    o1 = E * vr
+    nv4 = nv2 * nv2
+    vr4 = vr2 * vr2
+    radial2 = A * (T1 + K2C * nv4 + K3C * vr4 - K4C * vr2 * nv2 - K5C * nv2 - K6C * vr2)
+    ortho2 = A05 * vr * (Pc * nv2 - Qc - R3 * vr2)
+    rad = radial1 + radial2
+    ort = o1 + ortho2
+    gacc = [rad * nn[k] + ort * hv[k] for k in range(3)]
+    # spin-orbit (general_relativity.rs:300-400, component-wise first term as written there)
+    sL = [hmoi * H[k] for k in range(3)]
+    pL = [moi * S[k] for k in range(3)]
+    mfm = hm - m
+    ms = [mfm * (pL[k] / m - sL[k] / hm) for k in range(3)]
+    t = [sL[k] + pL[k] for k in range(3)]
+    nxv = cross(nn, hv)
+    e1 = [6.0 * nn[k] * (nxv[k] * (2.0 * t[k] + ms[k])) for k in range(3)]
+    e7 = [7.0 * t[k] + 3.0 * ms[k] for k in range(3)]
+    e3s = [3.0 * t[k] + ms[k] for k in range(3)]
+    v3 = 3.0 * vr
+    hxe7 = cross(hv, e7)
+    nxe3 = cross(nn, e3s)
+    a = [gacc[k] + fa * (e1[k] - hxe7[k] + v3 * nxe3[k]) for k in range(3)]
+    # Kidder 1995 eq. 2.4a / 2.4b (general_relativity.rs:400-456)
+    mu = hm * m / (hm + m)
+    fm = 2.0 + 1.5 * m / hm
+    fm2 = 2.0 + 1.5 * hm / m
+    h = cross(r, hv)
+    lo = [mu * h[k] for k in range(3)]
+    h2 = cross(pL, sL)
+    sp3 = 3.0 * dot(nn, pL)
+    ss3 = 3.0 * dot(nn, sL)
+    loxs, loxp = cross(lo, sL), cross(lo, pL)
+    nxs, nxp = cross(nn, sL), cross(nn, pL)
+    th = [fa * (fm * loxs[k] - h2[k] + sp3 * nxs[k]) for k in range(3)]
+    dl = [fa * (fm2 * loxp[k] + h2[k] + ss3 * nxp[k]) for k in range(3)]
+    return a + dl + th
+
+
+OUTPUTS = ["a0", "a1", "a2", "dl0", "dl1", "dl2", "th0", "th1", "th2"]
+
+
+# ---------------------------------------------------------------------------
+# Emission
+# ---------------------------------------------------------------------------
+def _fmt(v):
+    r = repr(float(v))
+    return r if ("e" in r or "." in r or "n" in r) else r + ".0"
+
+
+def _expr(n, names):
+    a = [names[x.id] for x in n.args]
+    if n.op == "add":
+        return f"{a[0]} + {a[1]}"
+    if n.op == "sub":
+        return f"{a[0]} - {a[1]}"
+    if n.op == "mul":
+        return f"{a[0]} * {a[1]}"
+    if n.op == "div":
+        return f"{a[0]} / {a[1]}"
+    if n.op == "neg":
+        return f"-{a[0]}"
+    if n.op == "sqrt":
+        return f"sqrt({a[0]})"
+    raise ValueError(n.op)
+
+
+def _live(outputs):
+    """Nodes reachable from the outputs, in topological (creation) order."""
+    seen = set()
+    stack = list(outputs)
+    while stack:
+        n = stack.pop()
+        if n.id in seen:
+            continue
+        seen.add(n.id)
+        stack.extend(n.args)
+    return seen
+
+
+def emit(name, builder):
+    global GRAPH
+    GRAPH = g = Graph()
+    outs = builder(g)
+    live = _live(outs)
+    nodes = [n for n in g.nodes if n.id in live]
+    inputs = [n for n in g.inputs]
+    consts = [n for n in g.consts]
+    names = {}
+    for n in nodes:
+        if n.op == "lit":
+            names[n.id] = _fmt(n.val)
+        elif n.op == "in":
+            names[n.id] = f"in_{n.name}"
+        elif n.op == "cst":
+            names[n.id] = n.name if n.name in GLOBALS else f"c_{n.name}"
+        else:
+            names[n.id] = f"t{n.id}"
+    # which nodes carry an adjoint: depend on a differentiable input
+    grad = {}
+    for n in nodes:
+        if n.op == "in":
+            grad[n.id] = True
+        elif n.op in ("lit", "cst"):
+            grad[n.id] = False
+        else:
+            grad[n.id] = any(grad[a.id] for a in n.args)
+    in_names = [n.name for n in inputs]
+    cst_names = sorted({n.name for n in consts if n.name not in GLOBALS})
+    sig_in = ", ".join(f"double in_{x}" for x in in_names)
+    sig_c = ", ".join(f"double c_{x}" for x in cst_names)
+    fwd_lines = []
+    for n in nodes:
+        if n.op in ("lit", "in", "cst"):
+            continue
+        fwd_lines.append(f"    const double {names[n.id]} = {_expr(n, names)};")
+    out_names = [names[o.id] for o in outs]
+    L = []
+    L.append(f"// {name}: forward.  Outputs: a[3] (planet acceleration), dl[3] (planet dL/dt),")
+    L.append("// th[3] (dL/dt of the host due to this planet).")
+    L.append(f"__host__ __device__ __forceinline__ void {name}_fwd({sig_in},")
+    L.append(f"        {sig_c}, double* __restrict__ out) {{")
+    L.extend(fwd_lines)
+    for k, on in enumerate(out_names):
+        L.append(f"    out[{k}] = {on};")
+    L.append("}")
+    L.append("")
+    # VJP: recompute, then reverse sweep
+    L.append(f"// {name}: vector-Jacobian product.  bout[9] = adjoints of the outputs;")
+    L.append(f"// bin[{len(in_names)}] += adjoints of the inputs ({', '.join(in_names)}).")
+    L.append(f"__host__ __device__ __forceinline__ void {name}_vjp({sig_in},")
+    L.append(f"        {sig_c}, const double* __restrict__ bout, double* __restrict__ bin) {{")
+    L.extend(fwd_lines)
+    adj = {}          # node id -> adjoint variable name, once declared
+    body = []
+    seed = {}
+    for k, o in enumerate(outs):
+        if grad[o.id]:
+            seed.setdefault(o.id, []).append(f"bout[{k}]")
+
+    def contrib(n, term):
+        if not grad[n.id]:
+            return
+        if n.id in adj:
+            body.append(f"    {adj[n.id]} += {term};")
+        else:
+            adj[n.id] = f"b{n.id}" if n.op != "in" else f"b_{n.name}"
+            body.append(f"    double {adj[n.id]} = {term};")
+
+    for oid, terms in seed.items():
+        n = g.nodes[oid]
+        for tm in terms:
+            contrib(n, tm)
+    for n in reversed(nodes):
+        if n.op in ("lit", "in", "cst") or n.id not in adj:
+            continue
+        bn = adj[n.id]
+        a = n.args
+        nm = [names[x.id] for x in a]
+        if n.op == "add":
+            contrib(a[0], bn)
+            contrib(a[1], bn)
+        elif n.op == "sub":
+            contrib(a[0], bn)
+            contrib(a[1], f"-{bn}")
+        elif n.op == "neg":
+            contrib(a[0], f"-{bn}")
+        elif n.op == "mul":
+            if a[0].id == a[1].id:
+                contrib(a[0], f"2.0 * {bn} * {nm[0]}")
+            else:
+                contrib(a[0], f"{bn} * {nm[1]}")
+                contrib(a[1], f"{bn} * {nm[0]}")
+        elif n.op == "div":
+            contrib(a[0], f"{bn} / {nm[1]}")
+            contrib(a[1], f"-{bn} * {names[n.id]} / {nm[1]}")
+        elif n.op == "sqrt":
+            contrib(a[0], f"0.5 * {bn} / {names[n.id]}")
+    L.extend(body)
+    for k, n in enumerate(inputs):
+        if n.id in adj:
+            L.append(f"    bin[{k}] += {adj[n.id]};")
+    L.append("}")
+    L.append("")
+    return L, in_names, cst_names, len(fwd_lines), len(body)
+
+
+def generate():
+    blocks = [("adj_tides", block_tides), ("adj_flat", block_flat), ("adj_gr", block_gr)]
+    out = ["// adjoint_effects.cuh -- GENERATED by posidonius_gb300/adjoint_codegen.py; do not edit.",
+           "//",
+           "// Forward functions and vector-Jacobian products of the per-planet",
+           "// additional-effect blocks (constant-time-lag tides, oblate flattening,",
+           "// Kidder 1995 general relativity) in the formulation of the FAST build.",
+           "#pragma once",
+           "#include <cmath>",
+           "",
+           "#include \"adjoint_blocks.cuh\"",
+           "",
+           "namespace posi_adj {",
+           ""]
+    stats = []
+    for name, fn in blocks:
+        lines, ins, csts, nf, nr = emit(name, fn)
+        out.append(f"// inputs of {name}: {', '.join(ins)}")
+        out.append(f"// constants of {name}: {', '.join(csts)}")
+        out.extend(lines)
+        stats.append((name, nf, nr))
+    out.append("}  // namespace posi_adj")
+    out.append("")
+    return "\n".join(out), stats
+
+
+def main():
+    text, stats = generate()
+    with open(OUT, "w") as f:
+        f.write(text)
+    for name, nf, nr in stats:
+        print(f"{name}: {nf} forward statements, {nr} reverse statements")
+    print(OUT)
+
+
+if __name__ == "__main__":
+    main()

@@ -27,6 +27,7 @@ UNITS = [
     ("case_reader.cpp", ["-x", "cu", "-fmad=false"]),
     ("diagnostics.cu", ["-fmad=true"]),
     ("snapshot.cpp", ["-x", "cu", "-fmad=false"]),
+    ("adjoint.cu", ["-fmad=true"]),
 ]
 
 

@@ -51,4 +51,24 @@ inline int group_size_for(int64_t n) {
 
 constexpr int kBlockThreads = 128;
 
+// Adjoint kernels (adjoint.cu): which = 0 records a chunk's tape, 1 runs its
+// reverse sweep.  Systems of up to 8 bodies, Jacobi coordinates.
+struct AdjView {
+    int64_t n_sys, nmax, stride;
+    const double* bf;
+    const int64_t* bi;
+    const double* sf;
+    const int64_t* si;
+    const int32_t* list;
+    int32_t n_list;
+    double* tape;
+    double* lam;
+    double* grad;
+    int32_t* err;
+};
+int adjoint_group_size(int64_t n);
+constexpr int kAdjTapeFields = 27 + 2 * (1 + 9 * 10);  // per-step record of the adjoint, doubles per body
+cudaError_t launch_adjoint(const AdjView& v, int which, int64_t k_steps, int G, cudaStream_t stream);
+cudaError_t prepare_adjoint();
+
 }  // namespace posi

@@ -960,3 +960,210 @@ int posi_batch_last_timing(const posi_batch* b, double* ms, int64_t* launches) {
 }
 
 }  // extern "C"
+
+// ---- adjoint ----------------------------------------------------------------
+// Checkpointed reverse mode over a batch (no reference counterpart: the
+// reference has no derivatives; its users take finite differences).
+struct posi_adjoint {
+    posi_batch* b = nullptr;
+    int64_t n_steps = 0, every = 0, n_chunks = 0;
+    bool have_forward = false;
+    size_t bytes_bf = 0, bytes_sf = 0, bytes_si = 0, bytes_ck = 0;
+    char* d_ckpt = nullptr;   // n_chunks + 1 states: chunk starts, then the final state
+    double* d_tape = nullptr;  // step records of one chunk
+    double* d_lam = nullptr;
+    double* d_grad = nullptr;
+    int32_t* d_err = nullptr;
+    int32_t* d_list = nullptr;
+    std::vector<Bucket> buckets;  // by adjoint lane group
+    double fwd_ms = 0., bwd_ms = 0.;
+};
+
+namespace {
+void free_adjoint(posi_adjoint* a) {
+    if (!a) return;
+    cudaFree(a->d_ckpt); cudaFree(a->d_tape); cudaFree(a->d_lam); cudaFree(a->d_grad);
+    cudaFree(a->d_err); cudaFree(a->d_list);
+    delete a;
+}
+
+int adj_copy_state(posi_adjoint* a, int64_t slot, bool save) {
+    posi_batch* b = a->b;
+    char* base = a->d_ckpt + (size_t)slot * a->bytes_ck;
+    auto cp = [&](void* dst, const void* src, size_t n) { return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, b->stream); };
+    if (save) {
+        CK(cp(base, b->d_bf, a->bytes_bf));
+        CK(cp(base + a->bytes_bf, b->d_sf, a->bytes_sf));
+        CK(cp(base + a->bytes_bf + a->bytes_sf, b->d_si, a->bytes_si));
+    } else {
+        CK(cp(b->d_bf, base, a->bytes_bf));
+        CK(cp(b->d_sf, base + a->bytes_bf, a->bytes_sf));
+        CK(cp(b->d_si, base + a->bytes_bf + a->bytes_sf, a->bytes_si));
+    }
+    return POSI_OK;
+}
+
+posi::AdjView adj_view(const posi_adjoint* a, const Bucket& bk) {
+    const posi_batch* b = a->b;
+    posi::AdjView v;
+    v.n_sys = b->n_sys; v.nmax = b->nmax; v.stride = b->stride;
+    v.bf = b->d_bf; v.bi = b->d_bi; v.sf = b->d_sf; v.si = b->d_si;
+    v.list = a->d_list + bk.offset; v.n_list = bk.count;
+    v.tape = a->d_tape; v.lam = a->d_lam; v.grad = a->d_grad; v.err = a->d_err;
+    return v;
+}
+}  // namespace
+
+posi_adjoint* posi_adjoint_create(posi_batch* b, int64_t n_steps, int64_t checkpoint_every, int* status) {
+    auto fail = [&](int code, const std::string& msg, posi_adjoint* a) -> posi_adjoint* {
+        g_last_error = msg;
+        free_adjoint(a);
+        if (status) *status = code;
+        return nullptr;
+    };
+    if (!b || n_steps < 1 || checkpoint_every < 1) return fail(POSI_ERR_ARG, "bad arguments", nullptr);
+    std::vector<int64_t> si((size_t)b->n_sys * POSI_SI_COUNT);
+    if (batch_get(b, si.data(), nullptr, nullptr, nullptr, nullptr) != POSI_OK) return fail(POSI_ERR_CUDA, g_last_error, nullptr);
+    std::map<int, std::vector<int32_t>> by_g;
+    for (int64_t s = 0; s < b->n_sys; ++s) {
+        const int64_t* x = si.data() + s * POSI_SI_COUNT;
+        if (x[POSI_SI_COORDS] != POSI_JACOBI)
+            return fail(POSI_ERR_UNSUPPORTED, "the adjoint supports Jacobi coordinates only", nullptr);
+        if (x[POSI_SI_EVOLUTION] != 0)
+            return fail(POSI_ERR_UNSUPPORTED, "the adjoint supports non-evolving bodies only", nullptr);
+        const int G = posi::adjoint_group_size(x[POSI_SI_N]);
+        if (G == 0) return fail(POSI_ERR_UNSUPPORTED, "the adjoint supports systems of up to 8 bodies", nullptr);
+        by_g[G].push_back((int32_t)s);
+    }
+    posi_adjoint* a = new posi_adjoint();
+    a->b = b;
+    a->n_steps = n_steps;
+    a->every = checkpoint_every;
+    a->n_chunks = (n_steps + checkpoint_every - 1) / checkpoint_every;
+    const size_t nb = (size_t)b->stride;
+    a->bytes_bf = nb * POSI_BF_COUNT * sizeof(double);
+    a->bytes_sf = (size_t)b->n_sys * POSI_SF_COUNT * sizeof(double);
+    a->bytes_si = (size_t)b->n_sys * POSI_SI_COUNT * sizeof(int64_t);
+    a->bytes_ck = (a->bytes_bf + a->bytes_sf + a->bytes_si + 255) / 256 * 256;
+    std::vector<int32_t> list;
+    for (auto& kv : by_g) {
+        Bucket bk;
+        bk.G = kv.first;
+        bk.offset = (int32_t)list.size();
+        bk.count = (int32_t)kv.second.size();
+        list.insert(list.end(), kv.second.begin(), kv.second.end());
+        a->buckets.push_back(bk);
+    }
+    auto ok = [&](cudaError_t e) {
+        if (e != cudaSuccess) { g_last_error = cudaGetErrorString(e); return false; }
+        return true;
+    };
+    if (!ok(posi::prepare_adjoint()) ||
+        !ok(cudaMalloc(&a->d_ckpt, a->bytes_ck * (size_t)(a->n_chunks + 1))) ||
+        !ok(cudaMalloc(&a->d_tape, (size_t)checkpoint_every * posi::kAdjTapeFields * nb * sizeof(double))) ||
+        !ok(cudaMalloc(&a->d_lam, nb * 12 * sizeof(double))) || !ok(cudaMalloc(&a->d_grad, nb * 2 * sizeof(double))) ||
+        !ok(cudaMalloc(&a->d_err, (size_t)b->n_sys * sizeof(int32_t))) ||
+        !ok(cudaMalloc(&a->d_list, list.size() * sizeof(int32_t))) ||
+        !ok(cudaMemcpyAsync(a->d_list, list.data(), list.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream)) ||
+        !ok(cudaStreamSynchronize(b->stream)))
+        return fail(POSI_ERR_CUDA, g_last_error, a);
+    if (status) *status = POSI_OK;
+    return a;
+}
+
+void posi_adjoint_destroy(posi_adjoint* a) { free_adjoint(a); }
+
+int posi_adjoint_forward(posi_adjoint* a) {
+    if (!a) return POSI_ERR_ARG;
+    posi_batch* b = a->b;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, b->stream));
+    int rc = POSI_OK;
+    for (int64_t c = 0; c < a->n_chunks && rc == POSI_OK; ++c) {
+        if ((rc = adj_copy_state(a, c, true)) != POSI_OK) break;
+        const int64_t len = std::min(a->every, a->n_steps - c * a->every);
+        rc = posi_batch_iterate(b, len, len);
+    }
+    if (rc == POSI_OK) rc = adj_copy_state(a, a->n_chunks, true);
+    CK(cudaEventRecord(e1, b->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    a->fwd_ms = ms;
+    a->have_forward = rc == POSI_OK;
+    return rc;
+}
+
+int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_initial, double* grad,
+                          int32_t* system_flags) {
+    if (!a || !lam_final) return POSI_ERR_ARG;
+    if (!a->have_forward) {
+        g_last_error = "posi_adjoint_forward must run first";
+        return POSI_ERR_STATE;
+    }
+    posi_batch* b = a->b;
+    const int64_t nb = b->stride;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, b->stream));
+    // adjoint of the final state, [system][body][12] -> field-major
+    CK(cudaMemcpyAsync(b->d_stage, lam_final, (size_t)nb * 12 * sizeof(double), cudaMemcpyDefault, b->stream));
+    aos_to_soa<double><<<grid_for(nb * 12), 256, 0, b->stream>>>((const double*)b->d_stage, a->d_lam, nb, 12);
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(a->d_grad, 0, (size_t)nb * 2 * sizeof(double), b->stream));
+    CK(cudaMemsetAsync(a->d_err, 0, (size_t)b->n_sys * sizeof(int32_t), b->stream));
+    int rc = POSI_OK;
+    for (int64_t c = a->n_chunks - 1; c >= 0 && rc == POSI_OK; --c) {
+        if ((rc = adj_copy_state(a, c, false)) != POSI_OK) break;
+        const int64_t len = std::min(a->every, a->n_steps - c * a->every);
+        for (const Bucket& bk : a->buckets) CK(posi::launch_adjoint(adj_view(a, bk), 0, len, bk.G, b->stream));
+        for (const Bucket& bk : a->buckets) CK(posi::launch_adjoint(adj_view(a, bk), 1, len, bk.G, b->stream));
+    }
+    if (rc != POSI_OK) return rc;
+    CK(cudaEventRecord(e1, b->stream));
+    // results, [system][body][12] and [system][body][2]
+    if (lam_initial) {
+        soa_to_aos<double><<<grid_for(nb * 12), 256, 0, b->stream>>>(a->d_lam, (double*)b->d_stage, nb, 12);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(lam_initial, b->d_stage, (size_t)nb * 12 * sizeof(double), cudaMemcpyDefault, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+    }
+    if (grad) {
+        soa_to_aos<double><<<grid_for(nb * 2), 256, 0, b->stream>>>(a->d_grad, (double*)b->d_stage, nb, 2);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(grad, b->d_stage, (size_t)nb * 2 * sizeof(double), cudaMemcpyDefault, b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+    }
+    std::vector<int32_t> err((size_t)b->n_sys);
+    CK(cudaMemcpyAsync(err.data(), a->d_err, err.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream));
+    // leave the batch at the end of the forward run
+    if ((rc = adj_copy_state(a, a->n_chunks, false)) != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    a->bwd_ms = ms;
+    if (system_flags) {
+        // systems the forward run froze (collision, Roche limit, ejection...)
+        std::vector<int64_t> si((size_t)b->n_sys * POSI_SI_COUNT);
+        if ((rc = batch_get(b, si.data(), nullptr, nullptr, nullptr, nullptr)) != POSI_OK) return rc;
+        for (int64_t s = 0; s < b->n_sys; ++s) {
+            const int64_t st = si[(size_t)s * POSI_SI_COUNT + POSI_SI_STATUS] & POSI_SYS_FATAL_MASK;
+            system_flags[s] = err[(size_t)s] | ((st != 0 && st != POSI_SYS_COMPLETED) ? POSI_ADJ_FROZEN : 0);
+        }
+    }
+    return POSI_OK;
+}
+
+int posi_adjoint_last_timing(const posi_adjoint* a, double* forward_ms, double* backward_ms) {
+    if (!a) return POSI_ERR_ARG;
+    if (forward_ms) *forward_ms = a->fwd_ms;
+    if (backward_ms) *backward_ms = a->bwd_ms;
+    return POSI_OK;
+}

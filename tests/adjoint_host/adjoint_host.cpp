@@ -1,0 +1,55 @@
+// Host build of the adjoint building blocks, for the CPU tests of
+// tests/test_adjoint_blocks.py (finite-difference checks of every VJP).
+#include "../../posidonius_gb300/csrc/adjoint_effects.cuh"
+
+using namespace posi_adj;
+
+extern "C" {
+
+void h_stumpff6(double z, double* c) { stumpff6(z, c); }
+
+// in: r[3], v[3]; out: r1[3], v1[3]; returns X (NaN when not converged)
+double h_kepler_fwd(double mu, double dt, const double* r, const double* v, double* r1, double* v1) {
+    KeplerScalars s = kepler_scalars(mu, r, v);
+    bool ok = false;
+    double X = kepler_solve(s, dt, &ok);
+    if (!ok) return NAN;
+    kepler_apply(mu, dt, r, v, s, X, r1, v1);
+    return X;
+}
+
+void h_kepler_vjp(double mu, double dt, const double* r, const double* v, double X, const double* lr1,
+                  const double* lv1, double* lr0, double* lv0) {
+    kepler_vjp(mu, dt, r, v, X, lr1, lv1, lr0, lv0);
+}
+
+// in: 22 inputs (x y z hv S H P Q sig_p sig_h k2_p k2_h); c: m hm R hR k2f hk2f mg hmg moi hmoi
+void h_effects_fwd(int which, const double* in, const double* c, double* out) {
+    const double m = c[0], hm = c[1], R = c[2], hR = c[3], k2f = c[4], hk2f = c[5], mg = c[6], hmg = c[7];
+    const double moi = c[8], hmoi = c[9];
+    if (which == 0)
+        adj_tides_fwd(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
+                      in[13], in[14], in[15], in[16], in[17], in[18], in[19], in[20], in[21], R, hR, hm, m, out);
+    else if (which == 1)
+        adj_flat_fwd(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
+                     in[13], in[14], in[15], in[16], in[17], R, hR, hk2f, hm, k2f, m, out);
+    else
+        adj_gr_fwd(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
+                   in[13], in[14], in[15], in[16], in[17], hm, hmg, hmoi, m, mg, moi, out);
+}
+
+void h_effects_vjp(int which, const double* in, const double* c, const double* bout, double* bin) {
+    const double m = c[0], hm = c[1], R = c[2], hR = c[3], k2f = c[4], hk2f = c[5], mg = c[6], hmg = c[7];
+    const double moi = c[8], hmoi = c[9];
+    if (which == 0)
+        adj_tides_vjp(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
+                      in[13], in[14], in[15], in[16], in[17], in[18], in[19], in[20], in[21], R, hR, hm, m, bout, bin);
+    else if (which == 1)
+        adj_flat_vjp(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
+                     in[13], in[14], in[15], in[16], in[17], R, hR, hk2f, hm, k2f, m, bout, bin);
+    else
+        adj_gr_vjp(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
+                   in[13], in[14], in[15], in[16], in[17], hm, hmg, hmoi, m, mg, moi, bout, bin);
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+"""GPU: the adjoint of the WHFast + tides step against finite differences.
+
+Gradients of the differentiation workload's loss (squared final
+eccentricities, relative semi-major-axis drifts, relative planetary spin-rate
+changes) with respect to every body's dissipation factor and Love number and
+every planet's six initial orbital elements, by the checkpointed adjoint
+(torch autograd around posi_adjoint_*), against central finite differences of
+the same loss integrated by the forward kernel (relative step 1e-6 for the
+orbital elements).  At physical values the dissipation factors and Love
+numbers change the loss of a short run by less than its rounding level, so
+their gradients are checked with both amplified (same code path) and a
+1e-3 relative step, over which the loss is linear in them.
+"""
+import numpy as np
+import pytest
+
+import posidonius_gb300 as pg
+from posidonius_gb300 import adjoint as A, ensemble as E, layout as L
+
+pytestmark = pytest.mark.gpu
+
+# relative agreement with central differences where they resolve the derivative
+ADJ_FD_TOL = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from posidonius_gb300 import build
+    build.build()
+
+
+def _check(adj, fd, fd2):
+    """Worst ratio |adj - fd| / (ADJ_FD_TOL |fd| + 3 |fd - fd2|): the adjoint
+    must agree with the difference quotient fd to ADJ_FD_TOL relative, up to
+    the quotient's own error, estimated by its change |fd - fd2| between two
+    step sizes (rounding noise of the loss dominates where the derivative is
+    small)."""
+    adj, fd, fd2 = (x.reshape(x.shape[0], -1) for x in (adj, fd, fd2))
+    bound = ADJ_FD_TOL * np.abs(fd) + 3.0 * np.abs(fd - fd2) + 1e-300
+    return float((np.abs(adj - fd) / bound).max())
+
+
+@pytest.mark.parametrize("n_steps,every", [(120, 50), (400, 100)])
+def test_adjoint_elements_match_finite_differences(n_steps, every):
+    """Physical parameters: the orbital-element gradients (relative steps 1e-6
+    and 1e-5)."""
+    ens, el, ms, moi, ss = A.gradient_workload(4, seed=7)
+    sig = ens["body_f64"][:, :, L.BF_SIGMA].copy()
+    k2 = ens["body_f64"][:, :, L.BF_K2].copy()
+    loss, g_sig, g_k2, g_el, _, flags = A.adjoint_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, every)
+    assert not flags.any()
+    _, _, f_el = A.finite_difference_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, rel_step=1e-6)
+    _, _, f_el2 = A.finite_difference_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, rel_step=1e-5)
+    ref = A.loss_of_parameters(ens, el, sig, k2, ms, moi, ss, n_steps)
+    assert np.allclose(loss, ref, rtol=1e-10, atol=0)
+    err = _check(g_el, f_el, f_el2)
+    assert err <= 1.0, (err, g_el, f_el, f_el2)
+
+
+def test_adjoint_tidal_parameters_match_finite_differences():
+    """Dissipation factors x 5e7 and Love numbers x 1e6: their effect on the
+    loss becomes large enough for central differences (relative steps 1e-2
+    and 1e-3; the loss is linear in them over that range) to resolve it; the
+    code path is the one the physical parameters take.  A system the forward
+    run froze (Roche limit) is flagged and left out."""
+    ens, el, ms, moi, ss = A.gradient_workload(4, seed=11)
+    sig = ens["body_f64"][:, :, L.BF_SIGMA].copy() * 5e7
+    k2 = ens["body_f64"][:, :, L.BF_K2].copy() * 1e6
+    ens["body_f64"][:, :, L.BF_SIGMA] = sig
+    ens["body_f64"][:, :, L.BF_K2] = k2
+    n_steps, every = 300, 100
+    loss, g_sig, g_k2, g_el, _, flags = A.adjoint_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, every)
+    assert flags[2] == A.FLAG_FROZEN and flags.sum() == A.FLAG_FROZEN
+    keep = flags == 0
+    f_sig, f_k2, _ = A.finite_difference_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, rel_step_tidal=1e-2)
+    f_sig2, f_k22, _ = A.finite_difference_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, rel_step_tidal=1e-3)
+    errs = {"sigma": _check(g_sig[keep], f_sig[keep], f_sig2[keep]),
+            "k2": _check(g_k2[keep], f_k2[keep], f_k22[keep])}
+    assert max(errs.values()) <= 1.0, (errs, g_sig * sig, f_sig * sig, f_sig2 * sig, g_k2 * k2, f_k2 * k2,
+                                       f_k22 * k2)
+
+
+def test_adjoint_of_identity_seed_is_consistent():
+    """lam_final = e_k (one coordinate of one body): one backward run gives a
+    row of the Jacobian; central differences of that coordinate agree."""
+    ens, el, ms, moi, ss = A.gradient_workload(2, seed=3)
+    b = pg.Batch(ens, mode=pg.FAST)
+    b.initialize_physical_values()
+    base = b.get_state()
+    adj = A.Adjoint(b, 60, 25)
+    adj.forward()
+    lam = np.zeros((b.n_sys, b.nmax, 12))
+    lam[:, 2, 0] = 1.0  # x of planet 2
+    lam_i, grad = adj.backward(lam)
+    # derivative of x_2(T) with respect to vx of planet 1 at t = 0, by differences
+    h = 1e-6 * np.abs(base["body_f64"][:, 1, L.BF_VX]).max()
+    outs = []
+    for sgn in (1.0, -1.0):
+        st = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in base.items()}
+        st["body_f64"][:, 1, L.BF_VX] += sgn * h
+        b.set_state(st)
+        b.iterate(60, 60)
+        outs.append(b.get_state()["body_f64"][:, 2, L.BF_PX])
+    fd = (outs[0] - outs[1]) / (2 * h)
+    assert np.abs(lam_i[:, 1, 3] - fd).max() <= 1e-5 * np.abs(fd).max(), (lam_i[:, 1, 3], fd)
+
+
+def test_adjoint_rejects_unsupported_and_out_of_order():
+    ens = E.workload_single(seed=1, coords=L.DEMOCRATIC_HELIOCENTRIC)
+    b = pg.Batch(ens, mode=pg.FAST)
+    with pytest.raises(pg.PosiError) as e:
+        A.Adjoint(b, 10, 5)
+    assert e.value.status == L.ERR_UNSUPPORTED
+    ens = E.workload_single(seed=1)
+    b = pg.Batch(ens, mode=pg.FAST)
+    b.initialize_physical_values()
+    adj = A.Adjoint(b, 10, 5)
+    with pytest.raises(pg.PosiError) as e:
+        adj.backward(np.zeros((1, b.nmax, 12)))
+    assert e.value.status == L.ERR_STATE
