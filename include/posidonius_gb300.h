@@ -334,8 +334,10 @@ enum posi_adjoint_flag {
  * Host or device pointers (unified addressing). */
 int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_initial, double* grad,
                           int32_t* system_flags);
-/* CUDA-event times of the last forward and backward runs. */
-int posi_adjoint_last_timing(const posi_adjoint* a, double* forward_ms, double* backward_ms);
+/* CUDA-event times of the last forward and backward runs, and the backward
+ * run's split into chunk re-integration (record) and reverse sweeps. */
+int posi_adjoint_last_timing(const posi_adjoint* a, double* forward_ms, double* backward_ms, double* record_ms,
+                             double* reverse_ms);
 
 #ifdef __cplusplus
 }

@@ -58,7 +58,7 @@ SIGNATURES = {
     "posi_adjoint_destroy": (None, [_vp]),
     "posi_adjoint_forward": (ctypes.c_int, [_vp]),
     "posi_adjoint_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
-    "posi_adjoint_last_timing": (ctypes.c_int, [_vp, _f64p, _f64p]),
+    "posi_adjoint_last_timing": (ctypes.c_int, [_vp, _f64p, _f64p, _f64p, _f64p]),
 }
 
 _lib = None

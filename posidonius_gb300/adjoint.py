@@ -90,9 +90,10 @@ class Adjoint:
         return lam_initial, grad
 
     def last_timing(self):
-        f, b = ctypes.c_double(), ctypes.c_double()
-        check(lib().posi_adjoint_last_timing(self._h, ctypes.byref(f), ctypes.byref(b)))
-        return f.value, b.value
+        """(forward_ms, backward_ms, record_ms, reverse_ms) of the last runs."""
+        v = [ctypes.c_double() for _ in range(4)]
+        check(lib().posi_adjoint_last_timing(self._h, *[ctypes.byref(x) for x in v]))
+        return tuple(x.value for x in v)
 
 
 def _torch():
@@ -309,17 +310,13 @@ def _state_arrays(elements, sigma, k2, masses, moi, star_spin):
     return r0, v0, L0, S0
 
 
-def loss_of_parameters(ens, elements, sigma, k2, masses, moi, star_spin, n_steps, mode=None):
-    """Per-system loss after n_steps for parameter sets given per system (no
-    gradient): one batched GPU run of all of them."""
-    import posidonius_gb300 as pg
-    torch = _torch()
-    batch = pg.Batch(ens, mode=pg.FAST if mode is None else mode)
-    batch.initialize_physical_values()
-    st = batch.get_state()
+def initial_ensemble(ens, elements, sigma, k2, masses, moi, star_spin):
+    """Copy of the workload ensemble with the initial state built from the
+    given parameters (one parameter set per system)."""
     r0, v0, L0, S0 = _state_arrays(elements, sigma, k2, masses, moi, star_spin)
+    out = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in ens.items()}
     n = r0.shape[1]
-    bf = st["body_f64"]
+    bf = out["body_f64"]
     bf[:, :n, L.POS] = r0
     bf[:, :n, L.VEL] = v0
     bf[:, :n, L.ANG] = L0
@@ -327,22 +324,48 @@ def loss_of_parameters(ens, elements, sigma, k2, masses, moi, star_spin, n_steps
     bf[:, :n, L.BF_NSV2] = np.sum(S0 ** 2, axis=-1)
     bf[:, :n, L.BF_SIGMA] = sigma
     bf[:, :n, L.BF_K2] = k2
-    batch.set_state(st)
-    batch.iterate(n_steps, min(n_steps, 1000))
-    fin = batch.get_state()["body_f64"][:, :n]
+    return out
+
+
+def loss_from_final(final_body_f64, elements, masses, moi):
+    """Per-system loss of final states [S, n, BF_COUNT] (numpy)."""
+    torch = _torch()
     t = lambda x: torch.as_tensor(np.asarray(x), dtype=torch.float64)
+    n = np.asarray(masses).shape[1]
+    fin = final_body_f64[:, :n]
     with torch.no_grad():
         el = t(elements)
         a0 = el[..., 0]
         spin0 = torch.linalg.norm(pseudo_synchronous_spin(el[..., 0], el[..., 1], el[..., 2], el[..., 4],
                                                           t(masses)[:, :1], t(masses)[:, 1:]), dim=-1)
         out = tidal_loss(t(fin[..., L.POS]), t(fin[..., L.VEL]), t(fin[..., L.ANG]), t(masses), t(moi), a0, spin0)
-    batch.close()
     return out.numpy()
 
 
+def gpu_runner(mode=None):
+    """Runner for loss_of_parameters: integrates an ensemble on the GPU and
+    returns the final body_f64."""
+    def run(ens, n_steps):
+        import posidonius_gb300 as pg
+        batch = pg.Batch(ens, mode=pg.FAST if mode is None else mode)
+        batch.initialize_physical_values()
+        batch.iterate(n_steps, min(n_steps, 1000))
+        fin = batch.get_state()["body_f64"]
+        batch.close()
+        return fin
+    return run
+
+
+def loss_of_parameters(ens, elements, sigma, k2, masses, moi, star_spin, n_steps, mode=None, runner=None):
+    """Per-system loss after n_steps for parameter sets given per system (no
+    gradient): one batched run of all of them (GPU unless a runner is given)."""
+    run = runner or gpu_runner(mode)
+    e0 = initial_ensemble(ens, elements, sigma, k2, masses, moi, star_spin)
+    return loss_from_final(run(e0, n_steps), elements, masses, moi)
+
+
 def finite_difference_gradient(ens, elements, sigma, k2, masses, moi, star_spin, n_steps, rel_step=1e-6,
-                               rel_step_tidal=None, mode=None):
+                               rel_step_tidal=None, mode=None, runner=None):
     """Central finite differences of the per-system loss with respect to
     (sigma [nb], k2 [nb], elements [np, 6]) of every system, all perturbed
     copies integrated in one batch.  Returns (d/dsigma, d/dk2, d/delements).
@@ -382,7 +405,8 @@ def finite_difference_gradient(ens, elements, sigma, k2, masses, moi, star_spin,
                     el2[row, b, c] += sgn * h
                 steps[s, j] = h
     loss = loss_of_parameters(E2, el2, sg2, k22, np.repeat(masses, reps, axis=0), np.repeat(moi, reps, axis=0),
-                              np.repeat(star_spin, reps, axis=0), n_steps, mode=mode).reshape(S, P, 2)
+                              np.repeat(star_spin, reps, axis=0), n_steps, mode=mode,
+                              runner=runner).reshape(S, P, 2)
     g = (loss[..., 0] - loss[..., 1]) / (2.0 * steps)
     g = np.where(steps > 0, g, 0.0)
     return g[:, :nb], g[:, nb:2 * nb], g[:, 2 * nb:].reshape(S, npl, 6)

@@ -336,14 +336,24 @@ def _live(outputs):
     return seen
 
 
+PRE_INPUTS = {"x", "y", "z", "sig_p", "sig_h", "k2_p", "k2_h"}
+
+
 def emit(name, builder):
+    """Emit, for one block, the split the midpoint loop needs: a 'pre' part
+    (everything that depends only on the heliocentric position and the tidal
+    parameters, fixed during a half kick) evaluated once per half kick, and an
+    'iter' part evaluated per midpoint iteration from the pre values and the
+    velocity / spin inputs; with the reverse sweeps of both (the iteration
+    sweeps accumulate the adjoints of the pre values, which one pre sweep per
+    half kick then takes back to the position and parameters)."""
     global GRAPH
     GRAPH = g = Graph()
     outs = builder(g)
     live = _live(outs)
     nodes = [n for n in g.nodes if n.id in live]
-    inputs = [n for n in g.inputs]
-    consts = [n for n in g.consts]
+    inputs = list(g.inputs)
+    consts = list(g.consts)
     names = {}
     for n in nodes:
         if n.op == "lit":
@@ -354,102 +364,161 @@ def emit(name, builder):
             names[n.id] = n.name if n.name in GLOBALS else f"c_{n.name}"
         else:
             names[n.id] = f"t{n.id}"
-    # which nodes carry an adjoint: depend on a differentiable input
     grad = {}
+    pre = {}
     for n in nodes:
         if n.op == "in":
             grad[n.id] = True
+            pre[n.id] = n.name in PRE_INPUTS
         elif n.op in ("lit", "cst"):
             grad[n.id] = False
+            pre[n.id] = True
         else:
             grad[n.id] = any(grad[a.id] for a in n.args)
-    in_names = [n.name for n in inputs]
+            pre[n.id] = all(pre[a.id] for a in n.args)
+    pre_in = [n for n in inputs if n.name in PRE_INPUTS]
+    it_in = [n for n in inputs if n.name not in PRE_INPUTS]
     cst_names = sorted({n.name for n in consts if n.name not in GLOBALS})
-    sig_in = ", ".join(f"double in_{x}" for x in in_names)
+    # pre values the iteration part reads (non-literal, non-constant pre nodes
+    # used by iteration nodes or returned as outputs)
+    it_nodes = [n for n in nodes if not pre[n.id]]
+    pre_nodes = [n for n in nodes if pre[n.id] and n.op not in ("lit", "cst")]
+    used = []
+    seen = set()
+    for n in it_nodes:
+        for a in n.args:
+            if pre[a.id] and a.op not in ("lit", "cst") and a.id not in seen:
+                seen.add(a.id)
+                used.append(a)
+    for o in outs:
+        if pre[o.id] and o.op not in ("lit", "cst") and o.id not in seen:
+            seen.add(o.id)
+            used.append(o)
+    slot = {n.id: k for k, n in enumerate(used)}
+    NPRE = len(used)
     sig_c = ", ".join(f"double c_{x}" for x in cst_names)
-    fwd_lines = []
-    for n in nodes:
-        if n.op in ("lit", "in", "cst"):
-            continue
-        fwd_lines.append(f"    const double {names[n.id]} = {_expr(n, names)};")
-    out_names = [names[o.id] for o in outs]
+    sig_pre_in = ", ".join(f"double in_{n.name}" for n in pre_in)
+    sig_it_in = ", ".join(f"double in_{n.name}" for n in it_in)
     L = []
-    L.append(f"// {name}: forward.  Outputs: a[3] (planet acceleration), dl[3] (planet dL/dt),")
-    L.append("// th[3] (dL/dt of the host due to this planet).")
-    L.append(f"__host__ __device__ __forceinline__ void {name}_fwd({sig_in},")
-    L.append(f"        {sig_c}, double* __restrict__ out) {{")
-    L.extend(fwd_lines)
-    for k, on in enumerate(out_names):
-        L.append(f"    out[{k}] = {on};")
+    L.append(f"constexpr int {name}_NPRE = {NPRE};")
+    L.append("")
+    # ---- pre forward
+    L.append(f"// {name}: values fixed during a half kick (position, tidal parameters).")
+    L.append(f"__host__ __device__ __forceinline__ void {name}_pre({sig_pre_in},")
+    L.append(f"        {sig_c}, double* __restrict__ pre) {{")
+    for n in pre_nodes:
+        if n.op == "in":
+            continue
+        L.append(f"    const double {names[n.id]} = {_expr(n, names)};")
+    for n in used:
+        L.append(f"    pre[{slot[n.id]}] = {names[n.id]};")
     L.append("}")
     L.append("")
-    # VJP: recompute, then reverse sweep
-    L.append(f"// {name}: vector-Jacobian product.  bout[9] = adjoints of the outputs;")
-    L.append(f"// bin[{len(in_names)}] += adjoints of the inputs ({', '.join(in_names)}).")
-    L.append(f"__host__ __device__ __forceinline__ void {name}_vjp({sig_in},")
-    L.append(f"        {sig_c}, const double* __restrict__ bout, double* __restrict__ bin) {{")
-    L.extend(fwd_lines)
-    adj = {}          # node id -> adjoint variable name, once declared
-    body = []
-    seed = {}
+    # ---- iteration forward
+    def it_names():
+        nm = dict(names)
+        for n in used:
+            nm[n.id] = f"pre[{slot[n.id]}]"
+        return nm
+    nm_it = it_names()
+    it_fwd = [f"    const double {nm_it[n.id]} = {_expr(n, nm_it)};" for n in it_nodes if n.op != "in"]
+    L.append(f"// {name}: one midpoint iteration.  Outputs: a[3] (planet acceleration),")
+    L.append("// dl[3] (planet dL/dt), th[3] (dL/dt of the host due to this planet).")
+    L.append(f"__host__ __device__ __forceinline__ void {name}_iter(const double* __restrict__ pre, {sig_it_in},")
+    L.append(f"        {sig_c}, double* __restrict__ out) {{")
+    L.extend(it_fwd)
     for k, o in enumerate(outs):
-        if grad[o.id]:
-            seed.setdefault(o.id, []).append(f"bout[{k}]")
+        L.append(f"    out[{k}] = {nm_it[o.id]};")
+    L.append("}")
+    L.append("")
 
-    def contrib(n, term):
-        if not grad[n.id]:
-            return
-        if n.id in adj:
-            body.append(f"    {adj[n.id]} += {term};")
-        else:
-            adj[n.id] = f"b{n.id}" if n.op != "in" else f"b_{n.name}"
-            body.append(f"    double {adj[n.id]} = {term};")
+    def reverse(node_list, nmap, seeds, boundary_pre):
+        """Reverse sweep over node_list; contributions to pre values go to
+        bpre[slot] when boundary_pre, else follow the nodes."""
+        adj = {}
+        body = []
 
-    for oid, terms in seed.items():
-        n = g.nodes[oid]
-        for tm in terms:
-            contrib(n, tm)
-    for n in reversed(nodes):
-        if n.op in ("lit", "in", "cst") or n.id not in adj:
-            continue
-        bn = adj[n.id]
-        a = n.args
-        nm = [names[x.id] for x in a]
-        if n.op == "add":
-            contrib(a[0], bn)
-            contrib(a[1], bn)
-        elif n.op == "sub":
-            contrib(a[0], bn)
-            contrib(a[1], f"-{bn}")
-        elif n.op == "neg":
-            contrib(a[0], f"-{bn}")
-        elif n.op == "mul":
-            if a[0].id == a[1].id:
-                contrib(a[0], f"2.0 * {bn} * {nm[0]}")
+        def contrib(n, term):
+            if not grad[n.id] or n.op in ("lit", "cst"):
+                return
+            if boundary_pre and pre[n.id]:
+                body.append(f"    bpre[{slot[n.id]}] += {term};")
+                return
+            if n.id in adj:
+                body.append(f"    {adj[n.id]} += {term};")
             else:
-                contrib(a[0], f"{bn} * {nm[1]}")
-                contrib(a[1], f"{bn} * {nm[0]}")
-        elif n.op == "div":
-            contrib(a[0], f"{bn} / {nm[1]}")
-            contrib(a[1], f"-{bn} * {names[n.id]} / {nm[1]}")
-        elif n.op == "sqrt":
-            contrib(a[0], f"0.5 * {bn} / {names[n.id]}")
+                adj[n.id] = f"b{n.id}" if n.op != "in" else f"b_{n.name}"
+                body.append(f"    double {adj[n.id]} = {term};")
+
+        for n, term in seeds:
+            contrib(n, term)
+        for n in reversed(node_list):
+            if n.op in ("lit", "in", "cst") or n.id not in adj:
+                continue
+            bn = adj[n.id]
+            a = n.args
+            an = [nmap[x.id] for x in a]
+            if n.op == "add":
+                contrib(a[0], bn)
+                contrib(a[1], bn)
+            elif n.op == "sub":
+                contrib(a[0], bn)
+                contrib(a[1], f"-{bn}")
+            elif n.op == "neg":
+                contrib(a[0], f"-{bn}")
+            elif n.op == "mul":
+                if a[0].id == a[1].id:
+                    contrib(a[0], f"2.0 * {bn} * {an[0]}")
+                else:
+                    contrib(a[0], f"{bn} * {an[1]}")
+                    contrib(a[1], f"{bn} * {an[0]}")
+            elif n.op == "div":
+                contrib(a[0], f"{bn} / {an[1]}")
+                contrib(a[1], f"-{bn} * {nmap[n.id]} / {an[1]}")
+            elif n.op == "sqrt":
+                contrib(a[0], f"0.5 * {bn} / {nmap[n.id]}")
+        return body, adj
+
+    # ---- iteration VJP
+    seeds = [(o, f"bout[{k}]") for k, o in enumerate(outs)]
+    body, adj = reverse(it_nodes, nm_it, seeds, True)
+    L.append(f"// {name}: VJP of one iteration.  bin[{len(it_in)}] += adjoints of ({', '.join(n.name for n in it_in)});")
+    L.append(f"// bpre[{name}_NPRE] += adjoints of the pre values.")
+    L.append(f"__host__ __device__ __forceinline__ void {name}_iter_vjp(const double* __restrict__ pre, {sig_it_in},")
+    L.append(f"        {sig_c}, const double* __restrict__ bout, double* __restrict__ bin, double* __restrict__ bpre) {{")
+    L.extend(it_fwd)
     L.extend(body)
-    for k, n in enumerate(inputs):
+    for k, n in enumerate(it_in):
         if n.id in adj:
             L.append(f"    bin[{k}] += {adj[n.id]};")
     L.append("}")
     L.append("")
-    return L, in_names, cst_names, len(fwd_lines), len(body)
+    # ---- pre VJP
+    pre_fwd = [f"    const double {names[n.id]} = {_expr(n, names)};" for n in pre_nodes if n.op != "in"]
+    seeds = [(n, f"bpre[{slot[n.id]}]") for n in used]
+    body, adj = reverse(pre_nodes, names, seeds, False)
+    L.append(f"// {name}: VJP of the pre values.  bin[{len(pre_in)}] += adjoints of ({', '.join(n.name for n in pre_in)}).")
+    L.append(f"__host__ __device__ __forceinline__ void {name}_pre_vjp({sig_pre_in},")
+    L.append(f"        {sig_c}, const double* __restrict__ bpre, double* __restrict__ bin) {{")
+    L.extend(pre_fwd)
+    L.extend(body)
+    for k, n in enumerate(pre_in):
+        if n.id in adj:
+            L.append(f"    bin[{k}] += {adj[n.id]};")
+    L.append("}")
+    L.append("")
+    return L, [n.name for n in pre_in], [n.name for n in it_in], cst_names, NPRE, len(it_fwd), len(body)
 
 
 def generate():
     blocks = [("adj_tides", block_tides), ("adj_flat", block_flat), ("adj_gr", block_gr)]
     out = ["// adjoint_effects.cuh -- GENERATED by posidonius_gb300/adjoint_codegen.py; do not edit.",
            "//",
-           "// Forward functions and vector-Jacobian products of the per-planet",
-           "// additional-effect blocks (constant-time-lag tides, oblate flattening,",
-           "// Kidder 1995 general relativity) in the formulation of the FAST build.",
+           "// Per-planet additional-effect blocks (constant-time-lag tides, oblate",
+           "// flattening, Kidder 1995 general relativity) in the formulation of the FAST",
+           "// build, split for the implicit-midpoint loop: <block>_pre (once per half",
+           "// kick: position and tidal-parameter terms), <block>_iter (per iteration),",
+           "// and the reverse sweeps <block>_iter_vjp / <block>_pre_vjp.",
            "#pragma once",
            "#include <cmath>",
            "",
@@ -459,11 +528,11 @@ def generate():
            ""]
     stats = []
     for name, fn in blocks:
-        lines, ins, csts, nf, nr = emit(name, fn)
-        out.append(f"// inputs of {name}: {', '.join(ins)}")
-        out.append(f"// constants of {name}: {', '.join(csts)}")
+        lines, pin, iin, csts, npre, nit, nrev = emit(name, fn)
+        out.append(f"// {name}: pre inputs ({', '.join(pin)}); iteration inputs ({', '.join(iin)});")
+        out.append(f"// constants ({', '.join(csts)})")
         out.extend(lines)
-        stats.append((name, nf, nr))
+        stats.append((name, npre, nit, nrev))
     out.append("}  // namespace posi_adj")
     out.append("")
     return "\n".join(out), stats
@@ -473,8 +542,8 @@ def main():
     text, stats = generate()
     with open(OUT, "w") as f:
         f.write(text)
-    for name, nf, nr in stats:
-        print(f"{name}: {nf} forward statements, {nr} reverse statements")
+    for name, npre, nit, nrev in stats:
+        print(f"{name}: {npre} pre values, {nit} iteration statements, {nrev} pre-reverse statements")
     print(OUT)
 
 

@@ -210,22 +210,33 @@ struct AdjSys {
         }
     }
 
-    // Inputs of the effect blocks of this planet (host values from the card).
-    __device__ __forceinline__ void block_inputs(const double pos[3], const double vc[3], const double Sc[3],
-                                                 const double Sp[3], double in[22]) const {
-        in[0] = pos[0] - card[AC_PX]; in[1] = pos[1] - card[AC_PY]; in[2] = pos[2] - card[AC_PZ];
-        in[3] = vc[0] - card[AC_VX]; in[4] = vc[1] - card[AC_VY]; in[5] = vc[2] - card[AC_VZ];
-        in[6] = Sc[0]; in[7] = Sc[1]; in[8] = Sc[2];
-        in[9] = card[AC_H0]; in[10] = card[AC_H1]; in[11] = card[AC_H2];
-        in[12] = Sp[0]; in[13] = Sp[1]; in[14] = Sp[2];
-        in[15] = card[AC_Q0]; in[16] = card[AC_Q1]; in[17] = card[AC_Q2];
-        in[18] = sig; in[19] = card[AC_SIG]; in[20] = k2; in[21] = card[AC_K2];
+    // ---- additional effects (src/particles/universe.rs:428-538) ----
+    // Per-planet block values fixed during a half kick (the heliocentric
+    // position and the tidal parameters), from the host card.
+    struct Pre {
+        double t[adj_tides_NPRE], f[adj_flat_NPRE], g[adj_gr_NPRE];
+    };
+    __device__ __forceinline__ bool tides_on() const { return tides && tk == POSI_EFFECT_ORBITING; }
+    __device__ __forceinline__ bool flat_on() const { return flat && fk == POSI_EFFECT_ORBITING; }
+    __device__ __forceinline__ bool gr_on() const { return gr && gk == POSI_EFFECT_ORBITING; }
+
+    __device__ __forceinline__ void helio(const double pos[3], double x[3]) const {
+        x[0] = pos[0] - card[AC_PX]; x[1] = pos[1] - card[AC_PY]; x[2] = pos[2] - card[AC_PZ];
+    }
+    __device__ void pre_fwd(const double pos[3], Pre& pr) const {
+        if (!planet()) return;
+        double x[3];
+        helio(pos, x);
+        const double hm = card[AC_M], hR = card[AC_R], hmg = card[AC_MG], hmoi = card[AC_MOI], hk2f = card[AC_K2F];
+        if (tides_on()) adj_tides_pre(x[0], x[1], x[2], sig, card[AC_SIG], k2, card[AC_K2], R, hR, hm, m, pr.t);
+        if (flat_on()) adj_flat_pre(x[0], x[1], x[2], R, hR, hk2f, hm, k2f, m, pr.f);
+        if (gr_on()) adj_gr_pre(x[0], x[1], x[2], hm, hmg, hmoi, m, mg, moi, pr.g);
     }
 
-    // One evaluation of the additional effects (src/particles/universe.rs:428-538):
-    // spins Sc = Lc / I, the r.Omega products from Sp; outputs a_add, dL/dt.
-    __device__ void effects_fwd(const double pos[3], const double vc[3], const double Lc[3], const double Sp[3],
-                                double a[3], double dl[3], double Sc[3]) {
+    // One evaluation: spins Sc = Lc / I, the r.Omega products from Sp;
+    // outputs a_add, dL/dt.
+    __device__ void effects_fwd(const Pre& pr, const double vc[3], const double Lc[3], const double Sp[3], double a[3],
+                                double dl[3], double Sc[3]) {
         spin_of(Lc, Sc);
         sync();
         if (is_host) {
@@ -238,25 +249,25 @@ struct AdjSys {
         dl[0] = dl[1] = dl[2] = 0.;
         double th[3] = {0., 0., 0.};
         if (planet()) {
-            double in[22];
-            block_inputs(pos, vc, Sc, Sp, in);
+            const double h0 = vc[0] - card[AC_VX], h1 = vc[1] - card[AC_VY], h2 = vc[2] - card[AC_VZ];
+            const double H0 = card[AC_H0], H1 = card[AC_H1], H2 = card[AC_H2];
+            const double Q0 = card[AC_Q0], Q1 = card[AC_Q1], Q2 = card[AC_Q2];
             const double hm = card[AC_M], hR = card[AC_R], hmg = card[AC_MG], hmoi = card[AC_MOI],
                          hk2f = card[AC_K2F];
             double out[9];
-            if (tides && tk == POSI_EFFECT_ORBITING) {
-                adj_tides_fwd(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11],
-                              in[12], in[13], in[14], in[15], in[16], in[17], in[18], in[19], in[20], in[21], R, hR,
-                              hm, m, out);
+            if (tides_on()) {
+                adj_tides_iter(pr.t, h0, h1, h2, Sc[0], Sc[1], Sc[2], H0, H1, H2, Sp[0], Sp[1], Sp[2], Q0, Q1, Q2, R, hR,
+                               hm, m, out);
                 for (int c = 0; c < 3; ++c) { a[c] += out[c]; dl[c] += out[3 + c]; th[c] += out[6 + c]; }
             }
-            if (flat && fk == POSI_EFFECT_ORBITING) {
-                adj_flat_fwd(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11],
-                             in[12], in[13], in[14], in[15], in[16], in[17], R, hR, hk2f, hm, k2f, m, out);
+            if (flat_on()) {
+                adj_flat_iter(pr.f, h0, h1, h2, Sc[0], Sc[1], Sc[2], H0, H1, H2, Sp[0], Sp[1], Sp[2], Q0, Q1, Q2, R, hR,
+                              hk2f, hm, k2f, m, out);
                 for (int c = 0; c < 3; ++c) { a[c] += out[c]; dl[c] += out[3 + c]; th[c] += out[6 + c]; }
             }
-            if (gr && gk == POSI_EFFECT_ORBITING) {
-                adj_gr_fwd(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11],
-                           in[12], in[13], in[14], in[15], in[16], in[17], hm, hmg, hmoi, m, mg, moi, out);
+            if (gr_on()) {
+                adj_gr_iter(pr.g, h0, h1, h2, Sc[0], Sc[1], Sc[2], H0, H1, H2, Sp[0], Sp[1], Sp[2], Q0, Q1, Q2, hm, hmg,
+                            hmoi, m, mg, moi, out);
                 for (int c = 0; c < 3; ++c) { a[c] += out[c]; dl[c] += out[3 + c]; th[c] += out[6 + c]; }
             }
             for (int c = 0; c < 3; ++c) {
@@ -271,11 +282,20 @@ struct AdjSys {
         sync();
     }
 
-    // VJP of effects_fwd: adjoints la, ld of (a, dl) in; adjoints of vc, Sc,
-    // Sp out (assigned), position adjoint and parameter gradients accumulated.
-    __device__ void effects_vjp(const double pos[3], const double vc[3], const double Sc[3], const double Sp[3],
-                                const double la[3], const double ld[3], double lvc[3], double lSc[3], double lSp[3],
-                                double lpos[3], double& gsig, double& gk2) {
+    // Bpre: adjoints of the pre values, accumulated over the iterations.
+    struct Bpre {
+        double t[adj_tides_NPRE], f[adj_flat_NPRE], g[adj_gr_NPRE];
+        __device__ void zero() {
+            for (int k = 0; k < adj_tides_NPRE; ++k) t[k] = 0.;
+            for (int k = 0; k < adj_flat_NPRE; ++k) f[k] = 0.;
+            for (int k = 0; k < adj_gr_NPRE; ++k) g[k] = 0.;
+        }
+    };
+
+    // VJP of one effects_fwd evaluation: adjoints la, ld of (a, dl) in;
+    // adjoints of vc, Sc, Sp out (assigned); the pre adjoints accumulated.
+    __device__ void effects_vjp(const Pre& pr, Bpre& bp, const double vc[3], const double Sc[3], const double Sp[3],
+                                const double la[3], const double ld[3], double lvc[3], double lSc[3], double lSp[3]) {
         sync();
         if (is_host) {
             card[AC_VX] = vc[0]; card[AC_VY] = vc[1]; card[AC_VZ] = vc[2];
@@ -287,52 +307,75 @@ struct AdjSys {
         sync();
         for (int c = 0; c < 3; ++c) lvc[c] = lSc[c] = lSp[c] = 0.;
         if (planet()) {
-            double in[22];
-            block_inputs(pos, vc, Sc, Sp, in);
+            const double h0 = vc[0] - card[AC_VX], h1 = vc[1] - card[AC_VY], h2 = vc[2] - card[AC_VZ];
+            const double H0 = card[AC_H0], H1 = card[AC_H1], H2 = card[AC_H2];
+            const double Q0 = card[AC_Q0], Q1 = card[AC_Q1], Q2 = card[AC_Q2];
             const double hm = card[AC_M], hR = card[AC_R], hmg = card[AC_MG], hmoi = card[AC_MOI],
                          hk2f = card[AC_K2F];
-            double bout[9], bin[22];
+            double bout[9], bin[15];
             for (int c = 0; c < 3; ++c) {
                 bout[c] = la[c] - mr * card[AC_LA0 + c];
                 bout[3 + c] = ld[c];
                 bout[6 + c] = card[AC_LD0 + c];
             }
-            for (int k = 0; k < 22; ++k) bin[k] = 0.;
-            if (tides && tk == POSI_EFFECT_ORBITING)
-                adj_tides_vjp(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11],
-                              in[12], in[13], in[14], in[15], in[16], in[17], in[18], in[19], in[20], in[21], R, hR,
-                              hm, m, bout, bin);
-            if (flat && fk == POSI_EFFECT_ORBITING)
-                adj_flat_vjp(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11],
-                             in[12], in[13], in[14], in[15], in[16], in[17], R, hR, hk2f, hm, k2f, m, bout, bin);
-            if (gr && gk == POSI_EFFECT_ORBITING)
-                adj_gr_vjp(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11],
-                           in[12], in[13], in[14], in[15], in[16], in[17], hm, hmg, hmoi, m, mg, moi, bout, bin);
+            for (int k = 0; k < 15; ++k) bin[k] = 0.;
+            if (tides_on())
+                adj_tides_iter_vjp(pr.t, h0, h1, h2, Sc[0], Sc[1], Sc[2], H0, H1, H2, Sp[0], Sp[1], Sp[2], Q0, Q1, Q2, R,
+                                   hR, hm, m, bout, bin, bp.t);
+            if (flat_on())
+                adj_flat_iter_vjp(pr.f, h0, h1, h2, Sc[0], Sc[1], Sc[2], H0, H1, H2, Sp[0], Sp[1], Sp[2], Q0, Q1, Q2, R,
+                                  hR, hk2f, hm, k2f, m, bout, bin, bp.f);
+            if (gr_on())
+                adj_gr_iter_vjp(pr.g, h0, h1, h2, Sc[0], Sc[1], Sc[2], H0, H1, H2, Sp[0], Sp[1], Sp[2], Q0, Q1, Q2, hm,
+                                hmg, hmoi, m, mg, moi, bout, bin, bp.g);
             for (int c = 0; c < 3; ++c) {
-                lpos[c] += bin[c];
-                lvc[c] = bin[3 + c];
-                lSc[c] = bin[6 + c];
-                lSp[c] = bin[12 + c];
+                lvc[c] = bin[c];
+                lSc[c] = bin[3 + c];
+                lSp[c] = bin[9 + c];
                 X(c, lane) = -bin[c];
-                X(3 + c, lane) = -bin[3 + c];
-                X(6 + c, lane) = bin[9 + c];
-                X(9 + c, lane) = bin[15 + c];
+                X(3 + c, lane) = bin[6 + c];
+                X(6 + c, lane) = bin[12 + c];
             }
-            gsig += bin[18];
-            gk2 += bin[20];
-            X(12, lane) = bin[19];
-            X(13, lane) = bin[21];
         }
-        colsum(0, 14);
+        colsum(0, 9);
         if (is_host) {
             for (int c = 0; c < 3; ++c) {
-                lpos[c] += sums[c];
-                lvc[c] = sums[3 + c];
-                lSc[c] = sums[6 + c];
-                lSp[c] = sums[9 + c];
+                lvc[c] = sums[c];
+                lSc[c] = sums[3 + c];
+                lSp[c] = sums[6 + c];
             }
-            gsig += sums[12];
-            gk2 += sums[13];
+        }
+        sync();
+    }
+
+    // VJP of the pre values of a half kick: position adjoint and parameter
+    // gradients accumulated (the host's from the sums over its planets).
+    __device__ void pre_vjp(const double pos[3], const Bpre& bp, double lpos[3], double& gsig, double& gk2) {
+        sync();
+        double bin[7] = {0., 0., 0., 0., 0., 0., 0.};
+        if (planet()) {
+            double x[3];
+            helio(pos, x);
+            const double hm = card[AC_M], hR = card[AC_R], hmg = card[AC_MG], hmoi = card[AC_MOI],
+                         hk2f = card[AC_K2F];
+            if (tides_on())
+                adj_tides_pre_vjp(x[0], x[1], x[2], sig, card[AC_SIG], k2, card[AC_K2], R, hR, hm, m, bp.t, bin);
+            if (flat_on()) adj_flat_pre_vjp(x[0], x[1], x[2], R, hR, hk2f, hm, k2f, m, bp.f, bin);
+            if (gr_on()) adj_gr_pre_vjp(x[0], x[1], x[2], hm, hmg, hmoi, m, mg, moi, bp.g, bin);
+            for (int c = 0; c < 3; ++c) {
+                lpos[c] += bin[c];
+                X(c, lane) = -bin[c];
+            }
+            gsig += bin[3];
+            gk2 += bin[5];
+            X(3, lane) = bin[4];
+            X(4, lane) = bin[6];
+        }
+        colsum(0, 5);
+        if (is_host) {
+            for (int c = 0; c < 3; ++c) lpos[c] += sums[c];
+            gsig += sums[3];
+            gk2 += sums[4];
         }
         sync();
     }
@@ -342,6 +385,8 @@ struct AdjSys {
         sync();
         if (is_host) { card[AC_PX] = r[0]; card[AC_PY] = r[1]; card[AC_PZ] = r[2]; }
         sync();
+        Pre pr;
+        pre_fwd(r, pr);
         double v0[3], L0[3], vc[3], Lc[3], Sp[3], vf[3], Lf[3], pv[3], pL[3], a[3], dl[3], Sc[3];
         double dvc[3] = {0., 0., 0.}, dLc[3] = {0., 0., 0.};
         for (int c = 0; c < 3; ++c) {
@@ -357,7 +402,7 @@ struct AdjSys {
                 }
                 pv[c] = vf[c]; pL[c] = Lf[c];
             }
-            effects_fwd(r, vc, Lc, Sp, a, dl, Sc);
+            effects_fwd(pr, vc, Lc, Sp, a, dl, Sc);
             for (int c = 0; c < 3; ++c) {
                 dvc[c] = hdt * a[c] - ev[c];
                 vf[c] = v0[c] + dvc[c];
@@ -405,6 +450,10 @@ struct AdjSys {
         sync();
         if (is_host) { card[AC_PX] = pos[0]; card[AC_PY] = pos[1]; card[AC_PZ] = pos[2]; }
         sync();
+        Pre pr;
+        pre_fwd(pos, pr);
+        Bpre bp;
+        bp.zero();
         double lvf[3], lLf[3], lSn[3], lv0[3] = {0., 0., 0.}, lL0[3] = {0., 0., 0.};
         for (int c = 0; c < 3; ++c) { lvf[c] = lv[c]; lLf[c] = lL[c]; lSn[c] = lS[c]; }
         // the iteration count is group-uniform: every lane takes the host's
@@ -425,7 +474,7 @@ struct AdjSys {
             }
             spin_of(Lc, Sc);
             double lvc[3], lSc[3], lSp[3];
-            effects_vjp(pos, vc, Sc, Sp, la, ld, lvc, lSc, lSp, lr, gsig, gk2);
+            effects_vjp(pr, bp, vc, Sc, Sp, la, ld, lvc, lSc, lSp);
             const double im = (has && moi != 0.) ? 1. / moi : 0.;
             for (int c = 0; c < 3; ++c) {
                 lSc[c] += lSn[c];
@@ -443,6 +492,7 @@ struct AdjSys {
                 }
             }
         }
+        pre_vjp(pos, bp, lr, gsig, gk2);
         for (int c = 0; c < 3; ++c) { lv[c] = lv0[c]; lL[c] = lL0[c]; lS[c] = lSn[c]; }
     }
 

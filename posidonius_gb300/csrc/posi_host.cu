@@ -976,7 +976,7 @@ struct posi_adjoint {
     int32_t* d_err = nullptr;
     int32_t* d_list = nullptr;
     std::vector<Bucket> buckets;  // by adjoint lane group
-    double fwd_ms = 0., bwd_ms = 0.;
+    double fwd_ms = 0., bwd_ms = 0., record_ms = 0., reverse_ms = 0.;
 };
 
 namespace {
@@ -1118,13 +1118,29 @@ int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_
     CK(cudaMemsetAsync(a->d_grad, 0, (size_t)nb * 2 * sizeof(double), b->stream));
     CK(cudaMemsetAsync(a->d_err, 0, (size_t)b->n_sys * sizeof(int32_t), b->stream));
     int rc = POSI_OK;
+    // per chunk: [restore + record | reverse] marks, for the time split
+    std::vector<cudaEvent_t> marks((size_t)a->n_chunks * 3);
+    for (auto& e : marks) CK(cudaEventCreate(&e));
     for (int64_t c = a->n_chunks - 1; c >= 0 && rc == POSI_OK; --c) {
+        CK(cudaEventRecord(marks[(size_t)c * 3], b->stream));
         if ((rc = adj_copy_state(a, c, false)) != POSI_OK) break;
         const int64_t len = std::min(a->every, a->n_steps - c * a->every);
         for (const Bucket& bk : a->buckets) CK(posi::launch_adjoint(adj_view(a, bk), 0, len, bk.G, b->stream));
+        CK(cudaEventRecord(marks[(size_t)c * 3 + 1], b->stream));
         for (const Bucket& bk : a->buckets) CK(posi::launch_adjoint(adj_view(a, bk), 1, len, bk.G, b->stream));
+        CK(cudaEventRecord(marks[(size_t)c * 3 + 2], b->stream));
     }
     if (rc != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    a->record_ms = a->reverse_ms = 0.;
+    for (int64_t c = 0; c < a->n_chunks; ++c) {
+        float m1 = 0.f, m2 = 0.f;
+        cudaEventElapsedTime(&m1, marks[(size_t)c * 3], marks[(size_t)c * 3 + 1]);
+        cudaEventElapsedTime(&m2, marks[(size_t)c * 3 + 1], marks[(size_t)c * 3 + 2]);
+        a->record_ms += m1;
+        a->reverse_ms += m2;
+    }
+    for (auto& e : marks) cudaEventDestroy(e);
     CK(cudaEventRecord(e1, b->stream));
     // results, [system][body][12] and [system][body][2]
     if (lam_initial) {
@@ -1161,9 +1177,12 @@ int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_
     return POSI_OK;
 }
 
-int posi_adjoint_last_timing(const posi_adjoint* a, double* forward_ms, double* backward_ms) {
+int posi_adjoint_last_timing(const posi_adjoint* a, double* forward_ms, double* backward_ms, double* record_ms,
+                             double* reverse_ms) {
     if (!a) return POSI_ERR_ARG;
     if (forward_ms) *forward_ms = a->fwd_ms;
     if (backward_ms) *backward_ms = a->bwd_ms;
+    if (record_ms) *record_ms = a->record_ms;
+    if (reverse_ms) *reverse_ms = a->reverse_ms;
     return POSI_OK;
 }

@@ -24,32 +24,49 @@ void h_kepler_vjp(double mu, double dt, const double* r, const double* v, double
 }
 
 // in: 22 inputs (x y z hv S H P Q sig_p sig_h k2_p k2_h); c: m hm R hR k2f hk2f mg hmg moi hmoi
+#define ITER_ARGS(in) in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12], in[13], in[14], \
+                      in[15], in[16], in[17]
+
 void h_effects_fwd(int which, const double* in, const double* c, double* out) {
     const double m = c[0], hm = c[1], R = c[2], hR = c[3], k2f = c[4], hk2f = c[5], mg = c[6], hmg = c[7];
     const double moi = c[8], hmoi = c[9];
-    if (which == 0)
-        adj_tides_fwd(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
-                      in[13], in[14], in[15], in[16], in[17], in[18], in[19], in[20], in[21], R, hR, hm, m, out);
-    else if (which == 1)
-        adj_flat_fwd(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
-                     in[13], in[14], in[15], in[16], in[17], R, hR, hk2f, hm, k2f, m, out);
-    else
-        adj_gr_fwd(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
-                   in[13], in[14], in[15], in[16], in[17], hm, hmg, hmoi, m, mg, moi, out);
+    double pre[64];
+    if (which == 0) {
+        adj_tides_pre(in[0], in[1], in[2], in[18], in[19], in[20], in[21], R, hR, hm, m, pre);
+        adj_tides_iter(pre, ITER_ARGS(in), R, hR, hm, m, out);
+    } else if (which == 1) {
+        adj_flat_pre(in[0], in[1], in[2], R, hR, hk2f, hm, k2f, m, pre);
+        adj_flat_iter(pre, ITER_ARGS(in), R, hR, hk2f, hm, k2f, m, out);
+    } else {
+        adj_gr_pre(in[0], in[1], in[2], hm, hmg, hmoi, m, mg, moi, pre);
+        adj_gr_iter(pre, ITER_ARGS(in), hm, hmg, hmoi, m, mg, moi, out);
+    }
 }
 
+// bin[22] += adjoints in the input order of h_effects_fwd
 void h_effects_vjp(int which, const double* in, const double* c, const double* bout, double* bin) {
     const double m = c[0], hm = c[1], R = c[2], hR = c[3], k2f = c[4], hk2f = c[5], mg = c[6], hmg = c[7];
     const double moi = c[8], hmoi = c[9];
-    if (which == 0)
-        adj_tides_vjp(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
-                      in[13], in[14], in[15], in[16], in[17], in[18], in[19], in[20], in[21], R, hR, hm, m, bout, bin);
-    else if (which == 1)
-        adj_flat_vjp(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
-                     in[13], in[14], in[15], in[16], in[17], R, hR, hk2f, hm, k2f, m, bout, bin);
-    else
-        adj_gr_vjp(in[0], in[1], in[2], in[3], in[4], in[5], in[6], in[7], in[8], in[9], in[10], in[11], in[12],
-                   in[13], in[14], in[15], in[16], in[17], hm, hmg, hmoi, m, mg, moi, bout, bin);
+    double pre[64], bpre[64], bit[15], bp[7];
+    for (int k = 0; k < 64; ++k) bpre[k] = 0.;
+    for (int k = 0; k < 15; ++k) bit[k] = 0.;
+    for (int k = 0; k < 7; ++k) bp[k] = 0.;
+    if (which == 0) {
+        adj_tides_pre(in[0], in[1], in[2], in[18], in[19], in[20], in[21], R, hR, hm, m, pre);
+        adj_tides_iter_vjp(pre, ITER_ARGS(in), R, hR, hm, m, bout, bit, bpre);
+        adj_tides_pre_vjp(in[0], in[1], in[2], in[18], in[19], in[20], in[21], R, hR, hm, m, bpre, bp);
+    } else if (which == 1) {
+        adj_flat_pre(in[0], in[1], in[2], R, hR, hk2f, hm, k2f, m, pre);
+        adj_flat_iter_vjp(pre, ITER_ARGS(in), R, hR, hk2f, hm, k2f, m, bout, bit, bpre);
+        adj_flat_pre_vjp(in[0], in[1], in[2], R, hR, hk2f, hm, k2f, m, bpre, bp);
+    } else {
+        adj_gr_pre(in[0], in[1], in[2], hm, hmg, hmoi, m, mg, moi, pre);
+        adj_gr_iter_vjp(pre, ITER_ARGS(in), hm, hmg, hmoi, m, mg, moi, bout, bit, bpre);
+        adj_gr_pre_vjp(in[0], in[1], in[2], hm, hmg, hmoi, m, mg, moi, bpre, bp);
+    }
+    for (int k = 0; k < 3; ++k) bin[k] += bp[k];
+    for (int k = 0; k < 15; ++k) bin[3 + k] += bit[k];
+    for (int k = 0; k < 4; ++k) bin[18 + k] += bp[3 + k];
 }
 
 }  // extern "C"
