@@ -326,7 +326,8 @@ int posi_adjoint_forward(posi_adjoint* a);
 enum posi_adjoint_flag {
     POSI_ADJ_KEPLER = 1,        /* a Kepler root did not converge */
     POSI_ADJ_ZERO_INERTIA = 2,  /* a body has no moment of inertia */
-    POSI_ADJ_FROZEN = 4         /* the forward run froze the system (collision, Roche limit, ejection) */
+    POSI_ADJ_FROZEN = 4,        /* the forward run froze the system (collision, Roche limit, ejection) */
+    POSI_ADJ_UNSUPPORTED = 8    /* not Jacobi, evolving bodies, or too many bodies (posi_adjoint_vjp_static) */
 };
 /* lam_final: [n_systems][nmax][12] adjoints of the final (r, v, L, S); out:
  * lam_initial (same layout, may be NULL), grad [n_systems][nmax][2] (d/d
@@ -334,6 +335,36 @@ enum posi_adjoint_flag {
  * Host or device pointers (unified addressing). */
 int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_initial, double* grad,
                           int32_t* system_flags);
+/* Allocation-free adjoint of a short run.  No counterpart in the reference.
+ * For callers that may not allocate device memory -- an application whose
+ * device memory belongs to its own pool or arena (a framework's caching
+ * allocator that has reserved the GPU, an embedded solver with a fixed
+ * budget), or a latency-sensitive loop where a cudaMalloc, which can
+ * synchronise the device, is not acceptable.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine: the step records live in a
+ * file-scope device array of 48 MiB, enough for 48 MiB / (209 * 8 bytes) =
+ * 30,104 body-steps (n_steps * n_systems * nmax); larger requests fail with
+ * POSI_ERR_ARG and a message giving the limit.
+ * Same computation as one chunk of posi_adjoint_backward: from the state in
+ * the device arrays (the library's field-major layout: sys_i64
+ * [POSI_SI_COUNT][n_systems], sys_f64 [POSI_SF_COUNT][n_systems], body_i64
+ * [POSI_BI_COUNT][n_systems * nmax], body_f64 [POSI_BF_COUNT][n_systems *
+ * nmax]), re-integrate n_steps steps, recording them, and sweep them in
+ * reverse.  d_lam [12][n_systems * nmax] holds the adjoints of the final
+ * (r, v, L, S) on entry and those of the initial state on return; d_grad
+ * [2][n_systems * nmax] (d/d sigma, d/d k2) is added to; d_flags
+ * [n_systems] receives posi_adjoint_flag bits (cleared first).  All pointers
+ * are device pointers; the work is queued on `stream` (a cudaStream_t, or
+ * NULL) and the outputs are ready when the stream reaches it.
+ * The first call on a device takes the array's address
+ * (cudaGetSymbolAddress) and sets the kernels' shared-memory attributes:
+ * make that first call before any stream capture.  Every call on a device
+ * shares the one array: calls whose work overlaps on the GPU (other streams,
+ * other host threads) race on it and must be serialised by the caller. */
+int posi_adjoint_vjp_static(int64_t n_systems, int64_t nmax, const int64_t* d_sys_i64, const double* d_sys_f64,
+                            const int64_t* d_body_i64, const double* d_body_f64, int64_t n_steps, double* d_lam,
+                            double* d_grad, int32_t* d_flags, void* stream);
+
 /* CUDA-event times of the last forward and backward runs, and the backward
  * run's split into chunk re-integration (record) and reverse sweeps. */
 int posi_adjoint_last_timing(const posi_adjoint* a, double* forward_ms, double* backward_ms, double* record_ms,

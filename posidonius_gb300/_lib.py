@@ -59,6 +59,8 @@ SIGNATURES = {
     "posi_adjoint_forward": (ctypes.c_int, [_vp]),
     "posi_adjoint_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "posi_adjoint_last_timing": (ctypes.c_int, [_vp, _f64p, _f64p, _f64p, _f64p]),
+    "posi_adjoint_vjp_static": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_int64,
+                                               _vp, _vp, _vp, _vp]),
 }
 
 _lib = None

@@ -1,4 +1,7 @@
 // adjoint.cu -- launchers of the adjoint kernels (adjoint_device.cuh).
+#include <climits>
+#include <string>
+
 #include "adjoint_device.cuh"
 #include "kernels.h"
 
@@ -61,3 +64,112 @@ cudaError_t prepare_adjoint() {
 }
 
 }  // namespace posi
+
+// ---------------------------------------------------------------------------
+// Allocation-free adjoint of a short run (posi_adjoint_vjp_static).
+//
+// For callers that may not allocate device memory: applications whose device
+// memory is owned by their own pool or arena (a framework's caching
+// allocator that has reserved the GPU, an embedded solver given a fixed
+// budget), and latency-sensitive loops in which a cudaMalloc -- which can
+// synchronise the device -- is not acceptable.  The step records live in one
+// file-scope device array instead; its address is taken once per device.
+// ---------------------------------------------------------------------------
+namespace posi {
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(48) << 20;  // 48 MiB
+__device__ __align__(256) unsigned char g_adj_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+void* g_scratch_ptr[kMaxDevices] = {};
+
+__global__ void static_list_and_check(int32_t* list, int32_t n_sys, int64_t nmax, const int64_t* si,
+                                      int32_t* flags) {
+    const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_sys) return;
+    list[s] = s;
+    const int64_t n = si[(int64_t)POSI_SI_N * n_sys + s];
+    const bool ok = si[(int64_t)POSI_SI_COORDS * n_sys + s] == POSI_JACOBI &&
+                    si[(int64_t)POSI_SI_EVOLUTION * n_sys + s] == 0 && n >= 1 && n <= nmax;
+    flags[s] = ok ? 0 : POSI_ADJ_UNSUPPORTED;
+}
+
+}  // namespace
+}  // namespace posi
+
+extern "C" int posi_adjoint_vjp_static(int64_t n_systems, int64_t nmax, const int64_t* d_sys_i64,
+                                       const double* d_sys_f64, const int64_t* d_body_i64, const double* d_body_f64,
+                                       int64_t n_steps, double* d_lam, double* d_grad, int32_t* d_flags,
+                                       void* stream) {
+    using namespace posi;
+    if (n_systems < 1 || n_systems > INT32_MAX || nmax < 1 || n_steps < 1 || !d_sys_i64 || !d_sys_f64 ||
+        !d_body_i64 || !d_body_f64 || !d_lam || !d_grad || !d_flags) {
+        set_last_error("posi_adjoint_vjp_static: bad arguments");
+        return POSI_ERR_ARG;
+    }
+    const int G = adjoint_group_size(nmax);
+    if (G == 0) {
+        set_last_error("posi_adjoint_vjp_static: systems of up to 8 bodies only");
+        return POSI_ERR_UNSUPPORTED;
+    }
+    const int64_t stride = n_systems * nmax;
+    const size_t tape_bytes = ((size_t)n_steps * posi_adj::SV_COUNT * (size_t)stride * sizeof(double) + 255) / 256 * 256;
+    const size_t list_bytes = (size_t)n_systems * sizeof(int32_t);
+    if (tape_bytes + list_bytes > kStaticScratchBytes) {
+        set_last_error("posi_adjoint_vjp_static: n_steps x systems x bodies needs " +
+                       std::to_string(tape_bytes + list_bytes) + " bytes of step records, above the " +
+                       std::to_string(kStaticScratchBytes) + "-byte static scratch (at most " +
+                       std::to_string(kStaticScratchBytes / (posi_adj::SV_COUNT * sizeof(double))) +
+                       " body-steps)");
+        return POSI_ERR_ARG;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        set_last_error("posi_adjoint_vjp_static: no usable current device");
+        return POSI_ERR_CUDA;
+    }
+    // set-up, once per device (the first call on a device must come before
+    // any stream capture)
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_adj_scratch);
+        if (e != cudaSuccess || !p) {
+            set_last_error(std::string("posi_adjoint_vjp_static: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            return POSI_ERR_CUDA;
+        }
+        e = prepare_adjoint();
+        if (e != cudaSuccess) {
+            set_last_error(std::string("posi_adjoint_vjp_static: ") + cudaGetErrorString(e));
+            return POSI_ERR_CUDA;
+        }
+        g_scratch_ptr[dev] = p;
+    }
+    char* base = (char*)g_scratch_ptr[dev];
+    AdjView v;
+    v.n_sys = n_systems;
+    v.nmax = nmax;
+    v.stride = stride;
+    v.bf = d_body_f64;
+    v.bi = d_body_i64;
+    v.sf = d_sys_f64;
+    v.si = d_sys_i64;
+    v.tape = (double*)base;
+    int32_t* list = (int32_t*)(base + tape_bytes);
+    v.list = list;
+    v.n_list = (int32_t)n_systems;
+    v.lam = d_lam;
+    v.grad = d_grad;
+    v.err = d_flags;
+    cudaStream_t st = (cudaStream_t)stream;
+    static_list_and_check<<<(int)((n_systems + 255) / 256), 256, 0, st>>>(list, (int32_t)n_systems, nmax, d_sys_i64,
+                                                                       d_flags);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = launch_adjoint(v, 0, n_steps, G, st);
+    if (e == cudaSuccess) e = launch_adjoint(v, 1, n_steps, G, st);
+    if (e != cudaSuccess) {
+        set_last_error(std::string("posi_adjoint_vjp_static: ") + cudaGetErrorString(e));
+        return POSI_ERR_CUDA;
+    }
+    return POSI_OK;
+}

@@ -1,6 +1,8 @@
 // kernels.h -- host-side launch interface of the two arithmetic modes.
 #pragma once
 #include <cstdint>
+#include <string>
+
 #include <cuda_runtime.h>
 
 namespace posi {
@@ -70,5 +72,8 @@ int adjoint_group_size(int64_t n);
 constexpr int kAdjTapeFields = 27 + 2 * (1 + 9 * 10);  // per-step record of the adjoint, doubles per body
 cudaError_t launch_adjoint(const AdjView& v, int which, int64_t k_steps, int G, cudaStream_t stream);
 cudaError_t prepare_adjoint();
+
+// Sets the message posi_last_error() returns on the calling thread.
+void set_last_error(const std::string& msg);
 
 }  // namespace posi

@@ -961,6 +961,10 @@ int posi_batch_last_timing(const posi_batch* b, double* ms, int64_t* launches) {
 
 }  // extern "C"
 
+namespace posi {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace posi
+
 // ---- adjoint ----------------------------------------------------------------
 // Checkpointed reverse mode over a batch (no reference counterpart: the
 // reference has no derivatives; its users take finite differences).
