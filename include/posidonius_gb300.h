@@ -343,8 +343,9 @@ int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_
  * synchronise the device, is not acceptable.  It calls no cudaMalloc,
  * cudaFree or allocating library routine: the step records live in a
  * file-scope device array of 48 MiB, enough for 48 MiB / (209 * 8 bytes) =
- * 30,104 body-steps (n_steps * n_systems * nmax); larger requests fail with
- * POSI_ERR_ARG and a message giving the limit.
+ * 30,102 body-steps (n_steps * n_systems * nmax, less 4 bytes per system for
+ * the system list); larger requests fail with POSI_ERR_ARG and a message
+ * giving the limit.
  * Same computation as one chunk of posi_adjoint_backward: from the state in
  * the device arrays (the library's field-major layout: sys_i64
  * [POSI_SI_COUNT][n_systems], sys_f64 [POSI_SF_COUNT][n_systems], body_i64
