@@ -450,3 +450,28 @@ def adjoint_gradient(ens, elements, sigma, k2, masses, moi, star_spin, n_steps, 
     traj.adjoint.close()
     batch.close()
     return out
+
+
+def main(argv=None):
+    """``python -m posidonius_gb300.adjoint --systems S --steps K --every C``:
+    one gradient of the differentiation workload's loss; prints the forward
+    and backward times (CUDA events) as JSON."""
+    import argparse
+    import json
+    p = argparse.ArgumentParser(description=main.__doc__)
+    p.add_argument("--systems", type=int, default=1024)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--every", type=int, default=100)
+    p.add_argument("--seed", type=int, default=1)
+    a = p.parse_args(argv)
+    ens, el, ms, moi, ss = gradient_workload(a.systems, seed=a.seed)
+    sig = ens["body_f64"][:, :, L.BF_SIGMA].copy()
+    k2 = ens["body_f64"][:, :, L.BF_K2].copy()
+    loss, g_sig, g_k2, g_el, tm, flags = adjoint_gradient(ens, el, sig, k2, ms, moi, ss, a.steps, a.every)
+    print(json.dumps({"systems": a.systems, "steps": a.steps, "every": a.every, "forward_ms": tm[0],
+                      "backward_ms": tm[1], "record_ms": tm[2], "reverse_ms": tm[3],
+                      "systems_flagged": int((flags != 0).sum())}))
+
+
+if __name__ == "__main__":
+    main()
