@@ -371,6 +371,29 @@ int posi_adjoint_vjp_static(int64_t n_systems, int64_t nmax, const int64_t* d_sy
 int posi_adjoint_last_timing(const posi_adjoint* a, double* forward_ms, double* backward_ms, double* record_ms,
                              double* reverse_ms);
 
+/* ---- one system of many bodies ---------------------------------------------
+ * src/particles/universe.rs:198-303 and src/integrator/whfast.rs:235-305 for a
+ * single system beyond the batched kernels' 32 bodies (a star, tidally active
+ * planets and hundreds or thousands of small massive bodies): one cooperative
+ * grid, thread per body, the O(N^2) pair loop spread over the whole GPU.
+ * Democratic-heliocentric coordinates, non-evolving bodies, the host the most
+ * massive body; FAST arithmetic.  State arrays as posi_universe_from_arrays
+ * (one system of n bodies, row-major).  A physical event freezes the system
+ * (posi_large_iterate returns POSI_ERR_PHYSICS; sys_i64[POSI_SI_FAIL_PAIR] =
+ * i * n + j of the first failing pair). */
+typedef struct posi_large posi_large;
+posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* sys_f64, const int64_t* body_i64,
+                              const double* body_f64, int* status);
+void posi_large_destroy(posi_large* L);
+int posi_large_set_state(posi_large* L, const int64_t* sys_i64, const double* sys_f64, const int64_t* body_i64,
+                         const double* body_f64);
+int posi_large_get_state(const posi_large* L, int64_t* sys_i64, double* sys_f64, int64_t* body_i64,
+                         double* body_f64);
+int posi_large_initialize_physical_values(posi_large* L);
+/* n_steps steps in one launch (fewer when the run completes or freezes). */
+int posi_large_iterate(posi_large* L, int64_t n_steps);
+int posi_large_last_timing(const posi_large* L, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,7 +22,7 @@ from . import layout
 from . import layout as L
 from ._lib import PosiError, check, lib, ptr
 
-__all__ = ["WHFast", "Batch", "restore_snapshot", "read_case", "layout", "PosiError", "EXACT", "FAST"]
+__all__ = ["WHFast", "Batch", "ManyBody", "restore_snapshot", "read_case", "layout", "PosiError", "EXACT", "FAST"]
 
 EXACT = L.MODE_EXACT
 FAST = L.MODE_FAST
@@ -272,4 +272,59 @@ class Batch:
         arr = {k: np.ascontiguousarray(state[k], dtype=np.int64 if k.endswith("i64") else np.float64)
                for k in ("sys_i64", "sys_f64", "body_i64", "body_f64")}
         check(lib().posi_batch_set_state(self._h, ptr(arr["sys_i64"], "i"), ptr(arr["sys_f64"], "f"),
+                                         ptr(arr["body_i64"], "i"), ptr(arr["body_f64"], "f")))
+
+
+class ManyBody:
+    """One system of many bodies on the whole GPU (posi_large_*): democratic
+    heliocentric WHFast, thread per body, the O(N^2) pair loop spread over
+    every SM.  ``case`` is a single-system dict of the flat layout."""
+
+    def __init__(self, case):
+        st = ctypes.c_int(0)
+        arr = {k: np.ascontiguousarray(case[k], dtype=np.int64 if k.endswith("i64") else np.float64)
+               for k in ("sys_i64", "sys_f64", "body_i64", "body_f64")}
+        self.n = int(arr["sys_i64"][L.SI_N])
+        h = lib().posi_large_create(self.n, ptr(arr["sys_i64"], "i"), ptr(arr["sys_f64"], "f"),
+                                    ptr(arr["body_i64"], "i"), ptr(arr["body_f64"], "f"), ctypes.byref(st))
+        if not h:
+            check(st.value)
+        self._h = ctypes.c_void_p(h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().posi_large_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def initialize_physical_values(self):
+        check(lib().posi_large_initialize_physical_values(self._h))
+
+    def iterate(self, n_steps):
+        """Returns layout.OK or layout.COMPLETED; raises on a physical event."""
+        return check(lib().posi_large_iterate(self._h, int(n_steps)), ok=(L.OK, L.COMPLETED))
+
+    def last_timing(self):
+        ms = ctypes.c_double()
+        check(lib().posi_large_last_timing(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def get_state(self):
+        n = self.n
+        out = {"sys_i64": np.zeros(L.SI_COUNT, np.int64), "sys_f64": np.zeros(L.SF_COUNT, np.float64),
+               "body_i64": np.zeros((n, L.BI_COUNT), np.int64), "body_f64": np.zeros((n, L.BF_COUNT), np.float64),
+               "n": n}
+        check(lib().posi_large_get_state(self._h, ptr(out["sys_i64"], "i"), ptr(out["sys_f64"], "f"),
+                                         ptr(out["body_i64"], "i"), ptr(out["body_f64"], "f")))
+        return out
+
+    def set_state(self, state):
+        arr = {k: np.ascontiguousarray(state[k], dtype=np.int64 if k.endswith("i64") else np.float64)
+               for k in ("sys_i64", "sys_f64", "body_i64", "body_f64")}
+        check(lib().posi_large_set_state(self._h, ptr(arr["sys_i64"], "i"), ptr(arr["sys_f64"], "f"),
                                          ptr(arr["body_i64"], "i"), ptr(arr["body_f64"], "f")))

@@ -59,6 +59,13 @@ SIGNATURES = {
     "posi_adjoint_forward": (ctypes.c_int, [_vp]),
     "posi_adjoint_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "posi_adjoint_last_timing": (ctypes.c_int, [_vp, _f64p, _f64p, _f64p, _f64p]),
+    "posi_large_create": (_vp, [ctypes.c_int64, _i64p, _f64p, _i64p, _f64p, _intp]),
+    "posi_large_destroy": (None, [_vp]),
+    "posi_large_set_state": (ctypes.c_int, [_vp, _i64p, _f64p, _i64p, _f64p]),
+    "posi_large_get_state": (ctypes.c_int, [_vp, _i64p, _f64p, _i64p, _f64p]),
+    "posi_large_initialize_physical_values": (ctypes.c_int, [_vp]),
+    "posi_large_iterate": (ctypes.c_int, [_vp, ctypes.c_int64]),
+    "posi_large_last_timing": (ctypes.c_int, [_vp, _f64p]),
     "posi_adjoint_vjp_static": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_int64,
                                                _vp, _vp, _vp, _vp]),
 }

@@ -28,6 +28,7 @@ UNITS = [
     ("diagnostics.cu", ["-fmad=true"]),
     ("snapshot.cpp", ["-x", "cu", "-fmad=false"]),
     ("adjoint.cu", ["-fmad=true"]),
+    ("large.cu", ["-fmad=true"]),
 ]
 
 

@@ -15,7 +15,10 @@ Workloads (seed = 20261203 + workload id):
 * ``ensemble8`` -- star + 7 planets, a in [0.01, 0.07] AU with at least 8
   mutual Hill radii between neighbours;
 * ``uneven`` -- 2..10 bodies per system, 20 % circumbinary binaries, each of
-  tides / flattening / GR on with probability 0.7.
+  tides / flattening / GR on with probability 0.7;
+* ``large`` -- one system: a 1 Msun star, 2 tidally active planets (1-10
+  M_earth, 0.02-0.05 AU) and n_small massive bodies (1e-3 - 1e-1 M_earth,
+  a in 0.1-1 AU, e <= 0.1, i <= 2 deg), democratic heliocentric, dt = 0.1 d.
 
 Dissipation factors follow the reference's own cgs conversion (x 3.845764e64,
 ``tests/common/stars.rs:183``): star 2.006e-60 -> 2.006*3.845764e4, planet
@@ -298,3 +301,31 @@ def _binary_system(rng, n_bodies, flags, **kw):
     planets = [_planet(rng, m1 + m2, a[k], bary_pos, bary_vel) for k in range(n_pl)]
     return make_system([star, companion] + planets, tides=bool(flags[0]), flat=bool(flags[1]), gr=bool(flags[2]),
                        **kw)
+
+
+def workload_large(n_small=1021, seed=None, dt=0.1, coords=L.DEMOCRATIC_HELIOCENTRIC, **kw):
+    """One system of 3 + n_small bodies (the many-body workload).  Every body
+    is a tidal orbiting body of the star -- the reference sums the star's
+    torque over all bodies -- with zero dissipation factor and Love number for
+    the small bodies."""
+    rng = np.random.default_rng(SEED_BASE + WORKLOAD_IDS["large"] if seed is None else seed)
+    star = _star(mass=1.0, radius_factor=1.0, rg2=0.07, period_days=25.0, k2=0.03)
+    bodies = [star]
+    a_pl = np.sort(rng.uniform(0.02, 0.05, size=2))
+    for a in a_pl:
+        m = rng.uniform(1.0, 10.0) * M_EARTH
+        bodies.append(_planet(rng, star.mass, a, mass=m))
+    for _ in range(n_small):
+        m = np.exp(rng.uniform(np.log(1e-3), np.log(1e-1))) * M_EARTH
+        a = rng.uniform(0.1, 1.0)
+        b = _planet(rng, star.mass, a, e_max=0.1, i_max_deg=2.0, mass=m)
+        b.tides = (L.EFFECT_ORBITING, 0.0, 0.0)
+        b.flat = None
+        b.gr = L.EFFECT_DISABLED
+        bodies.append(b)
+    for b in bodies[1:3]:
+        b.flat = None
+        b.gr = L.EFFECT_DISABLED
+    star.flat = None
+    star.gr = L.EFFECT_DISABLED
+    return make_system(bodies, dt=dt, coords=coords, tides=True, flat=False, gr=False, **kw)
