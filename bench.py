@@ -42,7 +42,8 @@ def parse():
     p.add_argument("--steps", type=int, default=3000)
     p.add_argument("--warmup", type=int, default=300)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="ensemble8", choices=["ensemble8", "uneven", "single", "gradient"])
+    p.add_argument("--workload", default="ensemble8", choices=["ensemble8", "uneven", "single", "gradient", "large"])
+    p.add_argument("--large-bodies", type=int, default=1024, help="large workload: bodies in the system")
     p.add_argument("--grad-steps", type=int, default=10000, help="gradient workload: WHFast steps")
     p.add_argument("--checkpoint-every", type=int, default=100, help="gradient workload: checkpoint interval")
     p.add_argument("--fd-systems", type=int, default=32, help="gradient workload: systems checked by differences")
@@ -403,6 +404,82 @@ def run_gradient(args):
     print(json.dumps(result), flush=True)
 
 
+def run_large(args):
+    """Many-body workload: one system of N bodies (star, 2 tidal planets,
+    N - 3 small massive bodies), K steps in one cooperative launch."""
+    import torch
+
+    import posidonius_gb300 as pg
+    from posidonius_gb300 import ensemble as E
+    from posidonius_gb300 import layout as L
+
+    N = args.large_bodies
+    K = args.steps
+    case = E.workload_large(N - 3)
+    mb = pg.ManyBody(case)
+    mb.initialize_physical_values()
+    init = mb.get_state()
+    W = max(3, min(args.warmup, 50))
+    mb.iterate(W)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    mb.set_state(init)
+    clocks = ClockSampler(0)
+    clocks.start()
+    flush.fill_(1.0)
+    torch.cuda.synchronize()
+    st = mb.iterate(K)
+    ms = mb.last_timing()
+    clock_info = clocks.stop()
+    final = mb.get_state()
+    done = int(final["sys_i64"][L.SI_ITERATION])
+    value = done / (ms * 1e-3)
+    # e2e: host state in, K steps, host state out
+    t0 = time.perf_counter()
+    mb.set_state(init)
+    mb.iterate(K)
+    out = mb.get_state()
+    e2e_s = time.perf_counter() - t0
+    bytes_io = sum(init[k].nbytes for k in ("sys_i64", "sys_f64", "body_i64", "body_f64"))
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": done, "warmup": W,
+        "ms_per_step": ms / max(done, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded; posidonius_gb300.ensemble.workload_large)",
+        "config": {"workload": "large", "bodies": N, "dt_days": 0.1, "coordinates": "democratic heliocentric",
+                   "effects": "CTL tides (every body an orbiting tidal body of the star; the small bodies with "
+                              "zero dissipation and Love number)", "mode": "fast",
+                   "l2": "flushed (512 MiB write) before the timed launch",
+                   "pair_interactions_per_step": N * (N - 1)},
+        "pair_interactions_per_s": N * (N - 1) * value,
+        "e2e": {"value": done / e2e_s, "unit": UNIT, "h2d_bytes_per_step": bytes_io / max(done, 1),
+                "d2h_bytes_per_step": bytes_io / max(done, 1), "note": "posi_large_set_state, iterate, get_state"},
+        "gpu_launches": 1, "status": int(final["sys_i64"][L.SI_STATUS]), "clocks": clock_info,
+    }
+    if not args.no_cpu_baseline:
+        import oracle
+        from oracle.case_json import stack
+        oracle.build()
+        ens = stack([case])
+        state, _, _ = oracle.run(ens, op=oracle.INITIALIZE)
+        t0 = time.perf_counter()
+        n_cpu = 3
+        oracle.run(state, max_steps=n_cpu, nthreads=1)
+        cpu_s = time.perf_counter() - t0
+        _, _, _, cnt = oracle.run(state, max_steps=1, flops=True)
+        flops = float(cnt[0])
+        result["cpu_baseline"] = {"value": n_cpu / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+                                  "sample": f"{n_cpu} WHFast steps of the {N}-body system, C++ restatement of the "
+                                            f"Rust FP64 path, one thread (one system does not split), {cpu_s:.1f} s"}
+        peak = fp64_peak()
+        achieved = flops * done / (ms * 1e-3) / 1e12
+        result["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                              "frac": achieved / peak, "traffic": None, "flops_per_step": flops,
+                              "peak_source": "measured in-run: posi_fp64_probe (DFMA chains)",
+                              "note": "algorithmic flops of one step (oracle count, + - * / sqrt = 1) x steps / "
+                                      "CUDA-event launch time"}
+    print(json.dumps(result), flush=True)
+    mb.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -410,6 +487,9 @@ def main():
         return
     if args.workload == "gradient":
         run_gradient(args)
+        return
+    if args.workload == "large":
+        run_large(args)
         return
     world, rank, local = dist_setup(args)
     import torch

@@ -99,6 +99,32 @@ __host__ __device__ __forceinline__ KeplerScalars kepler_scalars(double mu, cons
     return s;
 }
 
+// c0..c3 only (the solver's iterations need no more): the series with the
+// same truncation, quartering and doubling as stumpff6.
+__host__ __device__ __forceinline__ void stumpff4(double z, double c[4]) {
+    const double f[20] = {1., 1., 1. / 2., 1. / 6., 1. / 24., 1. / 120., 1. / 720., 1. / 5040., 1. / 40320.,
+                          1. / 362880., 1. / 3628800., 1. / 39916800., 1. / 479001600., 1. / 6227020800.,
+                          1. / 87178291200., 1. / 1307674368000., 1. / 20922789888000., 1. / 355687428096000.,
+                          1. / 6402373705728000., 1. / 121645100408832000.};
+    double zz = z;
+    int n = 0;
+    while (fabs(zz) > 0.1 && n < 64) {
+        zz *= 0.25;
+        ++n;
+    }
+    for (int k = 0; k < 4; ++k) {
+        double s = f[k + 12];
+        for (int j = 5; j >= 0; --j) s = f[k + 2 * j] - zz * s;
+        c[k] = s;
+    }
+    for (int k = 0; k < n; ++k) {
+        c[3] = (c[2] + c[0] * c[3]) * 0.25;
+        c[2] = c[1] * c[1] * 0.5;
+        c[1] = c[0] * c[1];
+        c[0] = 2. * c[0] * c[0] - 1.;
+    }
+}
+
 // Root of Kepler's equation in universal variables by Newton's method from
 // the second-order guess of src/integrator/whfast.rs:716-720 (elliptic) or 0;
 // *ok = false when it did not converge.
@@ -110,10 +136,12 @@ __host__ __device__ __forceinline__ double kepler_solve(const KeplerScalars& s, 
     }
     *ok = false;
     for (int it = 0; it < kKEPLER_MAX_NEWTON; ++it) {
-        double G[6];
-        gfun6(s.beta, X, G);
-        const double F = s.r0 * X + s.eta0 * G[2] + s.zeta0 * G[3] - dt;
-        const double Fp = s.r0 + s.eta0 * G[1] + s.zeta0 * G[2];
+        double c[4];
+        stumpff4(s.beta * X * X, c);
+        const double X2 = X * X;
+        const double G1 = X * c[1], G2 = X2 * c[2], G3 = X2 * X * c[3];
+        const double F = s.r0 * X + s.eta0 * G2 + s.zeta0 * G3 - dt;
+        const double Fp = s.r0 + s.eta0 * G1 + s.zeta0 * G2;
         const double dX = F / Fp;
         X -= dX;
         if (fabs(dX) <= 1e-15 * fabs(X) || dX == 0.) {
@@ -127,8 +155,9 @@ __host__ __device__ __forceinline__ double kepler_solve(const KeplerScalars& s, 
 // (r1, v1) of the drift, given the root X.
 __host__ __device__ __forceinline__ void kepler_apply(double mu, double dt, const double r[3], const double v[3],
                                                       const KeplerScalars& s, double X, double r1[3], double v1[3]) {
-    double G[6];
-    gfun6(s.beta, X, G);
+    double c[4], G[4];
+    stumpff4(s.beta * X * X, c);
+    G[0] = c[0]; G[1] = X * c[1]; G[2] = X * X * c[2]; G[3] = X * X * X * c[3];
     const double rr = s.r0 + s.eta0 * G[1] + s.zeta0 * G[2];
     const double f = -mu * G[2] / s.r0;
     const double g = dt - mu * G[3];

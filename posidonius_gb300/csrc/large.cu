@@ -10,9 +10,9 @@
 
 struct posi_large {
     int64_t n = 0;
-    int grid = 0, nchunk = 0;
+    int grid = 0, nchunk = 0, per_block = 0;
     double *d_bf = nullptr, *d_sf = nullptr, *d_roche = nullptr, *d_pos = nullptr, *d_gpart = nullptr,
-           *d_bpart = nullptr;
+           *d_bpart = nullptr, *d_tot = nullptr;
     int64_t *d_bi = nullptr, *d_si = nullptr;
     unsigned* d_bar = nullptr;
     int* d_err = nullptr;
@@ -27,7 +27,7 @@ namespace {
 void free_large(posi_large* L) {
     if (!L) return;
     cudaFree(L->d_bf); cudaFree(L->d_sf); cudaFree(L->d_roche); cudaFree(L->d_pos); cudaFree(L->d_gpart);
-    cudaFree(L->d_bpart); cudaFree(L->d_bi); cudaFree(L->d_si); cudaFree(L->d_bar); cudaFree(L->d_err);
+    cudaFree(L->d_bpart); cudaFree(L->d_tot); cudaFree(L->d_bi); cudaFree(L->d_si); cudaFree(L->d_bar); cudaFree(L->d_err);
     cudaFree(L->d_bad);
     if (L->e0) cudaEventDestroy(L->e0);
     if (L->e1) cudaEventDestroy(L->e1);
@@ -94,7 +94,13 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
     if ((int64_t)L->grid * posi_many::kBlock < n)
         return fail(POSI_ERR_UNSUPPORTED, "too many bodies for one resident grid (" +
                                               std::to_string((int64_t)L->grid * posi_many::kBlock) + " at most)", L);
-    L->nchunk = (int)(((int64_t)L->grid * posi_many::kBlock) / n);
+    // slices of the pair loop: one thread per (body, slice), at least 16
+    // partners per slice
+    L->nchunk = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)L->grid * posi_many::kBlock) / n, n / 16));
+    {
+        const int64_t need = (n + L->grid - 1) / L->grid;
+        L->per_block = (int)std::min<int64_t>(posi_many::kBlock, std::max<int64_t>(32, (need + 31) / 32 * 32));
+    }
     auto ok = [&](cudaError_t e) {
         if (e != cudaSuccess) { posi::set_last_error(cudaGetErrorString(e)); return false; }
         return true;
@@ -109,6 +115,7 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
         !ok(cudaMalloc(&L->d_pos, (size_t)3 * n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_gpart, (size_t)L->nchunk * 3 * n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_bpart, (size_t)L->grid * posi_many::BP_SLOTS * sizeof(double))) ||
+        !ok(cudaMalloc(&L->d_tot, posi_many::BP_SLOTS * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_bar, 2 * sizeof(unsigned))) || !ok(cudaMalloc(&L->d_err, sizeof(int))) ||
         !ok(cudaMalloc(&L->d_bad, sizeof(unsigned long long))) ||
         !ok(cudaMemset(L->d_bar, 0, 2 * sizeof(unsigned))) || !ok(cudaMemset(L->d_err, 0, sizeof(int))))
@@ -196,9 +203,11 @@ int posi_large_iterate(posi_large* L, int64_t n_steps) {
     posi_many::LDev d;
     d.n = L->n;
     d.bf = L->d_bf; d.bi = L->d_bi; d.sf = L->d_sf; d.si = L->d_si; d.roche = L->d_roche;
-    d.pos = L->d_pos; d.gpart = L->d_gpart; d.bpart = L->d_bpart; d.bar = L->d_bar; d.err = L->d_err;
+    d.pos = L->d_pos; d.gpart = L->d_gpart; d.bpart = L->d_bpart; d.tot = L->d_tot; d.bar = L->d_bar;
+    d.err = L->d_err;
     d.bad = L->d_bad;
     d.nchunk = L->nchunk;
+    d.per_block = L->per_block;
     LCK(cudaMemsetAsync(L->d_bad, 0xff, sizeof(unsigned long long), L->stream));
     void* args[] = {&d, &n_steps};
     LCK(cudaEventRecord(L->e0, L->stream));

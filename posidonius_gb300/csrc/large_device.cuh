@@ -29,6 +29,8 @@
 #pragma once
 #include <cstdint>
 
+#include <cuda/atomic>
+
 #include "../../include/posidonius_gb300.h"
 #include "adjoint_effects.cuh"
 
@@ -38,7 +40,7 @@ using namespace posi_adj;
 
 constexpr int kBlock = 256;
 constexpr double kMAX_DISTANCE_2 = 100. * 100.;
-constexpr long long kBarrierSpinLimit = 1LL << 25;  // x 64 ns sleeps: about 2 s
+constexpr long long kBarrierWaitCycles = 4000000000LL;  // about 2 s at the maximum SM clock
 
 enum { BP_SLOTS = 16 };  // per-block partial sums
 enum { LE_BARRIER = 1, LE_KEPLER = 2, LE_ZERO_INERTIA = 4 };
@@ -53,68 +55,162 @@ struct LDev {
     double* pos;            // [3][n] positions for the pair loop
     double* gpart;          // [nchunk][3][n] partial accelerations
     double* bpart;          // [gridDim.x][BP_SLOTS]
+    double* tot;            // [BP_SLOTS] totals of the last reduction
     unsigned* bar;          // [2] arrival count, generation
     int* err;               // error flags (LE_*)
     unsigned long long* bad;  // first failing pair: min over (i n + j) * 4 + code; all ones if none
     int nchunk;
+    int per_block;          // bodies per block: body i is thread i % per_block of block i / per_block
 };
 
-// Sum of v over the block into slot s of this block's partial row; called by
-// every thread of the block with its own contribution (0 when it has none).
-__device__ __forceinline__ void block_partial(double* bpart, double (&vals)[BP_SLOTS], int nslots, double* shm) {
+// Sum of vals over the block into this block's partial row.  Only warps
+// that own bodies (active = the warp has a body) add: a warp's FP64 add holds
+// its SMSP's FP64 pipe 64 cycles, so the trees of empty warps would cost as
+// much as real ones; empty warps contribute zeros.
+__device__ __forceinline__ void block_partial(double* bpart, double (&vals)[BP_SLOTS], int nslots, double* shm,
+                                              bool warp_active) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int k = 0; k < nslots; ++k) {
-        double x = vals[k];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) shm[warp * BP_SLOTS + k] = x;
+    if (warp_active) {
+#pragma unroll
+        for (int k = 0; k < BP_SLOTS; ++k) {
+            if (k < nslots) {
+                double x = vals[k];
+                for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+                if (lane == 0) shm[warp * BP_SLOTS + k] = x;
+            }
+        }
     }
     __syncthreads();
-    if (threadIdx.x < nslots) {
-        double acc = 0.;
-        for (int w = 0; w < kBlock / 32; ++w) acc += shm[w * BP_SLOTS + threadIdx.x];
+    // the warps that own bodies are the first ones of the block
+    const int nw = __syncthreads_count(warp_active && lane == 0);
+    if (threadIdx.x < nslots && nw > 0) {
+        double acc = shm[threadIdx.x];
+        for (int w = 1; w < nw; ++w) acc += shm[w * BP_SLOTS + threadIdx.x];
         bpart[(size_t)blockIdx.x * BP_SLOTS + threadIdx.x] = acc;
     }
     __syncthreads();
 }
 
-// Totals of the block partials, in block order (every thread, same result).
-__device__ __forceinline__ void block_totals(const double* bpart, double* out, int nslots) {
-    for (int k = 0; k < nslots; ++k) out[k] = 0.;
-    for (unsigned b = 0; b < gridDim.x; ++b)
-        for (int k = 0; k < nslots; ++k) out[k] += __ldcg(&bpart[(size_t)b * BP_SLOTS + k]);
+// Totals of the block partials (every thread, same result).  The first warp
+// of each block adds them -- lane l takes blocks l, l + 32, ... in order, then
+// a fixed butterfly combines the lanes -- and shares them through shared
+// memory: the same order in every block, so every thread gets the same bits.
+__device__ __forceinline__ void block_totals(const double* bpart, double* out, int nslots, double* shm) {
+    if (threadIdx.x < 32) {
+        // all loads first (one latency), then the butterflies
+        double x[BP_SLOTS];
+#pragma unroll
+        for (int k = 0; k < BP_SLOTS; ++k) x[k] = 0.;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += 32) {
+            const double* row = bpart + (size_t)b * BP_SLOTS;
+#pragma unroll
+            for (int k = 0; k < BP_SLOTS; ++k)
+                if (k < nslots) x[k] += __ldcg(row + k);
+        }
+#pragma unroll
+        for (int k = 0; k < BP_SLOTS; ++k) {
+            if (k < nslots) {
+                double y = x[k];
+                for (int o = 16; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+                if (threadIdx.x == 0) shm[(kBlock / 32) * BP_SLOTS + k] = y;
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < nslots; ++k) out[k] = shm[(kBlock / 32) * BP_SLOTS + k];
+    __syncthreads();
 }
 
-// Grid-wide barrier with a bounded wait.  Returns false (and flags the error)
-// when the wait ran out; callers then leave the kernel.
+// Grid-wide barrier with a bounded wait: thread 0 of each block arrives with
+// a release-acquire add on the arrival count; the last block resets it and
+// releases the generation, the others poll it with acquire loads.  Returns
+// false (and flags the error) when the wait ran out; callers then leave the
+// kernel.
 __device__ bool grid_barrier(const LDev& D) {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned* gen = D.bar + 1;
-        const unsigned g = *gen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(D.bar, 1u) + 1u;
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(D.bar[0]), gen(D.bar[1]);
+        cuda::atomic_ref<int, cuda::thread_scope_device> err(*D.err);
+        const unsigned g = gen.load(cuda::memory_order_relaxed);
         int ok = 1;
-        if (arrived == gridDim.x) {
-            D.bar[0] = 0u;
-            __threadfence();
-            atomicAdd(D.bar + 1, 1u);
+        if (count.fetch_add(1u, cuda::memory_order_acq_rel) + 1u == gridDim.x) {
+            count.store(0u, cuda::memory_order_relaxed);
+            gen.fetch_add(1u, cuda::memory_order_release);
         } else {
-            long long spins = 0;
-            while (*gen == g) {
-                if (++spins > kBarrierSpinLimit || (*(volatile int*)D.err & LE_BARRIER)) {
+            const long long start = clock64();
+            while (gen.load(cuda::memory_order_relaxed) == g) {
+                if (clock64() - start > kBarrierWaitCycles || (err.load(cuda::memory_order_relaxed) & LE_BARRIER)) {
                     ok = 0;
-                    atomicOr(D.err, LE_BARRIER);
+                    err.fetch_or(LE_BARRIER, cuda::memory_order_relaxed);
                     break;
                 }
-                __nanosleep(64);
+                __nanosleep(20);
             }
+            cuda::atomic_thread_fence(cuda::memory_order_acquire, cuda::thread_scope_device);
         }
-        __threadfence();
         ok_s = ok;
     }
     __syncthreads();
     return ok_s != 0;
+}
+
+// Grid-wide sum: every block writes its partial row and arrives; the last
+// block to arrive adds the rows in block order (first warp, fixed butterfly),
+// publishes the totals and releases the others, which then read them once per
+// block.  One barrier, and only one block reads the partial rows.
+__device__ bool grid_reduce(const LDev& D, double (&vals)[BP_SLOTS], int nslots, double* out, double* shm,
+                            bool warp_active, unsigned rows) {
+    __shared__ int last_s, ok_s;
+    __shared__ unsigned gen_s;
+    block_partial(D.bpart, vals, nslots, shm, warp_active);
+    if (threadIdx.x == 0) {
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(D.bar[0]), gen(D.bar[1]);
+        gen_s = gen.load(cuda::memory_order_relaxed);
+        last_s = count.fetch_add(1u, cuda::memory_order_acq_rel) + 1u == gridDim.x;
+    }
+    __syncthreads();
+    int ok = 1;
+    if (last_s) {
+        // slot k is added by warp k mod 8 (the warps sit on different
+        // SMSPs); lane l takes rows l, l + 32, ... of the blocks that own
+        // bodies (the other rows are zero), then a fixed butterfly
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int k = warp; k < nslots; k += kBlock / 32) {
+            double x = 0.;
+            for (unsigned b = lane; b < rows; b += 32) x += __ldcg(D.bpart + (size_t)b * BP_SLOTS + k);
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) D.tot[k] = x;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(D.bar[0]), gen(D.bar[1]);
+            count.store(0u, cuda::memory_order_relaxed);
+            gen.fetch_add(1u, cuda::memory_order_release);
+        }
+    } else if (threadIdx.x == 0) {
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(D.bar[1]);
+        cuda::atomic_ref<int, cuda::thread_scope_device> err(*D.err);
+        const long long start = clock64();
+        while (gen.load(cuda::memory_order_relaxed) == gen_s) {
+            if (clock64() - start > kBarrierWaitCycles || (err.load(cuda::memory_order_relaxed) & LE_BARRIER)) {
+                ok = 0;
+                err.fetch_or(LE_BARRIER, cuda::memory_order_relaxed);
+                break;
+            }
+            __nanosleep(20);
+        }
+        cuda::atomic_thread_fence(cuda::memory_order_acquire, cuda::thread_scope_device);
+    }
+    if (threadIdx.x == 0) {
+        ok_s = ok;
+        for (int k = 0; k < nslots; ++k) shm[(kBlock / 32) * BP_SLOTS + k] = __ldcg(D.tot + k);
+    }
+    __syncthreads();
+    for (int k = 0; k < nslots; ++k) out[k] = shm[(kBlock / 32) * BP_SLOTS + k];
+    const bool r = ok_s != 0;
+    __syncthreads();
+    return r;
 }
 
 struct BodyConst {
@@ -165,7 +261,9 @@ struct Large {
     BodyState b, h;         // own and host state (host: redundant copy)
     double a[3];            // gravity acceleration (own)
     double* shm;
-    double Mtot;
+    double Mtot, inv_M, inv_hm;
+    bool warp_bodies;       // this thread's warp owns at least one body
+    unsigned body_rows;     // blocks that own bodies (the partial rows that can be nonzero)
 
     __device__ Large(const LDev& D_, double* shm_) : D(D_), shm(shm_) {}
 
@@ -183,7 +281,9 @@ struct Large {
     }
 
     // ---- implicit midpoint (src/integrator/whfast.rs:322-466) ----
-    __device__ bool midpoint(double hdt) {
+    // With cm != nullptr the last convergence reduction also carries the sums
+    // of m r and m v over all bodies at the final velocities (cm[0..5]).
+    __device__ bool midpoint(double hdt, double* cm) {
         double x[3] = {0., 0., 0.};
         Pre pr;
         if (planet) {
@@ -203,8 +303,10 @@ struct Large {
         }
         for (int it = 0; it < kMIDPOINT_MAX; ++it) {
             for (int q = 0; q < 3; ++q) { pv[q] = vf[q]; pL[q] = Lf[q]; hpv[q] = hvf[q]; hpL[q] = hLf[q]; }
-            spin_of(c, Lc, Sc);
-            spin_of(hc, hLc, hSc);
+            if (has) {
+                spin_of(c, Lc, Sc);
+                spin_of(hc, hLc, hSc);
+            }
             double aa[3] = {0., 0., 0.}, dl[3] = {0., 0., 0.}, th[3] = {0., 0., 0.};
             if (planet) {
                 const double h0 = vc[0] - hvc[0], h1 = vc[1] - hvc[1], h2 = vc[2] - hvc[2];
@@ -227,16 +329,14 @@ struct Large {
             }
             double vals[BP_SLOTS] = {};
             for (int q = 0; q < 3; ++q) { vals[q] = mr * aa[q]; vals[3 + q] = th[q]; }
-            block_partial(D.bpart, vals, 6, shm);
-            if (!grid_barrier(D)) return false;
             double tot[6];
-            block_totals(D.bpart, tot, 6);
+            if (!grid_reduce(D, vals, 6, tot, shm, warp_bodies, body_rows)) return false;
             // the host's outputs, computed by every thread
             double haa[3], hdl[3];
             for (int q = 0; q < 3; ++q) { haa[q] = -tot[q]; hdl[q] = tot[3 + q]; }
             if (is_host)
                 for (int q = 0; q < 3; ++q) { aa[q] = haa[q]; dl[q] = hdl[q]; }
-            for (int q = 0; q < 3; ++q) {
+            if (has) for (int q = 0; q < 3; ++q) {
                 dvc[q] = hdt * aa[q] - b.ev[q];
                 vf[q] = v0[q] + dvc[q];
                 dLc[q] = hdt * dl[q] - b.eL[q];
@@ -254,15 +354,18 @@ struct Large {
                         cv[1] += vf[q] * vf[q];
                         cv[2] += (Lf[q] - pL[q]) * (Lf[q] - pL[q]);
                         cv[3] += Lf[q] * Lf[q];
+                        cv[4 + q] = c.m * b.r[q];
+                        cv[7 + q] = c.m * vf[q];
                     }
                 }
-                block_partial(D.bpart, cv, 4, shm);
-                if (!grid_barrier(D)) return false;
-                double s4[4];
-                block_totals(D.bpart, s4, 4);
+                const int ns = cm ? 10 : 4;
+                double s4[10];
+                if (!grid_reduce(D, cv, ns, s4, shm, warp_bodies, body_rows)) return false;
+                if (cm)
+                    for (int q = 0; q < 6; ++q) cm[q] = s4[4 + q];
                 if (s4[0] / s4[1] < kDBL_EPSILON_2 && (s4[3] == 0. || s4[2] / s4[3] < kDBL_EPSILON_2)) break;
             }
-            for (int q = 0; q < 3; ++q) {
+            if (has) for (int q = 0; q < 3; ++q) {
                 vc[q] = 0.5 * (v0[q] + vf[q]);
                 Lc[q] = 0.5 * (L0[q] + Lf[q]);
                 Sp[q] = Sc[q];
@@ -271,6 +374,7 @@ struct Large {
                 hSp[q] = hSc[q];
             }
         }
+        if (!has) return true;
         for (int q = 0; q < 3; ++q) {
             b.v[q] = vf[q]; b.L[q] = Lf[q]; b.S[q] = Sc[q];
             b.ev[q] = (vf[q] - v0[q]) - dvc[q];
@@ -288,26 +392,30 @@ struct Large {
     };
 
     // ---- gravity over all ordered pairs, with the pair checks ----
-    __device__ bool gravity() {
+    // pos[] holds heliocentric positions published before the preceding
+    // barrier (differences of heliocentric and of inertial positions agree);
+    // the host sits at -shift (the jump moved every planet by +shift).
+    __device__ bool gravity(const double shift[3]) {
         const int64_t nn = n;
-        if (has)
-            for (int q = 0; q < 3; ++q) D.pos[q * nn + i] = b.r[q];
-        if (!grid_barrier(D)) return false;
         const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
         const int64_t gi = tid % nn, chunk = tid / nn;
         if (chunk < D.nchunk) {
             const int64_t j0 = chunk * nn / D.nchunk, j1 = (chunk + 1) * nn / D.nchunk;
-            const double xi = __ldcg(&D.pos[gi]), yi = __ldcg(&D.pos[nn + gi]), zi = __ldcg(&D.pos[2 * nn + gi]);
+            double xi, yi, zi;
+            if (gi == host) { xi = -shift[0]; yi = -shift[1]; zi = -shift[2]; }
+            else { xi = __ldcg(&D.pos[gi]); yi = __ldcg(&D.pos[nn + gi]); zi = __ldcg(&D.pos[2 * nn + gi]); }
             const double Ri = D.bf[POSI_BF_RADIUS * nn + gi];
             double ax = 0., ay = 0., az = 0.;
             unsigned long long bad = ~0ull;
             for (int64_t j = j0; j < j1; ++j) {
                 if (j == gi) continue;
-                const double dx = xi - __ldcg(&D.pos[j]), dy = yi - __ldcg(&D.pos[nn + j]),
-                             dz = zi - __ldcg(&D.pos[2 * nn + j]);
+                double xj, yj, zj;
+                if (j == host) { xj = -shift[0]; yj = -shift[1]; zj = -shift[2]; }
+                else { xj = __ldcg(&D.pos[j]); yj = __ldcg(&D.pos[nn + j]); zj = __ldcg(&D.pos[2 * nn + j]); }
+                const double dx = xi - xj, dy = yi - yj, dz = zi - zj;
                 const double d2 = dx * dx + dy * dy + dz * dz;
                 if (gi < j && bad == ~0ull) {
-                    const double rr = D.roche[gi * nn + j];
+                    const double rr = D.roche[j * nn + gi];  // symmetric: coalesced across the warp
                     const double Rs = Ri + D.bf[POSI_BF_RADIUS * nn + j];
                     const unsigned long long key = (unsigned long long)(gi * nn + j) * 4ull;
                     if (d2 <= rr * rr) bad = key + POSI_SYS_ROCHE;
@@ -335,56 +443,7 @@ struct Large {
         return true;
     }
 
-    // sums over all bodies (host included) of m * w, for 1 or 2 vectors
-    __device__ bool msum(const double w1[3], const double* w2, bool with_host, double out[6]) {
-        double vals[BP_SLOTS] = {};
-        const bool take = has && (with_host || !is_host);
-        for (int q = 0; q < 3; ++q) {
-            vals[q] = take ? c.m * w1[q] : 0.;
-            vals[3 + q] = (take && w2) ? c.m * w2[q] : 0.;
-        }
-        block_partial(D.bpart, vals, w2 ? 6 : 3, shm);
-        if (!grid_barrier(D)) return false;
-        block_totals(D.bpart, out, w2 ? 6 : 3);
-        return true;
-    }
-
-    // ---- one step (src/integrator/whfast.rs:235-305), democratic heliocentric ----
-    __device__ bool step() {
-        const bool first = last_hist < 0.;
-        if (first || last_hist + hist_period <= t) {
-            spin_of(c, b.L, b.S);
-            spin_of(hc, h.L, h.S);
-            last_hist = first ? 0. : last_hist + hist_period;
-        }
-        if (!midpoint(half_dt)) return false;
-        // inertial -> democratic heliocentric (barycentre and its velocity)
-        double tot[6];
-        if (!msum(b.r, b.v, true, tot)) return false;
-        double Rc[3], Vc[3];
-        for (int q = 0; q < 3; ++q) { Rc[q] = tot[q] / Mtot; Vc[q] = tot[3 + q] / Mtot; }
-        double x[3] = {0., 0., 0.}, u[3] = {0., 0., 0.};
-        if (planet)
-            for (int q = 0; q < 3; ++q) { x[q] = b.r[q] - h.r[q]; u[q] = b.v[q] - Vc[q]; }
-        // Kepler drift, barycentre drift, jump
-        if (!drift(x, u, Rc, Vc)) return false;
-        // back to inertial
-        if (!to_inertial(x, u, Rc, Vc)) return false;
-        if (!gravity()) return false;
-        if (__ldcg(D.bad) != ~0ull) return false;  // frozen at the first failing pair
-        // interaction: u += dt a (inertial accelerations)
-        if (planet)
-            for (int q = 0; q < 3; ++q) u[q] += dt * a[q];
-        if (!jump(x, u)) return false;
-        if (!kepler(x, u)) return false;
-        for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
-        if (!to_inertial(x, u, Rc, Vc)) return false;
-        if (!midpoint(half_dt)) return false;
-        t += dt;
-        return true;
-    }
-
-    __device__ bool kepler(double x[3], double u[3]) {
+    __device__ void kepler(double x[3], double u[3]) {
         if (planet) {
             const KeplerScalars ks = kepler_scalars(hc.mg, x, u);
             bool ok = false;
@@ -394,47 +453,103 @@ struct Large {
             kepler_apply(hc.mg, half_dt, x, u, ks, X, r1, v1);
             for (int q = 0; q < 3; ++q) { x[q] = r1[q]; u[q] = v1[q]; }
         }
-        return true;
     }
 
-    // src/integrator/whfast.rs:507-530: x += dt/2 * sum_p m_p u_p / m_host
-    __device__ bool jump(double x[3], double u[3]) {
-        double P[6];
-        if (!msum(u, nullptr, false, P)) return false;
-        if (planet)
-            for (int q = 0; q < 3; ++q) x[q] += half_dt * P[q] / hc.m;
-        return true;
-    }
-
-    __device__ bool drift(double x[3], double u[3], double Rc[3], const double Vc[3]) {
-        kepler(x, u);
-        for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
-        return jump(x, u);
-    }
-
-    // src/integrator/whfast.rs:1082-1155
-    __device__ bool to_inertial(const double x[3], const double u[3], const double Rc[3], const double Vc[3]) {
-        double tot[6];
-        if (!msum(x, u, false, tot)) return false;
+    // inertial positions and velocities from the heliocentric x, barycentric
+    // u, the barycentre (Rc, Vc) and the sums S[0..2] = sum_p m_p x_p,
+    // S[3..5] = sum_p m_p u_p (src/integrator/whfast.rs:1082-1155)
+    __device__ void to_inertial(const double x[3], const double u[3], const double Rc[3], const double Vc[3],
+                                const double S[6]) {
+        if (!has) return;
         for (int q = 0; q < 3; ++q) {
-            h.r[q] = Rc[q] - tot[q] / Mtot;
-            h.v[q] = Vc[q] - tot[3 + q] / hc.m;
+            h.r[q] = Rc[q] - S[q] * inv_M;
+            h.v[q] = Vc[q] - S[3 + q] * inv_hm;
         }
         if (planet)
             for (int q = 0; q < 3; ++q) { b.r[q] = x[q] + h.r[q]; b.v[q] = u[q] + Vc[q]; }
         if (is_host)
             for (int q = 0; q < 3; ++q) { b.r[q] = h.r[q]; b.v[q] = h.v[q]; }
+    }
+
+    // ---- one step (src/integrator/whfast.rs:235-305), democratic heliocentric ----
+    // Eleven grid barriers: four per half kick (three midpoint iterations),
+    // one for the jump and back-transform of the first drift (the positions
+    // for the pair loop published before it), one for the pair loop, one
+    // for the back-transform of the second drift.  The second jump uses the
+    // planets' total momentum from the first: the interaction kick adds
+    // dt sum_p m_p a_p, which is zero (the planets' mutual forces cancel and
+    // the host's are left out of the kick).
+    __device__ bool step() {
+        const bool first = last_hist < 0.;
+        if (first || last_hist + hist_period <= t) {
+            spin_of(c, b.L, b.S);
+            spin_of(hc, h.L, h.S);
+            last_hist = first ? 0. : last_hist + hist_period;
+        }
+        double cm[6];
+        if (!midpoint(half_dt, cm)) return false;
+        // inertial -> democratic heliocentric
+        double Rc[3], Vc[3], x[3] = {0., 0., 0.}, u[3] = {0., 0., 0.};
+        for (int q = 0; q < 3; ++q) { Rc[q] = cm[q] * inv_M; Vc[q] = cm[3 + q] * inv_M; }
+        if (planet)
+            for (int q = 0; q < 3; ++q) { x[q] = b.r[q] - h.r[q]; u[q] = b.v[q] - Vc[q]; }
+        // part 1: Kepler drift (and the barycentre's), jump, back to inertial
+        kepler(x, u);
+        for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
+        double vals[BP_SLOTS] = {};
+        if (planet) {
+            for (int q = 0; q < 3; ++q) {
+                D.pos[q * n + i] = x[q];
+                vals[q] = c.m * x[q];
+                vals[3 + q] = c.m * u[q];
+            }
+        }
+        double S[6];
+        if (!grid_reduce(D, vals, 6, S, shm, warp_bodies, body_rows)) return false;
+        double shift[3];
+        for (int q = 0; q < 3; ++q) {
+            shift[q] = half_dt * S[3 + q] * inv_hm;        // jump: dt/2 P / m_host
+            S[q] += shift[q] * (Mtot - hc.m);              // sum_p m_p (x_p + shift)
+        }
+        const double P[3] = {S[3], S[4], S[5]};
+        if (planet)
+            for (int q = 0; q < 3; ++q) x[q] += shift[q];
+        to_inertial(x, u, Rc, Vc, S);
+        // gravity and the interaction kick
+        if (!gravity(shift)) return false;
+        if (__ldcg(D.bad) != ~0ull) return false;  // frozen at the first failing pair
+        if (planet)
+            for (int q = 0; q < 3; ++q) u[q] += dt * a[q];
+        // part 2: jump, Kepler drift, back to inertial
+        if (planet)
+            for (int q = 0; q < 3; ++q) x[q] += half_dt * P[q] * inv_hm;
+        kepler(x, u);
+        for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
+        for (int q = 0; q < 6; ++q) vals[q] = 0.;
+        if (planet)
+            for (int q = 0; q < 3; ++q) { vals[q] = c.m * x[q]; vals[3 + q] = c.m * u[q]; }
+        if (!grid_reduce(D, vals, 6, S, shm, warp_bodies, body_rows)) return false;
+        to_inertial(x, u, Rc, Vc, S);
+        if (!midpoint(half_dt, nullptr)) return false;
+        t += dt;
         return true;
     }
 };
 
 __global__ void __launch_bounds__(kBlock) large_steps_kernel(LDev D, int64_t n_steps) {
-    __shared__ double shm[(kBlock / 32) * BP_SLOTS];
+    __shared__ double shm[(kBlock / 32 + 1) * BP_SLOTS];
     Large S(D, shm);
     S.n = D.n;
-    S.i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // bodies spread over the blocks, at most one warp of bodies per SMSP
+    // while the grid has room: the per-body work runs on as many SMSPs as it can
+    S.i = threadIdx.x < D.per_block ? (int64_t)blockIdx.x * D.per_block + threadIdx.x : INT64_MAX;
     S.host = (int)D.si[POSI_SI_HOST];
     S.has = S.i < S.n;
+    {
+        const int64_t warp_first = (int64_t)blockIdx.x * D.per_block + (threadIdx.x & ~31);
+        S.warp_bodies = (int)(threadIdx.x & ~31) < D.per_block && warp_first < S.n;
+        S.body_rows = (unsigned)((S.n + D.per_block - 1) / D.per_block);
+    }
     S.is_host = S.has && S.i == S.host;
     S.planet = S.has && !S.is_host;
     S.tides = D.si[POSI_SI_TIDES] != 0;
@@ -460,11 +575,11 @@ __global__ void __launch_bounds__(kBlock) large_steps_kernel(LDev D, int64_t n_s
     {
         double vals[BP_SLOTS] = {};
         vals[0] = S.has ? S.c.m : 0.;
-        block_partial(D.bpart, vals, 1, shm);
-        if (!grid_barrier(D)) return;
         double tot[1];
-        block_totals(D.bpart, tot, 1);
+        if (!grid_reduce(D, vals, 1, tot, shm, S.warp_bodies, S.body_rows)) return;
         S.Mtot = tot[0];
+        S.inv_M = 1. / S.Mtot;
+        S.inv_hm = 1. / S.hc.m;
     }
     const bool live = (D.si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) == 0;
     int64_t done = 0;
