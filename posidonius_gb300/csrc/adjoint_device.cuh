@@ -29,6 +29,7 @@
 
 #include "../../include/posidonius_gb300.h"
 #include "adjoint_effects.cuh"
+#include "adjoint_record.h"
 
 namespace posi_adj {
 
@@ -65,17 +66,12 @@ struct AdjSmem {
 
 enum { AC_PX = 0, AC_PY, AC_PZ, AC_VX, AC_VY, AC_VZ, AC_H0, AC_H1, AC_H2, AC_Q0, AC_Q1, AC_Q2,
        AC_LA0, AC_LA1, AC_LA2, AC_LD0, AC_LD1, AC_LD2, AC_M, AC_MG, AC_R, AC_MOI, AC_SIG, AC_K2, AC_K2F, AC_K,
-       AC_COUNT };
+       AC_SKIP, AC_COUNT };
 static_assert(AC_COUNT <= kACARD, "card");
 
-// Per-step record written by the record kernel and read back, field by
-// field, by the reverse sweep: [field][body of the ensemble] for each step.
-// Midpoint blocks: iteration count, then per iteration (v, L, previous spin).
-enum {
-    SV_TRIG = 0, SV_R0 = 1, SV_RJA = 4, SV_VJA = 7, SV_X1 = 10, SV_RJB = 11, SV_VJB = 14, SV_RG = 17, SV_VJC = 20,
-    SV_X2 = 23, SV_R2 = 24, SV_H1 = 27, SV_MID = 1 + 9 * kMIDPOINT_MAX, SV_H2 = SV_H1 + SV_MID,
-    SV_COUNT = SV_H2 + SV_MID
-};
+// Per-step record (adjoint_record.h).
+using namespace posi_rec;
+static_assert(kMidMax == kMIDPOINT_MAX, "record layout");
 
 struct SaveRef {
     double* p;
@@ -91,7 +87,7 @@ struct AdjSys {
     double dt, half_dt, t, last_hist, hist_period;
     double *xs, *card, *sums, *gm, *geta, *gord;
     // own body constants
-    double m, mg, R, moi, sig, k2, k2f, mr, kep_gm, eta_q, eta_prev, M;
+    double m, mg, R, moi, sig, k2, k2f, mr, kep_gm, eta_q, eta_prev, M, inv_moi;
     int tk, fk, gk;
     // state
     double r[3], v[3], L[3], S[3], ev[3], eL[3];
@@ -140,7 +136,7 @@ struct AdjSys {
         errf = 0;
         const int64_t st = D.stride;
         const int64_t k = (int64_t)s * D.nmax + lane;
-        m = mg = R = moi = sig = k2 = k2f = 0.;
+        m = mg = R = moi = sig = k2 = k2f = inv_moi = 0.;
         tk = fk = gk = 0;
         if (has) {
             const double* F = D.bf + k;
@@ -151,6 +147,7 @@ struct AdjSys {
             sig = F[POSI_BF_SIGMA * st];
             k2 = F[POSI_BF_K2 * st];
             k2f = F[POSI_BF_K2F * st];
+            inv_moi = moi != 0. ? 1. / moi : 0.;
             tk = (int)D.bi[POSI_BI_TIDES_KIND * st + k];
             fk = (int)D.bi[POSI_BI_FLAT_KIND * st + k];
             gk = (int)D.bi[POSI_BI_GR_KIND * st + k];
@@ -202,7 +199,7 @@ struct AdjSys {
     }
     __device__ __forceinline__ void spin_of(const double Lc[3], double out[3]) {
         if (has && moi != 0.) {
-            const double im = 1. / moi;
+            const double im = inv_moi;
             out[0] = Lc[0] * im; out[1] = Lc[1] * im; out[2] = Lc[2] * im;
         } else {
             out[0] = out[1] = out[2] = 0.;
@@ -457,8 +454,12 @@ struct AdjSys {
         double lvf[3], lLf[3], lSn[3], lv0[3] = {0., 0., 0.}, lL0[3] = {0., 0., 0.};
         for (int c = 0; c < 3; ++c) { lvf[c] = lv[c]; lLf[c] = lL[c]; lSn[c] = lS[c]; }
         // the iteration count is group-uniform: every lane takes the host's
+        // (clamped: a record is never trusted to bound a loop)
         sync();
-        if (is_host) card[AC_K] = sv(base);
+        if (is_host) {
+            const double kr = sv(base);
+            card[AC_K] = (kr >= 0. && kr <= (double)kMIDPOINT_MAX) ? kr : 0.;
+        }
         sync();
         const int K = (int)card[AC_K];
         for (int i = K - 1; i >= 0; --i) {
@@ -475,7 +476,7 @@ struct AdjSys {
             spin_of(Lc, Sc);
             double lvc[3], lSc[3], lSp[3];
             effects_vjp(pr, bp, vc, Sc, Sp, la, ld, lvc, lSc, lSp);
-            const double im = (has && moi != 0.) ? 1. / moi : 0.;
+            const double im = has ? inv_moi : 0.;
             for (int c = 0; c < 3; ++c) {
                 lSc[c] += lSn[c];
                 const double lLc = lSc[c] * im;
@@ -682,6 +683,12 @@ struct AdjSys {
     // Adjoint of one step: lam (r, v, L, S) of the output -> of the input.
     __device__ void step_vjp(const SaveRef& sv, double lr[3], double lv[3], double lL[3], double lS[3],
                              double& gsig, double& gk2) {
+        // a step the forward run did not take (the system was frozen): the
+        // adjoint passes through unchanged
+        sync();
+        if (is_host) card[AC_SKIP] = sv(SV_TRIG) < 0. ? 1. : 0.;
+        sync();
+        if (card[AC_SKIP] != 0.) return;
         double r0[3], rjA[3], vjA[3], rjB[3], rg[3], vjC[3], r2[3], X1 = 0., X2 = 0.;
         bool trig = false;
         for (int c = 0; c < 3; ++c) r0[c] = rjA[c] = vjA[c] = rjB[c] = rg[c] = vjC[c] = r2[c] = 0.;

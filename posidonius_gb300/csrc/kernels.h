@@ -20,9 +20,12 @@ struct DevView {
     int32_t n_list;
     int32_t* step_flags;
     double* hist;
+    double* rec;
 };
 
-enum KernelOp { OP_STEPS = 0, OP_INIT = 1, OP_GRAVITY = 2, OP_EFFECTS = 3 };
+// OP_STEPS_REC: OP_STEPS writing the adjoint's step records to DevView::rec
+// (FAST build only).
+enum KernelOp { OP_STEPS = 0, OP_INIT = 1, OP_GRAVITY = 2, OP_EFFECTS = 3, OP_STEPS_REC = 4 };
 
 struct LaunchArgs {
     int op;

@@ -15,6 +15,7 @@ static cudaError_t launch_g(const posi::DevView& v, const posi::LaunchArgs& a, c
     d.roche = v.roche; d.tables = v.tables; d.list = v.list; d.n_list = v.n_list;
     d.step_flags = v.step_flags;
     d.hist = v.hist;
+    d.rec = v.rec;
     const int threads = posi::kBlockThreads;
     const int groups_per_block = threads / G;
     const int blocks = (int)((v.n_list + groups_per_block - 1) / groups_per_block);
@@ -24,6 +25,12 @@ static cudaError_t launch_g(const posi::DevView& v, const posi::LaunchArgs& a, c
         case posi::OP_STEPS:
             whfast_steps_kernel<G><<<blocks, threads, smem, stream>>>(d, a.n_steps);
             break;
+#if !POSI_EXACT
+        case posi::OP_STEPS_REC:
+            if (!d.rec) return cudaErrorInvalidValue;
+            whfast_steps_kernel<G, true><<<blocks, threads, smem, stream>>>(d, a.n_steps);
+            break;
+#endif
         case posi::OP_INIT:
             init_physical_kernel<G><<<blocks, threads, smem, stream>>>(d);
             break;
@@ -44,6 +51,9 @@ static cudaError_t prepare_g() {
     const int smem = (posi::kBlockThreads / G) * GroupSmem<G>::bytes;
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(whfast_steps_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
+#if !POSI_EXACT
+    if ((e = cudaFuncSetAttribute(whfast_steps_kernel<G, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
+#endif
     if ((e = cudaFuncSetAttribute(init_physical_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(gravity_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
     return cudaFuncSetAttribute(additional_effects_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

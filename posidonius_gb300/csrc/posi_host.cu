@@ -115,6 +115,7 @@ struct posi_batch {
         v.list = d_list + list_offset; v.n_list = count;
         v.step_flags = d_flags;
         v.hist = d_hist;
+        v.rec = nullptr;
         return v;
     }
     cudaError_t launch(const Bucket& bk, const LaunchArgs& a0) const {
@@ -1129,7 +1130,21 @@ int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_
         CK(cudaEventRecord(marks[(size_t)c * 3], b->stream));
         if ((rc = adj_copy_state(a, c, false)) != POSI_OK) break;
         const int64_t len = std::min(a->every, a->n_steps - c * a->every);
-        for (const Bucket& bk : a->buckets) CK(posi::launch_adjoint(adj_view(a, bk), 0, len, bk.G, b->stream));
+        if (b->mode == POSI_MODE_FAST) {
+            // re-integrate the chunk with the forward kernel itself, writing
+            // the step records as it goes
+            LaunchArgs la{};
+            la.op = posi::OP_STEPS_REC;
+            la.n_steps = len;
+            for (const Bucket& bk : b->buckets) {
+                la.G = bk.G;
+                DevView v = b->view(bk.offset, bk.count);
+                v.rec = a->d_tape;
+                CK(posi::launch_fast(v, la, b->stream));
+            }
+        } else {
+            for (const Bucket& bk : a->buckets) CK(posi::launch_adjoint(adj_view(a, bk), 0, len, bk.G, b->stream));
+        }
         CK(cudaEventRecord(marks[(size_t)c * 3 + 1], b->stream));
         for (const Bucket& bk : a->buckets) CK(posi::launch_adjoint(adj_view(a, bk), 1, len, bk.G, b->stream));
         CK(cudaEventRecord(marks[(size_t)c * 3 + 2], b->stream));

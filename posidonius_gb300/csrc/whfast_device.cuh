@@ -40,6 +40,7 @@
 #include <cstdint>
 
 #include "../../include/posidonius_gb300.h"
+#include "adjoint_record.h"
 
 #ifndef POSI_EXACT
 #error "POSI_EXACT must be defined (1: reference operation order, 0: fast)"
@@ -113,6 +114,7 @@ struct Dev {
     int32_t n_list;
     int32_t* step_flags;           // per system: bit0 recovery trigger, bit1 historic trigger
     double* hist;                  // optional: [n_sys][nmax][HR_COUNT], last historic record
+    double* rec;                   // optional: adjoint step records [step][POSI_REC_COUNT][stride]
 };
 
 // Per-planet constants of one half kick, slot k of lane j at P[k * G + j].
@@ -180,6 +182,13 @@ struct Sys {
     // own body
     bool has, is_host;
     Body b;
+    // adjoint step record of the current step (null: none)
+    double* rp;
+    int64_t rst;
+    double kep_x;
+    __device__ __forceinline__ void recw(int f, double v) const {
+        if (rp && has) rp[(int64_t)f * rst] = v;
+    }
 #if !POSI_EXACT
     // mass-only constants of the launch
     double inv_m, inv_moi, inv_eta_excl, jac_c, eta_incl, kep_gm, gm_neg, whds_f, whds_w, dh_w;
@@ -219,6 +228,9 @@ struct Sys {
     // load / store
     // ------------------------------------------------------------------
     __device__ void load(const Dev& D, int sys, int lane_, unsigned mask_, double* smem) {
+        rp = nullptr;
+        rst = D.stride;
+        kep_x = 0.;
         s = sys;
         lane = lane_;
         mask = mask_;
@@ -1011,7 +1023,7 @@ struct Sys {
     // ------------------------------------------------------------------
     // src/integrator/whfast.rs:322-466 implicit midpoint with Kahan sums
     // ------------------------------------------------------------------
-    __device__ void integrate_velocity_dependent_forces(const Dev& D, double hdt, bool evolution) {
+    __device__ void integrate_velocity_dependent_forces(const Dev& D, double hdt, bool evolution, int rbase = -1) {
         // heliocentric positions are fixed during the iterations
         sync();
         if (is_host) { card[HC_PX] = b.r[0]; card[HC_PY] = b.r[1]; card[HC_PZ] = b.r[2];
@@ -1029,6 +1041,14 @@ struct Sys {
             double pv[3], pL[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k) { pv[k] = fv[k]; pL[k] = fL[k]; }
+            if (rbase >= 0) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    recw(rbase + 1 + 9 * it + k, b.v[k]);
+                    recw(rbase + 4 + 9 * it + k, b.L[k]);
+                    recw(rbase + 7 + 9 * it + k, b.S[k]);
+                }
+            }
             additional_effects(D, it, evolution && it == 0);
             if (fatal()) return;
             if (has) {
@@ -1069,6 +1089,7 @@ struct Sys {
             }
         }
         mid_iters = iters;
+        if (rbase >= 0) recw(rbase, (double)iters);
         if (!converged) status |= POSI_SYS_WARN_NONCONVERGED;
         if (has) {
 #pragma unroll
@@ -1557,6 +1578,7 @@ struct Sys {
             ri = 1. / (r0 + e);
         }
         if (isnan(ri)) { ri = 0.; gs[1] = 0.; gs[2] = 0.; gs[3] = 0.; }
+        kep_x = x;
         const double f = -mass_g * gs[2] * r0i;
         const double g = kdt - mass_g * gs[3];
         const double fd = -mass_g * gs[1] * r0i * ri;
@@ -1687,21 +1709,43 @@ struct Sys {
             n_hist += 1;
         }
         const int ignore = coords == POSI_JACOBI ? 1 : 2;
-        integrate_velocity_dependent_forces(D, half_dt, true);
+        if (rp) {
+            recw(posi_rec::SV_TRIG, (first || hist_trig) ? 1. : 0.);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) recw(posi_rec::SV_R0 + k, b.r[k]);
+        }
+        integrate_velocity_dependent_forces(D, half_dt, true, rp ? posi_rec::SV_H1 : -1);
         if (fatal()) return false;
         inertial_to_alternative();
+        if (rp)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { recw(posi_rec::SV_RJA + k, b.ap[k]); recw(posi_rec::SV_VJA + k, b.av[k]); }
         kepler_steps(half_dt);
+        if (rp && planet()) recw(posi_rec::SV_X1, kep_x);
         jump_step(half_dt);
+        if (rp)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { recw(posi_rec::SV_RJB + k, b.ap[k]); recw(posi_rec::SV_VJB + k, b.av[k]); }
         alternative_to_inertial();
+        if (rp)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) recw(posi_rec::SV_RG + k, b.r[k]);
         if (fatal()) return false;
         gravity(D, ignore);
         if (fatal()) return false;
         interaction_step(dt);
         jump_step(half_dt);
+        if (rp)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) recw(posi_rec::SV_VJC + k, b.av[k]);
         kepler_steps(half_dt);
+        if (rp && planet()) recw(posi_rec::SV_X2, kep_x);
         alternative_to_inertial();
+        if (rp)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) recw(posi_rec::SV_R2 + k, b.r[k]);
         if (fatal()) return false;
-        integrate_velocity_dependent_forces(D, half_dt, false);
+        integrate_velocity_dependent_forces(D, half_dt, false, rp ? posi_rec::SV_H2 : -1);
         if (fatal()) return false;
         t += dt;
         iteration += 1;
@@ -1735,7 +1779,7 @@ __device__ __forceinline__ bool group_setup(const Dev& D, int& sys, int& lane, u
 // Advance each listed system by up to n_steps steps (the plain path launches
 // it with one system and n_steps = 1; the batched path with many systems and
 // many steps per launch).
-template <int G>
+template <int G, bool REC = false>
 __global__ void __launch_bounds__(128) whfast_steps_kernel(Dev D, int64_t n_steps) {
     int sys, lane;
     unsigned mask;
@@ -1743,9 +1787,28 @@ __global__ void __launch_bounds__(128) whfast_steps_kernel(Dev D, int64_t n_step
     if (!group_setup<G>(D, sys, lane, mask, smem)) return;
     Sys<G> S;
     S.load(D, sys, lane, mask, smem);
+    S.rp = nullptr;
+    S.rst = D.stride;
+    int64_t k = 0;
     if (!S.fatal()) {
-        for (int64_t k = 0; k < n_steps; ++k) {
-            if (!S.iterate(D)) break;
+        for (; k < n_steps; ++k) {
+            // with REC, step k's record (the adjoint re-integration of a chunk)
+            if (REC) S.rp = D.rec + k * posi_rec::SV_COUNT * D.stride + (int64_t)sys * D.nmax + lane;
+            if (!S.iterate(D)) {
+                // a completed step keeps its record; an abandoned one does not
+                if ((S.status & POSI_SYS_FATAL_MASK) == POSI_SYS_COMPLETED) ++k;
+                break;
+            }
+        }
+    }
+    if (REC) {
+        // steps the system did not take: "no step" records (the reverse
+        // sweep passes them through unchanged)
+        for (; k < n_steps; ++k) {
+            S.rp = D.rec + k * posi_rec::SV_COUNT * D.stride + (int64_t)sys * D.nmax + lane;
+            S.recw(posi_rec::SV_TRIG, -1.);
+            S.recw(posi_rec::SV_H1, 0.);
+            S.recw(posi_rec::SV_H2, 0.);
         }
     }
     S.store(D);

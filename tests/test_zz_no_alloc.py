@@ -37,7 +37,9 @@ def test_static_adjoint_matches_allocating_adjoint_twice():
     torch = pytest.importorskip("torch")
     n_steps = 30
     ens, el, ms, moi, ss = A.gradient_workload(12, seed=5)
-    batch = pg.Batch(ens, mode=pg.FAST)
+    # an EXACT batch: its backward pass re-integrates with the adjoint's own
+    # forward, as the allocation-free entry point does
+    batch = pg.Batch(ens, mode=pg.EXACT)
     batch.initialize_physical_values()
     state = batch.get_state()
     ns, nm = batch.n_sys, batch.nmax
