@@ -510,6 +510,162 @@ def emit(name, builder):
     return L, [n.name for n in pre_in], [n.name for n in it_in], cst_names, NPRE, len(it_fwd), len(body)
 
 
+def emit_jvp(name, builder):
+    """Forward-mode (tangent) versions of one block, for NT tangent directions
+    (a template parameter): <block>_pre_jvp (values and tangents of the pre
+    values) and <block>_iter_jvp (outputs and their tangents)."""
+    global GRAPH
+    GRAPH = g = Graph()
+    outs = builder(g)
+    live = _live(outs)
+    nodes = [n for n in g.nodes if n.id in live]
+    names = {}
+    for n in nodes:
+        if n.op == "lit":
+            names[n.id] = _fmt(n.val)
+        elif n.op == "in":
+            names[n.id] = f"in_{n.name}"
+        elif n.op == "cst":
+            names[n.id] = n.name if n.name in GLOBALS else f"c_{n.name}"
+        else:
+            names[n.id] = f"t{n.id}"
+    grad, pre = {}, {}
+    for n in nodes:
+        if n.op == "in":
+            grad[n.id] = True
+            pre[n.id] = n.name in PRE_INPUTS
+        elif n.op in ("lit", "cst"):
+            grad[n.id] = False
+            pre[n.id] = True
+        else:
+            grad[n.id] = any(grad[a.id] for a in n.args)
+            pre[n.id] = all(pre[a.id] for a in n.args)
+    inputs, consts = list(g.inputs), list(g.consts)
+    pre_in = [n for n in inputs if n.name in PRE_INPUTS]
+    it_in = [n for n in inputs if n.name not in PRE_INPUTS]
+    cst_names = sorted({n.name for n in consts if n.name not in GLOBALS})
+    it_nodes = [n for n in nodes if not pre[n.id]]
+    pre_nodes = [n for n in nodes if pre[n.id] and n.op not in ("lit", "cst")]
+    used, seen = [], set()
+    for n in it_nodes:
+        for a in n.args:
+            if pre[a.id] and a.op not in ("lit", "cst") and a.id not in seen:
+                seen.add(a.id)
+                used.append(a)
+    for o in outs:
+        if pre[o.id] and o.op not in ("lit", "cst") and o.id not in seen:
+            seen.add(o.id)
+            used.append(o)
+    slot = {n.id: k for k, n in enumerate(used)}
+    sig_c = ", ".join(f"double c_{x}" for x in cst_names)
+    sig_pre_in = ", ".join(f"double in_{n.name}" for n in pre_in)
+    sig_it_in = ", ".join(f"double in_{n.name}" for n in it_in)
+
+    def tangent_lines(node_list, nm, dn):
+        """dn(node) -> C expression of its tangent array element [k]."""
+        L = []
+        for n in node_list:
+            if n.op in ("lit", "cst", "in") or not grad[n.id]:
+                continue
+            a = n.args
+            an = [nm[x.id] for x in a]
+            da = [dn(x) if grad[x.id] else None for x in a]
+            if n.op == "add":
+                e = " + ".join(d for d in da if d) or "0.0"
+            elif n.op == "sub":
+                e = da[0] if da[0] else ""
+                if da[1]:
+                    e = f"{e} - {da[1]}" if e else f"-{da[1]}"
+            elif n.op == "neg":
+                e = f"-{da[0]}"
+            elif n.op == "mul":
+                if a[0].id == a[1].id:
+                    e = f"2.0 * {an[0]} * {da[0]}"
+                else:
+                    terms = []
+                    if da[0]:
+                        terms.append(f"{da[0]} * {an[1]}")
+                    if da[1]:
+                        terms.append(f"{an[0]} * {da[1]}")
+                    e = " + ".join(terms)
+            elif n.op == "div":
+                if da[0] and da[1]:
+                    e = f"({da[0]} - {nm[n.id]} * {da[1]}) / {an[1]}"
+                elif da[0]:
+                    e = f"{da[0]} / {an[1]}"
+                else:
+                    e = f"-{nm[n.id]} * {da[1]} / {an[1]}"
+            elif n.op == "sqrt":
+                e = f"0.5 * {da[0]} / {nm[n.id]}"
+            L.append(f"    double d{n.id}[NT];")
+            L.append(f"#pragma unroll")
+            L.append(f"    for (int k = 0; k < NT; ++k) d{n.id}[k] = {e};")
+        return L
+
+    out = []
+    # ---- pre JVP
+    out.append(f"// {name}: pre values and their tangents (din[i * NT + k]: tangent k of pre input i).")
+    out.append("template <int NT>")
+    out.append(f"__host__ __device__ __forceinline__ void {name}_pre_jvp({sig_pre_in},")
+    out.append(f"        {sig_c}, const double* __restrict__ din, double* __restrict__ pre,")
+    out.append("        double* __restrict__ dpre) {")
+    for n in pre_nodes:
+        if n.op != "in":
+            out.append(f"    const double {names[n.id]} = {_expr(n, names)};")
+    in_idx = {n.id: k for k, n in enumerate(pre_in)}
+
+    def dn_pre(x):
+        if x.op == "in":
+            return f"din[{in_idx[x.id]} * NT + k]"
+        return f"d{x.id}[k]"
+    out.extend(tangent_lines(pre_nodes, names, dn_pre))
+    for n in used:
+        out.append(f"    pre[{slot[n.id]}] = {names[n.id]};")
+        if grad[n.id]:
+            out.append(f"#pragma unroll")
+            out.append(f"    for (int k = 0; k < NT; ++k) dpre[{slot[n.id]} * NT + k] = {dn_pre(n)};")
+        else:
+            out.append(f"#pragma unroll")
+            out.append(f"    for (int k = 0; k < NT; ++k) dpre[{slot[n.id]} * NT + k] = 0.0;")
+    out.append("}")
+    out.append("")
+    # ---- iteration JVP
+    nm = dict(names)
+    for n in used:
+        nm[n.id] = f"pre[{slot[n.id]}]"
+    it_idx = {n.id: k for k, n in enumerate(it_in)}
+
+    def dn_it(x):
+        if x.id in slot:
+            return f"dpre[{slot[x.id]} * NT + k]"
+        if x.op == "in":
+            return f"din[{it_idx[x.id]} * NT + k]"
+        return f"d{x.id}[k]"
+    out.append(f"// {name}: one iteration, outputs and their tangents (din[i * NT + k] for the")
+    out.append(f"// iteration inputs; dout[o * NT + k]).")
+    out.append("template <int NT>")
+    out.append(f"__host__ __device__ __forceinline__ void {name}_iter_jvp(const double* __restrict__ pre,")
+    out.append(f"        const double* __restrict__ dpre, {sig_it_in},")
+    out.append(f"        {sig_c}, const double* __restrict__ din, double* __restrict__ out,")
+    out.append("        double* __restrict__ dout) {")
+    for n in it_nodes:
+        if n.op != "in":
+            out.append(f"    const double {nm[n.id]} = {_expr(n, nm)};")
+    # grad of pre values used: they are grad if the pre node is grad
+    out.extend(tangent_lines([n for n in it_nodes], nm, lambda x: dn_it(x) if (grad[x.id]) else None))
+    for k_o, o in enumerate(outs):
+        out.append(f"    out[{k_o}] = {nm[o.id]};")
+        if grad[o.id]:
+            out.append(f"#pragma unroll")
+            out.append(f"    for (int k = 0; k < NT; ++k) dout[{k_o} * NT + k] = {dn_it(o)};")
+        else:
+            out.append(f"#pragma unroll")
+            out.append(f"    for (int k = 0; k < NT; ++k) dout[{k_o} * NT + k] = 0.0;")
+    out.append("}")
+    out.append("")
+    return out
+
+
 def generate():
     blocks = [("adj_tides", block_tides), ("adj_flat", block_flat), ("adj_gr", block_gr)]
     out = ["// adjoint_effects.cuh -- GENERATED by posidonius_gb300/adjoint_codegen.py; do not edit.",
@@ -518,7 +674,8 @@ def generate():
            "// flattening, Kidder 1995 general relativity) in the formulation of the FAST",
            "// build, split for the implicit-midpoint loop: <block>_pre (once per half",
            "// kick: position and tidal-parameter terms), <block>_iter (per iteration),",
-           "// and the reverse sweeps <block>_iter_vjp / <block>_pre_vjp.",
+           "// the reverse sweeps <block>_iter_vjp / <block>_pre_vjp and the",
+           "// forward-mode (tangent) sweeps <block>_pre_jvp / <block>_iter_jvp.",
            "#pragma once",
            "#include <cmath>",
            "",
@@ -532,6 +689,7 @@ def generate():
         out.append(f"// {name}: pre inputs ({', '.join(pin)}); iteration inputs ({', '.join(iin)});")
         out.append(f"// constants ({', '.join(csts)})")
         out.extend(lines)
+        out.extend(emit_jvp(name, fn))
         stats.append((name, npre, nit, nrev))
     out.append("}  // namespace posi_adj")
     out.append("")

@@ -235,6 +235,46 @@ __host__ __device__ __forceinline__ void kepler_vjp(double mu, double dt, const 
     }
 }
 
+// Jacobian-vector product of the drift: tangent (dr, dv) of the start ->
+// tangent (dr1, dv1) of the end, at the converged root X (same derivatives as
+// kepler_vjp, applied forwards).
+__host__ __device__ __forceinline__ void kepler_jvp(double mu, double dt, const double r[3], const double v[3],
+                                                    double X, const double dr[3], const double dv[3], double dr1[3],
+                                                    double dv1[3]) {
+    const KeplerScalars s = kepler_scalars(mu, r, v);
+    double G[6];
+    gfun6(s.beta, X, G);
+    const double r0 = s.r0;
+    const double rr = r0 + s.eta0 * G[1] + s.zeta0 * G[2];
+    const double f = -mu * G[2] / r0;
+    const double g = dt - mu * G[3];
+    const double fd = -mu * G[1] / (r0 * rr);
+    const double gd = -mu * G[2] / rr;
+    const double dr0s = (r[0] * dr[0] + r[1] * dr[1] + r[2] * dr[2]) / r0;
+    const double dv2 = 2. * (v[0] * dv[0] + v[1] * dv[1] + v[2] * dv[2]);
+    const double dbeta = -2. * mu / (r0 * r0) * dr0s - dv2;
+    const double deta = dr[0] * v[0] + dr[1] * v[1] + dr[2] * v[2] + r[0] * dv[0] + r[1] * dv[1] + r[2] * dv[2];
+    const double dzeta = -s.beta * dr0s - r0 * dbeta;
+    const double dG1b = 0.5 * (G[3] - X * G[2]);
+    const double dG2b = 0.5 * (2. * G[4] - X * G[3]);
+    const double dG3b = 0.5 * (3. * G[5] - X * G[4]);
+    const double Fb = s.eta0 * dG2b + s.zeta0 * dG3b;
+    const double dX = -(X * dr0s + G[2] * deta + G[3] * dzeta + Fb * dbeta) / rr;
+    const double dG1 = G[0] * dX + dG1b * dbeta;
+    const double dG2 = G[1] * dX + dG2b * dbeta;
+    const double dG3 = G[2] * dX + dG3b * dbeta;
+    const double drr = dr0s + deta * G[1] + s.eta0 * dG1 + dzeta * G[2] + s.zeta0 * dG2;
+    const double df = -mu * (dG2 * r0 - G[2] * dr0s) / (r0 * r0);
+    const double dg = -mu * dG3;
+    const double den = r0 * rr;
+    const double dfd = -mu * (dG1 * den - G[1] * (dr0s * rr + r0 * drr)) / (den * den);
+    const double dgd = -mu * (dG2 * rr - G[2] * drr) / (rr * rr);
+    for (int k = 0; k < 3; ++k) {
+        dr1[k] = dr[k] + df * r[k] + f * dr[k] + dg * v[k] + g * dv[k];
+        dv1[k] = dv[k] + dfd * r[k] + fd * dr[k] + dgd * v[k] + gd * dv[k];
+    }
+}
+
 // Jacobi interaction term of planet i > 0 (src/integrator/whfast.rs:566-592):
 // v += dt G eta r / (|r|^2 + softening)^(3/2).
 __host__ __device__ __forceinline__ void jacobi_indirect(double dt_g_eta, const double r[3], double dv[3]) {

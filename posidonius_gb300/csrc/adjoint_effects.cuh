@@ -4,7 +4,8 @@
 // flattening, Kidder 1995 general relativity) in the formulation of the FAST
 // build, split for the implicit-midpoint loop: <block>_pre (once per half
 // kick: position and tidal-parameter terms), <block>_iter (per iteration),
-// and the reverse sweeps <block>_iter_vjp / <block>_pre_vjp.
+// the reverse sweeps <block>_iter_vjp / <block>_pre_vjp and the
+// forward-mode (tangent) sweeps <block>_pre_jvp / <block>_iter_jvp.
 #pragma once
 #include <cmath>
 
@@ -701,6 +702,697 @@ __host__ __device__ __forceinline__ void adj_tides_pre_vjp(double in_x, double i
     bin[6] += b_k2_h;
 }
 
+// adj_tides: pre values and their tangents (din[i * NT + k]: tangent k of pre input i).
+template <int NT>
+__host__ __device__ __forceinline__ void adj_tides_pre_jvp(double in_x, double in_y, double in_z, double in_sig_p, double in_sig_h, double in_k2_p, double in_k2_h,
+        double c_R, double c_hR, double c_hm, double c_m, const double* __restrict__ din, double* __restrict__ pre,
+        double* __restrict__ dpre) {
+    const double t18 = in_x * in_x;
+    const double t19 = in_y * in_y;
+    const double t20 = t18 + t19;
+    const double t21 = in_z * in_z;
+    const double t22 = t20 + t21;
+    const double t23 = sqrt(t22);
+    const double t33 = 1.0 / t23;
+    const double t34 = in_x * t33;
+    const double t35 = in_y * t33;
+    const double t36 = in_z * t33;
+    const double t62 = t23 * t23;
+    const double t63 = t23 * t62;
+    const double t64 = t62 * t62;
+    const double t65 = t63 * t64;
+    const double t66 = t23 * t65;
+    const double t67 = c_m * c_m;
+    const double t68 = c_hm * c_hm;
+    const double t69 = c_hR * c_hR;
+    const double t70 = t69 * t69;
+    const double t71 = t70 * t70;
+    const double t72 = t69 * t71;
+    const double t73 = t67 * t72;
+    const double t74 = in_sig_h * t73;
+    const double t75 = c_R * c_R;
+    const double t76 = t75 * t75;
+    const double t77 = t76 * t76;
+    const double t78 = t75 * t77;
+    const double t79 = t68 * t78;
+    const double t80 = in_sig_p * t79;
+    const double t82 = t74 * 4.5;
+    const double t83 = t82 / t65;
+    const double t84 = t80 * 4.5;
+    const double t85 = t84 / t65;
+    const double t88 = kK2 * -3.0;
+    const double t89 = t88 / t65;
+    const double t90 = c_hR * t70;
+    const double t91 = t67 * t90;
+    const double t92 = in_k2_h * t91;
+    const double t93 = c_R * t76;
+    const double t94 = t68 * t93;
+    const double t95 = in_k2_p * t94;
+    const double t96 = t92 + t95;
+    const double t97 = t89 * t96;
+    const double t98 = t33 * t83;
+    const double t99 = t33 * t85;
+    const double t101 = -13.5 / t66;
+    const double t103 = t74 + t80;
+    const double t106 = t83 + t85;
+    const double t107 = t33 * t106;
+    const double t149 = 1.0 / c_m;
+    const double t153 = t23 * t85;
+    const double t154 = t23 * t83;
+    double d18[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d18[k] = 2.0 * in_x * din[0 * NT + k];
+    double d19[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d19[k] = 2.0 * in_y * din[1 * NT + k];
+    double d20[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d20[k] = d18[k] + d19[k];
+    double d21[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d21[k] = 2.0 * in_z * din[2 * NT + k];
+    double d22[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d22[k] = d20[k] + d21[k];
+    double d23[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d23[k] = 0.5 * d22[k] / t23;
+    double d33[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d33[k] = -t33 * d23[k] / t23;
+    double d34[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d34[k] = din[0 * NT + k] * t33 + in_x * d33[k];
+    double d35[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d35[k] = din[1 * NT + k] * t33 + in_y * d33[k];
+    double d36[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d36[k] = din[2 * NT + k] * t33 + in_z * d33[k];
+    double d62[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d62[k] = 2.0 * t23 * d23[k];
+    double d63[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d63[k] = d23[k] * t62 + t23 * d62[k];
+    double d64[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d64[k] = 2.0 * t62 * d62[k];
+    double d65[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d65[k] = d63[k] * t64 + t63 * d64[k];
+    double d66[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d66[k] = d23[k] * t65 + t23 * d65[k];
+    double d74[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d74[k] = din[4 * NT + k] * t73;
+    double d80[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d80[k] = din[3 * NT + k] * t79;
+    double d82[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d82[k] = d74[k] * 4.5;
+    double d83[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d83[k] = (d82[k] - t83 * d65[k]) / t65;
+    double d84[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d84[k] = d80[k] * 4.5;
+    double d85[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d85[k] = (d84[k] - t85 * d65[k]) / t65;
+    double d89[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d89[k] = -t89 * d65[k] / t65;
+    double d92[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d92[k] = din[6 * NT + k] * t91;
+    double d95[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d95[k] = din[5 * NT + k] * t94;
+    double d96[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d96[k] = d92[k] + d95[k];
+    double d97[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d97[k] = d89[k] * t96 + t89 * d96[k];
+    double d98[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d98[k] = d33[k] * t83 + t33 * d83[k];
+    double d99[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d99[k] = d33[k] * t85 + t33 * d85[k];
+    double d101[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d101[k] = -t101 * d66[k] / t66;
+    double d103[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d103[k] = d74[k] + d80[k];
+    double d106[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d106[k] = d83[k] + d85[k];
+    double d107[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d107[k] = d33[k] * t106 + t33 * d106[k];
+    double d153[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d153[k] = d23[k] * t85 + t23 * d85[k];
+    double d154[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d154[k] = d23[k] * t83 + t23 * d83[k];
+    pre[0] = in_x;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[0 * NT + k] = din[0 * NT + k];
+    pre[1] = in_y;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[1 * NT + k] = din[1 * NT + k];
+    pre[2] = in_z;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[2 * NT + k] = din[2 * NT + k];
+    pre[3] = t33;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[3 * NT + k] = d33[k];
+    pre[4] = t101;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[4 * NT + k] = d101[k];
+    pre[5] = t103;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[5 * NT + k] = d103[k];
+    pre[6] = t97;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[6 * NT + k] = d97[k];
+    pre[7] = t107;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[7 * NT + k] = d107[k];
+    pre[8] = t34;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[8 * NT + k] = d34[k];
+    pre[9] = t98;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[9 * NT + k] = d98[k];
+    pre[10] = t99;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[10 * NT + k] = d99[k];
+    pre[11] = t35;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[11 * NT + k] = d35[k];
+    pre[12] = t36;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[12 * NT + k] = d36[k];
+    pre[13] = t149;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[13 * NT + k] = 0.0;
+    pre[14] = t85;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[14 * NT + k] = d85[k];
+    pre[15] = t83;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[15 * NT + k] = d83[k];
+    pre[16] = t153;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[16 * NT + k] = d153[k];
+    pre[17] = t154;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[17 * NT + k] = d154[k];
+}
+
+// adj_tides: one iteration, outputs and their tangents (din[i * NT + k] for the
+// iteration inputs; dout[o * NT + k]).
+template <int NT>
+__host__ __device__ __forceinline__ void adj_tides_iter_jvp(const double* __restrict__ pre,
+        const double* __restrict__ dpre, double in_hv0, double in_hv1, double in_hv2, double in_S0, double in_S1, double in_S2, double in_H0, double in_H1, double in_H2, double in_P0, double in_P1, double in_P2, double in_Q0, double in_Q1, double in_Q2,
+        double c_R, double c_hR, double c_hm, double c_m, const double* __restrict__ din, double* __restrict__ out,
+        double* __restrict__ dout) {
+    const double t37 = pre[0] * in_hv0;
+    const double t38 = pre[1] * in_hv1;
+    const double t39 = t37 + t38;
+    const double t40 = pre[2] * in_hv2;
+    const double t41 = t39 + t40;
+    const double t42 = pre[3] * t41;
+    const double t43 = pre[0] * in_Q0;
+    const double t44 = pre[1] * in_Q1;
+    const double t45 = t43 + t44;
+    const double t46 = pre[2] * in_Q2;
+    const double t47 = t45 + t46;
+    const double t48 = pre[0] * in_P0;
+    const double t49 = pre[1] * in_P1;
+    const double t50 = t48 + t49;
+    const double t51 = pre[2] * in_P2;
+    const double t52 = t50 + t51;
+    const double t53 = pre[1] * in_hv2;
+    const double t54 = pre[2] * in_hv1;
+    const double t55 = t53 - t54;
+    const double t56 = pre[2] * in_hv0;
+    const double t57 = pre[0] * in_hv2;
+    const double t58 = t56 - t57;
+    const double t59 = pre[0] * in_hv1;
+    const double t60 = pre[1] * in_hv0;
+    const double t61 = t59 - t60;
+    const double t102 = t42 * pre[4];
+    const double t104 = t102 * pre[5];
+    const double t105 = pre[6] + t104;
+    const double t108 = t42 * pre[7];
+    const double t109 = t105 + t108;
+    const double t110 = pre[2] * in_H1;
+    const double t111 = pre[1] * in_H2;
+    const double t112 = t110 - t111;
+    const double t113 = pre[0] * in_H2;
+    const double t114 = pre[2] * in_H0;
+    const double t115 = t113 - t114;
+    const double t116 = pre[1] * in_H0;
+    const double t117 = pre[0] * in_H1;
+    const double t118 = t116 - t117;
+    const double t119 = pre[2] * in_S1;
+    const double t120 = pre[1] * in_S2;
+    const double t121 = t119 - t120;
+    const double t122 = pre[0] * in_S2;
+    const double t123 = pre[2] * in_S0;
+    const double t124 = t122 - t123;
+    const double t125 = pre[1] * in_S0;
+    const double t126 = pre[0] * in_S1;
+    const double t127 = t125 - t126;
+    const double t128 = pre[8] * t109;
+    const double t129 = t112 - in_hv0;
+    const double t130 = pre[9] * t129;
+    const double t131 = t128 + t130;
+    const double t132 = t121 - in_hv0;
+    const double t133 = pre[10] * t132;
+    const double t134 = t131 + t133;
+    const double t135 = pre[11] * t109;
+    const double t136 = t115 - in_hv1;
+    const double t137 = pre[9] * t136;
+    const double t138 = t135 + t137;
+    const double t139 = t124 - in_hv1;
+    const double t140 = pre[10] * t139;
+    const double t141 = t138 + t140;
+    const double t142 = pre[12] * t109;
+    const double t143 = t118 - in_hv2;
+    const double t144 = pre[9] * t143;
+    const double t145 = t142 + t144;
+    const double t146 = t127 - in_hv2;
+    const double t147 = pre[10] * t146;
+    const double t148 = t145 + t147;
+    const double t150 = t134 * pre[13];
+    const double t151 = t141 * pre[13];
+    const double t152 = t148 * pre[13];
+    const double t155 = t52 * pre[14];
+    const double t156 = t47 * pre[15];
+    const double t157 = in_S0 * pre[16];
+    const double t158 = pre[8] * t155;
+    const double t159 = t157 - t158;
+    const double t160 = t55 * pre[10];
+    const double t161 = t159 - t160;
+    const double t162 = -t161;
+    const double t163 = in_S1 * pre[16];
+    const double t164 = pre[11] * t155;
+    const double t165 = t163 - t164;
+    const double t166 = t58 * pre[10];
+    const double t167 = t165 - t166;
+    const double t168 = -t167;
+    const double t169 = in_S2 * pre[16];
+    const double t170 = pre[12] * t155;
+    const double t171 = t169 - t170;
+    const double t172 = t61 * pre[10];
+    const double t173 = t171 - t172;
+    const double t174 = -t173;
+    const double t175 = in_H0 * pre[17];
+    const double t176 = pre[8] * t156;
+    const double t177 = t175 - t176;
+    const double t178 = t55 * pre[9];
+    const double t179 = t177 - t178;
+    const double t180 = -t179;
+    const double t181 = in_H1 * pre[17];
+    const double t182 = pre[11] * t156;
+    const double t183 = t181 - t182;
+    const double t184 = t58 * pre[9];
+    const double t185 = t183 - t184;
+    const double t186 = -t185;
+    const double t187 = in_H2 * pre[17];
+    const double t188 = pre[12] * t156;
+    const double t189 = t187 - t188;
+    const double t190 = t61 * pre[9];
+    const double t191 = t189 - t190;
+    const double t192 = -t191;
+    double d37[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d37[k] = dpre[0 * NT + k] * in_hv0 + pre[0] * din[0 * NT + k];
+    double d38[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d38[k] = dpre[1 * NT + k] * in_hv1 + pre[1] * din[1 * NT + k];
+    double d39[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d39[k] = d37[k] + d38[k];
+    double d40[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d40[k] = dpre[2 * NT + k] * in_hv2 + pre[2] * din[2 * NT + k];
+    double d41[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d41[k] = d39[k] + d40[k];
+    double d42[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d42[k] = dpre[3 * NT + k] * t41 + pre[3] * d41[k];
+    double d43[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d43[k] = dpre[0 * NT + k] * in_Q0 + pre[0] * din[12 * NT + k];
+    double d44[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d44[k] = dpre[1 * NT + k] * in_Q1 + pre[1] * din[13 * NT + k];
+    double d45[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d45[k] = d43[k] + d44[k];
+    double d46[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d46[k] = dpre[2 * NT + k] * in_Q2 + pre[2] * din[14 * NT + k];
+    double d47[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d47[k] = d45[k] + d46[k];
+    double d48[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d48[k] = dpre[0 * NT + k] * in_P0 + pre[0] * din[9 * NT + k];
+    double d49[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d49[k] = dpre[1 * NT + k] * in_P1 + pre[1] * din[10 * NT + k];
+    double d50[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d50[k] = d48[k] + d49[k];
+    double d51[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d51[k] = dpre[2 * NT + k] * in_P2 + pre[2] * din[11 * NT + k];
+    double d52[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d52[k] = d50[k] + d51[k];
+    double d53[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d53[k] = dpre[1 * NT + k] * in_hv2 + pre[1] * din[2 * NT + k];
+    double d54[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d54[k] = dpre[2 * NT + k] * in_hv1 + pre[2] * din[1 * NT + k];
+    double d55[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d55[k] = d53[k] - d54[k];
+    double d56[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d56[k] = dpre[2 * NT + k] * in_hv0 + pre[2] * din[0 * NT + k];
+    double d57[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d57[k] = dpre[0 * NT + k] * in_hv2 + pre[0] * din[2 * NT + k];
+    double d58[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d58[k] = d56[k] - d57[k];
+    double d59[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d59[k] = dpre[0 * NT + k] * in_hv1 + pre[0] * din[1 * NT + k];
+    double d60[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d60[k] = dpre[1 * NT + k] * in_hv0 + pre[1] * din[0 * NT + k];
+    double d61[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d61[k] = d59[k] - d60[k];
+    double d102[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d102[k] = d42[k] * pre[4] + t42 * dpre[4 * NT + k];
+    double d104[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d104[k] = d102[k] * pre[5] + t102 * dpre[5 * NT + k];
+    double d105[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d105[k] = dpre[6 * NT + k] + d104[k];
+    double d108[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d108[k] = d42[k] * pre[7] + t42 * dpre[7 * NT + k];
+    double d109[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d109[k] = d105[k] + d108[k];
+    double d110[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d110[k] = dpre[2 * NT + k] * in_H1 + pre[2] * din[7 * NT + k];
+    double d111[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d111[k] = dpre[1 * NT + k] * in_H2 + pre[1] * din[8 * NT + k];
+    double d112[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d112[k] = d110[k] - d111[k];
+    double d113[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d113[k] = dpre[0 * NT + k] * in_H2 + pre[0] * din[8 * NT + k];
+    double d114[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d114[k] = dpre[2 * NT + k] * in_H0 + pre[2] * din[6 * NT + k];
+    double d115[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d115[k] = d113[k] - d114[k];
+    double d116[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d116[k] = dpre[1 * NT + k] * in_H0 + pre[1] * din[6 * NT + k];
+    double d117[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d117[k] = dpre[0 * NT + k] * in_H1 + pre[0] * din[7 * NT + k];
+    double d118[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d118[k] = d116[k] - d117[k];
+    double d119[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d119[k] = dpre[2 * NT + k] * in_S1 + pre[2] * din[4 * NT + k];
+    double d120[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d120[k] = dpre[1 * NT + k] * in_S2 + pre[1] * din[5 * NT + k];
+    double d121[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d121[k] = d119[k] - d120[k];
+    double d122[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d122[k] = dpre[0 * NT + k] * in_S2 + pre[0] * din[5 * NT + k];
+    double d123[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d123[k] = dpre[2 * NT + k] * in_S0 + pre[2] * din[3 * NT + k];
+    double d124[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d124[k] = d122[k] - d123[k];
+    double d125[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d125[k] = dpre[1 * NT + k] * in_S0 + pre[1] * din[3 * NT + k];
+    double d126[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d126[k] = dpre[0 * NT + k] * in_S1 + pre[0] * din[4 * NT + k];
+    double d127[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d127[k] = d125[k] - d126[k];
+    double d128[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d128[k] = dpre[8 * NT + k] * t109 + pre[8] * d109[k];
+    double d129[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d129[k] = d112[k] - din[0 * NT + k];
+    double d130[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d130[k] = dpre[9 * NT + k] * t129 + pre[9] * d129[k];
+    double d131[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d131[k] = d128[k] + d130[k];
+    double d132[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d132[k] = d121[k] - din[0 * NT + k];
+    double d133[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d133[k] = dpre[10 * NT + k] * t132 + pre[10] * d132[k];
+    double d134[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d134[k] = d131[k] + d133[k];
+    double d135[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d135[k] = dpre[11 * NT + k] * t109 + pre[11] * d109[k];
+    double d136[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d136[k] = d115[k] - din[1 * NT + k];
+    double d137[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d137[k] = dpre[9 * NT + k] * t136 + pre[9] * d136[k];
+    double d138[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d138[k] = d135[k] + d137[k];
+    double d139[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d139[k] = d124[k] - din[1 * NT + k];
+    double d140[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d140[k] = dpre[10 * NT + k] * t139 + pre[10] * d139[k];
+    double d141[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d141[k] = d138[k] + d140[k];
+    double d142[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d142[k] = dpre[12 * NT + k] * t109 + pre[12] * d109[k];
+    double d143[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d143[k] = d118[k] - din[2 * NT + k];
+    double d144[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d144[k] = dpre[9 * NT + k] * t143 + pre[9] * d143[k];
+    double d145[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d145[k] = d142[k] + d144[k];
+    double d146[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d146[k] = d127[k] - din[2 * NT + k];
+    double d147[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d147[k] = dpre[10 * NT + k] * t146 + pre[10] * d146[k];
+    double d148[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d148[k] = d145[k] + d147[k];
+    double d150[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d150[k] = d134[k] * pre[13];
+    double d151[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d151[k] = d141[k] * pre[13];
+    double d152[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d152[k] = d148[k] * pre[13];
+    double d155[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d155[k] = d52[k] * pre[14] + t52 * dpre[14 * NT + k];
+    double d156[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d156[k] = d47[k] * pre[15] + t47 * dpre[15 * NT + k];
+    double d157[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d157[k] = din[3 * NT + k] * pre[16] + in_S0 * dpre[16 * NT + k];
+    double d158[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d158[k] = dpre[8 * NT + k] * t155 + pre[8] * d155[k];
+    double d159[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d159[k] = d157[k] - d158[k];
+    double d160[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d160[k] = d55[k] * pre[10] + t55 * dpre[10 * NT + k];
+    double d161[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d161[k] = d159[k] - d160[k];
+    double d162[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d162[k] = -d161[k];
+    double d163[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d163[k] = din[4 * NT + k] * pre[16] + in_S1 * dpre[16 * NT + k];
+    double d164[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d164[k] = dpre[11 * NT + k] * t155 + pre[11] * d155[k];
+    double d165[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d165[k] = d163[k] - d164[k];
+    double d166[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d166[k] = d58[k] * pre[10] + t58 * dpre[10 * NT + k];
+    double d167[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d167[k] = d165[k] - d166[k];
+    double d168[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d168[k] = -d167[k];
+    double d169[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d169[k] = din[5 * NT + k] * pre[16] + in_S2 * dpre[16 * NT + k];
+    double d170[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d170[k] = dpre[12 * NT + k] * t155 + pre[12] * d155[k];
+    double d171[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d171[k] = d169[k] - d170[k];
+    double d172[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d172[k] = d61[k] * pre[10] + t61 * dpre[10 * NT + k];
+    double d173[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d173[k] = d171[k] - d172[k];
+    double d174[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d174[k] = -d173[k];
+    double d175[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d175[k] = din[6 * NT + k] * pre[17] + in_H0 * dpre[17 * NT + k];
+    double d176[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d176[k] = dpre[8 * NT + k] * t156 + pre[8] * d156[k];
+    double d177[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d177[k] = d175[k] - d176[k];
+    double d178[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d178[k] = d55[k] * pre[9] + t55 * dpre[9 * NT + k];
+    double d179[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d179[k] = d177[k] - d178[k];
+    double d180[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d180[k] = -d179[k];
+    double d181[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d181[k] = din[7 * NT + k] * pre[17] + in_H1 * dpre[17 * NT + k];
+    double d182[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d182[k] = dpre[11 * NT + k] * t156 + pre[11] * d156[k];
+    double d183[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d183[k] = d181[k] - d182[k];
+    double d184[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d184[k] = d58[k] * pre[9] + t58 * dpre[9 * NT + k];
+    double d185[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d185[k] = d183[k] - d184[k];
+    double d186[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d186[k] = -d185[k];
+    double d187[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d187[k] = din[8 * NT + k] * pre[17] + in_H2 * dpre[17 * NT + k];
+    double d188[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d188[k] = dpre[12 * NT + k] * t156 + pre[12] * d156[k];
+    double d189[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d189[k] = d187[k] - d188[k];
+    double d190[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d190[k] = d61[k] * pre[9] + t61 * dpre[9 * NT + k];
+    double d191[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d191[k] = d189[k] - d190[k];
+    double d192[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d192[k] = -d191[k];
+    out[0] = t150;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[0 * NT + k] = d150[k];
+    out[1] = t151;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[1 * NT + k] = d151[k];
+    out[2] = t152;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[2 * NT + k] = d152[k];
+    out[3] = t162;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[3 * NT + k] = d162[k];
+    out[4] = t168;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[4 * NT + k] = d168[k];
+    out[5] = t174;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[5 * NT + k] = d174[k];
+    out[6] = t180;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[6 * NT + k] = d180[k];
+    out[7] = t186;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[7 * NT + k] = d186[k];
+    out[8] = t192;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[8 * NT + k] = d192[k];
+}
+
 // adj_flat: pre inputs (x, y, z); iteration inputs (hv0, hv1, hv2, S0, S1, S2, H0, H1, H2, P0, P1, P2, Q0, Q1, Q2);
 // constants (R, hR, hk2f, hm, k2f, m)
 constexpr int adj_flat_NPRE = 10;
@@ -1163,6 +1855,482 @@ __host__ __device__ __forceinline__ void adj_flat_pre_vjp(double in_x, double in
     bin[0] += b_x;
     bin[1] += b_y;
     bin[2] += b_z;
+}
+
+// adj_flat: pre values and their tangents (din[i * NT + k]: tangent k of pre input i).
+template <int NT>
+__host__ __device__ __forceinline__ void adj_flat_pre_jvp(double in_x, double in_y, double in_z,
+        double c_R, double c_hR, double c_hk2f, double c_hm, double c_k2f, double c_m, const double* __restrict__ din, double* __restrict__ pre,
+        double* __restrict__ dpre) {
+    const double t18 = in_x * in_x;
+    const double t19 = in_y * in_y;
+    const double t20 = t18 + t19;
+    const double t21 = in_z * in_z;
+    const double t22 = t20 + t21;
+    const double t23 = sqrt(t22);
+    const double t40 = c_m * c_hk2f;
+    const double t41 = c_hR * c_hR;
+    const double t42 = t41 * t41;
+    const double t43 = c_hR * t42;
+    const double t44 = t40 * t43;
+    const double t46 = t44 * 0.16666666666666666;
+    const double t47 = c_hm * c_k2f;
+    const double t48 = c_R * c_R;
+    const double t49 = t48 * t48;
+    const double t50 = c_R * t49;
+    const double t51 = t47 * t50;
+    const double t52 = 0.16666666666666666 * t51;
+    const double t53 = t23 * t23;
+    const double t54 = t53 * t53;
+    const double t55 = t23 * t54;
+    const double t56 = t23 * t55;
+    const double t57 = t23 * t56;
+    const double t59 = 1.0 / t55;
+    const double t61 = t46 * -6.0;
+    const double t62 = t59 * t61;
+    const double t64 = t52 * -6.0;
+    const double t65 = t59 * t64;
+    const double t78 = -3.0 / t55;
+    const double t84 = 15.0 / t57;
+    const double t107 = 1.0 / c_m;
+    double d18[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d18[k] = 2.0 * in_x * din[0 * NT + k];
+    double d19[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d19[k] = 2.0 * in_y * din[1 * NT + k];
+    double d20[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d20[k] = d18[k] + d19[k];
+    double d21[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d21[k] = 2.0 * in_z * din[2 * NT + k];
+    double d22[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d22[k] = d20[k] + d21[k];
+    double d23[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d23[k] = 0.5 * d22[k] / t23;
+    double d53[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d53[k] = 2.0 * t23 * d23[k];
+    double d54[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d54[k] = 2.0 * t53 * d53[k];
+    double d55[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d55[k] = d23[k] * t54 + t23 * d54[k];
+    double d56[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d56[k] = d23[k] * t55 + t23 * d55[k];
+    double d57[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d57[k] = d23[k] * t56 + t23 * d56[k];
+    double d59[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d59[k] = -t59 * d55[k] / t55;
+    double d62[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d62[k] = d59[k] * t61;
+    double d65[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d65[k] = d59[k] * t64;
+    double d78[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d78[k] = -t78 * d55[k] / t55;
+    double d84[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d84[k] = -t84 * d57[k] / t57;
+    pre[0] = in_x;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[0 * NT + k] = din[0 * NT + k];
+    pre[1] = in_y;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[1 * NT + k] = din[1 * NT + k];
+    pre[2] = in_z;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[2 * NT + k] = din[2 * NT + k];
+    pre[3] = t62;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[3 * NT + k] = d62[k];
+    pre[4] = t65;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[4 * NT + k] = d65[k];
+    pre[5] = t52;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[5 * NT + k] = 0.0;
+    pre[6] = t46;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[6 * NT + k] = 0.0;
+    pre[7] = t78;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[7 * NT + k] = d78[k];
+    pre[8] = t84;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[8 * NT + k] = d84[k];
+    pre[9] = t107;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[9 * NT + k] = 0.0;
+}
+
+// adj_flat: one iteration, outputs and their tangents (din[i * NT + k] for the
+// iteration inputs; dout[o * NT + k]).
+template <int NT>
+__host__ __device__ __forceinline__ void adj_flat_iter_jvp(const double* __restrict__ pre,
+        const double* __restrict__ dpre, double in_hv0, double in_hv1, double in_hv2, double in_S0, double in_S1, double in_S2, double in_H0, double in_H1, double in_H2, double in_P0, double in_P1, double in_P2, double in_Q0, double in_Q1, double in_Q2,
+        double c_R, double c_hR, double c_hk2f, double c_hm, double c_k2f, double c_m, const double* __restrict__ din, double* __restrict__ out,
+        double* __restrict__ dout) {
+    const double t30 = pre[0] * in_Q0;
+    const double t31 = pre[1] * in_Q1;
+    const double t32 = t30 + t31;
+    const double t33 = pre[2] * in_Q2;
+    const double t34 = t32 + t33;
+    const double t35 = pre[0] * in_P0;
+    const double t36 = pre[1] * in_P1;
+    const double t37 = t35 + t36;
+    const double t38 = pre[2] * in_P2;
+    const double t39 = t37 + t38;
+    const double t63 = t34 * pre[3];
+    const double t66 = t39 * pre[4];
+    const double t67 = in_S0 * in_S0;
+    const double t68 = in_S1 * in_S1;
+    const double t69 = t67 + t68;
+    const double t70 = in_S2 * in_S2;
+    const double t71 = t69 + t70;
+    const double t72 = in_H0 * in_H0;
+    const double t73 = in_H1 * in_H1;
+    const double t74 = t72 + t73;
+    const double t75 = in_H2 * in_H2;
+    const double t76 = t74 + t75;
+    const double t79 = pre[5] * t71;
+    const double t80 = pre[6] * t76;
+    const double t81 = t79 + t80;
+    const double t82 = pre[7] * t81;
+    const double t85 = t34 * pre[6];
+    const double t86 = t34 * t85;
+    const double t87 = t39 * pre[5];
+    const double t88 = t39 * t87;
+    const double t89 = t86 + t88;
+    const double t90 = pre[8] * t89;
+    const double t91 = t82 + t90;
+    const double t92 = pre[0] * t91;
+    const double t93 = in_S0 * t66;
+    const double t94 = t92 + t93;
+    const double t95 = in_H0 * t63;
+    const double t96 = t94 + t95;
+    const double t97 = pre[1] * t91;
+    const double t98 = in_S1 * t66;
+    const double t99 = t97 + t98;
+    const double t100 = in_H1 * t63;
+    const double t101 = t99 + t100;
+    const double t102 = pre[2] * t91;
+    const double t103 = in_S2 * t66;
+    const double t104 = t102 + t103;
+    const double t105 = in_H2 * t63;
+    const double t106 = t104 + t105;
+    const double t108 = t96 * pre[9];
+    const double t109 = t101 * pre[9];
+    const double t110 = t106 * pre[9];
+    const double t111 = pre[1] * in_S2;
+    const double t112 = pre[2] * in_S1;
+    const double t113 = t111 - t112;
+    const double t114 = pre[2] * in_S0;
+    const double t115 = pre[0] * in_S2;
+    const double t116 = t114 - t115;
+    const double t117 = pre[0] * in_S1;
+    const double t118 = pre[1] * in_S0;
+    const double t119 = t117 - t118;
+    const double t120 = pre[1] * in_H2;
+    const double t121 = pre[2] * in_H1;
+    const double t122 = t120 - t121;
+    const double t123 = pre[2] * in_H0;
+    const double t124 = pre[0] * in_H2;
+    const double t125 = t123 - t124;
+    const double t126 = pre[0] * in_H1;
+    const double t127 = pre[1] * in_H0;
+    const double t128 = t126 - t127;
+    const double t129 = t66 * t113;
+    const double t130 = -t129;
+    const double t131 = t66 * t116;
+    const double t132 = -t131;
+    const double t133 = t66 * t119;
+    const double t134 = -t133;
+    const double t135 = t63 * t122;
+    const double t136 = -t135;
+    const double t137 = t63 * t125;
+    const double t138 = -t137;
+    const double t139 = t63 * t128;
+    const double t140 = -t139;
+    double d30[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d30[k] = dpre[0 * NT + k] * in_Q0 + pre[0] * din[12 * NT + k];
+    double d31[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d31[k] = dpre[1 * NT + k] * in_Q1 + pre[1] * din[13 * NT + k];
+    double d32[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d32[k] = d30[k] + d31[k];
+    double d33[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d33[k] = dpre[2 * NT + k] * in_Q2 + pre[2] * din[14 * NT + k];
+    double d34[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d34[k] = d32[k] + d33[k];
+    double d35[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d35[k] = dpre[0 * NT + k] * in_P0 + pre[0] * din[9 * NT + k];
+    double d36[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d36[k] = dpre[1 * NT + k] * in_P1 + pre[1] * din[10 * NT + k];
+    double d37[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d37[k] = d35[k] + d36[k];
+    double d38[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d38[k] = dpre[2 * NT + k] * in_P2 + pre[2] * din[11 * NT + k];
+    double d39[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d39[k] = d37[k] + d38[k];
+    double d63[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d63[k] = d34[k] * pre[3] + t34 * dpre[3 * NT + k];
+    double d66[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d66[k] = d39[k] * pre[4] + t39 * dpre[4 * NT + k];
+    double d67[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d67[k] = 2.0 * in_S0 * din[3 * NT + k];
+    double d68[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d68[k] = 2.0 * in_S1 * din[4 * NT + k];
+    double d69[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d69[k] = d67[k] + d68[k];
+    double d70[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d70[k] = 2.0 * in_S2 * din[5 * NT + k];
+    double d71[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d71[k] = d69[k] + d70[k];
+    double d72[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d72[k] = 2.0 * in_H0 * din[6 * NT + k];
+    double d73[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d73[k] = 2.0 * in_H1 * din[7 * NT + k];
+    double d74[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d74[k] = d72[k] + d73[k];
+    double d75[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d75[k] = 2.0 * in_H2 * din[8 * NT + k];
+    double d76[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d76[k] = d74[k] + d75[k];
+    double d79[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d79[k] = pre[5] * d71[k];
+    double d80[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d80[k] = pre[6] * d76[k];
+    double d81[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d81[k] = d79[k] + d80[k];
+    double d82[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d82[k] = dpre[7 * NT + k] * t81 + pre[7] * d81[k];
+    double d85[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d85[k] = d34[k] * pre[6];
+    double d86[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d86[k] = d34[k] * t85 + t34 * d85[k];
+    double d87[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d87[k] = d39[k] * pre[5];
+    double d88[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d88[k] = d39[k] * t87 + t39 * d87[k];
+    double d89[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d89[k] = d86[k] + d88[k];
+    double d90[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d90[k] = dpre[8 * NT + k] * t89 + pre[8] * d89[k];
+    double d91[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d91[k] = d82[k] + d90[k];
+    double d92[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d92[k] = dpre[0 * NT + k] * t91 + pre[0] * d91[k];
+    double d93[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d93[k] = din[3 * NT + k] * t66 + in_S0 * d66[k];
+    double d94[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d94[k] = d92[k] + d93[k];
+    double d95[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d95[k] = din[6 * NT + k] * t63 + in_H0 * d63[k];
+    double d96[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d96[k] = d94[k] + d95[k];
+    double d97[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d97[k] = dpre[1 * NT + k] * t91 + pre[1] * d91[k];
+    double d98[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d98[k] = din[4 * NT + k] * t66 + in_S1 * d66[k];
+    double d99[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d99[k] = d97[k] + d98[k];
+    double d100[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d100[k] = din[7 * NT + k] * t63 + in_H1 * d63[k];
+    double d101[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d101[k] = d99[k] + d100[k];
+    double d102[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d102[k] = dpre[2 * NT + k] * t91 + pre[2] * d91[k];
+    double d103[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d103[k] = din[5 * NT + k] * t66 + in_S2 * d66[k];
+    double d104[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d104[k] = d102[k] + d103[k];
+    double d105[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d105[k] = din[8 * NT + k] * t63 + in_H2 * d63[k];
+    double d106[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d106[k] = d104[k] + d105[k];
+    double d108[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d108[k] = d96[k] * pre[9];
+    double d109[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d109[k] = d101[k] * pre[9];
+    double d110[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d110[k] = d106[k] * pre[9];
+    double d111[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d111[k] = dpre[1 * NT + k] * in_S2 + pre[1] * din[5 * NT + k];
+    double d112[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d112[k] = dpre[2 * NT + k] * in_S1 + pre[2] * din[4 * NT + k];
+    double d113[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d113[k] = d111[k] - d112[k];
+    double d114[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d114[k] = dpre[2 * NT + k] * in_S0 + pre[2] * din[3 * NT + k];
+    double d115[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d115[k] = dpre[0 * NT + k] * in_S2 + pre[0] * din[5 * NT + k];
+    double d116[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d116[k] = d114[k] - d115[k];
+    double d117[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d117[k] = dpre[0 * NT + k] * in_S1 + pre[0] * din[4 * NT + k];
+    double d118[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d118[k] = dpre[1 * NT + k] * in_S0 + pre[1] * din[3 * NT + k];
+    double d119[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d119[k] = d117[k] - d118[k];
+    double d120[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d120[k] = dpre[1 * NT + k] * in_H2 + pre[1] * din[8 * NT + k];
+    double d121[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d121[k] = dpre[2 * NT + k] * in_H1 + pre[2] * din[7 * NT + k];
+    double d122[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d122[k] = d120[k] - d121[k];
+    double d123[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d123[k] = dpre[2 * NT + k] * in_H0 + pre[2] * din[6 * NT + k];
+    double d124[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d124[k] = dpre[0 * NT + k] * in_H2 + pre[0] * din[8 * NT + k];
+    double d125[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d125[k] = d123[k] - d124[k];
+    double d126[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d126[k] = dpre[0 * NT + k] * in_H1 + pre[0] * din[7 * NT + k];
+    double d127[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d127[k] = dpre[1 * NT + k] * in_H0 + pre[1] * din[6 * NT + k];
+    double d128[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d128[k] = d126[k] - d127[k];
+    double d129[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d129[k] = d66[k] * t113 + t66 * d113[k];
+    double d130[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d130[k] = -d129[k];
+    double d131[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d131[k] = d66[k] * t116 + t66 * d116[k];
+    double d132[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d132[k] = -d131[k];
+    double d133[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d133[k] = d66[k] * t119 + t66 * d119[k];
+    double d134[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d134[k] = -d133[k];
+    double d135[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d135[k] = d63[k] * t122 + t63 * d122[k];
+    double d136[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d136[k] = -d135[k];
+    double d137[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d137[k] = d63[k] * t125 + t63 * d125[k];
+    double d138[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d138[k] = -d137[k];
+    double d139[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d139[k] = d63[k] * t128 + t63 * d128[k];
+    double d140[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d140[k] = -d139[k];
+    out[0] = t108;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[0 * NT + k] = d108[k];
+    out[1] = t109;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[1 * NT + k] = d109[k];
+    out[2] = t110;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[2 * NT + k] = d110[k];
+    out[3] = t130;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[3 * NT + k] = d130[k];
+    out[4] = t132;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[4 * NT + k] = d132[k];
+    out[5] = t134;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[5 * NT + k] = d134[k];
+    out[6] = t136;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[6 * NT + k] = d136[k];
+    out[7] = t138;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[7 * NT + k] = d138[k];
+    out[8] = t140;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[8 * NT + k] = d140[k];
 }
 
 // adj_gr: pre inputs (x, y, z); iteration inputs (hv0, hv1, hv2, S0, S1, S2, H0, H1, H2, P0, P1, P2, Q0, Q1, Q2);
@@ -2343,6 +3511,1248 @@ __host__ __device__ __forceinline__ void adj_gr_pre_vjp(double in_x, double in_y
     bin[0] += b_x;
     bin[1] += b_y;
     bin[2] += b_z;
+}
+
+// adj_gr: pre values and their tangents (din[i * NT + k]: tangent k of pre input i).
+template <int NT>
+__host__ __device__ __forceinline__ void adj_gr_pre_jvp(double in_x, double in_y, double in_z,
+        double c_hm, double c_hmg, double c_hmoi, double c_m, double c_mg, double c_moi, const double* __restrict__ din, double* __restrict__ pre,
+        double* __restrict__ dpre) {
+    const double t18 = in_x * in_x;
+    const double t19 = in_y * in_y;
+    const double t20 = t18 + t19;
+    const double t21 = in_z * in_z;
+    const double t22 = t20 + t21;
+    const double t23 = sqrt(t22);
+    const double t33 = 1.0 / t23;
+    const double t34 = in_x * t33;
+    const double t35 = in_y * t33;
+    const double t36 = in_z * t33;
+    const double t48 = c_mg + c_hmg;
+    const double t49 = c_mg * c_hmg;
+    const double t50 = t48 * t48;
+    const double t51 = t49 / t50;
+    const double t52 = t23 * t23;
+    const double t53 = t33 * t48;
+    const double t54 = -t48;
+    const double t55 = kC2 * t52;
+    const double t56 = t54 / t55;
+    const double t58 = t51 * 3.0;
+    const double t59 = 1.0 + t58;
+    const double t61 = t51 + 2.0;
+    const double t62 = 2.0 * t61;
+    const double t63 = t53 * t62;
+    const double t65 = t51 * 1.5;
+    const double t66 = t48 / t55;
+    const double t67 = 2.0 * t66;
+    const double t68 = 2.0 - t51;
+    const double t69 = t67 * t68;
+    const double t71 = t51 * 29.0;
+    const double t73 = t71 + 12.0;
+    const double t75 = t73 * 0.75;
+    const double t76 = t50 / t52;
+    const double t77 = t75 * t76;
+    const double t79 = t51 * 4.0;
+    const double t80 = 3.0 - t79;
+    const double t81 = t51 * t80;
+    const double t83 = t51 * 1.875;
+    const double t84 = 1.0 - t58;
+    const double t85 = t83 * t84;
+    const double t86 = t65 * t80;
+    const double t88 = t51 * 0.5;
+    const double t90 = 13.0 - t79;
+    const double t91 = t88 * t90;
+    const double t92 = t53 * t91;
+    const double t94 = t51 * 25.0;
+    const double t95 = 2.0 + t94;
+    const double t96 = t51 * 2.0;
+    const double t97 = t51 * t96;
+    const double t98 = t95 + t97;
+    const double t99 = t53 * t98;
+    const double t101 = t56 * -0.5;
+    const double t103 = t79 + 15.0;
+    const double t104 = t51 * t103;
+    const double t106 = t51 * 41.0;
+    const double t107 = 4.0 + t106;
+    const double t109 = t51 * 8.0;
+    const double t110 = t51 * t109;
+    const double t111 = t107 + t110;
+    const double t112 = t53 * t111;
+    const double t113 = 3.0 + t96;
+    const double t114 = t58 * t113;
+    const double t159 = c_hm - c_m;
+    const double t185 = t34 * 6.0;
+    const double t190 = t35 * 6.0;
+    const double t195 = t36 * 6.0;
+    const double t250 = c_m * c_hm;
+    const double t251 = c_m + c_hm;
+    const double t252 = t250 / t251;
+    const double t253 = c_m * 1.5;
+    const double t254 = t253 / c_hm;
+    const double t255 = 2.0 + t254;
+    const double t256 = c_hm * 1.5;
+    const double t257 = t256 / c_m;
+    const double t258 = 2.0 + t257;
+    double d18[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d18[k] = 2.0 * in_x * din[0 * NT + k];
+    double d19[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d19[k] = 2.0 * in_y * din[1 * NT + k];
+    double d20[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d20[k] = d18[k] + d19[k];
+    double d21[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d21[k] = 2.0 * in_z * din[2 * NT + k];
+    double d22[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d22[k] = d20[k] + d21[k];
+    double d23[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d23[k] = 0.5 * d22[k] / t23;
+    double d33[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d33[k] = -t33 * d23[k] / t23;
+    double d34[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d34[k] = din[0 * NT + k] * t33 + in_x * d33[k];
+    double d35[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d35[k] = din[1 * NT + k] * t33 + in_y * d33[k];
+    double d36[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d36[k] = din[2 * NT + k] * t33 + in_z * d33[k];
+    double d52[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d52[k] = 2.0 * t23 * d23[k];
+    double d53[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d53[k] = d33[k] * t48;
+    double d55[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d55[k] = kC2 * d52[k];
+    double d56[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d56[k] = -t56 * d55[k] / t55;
+    double d63[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d63[k] = d53[k] * t62;
+    double d66[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d66[k] = -t66 * d55[k] / t55;
+    double d67[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d67[k] = 2.0 * d66[k];
+    double d69[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d69[k] = d67[k] * t68;
+    double d76[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d76[k] = -t76 * d52[k] / t52;
+    double d77[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d77[k] = t75 * d76[k];
+    double d92[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d92[k] = d53[k] * t91;
+    double d99[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d99[k] = d53[k] * t98;
+    double d101[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d101[k] = d56[k] * -0.5;
+    double d112[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d112[k] = d53[k] * t111;
+    double d185[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d185[k] = d34[k] * 6.0;
+    double d190[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d190[k] = d35[k] * 6.0;
+    double d195[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d195[k] = d36[k] * 6.0;
+    pre[0] = in_x;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[0 * NT + k] = din[0 * NT + k];
+    pre[1] = in_y;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[1 * NT + k] = din[1 * NT + k];
+    pre[2] = in_z;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[2 * NT + k] = din[2 * NT + k];
+    pre[3] = t33;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[3 * NT + k] = d33[k];
+    pre[4] = t59;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[4 * NT + k] = 0.0;
+    pre[5] = t63;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[5 * NT + k] = d63[k];
+    pre[6] = t65;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[6 * NT + k] = 0.0;
+    pre[7] = t56;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[7 * NT + k] = d56[k];
+    pre[8] = t69;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[8 * NT + k] = d69[k];
+    pre[9] = t81;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[9 * NT + k] = 0.0;
+    pre[10] = t77;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[10 * NT + k] = d77[k];
+    pre[11] = t85;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[11 * NT + k] = 0.0;
+    pre[12] = t86;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[12 * NT + k] = 0.0;
+    pre[13] = t92;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[13 * NT + k] = d92[k];
+    pre[14] = t99;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[14 * NT + k] = d99[k];
+    pre[15] = t101;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[15 * NT + k] = d101[k];
+    pre[16] = t104;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[16 * NT + k] = 0.0;
+    pre[17] = t112;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[17 * NT + k] = d112[k];
+    pre[18] = t114;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[18 * NT + k] = 0.0;
+    pre[19] = t34;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[19 * NT + k] = d34[k];
+    pre[20] = t35;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[20 * NT + k] = d35[k];
+    pre[21] = t36;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[21 * NT + k] = d36[k];
+    pre[22] = t159;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[22 * NT + k] = 0.0;
+    pre[23] = t185;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[23 * NT + k] = d185[k];
+    pre[24] = t190;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[24 * NT + k] = d190[k];
+    pre[25] = t195;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[25 * NT + k] = d195[k];
+    pre[26] = t252;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[26 * NT + k] = 0.0;
+    pre[27] = t255;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[27 * NT + k] = 0.0;
+    pre[28] = t258;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dpre[28 * NT + k] = 0.0;
+}
+
+// adj_gr: one iteration, outputs and their tangents (din[i * NT + k] for the
+// iteration inputs; dout[o * NT + k]).
+template <int NT>
+__host__ __device__ __forceinline__ void adj_gr_iter_jvp(const double* __restrict__ pre,
+        const double* __restrict__ dpre, double in_hv0, double in_hv1, double in_hv2, double in_S0, double in_S1, double in_S2, double in_H0, double in_H1, double in_H2, double in_P0, double in_P1, double in_P2, double in_Q0, double in_Q1, double in_Q2,
+        double c_hm, double c_hmg, double c_hmoi, double c_m, double c_mg, double c_moi, const double* __restrict__ din, double* __restrict__ out,
+        double* __restrict__ dout) {
+    const double t37 = pre[0] * in_hv0;
+    const double t38 = pre[1] * in_hv1;
+    const double t39 = t37 + t38;
+    const double t40 = pre[2] * in_hv2;
+    const double t41 = t39 + t40;
+    const double t42 = pre[3] * t41;
+    const double t43 = in_hv0 * in_hv0;
+    const double t44 = in_hv1 * in_hv1;
+    const double t45 = t43 + t44;
+    const double t46 = in_hv2 * in_hv2;
+    const double t47 = t45 + t46;
+    const double t115 = t42 * t42;
+    const double t116 = t47 * pre[4];
+    const double t117 = t116 - pre[5];
+    const double t118 = pre[6] * t115;
+    const double t119 = t117 - t118;
+    const double t120 = pre[7] * t119;
+    const double t121 = t42 * pre[8];
+    const double t122 = t47 * t47;
+    const double t123 = t115 * t115;
+    const double t124 = pre[9] * t122;
+    const double t125 = pre[10] + t124;
+    const double t126 = pre[11] * t123;
+    const double t127 = t125 + t126;
+    const double t128 = pre[12] * t115;
+    const double t129 = t47 * t128;
+    const double t130 = t127 - t129;
+    const double t131 = t47 * pre[13];
+    const double t132 = t130 - t131;
+    const double t133 = pre[14] * t115;
+    const double t134 = t132 - t133;
+    const double t135 = pre[7] * t134;
+    const double t136 = t42 * pre[15];
+    const double t137 = t47 * pre[16];
+    const double t138 = t137 - pre[17];
+    const double t139 = pre[18] * t115;
+    const double t140 = t138 - t139;
+    const double t141 = t136 * t140;
+    const double t142 = t120 + t135;
+    const double t143 = t121 + t141;
+    const double t144 = pre[19] * t142;
+    const double t145 = in_hv0 * t143;
+    const double t146 = t144 + t145;
+    const double t147 = pre[20] * t142;
+    const double t148 = in_hv1 * t143;
+    const double t149 = t147 + t148;
+    const double t150 = pre[21] * t142;
+    const double t151 = in_hv2 * t143;
+    const double t152 = t150 + t151;
+    const double t153 = in_H0 * c_hmoi;
+    const double t154 = in_H1 * c_hmoi;
+    const double t155 = in_H2 * c_hmoi;
+    const double t156 = in_S0 * c_moi;
+    const double t157 = in_S1 * c_moi;
+    const double t158 = in_S2 * c_moi;
+    const double t160 = t156 / c_m;
+    const double t161 = t153 / c_hm;
+    const double t162 = t160 - t161;
+    const double t163 = pre[22] * t162;
+    const double t164 = t157 / c_m;
+    const double t165 = t154 / c_hm;
+    const double t166 = t164 - t165;
+    const double t167 = pre[22] * t166;
+    const double t168 = t158 / c_m;
+    const double t169 = t155 / c_hm;
+    const double t170 = t168 - t169;
+    const double t171 = pre[22] * t170;
+    const double t172 = t153 + t156;
+    const double t173 = t154 + t157;
+    const double t174 = t155 + t158;
+    const double t175 = in_hv2 * pre[20];
+    const double t176 = in_hv1 * pre[21];
+    const double t177 = t175 - t176;
+    const double t178 = in_hv0 * pre[21];
+    const double t179 = in_hv2 * pre[19];
+    const double t180 = t178 - t179;
+    const double t181 = in_hv1 * pre[19];
+    const double t182 = in_hv0 * pre[20];
+    const double t183 = t181 - t182;
+    const double t186 = 2.0 * t172;
+    const double t187 = t163 + t186;
+    const double t188 = t177 * t187;
+    const double t189 = pre[23] * t188;
+    const double t191 = 2.0 * t173;
+    const double t192 = t167 + t191;
+    const double t193 = t180 * t192;
+    const double t194 = pre[24] * t193;
+    const double t196 = 2.0 * t174;
+    const double t197 = t171 + t196;
+    const double t198 = t183 * t197;
+    const double t199 = pre[25] * t198;
+    const double t201 = t172 * 7.0;
+    const double t202 = 3.0 * t163;
+    const double t203 = t201 + t202;
+    const double t204 = t173 * 7.0;
+    const double t205 = 3.0 * t167;
+    const double t206 = t204 + t205;
+    const double t207 = t174 * 7.0;
+    const double t208 = 3.0 * t171;
+    const double t209 = t207 + t208;
+    const double t210 = 3.0 * t172;
+    const double t211 = t163 + t210;
+    const double t212 = 3.0 * t173;
+    const double t213 = t167 + t212;
+    const double t214 = 3.0 * t174;
+    const double t215 = t171 + t214;
+    const double t216 = t42 * 3.0;
+    const double t217 = in_hv1 * t209;
+    const double t218 = in_hv2 * t206;
+    const double t219 = t217 - t218;
+    const double t220 = in_hv2 * t203;
+    const double t221 = in_hv0 * t209;
+    const double t222 = t220 - t221;
+    const double t223 = in_hv0 * t206;
+    const double t224 = in_hv1 * t203;
+    const double t225 = t223 - t224;
+    const double t226 = pre[20] * t215;
+    const double t227 = pre[21] * t213;
+    const double t228 = t226 - t227;
+    const double t229 = pre[21] * t211;
+    const double t230 = pre[19] * t215;
+    const double t231 = t229 - t230;
+    const double t232 = pre[19] * t213;
+    const double t233 = pre[20] * t211;
+    const double t234 = t232 - t233;
+    const double t235 = t189 - t219;
+    const double t236 = t216 * t228;
+    const double t237 = t235 + t236;
+    const double t238 = kFA * t237;
+    const double t239 = t146 + t238;
+    const double t240 = t194 - t222;
+    const double t241 = t216 * t231;
+    const double t242 = t240 + t241;
+    const double t243 = kFA * t242;
+    const double t244 = t149 + t243;
+    const double t245 = t199 - t225;
+    const double t246 = t216 * t234;
+    const double t247 = t245 + t246;
+    const double t248 = kFA * t247;
+    const double t249 = t152 + t248;
+    const double t259 = pre[1] * in_hv2;
+    const double t260 = pre[2] * in_hv1;
+    const double t261 = t259 - t260;
+    const double t262 = pre[2] * in_hv0;
+    const double t263 = pre[0] * in_hv2;
+    const double t264 = t262 - t263;
+    const double t265 = pre[0] * in_hv1;
+    const double t266 = pre[1] * in_hv0;
+    const double t267 = t265 - t266;
+    const double t268 = pre[26] * t261;
+    const double t269 = pre[26] * t264;
+    const double t270 = pre[26] * t267;
+    const double t271 = t155 * t157;
+    const double t272 = t154 * t158;
+    const double t273 = t271 - t272;
+    const double t274 = t153 * t158;
+    const double t275 = t155 * t156;
+    const double t276 = t274 - t275;
+    const double t277 = t154 * t156;
+    const double t278 = t153 * t157;
+    const double t279 = t277 - t278;
+    const double t280 = pre[19] * t156;
+    const double t281 = pre[20] * t157;
+    const double t282 = t280 + t281;
+    const double t283 = pre[21] * t158;
+    const double t284 = t282 + t283;
+    const double t285 = 3.0 * t284;
+    const double t286 = pre[19] * t153;
+    const double t287 = pre[20] * t154;
+    const double t288 = t286 + t287;
+    const double t289 = pre[21] * t155;
+    const double t290 = t288 + t289;
+    const double t291 = 3.0 * t290;
+    const double t292 = t155 * t269;
+    const double t293 = t154 * t270;
+    const double t294 = t292 - t293;
+    const double t295 = t153 * t270;
+    const double t296 = t155 * t268;
+    const double t297 = t295 - t296;
+    const double t298 = t154 * t268;
+    const double t299 = t153 * t269;
+    const double t300 = t298 - t299;
+    const double t301 = t158 * t269;
+    const double t302 = t157 * t270;
+    const double t303 = t301 - t302;
+    const double t304 = t156 * t270;
+    const double t305 = t158 * t268;
+    const double t306 = t304 - t305;
+    const double t307 = t157 * t268;
+    const double t308 = t156 * t269;
+    const double t309 = t307 - t308;
+    const double t310 = pre[20] * t155;
+    const double t311 = pre[21] * t154;
+    const double t312 = t310 - t311;
+    const double t313 = pre[21] * t153;
+    const double t314 = pre[19] * t155;
+    const double t315 = t313 - t314;
+    const double t316 = pre[19] * t154;
+    const double t317 = pre[20] * t153;
+    const double t318 = t316 - t317;
+    const double t319 = pre[20] * t158;
+    const double t320 = pre[21] * t157;
+    const double t321 = t319 - t320;
+    const double t322 = pre[21] * t156;
+    const double t323 = pre[19] * t158;
+    const double t324 = t322 - t323;
+    const double t325 = pre[19] * t157;
+    const double t326 = pre[20] * t156;
+    const double t327 = t325 - t326;
+    const double t328 = pre[27] * t294;
+    const double t329 = t328 - t273;
+    const double t330 = t285 * t312;
+    const double t331 = t329 + t330;
+    const double t332 = kFA * t331;
+    const double t333 = pre[27] * t297;
+    const double t334 = t333 - t276;
+    const double t335 = t285 * t315;
+    const double t336 = t334 + t335;
+    const double t337 = kFA * t336;
+    const double t338 = pre[27] * t300;
+    const double t339 = t338 - t279;
+    const double t340 = t285 * t318;
+    const double t341 = t339 + t340;
+    const double t342 = kFA * t341;
+    const double t343 = pre[28] * t303;
+    const double t344 = t273 + t343;
+    const double t345 = t291 * t321;
+    const double t346 = t344 + t345;
+    const double t347 = kFA * t346;
+    const double t348 = pre[28] * t306;
+    const double t349 = t276 + t348;
+    const double t350 = t291 * t324;
+    const double t351 = t349 + t350;
+    const double t352 = kFA * t351;
+    const double t353 = pre[28] * t309;
+    const double t354 = t279 + t353;
+    const double t355 = t291 * t327;
+    const double t356 = t354 + t355;
+    const double t357 = kFA * t356;
+    double d37[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d37[k] = dpre[0 * NT + k] * in_hv0 + pre[0] * din[0 * NT + k];
+    double d38[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d38[k] = dpre[1 * NT + k] * in_hv1 + pre[1] * din[1 * NT + k];
+    double d39[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d39[k] = d37[k] + d38[k];
+    double d40[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d40[k] = dpre[2 * NT + k] * in_hv2 + pre[2] * din[2 * NT + k];
+    double d41[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d41[k] = d39[k] + d40[k];
+    double d42[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d42[k] = dpre[3 * NT + k] * t41 + pre[3] * d41[k];
+    double d43[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d43[k] = 2.0 * in_hv0 * din[0 * NT + k];
+    double d44[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d44[k] = 2.0 * in_hv1 * din[1 * NT + k];
+    double d45[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d45[k] = d43[k] + d44[k];
+    double d46[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d46[k] = 2.0 * in_hv2 * din[2 * NT + k];
+    double d47[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d47[k] = d45[k] + d46[k];
+    double d115[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d115[k] = 2.0 * t42 * d42[k];
+    double d116[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d116[k] = d47[k] * pre[4];
+    double d117[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d117[k] = d116[k] - dpre[5 * NT + k];
+    double d118[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d118[k] = pre[6] * d115[k];
+    double d119[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d119[k] = d117[k] - d118[k];
+    double d120[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d120[k] = dpre[7 * NT + k] * t119 + pre[7] * d119[k];
+    double d121[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d121[k] = d42[k] * pre[8] + t42 * dpre[8 * NT + k];
+    double d122[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d122[k] = 2.0 * t47 * d47[k];
+    double d123[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d123[k] = 2.0 * t115 * d115[k];
+    double d124[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d124[k] = pre[9] * d122[k];
+    double d125[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d125[k] = dpre[10 * NT + k] + d124[k];
+    double d126[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d126[k] = pre[11] * d123[k];
+    double d127[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d127[k] = d125[k] + d126[k];
+    double d128[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d128[k] = pre[12] * d115[k];
+    double d129[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d129[k] = d47[k] * t128 + t47 * d128[k];
+    double d130[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d130[k] = d127[k] - d129[k];
+    double d131[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d131[k] = d47[k] * pre[13] + t47 * dpre[13 * NT + k];
+    double d132[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d132[k] = d130[k] - d131[k];
+    double d133[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d133[k] = dpre[14 * NT + k] * t115 + pre[14] * d115[k];
+    double d134[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d134[k] = d132[k] - d133[k];
+    double d135[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d135[k] = dpre[7 * NT + k] * t134 + pre[7] * d134[k];
+    double d136[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d136[k] = d42[k] * pre[15] + t42 * dpre[15 * NT + k];
+    double d137[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d137[k] = d47[k] * pre[16];
+    double d138[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d138[k] = d137[k] - dpre[17 * NT + k];
+    double d139[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d139[k] = pre[18] * d115[k];
+    double d140[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d140[k] = d138[k] - d139[k];
+    double d141[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d141[k] = d136[k] * t140 + t136 * d140[k];
+    double d142[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d142[k] = d120[k] + d135[k];
+    double d143[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d143[k] = d121[k] + d141[k];
+    double d144[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d144[k] = dpre[19 * NT + k] * t142 + pre[19] * d142[k];
+    double d145[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d145[k] = din[0 * NT + k] * t143 + in_hv0 * d143[k];
+    double d146[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d146[k] = d144[k] + d145[k];
+    double d147[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d147[k] = dpre[20 * NT + k] * t142 + pre[20] * d142[k];
+    double d148[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d148[k] = din[1 * NT + k] * t143 + in_hv1 * d143[k];
+    double d149[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d149[k] = d147[k] + d148[k];
+    double d150[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d150[k] = dpre[21 * NT + k] * t142 + pre[21] * d142[k];
+    double d151[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d151[k] = din[2 * NT + k] * t143 + in_hv2 * d143[k];
+    double d152[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d152[k] = d150[k] + d151[k];
+    double d153[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d153[k] = din[6 * NT + k] * c_hmoi;
+    double d154[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d154[k] = din[7 * NT + k] * c_hmoi;
+    double d155[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d155[k] = din[8 * NT + k] * c_hmoi;
+    double d156[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d156[k] = din[3 * NT + k] * c_moi;
+    double d157[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d157[k] = din[4 * NT + k] * c_moi;
+    double d158[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d158[k] = din[5 * NT + k] * c_moi;
+    double d160[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d160[k] = d156[k] / c_m;
+    double d161[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d161[k] = d153[k] / c_hm;
+    double d162[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d162[k] = d160[k] - d161[k];
+    double d163[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d163[k] = pre[22] * d162[k];
+    double d164[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d164[k] = d157[k] / c_m;
+    double d165[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d165[k] = d154[k] / c_hm;
+    double d166[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d166[k] = d164[k] - d165[k];
+    double d167[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d167[k] = pre[22] * d166[k];
+    double d168[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d168[k] = d158[k] / c_m;
+    double d169[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d169[k] = d155[k] / c_hm;
+    double d170[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d170[k] = d168[k] - d169[k];
+    double d171[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d171[k] = pre[22] * d170[k];
+    double d172[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d172[k] = d153[k] + d156[k];
+    double d173[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d173[k] = d154[k] + d157[k];
+    double d174[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d174[k] = d155[k] + d158[k];
+    double d175[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d175[k] = din[2 * NT + k] * pre[20] + in_hv2 * dpre[20 * NT + k];
+    double d176[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d176[k] = din[1 * NT + k] * pre[21] + in_hv1 * dpre[21 * NT + k];
+    double d177[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d177[k] = d175[k] - d176[k];
+    double d178[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d178[k] = din[0 * NT + k] * pre[21] + in_hv0 * dpre[21 * NT + k];
+    double d179[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d179[k] = din[2 * NT + k] * pre[19] + in_hv2 * dpre[19 * NT + k];
+    double d180[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d180[k] = d178[k] - d179[k];
+    double d181[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d181[k] = din[1 * NT + k] * pre[19] + in_hv1 * dpre[19 * NT + k];
+    double d182[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d182[k] = din[0 * NT + k] * pre[20] + in_hv0 * dpre[20 * NT + k];
+    double d183[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d183[k] = d181[k] - d182[k];
+    double d186[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d186[k] = 2.0 * d172[k];
+    double d187[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d187[k] = d163[k] + d186[k];
+    double d188[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d188[k] = d177[k] * t187 + t177 * d187[k];
+    double d189[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d189[k] = dpre[23 * NT + k] * t188 + pre[23] * d188[k];
+    double d191[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d191[k] = 2.0 * d173[k];
+    double d192[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d192[k] = d167[k] + d191[k];
+    double d193[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d193[k] = d180[k] * t192 + t180 * d192[k];
+    double d194[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d194[k] = dpre[24 * NT + k] * t193 + pre[24] * d193[k];
+    double d196[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d196[k] = 2.0 * d174[k];
+    double d197[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d197[k] = d171[k] + d196[k];
+    double d198[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d198[k] = d183[k] * t197 + t183 * d197[k];
+    double d199[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d199[k] = dpre[25 * NT + k] * t198 + pre[25] * d198[k];
+    double d201[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d201[k] = d172[k] * 7.0;
+    double d202[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d202[k] = 3.0 * d163[k];
+    double d203[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d203[k] = d201[k] + d202[k];
+    double d204[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d204[k] = d173[k] * 7.0;
+    double d205[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d205[k] = 3.0 * d167[k];
+    double d206[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d206[k] = d204[k] + d205[k];
+    double d207[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d207[k] = d174[k] * 7.0;
+    double d208[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d208[k] = 3.0 * d171[k];
+    double d209[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d209[k] = d207[k] + d208[k];
+    double d210[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d210[k] = 3.0 * d172[k];
+    double d211[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d211[k] = d163[k] + d210[k];
+    double d212[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d212[k] = 3.0 * d173[k];
+    double d213[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d213[k] = d167[k] + d212[k];
+    double d214[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d214[k] = 3.0 * d174[k];
+    double d215[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d215[k] = d171[k] + d214[k];
+    double d216[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d216[k] = d42[k] * 3.0;
+    double d217[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d217[k] = din[1 * NT + k] * t209 + in_hv1 * d209[k];
+    double d218[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d218[k] = din[2 * NT + k] * t206 + in_hv2 * d206[k];
+    double d219[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d219[k] = d217[k] - d218[k];
+    double d220[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d220[k] = din[2 * NT + k] * t203 + in_hv2 * d203[k];
+    double d221[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d221[k] = din[0 * NT + k] * t209 + in_hv0 * d209[k];
+    double d222[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d222[k] = d220[k] - d221[k];
+    double d223[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d223[k] = din[0 * NT + k] * t206 + in_hv0 * d206[k];
+    double d224[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d224[k] = din[1 * NT + k] * t203 + in_hv1 * d203[k];
+    double d225[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d225[k] = d223[k] - d224[k];
+    double d226[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d226[k] = dpre[20 * NT + k] * t215 + pre[20] * d215[k];
+    double d227[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d227[k] = dpre[21 * NT + k] * t213 + pre[21] * d213[k];
+    double d228[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d228[k] = d226[k] - d227[k];
+    double d229[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d229[k] = dpre[21 * NT + k] * t211 + pre[21] * d211[k];
+    double d230[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d230[k] = dpre[19 * NT + k] * t215 + pre[19] * d215[k];
+    double d231[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d231[k] = d229[k] - d230[k];
+    double d232[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d232[k] = dpre[19 * NT + k] * t213 + pre[19] * d213[k];
+    double d233[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d233[k] = dpre[20 * NT + k] * t211 + pre[20] * d211[k];
+    double d234[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d234[k] = d232[k] - d233[k];
+    double d235[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d235[k] = d189[k] - d219[k];
+    double d236[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d236[k] = d216[k] * t228 + t216 * d228[k];
+    double d237[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d237[k] = d235[k] + d236[k];
+    double d238[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d238[k] = kFA * d237[k];
+    double d239[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d239[k] = d146[k] + d238[k];
+    double d240[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d240[k] = d194[k] - d222[k];
+    double d241[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d241[k] = d216[k] * t231 + t216 * d231[k];
+    double d242[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d242[k] = d240[k] + d241[k];
+    double d243[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d243[k] = kFA * d242[k];
+    double d244[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d244[k] = d149[k] + d243[k];
+    double d245[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d245[k] = d199[k] - d225[k];
+    double d246[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d246[k] = d216[k] * t234 + t216 * d234[k];
+    double d247[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d247[k] = d245[k] + d246[k];
+    double d248[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d248[k] = kFA * d247[k];
+    double d249[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d249[k] = d152[k] + d248[k];
+    double d259[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d259[k] = dpre[1 * NT + k] * in_hv2 + pre[1] * din[2 * NT + k];
+    double d260[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d260[k] = dpre[2 * NT + k] * in_hv1 + pre[2] * din[1 * NT + k];
+    double d261[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d261[k] = d259[k] - d260[k];
+    double d262[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d262[k] = dpre[2 * NT + k] * in_hv0 + pre[2] * din[0 * NT + k];
+    double d263[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d263[k] = dpre[0 * NT + k] * in_hv2 + pre[0] * din[2 * NT + k];
+    double d264[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d264[k] = d262[k] - d263[k];
+    double d265[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d265[k] = dpre[0 * NT + k] * in_hv1 + pre[0] * din[1 * NT + k];
+    double d266[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d266[k] = dpre[1 * NT + k] * in_hv0 + pre[1] * din[0 * NT + k];
+    double d267[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d267[k] = d265[k] - d266[k];
+    double d268[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d268[k] = pre[26] * d261[k];
+    double d269[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d269[k] = pre[26] * d264[k];
+    double d270[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d270[k] = pre[26] * d267[k];
+    double d271[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d271[k] = d155[k] * t157 + t155 * d157[k];
+    double d272[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d272[k] = d154[k] * t158 + t154 * d158[k];
+    double d273[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d273[k] = d271[k] - d272[k];
+    double d274[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d274[k] = d153[k] * t158 + t153 * d158[k];
+    double d275[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d275[k] = d155[k] * t156 + t155 * d156[k];
+    double d276[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d276[k] = d274[k] - d275[k];
+    double d277[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d277[k] = d154[k] * t156 + t154 * d156[k];
+    double d278[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d278[k] = d153[k] * t157 + t153 * d157[k];
+    double d279[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d279[k] = d277[k] - d278[k];
+    double d280[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d280[k] = dpre[19 * NT + k] * t156 + pre[19] * d156[k];
+    double d281[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d281[k] = dpre[20 * NT + k] * t157 + pre[20] * d157[k];
+    double d282[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d282[k] = d280[k] + d281[k];
+    double d283[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d283[k] = dpre[21 * NT + k] * t158 + pre[21] * d158[k];
+    double d284[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d284[k] = d282[k] + d283[k];
+    double d285[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d285[k] = 3.0 * d284[k];
+    double d286[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d286[k] = dpre[19 * NT + k] * t153 + pre[19] * d153[k];
+    double d287[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d287[k] = dpre[20 * NT + k] * t154 + pre[20] * d154[k];
+    double d288[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d288[k] = d286[k] + d287[k];
+    double d289[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d289[k] = dpre[21 * NT + k] * t155 + pre[21] * d155[k];
+    double d290[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d290[k] = d288[k] + d289[k];
+    double d291[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d291[k] = 3.0 * d290[k];
+    double d292[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d292[k] = d155[k] * t269 + t155 * d269[k];
+    double d293[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d293[k] = d154[k] * t270 + t154 * d270[k];
+    double d294[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d294[k] = d292[k] - d293[k];
+    double d295[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d295[k] = d153[k] * t270 + t153 * d270[k];
+    double d296[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d296[k] = d155[k] * t268 + t155 * d268[k];
+    double d297[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d297[k] = d295[k] - d296[k];
+    double d298[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d298[k] = d154[k] * t268 + t154 * d268[k];
+    double d299[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d299[k] = d153[k] * t269 + t153 * d269[k];
+    double d300[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d300[k] = d298[k] - d299[k];
+    double d301[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d301[k] = d158[k] * t269 + t158 * d269[k];
+    double d302[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d302[k] = d157[k] * t270 + t157 * d270[k];
+    double d303[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d303[k] = d301[k] - d302[k];
+    double d304[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d304[k] = d156[k] * t270 + t156 * d270[k];
+    double d305[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d305[k] = d158[k] * t268 + t158 * d268[k];
+    double d306[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d306[k] = d304[k] - d305[k];
+    double d307[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d307[k] = d157[k] * t268 + t157 * d268[k];
+    double d308[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d308[k] = d156[k] * t269 + t156 * d269[k];
+    double d309[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d309[k] = d307[k] - d308[k];
+    double d310[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d310[k] = dpre[20 * NT + k] * t155 + pre[20] * d155[k];
+    double d311[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d311[k] = dpre[21 * NT + k] * t154 + pre[21] * d154[k];
+    double d312[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d312[k] = d310[k] - d311[k];
+    double d313[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d313[k] = dpre[21 * NT + k] * t153 + pre[21] * d153[k];
+    double d314[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d314[k] = dpre[19 * NT + k] * t155 + pre[19] * d155[k];
+    double d315[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d315[k] = d313[k] - d314[k];
+    double d316[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d316[k] = dpre[19 * NT + k] * t154 + pre[19] * d154[k];
+    double d317[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d317[k] = dpre[20 * NT + k] * t153 + pre[20] * d153[k];
+    double d318[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d318[k] = d316[k] - d317[k];
+    double d319[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d319[k] = dpre[20 * NT + k] * t158 + pre[20] * d158[k];
+    double d320[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d320[k] = dpre[21 * NT + k] * t157 + pre[21] * d157[k];
+    double d321[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d321[k] = d319[k] - d320[k];
+    double d322[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d322[k] = dpre[21 * NT + k] * t156 + pre[21] * d156[k];
+    double d323[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d323[k] = dpre[19 * NT + k] * t158 + pre[19] * d158[k];
+    double d324[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d324[k] = d322[k] - d323[k];
+    double d325[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d325[k] = dpre[19 * NT + k] * t157 + pre[19] * d157[k];
+    double d326[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d326[k] = dpre[20 * NT + k] * t156 + pre[20] * d156[k];
+    double d327[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d327[k] = d325[k] - d326[k];
+    double d328[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d328[k] = pre[27] * d294[k];
+    double d329[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d329[k] = d328[k] - d273[k];
+    double d330[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d330[k] = d285[k] * t312 + t285 * d312[k];
+    double d331[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d331[k] = d329[k] + d330[k];
+    double d332[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d332[k] = kFA * d331[k];
+    double d333[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d333[k] = pre[27] * d297[k];
+    double d334[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d334[k] = d333[k] - d276[k];
+    double d335[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d335[k] = d285[k] * t315 + t285 * d315[k];
+    double d336[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d336[k] = d334[k] + d335[k];
+    double d337[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d337[k] = kFA * d336[k];
+    double d338[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d338[k] = pre[27] * d300[k];
+    double d339[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d339[k] = d338[k] - d279[k];
+    double d340[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d340[k] = d285[k] * t318 + t285 * d318[k];
+    double d341[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d341[k] = d339[k] + d340[k];
+    double d342[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d342[k] = kFA * d341[k];
+    double d343[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d343[k] = pre[28] * d303[k];
+    double d344[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d344[k] = d273[k] + d343[k];
+    double d345[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d345[k] = d291[k] * t321 + t291 * d321[k];
+    double d346[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d346[k] = d344[k] + d345[k];
+    double d347[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d347[k] = kFA * d346[k];
+    double d348[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d348[k] = pre[28] * d306[k];
+    double d349[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d349[k] = d276[k] + d348[k];
+    double d350[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d350[k] = d291[k] * t324 + t291 * d324[k];
+    double d351[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d351[k] = d349[k] + d350[k];
+    double d352[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d352[k] = kFA * d351[k];
+    double d353[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d353[k] = pre[28] * d309[k];
+    double d354[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d354[k] = d279[k] + d353[k];
+    double d355[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d355[k] = d291[k] * t327 + t291 * d327[k];
+    double d356[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d356[k] = d354[k] + d355[k];
+    double d357[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d357[k] = kFA * d356[k];
+    out[0] = t239;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[0 * NT + k] = d239[k];
+    out[1] = t244;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[1 * NT + k] = d244[k];
+    out[2] = t249;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[2 * NT + k] = d249[k];
+    out[3] = t347;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[3 * NT + k] = d347[k];
+    out[4] = t352;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[4 * NT + k] = d352[k];
+    out[5] = t357;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[5 * NT + k] = d357[k];
+    out[6] = t332;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[6 * NT + k] = d332[k];
+    out[7] = t337;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[7 * NT + k] = d337[k];
+    out[8] = t342;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) dout[8 * NT + k] = d342[k];
 }
 
 }  // namespace posi_adj

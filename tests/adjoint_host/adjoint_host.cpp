@@ -69,4 +69,29 @@ void h_effects_vjp(int which, const double* in, const double* c, const double* b
     for (int k = 0; k < 4; ++k) bin[18 + k] += bp[3 + k];
 }
 
+void h_kepler_jvp(double mu, double dt, const double* r, const double* v, double X, const double* dr,
+                  const double* dv, double* dr1, double* dv1) {
+    kepler_jvp(mu, dt, r, v, X, dr, dv, dr1, dv1);
+}
+
+// tangent of the 9 outputs along din (22 inputs, one direction)
+void h_effects_jvp(int which, const double* in, const double* c, const double* din, double* dout) {
+    const double m = c[0], hm = c[1], R = c[2], hR = c[3], k2f = c[4], hk2f = c[5], mg = c[6], hmg = c[7];
+    const double moi = c[8], hmoi = c[9];
+    double pre[64], dpre[64], out[9], dpin[7], dit[15];
+    for (int k = 0; k < 3; ++k) dpin[k] = din[k];
+    for (int k = 0; k < 4; ++k) dpin[3 + k] = din[18 + k];
+    for (int k = 0; k < 15; ++k) dit[k] = din[3 + k];
+    if (which == 0) {
+        adj_tides_pre_jvp<1>(in[0], in[1], in[2], in[18], in[19], in[20], in[21], R, hR, hm, m, dpin, pre, dpre);
+        adj_tides_iter_jvp<1>(pre, dpre, ITER_ARGS(in), R, hR, hm, m, dit, out, dout);
+    } else if (which == 1) {
+        adj_flat_pre_jvp<1>(in[0], in[1], in[2], R, hR, hk2f, hm, k2f, m, dpin, pre, dpre);
+        adj_flat_iter_jvp<1>(pre, dpre, ITER_ARGS(in), R, hR, hk2f, hm, k2f, m, dit, out, dout);
+    } else {
+        adj_gr_pre_jvp<1>(in[0], in[1], in[2], hm, hmg, hmoi, m, mg, moi, dpin, pre, dpre);
+        adj_gr_iter_jvp<1>(pre, dpre, ITER_ARGS(in), hm, hmg, hmoi, m, mg, moi, dit, out, dout);
+    }
+}
+
 }  // extern "C"

@@ -44,6 +44,9 @@ def lib():
     h.h_kepler_vjp.argtypes = [ctypes.c_double, ctypes.c_double, f64p, f64p, ctypes.c_double, f64p, f64p, f64p, f64p]
     h.h_effects_fwd.argtypes = [ctypes.c_int, f64p, f64p, f64p]
     h.h_effects_vjp.argtypes = [ctypes.c_int, f64p, f64p, f64p, f64p]
+    h.h_kepler_jvp.argtypes = [ctypes.c_double, ctypes.c_double, f64p, f64p, ctypes.c_double, f64p, f64p, f64p,
+                               f64p]
+    h.h_effects_jvp.argtypes = [ctypes.c_int, f64p, f64p, f64p, f64p]
     return h
 
 
@@ -231,3 +234,43 @@ def test_effect_block_vjp_matches_finite_differences(lib, which):
             err = abs(bin_[k] - fd) * (scale if scale > 0 else 1.0)
             ref = max(abs(fd) * (scale if scale > 0 else 1.0), 1e-9)
             assert err <= 1e-5 * ref + 1e-12, (which, p, k, bin_[k], fd)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_kepler_jvp_matches_finite_differences(lib, seed):
+    rng = np.random.default_rng(200 + seed)
+    mu = E.G * rng.uniform(0.08, 1.0)
+    r, v = _orbit(rng, mu)
+    dt = 0.05
+    dr, dv = rng.normal(size=3) * np.linalg.norm(r), rng.normal(size=3) * np.linalg.norm(v)
+    r1, v1 = np.zeros(3), np.zeros(3)
+    X = lib.h_kepler_fwd(mu, dt, P(r), P(v), r1.ctypes.data_as(f64p), v1.ctypes.data_as(f64p))
+    dr1, dv1 = np.zeros(3), np.zeros(3)
+    lib.h_kepler_jvp(mu, dt, P(r), P(v), X, P(dr), P(dv), dr1.ctypes.data_as(f64p), dv1.ctypes.data_as(f64p))
+    h = 1e-6
+    outs = []
+    for sg in (1.0, -1.0):
+        a, b = np.zeros(3), np.zeros(3)
+        lib.h_kepler_fwd(mu, dt, P(r + sg * h * dr), P(v + sg * h * dv), a.ctypes.data_as(f64p),
+                         b.ctypes.data_as(f64p))
+        outs.append(np.concatenate([a, b]))
+    fd = (outs[0] - outs[1]) / (2 * h)
+    got = np.concatenate([dr1, dv1])
+    assert np.abs(got - fd).max() <= 1e-7 * np.abs(fd).max(), (got, fd)
+
+
+@pytest.mark.parametrize("which", [0, 1, 2])
+def test_effect_block_jvp_matches_vjp(lib, which):
+    """<v, J u> from the tangent sweep equals <J^T v, u> from the reverse sweep."""
+    st = _system(3)
+    rng = np.random.default_rng(10 + which)
+    for p in (1, 2, 3):
+        inp, c = _planet_inputs(st, p)
+        u = rng.normal(size=22) * np.abs(inp)
+        vv = rng.normal(size=9)
+        dout = np.zeros(9)
+        lib.h_effects_jvp(which, P(inp), P(c), P(u), dout.ctypes.data_as(f64p))
+        bin_ = np.zeros(22)
+        lib.h_effects_vjp(which, P(inp), P(c), P(vv), bin_.ctypes.data_as(f64p))
+        lhs, rhs = vv @ dout, bin_ @ u
+        assert abs(lhs - rhs) <= 1e-10 * (np.abs(vv * dout).sum() + 1e-300), (which, p, lhs, rhs)
