@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--launches", type=int, default=10, help="timed launches (L2 flushed before each)")
     p.add_argument("--mode", default="fast", choices=["fast", "exact"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-derivative", action="store_true",
+                   help="large workload: skip the timed derivative run (dissipation-factor tangents)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     return p.parse_args()
 
@@ -404,6 +406,54 @@ def run_gradient(args):
     print(json.dumps(result), flush=True)
 
 
+def large_derivative(mb, init, K, forward_ms, flush):
+    """Derivatives of the many-body run with respect to the two tidal
+    planets' dissipation factors: one launch of the engine carrying both
+    tangent directions over the same K steps (forward mode; two parameters),
+    then the loss gradient (torch) from the final state and the tangents."""
+    import torch
+
+    from posidonius_gb300 import adjoint as A
+    from posidonius_gb300 import layout as L
+
+    planets = (1, 2)
+    seeds = [(p, L.SEED_SIGMA) for p in planets]
+    host = int(init["sys_i64"][L.SI_HOST])
+    idx = [host, *planets]
+    b0 = init["body_f64"][idx]
+    with torch.no_grad():
+        t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64)
+        a0, _ = A.orbital_elements(t(b0[:, L.POS])[None], t(b0[:, L.VEL])[None], t(b0[:, L.BF_MASS])[None])
+    a0 = a0[0].numpy()
+    spin0 = np.linalg.norm(b0[1:, L.ANG], axis=-1) / b0[1:, L.BF_MOI]
+    mb.set_state(init)
+    mb.iterate_tangent(3, seeds)              # warm-up
+    mb.set_state(init)
+    flush.fill_(1.0)
+    torch.cuda.synchronize()
+    _, tan = mb.iterate_tangent(K, seeds)
+    tan_ms = mb.last_timing()
+    final = mb.get_state()
+    loss, grad = A.tangent_loss_gradient(final["body_f64"], tan, host, planets, a0, spin0)
+    # end to end: host state and zero tangents in, K steps, state, tangents and gradient out
+    t0 = time.perf_counter()
+    mb.set_state(init)
+    _, tan2 = mb.iterate_tangent(K, seeds)
+    fin2 = mb.get_state()
+    A.tangent_loss_gradient(fin2["body_f64"], tan2, host, planets, a0, spin0)
+    e2e_s = time.perf_counter() - t0
+    sig = init["body_f64"][list(planets), L.BF_SIGMA]
+    return {
+        "kind": "forward mode: tangents of every body's state along each planet's dissipation factor, both "
+                "directions in one launch of the engine; loss gradient = final-state gradient (torch) . tangents",
+        "parameters": [f"dissipation factor of body {p}" for p in planets],
+        "loss": "sum over the 2 planets of e^2 + ((a - a0)/a0)^2 + ((|Omega| - |Omega0|)/|Omega0|)^2",
+        "loss_value": loss, "dloss_dsigma": grad.tolist(), "dloss_dlog_sigma": (grad * sig).tolist(),
+        "ms": tan_ms, "ms_per_step": tan_ms / K, "over_forward": tan_ms / forward_ms,
+        "e2e_s": e2e_s, "gpu_launches": 1,
+    }
+
+
 def run_large(args):
     """Many-body workload: one system of N bodies (star, 2 tidal planets,
     N - 3 small massive bodies), K steps in one cooperative launch."""
@@ -454,14 +504,20 @@ def run_large(args):
                 "d2h_bytes_per_step": bytes_io / max(done, 1), "note": "posi_large_set_state, iterate, get_state"},
         "gpu_launches": 1, "status": int(final["sys_i64"][L.SI_STATUS]), "clocks": clock_info,
     }
+    if not args.no_derivative:
+        result["derivative"] = large_derivative(mb, init, K, ms, flush)
     if not args.no_cpu_baseline:
         import oracle
         from oracle.case_json import stack
         oracle.build()
         ens = stack([case])
         state, _, _ = oracle.run(ens, op=oracle.INITIALIZE)
+        # a short calibration run, then a sample of about --cpu-seconds
         t0 = time.perf_counter()
-        n_cpu = 3
+        oracle.run(state, max_steps=3, nthreads=1)
+        per_step = (time.perf_counter() - t0) / 3
+        n_cpu = max(3, int(args.cpu_seconds / max(per_step, 1e-9)))
+        t0 = time.perf_counter()
         oracle.run(state, max_steps=n_cpu, nthreads=1)
         cpu_s = time.perf_counter() - t0
         _, _, _, cnt = oracle.run(state, max_steps=1, flops=True)

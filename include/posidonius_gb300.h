@@ -392,6 +392,19 @@ int posi_large_get_state(const posi_large* L, int64_t* sys_i64, double* sys_f64,
 int posi_large_initialize_physical_values(posi_large* L);
 /* n_steps steps in one launch (fewer when the run completes or freezes). */
 int posi_large_iterate(posi_large* L, int64_t n_steps);
+/* Forward-mode derivatives (no reference counterpart: the reference computes
+ * no derivatives).  Integrates n_steps like posi_large_iterate while carrying
+ * the tangents of every body's state along n_dirs directions (1 to 4).
+ * tangents[d][i][12] (host memory; r, v, L, S of body i), in and out: on
+ * entry the tangent of the state along direction d (zeros for a pure
+ * parameter derivative), on return the tangent after the steps.  Direction d
+ * also perturbs, at unit rate, the parameter seed_param[d] of body
+ * seed_body[d]: POSI_SEED_SIGMA (dissipation factor) or POSI_SEED_K2 (Love
+ * number k2); seed_body[d] = -1 perturbs no parameter.  The primal state
+ * advances exactly as posi_large_iterate advances it. */
+enum posi_seed_param { POSI_SEED_SIGMA = 0, POSI_SEED_K2 = 1 };
+int posi_large_iterate_tangent(posi_large* L, int64_t n_steps, int32_t n_dirs, const int32_t* seed_body,
+                               const int32_t* seed_param, double* tangents);
 int posi_large_last_timing(const posi_large* L, double* ms);
 
 #ifdef __cplusplus

@@ -309,6 +309,23 @@ class ManyBody:
         """Returns layout.OK or layout.COMPLETED; raises on a physical event."""
         return check(lib().posi_large_iterate(self._h, int(n_steps)), ok=(L.OK, L.COMPLETED))
 
+    def iterate_tangent(self, n_steps, seeds, tangents=None):
+        """Forward-mode derivatives over n_steps (posi_large_iterate_tangent).
+
+        ``seeds``: up to 4 directions, each ``(body, param)`` with param
+        layout.SEED_SIGMA or layout.SEED_K2 (body -1: no parameter).
+        ``tangents``: [len(seeds), n, 12] initial state tangents (r, v, L, S
+        per body), zeros when None.  Returns (status, tangents after the
+        steps): d state / d parameter for a pure parameter seed."""
+        nd = len(seeds)
+        body = np.ascontiguousarray([int(b) for b, _ in seeds], dtype=np.int32)
+        param = np.ascontiguousarray([int(p) for _, p in seeds], dtype=np.int32)
+        tan = np.zeros((nd, self.n, 12), np.float64) if tangents is None else \
+            np.array(tangents, dtype=np.float64, order="C").reshape(nd, self.n, 12)
+        rc = check(lib().posi_large_iterate_tangent(self._h, int(n_steps), nd, ptr(body, "i32"), ptr(param, "i32"),
+                                                    ptr(tan, "f")), ok=(L.OK, L.COMPLETED))
+        return rc, tan
+
     def last_timing(self):
         ms = ctypes.c_double()
         check(lib().posi_large_last_timing(self._h, ctypes.byref(ms)))

@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libposidonius_gb300.so")
 _i64p = ctypes.POINTER(ctypes.c_int64)
 _f64p = ctypes.POINTER(ctypes.c_double)
 _intp = ctypes.POINTER(ctypes.c_int)
+_i32p = ctypes.POINTER(ctypes.c_int32)
 _vp = ctypes.c_void_p
 
 # name -> (restype, argtypes); every symbol declared in the C header.
@@ -65,6 +66,7 @@ SIGNATURES = {
     "posi_large_get_state": (ctypes.c_int, [_vp, _i64p, _f64p, _i64p, _f64p]),
     "posi_large_initialize_physical_values": (ctypes.c_int, [_vp]),
     "posi_large_iterate": (ctypes.c_int, [_vp, ctypes.c_int64]),
+    "posi_large_iterate_tangent": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int32, _i32p, _i32p, _f64p]),
     "posi_large_last_timing": (ctypes.c_int, [_vp, _f64p]),
     "posi_adjoint_vjp_static": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_int64,
                                                _vp, _vp, _vp, _vp]),
@@ -108,4 +110,4 @@ def check(status, ok=(L.OK,)):
 def ptr(a, kind):
     if a is None:
         return None
-    return a.ctypes.data_as(_i64p if kind == "i" else _f64p)
+    return a.ctypes.data_as({"i": _i64p, "i32": _i32p}.get(kind, _f64p))

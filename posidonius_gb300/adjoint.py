@@ -20,6 +20,14 @@ in src/tools.rs, and the pseudo-synchronous spin of src/tools.rs:909-927),
 and :func:`tidal_loss` is the objective of the differentiation workload: the
 sum of squared final eccentricities, squared relative semi-major-axis drifts
 and squared relative planetary spin-rate changes.
+
+For one system of many bodies (:class:`~posidonius_gb300.ManyBody`) with a
+few tidal parameters of interest, :func:`many_body_dissipation_gradient`
+takes the same loss's derivatives in forward mode: the engine carries the
+tangents of every body's state along each parameter direction
+(``posi_large_iterate_tangent``), and the derivative of the loss is the
+final-state gradient (torch) dotted with each tangent -- the same numbers a
+reverse sweep yields, at the cost of one run with a few directions.
 """
 import ctypes
 import math
@@ -450,6 +458,55 @@ def adjoint_gradient(ens, elements, sigma, k2, masses, moi, star_spin, n_steps, 
     traj.adjoint.close()
     batch.close()
     return out
+
+
+def tangent_loss_gradient(final_body_f64, tangents, host, planets, a0, spin0):
+    """Loss of :func:`tidal_loss` over ``planets`` (relative to ``host``) of a
+    final many-body state [n, BF_COUNT], and its derivative along each
+    tangent direction (tangents [D, n, 12]: r, v, L, S per body):
+    d loss = sum over bodies of (d loss / d r, v, L) . tangent."""
+    torch = _torch()
+    idx = [int(host)] + [int(p) for p in planets]
+    fin = np.asarray(final_body_f64)[idx]
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64)
+    r = t(fin[:, L.POS])[None].requires_grad_(True)
+    v = t(fin[:, L.VEL])[None].requires_grad_(True)
+    Ls = t(fin[:, L.ANG])[None].requires_grad_(True)
+    loss = tidal_loss(r, v, Ls, t(fin[:, L.BF_MASS])[None], t(fin[:, L.BF_MOI])[None], t(a0)[None],
+                      t(spin0)[None]).sum()
+    gr, gv, gL = torch.autograd.grad(loss, (r, v, Ls))
+    tan = t(np.asarray(tangents)[:, idx])
+    grad = (gr[0] * tan[..., 0:3]).sum((1, 2)) + (gv[0] * tan[..., 3:6]).sum((1, 2)) + \
+        (gL[0] * tan[..., 6:9]).sum((1, 2))
+    return float(loss.detach()), grad.numpy()
+
+
+def many_body_dissipation_gradient(case, n_steps, planets=(1, 2)):
+    """d loss / d (dissipation factor) of each of ``planets`` after ``n_steps``
+    of the many-body engine, the loss :func:`tidal_loss` of those planets
+    (initial semi-major axes and spin rates as the targets).  Returns
+    (loss, gradient [len(planets)], engine milliseconds of the tangent run,
+    final state)."""
+    from . import ManyBody
+    torch = _torch()
+    mb = ManyBody(case)
+    try:
+        mb.initialize_physical_values()
+        init = mb.get_state()
+        host = int(init["sys_i64"][L.SI_HOST])
+        idx = [host] + list(planets)
+        b0 = init["body_f64"][idx]
+        t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64)
+        with torch.no_grad():
+            a0, _ = orbital_elements(t(b0[:, L.POS])[None], t(b0[:, L.VEL])[None], t(b0[:, L.BF_MASS])[None])
+        spin0 = np.linalg.norm(b0[1:, L.ANG], axis=-1) / b0[1:, L.BF_MOI]
+        _, tan = mb.iterate_tangent(n_steps, [(int(p), L.SEED_SIGMA) for p in planets])
+        ms = mb.last_timing()
+        final = mb.get_state()
+    finally:
+        mb.close()
+    loss, grad = tangent_loss_gradient(final["body_f64"], tan, host, planets, a0[0].numpy(), spin0)
+    return loss, grad, ms, final
 
 
 def main(argv=None):

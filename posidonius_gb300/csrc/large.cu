@@ -12,7 +12,7 @@ struct posi_large {
     int64_t n = 0;
     int grid = 0, nchunk = 0, per_block = 0;
     double *d_bf = nullptr, *d_sf = nullptr, *d_roche = nullptr, *d_pos = nullptr, *d_gpart = nullptr,
-           *d_bpart = nullptr, *d_tot = nullptr;
+           *d_bpart = nullptr, *d_tot = nullptr, *d_tan = nullptr, *d_dpos = nullptr;
     int64_t *d_bi = nullptr, *d_si = nullptr;
     unsigned* d_bar = nullptr;
     int* d_err = nullptr;
@@ -28,7 +28,7 @@ void free_large(posi_large* L) {
     if (!L) return;
     cudaFree(L->d_bf); cudaFree(L->d_sf); cudaFree(L->d_roche); cudaFree(L->d_pos); cudaFree(L->d_gpart);
     cudaFree(L->d_bpart); cudaFree(L->d_tot); cudaFree(L->d_bi); cudaFree(L->d_si); cudaFree(L->d_bar); cudaFree(L->d_err);
-    cudaFree(L->d_bad);
+    cudaFree(L->d_bad); cudaFree(L->d_tan); cudaFree(L->d_dpos);
     if (L->e0) cudaEventDestroy(L->e0);
     if (L->e1) cudaEventDestroy(L->e1);
     if (L->stream) cudaStreamDestroy(L->stream);
@@ -85,7 +85,7 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return fail(POSI_ERR_CUDA, "no CUDA device", nullptr);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, posi_many::large_steps_kernel, posi_many::kBlock, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, posi_many::large_steps_kernel<0>, posi_many::kBlock, 0) !=
             cudaSuccess || per_sm < 1)
         return fail(POSI_ERR_CUDA, "occupancy query failed", nullptr);
     posi_large* L = new posi_large();
@@ -113,9 +113,11 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
         !ok(cudaMalloc(&L->d_si, POSI_SI_COUNT * sizeof(int64_t))) ||
         !ok(cudaMalloc(&L->d_roche, (size_t)n * n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_pos, (size_t)3 * n * sizeof(double))) ||
-        !ok(cudaMalloc(&L->d_gpart, (size_t)L->nchunk * 3 * n * sizeof(double))) ||
-        !ok(cudaMalloc(&L->d_bpart, (size_t)L->grid * posi_many::BP_SLOTS * sizeof(double))) ||
-        !ok(cudaMalloc(&L->d_tot, posi_many::BP_SLOTS * sizeof(double))) ||
+        !ok(cudaMalloc(&L->d_gpart, (size_t)L->nchunk * 3 * (1 + posi_many::kMaxTangents) * n * sizeof(double))) ||
+        !ok(cudaMalloc(&L->d_bpart, (size_t)L->grid * posi_many::BP_ROW * sizeof(double))) ||
+        !ok(cudaMalloc(&L->d_tot, posi_many::BP_ROW * sizeof(double))) ||
+        !ok(cudaMalloc(&L->d_tan, (size_t)posi_many::kMaxTangents * 12 * n * sizeof(double))) ||
+        !ok(cudaMalloc(&L->d_dpos, (size_t)posi_many::kMaxTangents * 3 * n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_bar, 2 * sizeof(unsigned))) || !ok(cudaMalloc(&L->d_err, sizeof(int))) ||
         !ok(cudaMalloc(&L->d_bad, sizeof(unsigned long long))) ||
         !ok(cudaMemset(L->d_bar, 0, 2 * sizeof(unsigned))) || !ok(cudaMemset(L->d_err, 0, sizeof(int))))
@@ -197,10 +199,21 @@ int posi_large_initialize_physical_values(posi_large* L) {
     return POSI_OK;
 }
 
-int posi_large_iterate(posi_large* L, int64_t n_steps) {
-    if (!L || n_steps < 0) return POSI_ERR_ARG;
-    if (n_steps == 0) return POSI_OK;
-    posi_many::LDev d;
+}  // extern "C"
+
+namespace {
+
+// One cooperative launch of the engine (NT tangent directions) and its
+// error report.
+template <int NT>
+int run_large(posi_large* L, int64_t n_steps, const int32_t* seed_body, const int32_t* seed_param) {
+    int per_sm = 0;
+    LCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, posi_many::large_steps_kernel<NT>, posi_many::kBlock, 0));
+    if (per_sm < 1) {
+        posi::set_last_error("the engine's blocks do not fit one per SM");
+        return POSI_ERR_CUDA;
+    }
+    posi_many::LDev d{};
     d.n = L->n;
     d.bf = L->d_bf; d.bi = L->d_bi; d.sf = L->d_sf; d.si = L->d_si; d.roche = L->d_roche;
     d.pos = L->d_pos; d.gpart = L->d_gpart; d.bpart = L->d_bpart; d.tot = L->d_tot; d.bar = L->d_bar;
@@ -208,10 +221,16 @@ int posi_large_iterate(posi_large* L, int64_t n_steps) {
     d.bad = L->d_bad;
     d.nchunk = L->nchunk;
     d.per_block = L->per_block;
+    d.tan = L->d_tan;
+    d.dpos = L->d_dpos;
+    for (int k = 0; k < posi_many::kMaxTangents; ++k) {
+        d.seed_body[k] = seed_body ? seed_body[k] : -1;
+        d.seed_param[k] = seed_param ? seed_param[k] : 0;
+    }
     LCK(cudaMemsetAsync(L->d_bad, 0xff, sizeof(unsigned long long), L->stream));
     void* args[] = {&d, &n_steps};
     LCK(cudaEventRecord(L->e0, L->stream));
-    LCK(cudaLaunchCooperativeKernel((const void*)posi_many::large_steps_kernel, dim3(L->grid),
+    LCK(cudaLaunchCooperativeKernel((const void*)posi_many::large_steps_kernel<NT>, dim3(L->grid),
                                     dim3(posi_many::kBlock), args, 0, L->stream));
     LCK(cudaEventRecord(L->e1, L->stream));
     LCK(cudaEventSynchronize(L->e1));
@@ -241,6 +260,58 @@ int posi_large_iterate(posi_large* L, int64_t n_steps) {
         return POSI_ERR_PHYSICS;
     }
     return POSI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int posi_large_iterate(posi_large* L, int64_t n_steps) {
+    if (!L || n_steps < 0) return POSI_ERR_ARG;
+    if (n_steps == 0) return POSI_OK;
+    return run_large<0>(L, n_steps, nullptr, nullptr);
+}
+
+int posi_large_iterate_tangent(posi_large* L, int64_t n_steps, int32_t n_dirs, const int32_t* seed_body,
+                               const int32_t* seed_param, double* tangents) {
+    if (!L || n_steps < 0 || n_dirs < 1 || n_dirs > posi_many::kMaxTangents || !seed_body || !seed_param || !tangents) {
+        posi::set_last_error("bad arguments (1 to 4 directions, seeds and tangents required)");
+        return POSI_ERR_ARG;
+    }
+    const int64_t n = L->n;
+    for (int d = 0; d < n_dirs; ++d) {
+        if (seed_body[d] < -1 || seed_body[d] >= n || (seed_param[d] != posi_many::SEED_SIGMA &&
+                                                        seed_param[d] != posi_many::SEED_K2)) {
+            posi::set_last_error("seed " + std::to_string(d) + " out of range");
+            return POSI_ERR_ARG;
+        }
+    }
+    // the kernels carry 1, 2 or 4 directions; padding directions are zero
+    const int nt = n_dirs == 1 ? 1 : n_dirs == 2 ? 2 : 4;
+    int32_t sb[posi_many::kMaxTangents], sp[posi_many::kMaxTangents];
+    for (int d = 0; d < posi_many::kMaxTangents; ++d) {
+        sb[d] = d < n_dirs ? seed_body[d] : -1;
+        sp[d] = d < n_dirs ? seed_param[d] : 0;
+    }
+    // host [dir][body][12] <-> device [dir][12][body]
+    std::vector<double> dev((size_t)nt * 12 * n, 0.);
+    for (int d = 0; d < n_dirs; ++d)
+        for (int64_t i = 0; i < n; ++i)
+            for (int f = 0; f < 12; ++f) dev[((size_t)d * 12 + f) * n + i] = tangents[((size_t)d * n + i) * 12 + f];
+    LCK(cudaMemcpy(L->d_tan, dev.data(), dev.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (n_steps == 0) return POSI_OK;
+    int rc;
+    switch (nt) {
+        case 1: rc = run_large<1>(L, n_steps, sb, sp); break;
+        case 2: rc = run_large<2>(L, n_steps, sb, sp); break;
+        default: rc = run_large<4>(L, n_steps, sb, sp); break;
+    }
+    if (rc == POSI_ERR_CUDA) return rc;  // barrier failure: the launch wrote nothing back
+    LCK(cudaMemcpy(dev.data(), L->d_tan, dev.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int d = 0; d < n_dirs; ++d)
+        for (int64_t i = 0; i < n; ++i)
+            for (int f = 0; f < 12; ++f) tangents[((size_t)d * n + i) * 12 + f] = dev[((size_t)d * 12 + f) * n + i];
+    return rc;
 }
 
 int posi_large_last_timing(const posi_large* L, double* ms) {

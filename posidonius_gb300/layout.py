@@ -95,3 +95,7 @@ ADJ_KEPLER = 1
 ADJ_ZERO_INERTIA = 2
 ADJ_FROZEN = 4
 ADJ_UNSUPPORTED = 8
+
+# posi_seed_param (parameters a tangent direction of the many-body engine perturbs)
+SEED_SIGMA = 0
+SEED_K2 = 1
