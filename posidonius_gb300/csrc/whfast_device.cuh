@@ -194,6 +194,12 @@ struct Sys {
     double inv_m, inv_moi, inv_eta_excl, jac_c, eta_incl, kep_gm, gm_neg, whds_f, whds_w, dh_w;
     double inv_mtot, inv_hm;
     bool first_planet;
+    // The per-planet constants of a half kick depend on the heliocentric
+    // positions and on masses, radii and tidal parameters only.  Between the
+    // closing half kick of one step and the opening half kick of the next
+    // nothing moves, so without evolution the opening kick reuses them.
+    bool pc_valid;   // P(PC_*) hold the constants of the current positions
+    bool pc_reuse;   // this half kick reuses them
 #endif
 
     __device__ __forceinline__ void sync() const {
@@ -315,6 +321,8 @@ struct Sys {
         sync();
 #if !POSI_EXACT
         mass_constants();
+        pc_valid = false;
+        pc_reuse = false;
 #endif
     }
 
@@ -543,6 +551,87 @@ struct Sys {
         P(PC_ZD) = z * inv_d;
     }
 
+#if !POSI_EXACT
+    // FAST: the same constants from powers of 1 / d and two reciprocals
+    // (1 / (m_host + m) and 1 / (mg_host + mg)) instead of a division each.
+    __device__ void planet_constants() {
+        const double hm = card[HC_M], hmg = card[HC_MG], hR = card[HC_R], hsig = card[HC_SIG];
+        const double hk2 = card[HC_K2], hk2f = card[HC_K2F];
+        const double id = P(PC_INV_D);
+        const double id2 = id * id, id5 = id2 * id2 * id, id7 = id5 * id2;
+        if (tides && b.tk == POSI_EFFECT_ORBITING) {
+            // src/effects/tides/constant_time_lag.rs:229-264, :266-307
+            const double hm2 = hm * hm, m2 = b.m * b.m;
+            const double term1 = m2 * powi<10>(hR) * hsig;
+            const double term2 = hm2 * powi<10>(b.R) * b.sig;
+            const double o_s = 4.5 * term1 * id7;
+            const double o_p = 4.5 * term2 * id7;
+            P(PC_OS) = o_s;
+            P(PC_OP) = o_p;
+            P(PC_OSD) = o_s * id;
+            P(PC_OPD) = o_p * id;
+            P(PC_CONS) = kMINUS_3K2 * id7 * (m2 * powi<5>(hR) * hk2 + hm2 * powi<5>(b.R) * b.k2);
+            P(PC_TERM2) = term2;
+            P(PC_OSPD) = (o_s + o_p) * id;
+            const double d = P(PC_D);
+            P(PC_OSDD) = o_s * d;
+            P(PC_OPDD) = o_p * d;
+            P(PC_C13) = -13.5 * (id7 * id);
+            P(PC_T12) = term1 + term2;
+        }
+        if (flat && b.fk == POSI_EFFECT_ORBITING) {
+            // src/effects/rotational_flattening/oblate_spheroid.rs:12-60
+            P(PC_N3D5) = -3. * id5;
+            P(PC_F15D7) = 15. * id7;
+            // factor_star = cfs |Omega_host|^2, ortho_star = cofs (r . Omega_host(previous))
+            const double cfs = b.m * hk2f * powi<5>(hR) * (1. / 6.);
+            const double cfp = hm * b.k2f * powi<5>(b.R) * (1. / 6.);
+            P(PC_CFS) = cfs;
+            P(PC_CFP) = cfp;
+            P(PC_COFS) = -6. * cfs * id5;
+            P(PC_COFP) = -6. * cfp * id5;
+        }
+        if (gr && b.gk == POSI_EFFECT_ORBITING) {
+            // src/effects/general_relativity.rs:98, :187-298, :300-456
+            const double mgs = hmg + b.mg;
+            const double imgs = 1. / mgs;
+            const double f = hmg * b.mg * (imgs * imgs);
+            const double mgd = mgs * id;
+            const double f2 = f * f;
+            const double gd2 = mgs * id2 * (1. / kC2);
+            const double A = -gd2;
+            P(PC_A) = A;
+            P(PC_B) = 1.0 + 3.0 * f;
+            P(PC_C) = 2.0 * (2.0 + f) * mgd;
+            P(PC_DD) = 1.5 * f;
+            P(PC_E) = gd2 * 2.0 * (2.0 - f);
+            P(PC_T1) = (3.0 / 4.0) * (12.0 + 29.0 * f) * (mgd * mgd);
+            P(PC_K2C) = f * (3.0 - 4.0 * f);
+            P(PC_K3C) = (15.0 / 8.0) * f * (1.0 - 3.0 * f);
+            P(PC_K4C) = (3.0 / 2.0) * f * (3.0 - 4.0 * f);
+            P(PC_K5C) = 0.5 * f * (13.0 - 4.0 * f) * mgd;
+            P(PC_K6C) = (2.0 + 25.0 * f + 2.0 * f2) * mgd;
+            P(PC_A05) = A * (-0.5);
+            P(PC_P) = f * (15.0 + 4.0 * f);
+            P(PC_Q) = (4.0 + 41.0 * f + 8.0 * f2) * mgd;
+            P(PC_R3) = 3.0 * f * (3.0 + 2.0 * f);
+            const double M = hm + b.m;
+            const double iM = 1. / M;
+            P(PC_MFM) = hm - b.m;                    // ((m_host - m) / M) M
+            P(PC_MU) = (hm * b.m) * iM;
+            P(PC_FM) = 2. + (3. / 2.) * b.m * inv_hm;
+            P(PC_FM2) = 2. + (3. / 2.) * hm * inv_m;
+            const double n0 = P(PC_XD), n1 = P(PC_YD), n2 = P(PC_ZD);
+            P(PC_NN0) = n0;
+            P(PC_NN1) = n1;
+            P(PC_NN2) = n2;
+            P(PC_C6NN0) = 6. * n0;
+            P(PC_C6NN1) = 6. * n1;
+            P(PC_C6NN2) = 6. * n2;
+        }
+        P(PC_MRATIO) = b.m * hm == 0. ? 0. : b.m * inv_hm;
+    }
+#else
     __device__ void planet_constants() {
         const double hm = card[HC_M], hmg = card[HC_MG], hR = card[HC_R], hsig = card[HC_SIG];
         const double hk2 = card[HC_K2], hk2f = card[HC_K2F];
@@ -566,13 +655,6 @@ struct Sys {
             const double term2 = hm2 * powi<10>(b.R) * b.sig;
             P(PC_TERM1) = term1;
             P(PC_TERM2) = term2;
-#if !POSI_EXACT
-            P(PC_OSPD) = (o_s + o_p) * inv_d;
-            P(PC_OSDD) = o_s * d;
-            P(PC_OPDD) = o_p * d;
-            P(PC_C13) = -13.5 / d8;
-            P(PC_T12) = term1 + term2;
-#endif
         }
         if (flat && b.fk == POSI_EFFECT_ORBITING) {
             // src/effects/rotational_flattening/oblate_spheroid.rs:12-60
@@ -583,16 +665,6 @@ struct Sys {
             P(PC_D5) = powi<5>(d);
             P(PC_N3D5) = -3. / powi<5>(d);
             P(PC_F15D7) = 15. / powi<7>(d);
-#if !POSI_EXACT
-            // factor_star = cfs |Omega_host|^2, ortho_star = cofs (r . Omega_host(previous))
-            const double cfs = b.m * hk2f * powi<5>(hR) * (1. / 6.);
-            const double cfp = hm * b.k2f * powi<5>(b.R) * (1. / 6.);
-            const double inv_d5 = 1. / powi<5>(d);
-            P(PC_CFS) = cfs;
-            P(PC_CFP) = cfp;
-            P(PC_COFS) = -6. * cfs * inv_d5;
-            P(PC_COFP) = -6. * cfp * inv_d5;
-#endif
         }
         if (gr && b.gk == POSI_EFFECT_ORBITING) {
             // src/effects/general_relativity.rs:98, :187-298, :300-456
@@ -632,10 +704,8 @@ struct Sys {
             P(PC_C6NN1) = 6. * n1;
             P(PC_C6NN2) = 6. * n2;
         }
-#if !POSI_EXACT
-        if (!(gr && b.gk == POSI_EFFECT_ORBITING)) P(PC_MRATIO) = b.m * card[HC_M] == 0. ? 0. : b.m / hm;
-#endif
     }
+#endif
 
     // ------------------------------------------------------------------
     // One evaluation of src/particles/universe.rs:428-538 (after
@@ -907,7 +977,7 @@ struct Sys {
             card[HC_SLX] = b.moi * b.S[0]; card[HC_SLY] = b.moi * b.S[1]; card[HC_SLZ] = b.moi * b.S[2];
         }
         sync();
-        if (it == 0 && planet()) planet_constants();
+        if (it == 0 && planet() && !pc_reuse) planet_constants();
         sync();
         const double hS0 = card[HC_SX], hS1 = card[HC_SY], hS2 = card[HC_SZ];
         double aa0 = 0., aa1 = 0., aa2 = 0., dl0 = 0., dl1 = 0., dl2 = 0.;  // own outputs
@@ -1030,7 +1100,12 @@ struct Sys {
                        card[HC_M] = b.m; card[HC_MG] = b.mg; card[HC_R] = b.R; card[HC_SIG] = b.sig;
                        card[HC_K2] = b.k2; card[HC_K2F] = b.k2f; }
         sync();
+#if POSI_EXACT
         if (planet()) set_geometry(b.r[0] - card[HC_PX], b.r[1] - card[HC_PY], b.r[2] - card[HC_PZ]);
+#else
+        pc_reuse = pc_valid && !evo;
+        if (planet() && !pc_reuse) set_geometry(b.r[0] - card[HC_PX], b.r[1] - card[HC_PY], b.r[2] - card[HC_PZ]);
+#endif
         double ov[3], oL[3], fv[3], fL[3], dvc[3] = {0., 0., 0.}, dLc[3] = {0., 0., 0.};
 #pragma unroll
         for (int k = 0; k < 3; ++k) { ov[k] = b.v[k]; oL[k] = b.L[k]; fv[k] = ov[k]; fL[k] = oL[k]; }
@@ -1076,8 +1151,13 @@ struct Sys {
                 colfold(0, spin_on ? 4 : 2, nullptr, false, false);
                 const double dv2 = sums[0], fv2 = sums[1];
                 bool conv;
+#if POSI_EXACT
                 if (spin_on) conv = dv2 / fv2 < kDBL_EPSILON_2 && sums[2] / sums[3] < kDBL_EPSILON_2;
                 else conv = dv2 / fv2 < kDBL_EPSILON_2;
+#else
+                // a / b < eps^2 as a < eps^2 b (b >= 0; b = 0 fails both ways)
+                conv = dv2 < kDBL_EPSILON_2 * fv2 && (!spin_on || sums[2] < kDBL_EPSILON_2 * sums[3]);
+#endif
                 if (conv) { converged = true; break; }
             }
             if (has) {
@@ -1550,7 +1630,28 @@ struct Sys {
                 e = eta0 * gs[1] + zeta0 * gs[2];
                 ri = 1. / (r0 + e);
                 x = ri * (x * e - eta0 * gs[2] - zeta0 * gs[3] + kdt);
+#if POSI_EXACT
                 if (x == old_x || x == old_x2) { converged = 1; break; }
+#else
+                // quadratic convergence: a step below 1e-15 |x| leaves the
+                // next one below rounding, so stop one iteration earlier and
+                // move the G functions to the new root by their derivatives
+                // (dG_n/dx = G_(n-1), dG_0/dx = -beta G_1; second-order error
+                // about 1e-30): the drift stays a smooth function of x.
+                if (x == old_x || x == old_x2) { converged = 1; break; }
+                if (fabs(x - old_x) <= 1e-15 * fabs(x)) {
+                    const double dx = x - old_x;
+                    const double g0 = gs[0], g1 = gs[1], g2 = gs[2];
+                    gs[0] = g0 - beta * g1 * dx;
+                    gs[1] = g1 + g0 * dx;
+                    gs[2] = g2 + g1 * dx;
+                    gs[3] = gs[3] + g2 * dx;
+                    e = eta0 * gs[1] + zeta0 * gs[2];
+                    ri = 1. / (r0 + e);
+                    converged = 1;
+                    break;
+                }
+#endif
             }
         }
         if (converged == 0) {
@@ -1716,6 +1817,9 @@ struct Sys {
         }
         integrate_velocity_dependent_forces(D, half_dt, true, rp ? posi_rec::SV_H1 : -1);
         if (fatal()) return false;
+#if !POSI_EXACT
+        pc_valid = false;  // the drifts move every body
+#endif
         inertial_to_alternative();
         if (rp)
 #pragma unroll
@@ -1747,6 +1851,9 @@ struct Sys {
         if (fatal()) return false;
         integrate_velocity_dependent_forces(D, half_dt, false, rp ? posi_rec::SV_H2 : -1);
         if (fatal()) return false;
+#if !POSI_EXACT
+        pc_valid = true;
+#endif
         t += dt;
         iteration += 1;
         if (lane == 0 && D.step_flags) D.step_flags[s] = (rec_trig || first ? 1 : 0) | ((first || hist_trig) ? 2 : 0);
