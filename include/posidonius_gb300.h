@@ -33,7 +33,7 @@ enum posi_status {
     POSI_ERR_IO = -2,            /* file missing or unreadable (src/integrator/output.rs:178-203) */
     POSI_ERR_PARSE = -3,         /* malformed JSON case */
     POSI_ERR_UNSUPPORTED = -4,   /* case uses an effect outside this path (Kaula, creep, disk, wind,
-                                    dynamic tides, Anderson/Newhall GR, non-WHFast integrator, ...) */
+                                    dynamic tides, non-WHFast integrator, ...) */
     POSI_ERR_CUDA = -5,          /* CUDA runtime error or no device */
     POSI_ERR_PHYSICS = -6,       /* a system hit a reference panic (see posi_system_status) */
     POSI_ERR_STATE = -7          /* call not valid in this state (e.g. initialise a resumed run) */
@@ -63,6 +63,8 @@ enum posi_system_status {
  */
 enum posi_coords { POSI_JACOBI = 0, POSI_DEMOCRATIC_HELIOCENTRIC = 1, POSI_WHDS = 2 };
 enum posi_effect_kind { POSI_EFFECT_DISABLED = 0, POSI_EFFECT_CENTRAL = 1, POSI_EFFECT_ORBITING = 2 };
+/* GeneralRelativityImplementation (src/effects/general_relativity.rs) */
+enum posi_gr_impl { POSI_GR_KIDDER1995 = 0, POSI_GR_ANDERSON1975 = 1, POSI_GR_NEWHALL1983 = 2 };
 enum posi_evolution {
     POSI_EVO_NON_EVOLVING = 0,
     POSI_EVO_LECONTE2011 = 1,
@@ -77,7 +79,7 @@ enum posi_sys_i64_field {
     POSI_SI_COORDS,              /* WHFast.alternative_coordinates_type */
     POSI_SI_TIDES,               /* ConsiderEffects.tides */
     POSI_SI_FLAT,                /* ConsiderEffects.rotational_flattening */
-    POSI_SI_GR,                  /* ConsiderEffects.general_relativity (Kidder1995) */
+    POSI_SI_GR,                  /* ConsiderEffects.general_relativity */
     POSI_SI_EVOLUTION,           /* ConsiderEffects.evolution */
     POSI_SI_ITERATION,           /* WHFast.current_iteration */
     POSI_SI_N_HIST,              /* WHFast.n_historic_snapshots */
@@ -86,6 +88,7 @@ enum posi_sys_i64_field {
     POSI_SI_FAIL_STEP,           /* iteration at which a fatal event froze the system */
     POSI_SI_FAIL_PAIR,           /* i*1024 + j of the offending pair */
     POSI_SI_LAST_MIDPOINT_ITERS, /* midpoint iterations of the last half kick */
+    POSI_SI_GR_IMPL,             /* Universe.general_relativity_implementation (posi_gr_impl) */
     POSI_SI_COUNT
 };
 
@@ -105,7 +108,7 @@ enum posi_sys_f64_field {
 enum posi_body_i64_field {
     POSI_BI_TIDES_KIND = 0,      /* TidesEffect: posi_effect_kind (ConstantTimeLag model) */
     POSI_BI_FLAT_KIND,           /* RotationalFlatteningEffect: posi_effect_kind (OblateSpheroid) */
-    POSI_BI_GR_KIND,             /* GeneralRelativityEffect: posi_effect_kind (Kidder1995) */
+    POSI_BI_GR_KIND,             /* GeneralRelativityEffect: posi_effect_kind */
     POSI_BI_EVO_TYPE,            /* posi_evolution */
     POSI_BI_EVO_OFFSET,          /* offset of this body's tables in `tables` */
     POSI_BI_EVO_LEN,             /* rows per table (time, radius, rg2, love: 4*len doubles) */

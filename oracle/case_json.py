@@ -71,11 +71,12 @@ def load_case(path_or_dict):
     if ce["disk"] or ce["wind"]:
         raise Unsupported("disk/wind effects")
     gr_impl = u["general_relativity_implementation"]
-    if ce["general_relativity"] and gr_impl != "Kidder1995":
+    gr_codes = {"Kidder1995": L.GR_KIDDER1995, "Anderson1975": L.GR_ANDERSON1975, "Newhall1983": L.GR_NEWHALL1983}
+    if ce["general_relativity"] and gr_impl not in gr_codes:
         raise Unsupported(f"general relativity {gr_impl}")
     hosts = u["hosts"]
     host = int(hosts["index"]["most_massive"])
-    for eff in ("tides", "rotational_flattening"):
+    for eff in ("tides", "rotational_flattening", "general_relativity"):
         if ce[eff] and int(hosts["index"][eff]) != host:
             raise Unsupported(f"{eff} host is not the most massive body")
 
@@ -90,6 +91,7 @@ def load_case(path_or_dict):
     si[L.SI_TIDES] = int(ce["tides"])
     si[L.SI_FLAT] = int(ce["rotational_flattening"])
     si[L.SI_GR] = int(ce["general_relativity"])
+    si[L.SI_GR_IMPL] = gr_codes.get(gr_impl, L.GR_KIDDER1995)
     si[L.SI_EVOLUTION] = int(ce["evolution"])
     si[L.SI_ITERATION] = int(d["current_iteration"])
     si[L.SI_N_HIST] = int(d["n_historic_snapshots"])
@@ -115,8 +117,8 @@ def load_case(path_or_dict):
         if p["wind"]["effect"] != "Disabled" or p["disk"]["effect"] != "Disabled":
             if ce["wind"] or ce["disk"]:
                 raise Unsupported("wind/disk body")
-        if gk == L.EFFECT_CENTRAL and gimpl != "Kidder1995" and ce["general_relativity"]:
-            raise Unsupported(f"general relativity {gimpl}")
+        if gk == L.EFFECT_CENTRAL and gimpl != gr_impl and ce["general_relativity"]:
+            raise Unsupported(f"general relativity host {gimpl} differs from the universe's {gr_impl}")
         if ce["tides"] and b != host and tk != L.EFFECT_ORBITING:
             # The reference's host torque loop visits every body and divides
             # by the stale distance 0 of a non-orbiting one (NaN spin).

@@ -176,6 +176,7 @@ struct AltCoords {
 struct Sim {
     int n = 0, host = 0, coords = POSI_JACOBI;
     bool tides = false, flat = false, gr = false, evolution = false;
+    int gr_impl = POSI_GR_KIDDER1995;   // Universe.general_relativity_implementation
     real dt = 0., half_dt = 0., t = 0., time_limit = 0.;
     real last_hist = -1., hist_period = 0., last_rec = -1., rec_period = 0.;
     int64_t iteration = 0, n_hist = 0, timestep_warning = 0, status = 0, fail_step = 0, fail_pair = 0;
@@ -390,7 +391,7 @@ static void inertial_to_heliocentric(Sim& s) {
 static void initialize(Sim& s, bool dl, bool acc) {
     const bool it = (dl && s.tides) || (acc && s.tides);
     const bool ifl = (dl && s.flat) || (acc && s.flat);
-    const bool igr = (dl && s.gr) || (acc && s.gr);
+    const bool igr = (dl && s.gr && s.gr_impl == POSI_GR_KIDDER1995) || (acc && s.gr);
     if (it || ifl || igr) {
         Particle& h = s.p[s.host];
         if (it && h.tides.kind == POSI_EFFECT_CENTRAL) {
@@ -446,14 +447,17 @@ static void initialize(Sim& s, bool dl, bool acc) {
                     q.gr.norm_v = q.hnv; q.gr.norm_v2 = q.hnv2;
                 }
             }
-            h.gr.factor = 0.;
-            h.gr.out_acc = V3{0., 0., 0.}; h.gr.out_dldt = V3{0., 0., 0.};
-            for (int i = 0; i < s.n; ++i) {
-                if (i == s.host) continue;
-                Particle& q = s.p[i];
-                if (q.gr.kind == POSI_EFFECT_ORBITING) {
-                    q.gr.factor = h.mass_g * q.mass_g / powi(h.mass_g + q.mass_g, 2);
-                    q.gr.out_acc = V3{0., 0., 0.}; q.gr.out_dldt = V3{0., 0., 0.};
+            // general_relativity::initialize: not for Newhall1983
+            if (s.gr_impl != POSI_GR_NEWHALL1983) {
+                h.gr.factor = 0.;
+                h.gr.out_acc = V3{0., 0., 0.}; h.gr.out_dldt = V3{0., 0., 0.};
+                for (int i = 0; i < s.n; ++i) {
+                    if (i == s.host) continue;
+                    Particle& q = s.p[i];
+                    if (q.gr.kind == POSI_EFFECT_ORBITING) {
+                        q.gr.factor = h.mass_g * q.mass_g / powi(h.mass_g + q.mass_g, 2);
+                        q.gr.out_acc = V3{0., 0., 0.}; q.gr.out_dldt = V3{0., 0., 0.};
+                    }
                 }
             }
         }
@@ -862,6 +866,224 @@ static void gr_spin_orbit(Sim& s) {
     h.gr.out_acc.z += real(-1.0) * sum.z;
 }
 
+// ---------------------------------------------------------------------------
+// General relativity after REBOUNDx gr.c: src/effects/general_relativity.rs
+// ---------------------------------------------------------------------------
+// Bodies other than the host, in index order (the reference's
+// particles.iter().chain(more_particles.iter())).
+static std::vector<int> others(const Sim& s) {
+    std::vector<int> o;
+    for (int i = 0; i < s.n; ++i)
+        if (i != s.host) o.push_back(i);
+    return o;
+}
+
+// :661-697 -- the integrator's gravity accelerations plus the host terms it
+// ignored (WHFastOne: the first other body only; WHFastTwo: all).  The
+// separation is the host's inertial position minus the body's heliocentric
+// (GR) position, as in the reference.
+static void gr_newtonian_accelerations(Sim& s, int ignore, V3& ha, std::vector<V3>& na) {
+    const std::vector<int> o = others(s);
+    Particle& h = s.p[s.host];
+    ha = h.a;
+    na.assign(o.size(), V3{0., 0., 0.});
+    for (size_t k = 0; k < o.size(); ++k) na[k] = s.p[o[k]].a;
+    if (ignore == 1 || ignore == 2) {
+        const size_t np = ignore == 1 ? 1 : o.size();
+        for (size_t k = 0; k < np && k < o.size(); ++k) {
+            const Particle& q = s.p[o[k]];
+            real dx = h.r.x - q.gr.pos.x, dy = h.r.y - q.gr.pos.y, dz = h.r.z - q.gr.pos.z;
+            real r2 = powi(dx, 2) + powi(dy, 2) + powi(dz, 2);
+            real r = rsqrt_(r2);
+            real prefac = G / (r2 * r);
+            real pms = prefac * h.mass;
+            real pmp = prefac * q.mass;
+            ha.x -= pmp * dx; ha.y -= pmp * dy; ha.z -= pmp * dz;
+            na[k].x += pms * dx; na[k].y += pms * dy; na[k].z += pms * dz;
+        }
+    }
+}
+
+// :461-535 with the Jacobi transforms :537-634
+static void gr_anderson1975(Sim& s, int ignore) {
+    const std::vector<int> o = others(s);
+    const size_t no = o.size();
+    Particle& h = s.p[s.host];
+    V3 ha;
+    std::vector<V3> na;
+    gr_newtonian_accelerations(s, ignore, ha, na);
+    std::vector<V3> jp(no, V3{0., 0., 0.}), jv(no, V3{0., 0., 0.}), ja(no, V3{0., 0., 0.});
+    real eta = h.mass;
+    real sx = eta * h.r.x, sy = eta * h.r.y, sz = eta * h.r.z;
+    real svx = eta * h.v.x, svy = eta * h.v.y, svz = eta * h.v.z;
+    real sax = eta * ha.x, say = eta * ha.y, saz = eta * ha.z;
+    for (size_t k = 0; k < no; ++k) {
+        const Particle& q = s.p[o[k]];
+        if (q.gr.kind != POSI_EFFECT_ORBITING) continue;
+        real ei = real(1.) / eta;
+        eta += q.mass;
+        real pme = eta * ei;
+        jp[k].x = q.r.x - sx * ei; jp[k].y = q.r.y - sy * ei; jp[k].z = q.r.z - sz * ei;
+        jv[k].x = q.v.x - svx * ei; jv[k].y = q.v.y - svy * ei; jv[k].z = q.v.z - svz * ei;
+        ja[k].x = na[k].x - sax * ei; ja[k].y = na[k].y - say * ei; ja[k].z = na[k].z - saz * ei;
+        sx = sx * pme + q.mass * jp[k].x; sy = sy * pme + q.mass * jp[k].y; sz = sz * pme + q.mass * jp[k].z;
+        svx = svx * pme + q.mass * jv[k].x; svy = svy * pme + q.mass * jv[k].y; svz = svz * pme + q.mass * jv[k].z;
+        sax = sax * pme + q.mass * ja[k].x; say = say * pme + q.mass * ja[k].y; saz = saz * pme + q.mass * ja[k].z;
+    }
+    const real mtot = eta;
+    const real mu = h.mass_g;
+    for (size_t k = 0; k < no; ++k) {
+        const Particle& q = s.p[o[k]];
+        if (q.gr.kind != POSI_EFFECT_ORBITING) continue;
+        V3 vi = jv[k];
+        real vi2 = powi(jv[k].x, 2) + powi(jv[k].y, 2) + powi(jv[k].z, 2);
+        real ri = rsqrt_(powi(jp[k].x, 2) + powi(jp[k].y, 2) + powi(jp[k].z, 2));
+        real fa = (real(0.5) * vi2 + real(3.) * mu / ri) / SPEED_OF_LIGHT_2;
+        for (int it = 0; it < 10; ++it) {
+            V3 old = vi;
+            vi.x = jv[k].x / (real(1.) - fa);
+            vi.y = jv[k].y / (real(1.) - fa);
+            vi.z = jv[k].z / (real(1.) - fa);
+            vi2 = vi.x * vi.x + vi.y * vi.y + vi.z * vi.z;
+            fa = (real(0.5) * vi2 + real(3.) * mu / ri) / SPEED_OF_LIGHT_2;
+            real dvx = vi.x - old.x, dvy = vi.y - old.y, dvz = vi.z - old.z;
+            if ((dvx * dvx + dvy * dvy + dvz * dvz) / vi2 < DBL_EPSILON_2) break;
+        }
+        real fb = (mu / ri - real(1.5) * vi2) * mu / (ri * ri * ri) / SPEED_OF_LIGHT_2;
+        real rdotrdot = jp[k].x * jv[k].x + jp[k].y * jv[k].y + jp[k].z * jv[k].z;
+        V3 vidot{ja[k].x + fb * jp[k].x, ja[k].y + fb * jp[k].y, ja[k].z + fb * jp[k].z};
+        real vdotvdot = vi.x * vidot.x + vi.y * vidot.y + vi.z * vidot.z;
+        real fd = (vdotvdot - real(3.) * mu / (ri * ri * ri) * rdotrdot) / SPEED_OF_LIGHT_2;
+        ja[k].x = fb * (real(1.) - fa) * jp[k].x - fa * ja[k].x - fd * vi.x;
+        ja[k].y = fb * (real(1.) - fa) * jp[k].y - fa * ja[k].y - fd * vi.y;
+        ja[k].z = fb * (real(1.) - fa) * jp[k].z - fa * ja[k].z - fd * vi.z;
+    }
+    // Jacobi -> inertial with a zero Jacobi star acceleration
+    eta = mtot;
+    sax = eta * real(0.); say = eta * real(0.); saz = eta * real(0.);
+    std::vector<V3> pa(no, V3{0., 0., 0.});
+    for (size_t kk = no; kk-- > 0;) {
+        const Particle& q = s.p[o[kk]];
+        if (q.gr.kind != POSI_EFFECT_ORBITING) continue;
+        real ei = real(1.) / eta;
+        sax = (sax - q.mass * ja[kk].x) * ei;
+        say = (say - q.mass * ja[kk].y) * ei;
+        saz = (saz - q.mass * ja[kk].z) * ei;
+        pa[kk].x = ja[kk].x + sax; pa[kk].y = ja[kk].y + say; pa[kk].z = ja[kk].z + saz;
+        eta -= q.mass;
+        sax *= eta; say *= eta; saz *= eta;
+    }
+    real mi = real(1.) / eta;
+    for (size_t k = 0; k < no; ++k) {
+        Particle& q = s.p[o[k]];
+        if (q.gr.kind == POSI_EFFECT_ORBITING) q.gr.out_acc = pa[k];
+    }
+    h.gr.out_acc = V3{sax * mi, say * mi, saz * mi};
+}
+
+// :702-898 -- every pair of bodies, the host first then the others in index
+// order; the constant part once, the acceleration-dependent part iterated.
+// The convergence test keeps the reference's form: a component's relative
+// change is taken only where |a| < 1e-30, otherwise the previous value stays.
+static void gr_newhall1983(Sim& s, int ignore) {
+    std::vector<int> ord{s.host};
+    for (int i : others(s)) ord.push_back(i);
+    const size_t N = ord.size();
+    V3 ha;
+    std::vector<V3> na;
+    gr_newtonian_accelerations(s, ignore, ha, na);
+    std::vector<V3> an(N);
+    an[0] = ha;
+    for (size_t k = 1; k < N; ++k) an[k] = na[k - 1];
+    auto P = [&](size_t t) -> const Particle& { return s.p[ord[t]]; };
+    auto on = [&](size_t t) { return P(t).gr.kind != POSI_EFFECT_DISABLED; };
+    std::vector<std::vector<real>> rs(N, std::vector<real>(N, real(0.)));
+    std::vector<std::vector<V3>> drs(N, std::vector<V3>(N, V3{0., 0., 0.}));
+    for (size_t i = 0; i < N; ++i)
+        for (size_t j = 0; j < N; ++j) {
+            if (j == i || !(on(i) || on(j))) continue;
+            drs[i][j] = V3{P(i).r.x - P(j).r.x, P(i).r.y - P(j).r.y, P(i).r.z - P(j).r.z};
+            rs[i][j] = rsqrt_(powi(drs[i][j].x, 2) + powi(drs[i][j].y, 2) + powi(drs[i][j].z, 2));
+        }
+    std::vector<V3> ac(N, V3{0., 0., 0.});
+    for (size_t i = 0; i < N; ++i) {
+        const Particle& pi = P(i);
+        real cx = 0., cy = 0., cz = 0.;
+        for (size_t j = 0; j < N; ++j) {
+            if (j == i || !(on(i) || on(j))) continue;
+            const Particle& pj = P(j);
+            real dxij = drs[i][j].x, dyij = drs[i][j].y, dzij = drs[i][j].z;
+            real rij2 = powi(rs[i][j], 2);
+            real rij3 = rij2 * rs[i][j];
+            real a1 = 0.;
+            for (size_t k = 0; k < N; ++k)
+                if (k != i) a1 += (real(4.) / SPEED_OF_LIGHT_2) * G * P(k).mass / rs[i][k];
+            real a2 = 0.;
+            for (size_t l = 0; l < N; ++l)
+                if (l != j) a2 += (real(1.) / SPEED_OF_LIGHT_2) * G * P(l).mass / rs[l][j];
+            real vi2 = powi(pi.v.x, 2) + powi(pi.v.y, 2) + powi(pi.v.z, 2);
+            real a3 = -vi2 / SPEED_OF_LIGHT_2;
+            real vj2 = powi(pj.v.x, 2) + powi(pj.v.y, 2) + powi(pj.v.z, 2);
+            real a4 = real(-2.) * vj2 / SPEED_OF_LIGHT_2;
+            real a5 = (real(4.) / SPEED_OF_LIGHT_2) * (pi.v.x * pj.v.x + pi.v.y * pj.v.y + pi.v.z * pj.v.z);
+            real a6_0 = dxij * pj.v.x + dyij * pj.v.y + dzij * pj.v.z;
+            real a6 = (real(3.) / (real(2.) * SPEED_OF_LIGHT_2)) * powi(a6_0, 2) / rij2;
+            real f1 = a1 + a2 + a3 + a4 + a5 + a6;
+            cx += G * pj.mass * dxij * f1 / rij3;
+            cy += G * pj.mass * dyij * f1 / rij3;
+            cz += G * pj.mass * dzij * f1 / rij3;
+            real dvx = pi.v.x - pj.v.x, dvy = pi.v.y - pj.v.y, dvz = pi.v.z - pj.v.z;
+            real f2 = dxij * (real(4.) * pi.v.x - real(3.) * pj.v.x) + dyij * (real(4.) * pi.v.y - real(3.) * pj.v.y) +
+                      dzij * (real(4.) * pi.v.z - real(3.) * pj.v.z);
+            cx += G * pj.mass * f2 * dvx / rij3 / SPEED_OF_LIGHT_2;
+            cy += G * pj.mass * f2 * dvy / rij3 / SPEED_OF_LIGHT_2;
+            cz += G * pj.mass * f2 * dvz / rij3 / SPEED_OF_LIGHT_2;
+        }
+        ac[i] = V3{cx, cy, cz};
+    }
+    std::vector<V3> anew(N, V3{0., 0., 0.}), aold(N);
+    const real dev_limit = 1.0e-30;
+    for (int it = 0; it < 10; ++it) {
+        aold = anew;
+        for (size_t i = 0; i < N; ++i) {
+            real nx = 0., ny = 0., nz = 0.;
+            for (size_t j = 0; j < N; ++j) {
+                if (j == i || !(on(i) || on(j))) continue;
+                const Particle& pj = P(j);
+                real dxij = drs[i][j].x, dyij = drs[i][j].y, dzij = drs[i][j].z;
+                real rij = rs[i][j];
+                real rij2 = powi(rij, 2);
+                real rij3 = rij2 * rij;
+                real sx_ = an[j].x + aold[j].x, sy_ = an[j].y + aold[j].y, sz_ = an[j].z + aold[j].z;
+                real dot = dxij * sx_ + dyij * sy_ + dzij * sz_;
+                nx += (G * pj.mass * dxij / rij3) * dot / (real(2.) * SPEED_OF_LIGHT_2) +
+                      (real(7.) / (real(2.) * SPEED_OF_LIGHT_2)) * G * pj.mass * sx_ / rij;
+                ny += (G * pj.mass * dyij / rij3) * dot / (real(2.) * SPEED_OF_LIGHT_2) +
+                      (real(7.) / (real(2.) * SPEED_OF_LIGHT_2)) * G * pj.mass * sy_ / rij;
+                nz += (G * pj.mass * dzij / rij3) * dot / (real(2.) * SPEED_OF_LIGHT_2) +
+                      (real(7.) / (real(2.) * SPEED_OF_LIGHT_2)) * G * pj.mass * sz_ / rij;
+            }
+            anew[i] = V3{ac[i].x + nx, ac[i].y + ny, ac[i].z + nz};
+        }
+        real maxdev = 0., dx = 0., dy = 0., dz = 0.;
+        for (size_t i = 0; i < N; ++i) {
+            if (!on(i)) continue;
+            if (rabs(anew[i].x) < dev_limit) dx = rabs(anew[i].x - aold[i].x) / anew[i].x;
+            if (rabs(anew[i].y) < dev_limit) dy = rabs(anew[i].y - aold[i].y) / anew[i].y;
+            if (rabs(anew[i].z) < dev_limit) dz = rabs(anew[i].z - aold[i].z) / anew[i].z;
+            if (dx > maxdev) maxdev = dx;
+            if (dy > maxdev) maxdev = dy;
+            if (dz > maxdev) maxdev = dz;
+        }
+        if (maxdev < dev_limit) break;
+    }
+    for (size_t k = 1; k < N; ++k) {
+        Particle& q = s.p[ord[k]];
+        if (q.gr.kind == POSI_EFFECT_ORBITING) q.gr.out_acc = anew[k];
+    }
+    s.p[s.host].gr.out_acc = anew[0];
+}
+
 // src/particles/universe.rs:580-614
 static void calculate_dangular_momentum_dt(Sim& s) {
     for (int i = 0; i < s.n; ++i) {
@@ -883,7 +1105,7 @@ static void add_additional_acceleration_corrections(Sim& s) {
 }
 
 // src/particles/universe.rs:428-538
-static void calculate_additional_effects(Sim& s, real t, bool evolution, bool dl, bool acc) {
+static void calculate_additional_effects(Sim& s, real t, bool evolution, bool dl, bool acc, int ignore) {
     initialize(s, dl, acc);
     calculate_spin_and_evolving_quantities(s, t, evolution);
     if (s.fatal()) return;
@@ -903,13 +1125,19 @@ static void calculate_additional_effects(Sim& s, real t, bool evolution, bool dl
     }
     if (acc && s.gr) {
         if (s.p[s.host].gr.kind == POSI_EFFECT_CENTRAL) {
-            gr_first_order(s);
-            gr_second_order(s);
-            gr_spin_orbit(s);
+            if (s.gr_impl == POSI_GR_ANDERSON1975) {
+                gr_anderson1975(s, ignore);
+            } else if (s.gr_impl == POSI_GR_NEWHALL1983) {
+                gr_newhall1983(s, ignore);
+            } else {
+                gr_first_order(s);
+                gr_second_order(s);
+                gr_spin_orbit(s);
+            }
         }
     }
     if (dl) {
-        if (s.tides || s.flat || s.gr) calculate_dangular_momentum_dt(s);
+        if (s.tides || s.flat || (s.gr && s.gr_impl == POSI_GR_KIDDER1995)) calculate_dangular_momentum_dt(s);
     }
     if (acc) add_additional_acceleration_corrections(s);
 }
@@ -948,7 +1176,7 @@ static void integrate_velocity_dependent_forces(Sim& s, real dt, bool spin, bool
         iters = it + 1;
         pv = fv; pL = fL;
         inertial_to_heliocentric(s);
-        calculate_additional_effects(s, s.t, evolution && it == 0, spin, true);
+        calculate_additional_effects(s, s.t, evolution && it == 0, spin, true, s.coords == POSI_JACOBI ? 1 : 2);
         if (s.fatal()) return;
         for (int i = 0; i < n; ++i) {
             const Particle& q = s.p[i];
@@ -1491,7 +1719,8 @@ static int iterate(Sim& s, bool* recovery_trigger) {
         s.n_hist += 1;
     }
     const int ignore = (s.coords == POSI_JACOBI) ? 1 : 2;
-    const bool spin = s.tides || s.flat || s.evolution || s.gr;
+    // whfast.rs:270-274: GR adds a spin torque only in Kidder1995
+    const bool spin = s.tides || s.flat || s.evolution || (s.gr && s.gr_impl == POSI_GR_KIDDER1995);
     integrate_velocity_dependent_forces(s, s.half_dt, spin, true);
     if (s.fatal()) return POSI_ERR_PHYSICS;
     // part 1: :469-479
@@ -1528,6 +1757,7 @@ static void load(Sim& s, int64_t nmax, const int64_t* si, const double* sf, cons
     s.tides = si[POSI_SI_TIDES] != 0;
     s.flat = si[POSI_SI_FLAT] != 0;
     s.gr = si[POSI_SI_GR] != 0;
+    s.gr_impl = (int)si[POSI_SI_GR_IMPL];
     s.evolution = si[POSI_SI_EVOLUTION] != 0;
     s.iteration = si[POSI_SI_ITERATION];
     s.n_hist = si[POSI_SI_N_HIST];
@@ -1692,7 +1922,8 @@ int oracle_run(int op, int64_t n_sys, int64_t nmax, int64_t* sys_i64, double* sy
                 orc::gravity_calculate_acceleration(s, arg);
             } else if (op == ORACLE_ADDITIONAL_EFFECTS) {
                 orc::inertial_to_heliocentric(s);
-                orc::calculate_additional_effects(s, t_arg, (arg & 1) != 0, (arg & 2) != 0, (arg & 4) != 0);
+                orc::calculate_additional_effects(s, t_arg, (arg & 1) != 0, (arg & 2) != 0, (arg & 4) != 0,
+                                                  s.coords == POSI_JACOBI ? 1 : 2);
             } else if (op == ORACLE_INITIALIZE) {
                 rc = orc::initialize_physical_values(s);
             }

@@ -125,14 +125,19 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
     const bool evo = boolean(c, ce, "evolution");
     if (disk || wind) c.fail(POSI_ERR_UNSUPPORTED, "disk and wind effects are outside this path");
     const json::Value* gri = req(c, u, "general_relativity_implementation");
-    if (gr && gri && !(gri->is_string() && gri->text == "Kidder1995"))
-        c.fail(POSI_ERR_UNSUPPORTED, "general relativity other than Kidder1995");
+    int gr_code = POSI_GR_KIDDER1995;
+    std::string gr_name = gri && gri->is_string() ? gri->text : std::string();
+    if (gr_name == "Anderson1975") gr_code = POSI_GR_ANDERSON1975;
+    else if (gr_name == "Newhall1983") gr_code = POSI_GR_NEWHALL1983;
+    else if (gr && gr_name != "Kidder1995") c.fail(POSI_ERR_UNSUPPORTED, "general relativity implementation " + gr_name);
     const json::Value* hosts = req(c, u, "hosts");
     const json::Value* hidx = req(c, hosts, "index");
     const int64_t host = (int64_t)num(c, hidx, "most_massive");
     if (tides && (int64_t)num(c, hidx, "tides") != host) c.fail(POSI_ERR_UNSUPPORTED, "tidal host is not the most massive body");
     if (flat && (int64_t)num(c, hidx, "rotational_flattening") != host)
         c.fail(POSI_ERR_UNSUPPORTED, "flattening host is not the most massive body");
+    if (gr && (int64_t)num(c, hidx, "general_relativity") != host)
+        c.fail(POSI_ERR_UNSUPPORTED, "general-relativity host is not the most massive body");
     if (c.code != POSI_OK) { err = c.err; return c.code; }
     if (host < 0 || host >= n) { err = "host index out of range"; return POSI_ERR_PARSE; }
 
@@ -158,6 +163,7 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
     out.si[POSI_SI_TIDES] = tides;
     out.si[POSI_SI_FLAT] = flat;
     out.si[POSI_SI_GR] = gr;
+    out.si[POSI_SI_GR_IMPL] = gr_code;
     out.si[POSI_SI_EVOLUTION] = evo;
     out.si[POSI_SI_ITERATION] = (int64_t)num(c, &doc, "current_iteration");
     out.si[POSI_SI_N_HIST] = (int64_t)num(c, &doc, "n_historic_snapshots");
@@ -197,8 +203,8 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
         const int fk = effect_kind(c, req(c, flat_v, "effect"), "OblateSpheroid", &fparams);
         const int gk = effect_kind(c, req(c, gr_v, "effect"), nullptr, &gparams, &gr_impl);
         if (c.code != POSI_OK) { err = c.err; return c.code; }
-        if (gr && gk == POSI_EFFECT_CENTRAL && gr_impl != "Kidder1995")
-            c.fail(POSI_ERR_UNSUPPORTED, "general relativity other than Kidder1995");
+        if (gr && gk == POSI_EFFECT_CENTRAL && gr_impl != gr_name)
+            c.fail(POSI_ERR_UNSUPPORTED, "general-relativity host " + gr_impl + " differs from the universe's " + gr_name);
         if (tides && b != host && tk != POSI_EFFECT_ORBITING)
             c.fail(POSI_ERR_UNSUPPORTED, "tides on with a non-orbiting body (the reference's host torque is NaN)");
         if (tides && b == host && tk != POSI_EFFECT_CENTRAL) c.fail(POSI_ERR_UNSUPPORTED, "tidal host is not a central body");

@@ -171,6 +171,8 @@ struct Sys {
     // uniform per group
     int s, n, host, coords, lane;
     bool tides, flat, gr, evo, spin_on;
+    int gr_impl;     // posi_gr_impl; grk(): Kidder1995, the per-planet formulation
+    __device__ __forceinline__ bool grk() const { return gr && gr_impl == POSI_GR_KIDDER1995; }
     unsigned mask;
     double dt, half_dt, t, time_limit, last_hist, hist_period, last_rec, rec_period;
     int64_t iteration, n_hist, tw, status, fail_step, fail_pair, mid_iters;
@@ -253,7 +255,9 @@ struct Sys {
         flat = D.si[POSI_SI_FLAT * ns + s] != 0;
         gr = D.si[POSI_SI_GR * ns + s] != 0;
         evo = D.si[POSI_SI_EVOLUTION * ns + s] != 0;
-        spin_on = tides || flat || evo || gr;
+        gr_impl = (int)D.si[POSI_SI_GR_IMPL * ns + s];
+        // whfast.rs:270-274: GR adds a spin torque only in Kidder1995
+        spin_on = tides || flat || evo || grk();
         iteration = D.si[POSI_SI_ITERATION * ns + s];
         n_hist = D.si[POSI_SI_N_HIST * ns + s];
         tw = D.si[POSI_SI_TIMESTEP_WARNING * ns + s];
@@ -591,7 +595,7 @@ struct Sys {
             P(PC_COFS) = -6. * cfs * id5;
             P(PC_COFP) = -6. * cfp * id5;
         }
-        if (gr && b.gk == POSI_EFFECT_ORBITING) {
+        if (grk() && b.gk == POSI_EFFECT_ORBITING) {
             // src/effects/general_relativity.rs:98, :187-298, :300-456
             const double mgs = hmg + b.mg;
             const double imgs = 1. / mgs;
@@ -666,7 +670,7 @@ struct Sys {
             P(PC_N3D5) = -3. / powi<5>(d);
             P(PC_F15D7) = 15. / powi<7>(d);
         }
-        if (gr && b.gk == POSI_EFFECT_ORBITING) {
+        if (grk() && b.gk == POSI_EFFECT_ORBITING) {
             // src/effects/general_relativity.rs:98, :187-298, :300-456
             const double f = hmg * b.mg / powi<2>(hmg + b.mg);
             const double mgs = hmg + b.mg;
@@ -706,6 +710,281 @@ struct Sys {
         }
     }
 #endif
+
+
+    // ------------------------------------------------------------------
+    // General relativity after REBOUNDx gr.c (src/effects/general_relativity.rs
+    // :461-898): Anderson1975 (a central body, in Jacobi coordinates) and
+    // Newhall1983 (every pair of bodies).  Every lane publishes its body in
+    // the exchange slots and evaluates its own output; the sequential parts
+    // (Jacobi recurrences, the host's sums, the convergence test) are run by
+    // every lane over the shared slots in the reference's order, so that all
+    // lanes agree and the arithmetic is the reference's.  g: this body's GR
+    // acceleration (the host's included); bodies outside the effect get zero.
+    // ------------------------------------------------------------------
+    enum { GX_R = 0, GX_V = 3, GX_A = 6, GX_M = 9, GX_K = 10, GX_W = 11, GX_O = 14, GX_END = 17 };
+    static_assert(GX_END <= kXS, "exchange slots");
+
+    __device__ void gr_nbody(double g[3]) {
+        const int ignore = coords == POSI_JACOBI ? 1 : 2;   // WHFastOne / WHFastTwo
+        sync();
+        if (has) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { X(GX_R + k, lane) = b.r[k]; X(GX_V + k, lane) = b.v[k]; }
+            X(GX_M, lane) = b.m;
+            X(GX_K, lane) = (double)b.gk;
+        }
+        // :661-697 the gravity accelerations plus the host terms the
+        // integrator ignored: host inertial position minus the body's
+        // heliocentric (GR) position
+        const int np = ignore == 1 ? 1 : n - 1;
+        const int rank = lane < host ? lane : lane - 1;   // position among the other bodies
+        double na[3] = {b.a[0], b.a[1], b.a[2]};
+        if (planet() && rank < np) {
+            const double dx = card[HC_PX] - P(PC_X), dy = card[HC_PY] - P(PC_Y), dz = card[HC_PZ] - P(PC_Z);
+            const double r2 = powi<2>(dx) + powi<2>(dy) + powi<2>(dz);
+            const double r = sqrt(r2);
+            const double prefac = kG / (r2 * r);
+            const double pms = prefac * card[HC_M];
+            const double pmp = prefac * b.m;
+            na[0] += pms * dx; na[1] += pms * dy; na[2] += pms * dz;
+            X(GX_W + 0, lane) = pmp * dx; X(GX_W + 1, lane) = pmp * dy; X(GX_W + 2, lane) = pmp * dz;
+        }
+        sync();
+        if (is_host) {
+            for (int j = 0, rk = 0; j < n; ++j) {
+                if (j == host) continue;
+                if (rk++ >= np) break;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) na[k] -= X(GX_W + k, j);
+            }
+        }
+        sync();
+        if (has) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) X(GX_A + k, lane) = na[k];
+        }
+        sync();
+        g[0] = g[1] = g[2] = 0.;
+        if (gr_impl == POSI_GR_ANDERSON1975) gr_anderson1975(g);
+        else gr_newhall1983(g);
+    }
+
+    __device__ __forceinline__ bool gr_orbiting(int j) const { return X(GX_K, j) == (double)POSI_EFFECT_ORBITING; }
+
+    // :461-535 with the Jacobi transforms :537-634
+    __device__ void gr_anderson1975(double g[3]) {
+        const double m0 = X(GX_M, host);
+        double eta = m0;
+        double sr[3], sv[3], sa[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            sr[k] = eta * X(GX_R + k, host);
+            sv[k] = eta * X(GX_V + k, host);
+            sa[k] = eta * X(GX_A + k, host);
+        }
+        double jp[3] = {0., 0., 0.}, jv[3] = {0., 0., 0.}, ja[3] = {0., 0., 0.};
+        for (int j = 0; j < n; ++j) {
+            if (j == host || !gr_orbiting(j)) continue;
+            const double mj = X(GX_M, j);
+            const double ei = 1. / eta;
+            eta += mj;
+            const double pme = eta * ei;
+            double p[3], v[3], a[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                p[k] = X(GX_R + k, j) - sr[k] * ei;
+                v[k] = X(GX_V + k, j) - sv[k] * ei;
+                a[k] = X(GX_A + k, j) - sa[k] * ei;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                sr[k] = sr[k] * pme + mj * p[k];
+                sv[k] = sv[k] * pme + mj * v[k];
+                sa[k] = sa[k] * pme + mj * a[k];
+            }
+            if (j == lane) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) { jp[k] = p[k]; jv[k] = v[k]; ja[k] = a[k]; }
+            }
+        }
+        const double mtot = eta;
+        const bool own = planet() && b.gk == POSI_EFFECT_ORBITING;
+        if (own) {
+            const double mu = card[HC_MG];
+            double vi[3] = {jv[0], jv[1], jv[2]};
+            double vi2 = powi<2>(jv[0]) + powi<2>(jv[1]) + powi<2>(jv[2]);
+            const double ri = sqrt(powi<2>(jp[0]) + powi<2>(jp[1]) + powi<2>(jp[2]));
+            double fa = (0.5 * vi2 + 3. * mu / ri) / kC2;
+            for (int q = 0; q < 10; ++q) {
+                const double o0 = vi[0], o1 = vi[1], o2 = vi[2];
+                vi[0] = jv[0] / (1. - fa);
+                vi[1] = jv[1] / (1. - fa);
+                vi[2] = jv[2] / (1. - fa);
+                vi2 = vi[0] * vi[0] + vi[1] * vi[1] + vi[2] * vi[2];
+                fa = (0.5 * vi2 + 3. * mu / ri) / kC2;
+                const double dvx = vi[0] - o0, dvy = vi[1] - o1, dvz = vi[2] - o2;
+                if ((dvx * dvx + dvy * dvy + dvz * dvz) / vi2 < kDBL_EPSILON_2) break;
+            }
+            const double fb = (mu / ri - 1.5 * vi2) * mu / (ri * ri * ri) / kC2;
+            const double rdotrdot = jp[0] * jv[0] + jp[1] * jv[1] + jp[2] * jv[2];
+            const double vd0 = ja[0] + fb * jp[0], vd1 = ja[1] + fb * jp[1], vd2 = ja[2] + fb * jp[2];
+            const double vdotvdot = vi[0] * vd0 + vi[1] * vd1 + vi[2] * vd2;
+            const double fd = (vdotvdot - 3. * mu / (ri * ri * ri) * rdotrdot) / kC2;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) ja[k] = fb * (1. - fa) * jp[k] - fa * ja[k] - fd * vi[k];
+        }
+        sync();
+        if (own) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) X(GX_W + k, lane) = ja[k];
+        }
+        sync();
+        // Jacobi -> inertial, the Jacobi star acceleration zero
+        eta = mtot;
+        double s2[3] = {eta * 0., eta * 0., eta * 0.};
+        for (int j = n - 1; j >= 0; --j) {
+            if (j == host || !gr_orbiting(j)) continue;
+            const double mj = X(GX_M, j);
+            const double ei = 1. / eta;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) s2[k] = (s2[k] - mj * X(GX_W + k, j)) * ei;
+            if (j == lane) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) g[k] = X(GX_W + k, j) + s2[k];
+            }
+            eta -= mj;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) s2[k] *= eta;
+        }
+        if (is_host) {
+            const double mi = 1. / eta;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) g[k] = s2[k] * mi;
+        }
+    }
+
+    // :702-898: reference order of bodies is the host, then the others in
+    // index order.  rs between two bodies exists only where one of them is in
+    // the effect (zero otherwise, as in the reference).
+    __device__ __forceinline__ int gr_ord(int t) const { return t == 0 ? host : (t - 1 < host ? t - 1 : t); }
+    __device__ __forceinline__ bool gr_on(int j) const { return X(GX_K, j) != (double)POSI_EFFECT_DISABLED; }
+    __device__ __forceinline__ double gr_dist(int a, int c, double d[3]) const {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) d[k] = X(GX_R + k, a) - X(GX_R + k, c);
+        return sqrt(powi<2>(d[0]) + powi<2>(d[1]) + powi<2>(d[2]));
+    }
+    __device__ __forceinline__ double gr_rs(int a, int c) const {
+        if (a == c || !(gr_on(a) || gr_on(c))) return 0.;
+        double d[3];
+        return gr_dist(a, c, d);
+    }
+
+    __device__ void gr_newhall1983(double g[3]) {
+        const int i = lane;
+        double ac[3] = {0., 0., 0.};
+        if (has) {
+            const double vix = X(GX_V + 0, i), viy = X(GX_V + 1, i), viz = X(GX_V + 2, i);
+            for (int tj = 0; tj < n; ++tj) {
+                const int j = gr_ord(tj);
+                if (j == i || !(gr_on(i) || gr_on(j))) continue;
+                double d[3];
+                const double rij = gr_dist(i, j, d);
+                const double dxij = d[0], dyij = d[1], dzij = d[2];
+                const double rij2 = powi<2>(rij);
+                const double rij3 = rij2 * rij;
+                double a1 = 0.;
+                for (int tk = 0; tk < n; ++tk) {
+                    const int k = gr_ord(tk);
+                    if (k != i) a1 += (4. / kC2) * kG * X(GX_M, k) / gr_rs(i, k);
+                }
+                double a2 = 0.;
+                for (int tl = 0; tl < n; ++tl) {
+                    const int l = gr_ord(tl);
+                    if (l != j) a2 += (1. / kC2) * kG * X(GX_M, l) / gr_rs(l, j);
+                }
+                const double vjx = X(GX_V + 0, j), vjy = X(GX_V + 1, j), vjz = X(GX_V + 2, j);
+                const double vi2 = powi<2>(vix) + powi<2>(viy) + powi<2>(viz);
+                const double a3 = -vi2 / kC2;
+                const double vj2 = powi<2>(vjx) + powi<2>(vjy) + powi<2>(vjz);
+                const double a4 = -2. * vj2 / kC2;
+                const double a5 = (4. / kC2) * (vix * vjx + viy * vjy + viz * vjz);
+                const double a6_0 = dxij * vjx + dyij * vjy + dzij * vjz;
+                const double a6 = (3. / (2. * kC2)) * powi<2>(a6_0) / rij2;
+                const double f1 = a1 + a2 + a3 + a4 + a5 + a6;
+                const double gm = kG * X(GX_M, j);
+                ac[0] += gm * dxij * f1 / rij3;
+                ac[1] += gm * dyij * f1 / rij3;
+                ac[2] += gm * dzij * f1 / rij3;
+                const double dvx = vix - vjx, dvy = viy - vjy, dvz = viz - vjz;
+                const double f2 = dxij * (4. * vix - 3. * vjx) + dyij * (4. * viy - 3. * vjy) + dzij * (4. * viz - 3. * vjz);
+                ac[0] += gm * f2 * dvx / rij3 / kC2;
+                ac[1] += gm * f2 * dvy / rij3 / kC2;
+                ac[2] += gm * f2 * dvz / rij3 / kC2;
+            }
+        }
+        // substitution loop: a_new in GX_W, a_old in GX_O
+        sync();
+        if (has) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) X(GX_W + k, lane) = 0.;
+        }
+        double an[3] = {0., 0., 0.};
+        for (int it = 0; it < 10; ++it) {
+            sync();
+            if (has) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) X(GX_O + k, lane) = X(GX_W + k, lane);
+            }
+            sync();
+            if (has) {
+                double nc[3] = {0., 0., 0.};
+                for (int tj = 0; tj < n; ++tj) {
+                    const int j = gr_ord(tj);
+                    if (j == i || !(gr_on(i) || gr_on(j))) continue;
+                    double d[3];
+                    const double rij = gr_dist(i, j, d);
+                    const double dxij = d[0], dyij = d[1], dzij = d[2];
+                    const double rij2 = powi<2>(rij);
+                    const double rij3 = rij2 * rij;
+                    const double sx = X(GX_A + 0, j) + X(GX_O + 0, j);
+                    const double sy = X(GX_A + 1, j) + X(GX_O + 1, j);
+                    const double sz = X(GX_A + 2, j) + X(GX_O + 2, j);
+                    const double dot = dxij * sx + dyij * sy + dzij * sz;
+                    const double gm = kG * X(GX_M, j);
+                    nc[0] += (gm * dxij / rij3) * dot / (2. * kC2) + (7. / (2. * kC2)) * kG * X(GX_M, j) * sx / rij;
+                    nc[1] += (gm * dyij / rij3) * dot / (2. * kC2) + (7. / (2. * kC2)) * kG * X(GX_M, j) * sy / rij;
+                    nc[2] += (gm * dzij / rij3) * dot / (2. * kC2) + (7. / (2. * kC2)) * kG * X(GX_M, j) * sz / rij;
+                }
+#pragma unroll
+                for (int k = 0; k < 3; ++k) an[k] = ac[k] + nc[k];
+            }
+            sync();
+            if (has) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) X(GX_W + k, lane) = an[k];
+            }
+            sync();
+            // the reference's test: a component's relative change counts only
+            // where |a| < 1e-30, otherwise the previous value stays
+            double maxdev = 0., dx = 0., dy = 0., dz = 0.;
+            for (int t = 0; t < n; ++t) {
+                const int j = gr_ord(t);
+                if (!gr_on(j)) continue;
+                const double nx = X(GX_W + 0, j), ny = X(GX_W + 1, j), nz = X(GX_W + 2, j);
+                if (fabs(nx) < 1.0e-30) dx = fabs(nx - X(GX_O + 0, j)) / nx;
+                if (fabs(ny) < 1.0e-30) dy = fabs(ny - X(GX_O + 1, j)) / ny;
+                if (fabs(nz) < 1.0e-30) dz = fabs(nz - X(GX_O + 2, j)) / nz;
+                if (dx > maxdev) maxdev = dx;
+                if (dy > maxdev) maxdev = dy;
+                if (dz > maxdev) maxdev = dz;
+            }
+            if (maxdev < 1.0e-30) break;
+        }
+        if (is_host || (planet() && b.gk == POSI_EFFECT_ORBITING)) {
+            g[0] = an[0]; g[1] = an[1]; g[2] = an[2];
+        }
+    }
 
     // ------------------------------------------------------------------
     // One evaluation of src/particles/universe.rs:428-538 (after
@@ -755,7 +1034,7 @@ struct Sys {
         const double hnsv2 = card[HC_NSV2];
         double at[3] = {0., 0., 0.}, af[3] = {0., 0., 0.}, ag[3] = {0., 0., 0.};
         double dt_[3] = {0., 0., 0.}, df[3] = {0., 0., 0.}, dg[3] = {0., 0., 0.};
-        const int ncol = gr ? 24 : (flat ? 12 : (tides ? 6 : 0));
+        const int ncol = grk() ? 24 : (flat ? 12 : (tides ? 6 : 0));
         if (planet()) {
             for (int k = 0; k < ncol; ++k) X(k, lane) = 0.;
         }
@@ -813,7 +1092,7 @@ struct Sys {
                 col[10 * G] = -1.0 * (ofs * (z * hS0 - x * hS2));
                 col[11 * G] = -1.0 * (ofs * (x * hS1 - y * hS0));
             }
-            if (gr && b.gk == POSI_EFFECT_ORBITING) {
+            if (grk() && b.gk == POSI_EFFECT_ORBITING) {
                 const double vr2 = powi<2>(vr);
                 // first order (general_relativity.rs:187-239)
                 const double radial1 = P(PC_A) * (P(PC_B) * nv2 - P(PC_C) - P(PC_DD) * vr2);
@@ -921,16 +1200,17 @@ struct Sys {
                     P(PC_TD_VR) = 0.;
                 }
                 if (flat) { af[k] = -1.0 * factor2 * sums[6 + k]; df[k] = sums[9 + k]; }
-                if (gr) {
+                if (grk()) {
                     ag[k] = -1.0 * sums[12 + k] + -1.0 * sums[15 + k] + -1.0 * sums[18 + k];
                     dg[k] = sums[21 + k];
                 }
             }
         }
+        if (gr && !grk()) gr_nbody(ag);
         sync();
         if (has) {
             // universe.rs:580-614 (disabled effects contribute their zero outputs)
-            if (spin_on && (tides || flat || gr)) {
+            if (spin_on && (tides || flat || grk())) {
 #pragma unroll
                 for (int k = 0; k < 3; ++k) b.dl[k] = dt_[k] + df[k] + dg[k] + 0.;
             }
@@ -1025,7 +1305,7 @@ struct Sys {
                 th1 -= ofs * (z * hS0 - x * hS2);
                 th2 -= ofs * (x * hS1 - y * hS0);
             }
-            if (gr && b.gk == POSI_EFFECT_ORBITING) {
+            if (grk() && b.gk == POSI_EFFECT_ORBITING) {
                 const double vr2 = vr * vr;
                 // first order: ortho / |v| = E v_r
                 const double radial1 = P(PC_A) * (P(PC_B) * nv2 - P(PC_C) - P(PC_DD) * vr2);
@@ -1078,13 +1358,19 @@ struct Sys {
             X(0, lane) = mr * aa0; X(1, lane) = mr * aa1; X(2, lane) = mr * aa2;
             X(3, lane) = th0; X(4, lane) = th1; X(5, lane) = th2;
         }
-        if (tides || flat || gr) colfold(0, 6, nullptr, true, false);
-        if (is_host && (tides || flat || gr)) {
+        if (tides || flat || grk()) colfold(0, 6, nullptr, true, false);
+        if (is_host && (tides || flat || grk())) {
             aa0 = -sums[0]; aa1 = -sums[1]; aa2 = -sums[2];
             dl0 = sums[3]; dl1 = sums[4]; dl2 = sums[5];
         }
+        if (gr && !grk()) {
+            // Anderson1975 / Newhall1983: every body's GR acceleration, the host's included
+            double g[3] = {0., 0., 0.};
+            gr_nbody(g);
+            aa0 += g[0]; aa1 += g[1]; aa2 += g[2];
+        }
         if (has) {
-            if (spin_on && (tides || flat || gr)) { b.dl[0] = dl0; b.dl[1] = dl1; b.dl[2] = dl2; }
+            if (spin_on && (tides || flat || grk())) { b.dl[0] = dl0; b.dl[1] = dl1; b.dl[2] = dl2; }
             b.aa[0] = aa0; b.aa[1] = aa1; b.aa[2] = aa2;
         }
     }

@@ -39,6 +39,11 @@ EFFECT_DISABLED = 0
 EFFECT_CENTRAL = 1
 EFFECT_ORBITING = 2
 
+# posi_gr_impl
+GR_KIDDER1995 = 0
+GR_ANDERSON1975 = 1
+GR_NEWHALL1983 = 2
+
 # posi_evolution
 EVO_NON_EVOLVING = 0
 EVO_LECONTE2011 = 1
@@ -48,7 +53,7 @@ EVO_LECONTE_CHABRIER2013 = 4
 
 # posi_sys_i64_field
 (SI_N, SI_HOST, SI_COORDS, SI_TIDES, SI_FLAT, SI_GR, SI_EVOLUTION, SI_ITERATION, SI_N_HIST,
- SI_TIMESTEP_WARNING, SI_STATUS, SI_FAIL_STEP, SI_FAIL_PAIR, SI_LAST_MIDPOINT_ITERS, SI_COUNT) = range(15)
+ SI_TIMESTEP_WARNING, SI_STATUS, SI_FAIL_STEP, SI_FAIL_PAIR, SI_LAST_MIDPOINT_ITERS, SI_GR_IMPL, SI_COUNT) = range(16)
 
 # posi_sys_f64_field
 (SF_DT, SF_HALF_DT, SF_TIME, SF_TIME_LIMIT, SF_LAST_HIST, SF_HIST_PERIOD, SF_LAST_REC, SF_REC_PERIOD,

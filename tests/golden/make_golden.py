@@ -10,7 +10,7 @@ tests/common/universe.rs:36-44; tests/data/<case>/particle_<i>.json = final
 inertial position/velocity/acceleration after integrating to the time limit,
 tests/common/universe.rs:18-34) it writes <case>/case.json.gz and
 <case>/particles.json (the particle files merged).  Cases outside the path
-(wind, disk, IAS15, LeapFrog, Anderson/Newhall GR, dynamical tides) are skipped.
+(wind, disk, IAS15, LeapFrog, dynamical tides) are skipped.
 The Python-generated twins (posidonius/tests/data/<case>/case.json) of the three
 integrator cases, which the reference steps once and compares
 (tests/test_integrator.rs:58-70), are stored as <case>/python_case.json.gz.
@@ -31,6 +31,8 @@ IN_SCOPE = [
     "test_flattening-disabled_flattening",
     "test_general_relativity-kidder1995",
     "test_general_relativity-none",
+    "test_general_relativity-anderson1975",
+    "test_general_relativity-newhall1983",
     "test_evolution-brown_dwarf_non_evolving",
     "test_evolution-m_dwarf_non_evolving",
     "test_evolution-brown_dwarf_leconte2011",

@@ -50,7 +50,8 @@ def test_plain_path_exact_matches_golden_and_oracle(tmp_path, name):
 
 
 @pytest.mark.parametrize("name", ["test_integrator-whfast_jacobi", "test_integrator-whfast_democraticheliocentric",
-                                  "test_integrator-whfast_whds", "test_evolution-brown_dwarf_non_evolving"])
+                                  "test_integrator-whfast_whds", "test_evolution-brown_dwarf_non_evolving",
+                                  "test_general_relativity-anderson1975", "test_general_relativity-newhall1983"])
 def test_plain_path_fast_within_tolerance(tmp_path, name):
     w = pg.restore_snapshot(_json(tmp_path, name), mode=pg.FAST)
     w.run()
@@ -83,7 +84,8 @@ def test_fast_one_step_relative_error():
     assert max_rel_error(b.get_state(), ref) <= FAST_TOL_STEP
 
 
-@pytest.mark.parametrize("name", ["test_integrator-whfast_jacobi", "test_integrator-whfast_whds"])
+@pytest.mark.parametrize("name", ["test_integrator-whfast_jacobi", "test_integrator-whfast_whds",
+                                  "test_general_relativity-anderson1975", "test_general_relativity-newhall1983"])
 def test_universe_methods_exact(tmp_path, name):
     case = load_case(case_dict(name))
     w = pg.WHFast.from_json(_json(tmp_path, name), mode=pg.EXACT)
