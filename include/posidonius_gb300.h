@@ -32,7 +32,7 @@ enum posi_status {
     POSI_ERR_ARG = -1,           /* bad argument / null pointer */
     POSI_ERR_IO = -2,            /* file missing or unreadable (src/integrator/output.rs:178-203) */
     POSI_ERR_PARSE = -3,         /* malformed JSON case */
-    POSI_ERR_UNSUPPORTED = -4,   /* case uses an effect outside this path (Kaula, creep, disk, wind,
+    POSI_ERR_UNSUPPORTED = -4,   /* case uses an effect outside this path (Kaula, creep, disk,
                                     dynamic tides, non-WHFast integrator, ...) */
     POSI_ERR_CUDA = -5,          /* CUDA runtime error or no device */
     POSI_ERR_PHYSICS = -6,       /* a system hit a reference panic (see posi_system_status) */
@@ -89,6 +89,7 @@ enum posi_sys_i64_field {
     POSI_SI_FAIL_PAIR,           /* i*1024 + j of the offending pair */
     POSI_SI_LAST_MIDPOINT_ITERS, /* midpoint iterations of the last half kick */
     POSI_SI_GR_IMPL,             /* Universe.general_relativity_implementation (posi_gr_impl) */
+    POSI_SI_WIND,                /* ConsiderEffects.wind */
     POSI_SI_COUNT
 };
 
@@ -113,6 +114,7 @@ enum posi_body_i64_field {
     POSI_BI_EVO_OFFSET,          /* offset of this body's tables in `tables` */
     POSI_BI_EVO_LEN,             /* rows per table (time, radius, rg2, love: 4*len doubles) */
     POSI_BI_EVO_LEFT,            /* Evolver.left_index */
+    POSI_BI_WIND_KIND,           /* WindEffect: 1 Interaction, 0 Disabled */
     POSI_BI_COUNT
 };
 
@@ -140,6 +142,9 @@ enum posi_body_f64_field {
     POSI_BF_TD_PX, POSI_BF_TD_PY, POSI_BF_TD_PZ,
     POSI_BF_TD_VX, POSI_BF_TD_VY, POSI_BF_TD_VZ,
     POSI_BF_TD_LX, POSI_BF_TD_LY, POSI_BF_TD_LZ,
+    /* wind (src/effects/wind.rs:6-15): input k_factor, rotation_saturation,
+     * internal rotation_saturation_2 */
+    POSI_BF_WIND_K, POSI_BF_WIND_RSAT, POSI_BF_WIND_RSAT2,
     POSI_BF_COUNT
 };
 

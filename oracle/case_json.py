@@ -68,8 +68,8 @@ def load_case(path_or_dict):
     u = d["universe"]
     n = int(u["n_particles"])
     ce = u["consider_effects"]
-    if ce["disk"] or ce["wind"]:
-        raise Unsupported("disk/wind effects")
+    if ce["disk"]:
+        raise Unsupported("disk effect")
     gr_impl = u["general_relativity_implementation"]
     gr_codes = {"Kidder1995": L.GR_KIDDER1995, "Anderson1975": L.GR_ANDERSON1975, "Newhall1983": L.GR_NEWHALL1983}
     if ce["general_relativity"] and gr_impl not in gr_codes:
@@ -92,6 +92,7 @@ def load_case(path_or_dict):
     si[L.SI_FLAT] = int(ce["rotational_flattening"])
     si[L.SI_GR] = int(ce["general_relativity"])
     si[L.SI_GR_IMPL] = gr_codes.get(gr_impl, L.GR_KIDDER1995)
+    si[L.SI_WIND] = int(ce["wind"])
     si[L.SI_EVOLUTION] = int(ce["evolution"])
     si[L.SI_ITERATION] = int(d["current_iteration"])
     si[L.SI_N_HIST] = int(d["n_historic_snapshots"])
@@ -114,9 +115,16 @@ def load_case(path_or_dict):
         tk, tparams = _effect(p["tides"]["effect"], "ConstantTimeLag")
         fk, fparams = _effect(p["rotational_flattening"]["effect"], "OblateSpheroid")
         gk, gimpl = _effect(p["general_relativity"]["effect"], None)
-        if p["wind"]["effect"] != "Disabled" or p["disk"]["effect"] != "Disabled":
-            if ce["wind"] or ce["disk"]:
-                raise Unsupported("wind/disk body")
+        wk = 1 if p["wind"]["effect"] == "Interaction" else 0
+        if p["wind"]["effect"] not in ("Interaction", "Disabled"):
+            raise Unsupported(f"wind {p['wind']['effect']}")
+        # the wind torque output is summed into dL/dt whatever the flags
+        # (src/particles/universe.rs:589-591); only interacting bodies under
+        # the wind effect recompute it, the others must hold zero
+        if not (ce["wind"] and wk):
+            o = p["wind"]["parameters"]["output"]["dangular_momentum_dt"]
+            if o["x"] != 0.0 or o["y"] != 0.0 or o["z"] != 0.0:
+                raise Unsupported("stale wind torque output")
         if gk == L.EFFECT_CENTRAL and gimpl != gr_impl and ce["general_relativity"]:
             raise Unsupported(f"general relativity host {gimpl} differs from the universe's {gr_impl}")
         if ce["tides"] and b != host and tk != L.EFFECT_ORBITING:
@@ -138,6 +146,7 @@ def load_case(path_or_dict):
         bi[b, L.BI_TIDES_KIND] = tk
         bi[b, L.BI_FLAT_KIND] = fk
         bi[b, L.BI_GR_KIND] = gk
+        bi[b, L.BI_WIND_KIND] = wk
         evo_code = _evolution_code(p["evolution"])
         evo_ev = _evolution_code(ev["evolution"])
         if evo_code != evo_ev:
@@ -163,6 +172,9 @@ def load_case(path_or_dict):
         F[L.BF_RADIUS] = p["radius"]
         F[L.BF_RG2] = p["radius_of_gyration_2"]
         F[L.BF_MOI] = p["moment_of_inertia"]
+        F[L.BF_WIND_K] = p["wind"]["parameters"]["input"]["k_factor"]
+        F[L.BF_WIND_RSAT] = p["wind"]["parameters"]["input"]["rotation_saturation"]
+        F[L.BF_WIND_RSAT2] = p["wind"]["parameters"]["internal"]["rotation_saturation_2"]
         for k, key in enumerate(("x", "y", "z")):
             F[L.BF_PX + k] = p["inertial_position"][key]
             F[L.BF_VX + k] = p["inertial_velocity"][key]

@@ -110,6 +110,7 @@ static const double SPEED_OF_LIGHT = (2.99792458e8 / AU) * DAY;
 static const double SPEED_OF_LIGHT_2 = SPEED_OF_LIGHT * SPEED_OF_LIGHT;
 static const double G = G_SI / (AU * AU * AU) * M_SUN * (DAY * DAY);
 static const double K2 = G;
+static const double R_SUN = 6.957e8 / AU;
 static const double MAX_DISTANCE = 100.;
 static const double MAX_DISTANCE_2 = MAX_DISTANCE * MAX_DISTANCE;
 
@@ -156,7 +157,10 @@ struct Particle {
     Tides tides;
     Flat flat;
     GR gr;
-    V3 wind_dldt{0., 0., 0.};   // wind is disabled on this path: always zero
+    // src/effects/wind.rs:6-40
+    int wind_kind = 0;          // 1: Interaction
+    real wind_k = 0., wind_rsat = 0., wind_rsat2 = 0.;
+    V3 wind_dldt{0., 0., 0.};
     int evolution = POSI_EVO_NON_EVOLVING;
 };
 // src/effects/evolution.rs:20-28
@@ -175,7 +179,7 @@ struct AltCoords {
 // src/integrator/whfast.rs:99-120 + src/particles/universe.rs:50-63
 struct Sim {
     int n = 0, host = 0, coords = POSI_JACOBI;
-    bool tides = false, flat = false, gr = false, evolution = false;
+    bool tides = false, flat = false, gr = false, evolution = false, wind = false;
     int gr_impl = POSI_GR_KIDDER1995;   // Universe.general_relativity_implementation
     real dt = 0., half_dt = 0., t = 0., time_limit = 0.;
     real last_hist = -1., hist_period = 0., last_rec = -1., rec_period = 0.;
@@ -389,6 +393,11 @@ static void inertial_to_heliocentric(Sim& s) {
 // src/effects/rotational_flattening/common.rs:93-120,148-161,
 // src/effects/general_relativity.rs:86-109,153-174
 static void initialize(Sim& s, bool dl, bool acc) {
+    // src/effects/wind.rs:62-70
+    if (dl && s.wind) {
+        for (int i = 0; i < s.n; ++i)
+            if (s.p[i].wind_kind == 1) s.p[i].wind_dldt = V3{0., 0., 0.};
+    }
     const bool it = (dl && s.tides) || (acc && s.tides);
     const bool ifl = (dl && s.flat) || (acc && s.flat);
     const bool igr = (dl && s.gr && s.gr_impl == POSI_GR_KIDDER1995) || (acc && s.gr);
@@ -1084,6 +1093,19 @@ static void gr_newhall1983(Sim& s, int ignore) {
     s.p[s.host].gr.out_acc = anew[0];
 }
 
+// src/effects/wind.rs:72-91 (Bolmont & Mathis 2016 eq. 14)
+static void calculate_wind_factor(Sim& s) {
+    for (int i = 0; i < s.n; ++i) {
+        Particle& q = s.p[i];
+        if (q.wind_kind != 1) continue;
+        real threshold = rsqrt_(q.nsv2);
+        real w = threshold >= q.wind_rsat ? q.wind_rsat2 : q.nsv2;
+        q.wind_dldt.x = real(-1.) * q.wind_k * q.spin.x * w * rsqrt_(q.radius / R_SUN * real(1.) / q.mass);
+        q.wind_dldt.y = real(-1.) * q.wind_k * q.spin.y * w * rsqrt_(q.radius / R_SUN * real(1.) / q.mass);
+        q.wind_dldt.z = real(-1.) * q.wind_k * q.spin.z * w * rsqrt_(q.radius / R_SUN * real(1.) / q.mass);
+    }
+}
+
 // src/particles/universe.rs:580-614
 static void calculate_dangular_momentum_dt(Sim& s) {
     for (int i = 0; i < s.n; ++i) {
@@ -1109,6 +1131,7 @@ static void calculate_additional_effects(Sim& s, real t, bool evolution, bool dl
     initialize(s, dl, acc);
     calculate_spin_and_evolving_quantities(s, t, evolution);
     if (s.fatal()) return;
+    if (dl && s.wind) calculate_wind_factor(s);
     if (s.tides || s.flat) {
         if ((dl && (s.tides || s.flat)) || (acc && (s.tides || s.flat || s.gr))) {
             if (s.tides) tides_orthogonal(s);
@@ -1137,7 +1160,7 @@ static void calculate_additional_effects(Sim& s, real t, bool evolution, bool dl
         }
     }
     if (dl) {
-        if (s.tides || s.flat || (s.gr && s.gr_impl == POSI_GR_KIDDER1995)) calculate_dangular_momentum_dt(s);
+        if (s.tides || s.flat || (s.gr && s.gr_impl == POSI_GR_KIDDER1995) || s.wind) calculate_dangular_momentum_dt(s);
     }
     if (acc) add_additional_acceleration_corrections(s);
 }
@@ -1758,6 +1781,7 @@ static void load(Sim& s, int64_t nmax, const int64_t* si, const double* sf, cons
     s.flat = si[POSI_SI_FLAT] != 0;
     s.gr = si[POSI_SI_GR] != 0;
     s.gr_impl = (int)si[POSI_SI_GR_IMPL];
+    s.wind = si[POSI_SI_WIND] != 0;
     s.evolution = si[POSI_SI_EVOLUTION] != 0;
     s.iteration = si[POSI_SI_ITERATION];
     s.n_hist = si[POSI_SI_N_HIST];
@@ -1813,6 +1837,10 @@ static void load(Sim& s, int64_t nmax, const int64_t* si, const double* sf, cons
         q.flat.kind = (int)I[POSI_BI_FLAT_KIND];
         q.flat.love_number = F[POSI_BF_K2F];
         q.gr.kind = (int)I[POSI_BI_GR_KIND];
+        q.wind_kind = (int)I[POSI_BI_WIND_KIND];
+        q.wind_k = F[POSI_BF_WIND_K];
+        q.wind_rsat = F[POSI_BF_WIND_RSAT];
+        q.wind_rsat2 = F[POSI_BF_WIND_RSAT2];
         q.evolution = (int)I[POSI_BI_EVO_TYPE];
         Evolver& e = s.ev[b];
         e.type = q.evolution;

@@ -123,7 +123,7 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
     const bool disk = boolean(c, ce, "disk");
     const bool wind = boolean(c, ce, "wind");
     const bool evo = boolean(c, ce, "evolution");
-    if (disk || wind) c.fail(POSI_ERR_UNSUPPORTED, "disk and wind effects are outside this path");
+    if (disk) c.fail(POSI_ERR_UNSUPPORTED, "the disk effect is outside this path");
     const json::Value* gri = req(c, u, "general_relativity_implementation");
     int gr_code = POSI_GR_KIDDER1995;
     std::string gr_name = gri && gri->is_string() ? gri->text : std::string();
@@ -164,6 +164,7 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
     out.si[POSI_SI_FLAT] = flat;
     out.si[POSI_SI_GR] = gr;
     out.si[POSI_SI_GR_IMPL] = gr_code;
+    out.si[POSI_SI_WIND] = wind;
     out.si[POSI_SI_EVOLUTION] = evo;
     out.si[POSI_SI_ITERATION] = (int64_t)num(c, &doc, "current_iteration");
     out.si[POSI_SI_N_HIST] = (int64_t)num(c, &doc, "n_historic_snapshots");
@@ -221,6 +222,21 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
             c.fail(POSI_ERR_UNSUPPORTED, "stale flattening torque output");
         if ((!gr || (b != host && gk != POSI_EFFECT_ORBITING)) && !zero_axes(c, gout))
             c.fail(POSI_ERR_UNSUPPORTED, "stale general-relativity torque output");
+        // wind (src/effects/wind.rs): "Interaction" or "Disabled"; its torque
+        // output is summed whatever the flags (src/particles/universe.rs:589-591)
+        const json::Value* wind_v = req(c, &p, "wind");
+        const json::Value* weff = req(c, wind_v, "effect");
+        if (c.code != POSI_OK) { err = c.err; return c.code; }
+        int wk = 0;
+        if (weff->is_string() && weff->text == "Interaction") wk = 1;
+        else if (!(weff->is_string() && weff->text == "Disabled")) c.fail(POSI_ERR_UNSUPPORTED, "unknown wind effect");
+        const json::Value* wpar = req(c, wind_v, "parameters");
+        if (!(wind && wk) && !zero_axes(c, req(c, wpar, "output")))
+            c.fail(POSI_ERR_UNSUPPORTED, "stale wind torque output");
+        I[POSI_BI_WIND_KIND] = wk;
+        F[POSI_BF_WIND_K] = num(c, req(c, wpar, "input"), "k_factor");
+        F[POSI_BF_WIND_RSAT] = num(c, req(c, wpar, "input"), "rotation_saturation");
+        F[POSI_BF_WIND_RSAT2] = num(c, req(c, wpar, "internal"), "rotation_saturation_2");
         if (b == host) {
             double hv[3];
             axes(c, &p, "heliocentric_velocity", hv);

@@ -71,6 +71,7 @@ constexpr double kDBL_EPSILON_2 = 2.2204460492503131e-16 * 2.2204460492503131e-1
 constexpr double kMINUS_3K2 = -3.0 * kK2;
 constexpr double kFA = kG / kC2;
 constexpr double kTWO_PI = 2. * kPI;
+constexpr double kR_SUN = 6.957e8 / kAU;
 constexpr int kNMAX_QUART = 64;
 constexpr int kNMAX_NEWT = 32;
 constexpr int kMIDPOINT_MIN = 3;
@@ -161,6 +162,8 @@ struct Body {
     double aa[3], dl[3];
     double denergy, lag;
     int tk, fk, gk, evo;
+    int wk;                              // wind: 1 Interaction
+    double wind_k, wind_rsat, wind_rsat2;
     int64_t eoff, elen, eleft;
     // alternative (Jacobi / democratic-heliocentric / WHDS) coordinates
     double am, amg, ap[3], av[3], aacc[3];
@@ -170,7 +173,7 @@ template <int G>
 struct Sys {
     // uniform per group
     int s, n, host, coords, lane;
-    bool tides, flat, gr, evo, spin_on;
+    bool tides, flat, gr, evo, spin_on, wind;
     int gr_impl;     // posi_gr_impl; grk(): Kidder1995, the per-planet formulation
     __device__ __forceinline__ bool grk() const { return gr && gr_impl == POSI_GR_KIDDER1995; }
     unsigned mask;
@@ -254,6 +257,7 @@ struct Sys {
         tides = D.si[POSI_SI_TIDES * ns + s] != 0;
         flat = D.si[POSI_SI_FLAT * ns + s] != 0;
         gr = D.si[POSI_SI_GR * ns + s] != 0;
+        wind = D.si[POSI_SI_WIND * ns + s] != 0;
         evo = D.si[POSI_SI_EVOLUTION * ns + s] != 0;
         gr_impl = (int)D.si[POSI_SI_GR_IMPL * ns + s];
         // whfast.rs:270-274: GR adds a spin torque only in Kidder1995
@@ -316,6 +320,10 @@ struct Sys {
             b.tk = (int)I[POSI_BI_TIDES_KIND * st];
             b.fk = (int)I[POSI_BI_FLAT_KIND * st];
             b.gk = (int)I[POSI_BI_GR_KIND * st];
+            b.wk = (int)I[POSI_BI_WIND_KIND * st];
+            b.wind_k = F[POSI_BF_WIND_K * st];
+            b.wind_rsat = F[POSI_BF_WIND_RSAT * st];
+            b.wind_rsat2 = F[POSI_BF_WIND_RSAT2 * st];
             b.evo = (int)I[POSI_BI_EVO_TYPE * st];
             b.eoff = I[POSI_BI_EVO_OFFSET * st];
             b.elen = I[POSI_BI_EVO_LEN * st];
@@ -711,6 +719,17 @@ struct Sys {
     }
 #endif
 
+
+    // src/effects/wind.rs:72-91 (Bolmont & Mathis 2016 eq. 14): the spin-down
+    // torque of an interacting body, from the spin of this evaluation
+    __device__ void wind_torque(double w[3]) const {
+        w[0] = w[1] = w[2] = 0.;
+        if (!(wind && has && b.wk == 1)) return;
+        const double threshold = sqrt(b.nsv2);
+        const double ww = threshold >= b.wind_rsat ? b.wind_rsat2 : b.nsv2;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) w[k] = -1. * b.wind_k * b.S[k] * ww * sqrt(b.R / kR_SUN * 1. / b.m);
+    }
 
     // ------------------------------------------------------------------
     // General relativity after REBOUNDx gr.c (src/effects/general_relativity.rs
@@ -1210,9 +1229,11 @@ struct Sys {
         sync();
         if (has) {
             // universe.rs:580-614 (disabled effects contribute their zero outputs)
-            if (spin_on && (tides || flat || grk())) {
+            if (spin_on && (tides || flat || grk() || wind)) {
+                double dw[3];
+                wind_torque(dw);
 #pragma unroll
-                for (int k = 0; k < 3; ++k) b.dl[k] = dt_[k] + df[k] + dg[k] + 0.;
+                for (int k = 0; k < 3; ++k) b.dl[k] = dt_[k] + df[k] + dg[k] + dw[k];
             }
             // universe.rs:540-567
 #pragma unroll
@@ -1370,7 +1391,11 @@ struct Sys {
             aa0 += g[0]; aa1 += g[1]; aa2 += g[2];
         }
         if (has) {
-            if (spin_on && (tides || flat || grk())) { b.dl[0] = dl0; b.dl[1] = dl1; b.dl[2] = dl2; }
+            if (spin_on && (tides || flat || grk() || wind)) {
+                double dw[3];
+                wind_torque(dw);
+                b.dl[0] = dl0 + dw[0]; b.dl[1] = dl1 + dw[1]; b.dl[2] = dl2 + dw[2];
+            }
             b.aa[0] = aa0; b.aa[1] = aa1; b.aa[2] = aa2;
         }
     }

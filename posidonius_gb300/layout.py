@@ -53,15 +53,16 @@ EVO_LECONTE_CHABRIER2013 = 4
 
 # posi_sys_i64_field
 (SI_N, SI_HOST, SI_COORDS, SI_TIDES, SI_FLAT, SI_GR, SI_EVOLUTION, SI_ITERATION, SI_N_HIST,
- SI_TIMESTEP_WARNING, SI_STATUS, SI_FAIL_STEP, SI_FAIL_PAIR, SI_LAST_MIDPOINT_ITERS, SI_GR_IMPL, SI_COUNT) = range(16)
+ SI_TIMESTEP_WARNING, SI_STATUS, SI_FAIL_STEP, SI_FAIL_PAIR, SI_LAST_MIDPOINT_ITERS, SI_GR_IMPL, SI_WIND,
+ SI_COUNT) = range(17)
 
 # posi_sys_f64_field
 (SF_DT, SF_HALF_DT, SF_TIME, SF_TIME_LIMIT, SF_LAST_HIST, SF_HIST_PERIOD, SF_LAST_REC, SF_REC_PERIOD,
  SF_INITIAL_TIME, SF_COUNT) = range(10)
 
 # posi_body_i64_field
-(BI_TIDES_KIND, BI_FLAT_KIND, BI_GR_KIND, BI_EVO_TYPE, BI_EVO_OFFSET, BI_EVO_LEN, BI_EVO_LEFT,
- BI_COUNT) = range(8)
+(BI_TIDES_KIND, BI_FLAT_KIND, BI_GR_KIND, BI_EVO_TYPE, BI_EVO_OFFSET, BI_EVO_LEN, BI_EVO_LEFT, BI_WIND_KIND,
+ BI_COUNT) = range(9)
 
 # posi_body_f64_field
 (BF_MASS, BF_MASS_G, BF_RADIUS, BF_RG2, BF_MOI,
@@ -72,7 +73,7 @@ EVO_LECONTE_CHABRIER2013 = 4
  BF_ADDAX, BF_ADDAY, BF_ADDAZ, BF_DLX, BF_DLY, BF_DLZ,
  BF_DENERGY_DT, BF_LAG_ANGLE,
  BF_TD_DIST, BF_TD_VR, BF_TD_ORTHO, BF_TD_DPM, BF_TD_PX, BF_TD_PY, BF_TD_PZ, BF_TD_VX, BF_TD_VY, BF_TD_VZ,
- BF_TD_LX, BF_TD_LY, BF_TD_LZ, BF_COUNT) = range(52)
+ BF_TD_LX, BF_TD_LY, BF_TD_LZ, BF_WIND_K, BF_WIND_RSAT, BF_WIND_RSAT2, BF_COUNT) = range(55)
 
 MAX_BODIES = 32
 

@@ -10,7 +10,7 @@ tests/common/universe.rs:36-44; tests/data/<case>/particle_<i>.json = final
 inertial position/velocity/acceleration after integrating to the time limit,
 tests/common/universe.rs:18-34) it writes <case>/case.json.gz and
 <case>/particles.json (the particle files merged).  Cases outside the path
-(wind, disk, IAS15, LeapFrog, dynamical tides) are skipped.
+(disk, IAS15, LeapFrog, dynamical tides) are skipped.
 The Python-generated twins (posidonius/tests/data/<case>/case.json) of the three
 integrator cases, which the reference steps once and compares
 (tests/test_integrator.rs:58-70), are stored as <case>/python_case.json.gz.
@@ -40,6 +40,12 @@ IN_SCOPE = [
     "test_evolution-m_dwarf_baraffe2015",
     "test_star_types-brown_dwarf",
     "test_star_types-m_dwarf",
+    # wind (the solar-like star)
+    "test_evolution-solar_like_non_evolving",
+    "test_evolution-solar_like_baraffe1998",
+    "test_evolution-solar_like_baraffe2015",
+    "test_star_types-solar_like",
+    "test_disk-disabled_disk",
 ]
 
 
