@@ -292,6 +292,12 @@ int posi_large_iterate_tangent(posi_large* L, int64_t n_steps, int32_t n_dirs, c
     }
     // the kernels carry 1, 2 or 4 directions; padding directions are zero
     const int nt = n_dirs == 1 ? 1 : n_dirs == 2 ? 2 : 4;
+    // one warp per direction next to the primal warp of every 32 bodies
+    if (L->per_block != 32) {
+        posi::set_last_error("tangents need at most 32 bodies per block (" +
+                             std::to_string((int64_t)L->grid * 32) + " bodies on this device)");
+        return POSI_ERR_UNSUPPORTED;
+    }
     int32_t sb[posi_many::kMaxTangents], sp[posi_many::kMaxTangents];
     for (int d = 0; d < posi_many::kMaxTangents; ++d) {
         sb[d] = d < n_dirs ? seed_body[d] : -1;

@@ -238,36 +238,41 @@ __device__ __forceinline__ void load_state(const LDev& D, int64_t i, BodyState& 
     }
 }
 
-// Tangents of one body's state along NT directions ([component][direction]).
-template <int NT>
-struct Tangents {
-    static constexpr int A = NT > 0 ? NT : 1;
-    double r[3][A], v[3][A], L[3][A], S[3][A];
+// Tangent of one body's state along one direction.
+struct Tangent {
+    double r[3], v[3], L[3], S[3];
 };
 
 // One thread of the engine.  NT = 0: the plain integration.  NT > 0: the
-// same integration carrying the forward-mode derivatives (tangents) of every
+// same integration carrying forward-mode derivatives (tangents) of every
 // body's state along NT directions -- the derivative of the step map applied
 // to the incoming tangents, plus the unit rate of change of the seeded
 // parameter (a body's dissipation factor or Love number) where the seeded
-// body's tides enter.  The primal arithmetic is the plain engine's, in the
-// same order; the midpoint convergence tests only the primal values.  The
+// body's tides enter.
+//
+// Roles: a body is held by 1 + NT threads, one warp each.  Role 0 (dir = -1)
+// integrates the primal state and alone contributes the primal sums; role
+// r >= 1 repeats the primal arithmetic (identical, so every role holds the
+// same primal state) and carries the tangent of direction dir = r - 1.  A
+// warp's FP64 instructions cost the same whatever its active lanes, so
+// spreading the directions over warps keeps each warp's work at one primal
+// plus one tangent.  The midpoint convergence tests only primal values; the
 // compensated (Kahan) error terms of the kick carry no tangent.
 template <int NT>
 struct Large {
-    static constexpr int A = NT > 0 ? NT : 1;   // extent of the direction index
     static constexpr int NS = slots_for(NT);    // value slots of the reductions
     const LDev& D;
     int64_t n, i;
     int host;
+    int dir;                // tangent direction of this thread, -1: the primal role
     bool has, is_host, planet;
     bool tides, flat, gr;
     double dt, half_dt, t, time_limit, last_hist, hist_period;
     BodyConst c, hc;        // own and host constants
     BodyState b, h;         // own and host state (host: redundant copy)
     double a[3];            // gravity acceleration (own)
-    Tangents<NT> T, HT;     // own and host tangents (host: redundant copy)
-    double da[3][A];        // tangent of the gravity acceleration
+    Tangent T, HT;          // own and host tangents (host: redundant copy)
+    double da[3];           // tangent of the gravity acceleration
     double* shm;
     double Mtot, inv_M, inv_hm;
     bool warp_bodies;       // this thread's warp owns at least one body
@@ -278,10 +283,14 @@ struct Large {
     __device__ __forceinline__ bool tides_on() const { return tides && c.tk == POSI_EFFECT_ORBITING; }
     __device__ __forceinline__ bool flat_on() const { return flat && c.fk == POSI_EFFECT_ORBITING; }
     __device__ __forceinline__ bool gr_on() const { return gr && c.gk == POSI_EFFECT_ORBITING; }
+    __device__ __forceinline__ bool tan_on() const { return NT > 0 && dir >= 0; }
+    __device__ __forceinline__ bool primal_role() const { return dir < 0; }
+    // reduction slot of tangent component q of this thread's direction
+    __device__ __forceinline__ int tslot(int base, int q) const { return base + q * NT + dir; }
 
-    // unit rate of the seeded parameter of direction k for body j
-    __device__ __forceinline__ double seed(int k, int param, int64_t j) const {
-        return (D.seed_body[k] == j && D.seed_param[k] == param) ? 1. : 0.;
+    // unit rate of this direction's seeded parameter for body j
+    __device__ __forceinline__ double seed(int param, int64_t j) const {
+        return (D.seed_body[dir] == j && D.seed_param[dir] == param) ? 1. : 0.;
     }
 
     __device__ static void spin_of(const BodyConst& k, const double L[3], double S[3]) {
@@ -293,50 +302,43 @@ struct Large {
         }
     }
 
-    __device__ static void dspin_of(const BodyConst& k, const double (&dL)[3][A], double (&dS)[3][A]) {
+    __device__ static void dspin_of(const BodyConst& k, const double dL[3], double dS[3]) {
         const double im = k.moi != 0. ? 1. / k.moi : 0.;
-        for (int q = 0; q < 3; ++q)
-            for (int d = 0; d < NT; ++d) dS[q][d] = dL[q][d] * im;
+        for (int q = 0; q < 3; ++q) dS[q] = dL[q] * im;
     }
 
     struct Pre {
         double t[adj_tides_NPRE], f[adj_flat_NPRE], g[adj_gr_NPRE];
     };
-    struct DPre {
-        double t[adj_tides_NPRE * A], f[adj_flat_NPRE * A], g[adj_gr_NPRE * A];
-    };
 
     // ---- implicit midpoint (src/integrator/whfast.rs:322-466) ----
     // With cm != nullptr the last convergence reduction also carries the sums
     // of m r and m v over all bodies at the final velocities (cm[0..5]), and
-    // their tangents (dcm).
-    __device__ bool midpoint(double hdt, double* cm, double (*dcm)[A]) {
+    // their tangents (tcm).
+    __device__ bool midpoint(double hdt, double* cm, double* tcm) {
         double x[3] = {0., 0., 0.};
-        Pre pr;
-        DPre dpr;
+        Pre pr, dpr;
+        const bool tn = tan_on();
         if (planet) {
             for (int q = 0; q < 3; ++q) x[q] = b.r[q] - h.r[q];
             if (tides_on()) adj_tides_pre(x[0], x[1], x[2], c.sig, hc.sig, c.k2, hc.k2, c.R, hc.R, hc.m, c.m, pr.t);
             if (flat_on()) adj_flat_pre(x[0], x[1], x[2], c.R, hc.R, hc.k2f, hc.m, c.k2f, c.m, pr.f);
             if (gr_on()) adj_gr_pre(x[0], x[1], x[2], hc.m, hc.mg, hc.moi, c.m, c.mg, c.moi, pr.g);
-            if constexpr (NT > 0) {
-                // din[p * NT + d]: tangent d of pre input p (x, y, z, sig_p, sig_h, k2_p, k2_h)
-                double din[7 * A], scratch[adj_gr_NPRE];
-                for (int q = 0; q < 3; ++q)
-                    for (int d = 0; d < NT; ++d) din[q * NT + d] = T.r[q][d] - HT.r[q][d];
-                for (int d = 0; d < NT; ++d) {
-                    din[3 * NT + d] = seed(d, SEED_SIGMA, i);
-                    din[4 * NT + d] = seed(d, SEED_SIGMA, host);
-                    din[5 * NT + d] = seed(d, SEED_K2, i);
-                    din[6 * NT + d] = seed(d, SEED_K2, host);
-                }
+            if (tn) {
+                // tangents of the pre inputs (x, y, z, sig_p, sig_h, k2_p, k2_h)
+                double din[7], scratch[adj_gr_NPRE];
+                for (int q = 0; q < 3; ++q) din[q] = T.r[q] - HT.r[q];
+                din[3] = seed(SEED_SIGMA, i);
+                din[4] = seed(SEED_SIGMA, host);
+                din[5] = seed(SEED_K2, i);
+                din[6] = seed(SEED_K2, host);
                 if (tides_on())
-                    adj_tides_pre_jvp<NT>(x[0], x[1], x[2], c.sig, hc.sig, c.k2, hc.k2, c.R, hc.R, hc.m, c.m, din,
-                                          scratch, dpr.t);
+                    adj_tides_pre_jvp<1>(x[0], x[1], x[2], c.sig, hc.sig, c.k2, hc.k2, c.R, hc.R, hc.m, c.m, din, scratch,
+                                         dpr.t);
                 if (flat_on())
-                    adj_flat_pre_jvp<NT>(x[0], x[1], x[2], c.R, hc.R, hc.k2f, hc.m, c.k2f, c.m, din, scratch, dpr.f);
+                    adj_flat_pre_jvp<1>(x[0], x[1], x[2], c.R, hc.R, hc.k2f, hc.m, c.k2f, c.m, din, scratch, dpr.f);
                 if (gr_on())
-                    adj_gr_pre_jvp<NT>(x[0], x[1], x[2], hc.m, hc.mg, hc.moi, c.m, c.mg, c.moi, din, scratch, dpr.g);
+                    adj_gr_pre_jvp<1>(x[0], x[1], x[2], hc.m, hc.mg, hc.moi, c.m, c.mg, c.moi, din, scratch, dpr.g);
             }
         }
         const double mr = planet ? c.m / hc.m : 0.;
@@ -350,36 +352,28 @@ struct Large {
         }
         // tangents: the originals stay in T / HT (v, L); the previous spin is
         // T.S / HT.S, advanced with the primal's Sp
-        double tvf[3][A], tLf[3][A], tSc[3][A], thvf[3][A], thLf[3][A], thSc[3][A];
-        if constexpr (NT > 0) {
-            for (int q = 0; q < 3; ++q)
-                for (int d = 0; d < NT; ++d) {
-                    tvf[q][d] = T.v[q][d]; tLf[q][d] = T.L[q][d];
-                    thvf[q][d] = HT.v[q][d]; thLf[q][d] = HT.L[q][d];
-                    tSc[q][d] = T.S[q][d]; thSc[q][d] = HT.S[q][d];
-                }
+        double tvf[3], tLf[3], tSc[3], thvf[3], thLf[3], thSc[3];
+        for (int q = 0; q < 3; ++q) {
+            tvf[q] = T.v[q]; tLf[q] = T.L[q]; thvf[q] = HT.v[q]; thLf[q] = HT.L[q];
+            tSc[q] = T.S[q]; thSc[q] = HT.S[q];
         }
         for (int it = 0; it < kMIDPOINT_MAX; ++it) {
             for (int q = 0; q < 3; ++q) { pv[q] = vf[q]; pL[q] = Lf[q]; hpv[q] = hvf[q]; hpL[q] = hLf[q]; }
             if (has) {
                 spin_of(c, Lc, Sc);
                 spin_of(hc, hLc, hSc);
-                if constexpr (NT > 0) {
-                    double tLc[3][A], thLc[3][A];
-                    for (int q = 0; q < 3; ++q)
-                        for (int d = 0; d < NT; ++d) {
-                            tLc[q][d] = 0.5 * (T.L[q][d] + tLf[q][d]);
-                            thLc[q][d] = 0.5 * (HT.L[q][d] + thLf[q][d]);
-                        }
+                if (tn) {
+                    double tLc[3], thLc[3];
+                    for (int q = 0; q < 3; ++q) {
+                        tLc[q] = 0.5 * (T.L[q] + tLf[q]);
+                        thLc[q] = 0.5 * (HT.L[q] + thLf[q]);
+                    }
                     dspin_of(c, tLc, tSc);
                     dspin_of(hc, thLc, thSc);
                 }
             }
             double aa[3] = {0., 0., 0.}, dl[3] = {0., 0., 0.}, th[3] = {0., 0., 0.};
-            double taa[3][A], tdl[3][A], tth[3][A];
-            if constexpr (NT > 0)
-                for (int q = 0; q < 3; ++q)
-                    for (int d = 0; d < NT; ++d) taa[q][d] = tdl[q][d] = tth[q][d] = 0.;
+            double taa[3] = {0., 0., 0.}, tdl[3] = {0., 0., 0.}, tth[3] = {0., 0., 0.};
             if (planet) {
                 const double h0 = vc[0] - hvc[0], h1 = vc[1] - hvc[1], h2 = vc[2] - hvc[2];
                 double out[9];
@@ -398,53 +392,47 @@ struct Large {
                                 hSp[0], hSp[1], hSp[2], hc.m, hc.mg, hc.moi, c.m, c.mg, c.moi, out);
                     for (int q = 0; q < 3; ++q) { aa[q] += out[q]; dl[q] += out[3 + q]; th[q] += out[6 + q]; }
                 }
-                if constexpr (NT > 0) {
-                    // din[p * NT + d] over the 15 iteration inputs: relative
-                    // velocity, spin, host spin, previous spin, previous host spin
-                    double din[15 * A], dout[9 * A];
-                    for (int q = 0; q < 3; ++q)
-                        for (int d = 0; d < NT; ++d) {
-                            din[q * NT + d] = 0.5 * (T.v[q][d] + tvf[q][d]) - 0.5 * (HT.v[q][d] + thvf[q][d]);
-                            din[(3 + q) * NT + d] = tSc[q][d];
-                            din[(6 + q) * NT + d] = thSc[q][d];
-                            din[(9 + q) * NT + d] = T.S[q][d];
-                            din[(12 + q) * NT + d] = HT.S[q][d];
-                        }
+                if (tn) {
+                    // tangents of the 15 iteration inputs: relative velocity,
+                    // spin, host spin, previous spin, previous host spin
+                    double din[15], dout[9];
+                    for (int q = 0; q < 3; ++q) {
+                        din[q] = 0.5 * (T.v[q] + tvf[q]) - 0.5 * (HT.v[q] + thvf[q]);
+                        din[3 + q] = tSc[q];
+                        din[6 + q] = thSc[q];
+                        din[9 + q] = T.S[q];
+                        din[12 + q] = HT.S[q];
+                    }
                     auto add = [&]() {
-                        for (int q = 0; q < 3; ++q)
-                            for (int d = 0; d < NT; ++d) {
-                                taa[q][d] += dout[q * NT + d];
-                                tdl[q][d] += dout[(3 + q) * NT + d];
-                                tth[q][d] += dout[(6 + q) * NT + d];
-                            }
+                        for (int q = 0; q < 3; ++q) { taa[q] += dout[q]; tdl[q] += dout[3 + q]; tth[q] += dout[6 + q]; }
                     };
                     if (tides_on()) {
-                        adj_tides_iter_jvp<NT>(pr.t, dpr.t, h0, h1, h2, Sc[0], Sc[1], Sc[2], hSc[0], hSc[1], hSc[2], Sp[0],
-                                               Sp[1], Sp[2], hSp[0], hSp[1], hSp[2], c.R, hc.R, hc.m, c.m, din, out, dout);
+                        adj_tides_iter_jvp<1>(pr.t, dpr.t, h0, h1, h2, Sc[0], Sc[1], Sc[2], hSc[0], hSc[1], hSc[2], Sp[0],
+                                              Sp[1], Sp[2], hSp[0], hSp[1], hSp[2], c.R, hc.R, hc.m, c.m, din, out, dout);
                         add();
                     }
                     if (flat_on()) {
-                        adj_flat_iter_jvp<NT>(pr.f, dpr.f, h0, h1, h2, Sc[0], Sc[1], Sc[2], hSc[0], hSc[1], hSc[2], Sp[0],
-                                              Sp[1], Sp[2], hSp[0], hSp[1], hSp[2], c.R, hc.R, hc.k2f, hc.m, c.k2f, c.m,
-                                              din, out, dout);
+                        adj_flat_iter_jvp<1>(pr.f, dpr.f, h0, h1, h2, Sc[0], Sc[1], Sc[2], hSc[0], hSc[1], hSc[2], Sp[0],
+                                             Sp[1], Sp[2], hSp[0], hSp[1], hSp[2], c.R, hc.R, hc.k2f, hc.m, c.k2f, c.m,
+                                             din, out, dout);
                         add();
                     }
                     if (gr_on()) {
-                        adj_gr_iter_jvp<NT>(pr.g, dpr.g, h0, h1, h2, Sc[0], Sc[1], Sc[2], hSc[0], hSc[1], hSc[2], Sp[0],
-                                            Sp[1], Sp[2], hSp[0], hSp[1], hSp[2], hc.m, hc.mg, hc.moi, c.m, c.mg, c.moi,
-                                            din, out, dout);
+                        adj_gr_iter_jvp<1>(pr.g, dpr.g, h0, h1, h2, Sc[0], Sc[1], Sc[2], hSc[0], hSc[1], hSc[2], Sp[0],
+                                           Sp[1], Sp[2], hSp[0], hSp[1], hSp[2], hc.m, hc.mg, hc.moi, c.m, c.mg, c.moi,
+                                           din, out, dout);
                         add();
                     }
                 }
             }
             double vals[NS] = {};
-            for (int q = 0; q < 3; ++q) { vals[q] = mr * aa[q]; vals[3 + q] = th[q]; }
-            if constexpr (NT > 0)
-                for (int q = 0; q < 3; ++q)
-                    for (int d = 0; d < NT; ++d) {
-                        vals[6 + q * NT + d] = mr * taa[q][d];
-                        vals[6 + (3 + q) * NT + d] = tth[q][d];
-                    }
+            if (primal_role())
+                for (int q = 0; q < 3; ++q) { vals[q] = mr * aa[q]; vals[3 + q] = th[q]; }
+            if (tn)
+                for (int q = 0; q < 3; ++q) {
+                    vals[tslot(6, q)] = mr * taa[q];
+                    vals[tslot(6, 3 + q)] = tth[q];
+                }
             double tot[NS];
             if (!grid_reduce(D, vals, 6 + 6 * NT, tot, shm, warp_bodies, body_rows)) return false;
             // the host's outputs, computed by every thread
@@ -462,45 +450,40 @@ struct Large {
                 hdLc[q] = hdt * hdl[q] - h.eL[q];
                 hLf[q] = hL0[q] + hdLc[q];
             }
-            if constexpr (NT > 0) {
-                if (has)
-                    for (int q = 0; q < 3; ++q)
-                        for (int d = 0; d < NT; ++d) {
-                            const double thaa = -tot[6 + q * NT + d], thdl = tot[6 + (3 + q) * NT + d];
-                            if (is_host) { taa[q][d] = thaa; tdl[q][d] = thdl; }
-                            tvf[q][d] = T.v[q][d] + hdt * taa[q][d];
-                            tLf[q][d] = T.L[q][d] + hdt * tdl[q][d];
-                            thvf[q][d] = HT.v[q][d] + hdt * thaa;
-                            thLf[q][d] = HT.L[q][d] + hdt * thdl;
-                        }
-            }
+            if (tn && has)
+                for (int q = 0; q < 3; ++q) {
+                    const double thaa = -tot[tslot(6, q)], thdl = tot[tslot(6, 3 + q)];
+                    if (is_host) { taa[q] = thaa; tdl[q] = thdl; }
+                    tvf[q] = T.v[q] + hdt * taa[q];
+                    tLf[q] = T.L[q] + hdt * tdl[q];
+                    thvf[q] = HT.v[q] + hdt * thaa;
+                    thLf[q] = HT.L[q] + hdt * thdl;
+                }
             if (it >= kMIDPOINT_MIN - 1) {
                 double cv[NS] = {};
                 if (has) {
-                    for (int q = 0; q < 3; ++q) {
-                        cv[0] += (vf[q] - pv[q]) * (vf[q] - pv[q]);
-                        cv[1] += vf[q] * vf[q];
-                        cv[2] += (Lf[q] - pL[q]) * (Lf[q] - pL[q]);
-                        cv[3] += Lf[q] * Lf[q];
-                        cv[4 + q] = c.m * b.r[q];
-                        cv[7 + q] = c.m * vf[q];
-                    }
-                    if constexpr (NT > 0)
-                        if (cm)
-                            for (int q = 0; q < 3; ++q)
-                                for (int d = 0; d < NT; ++d) {
-                                    cv[10 + q * NT + d] = c.m * T.r[q][d];
-                                    cv[10 + (3 + q) * NT + d] = c.m * tvf[q][d];
-                                }
+                    if (primal_role())
+                        for (int q = 0; q < 3; ++q) {
+                            cv[0] += (vf[q] - pv[q]) * (vf[q] - pv[q]);
+                            cv[1] += vf[q] * vf[q];
+                            cv[2] += (Lf[q] - pL[q]) * (Lf[q] - pL[q]);
+                            cv[3] += Lf[q] * Lf[q];
+                            cv[4 + q] = c.m * b.r[q];
+                            cv[7 + q] = c.m * vf[q];
+                        }
+                    if (tn && cm)
+                        for (int q = 0; q < 3; ++q) {
+                            cv[tslot(10, q)] = c.m * T.r[q];
+                            cv[tslot(10, 3 + q)] = c.m * tvf[q];
+                        }
                 }
                 const int ns = cm ? 10 + 6 * NT : 4;
                 double s4[NS];
                 if (!grid_reduce(D, cv, ns, s4, shm, warp_bodies, body_rows)) return false;
                 if (cm) {
                     for (int q = 0; q < 6; ++q) cm[q] = s4[4 + q];
-                    if constexpr (NT > 0)
-                        for (int q = 0; q < 6; ++q)
-                            for (int d = 0; d < NT; ++d) dcm[q][d] = s4[10 + q * NT + d];
+                    if (tn)
+                        for (int q = 0; q < 6; ++q) tcm[q] = s4[tslot(10, q)];
                 }
                 if (s4[0] / s4[1] < kDBL_EPSILON_2 && (s4[3] == 0. || s4[2] / s4[3] < kDBL_EPSILON_2)) break;
             }
@@ -512,11 +495,8 @@ struct Large {
                 hLc[q] = 0.5 * (hL0[q] + hLf[q]);
                 hSp[q] = hSc[q];
             }
-            if constexpr (NT > 0) {
-                if (has)
-                    for (int q = 0; q < 3; ++q)
-                        for (int d = 0; d < NT; ++d) { T.S[q][d] = tSc[q][d]; HT.S[q][d] = thSc[q][d]; }
-            }
+            if (tn && has)
+                for (int q = 0; q < 3; ++q) { T.S[q] = tSc[q]; HT.S[q] = thSc[q]; }
         }
         if (!has) return true;
         for (int q = 0; q < 3; ++q) {
@@ -528,12 +508,11 @@ struct Large {
             h.eL[q] = (hLf[q] - hL0[q]) - hdLc[q];
         }
         if (is_host) b = h;
-        if constexpr (NT > 0) {
-            for (int q = 0; q < 3; ++q)
-                for (int d = 0; d < NT; ++d) {
-                    T.v[q][d] = tvf[q][d]; T.L[q][d] = tLf[q][d]; T.S[q][d] = tSc[q][d];
-                    HT.v[q][d] = thvf[q][d]; HT.L[q][d] = thLf[q][d]; HT.S[q][d] = thSc[q][d];
-                }
+        if (tn) {
+            for (int q = 0; q < 3; ++q) {
+                T.v[q] = tvf[q]; T.L[q] = tLf[q]; T.S[q] = tSc[q];
+                HT.v[q] = thvf[q]; HT.L[q] = thLf[q]; HT.S[q] = thSc[q];
+            }
             if (is_host) T = HT;
         }
         return true;
@@ -543,9 +522,13 @@ struct Large {
     // pos[] holds heliocentric positions published before the preceding
     // barrier (differences of heliocentric and of inertial positions agree);
     // the host sits at -shift (the jump moved every planet by +shift).  The
-    // tangent of the pair term -G m_j d / |d|^3 along dd is
-    // -G m_j (dd - 3 (d . dd) d / |d|^2) / |d|^3.
-    __device__ bool gravity(const double shift[3], const double (&tshift)[3][A]) {
+    // pair loop, spread over every thread of the grid, carries all NT
+    // tangent directions (positions published in dpos[]); the tangent of the
+    // pair term -G m_j d / |d|^3 along dd is
+    // -G m_j (dd - 3 (d . dd) d / |d|^2) / |d|^3.  tshift[d][q]: the
+    // tangents of the shift of every direction.
+    __device__ bool gravity(const double shift[3], const double (&tshift)[NT > 0 ? NT : 1][3]) {
+        constexpr int AN = NT > 0 ? NT : 1;
         const int64_t nn = n;
         constexpr int rows = 3 * (1 + NT);  // rows of one slice in gpart
         const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -555,11 +538,11 @@ struct Large {
             double xi, yi, zi;
             if (gi == host) { xi = -shift[0]; yi = -shift[1]; zi = -shift[2]; }
             else { xi = __ldcg(&D.pos[gi]); yi = __ldcg(&D.pos[nn + gi]); zi = __ldcg(&D.pos[2 * nn + gi]); }
-            double txi[3][A], tax[3][A];
+            double txi[3][AN], tax[3][AN];
             if constexpr (NT > 0)
                 for (int q = 0; q < 3; ++q)
                     for (int d = 0; d < NT; ++d) {
-                        txi[q][d] = gi == host ? -tshift[q][d] : __ldcg(&D.dpos[(d * 3 + q) * nn + gi]);
+                        txi[q][d] = gi == host ? -tshift[d][q] : __ldcg(&D.dpos[(d * 3 + q) * nn + gi]);
                         tax[q][d] = 0.;
                     }
             const double Ri = D.bf[POSI_BF_RADIUS * nn + gi];
@@ -612,20 +595,19 @@ struct Large {
                 for (int k = 0; k < D.nchunk; ++k) acc += __ldcg(&D.gpart[(k * rows + q) * nn + i]);
                 a[q] = acc;
             }
-            if constexpr (NT > 0)
-                for (int q = 0; q < 3; ++q)
-                    for (int d = 0; d < NT; ++d) {
-                        double acc = 0.;
-                        for (int k = 0; k < D.nchunk; ++k) acc += __ldcg(&D.gpart[(k * rows + 3 + q * NT + d) * nn + i]);
-                        da[q][d] = acc;
-                    }
+            if (tan_on())
+                for (int q = 0; q < 3; ++q) {
+                    double acc = 0.;
+                    for (int k = 0; k < D.nchunk; ++k) acc += __ldcg(&D.gpart[(k * rows + 3 + q * NT + dir) * nn + i]);
+                    da[q] = acc;
+                }
         }
         return true;
     }
 
-    // Kepler drift of a planet over half_dt, with the tangents (the implicit
+    // Kepler drift of a planet over half_dt, with the tangent (the implicit
     // derivative at the converged root).
-    __device__ void kepler(double x[3], double u[3], double (&tx)[3][A], double (&tu)[3][A]) {
+    __device__ void kepler(double x[3], double u[3], double tx[3], double tu[3]) {
         if (planet) {
             const KeplerScalars ks = kepler_scalars(hc.mg, x, u);
             bool ok = false;
@@ -633,24 +615,22 @@ struct Large {
             if (!ok) atomicOr(D.err, LE_KEPLER);
             double r1[3], v1[3];
             kepler_apply(hc.mg, half_dt, x, u, ks, X, r1, v1);
-            if constexpr (NT > 0)
-                for (int d = 0; d < NT; ++d) {
-                    const double e0[3] = {tx[0][d], tx[1][d], tx[2][d]}, f0[3] = {tu[0][d], tu[1][d], tu[2][d]};
-                    double e1[3], f1[3];
-                    kepler_jvp(hc.mg, half_dt, x, u, X, e0, f0, e1, f1);
-                    for (int q = 0; q < 3; ++q) { tx[q][d] = e1[q]; tu[q][d] = f1[q]; }
-                }
+            if (tan_on()) {
+                double e1[3], f1[3];
+                kepler_jvp(hc.mg, half_dt, x, u, X, tx, tu, e1, f1);
+                for (int q = 0; q < 3; ++q) { tx[q] = e1[q]; tu[q] = f1[q]; }
+            }
             for (int q = 0; q < 3; ++q) { x[q] = r1[q]; u[q] = v1[q]; }
         }
     }
 
     // inertial positions and velocities from the heliocentric x, barycentric
     // u, the barycentre (Rc, Vc) and the sums S[0..2] = sum_p m_p x_p,
-    // S[3..5] = sum_p m_p u_p (src/integrator/whfast.rs:1082-1155); tS[q][d]
-    // holds the tangents of S (the linear map applied to the tangents)
+    // S[3..5] = sum_p m_p u_p (src/integrator/whfast.rs:1082-1155); tS holds
+    // the tangents of S (the linear map applied to the tangents)
     __device__ void to_inertial(const double x[3], const double u[3], const double Rc[3], const double Vc[3],
-                                const double S[6], const double (&tx)[3][A], const double (&tu)[3][A],
-                                const double (&tRc)[3][A], const double (&tVc)[3][A], const double (&tS)[6][A]) {
+                                const double S[6], const double tx[3], const double tu[3], const double tRc[3],
+                                const double tVc[3], const double tS[6]) {
         if (!has) return;
         for (int q = 0; q < 3; ++q) {
             h.r[q] = Rc[q] - S[q] * inv_M;
@@ -660,42 +640,42 @@ struct Large {
             for (int q = 0; q < 3; ++q) { b.r[q] = x[q] + h.r[q]; b.v[q] = u[q] + Vc[q]; }
         if (is_host)
             for (int q = 0; q < 3; ++q) { b.r[q] = h.r[q]; b.v[q] = h.v[q]; }
-        if constexpr (NT > 0) {
-            for (int q = 0; q < 3; ++q)
-                for (int d = 0; d < NT; ++d) {
-                    HT.r[q][d] = tRc[q][d] - tS[q][d] * inv_M;
-                    HT.v[q][d] = tVc[q][d] - tS[3 + q][d] * inv_hm;
-                    if (planet) { T.r[q][d] = tx[q][d] + HT.r[q][d]; T.v[q][d] = tu[q][d] + tVc[q][d]; }
-                    if (is_host) { T.r[q][d] = HT.r[q][d]; T.v[q][d] = HT.v[q][d]; }
-                }
+        if (tan_on()) {
+            for (int q = 0; q < 3; ++q) {
+                HT.r[q] = tRc[q] - tS[q] * inv_M;
+                HT.v[q] = tVc[q] - tS[3 + q] * inv_hm;
+                if (planet) { T.r[q] = tx[q] + HT.r[q]; T.v[q] = tu[q] + tVc[q]; }
+                if (is_host) { T.r[q] = HT.r[q]; T.v[q] = HT.v[q]; }
+            }
         }
     }
 
-    // sums of m x and m u over the planets (and their tangents), optionally
-    // publishing the positions for the pair loop
-    __device__ bool planet_sums(const double x[3], const double u[3], const double (&tx)[3][A],
-                                const double (&tu)[3][A], bool publish, double S[6], double (&tS)[6][A]) {
+    // sums of m x and m u over the planets (and the tangents of every
+    // direction, tS_all[d][q]), optionally publishing the positions for the
+    // pair loop
+    __device__ bool planet_sums(const double x[3], const double u[3], const double tx[3], const double tu[3],
+                                bool publish, double S[6], double (&tS_all)[NT > 0 ? NT : 1][6]) {
         double vals[NS] = {};
         if (planet) {
-            for (int q = 0; q < 3; ++q) {
-                if (publish) D.pos[q * n + i] = x[q];
-                vals[q] = c.m * x[q];
-                vals[3 + q] = c.m * u[q];
-            }
-            if constexpr (NT > 0)
-                for (int q = 0; q < 3; ++q)
-                    for (int d = 0; d < NT; ++d) {
-                        if (publish) D.dpos[(d * 3 + q) * n + i] = tx[q][d];
-                        vals[6 + q * NT + d] = c.m * tx[q][d];
-                        vals[6 + (3 + q) * NT + d] = c.m * tu[q][d];
-                    }
+            if (primal_role())
+                for (int q = 0; q < 3; ++q) {
+                    if (publish) D.pos[q * n + i] = x[q];
+                    vals[q] = c.m * x[q];
+                    vals[3 + q] = c.m * u[q];
+                }
+            if (tan_on())
+                for (int q = 0; q < 3; ++q) {
+                    if (publish) D.dpos[(dir * 3 + q) * n + i] = tx[q];
+                    vals[tslot(6, q)] = c.m * tx[q];
+                    vals[tslot(6, 3 + q)] = c.m * tu[q];
+                }
         }
         double tot[NS];
         if (!grid_reduce(D, vals, 6 + 6 * NT, tot, shm, warp_bodies, body_rows)) return false;
         for (int q = 0; q < 6; ++q) S[q] = tot[q];
         if constexpr (NT > 0)
-            for (int q = 0; q < 6; ++q)
-                for (int d = 0; d < NT; ++d) tS[q][d] = tot[6 + q * NT + d];
+            for (int d = 0; d < NT; ++d)
+                for (int q = 0; q < 6; ++q) tS_all[d][q] = tot[6 + q * NT + d];
         return true;
     }
 
@@ -708,41 +688,41 @@ struct Large {
     // dt sum_p m_p a_p, which is zero (the planets' mutual forces cancel and
     // the host's are left out of the kick).
     __device__ __forceinline__ bool step() {
+        constexpr int AN = NT > 0 ? NT : 1;
+        const bool tn = tan_on();
         const bool first = last_hist < 0.;
         if (first || last_hist + hist_period <= t) {
             spin_of(c, b.L, b.S);
             spin_of(hc, h.L, h.S);
-            if constexpr (NT > 0) {
+            if (tn) {
                 dspin_of(c, T.L, T.S);
                 dspin_of(hc, HT.L, HT.S);
             }
             last_hist = first ? 0. : last_hist + hist_period;
         }
-        double cm[6], tcm[6][A];
+        double cm[6], tcm[6] = {0., 0., 0., 0., 0., 0.};
         if (!midpoint(half_dt, cm, tcm)) return false;
         // inertial -> democratic heliocentric
         double Rc[3], Vc[3], x[3] = {0., 0., 0.}, u[3] = {0., 0., 0.};
-        double tRc[3][A], tVc[3][A], tx[3][A], tu[3][A];
+        double tRc[3] = {0., 0., 0.}, tVc[3] = {0., 0., 0.}, tx[3] = {0., 0., 0.}, tu[3] = {0., 0., 0.};
         for (int q = 0; q < 3; ++q) { Rc[q] = cm[q] * inv_M; Vc[q] = cm[3 + q] * inv_M; }
         if (planet)
             for (int q = 0; q < 3; ++q) { x[q] = b.r[q] - h.r[q]; u[q] = b.v[q] - Vc[q]; }
-        if constexpr (NT > 0)
-            for (int q = 0; q < 3; ++q)
-                for (int d = 0; d < NT; ++d) {
-                    tRc[q][d] = tcm[q][d] * inv_M;
-                    tVc[q][d] = tcm[3 + q][d] * inv_M;
-                    tx[q][d] = planet ? T.r[q][d] - HT.r[q][d] : 0.;
-                    tu[q][d] = planet ? T.v[q][d] - tVc[q][d] : 0.;
-                }
+        if (tn)
+            for (int q = 0; q < 3; ++q) {
+                tRc[q] = tcm[q] * inv_M;
+                tVc[q] = tcm[3 + q] * inv_M;
+                tx[q] = planet ? T.r[q] - HT.r[q] : 0.;
+                tu[q] = planet ? T.v[q] - tVc[q] : 0.;
+            }
         // part 1: Kepler drift (and the barycentre's), jump, back to inertial
         kepler(x, u, tx, tu);
         for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
-        if constexpr (NT > 0)
-            for (int q = 0; q < 3; ++q)
-                for (int d = 0; d < NT; ++d) tRc[q][d] += half_dt * tVc[q][d];
-        double S[6], tS[6][A];
-        if (!planet_sums(x, u, tx, tu, true, S, tS)) return false;
-        double shift[3], tshift[3][A];
+        if (tn)
+            for (int q = 0; q < 3; ++q) tRc[q] += half_dt * tVc[q];
+        double S[6], tS_all[AN][6];
+        if (!planet_sums(x, u, tx, tu, true, S, tS_all)) return false;
+        double shift[3], tshift[AN][3];
         for (int q = 0; q < 3; ++q) {
             shift[q] = half_dt * S[3 + q] * inv_hm;        // jump: dt/2 P / m_host
             S[q] += shift[q] * (Mtot - hc.m);              // sum_p m_p (x_p + shift)
@@ -750,15 +730,20 @@ struct Large {
         const double P[3] = {S[3], S[4], S[5]};
         if (planet)
             for (int q = 0; q < 3; ++q) x[q] += shift[q];
-        double tP[3][A];
+        // every direction's shift (the pair loop needs them all), then this
+        // thread's own sums
         if constexpr (NT > 0)
-            for (int q = 0; q < 3; ++q)
-                for (int d = 0; d < NT; ++d) {
-                    tshift[q][d] = half_dt * tS[3 + q][d] * inv_hm;
-                    tS[q][d] += tshift[q][d] * (Mtot - hc.m);
-                    tP[q][d] = tS[3 + q][d];
-                    if (planet) tx[q][d] += tshift[q][d];
-                }
+            for (int d = 0; d < NT; ++d)
+                for (int q = 0; q < 3; ++q) tshift[d][q] = half_dt * tS_all[d][3 + q] * inv_hm;
+        double tS[6] = {0., 0., 0., 0., 0., 0.}, tP[3] = {0., 0., 0.};
+        if (tn) {
+            for (int q = 0; q < 6; ++q) tS[q] = tS_all[dir][q];
+            for (int q = 0; q < 3; ++q) {
+                tS[q] += tshift[dir][q] * (Mtot - hc.m);
+                tP[q] = tS[3 + q];
+                if (planet) tx[q] += tshift[dir][q];
+            }
+        }
         to_inertial(x, u, Rc, Vc, S, tx, tu, tRc, tVc, tS);
         // gravity and the interaction kick
         if (!gravity(shift, tshift)) return false;
@@ -768,19 +753,18 @@ struct Large {
         // part 2: jump, Kepler drift, back to inertial
         if (planet)
             for (int q = 0; q < 3; ++q) x[q] += half_dt * P[q] * inv_hm;
-        if constexpr (NT > 0)
-            if (planet)
-                for (int q = 0; q < 3; ++q)
-                    for (int d = 0; d < NT; ++d) {
-                        tu[q][d] += dt * da[q][d];
-                        tx[q][d] += half_dt * tP[q][d] * inv_hm;
-                    }
+        if (tn && planet)
+            for (int q = 0; q < 3; ++q) {
+                tu[q] += dt * da[q];
+                tx[q] += half_dt * tP[q] * inv_hm;
+            }
         kepler(x, u, tx, tu);
         for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
-        if constexpr (NT > 0)
-            for (int q = 0; q < 3; ++q)
-                for (int d = 0; d < NT; ++d) tRc[q][d] += half_dt * tVc[q][d];
-        if (!planet_sums(x, u, tx, tu, false, S, tS)) return false;
+        if (tn)
+            for (int q = 0; q < 3; ++q) tRc[q] += half_dt * tVc[q];
+        if (!planet_sums(x, u, tx, tu, false, S, tS_all)) return false;
+        if (tn)
+            for (int q = 0; q < 6; ++q) tS[q] = tS_all[dir][q];
         to_inertial(x, u, Rc, Vc, S, tx, tu, tRc, tVc, tS);
         if (!midpoint(half_dt, nullptr, nullptr)) return false;
         t += dt;
@@ -788,19 +772,23 @@ struct Large {
     }
 };
 
+// Thread roles: block b holds bodies [b per_block, (b + 1) per_block); thread
+// r per_block + l of the block is role r of body b per_block + l (r = 0..NT).
 template <int NT>
 __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t n_steps) {
     __shared__ double shm[(kBlock / 32 + 1) * BP_ROW];
     Large<NT> S(D, shm);
     S.n = D.n;
-    // bodies spread over the blocks, at most one warp of bodies per SMSP
-    // while the grid has room: the per-body work runs on as many SMSPs as it can
-    S.i = threadIdx.x < D.per_block ? (int64_t)blockIdx.x * D.per_block + threadIdx.x : INT64_MAX;
+    const int roles = 1 + NT;
+    const int role = (int)threadIdx.x / D.per_block;
+    S.i = role < roles ? (int64_t)blockIdx.x * D.per_block + (int64_t)(threadIdx.x % D.per_block) : INT64_MAX;
+    S.dir = NT > 0 && role >= 1 && role < roles ? role - 1 : -1;
     S.host = (int)D.si[POSI_SI_HOST];
     S.has = S.i < S.n;
     {
-        const int64_t warp_first = (int64_t)blockIdx.x * D.per_block + (threadIdx.x & ~31);
-        S.warp_bodies = (int)(threadIdx.x & ~31) < D.per_block && warp_first < S.n;
+        const int w0 = (int)(threadIdx.x & ~31);
+        const int64_t warp_first = (int64_t)blockIdx.x * D.per_block + (w0 % D.per_block);
+        S.warp_bodies = w0 < D.per_block * roles && warp_first < S.n;
         S.body_rows = (unsigned)((S.n + D.per_block - 1) / D.per_block);
     }
     S.is_host = S.has && S.i == S.host;
@@ -815,6 +803,7 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
     S.last_hist = D.sf[POSI_SF_LAST_HIST];
     S.hist_period = D.sf[POSI_SF_HIST_PERIOD];
     S.a[0] = S.a[1] = S.a[2] = 0.;
+    S.da[0] = S.da[1] = S.da[2] = 0.;
     S.hc = load_const(D, S.host);
     load_state(D, S.host, S.h);
     if (S.has) {
@@ -824,26 +813,28 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
         S.c = S.hc;
         S.b = S.h;
     }
-    if constexpr (NT > 0) {
+    for (int q = 0; q < 3; ++q) {
+        S.T.r[q] = S.T.v[q] = S.T.L[q] = S.T.S[q] = 0.;
+        S.HT.r[q] = S.HT.v[q] = S.HT.L[q] = S.HT.S[q] = 0.;
+    }
+    if (S.tan_on()) {
         const int64_t n = S.n, src = S.has ? S.i : S.host;
-        for (int q = 0; q < 3; ++q)
-            for (int d = 0; d < NT; ++d) {
-                const double* base = D.tan + (size_t)d * 12 * n;
-                S.HT.r[q][d] = base[(0 + q) * n + S.host];
-                S.HT.v[q][d] = base[(3 + q) * n + S.host];
-                S.HT.L[q][d] = base[(6 + q) * n + S.host];
-                S.HT.S[q][d] = base[(9 + q) * n + S.host];
-                S.T.r[q][d] = base[(0 + q) * n + src];
-                S.T.v[q][d] = base[(3 + q) * n + src];
-                S.T.L[q][d] = base[(6 + q) * n + src];
-                S.T.S[q][d] = base[(9 + q) * n + src];
-                S.da[q][d] = 0.;
-            }
+        const double* base = D.tan + (size_t)S.dir * 12 * n;
+        for (int q = 0; q < 3; ++q) {
+            S.HT.r[q] = base[(0 + q) * n + S.host];
+            S.HT.v[q] = base[(3 + q) * n + S.host];
+            S.HT.L[q] = base[(6 + q) * n + S.host];
+            S.HT.S[q] = base[(9 + q) * n + S.host];
+            S.T.r[q] = base[(0 + q) * n + src];
+            S.T.v[q] = base[(3 + q) * n + src];
+            S.T.L[q] = base[(6 + q) * n + src];
+            S.T.S[q] = base[(9 + q) * n + src];
+        }
     }
     // total mass, in block order
     {
         double vals[Large<NT>::NS] = {};
-        vals[0] = S.has ? S.c.m : 0.;
+        vals[0] = S.has && S.primal_role() ? S.c.m : 0.;
         double tot[1];
         if (!grid_reduce(D, vals, 1, tot, shm, S.warp_bodies, S.body_rows)) return;
         S.Mtot = tot[0];
@@ -862,7 +853,7 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
         }
     }
     if (__ldcg(D.err) & LE_BARRIER) return;  // state left as it was: the launch failed
-    if (S.has) {
+    if (S.has && S.primal_role()) {
         const int64_t n = S.n, i = S.i;
         for (int q = 0; q < 3; ++q) {
             D.bf[(POSI_BF_PX + q) * n + i] = S.b.r[q];
@@ -874,15 +865,16 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
             D.bf[(POSI_BF_AX + q) * n + i] = S.a[q];
         }
         D.bf[POSI_BF_NSV2 * n + i] = S.b.S[0] * S.b.S[0] + S.b.S[1] * S.b.S[1] + S.b.S[2] * S.b.S[2];
-        if constexpr (NT > 0)
-            for (int q = 0; q < 3; ++q)
-                for (int d = 0; d < NT; ++d) {
-                    double* base = D.tan + (size_t)d * 12 * n;
-                    base[(0 + q) * n + i] = S.T.r[q][d];
-                    base[(3 + q) * n + i] = S.T.v[q][d];
-                    base[(6 + q) * n + i] = S.T.L[q][d];
-                    base[(9 + q) * n + i] = S.T.S[q][d];
-                }
+    }
+    if (S.has && S.tan_on()) {
+        const int64_t n = S.n, i = S.i;
+        double* base = D.tan + (size_t)S.dir * 12 * n;
+        for (int q = 0; q < 3; ++q) {
+            base[(0 + q) * n + i] = S.T.r[q];
+            base[(3 + q) * n + i] = S.T.v[q];
+            base[(6 + q) * n + i] = S.T.L[q];
+            base[(9 + q) * n + i] = S.T.S[q];
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && live) {
         D.sf[POSI_SF_TIME] = S.t;
