@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-derivative", action="store_true",
                    help="large workload: skip the timed derivative run (dissipation-factor tangents)")
+    p.add_argument("--derivative-dirs", type=int, default=2, choices=[1, 2, 3, 4],
+                   help="large workload: tangent directions of the derivative run (the two planets' "
+                        "dissipation factors, then their Love numbers)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     return p.parse_args()
 
@@ -437,18 +440,20 @@ def run_gradient(args):
     print(json.dumps(result), flush=True)
 
 
-def large_derivative(mb, init, K, forward_ms, flush):
+def large_derivative(mb, init, K, forward_ms, flush, n_dirs=2):
     """Derivatives of the many-body run with respect to the two tidal
     planets' dissipation factors: one launch of the engine carrying both
     tangent directions over the same K steps (forward mode; two parameters),
-    then the loss gradient (torch) from the final state and the tangents."""
+    then the loss gradient (torch) from the final state and the tangents.
+    n_dirs != 2 times other direction counts (1: the first planet's
+    dissipation factor; 3, 4: the planets' Love numbers added)."""
     import torch
 
     from posidonius_gb300 import adjoint as A
     from posidonius_gb300 import layout as L
 
     planets = (1, 2)
-    seeds = [(p, L.SEED_SIGMA) for p in planets]
+    seeds = ([(p, L.SEED_SIGMA) for p in planets] + [(p, L.SEED_K2) for p in planets])[:n_dirs]
     host = int(init["sys_i64"][L.SI_HOST])
     idx = [host, *planets]
     b0 = init["body_f64"][idx]
@@ -465,21 +470,23 @@ def large_derivative(mb, init, K, forward_ms, flush):
     _, tan = mb.iterate_tangent(K, seeds)
     tan_ms = mb.last_timing()
     final = mb.get_state()
-    loss, grad = A.tangent_loss_gradient(final["body_f64"], tan, host, planets, a0, spin0)
+    loss, grad = A.tangent_loss_gradient(final["body_f64"], tan[:2], host, planets, a0, spin0)
     # end to end: host state and zero tangents in, K steps, state, tangents and gradient out
     t0 = time.perf_counter()
     mb.set_state(init)
     _, tan2 = mb.iterate_tangent(K, seeds)
     fin2 = mb.get_state()
-    A.tangent_loss_gradient(fin2["body_f64"], tan2, host, planets, a0, spin0)
+    A.tangent_loss_gradient(fin2["body_f64"], tan2[:2], host, planets, a0, spin0)
     e2e_s = time.perf_counter() - t0
     sig = init["body_f64"][list(planets), L.BF_SIGMA]
     return {
         "kind": "forward mode: tangents of every body's state along each planet's dissipation factor, both "
                 "directions in one launch of the engine; loss gradient = final-state gradient (torch) . tangents",
-        "parameters": [f"dissipation factor of body {p}" for p in planets],
+        "directions": [("dissipation factor" if q == L.SEED_SIGMA else "Love number") + f" of body {b}"
+                       for b, q in seeds],
+        "parameters": [f"dissipation factor of body {p}" for p in planets][:len(grad)],
         "loss": "sum over the 2 planets of e^2 + ((a - a0)/a0)^2 + ((|Omega| - |Omega0|)/|Omega0|)^2",
-        "loss_value": loss, "dloss_dsigma": grad.tolist(), "dloss_dlog_sigma": (grad * sig).tolist(),
+        "loss_value": loss, "dloss_dsigma": grad.tolist(), "dloss_dlog_sigma": (grad * sig[:len(grad)]).tolist(),
         "ms": tan_ms, "ms_per_step": tan_ms / K, "over_forward": tan_ms / forward_ms,
         "e2e_s": e2e_s, "gpu_launches": 1,
     }
@@ -536,7 +543,7 @@ def run_large(args):
         "gpu_launches": 1, "status": int(final["sys_i64"][L.SI_STATUS]), "clocks": clock_info,
     }
     if not args.no_derivative:
-        result["derivative"] = large_derivative(mb, init, K, ms, flush)
+        result["derivative"] = large_derivative(mb, init, K, ms, flush, args.derivative_dirs)
     if not args.no_cpu_baseline:
         import oracle
         from oracle.case_json import stack
