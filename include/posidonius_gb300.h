@@ -275,8 +275,14 @@ int posi_batch_initialize_physical_values(posi_batch* b);
 
 /* Advance every live system by n_steps WHFast steps, steps_per_launch steps per
  * persistent-kernel launch; the launches are captured once in a CUDA graph and
- * replayed.  Systems that complete or hit a fatal event are frozen. */
+ * replayed.  Systems that complete or hit a fatal event are frozen.  When a
+ * lane mapping leaves between one and two warps of systems per SMSP, a launch
+ * runs as a balanced schedule of sub-launches (warps alone on an SMSP take
+ * more steps, and the systems rotate), with the same results bit for bit. */
 int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch);
+/* Balanced schedules on (1, the default) or off (0).  No reference
+ * counterpart: a scheduling switch of this implementation. */
+int posi_batch_set_balanced(posi_batch* b, int on);
 
 /* Host <-> device copies of the whole ensemble (flat layout). */
 int posi_batch_get_state(const posi_batch* b, int64_t* sys_i64, double* sys_f64,

@@ -234,6 +234,10 @@ class Batch:
     def iterate(self, n_steps, steps_per_launch=0):
         check(lib().posi_batch_iterate(self._h, int(n_steps), int(steps_per_launch)))
 
+    def set_balanced(self, on=True):
+        """Balanced launch schedules on or off (posi_batch_set_balanced)."""
+        check(lib().posi_batch_set_balanced(self._h, int(bool(on))))
+
     def last_timing(self):
         ms = ctypes.c_double()
         n = ctypes.c_int64()

@@ -46,6 +46,7 @@ SIGNATURES = {
     "posi_batch_size": (ctypes.c_int, [_vp, _i64p, _i64p]),
     "posi_batch_initialize_physical_values": (ctypes.c_int, [_vp]),
     "posi_batch_iterate": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64]),
+    "posi_batch_set_balanced": (ctypes.c_int, [_vp, ctypes.c_int]),
     "posi_batch_get_state": (ctypes.c_int, [_vp, _i64p, _f64p, _i64p, _f64p, _f64p]),
     "posi_batch_set_state": (ctypes.c_int, [_vp, _i64p, _f64p, _i64p, _f64p]),
     "posi_batch_mapping_for": (ctypes.c_int, [_vp, ctypes.c_int64]),

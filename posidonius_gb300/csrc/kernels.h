@@ -25,7 +25,8 @@ struct DevView {
 
 // OP_STEPS_REC: OP_STEPS writing the adjoint's step records to DevView::rec
 // (FAST build only).
-enum KernelOp { OP_STEPS = 0, OP_INIT = 1, OP_GRAVITY = 2, OP_EFFECTS = 3, OP_STEPS_REC = 4 };
+// OP_STEPS_SCHED: OP_STEPS under a balanced schedule (whfast_sched_kernel)
+enum KernelOp { OP_STEPS = 0, OP_INIT = 1, OP_GRAVITY = 2, OP_EFFECTS = 3, OP_STEPS_REC = 4, OP_STEPS_SCHED = 5 };
 
 struct LaunchArgs {
     int op;
@@ -34,6 +35,10 @@ struct LaunchArgs {
     int ignore_terms;      // OP_GRAVITY
     double t_eval;         // OP_EFFECTS
     int evolution, dl, acc;
+    // OP_STEPS_SCHED: blocks, and per warp slot (blocks * 8) the job and steps
+    int sched_blocks;
+    const int32_t* slot_job;
+    const int32_t* slot_steps;
 };
 
 // Returns cudaSuccess or the launch error.
@@ -55,6 +60,8 @@ inline int group_size_for(int64_t n) {
 }
 
 constexpr int kBlockThreads = 128;
+// the balanced schedule's blocks: one per SM, eight warps (two per SMSP)
+constexpr int kSchedBlockThreads = 256;
 
 // Adjoint kernels (adjoint.cu): which = 0 records a chunk's tape, 1 runs its
 // reverse sweep.  Systems of up to 8 bodies, Jacobi coordinates.

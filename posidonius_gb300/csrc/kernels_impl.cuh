@@ -31,6 +31,16 @@ static cudaError_t launch_g(const posi::DevView& v, const posi::LaunchArgs& a, c
             whfast_steps_kernel<G, true><<<blocks, threads, smem, stream>>>(d, a.n_steps);
             break;
 #endif
+        case posi::OP_STEPS_SCHED:
+            if constexpr (G >= 4) {
+                if (!a.slot_job || !a.slot_steps || a.sched_blocks <= 0) return cudaErrorInvalidValue;
+                const size_t ssmem = (size_t)(posi::kSchedBlockThreads / G) * GroupSmem<G>::bytes;
+                whfast_sched_kernel<G><<<a.sched_blocks, posi::kSchedBlockThreads, ssmem, stream>>>(d, a.slot_job,
+                                                                                                   a.slot_steps);
+                break;
+            } else {
+                return cudaErrorInvalidValue;
+            }
         case posi::OP_INIT:
             init_physical_kernel<G><<<blocks, threads, smem, stream>>>(d);
             break;
@@ -54,6 +64,12 @@ static cudaError_t prepare_g() {
 #if !POSI_EXACT
     if ((e = cudaFuncSetAttribute(whfast_steps_kernel<G, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
 #endif
+    if constexpr (G >= 4) {
+        const int ssmem = (posi::kSchedBlockThreads / G) * GroupSmem<G>::bytes;
+        if ((e = cudaFuncSetAttribute(whfast_sched_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, ssmem)) !=
+            cudaSuccess)
+            return e;
+    }
     if ((e = cudaFuncSetAttribute(init_physical_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(gravity_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) return e;
     return cudaFuncSetAttribute(additional_effects_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

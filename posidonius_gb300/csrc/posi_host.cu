@@ -106,6 +106,10 @@ struct posi_batch {
     int64_t last_launches = 0;
     cudaGraphExec_t graph = nullptr;
     int64_t graph_steps = -1, graph_spl = -1;
+    // balanced schedules of the captured graph (whfast_sched_kernel tables)
+    bool balanced = true;
+    int sms = 0;
+    int32_t* d_sched = nullptr;
 
     DevView view(int32_t list_offset, int32_t count) const {
         DevView v;
@@ -142,6 +146,7 @@ namespace {
 void free_batch(posi_batch* b) {
     if (!b) return;
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    cudaFree(b->d_sched);
     cudaFree(b->d_bf); cudaFree(b->d_bi); cudaFree(b->d_sf); cudaFree(b->d_si);
     cudaFree(b->d_roche); cudaFree(b->d_tables); cudaFree(b->d_list); cudaFree(b->d_flags);
     cudaFree(b->d_stage);
@@ -229,6 +234,56 @@ int build_buckets(posi_batch* b, const int64_t* sys_i64, const std::map<int64_t,
     return POSI_OK;
 }
 
+// Balanced schedule of one bucket's launch of `steps` steps for
+// whfast_sched_kernel: one 256-thread block per SM, eight warp slots each.
+// With `jobs` warps of systems between one and two per SMSP, the first
+// `light` blocks hold four jobs (one warp per SMSP) and the others eight (two
+// per SMSP).  A lone warp runs kLoneSpeed times as many steps per unit time as
+// one sharing its SMSP (measured on GB300: 121 against 213 us per step of the
+// 8-body ensemble), so in every sub-launch the jobs in lone slots get that
+// many more steps, and the jobs with the most steps left take the lone slots.
+// table: per sub-launch, the job of every slot (-1: idle) then its steps.
+// Returns false when the bucket needs no schedule.
+bool build_schedule(int sms, int jobs, int64_t steps, std::vector<int32_t>& table, int& launches) {
+    constexpr double kLoneSpeed = 1.75;
+    constexpr int64_t kSubLaunches = 12;   // about this many per launch of `steps` steps
+    const int per = posi::kSchedBlockThreads / 32;
+    const int slots = sms * per;
+    if (sms <= 0 || jobs <= slots / 2 || jobs >= slots) return false;
+    const int light = (slots - jobs) / (per / 2);
+    if (light < 1) return false;
+    const int64_t q = std::max<int64_t>(1, steps / kSubLaunches);
+    const int64_t ql = std::max<int64_t>(1, (int64_t)std::llround(kLoneSpeed * (double)q));
+    std::vector<int64_t> rem((size_t)jobs, steps);
+    std::vector<int> order((size_t)jobs);
+    table.clear();
+    launches = 0;
+    for (;;) {
+        bool left = false;
+        for (int64_t r : rem) left = left || r > 0;
+        if (!left) break;
+        for (int j = 0; j < jobs; ++j) order[(size_t)j] = j;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return rem[(size_t)x] > rem[(size_t)y]; });
+        std::vector<int32_t> job((size_t)slots, -1), st((size_t)slots, 0);
+        int k = 0;
+        for (int blk = 0; blk < sms && k < jobs; ++blk) {
+            const bool lone = blk < light;
+            for (int w = 0; w < (lone ? per / 2 : per) && k < jobs; ++w) {
+                const int j = order[(size_t)k++];
+                const int64_t s = std::min(rem[(size_t)j], lone ? ql : q);
+                if (s <= 0) continue;
+                job[(size_t)(blk * per + w)] = j;
+                st[(size_t)(blk * per + w)] = (int32_t)s;
+                rem[(size_t)j] -= s;
+            }
+        }
+        table.insert(table.end(), job.begin(), job.end());
+        table.insert(table.end(), st.begin(), st.end());
+        if (++launches > 100000) return false;
+    }
+    return true;
+}
+
 posi_batch* create_batch(int64_t n_sys, int64_t nmax, const int64_t* si, const double* sf, const int64_t* bi,
                          const double* bf, const double* tables, int64_t n_tables, const double* roche, int mode,
                          int mapping, int* status) {
@@ -267,6 +322,11 @@ posi_batch* create_batch(int64_t n_sys, int64_t nmax, const int64_t* si, const d
         !ok(cudaEventCreate(&b->ev1)))
         return fail(POSI_ERR_CUDA, b);
     if (!ok(mode == POSI_MODE_EXACT ? posi::prepare_exact() : posi::prepare_fast())) return fail(POSI_ERR_CUDA, b);
+    {
+        int dev = 0;
+        if (!ok(cudaGetDevice(&dev)) || !ok(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev)))
+            return fail(POSI_ERR_CUDA, b);
+    }
     const size_t nb = (size_t)b->stride;
     b->stage_bytes = std::max({nb * POSI_BF_COUNT * sizeof(double), nb * POSI_BI_COUNT * sizeof(int64_t),
                                (size_t)n_sys * POSI_SF_COUNT * sizeof(double),
@@ -817,6 +877,32 @@ int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch)
     const int64_t chunks = (n_steps + steps_per_launch - 1) / steps_per_launch;
     if (!b->graph || b->graph_steps != n_steps || b->graph_spl != steps_per_launch) {
         if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+        // balanced schedules of every (chunk length, bucket), made before the
+        // capture and kept with the graph
+        const int slots = b->sms * (posi::kSchedBlockThreads / 32);
+        std::vector<int32_t> tables;
+        std::map<std::pair<int64_t, size_t>, std::pair<size_t, int>> plan;  // -> (offset, sub-launches)
+        for (int64_t c = 0; c < chunks; ++c) {
+            const int64_t len = std::min(steps_per_launch, n_steps - c * steps_per_launch);
+            for (size_t k = 0; k < b->buckets.size(); ++k) {
+                const Bucket& bk = b->buckets[k];
+                if (!b->balanced || bk.G < 4 || plan.count({len, k})) continue;
+                const int jobs = (int)((bk.count + (32 / bk.G) - 1) / (32 / bk.G));
+                std::vector<int32_t> t;
+                int launches = 0;
+                if (build_schedule(b->sms, jobs, len, t, launches)) {
+                    plan[{len, k}] = {tables.size(), launches};
+                    tables.insert(tables.end(), t.begin(), t.end());
+                }
+            }
+        }
+        cudaFree(b->d_sched);
+        b->d_sched = nullptr;
+        if (!tables.empty()) {
+            CK(cudaMalloc(&b->d_sched, tables.size() * sizeof(int32_t)));
+            CK(cudaMemcpy(b->d_sched, tables.data(), tables.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        }
+        b->last_launches = 0;
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         LaunchArgs a{};
@@ -824,9 +910,24 @@ int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch)
         cudaError_t err = cudaSuccess;
         for (int64_t c = 0; c < chunks && err == cudaSuccess; ++c) {
             a.n_steps = std::min(steps_per_launch, n_steps - c * steps_per_launch);
-            for (const Bucket& bk : b->buckets) {
-                err = b->launch(bk, a);
-                if (err != cudaSuccess) break;
+            for (size_t k = 0; k < b->buckets.size() && err == cudaSuccess; ++k) {
+                const Bucket& bk = b->buckets[k];
+                auto it = plan.find({a.n_steps, k});
+                if (it == plan.end()) {
+                    err = b->launch(bk, a);
+                    ++b->last_launches;
+                    continue;
+                }
+                LaunchArgs s = a;
+                s.op = posi::OP_STEPS_SCHED;
+                s.sched_blocks = b->sms;
+                for (int l = 0; l < it->second.second && err == cudaSuccess; ++l) {
+                    const int32_t* row = b->d_sched + it->second.first + (size_t)l * 2 * slots;
+                    s.slot_job = row;
+                    s.slot_steps = row + slots;
+                    err = b->launch(bk, s);
+                    ++b->last_launches;
+                }
             }
         }
         cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
@@ -845,7 +946,17 @@ int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch)
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     b->last_ms = ms;
-    b->last_launches = chunks * (int64_t)b->buckets.size();
+    return POSI_OK;
+}
+
+int posi_batch_set_balanced(posi_batch* b, int on) {
+    if (!b) return POSI_ERR_ARG;
+    if (b->balanced != (on != 0) && b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        b->graph_steps = -1;
+    }
+    b->balanced = on != 0;
     return POSI_OK;
 }
 

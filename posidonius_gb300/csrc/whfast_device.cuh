@@ -2194,15 +2194,11 @@ __device__ __forceinline__ bool group_setup(const Dev& D, int& sys, int& lane, u
     return true;
 }
 
-// Advance each listed system by up to n_steps steps (the plain path launches
-// it with one system and n_steps = 1; the batched path with many systems and
-// many steps per launch).
-template <int G, bool REC = false>
-__global__ void __launch_bounds__(128) whfast_steps_kernel(Dev D, int64_t n_steps) {
-    int sys, lane;
-    unsigned mask;
-    double* smem;
-    if (!group_setup<G>(D, sys, lane, mask, smem)) return;
+// n_steps WHFast steps of one system by its lane group (fewer when it
+// completes or freezes), state loaded from and stored to the device view.
+template <int G, bool REC>
+__device__ __forceinline__ void run_steps(const Dev& D, int sys, int lane, unsigned mask, double* smem,
+                                          int64_t n_steps) {
     Sys<G> S;
     S.load(D, sys, lane, mask, smem);
     S.rp = nullptr;
@@ -2230,6 +2226,43 @@ __global__ void __launch_bounds__(128) whfast_steps_kernel(Dev D, int64_t n_step
         }
     }
     S.store(D);
+}
+
+// Advance each listed system by up to n_steps steps (the plain path launches
+// it with one system and n_steps = 1; the batched path with many systems and
+// many steps per launch).
+template <int G, bool REC = false>
+__global__ void __launch_bounds__(128) whfast_steps_kernel(Dev D, int64_t n_steps) {
+    int sys, lane;
+    unsigned mask;
+    double* smem;
+    if (!group_setup<G>(D, sys, lane, mask, smem)) return;
+    run_steps<G, REC>(D, sys, lane, mask, smem, n_steps);
+}
+
+// The same steps under a balanced schedule: one 256-thread block per SM,
+// eight warps (two per SMSP).  Warp slot w = blockIdx.x * 8 + warp runs job
+// slot_job[w] -- the systems list[job * (32 / G) ...] of one warp -- for
+// slot_steps[w] steps; job -1 leaves the slot idle.  A warp alone on its
+// SMSP runs its FP64 work faster than two sharing one, so the host gives the
+// jobs in such slots more steps and rotates the jobs between sub-launches.
+template <int G>
+__global__ void __launch_bounds__(posi::kSchedBlockThreads, 1)
+whfast_sched_kernel(Dev D, const int32_t* slot_job, const int32_t* slot_steps) {
+    extern __shared__ double shm[];
+    const int tid = threadIdx.x;
+    const int slot = blockIdx.x * (posi::kSchedBlockThreads / 32) + (tid >> 5);
+    const int job = slot_job[slot];
+    const int64_t n_steps = slot_steps[slot];
+    if (job < 0 || n_steps <= 0) return;   // the whole warp
+    const int gib = tid / G;
+    const int lane = tid % G;
+    const int in_warp = (tid % 32) / G;
+    const unsigned mask = (G >= 32) ? 0xffffffffu : (((1u << G) - 1u) << (in_warp * G));
+    double* smem = shm + (size_t)gib * (GroupSmem<G>::bytes / 8);
+    const int64_t li = (int64_t)job * (32 / G) + in_warp;
+    if (li >= D.n_list) return;            // the whole group
+    run_steps<G, false>(D, D.list[li], lane, mask, smem, n_steps);
 }
 
 // src/integrator/whfast.rs:226-233 (the Roche radii are computed on the host)

@@ -1,0 +1,53 @@
+"""GPU: balanced launch schedules (posi_batch_set_balanced).
+
+With between one and two warps of systems per SMSP, a launch runs as
+sub-launches in which warps alone on an SMSP take more steps and the systems
+rotate.  Every system must still advance by exactly the requested steps, and
+the states must equal those of the plain launches bit for bit (a system's
+arithmetic does not depend on where or in how many pieces its steps run).
+"""
+import numpy as np
+import pytest
+
+import posidonius_gb300 as pg
+from posidonius_gb300 import ensemble as E, layout as L
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from posidonius_gb300 import build
+    build.build()
+
+
+def _run(ens, balanced, n_steps, spl, mode=pg.FAST):
+    b = pg.Batch(ens, mode=mode, mapping=L.MAP_LANES8)
+    b.set_balanced(balanced)
+    b.initialize_physical_values()
+    b.iterate(n_steps, spl)
+    st = b.get_state()
+    _, launches = b.last_timing()
+    b.close()
+    return st, launches
+
+
+@pytest.mark.parametrize("n_steps,spl", [(60, 60), (61, 25)])
+def test_balanced_schedule_matches_plain_launches(n_steps, spl):
+    # 4096 systems of 8 bodies: 1024 warps, between one and two per SMSP of a
+    # 152-SM part
+    ens = E.workload_ensemble8(4096, seed=5)
+    a, la = _run(ens, True, n_steps, spl)
+    b, lb = _run(ens, False, n_steps, spl)
+    assert np.all(a["sys_i64"][:, L.SI_ITERATION] == n_steps)
+    for k in ("sys_i64", "sys_f64", "body_f64"):
+        assert np.array_equal(np.asarray(a[k]).view(np.int64), np.asarray(b[k]).view(np.int64)), k
+    assert la >= lb
+
+
+def test_balanced_schedule_exact_mode():
+    ens = E.workload_ensemble8(3000, seed=6)
+    a, _ = _run(ens, True, 40, 40, mode=pg.EXACT)
+    b, _ = _run(ens, False, 40, 40, mode=pg.EXACT)
+    assert np.all(a["sys_i64"][:, L.SI_ITERATION] == 40)
+    assert np.array_equal(a["body_f64"].view(np.int64), b["body_f64"].view(np.int64))
