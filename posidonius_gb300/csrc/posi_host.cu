@@ -110,6 +110,11 @@ struct posi_batch {
     bool balanced = true;
     int sms = 0;
     int32_t* d_sched = nullptr;
+    // one stream per bucket: the buckets' launches of a chunk run side by
+    // side (disjoint systems), forked from and joined back to `stream`
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> side_done;
+    cudaEvent_t fork = nullptr;
 
     DevView view(int32_t list_offset, int32_t count) const {
         DevView v;
@@ -122,11 +127,12 @@ struct posi_batch {
         v.rec = nullptr;
         return v;
     }
-    cudaError_t launch(const Bucket& bk, const LaunchArgs& a0) const {
+    cudaError_t launch(const Bucket& bk, const LaunchArgs& a0, cudaStream_t on = nullptr) const {
         LaunchArgs a = a0;
         a.G = bk.G;
         DevView v = view(bk.offset, bk.count);
-        return mode == POSI_MODE_EXACT ? posi::launch_exact(v, a, stream) : posi::launch_fast(v, a, stream);
+        cudaStream_t st = on ? on : stream;
+        return mode == POSI_MODE_EXACT ? posi::launch_exact(v, a, st) : posi::launch_fast(v, a, st);
     }
 };
 
@@ -146,6 +152,9 @@ namespace {
 void free_batch(posi_batch* b) {
     if (!b) return;
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (cudaStream_t st : b->side) cudaStreamDestroy(st);
+    for (cudaEvent_t e : b->side_done) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
     cudaFree(b->d_sched);
     cudaFree(b->d_bf); cudaFree(b->d_bi); cudaFree(b->d_sf); cudaFree(b->d_si);
     cudaFree(b->d_roche); cudaFree(b->d_tables); cudaFree(b->d_list); cudaFree(b->d_flags);
@@ -903,6 +912,19 @@ int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch)
             CK(cudaMemcpy(b->d_sched, tables.data(), tables.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
         }
         b->last_launches = 0;
+        const size_t nbk = b->buckets.size();
+        const bool fan = nbk > 1;
+        if (fan) {
+            if (!b->fork) CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+            while (b->side.size() < nbk) {
+                cudaStream_t st;
+                cudaEvent_t e;
+                CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+                CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                b->side.push_back(st);
+                b->side_done.push_back(e);
+            }
+        }
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         LaunchArgs a{};
@@ -910,25 +932,31 @@ int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch)
         cudaError_t err = cudaSuccess;
         for (int64_t c = 0; c < chunks && err == cudaSuccess; ++c) {
             a.n_steps = std::min(steps_per_launch, n_steps - c * steps_per_launch);
-            for (size_t k = 0; k < b->buckets.size() && err == cudaSuccess; ++k) {
+            if (fan) err = cudaEventRecord(b->fork, b->stream);
+            for (size_t k = 0; k < nbk && err == cudaSuccess; ++k) {
                 const Bucket& bk = b->buckets[k];
+                cudaStream_t on = fan ? b->side[k] : b->stream;
+                if (fan && (err = cudaStreamWaitEvent(on, b->fork, 0)) != cudaSuccess) break;
                 auto it = plan.find({a.n_steps, k});
                 if (it == plan.end()) {
-                    err = b->launch(bk, a);
+                    err = b->launch(bk, a, on);
                     ++b->last_launches;
-                    continue;
+                } else {
+                    LaunchArgs s = a;
+                    s.op = posi::OP_STEPS_SCHED;
+                    s.sched_blocks = b->sms;
+                    for (int l = 0; l < it->second.second && err == cudaSuccess; ++l) {
+                        const int32_t* row = b->d_sched + it->second.first + (size_t)l * 2 * slots;
+                        s.slot_job = row;
+                        s.slot_steps = row + slots;
+                        err = b->launch(bk, s, on);
+                        ++b->last_launches;
+                    }
                 }
-                LaunchArgs s = a;
-                s.op = posi::OP_STEPS_SCHED;
-                s.sched_blocks = b->sms;
-                for (int l = 0; l < it->second.second && err == cudaSuccess; ++l) {
-                    const int32_t* row = b->d_sched + it->second.first + (size_t)l * 2 * slots;
-                    s.slot_job = row;
-                    s.slot_steps = row + slots;
-                    err = b->launch(bk, s);
-                    ++b->last_launches;
-                }
+                if (fan && err == cudaSuccess) err = cudaEventRecord(b->side_done[k], on);
             }
+            for (size_t k = 0; fan && k < nbk && err == cudaSuccess; ++k)
+                err = cudaStreamWaitEvent(b->stream, b->side_done[k], 0);
         }
         cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
         CK(err);
