@@ -70,7 +70,9 @@ enum posi_evolution {
     POSI_EVO_LECONTE2011 = 1,
     POSI_EVO_BARAFFE1998 = 2,
     POSI_EVO_BARAFFE2015 = 3,
-    POSI_EVO_LECONTE_CHABRIER2013 = 4     /* LeconteChabrier2013(false) */
+    POSI_EVO_LECONTE_CHABRIER2013 = 4,    /* LeconteChabrier2013(false) */
+    POSI_EVO_BOLMONT_MATHIS2016 = 5,      /* dynamical tides (a tidal host only); its */
+    POSI_EVO_GALLET_BOLMONT2017 = 6       /* table's 4th column holds inverse_tidal_q_factor */
 };
 
 enum posi_sys_i64_field {
@@ -145,6 +147,10 @@ enum posi_body_f64_field {
     /* wind (src/effects/wind.rs:6-15): input k_factor, rotation_saturation,
      * internal rotation_saturation_2 */
     POSI_BF_WIND_K, POSI_BF_WIND_RSAT, POSI_BF_WIND_RSAT2,
+    /* ConstantTimeLag input dissipation_factor and dissipation_factor_scale
+     * (src/effects/tides/constant_time_lag.rs:13-19), read by the dynamical
+     * tide of a BolmontMathis2016 / GalletBolmont2017 host */
+    POSI_BF_DISS_FACTOR, POSI_BF_DISS_SCALE,
     POSI_BF_COUNT
 };
 

@@ -20,7 +20,10 @@ EVOLUTION_CODES = {
     "Leconte2011": L.EVO_LECONTE2011,
     "Baraffe1998": L.EVO_BARAFFE1998,
     "Baraffe2015": L.EVO_BARAFFE2015,
+    "BolmontMathis2016": L.EVO_BOLMONT_MATHIS2016,
+    "GalletBolmont2017": L.EVO_GALLET_BOLMONT2017,
 }
+DYNAMICAL = (L.EVO_BOLMONT_MATHIS2016, L.EVO_GALLET_BOLMONT2017)
 
 
 class Unsupported(ValueError):
@@ -151,6 +154,10 @@ def load_case(path_or_dict):
         evo_ev = _evolution_code(ev["evolution"])
         if evo_code != evo_ev:
             raise Unsupported("particle and evolver evolution types differ")
+        if evo_code in DYNAMICAL and (b != host or not ce["tides"] or tk != L.EFFECT_CENTRAL):
+            # the planet-dependent branch keeps stale entries in the reference
+            # (src/effects/tides/constant_time_lag.rs:131-135 removes the host's key)
+            raise Unsupported("dynamical-tide evolution on a body other than the tidal host")
         bi[b, L.BI_EVO_TYPE] = evo_code
         bi[b, L.BI_EVO_LEFT] = int(ev["left_index"])
         nrow = len(ev["time"])
@@ -162,6 +169,12 @@ def load_case(path_or_dict):
                 block[2 * nrow:3 * nrow] = ev["radius_of_gyration_2"]
             if len(ev["love_number"]) == nrow:
                 block[3 * nrow:4 * nrow] = ev["love_number"]
+            if evo_code in DYNAMICAL:
+                # the dynamical-tide evolutions interpolate no Love number:
+                # their 4th column holds the inverse tidal Q factor
+                if len(ev.get("inverse_tidal_q_factor", [])) != nrow:
+                    raise Unsupported("dynamical-tide evolution without its inverse tidal Q factor")
+                block[3 * nrow:4 * nrow] = ev["inverse_tidal_q_factor"]
             bi[b, L.BI_EVO_OFFSET] = off
             bi[b, L.BI_EVO_LEN] = nrow
             tables.append(block)
@@ -172,6 +185,9 @@ def load_case(path_or_dict):
         F[L.BF_RADIUS] = p["radius"]
         F[L.BF_RG2] = p["radius_of_gyration_2"]
         F[L.BF_MOI] = p["moment_of_inertia"]
+        if tparams is not None:
+            F[L.BF_DISS_FACTOR] = tparams["dissipation_factor"]
+            F[L.BF_DISS_SCALE] = tparams["dissipation_factor_scale"]
         F[L.BF_WIND_K] = p["wind"]["parameters"]["input"]["k_factor"]
         F[L.BF_WIND_RSAT] = p["wind"]["parameters"]["input"]["rotation_saturation"]
         F[L.BF_WIND_RSAT2] = p["wind"]["parameters"]["internal"]["rotation_saturation_2"]

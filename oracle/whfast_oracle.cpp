@@ -111,6 +111,8 @@ static const double SPEED_OF_LIGHT_2 = SPEED_OF_LIGHT * SPEED_OF_LIGHT;
 static const double G = G_SI / (AU * AU * AU) * M_SUN * (DAY * DAY);
 static const double K2 = G;
 static const double R_SUN = 6.957e8 / AU;
+static const double SUN_DYN_FREQ_2 = K2 / (R_SUN * R_SUN * R_SUN);
+static const double SMOOTHING_FACTOR_DYN_TIDE_COROTATION = 1.0e-5 * 86400.;
 static const double MAX_DISTANCE = 100.;
 static const double MAX_DISTANCE_2 = MAX_DISTANCE * MAX_DISTANCE;
 
@@ -124,6 +126,11 @@ struct Tides {
     real rscal_star = 0., rscal_planet = 0.;
     real ortho_star = 0., ortho_planet = 0., radial = 0., radial_diss_pm = 0.;
     real denergy_dt = 0., lag_angle = 0.;
+    real diss_factor = 0., diss_scale = 0.;   // ConstantTimeLag inputs (:13-19)
+    // the host's pair-dependent dissipation factor for this body (:20-93);
+    // unset (false) when the dynamical tide is not excited
+    bool pair_set = false;
+    real pair_sigma = 0.;
     V3 out_acc{0., 0., 0.}, out_dldt{0., 0., 0.};
     V3 pos{0., 0., 0.}, vel{0., 0., 0.};
 };
@@ -295,10 +302,35 @@ static void non_spin_dependent_evolving_quantities(Sim& s, real t) {
     }
 }
 
-// src/effects/evolution.rs:548-567: only the dynamical-tide evolutions set a
-// non-zero lag angle, and those are outside this path.
-static void spin_dependent_evolving_quantities(Sim& s, real) {
-    for (int i = 0; i < s.n; ++i) s.p[i].tides.lag_angle = 0.;
+static bool dynamical(int type) {
+    return type == POSI_EVO_BOLMONT_MATHIS2016 || type == POSI_EVO_GALLET_BOLMONT2017;
+}
+
+// src/effects/evolution.rs:487-512 (the 4th table column of a dynamical-tide
+// evolution holds the inverse tidal Q factor)
+static real evolver_inverse_tidal_q_factor(Evolver& e, real t, real current) {
+    if (dynamical(e.type)) {
+        int64_t i0 = evolver_idx(e), left = 0;
+        real r = linear_interpolation(t, e.time + i0, e.love + i0, e.len - i0, &left);
+        e.left_index += left;
+        return r;
+    }
+    return current;
+}
+
+// src/effects/evolution.rs:548-567
+static void spin_dependent_evolving_quantities(Sim& s, real t) {
+    for (int i = 0; i < s.n; ++i) {
+        Particle& q = s.p[i];
+        Evolver& e = s.ev[i];
+        if (dynamical(e.type)) {
+            real inverse_tidal_q_factor = evolver_inverse_tidal_q_factor(e, t, 0.);
+            real epsilon_squared = q.nsv2 / SUN_DYN_FREQ_2;
+            q.tides.lag_angle = real(3.0) * epsilon_squared * inverse_tidal_q_factor / real(4.0);
+        } else {
+            q.tides.lag_angle = 0.;
+        }
+    }
 }
 
 // src/particles/universe.rs:305-316
@@ -481,6 +513,54 @@ static void initialize(Sim& s, bool dl, bool acc) {
 // ---------------------------------------------------------------------------
 // :206-264 (the pair-dependent dissipation factor is the particle's own for
 // every non-dynamical evolution, :144-165)
+// src/tools.rs:251-285
+static void perihelion_distance_and_eccentricity(real gm, V3 p, V3 v, real* q, real* e) {
+    real hx = p.y * v.z - p.z * v.y;
+    real hy = p.z * v.x - p.x * v.z;
+    real hz = p.x * v.y - p.y * v.x;
+    real h2 = real(std::pow(dv(hx), 2.)) + real(std::pow(dv(hy), 2.)) + real(std::pow(dv(hz), 2.));
+    real v2 = v.x * v.x + v.y * v.y + v.z * v.z;
+    real r = rsqrt_(p.x * p.x + p.y * p.y + p.z * p.z);
+    real sv = h2 / gm;
+    real temp = real(1.) + sv * (v2 / gm - real(2.) / r);
+    *e = temp <= real(0.) ? real(0.) : rsqrt_(temp);
+    *q = sv / (real(1.) + *e);
+}
+
+// src/effects/tides/constant_time_lag.rs:20-93: the host's dissipation factor
+// for each orbiting body when the host's evolution has a dynamical tide (the
+// planet-dependent branch, :95-140, is refused by the loader)
+static void pair_dependent_scaled_dissipation_factors(Sim& s) {
+    Particle& h = s.p[s.host];
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        q.tides.pair_set = false;
+        if (!dynamical(s.ev[s.host].type) || q.tides.kind != POSI_EFFECT_ORBITING) continue;
+        real host_norm_spin_vector = rsqrt_(h.nsv2);
+        real scale = h.tides.kind == POSI_EFFECT_CENTRAL ? h.tides.diss_scale : real(0.);
+        real factor = h.tides.kind == POSI_EFFECT_CENTRAL ? h.tides.diss_factor : real(0.);
+        real gm = h.mass_g + q.mass_g;
+        real peri, ecc;
+        perihelion_distance_and_eccentricity(gm, q.tides.pos, q.tides.vel, &peri, &ecc);
+        real mean_motion = rsqrt_(gm) * real(std::pow(dv(peri / (real(1.0) - ecc)), -1.5));
+        real half = rabs(host_norm_spin_vector - mean_motion);
+        if (half < host_norm_spin_vector) {
+            if (half < SMOOTHING_FACTOR_DYN_TIDE_COROTATION) half = SMOOTHING_FACTOR_DYN_TIDE_COROTATION;
+            real inv = real(1.) / half;
+            q.tides.pair_sigma = scale * (real(2.0) * K2 / (real(3.0) * powi(h.radius, 5)) * h.tides.lag_angle * inv + factor);
+            q.tides.pair_set = true;
+        }
+    }
+}
+
+// :144-165 get_pair_dependent_scaled_dissipation_factor_or_else for the host
+static real host_sigma_for(const Sim& s, const Particle& q) {
+    const Particle& h = s.p[s.host];
+    if (dynamical(s.ev[s.host].type) && q.tides.pair_set) return q.tides.pair_sigma;
+    return h.tides.scaled_dissipation_factor;
+}
+
 static void tides_orthogonal(Sim& s) {
     Particle& h = s.p[s.host];
     for (int pass = 0; pass < 2; ++pass) {
@@ -491,7 +571,7 @@ static void tides_orthogonal(Sim& s) {
             if (q.tides.kind != POSI_EFFECT_ORBITING) continue;
             real distance_7 = powi(q.tides.distance, 7);
             if (central_body) {
-                q.tides.ortho_star = real(4.5) * powi(q.mass, 2) * powi(h.radius, 10) * h.tides.scaled_dissipation_factor / distance_7;
+                q.tides.ortho_star = real(4.5) * powi(q.mass, 2) * powi(h.radius, 10) * host_sigma_for(s, q) / distance_7;
             } else {
                 q.tides.ortho_planet = real(4.5) * powi(h.mass, 2) * powi(q.radius, 10) * q.tides.scaled_dissipation_factor / distance_7;
             }
@@ -512,7 +592,7 @@ static void tides_radial(Sim& s) {
         real conservative = real(-3.0) * K2 / powi(q.tides.distance, 7)
             * (particle_mass_2 * powi(h.radius, 5) * host_love + host_mass_2 * powi(q.radius, 5) * q.tides.love_number);
         real factor1 = real(-13.5) * q.tides.radial_velocity / powi(q.tides.distance, 8);
-        real term1 = particle_mass_2 * powi(h.radius, 10) * h.tides.scaled_dissipation_factor;
+        real term1 = particle_mass_2 * powi(h.radius, 10) * host_sigma_for(s, q);
         real term2 = host_mass_2 * powi(q.radius, 10) * q.tides.scaled_dissipation_factor;
         q.tides.radial_diss_pm = factor1 * term2;
         real dissipative = q.tides.radial_diss_pm + factor1 * term1;
@@ -1134,6 +1214,7 @@ static void calculate_additional_effects(Sim& s, real t, bool evolution, bool dl
     if (dl && s.wind) calculate_wind_factor(s);
     if (s.tides || s.flat) {
         if ((dl && (s.tides || s.flat)) || (acc && (s.tides || s.flat || s.gr))) {
+            pair_dependent_scaled_dissipation_factors(s);
             if (s.tides) tides_orthogonal(s);
             if (s.flat) flat_orthogonal(s);
             if (acc && (s.tides || s.flat)) {
@@ -1838,6 +1919,8 @@ static void load(Sim& s, int64_t nmax, const int64_t* si, const double* sf, cons
         q.flat.love_number = F[POSI_BF_K2F];
         q.gr.kind = (int)I[POSI_BI_GR_KIND];
         q.wind_kind = (int)I[POSI_BI_WIND_KIND];
+        q.tides.diss_factor = F[POSI_BF_DISS_FACTOR];
+        q.tides.diss_scale = F[POSI_BF_DISS_SCALE];
         q.wind_k = F[POSI_BF_WIND_K];
         q.wind_rsat = F[POSI_BF_WIND_RSAT];
         q.wind_rsat2 = F[POSI_BF_WIND_RSAT2];

@@ -86,6 +86,8 @@ int evolution_code(Ctx& c, const json::Value* e) {
     if (name == "Leconte2011") return POSI_EVO_LECONTE2011;
     if (name == "Baraffe1998") return POSI_EVO_BARAFFE1998;
     if (name == "Baraffe2015") return POSI_EVO_BARAFFE2015;
+    if (name == "BolmontMathis2016") return POSI_EVO_BOLMONT_MATHIS2016;
+    if (name == "GalletBolmont2017") return POSI_EVO_GALLET_BOLMONT2017;
     if (name == "LeconteChabrier2013") {
         if (arg.kind == json::Value::Bool && arg.b) {
             c.fail(POSI_ERR_UNSUPPORTED, "LeconteChabrier2013(true) dynamical tides");
@@ -250,6 +252,13 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
         I[POSI_BI_TIDES_KIND] = tk;
         I[POSI_BI_FLAT_KIND] = fk;
         I[POSI_BI_GR_KIND] = gk;
+        const bool dynamical = evo_p == POSI_EVO_BOLMONT_MATHIS2016 || evo_p == POSI_EVO_GALLET_BOLMONT2017;
+        if (dynamical && (b != host || !tides || tk != POSI_EFFECT_CENTRAL)) {
+            // the planet-dependent branch keeps stale entries in the reference
+            // (src/effects/tides/constant_time_lag.rs:131-135 removes the host's key)
+            err = "dynamical-tide evolution on a body other than the tidal host";
+            return POSI_ERR_UNSUPPORTED;
+        }
         I[POSI_BI_EVO_TYPE] = evo_p;
         I[POSI_BI_EVO_LEFT] = (int64_t)num(c, &ev, "left_index");
         const json::Value* tt = req(c, &ev, "time");
@@ -258,7 +267,10 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
         if (evo_p != POSI_EVO_NON_EVOLVING && rows > 0) {
             const size_t off = out.tables.size();
             out.tables.resize(off + 4 * (size_t)rows, 0.);
-            const char* names[4] = {"time", "radius", "radius_of_gyration_2", "love_number"};
+            // the dynamical-tide evolutions interpolate no Love number: their
+            // 4th column holds the inverse tidal Q factor
+            const char* names[4] = {"time", "radius", "radius_of_gyration_2",
+                                    dynamical ? "inverse_tidal_q_factor" : "love_number"};
             for (int k = 0; k < 4; ++k) {
                 const json::Value* col = req(c, &ev, names[k]);
                 if (!col || !col->is_array()) continue;
@@ -306,6 +318,8 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
             axes(c, tout, "dangular_momentum_dt", &F[POSI_BF_TD_LX]);
         }
         F[POSI_BF_K2] = tparams ? num(c, tparams, "love_number") : 0.;
+        F[POSI_BF_DISS_FACTOR] = tparams ? num(c, tparams, "dissipation_factor") : 0.;
+        F[POSI_BF_DISS_SCALE] = tparams ? num(c, tparams, "dissipation_factor_scale") : 0.;
         F[POSI_BF_K2F] = fparams ? num(c, fparams, "love_number") : 0.;
         if (c.code != POSI_OK) { err = c.err; return c.code; }
     }

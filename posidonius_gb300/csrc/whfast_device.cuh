@@ -72,6 +72,22 @@ constexpr double kMINUS_3K2 = -3.0 * kK2;
 constexpr double kFA = kG / kC2;
 constexpr double kTWO_PI = 2. * kPI;
 constexpr double kR_SUN = 6.957e8 / kAU;
+constexpr double kSUN_DYN_FREQ_2 = kK2 / (kR_SUN * kR_SUN * kR_SUN);
+constexpr double kSMOOTHING_DYN_TIDE = 1.0e-5 * 86400.;
+
+// y^(-3/2) for the dynamical tide's mean motion (the reference's
+// powf(-1.5)): 1 / (y sqrt(y)) carried to about 100 bits in double-double
+// (sqrt's residual and the products' low parts by FMA) and rounded once, so
+// the result is the correctly rounded power except in vanishingly rare cases.
+__device__ __forceinline__ double pow_m1p5(double y) {
+    const double s = sqrt(y);
+    const double sl = fma(-s, s, y) / (2. * s);   // sqrt(y) = s + sl
+    const double th = y * s;
+    const double tl = fma(y, s, -th) + y * sl;    // y^1.5 = th + tl
+    const double q = 1. / th;
+    const double e = fma(-th, q, 1.) - tl * q;    // 1 - (th + tl) q
+    return fma(q, e, q);
+}
 constexpr int kNMAX_QUART = 64;
 constexpr int kNMAX_NEWT = 32;
 constexpr int kMIDPOINT_MIN = 3;
@@ -151,7 +167,8 @@ struct GroupSmem {
 
 // host card slots
 enum { HC_PX = 0, HC_PY, HC_PZ, HC_VX, HC_VY, HC_VZ, HC_SX, HC_SY, HC_SZ, HC_NSV2, HC_M, HC_MG, HC_R,
-       HC_SIG, HC_K2, HC_K2F, HC_MOI, HC_AM, HC_SLX, HC_SLY, HC_SLZ, HC_COUNT };
+       HC_SIG, HC_K2, HC_K2F, HC_MOI, HC_AM, HC_SLX, HC_SLY, HC_SLZ,
+       HC_LAG, HC_DFAC, HC_DSCALE, HC_COUNT };
 static_assert(HC_COUNT <= kCARD, "host card");
 
 struct Body {
@@ -164,6 +181,7 @@ struct Body {
     int tk, fk, gk, evo;
     int wk;                              // wind: 1 Interaction
     double wind_k, wind_rsat, wind_rsat2;
+    double diss_factor, diss_scale;      // ConstantTimeLag inputs (dynamical tide of a host)
     int64_t eoff, elen, eleft;
     // alternative (Jacobi / democratic-heliocentric / WHDS) coordinates
     double am, amg, ap[3], av[3], aacc[3];
@@ -175,6 +193,7 @@ struct Sys {
     int s, n, host, coords, lane;
     bool tides, flat, gr, evo, spin_on, wind;
     int gr_impl;     // posi_gr_impl; grk(): Kidder1995, the per-planet formulation
+    bool dyn_host;   // the tidal host's evolution has a dynamical tide
     __device__ __forceinline__ bool grk() const { return gr && gr_impl == POSI_GR_KIDDER1995; }
     unsigned mask;
     double dt, half_dt, t, time_limit, last_hist, hist_period, last_rec, rec_period;
@@ -214,6 +233,9 @@ struct Sys {
     __device__ __forceinline__ double& P(int slot) const { return pcs[slot * G + lane]; }
     __device__ __forceinline__ bool fatal() const { return (status & POSI_SYS_FATAL_MASK) != 0; }
     __device__ __forceinline__ bool planet() const { return has && !is_host; }
+    __device__ static __forceinline__ bool dynamical_evo(int e) {
+        return e == POSI_EVO_BOLMONT_MATHIS2016 || e == POSI_EVO_GALLET_BOLMONT2017;
+    }
 
 #if !POSI_EXACT
     // group collectives over the G lanes of this system
@@ -324,13 +346,17 @@ struct Sys {
             b.wind_k = F[POSI_BF_WIND_K * st];
             b.wind_rsat = F[POSI_BF_WIND_RSAT * st];
             b.wind_rsat2 = F[POSI_BF_WIND_RSAT2 * st];
+            b.diss_factor = F[POSI_BF_DISS_FACTOR * st];
+            b.diss_scale = F[POSI_BF_DISS_SCALE * st];
             b.evo = (int)I[POSI_BI_EVO_TYPE * st];
             b.eoff = I[POSI_BI_EVO_OFFSET * st];
             b.elen = I[POSI_BI_EVO_LEN * st];
             b.eleft = I[POSI_BI_EVO_LEFT * st];
             if (b.elen <= 0) b.evo = POSI_EVO_NON_EVOLVING;
         }
+        if (is_host) isc[5] = (tides && dynamical_evo(b.evo)) ? 1 : 0;
         sync();
+        dyn_host = isc[5] != 0;
 #if !POSI_EXACT
         mass_constants();
         pc_valid = false;
@@ -498,8 +524,43 @@ struct Sys {
 #endif
                 b.nsv2 = powi<2>(b.S[0]) + powi<2>(b.S[1]) + powi<2>(b.S[2]);
             }
-            if (evolution && evo) b.lag = 0.;
+            // src/effects/evolution.rs:548-567 (the dynamical-tide table's 4th
+            // column is the inverse tidal Q factor, src/effects/evolution.rs:487-512)
+            if (evolution && evo) {
+                if (dynamical_evo(b.evo)) {
+                    const double inverse_tidal_q_factor = interp(D, tt, 3);
+                    const double epsilon_squared = b.nsv2 / kSUN_DYN_FREQ_2;
+                    b.lag = 3.0 * epsilon_squared * inverse_tidal_q_factor / 4.0;
+                } else {
+                    b.lag = 0.;
+                }
+            }
         }
+    }
+
+    // src/effects/tides/constant_time_lag.rs:20-93 with src/tools.rs:251-285:
+    // the host's dissipation factor for this planet when the host's dynamical
+    // tide is excited, else its own (x: heliocentric position, v: heliocentric
+    // velocity; the host's values from the card)
+    __device__ double host_sigma_for(double x, double y, double z, double u, double v, double w) const {
+        const double host_norm_spin_vector = sqrt(card[HC_NSV2]);
+        const double gm = card[HC_MG] + b.mg;
+        const double hx = y * w - z * v;
+        const double hy = z * u - x * w;
+        const double hz = x * v - y * u;
+        const double h2 = hx * hx + hy * hy + hz * hz;   // powf(2.): the exact square, rounded once
+        const double v2 = u * u + v * v + w * w;
+        const double r = sqrt(x * x + y * y + z * z);
+        const double sv = h2 / gm;
+        const double temp = 1. + sv * (v2 / gm - 2. / r);
+        const double ecc = temp <= 0. ? 0. : sqrt(temp);
+        const double peri = sv / (1. + ecc);
+        const double mean_motion = sqrt(gm) * pow_m1p5(peri / (1.0 - ecc));
+        double half = fabs(host_norm_spin_vector - mean_motion);
+        if (!(half < host_norm_spin_vector)) return card[HC_SIG];
+        if (half < kSMOOTHING_DYN_TIDE) half = kSMOOTHING_DYN_TIDE;
+        const double inv = 1. / half;
+        return card[HC_DSCALE] * (2.0 * kK2 / (3.0 * powi<5>(card[HC_R])) * card[HC_LAG] * inv + card[HC_DFAC]);
     }
 
     __device__ void zero_inertia_check() {
@@ -1043,7 +1104,7 @@ struct Sys {
         if (fatal()) return;
         if (is_host) {
             card[HC_SX] = b.S[0]; card[HC_SY] = b.S[1]; card[HC_SZ] = b.S[2];
-            card[HC_NSV2] = b.nsv2; card[HC_R] = b.R; card[HC_MOI] = b.moi;
+            card[HC_NSV2] = b.nsv2; card[HC_R] = b.R; card[HC_MOI] = b.moi; card[HC_LAG] = b.lag;
         }
         sync();
         if (it == 0 && planet()) planet_constants();
@@ -1061,11 +1122,20 @@ struct Sys {
         if (planet()) {
             const double inv_m = 1. / b.m;
             if (tides && b.tk == POSI_EFFECT_ORBITING) {
-                const double o_s = P(PC_OS), o_p = P(PC_OP), osd = P(PC_OSD), opd = P(PC_OPD);
+                double o_s = P(PC_OS), osd = P(PC_OSD), term1 = P(PC_TERM1);
+                const double o_p = P(PC_OP), opd = P(PC_OPD);
+                if (dyn_host) {
+                    // the host's dissipation factor for this planet, per evaluation
+                    const double sh = host_sigma_for(x, y, z, hv[0], hv[1], hv[2]);
+                    const double hR = card[HC_R];
+                    o_s = 4.5 * powi<2>(b.m) * powi<10>(hR) * sh / powi<7>(d);
+                    osd = o_s / d;
+                    term1 = (b.m * b.m) * powi<10>(hR) * sh;
+                }
                 // radial component (constant_time_lag.rs:266-307)
                 const double factor1 = -13.5 * vr / P(PC_D8);
                 const double diss_pm = factor1 * P(PC_TERM2);
-                const double radial = P(PC_CONS) + (diss_pm + factor1 * P(PC_TERM1));
+                const double radial = P(PC_CONS) + (diss_pm + factor1 * term1);
                 // force (constant_time_lag.rs:309-332)
                 const double factor3 = radial + (o_s + o_p) * vr / d;
                 double F[3];
@@ -1274,7 +1344,7 @@ struct Sys {
         if (fatal()) return;
         if (is_host) {
             card[HC_SX] = b.S[0]; card[HC_SY] = b.S[1]; card[HC_SZ] = b.S[2];
-            card[HC_NSV2] = b.nsv2; card[HC_R] = b.R; card[HC_MOI] = b.moi;
+            card[HC_NSV2] = b.nsv2; card[HC_R] = b.R; card[HC_MOI] = b.moi; card[HC_LAG] = b.lag;
             card[HC_SLX] = b.moi * b.S[0]; card[HC_SLY] = b.moi * b.S[1]; card[HC_SLZ] = b.moi * b.S[2];
         }
         sync();
@@ -1291,16 +1361,28 @@ struct Sys {
             const double h1 = z * hv0 - x * hv2;
             const double h2 = x * hv1 - y * hv0;
             if (tides && b.tk == POSI_EFFECT_ORBITING) {
-                const double osd = P(PC_OSD), opd = P(PC_OPD);
+                double osd = P(PC_OSD), t12 = P(PC_T12), ospd = P(PC_OSPD), os_ = P(PC_OS), osdd = P(PC_OSDD);
+                const double opd = P(PC_OPD);
+                if (dyn_host) {
+                    // the host's dissipation factor for this planet, per evaluation
+                    const double sh = host_sigma_for(x, y, z, hv0, hv1, hv2);
+                    const double id = P(PC_INV_D), id2 = id * id, id7 = id2 * id2 * id2 * id;
+                    const double term1 = (b.m * b.m) * powi<10>(card[HC_R]) * sh;
+                    os_ = 4.5 * term1 * id7;
+                    osd = os_ * id;
+                    ospd = (os_ + P(PC_OP)) * id;
+                    osdd = os_ * P(PC_D);
+                    t12 = term1 + P(PC_TERM2);
+                }
                 const double factor1 = vr * P(PC_C13);
-                const double radial = P(PC_CONS) + factor1 * P(PC_T12);
-                const double factor3 = radial + P(PC_OSPD) * vr;
+                const double radial = P(PC_CONS) + factor1 * t12;
+                const double factor3 = radial + ospd * vr;
                 const double F0 = factor3 * xd + osd * (hS1 * z - hS2 * y - hv0) + opd * (S1 * z - S2 * y - hv0);
                 const double F1 = factor3 * yd + osd * (hS2 * x - hS0 * z - hv1) + opd * (S2 * x - S0 * z - hv1);
                 const double F2 = factor3 * zd + osd * (hS0 * y - hS1 * x - hv2) + opd * (S0 * y - S1 * x - hv2);
                 aa0 += inv_m * F0; aa1 += inv_m * F1; aa2 += inv_m * F2;
-                const double qp = P(PC_OP) * rs_p, qs = P(PC_OS) * rs_s;
-                const double opdd = P(PC_OPDD), osdd = P(PC_OSDD);
+                const double qp = P(PC_OP) * rs_p, qs = os_ * rs_s;
+                const double opdd = P(PC_OPDD);
                 dl0 -= opdd * S0 - qp * xd - opd * h0;
                 dl1 -= opdd * S1 - qp * yd - opd * h1;
                 dl2 -= opdd * S2 - qp * zd - opd * h2;
@@ -1409,7 +1491,8 @@ struct Sys {
         sync();
         if (is_host) { card[HC_PX] = b.r[0]; card[HC_PY] = b.r[1]; card[HC_PZ] = b.r[2];
                        card[HC_M] = b.m; card[HC_MG] = b.mg; card[HC_R] = b.R; card[HC_SIG] = b.sig;
-                       card[HC_K2] = b.k2; card[HC_K2F] = b.k2f; }
+                       card[HC_K2] = b.k2; card[HC_K2F] = b.k2f;
+                       card[HC_DFAC] = b.diss_factor; card[HC_DSCALE] = b.diss_scale; }
         sync();
 #if POSI_EXACT
         if (planet()) set_geometry(b.r[0] - card[HC_PX], b.r[1] - card[HC_PY], b.r[2] - card[HC_PZ]);
@@ -2307,7 +2390,8 @@ __global__ void __launch_bounds__(128) additional_effects_kernel(Dev D, double t
     S.sync();
     if (S.is_host) { S.card[HC_PX] = S.b.r[0]; S.card[HC_PY] = S.b.r[1]; S.card[HC_PZ] = S.b.r[2];
                      S.card[HC_M] = S.b.m; S.card[HC_MG] = S.b.mg; S.card[HC_R] = S.b.R; S.card[HC_SIG] = S.b.sig;
-                     S.card[HC_K2] = S.b.k2; S.card[HC_K2F] = S.b.k2f; }
+                     S.card[HC_K2] = S.b.k2; S.card[HC_K2F] = S.b.k2f;
+                     S.card[HC_DFAC] = S.b.diss_factor; S.card[HC_DSCALE] = S.b.diss_scale; }
     S.sync();
     if (S.planet()) S.set_geometry(S.b.r[0] - S.card[HC_PX], S.b.r[1] - S.card[HC_PY], S.b.r[2] - S.card[HC_PZ]);
     S.additional_effects(D, 0, evolution != 0);
