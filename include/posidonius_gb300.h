@@ -32,7 +32,7 @@ enum posi_status {
     POSI_ERR_ARG = -1,           /* bad argument / null pointer */
     POSI_ERR_IO = -2,            /* file missing or unreadable (src/integrator/output.rs:178-203) */
     POSI_ERR_PARSE = -3,         /* malformed JSON case */
-    POSI_ERR_UNSUPPORTED = -4,   /* case uses an effect outside this path (Kaula, creep, disk,
+    POSI_ERR_UNSUPPORTED = -4,   /* case uses an effect outside this path (Kaula, creep,
                                     dynamic tides, non-WHFast integrator, ...) */
     POSI_ERR_CUDA = -5,          /* CUDA runtime error or no device */
     POSI_ERR_PHYSICS = -6,       /* a system hit a reference panic (see posi_system_status) */
@@ -92,6 +92,7 @@ enum posi_sys_i64_field {
     POSI_SI_LAST_MIDPOINT_ITERS, /* midpoint iterations of the last half kick */
     POSI_SI_GR_IMPL,             /* Universe.general_relativity_implementation (posi_gr_impl) */
     POSI_SI_WIND,                /* ConsiderEffects.wind */
+    POSI_SI_DISK,                /* ConsiderEffects.disk */
     POSI_SI_COUNT
 };
 
@@ -117,6 +118,7 @@ enum posi_body_i64_field {
     POSI_BI_EVO_LEN,             /* rows per table (time, radius, rg2, love: 4*len doubles) */
     POSI_BI_EVO_LEFT,            /* Evolver.left_index */
     POSI_BI_WIND_KIND,           /* WindEffect: 1 Interaction, 0 Disabled */
+    POSI_BI_DISK_KIND,           /* DiskEffect: posi_effect_kind */
     POSI_BI_COUNT
 };
 
@@ -151,6 +153,10 @@ enum posi_body_f64_field {
      * (src/effects/tides/constant_time_lag.rs:13-19), read by the dynamical
      * tide of a BolmontMathis2016 / GalletBolmont2017 host */
     POSI_BF_DISS_FACTOR, POSI_BF_DISS_SCALE,
+    /* DiskProperties of a disk host (src/effects/disk.rs:6-14) */
+    POSI_BF_DISK_INNER, POSI_BF_DISK_OUTER, POSI_BF_DISK_LIFETIME, POSI_BF_DISK_ALPHA,
+    POSI_BF_DISK_SIGMA0, POSI_BF_DISK_MU,
+    POSI_BF_DISK_MTS,                            /* disk migration_timescale of the last evaluation (history output) */
     POSI_BF_COUNT
 };
 

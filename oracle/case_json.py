@@ -71,15 +71,14 @@ def load_case(path_or_dict):
     u = d["universe"]
     n = int(u["n_particles"])
     ce = u["consider_effects"]
-    if ce["disk"]:
-        raise Unsupported("disk effect")
+
     gr_impl = u["general_relativity_implementation"]
     gr_codes = {"Kidder1995": L.GR_KIDDER1995, "Anderson1975": L.GR_ANDERSON1975, "Newhall1983": L.GR_NEWHALL1983}
     if ce["general_relativity"] and gr_impl not in gr_codes:
         raise Unsupported(f"general relativity {gr_impl}")
     hosts = u["hosts"]
     host = int(hosts["index"]["most_massive"])
-    for eff in ("tides", "rotational_flattening", "general_relativity"):
+    for eff in ("tides", "rotational_flattening", "general_relativity", "disk"):
         if ce[eff] and int(hosts["index"][eff]) != host:
             raise Unsupported(f"{eff} host is not the most massive body")
 
@@ -96,6 +95,7 @@ def load_case(path_or_dict):
     si[L.SI_GR] = int(ce["general_relativity"])
     si[L.SI_GR_IMPL] = gr_codes.get(gr_impl, L.GR_KIDDER1995)
     si[L.SI_WIND] = int(ce["wind"])
+    si[L.SI_DISK] = int(ce["disk"])
     si[L.SI_EVOLUTION] = int(ce["evolution"])
     si[L.SI_ITERATION] = int(d["current_iteration"])
     si[L.SI_N_HIST] = int(d["n_historic_snapshots"])
@@ -150,6 +150,11 @@ def load_case(path_or_dict):
         bi[b, L.BI_FLAT_KIND] = fk
         bi[b, L.BI_GR_KIND] = gk
         bi[b, L.BI_WIND_KIND] = wk
+        dk, dprops = _effect(p["disk"]["effect"], None)
+        if ce["disk"] and b == host and dk != L.EFFECT_CENTRAL:
+            raise Unsupported("disk host is not a central body")
+        bi[b, L.BI_DISK_KIND] = dk
+        bf[b, L.BF_DISK_MTS] = p["disk"]["parameters"]["internal"]["migration_timescale"]
         evo_code = _evolution_code(p["evolution"])
         evo_ev = _evolution_code(ev["evolution"])
         if evo_code != evo_ev:
@@ -188,6 +193,12 @@ def load_case(path_or_dict):
         if tparams is not None:
             F[L.BF_DISS_FACTOR] = tparams["dissipation_factor"]
             F[L.BF_DISS_SCALE] = tparams["dissipation_factor_scale"]
+        if dk == L.EFFECT_CENTRAL:
+            for f, key in ((L.BF_DISK_INNER, "inner_edge_distance"), (L.BF_DISK_OUTER, "outer_edge_distance"),
+                           (L.BF_DISK_LIFETIME, "lifetime"), (L.BF_DISK_ALPHA, "alpha"),
+                           (L.BF_DISK_SIGMA0, "surface_density_normalization"),
+                           (L.BF_DISK_MU, "mean_molecular_weight")):
+                F[f] = dprops[key]
         F[L.BF_WIND_K] = p["wind"]["parameters"]["input"]["k_factor"]
         F[L.BF_WIND_RSAT] = p["wind"]["parameters"]["input"]["rotation_saturation"]
         F[L.BF_WIND_RSAT2] = p["wind"]["parameters"]["internal"]["rotation_saturation_2"]

@@ -113,6 +113,8 @@ static const double K2 = G;
 static const double R_SUN = 6.957e8 / AU;
 static const double SUN_DYN_FREQ_2 = K2 / (R_SUN * R_SUN * R_SUN);
 static const double SMOOTHING_FACTOR_DYN_TIDE_COROTATION = 1.0e-5 * 86400.;
+static const double BOLTZMANN_CONSTANT = 1.380649e-23 / (M_SUN * AU * AU) * DAY * DAY;
+static const double MASS_HYDROGEN_ATOM = 1.672162841e-27 / M_SUN;
 static const double MAX_DISTANCE = 100.;
 static const double MAX_DISTANCE_2 = MAX_DISTANCE * MAX_DISTANCE;
 
@@ -150,6 +152,14 @@ struct GR {
     V3 out_acc{0., 0., 0.}, out_dldt{0., 0., 0.};
     V3 pos{0., 0., 0.}, vel{0., 0., 0.};
 };
+// src/effects/disk.rs:6-56
+struct Disk {
+    int kind = POSI_EFFECT_DISABLED;
+    real inner = 0., outer = 0., lifetime = 0., alpha = 0., sigma0 = 0., mu = 0.;   // DiskProperties
+    real distance = 0., nv = 0., nv2 = 0., migration_timescale = 0.;
+    V3 out_acc{0., 0., 0.};
+    V3 pos{0., 0., 0.}, vel{0., 0., 0.};
+};
 // src/particles/particle.rs:16-52
 struct Particle {
     int id = 0;
@@ -164,6 +174,7 @@ struct Particle {
     Tides tides;
     Flat flat;
     GR gr;
+    Disk disk;
     // src/effects/wind.rs:6-40
     int wind_kind = 0;          // 1: Interaction
     real wind_k = 0., wind_rsat = 0., wind_rsat2 = 0.;
@@ -186,7 +197,7 @@ struct AltCoords {
 // src/integrator/whfast.rs:99-120 + src/particles/universe.rs:50-63
 struct Sim {
     int n = 0, host = 0, coords = POSI_JACOBI;
-    bool tides = false, flat = false, gr = false, evolution = false, wind = false;
+    bool tides = false, flat = false, gr = false, evolution = false, wind = false, disk = false;
     int gr_impl = POSI_GR_KIDDER1995;   // Universe.general_relativity_implementation
     real dt = 0., half_dt = 0., t = 0., time_limit = 0.;
     real last_hist = -1., hist_period = 0., last_rec = -1., rec_period = 0.;
@@ -500,6 +511,25 @@ static void initialize(Sim& s, bool dl, bool acc) {
                         q.gr.out_acc = V3{0., 0., 0.}; q.gr.out_dldt = V3{0., 0., 0.};
                     }
                 }
+            }
+        }
+    }
+    // src/effects/disk.rs:83-97, :134-150
+    if (acc && s.disk) {
+        Particle& h = s.p[s.host];
+        if (h.disk.kind == POSI_EFFECT_CENTRAL) {
+            h.disk.pos = h.hr; h.disk.vel = h.hv; h.disk.distance = h.hd; h.disk.nv = h.hnv; h.disk.nv2 = h.hnv2;
+            for (int i = 0; i < s.n; ++i) {
+                if (i == s.host) continue;
+                Particle& q = s.p[i];
+                if (q.disk.kind == POSI_EFFECT_ORBITING) {
+                    q.disk.pos = q.hr; q.disk.vel = q.hv; q.disk.distance = q.hd; q.disk.nv = q.hnv; q.disk.nv2 = q.hnv2;
+                }
+            }
+            h.disk.out_acc = V3{0., 0., 0.};
+            for (int i = 0; i < s.n; ++i) {
+                if (i == s.host) continue;
+                if (s.p[i].disk.kind == POSI_EFFECT_ORBITING) s.p[i].disk.out_acc = V3{0., 0., 0.};
             }
         }
     }
@@ -1186,6 +1216,55 @@ static void calculate_wind_factor(Sim& s) {
     }
 }
 
+// src/effects/disk.rs:154-203 (DiskProperties::calculate_migration_timescale)
+static real disk_migration_timescale(const Disk& dp, real time, real host_mass, real host_mass_g,
+                                     real particle_mass, real distance, real semi_major_axis) {
+    real keplerian_frequency = rsqrt_(host_mass_g / powi(distance, 3));
+    real disk_temperature = real(280.0) * real(std::pow(dv(distance), -0.5)) * host_mass;
+    real speed_of_sound_squared = BOLTZMANN_CONSTANT * disk_temperature / (dp.mu * MASS_HYDROGEN_ATOM);
+    real viscosity = dp.alpha * speed_of_sound_squared / keplerian_frequency;
+    real gas_radial_velocity = real(-3.0) * viscosity / (real(2.0) * semi_major_axis);
+    real initial_density = dp.sigma0 * (real(1.) / distance) * real(std::exp(dv(real(-1.0) * distance / dp.outer))) *
+                           (real(1.0) - rsqrt_(dp.inner / distance));
+    real density = 0.;
+    if (distance > dp.inner) density = initial_density * real(std::exp(dv(-time / dp.lifetime)));
+    real y = real(2.0) * density * powi(semi_major_axis, 2) / particle_mass;
+    real m = y < real(1.0) ? y : real(1.0);   // f64::min(1.0, y)
+    real a_dot = gas_radial_velocity * m;
+    return -semi_major_axis / a_dot;
+}
+
+// src/effects/disk.rs:205-268
+static void disk_interaction_acceleration(Sim& s, real t) {
+    Particle& h = s.p[s.host];
+    if (h.disk.kind != POSI_EFFECT_CENTRAL) return;
+    real factor2 = real(1.) / h.mass;
+    V3 sum{0., 0., 0.};
+    for (int i = 0; i < s.n; ++i) {
+        if (i == s.host) continue;
+        Particle& q = s.p[i];
+        if (q.disk.kind == POSI_EFFECT_ORBITING) {
+            Disk& d = q.disk;
+            real sma = (q.mass_g + h.mass_g) * d.distance / (real(2.0) * (q.mass_g + h.mass_g) - d.distance * d.nv2);
+            d.migration_timescale = disk_migration_timescale(h.disk, t, h.mass, h.mass_g, q.mass, d.distance, sma);
+            real factor1 = real(1.) / q.mass;
+            real factor_migration = -q.mass / d.migration_timescale;
+            real ecc_ts = real(0.1) * d.migration_timescale;
+            real factor_ecc = -q.mass * real(2.0) / ecc_ts;
+            real inc_ts = ecc_ts;
+            real factor_inc = -q.mass * real(2.0) / inc_ts;
+            V3 fm{factor_migration * d.vel.x, factor_migration * d.vel.y, factor_migration * d.vel.z};
+            real sp = real(1.0) / (d.distance * d.distance) * (d.pos.x * d.vel.x + d.pos.y * d.vel.y + d.pos.z * d.vel.z);
+            V3 fe{factor_ecc * sp * d.pos.x, factor_ecc * sp * d.pos.y, factor_ecc * sp * d.pos.z};
+            V3 fi{0.0, 0.0, factor_inc * d.vel.z};
+            V3 ft{fm.x + fe.x + fi.x, fm.y + fe.y + fi.y, fm.z + fe.z + fi.z};
+            sum.x += ft.x; sum.y += ft.y; sum.z += ft.z;
+            d.out_acc = V3{factor1 * ft.x, factor1 * ft.y, factor1 * ft.z};
+        }
+        h.disk.out_acc = V3{real(-1.0) * factor2 * sum.x, real(-1.0) * factor2 * sum.y, real(-1.0) * factor2 * sum.z};
+    }
+}
+
 // src/particles/universe.rs:580-614
 static void calculate_dangular_momentum_dt(Sim& s) {
     for (int i = 0; i < s.n; ++i) {
@@ -1201,6 +1280,7 @@ static void add_additional_acceleration_corrections(Sim& s) {
     for (int i = 0; i < s.n; ++i) {
         Particle& q = s.p[i];
         if (s.tides) { q.a_add.x += q.tides.out_acc.x; q.a_add.y += q.tides.out_acc.y; q.a_add.z += q.tides.out_acc.z; }
+        if (s.disk) { q.a_add.x += q.disk.out_acc.x; q.a_add.y += q.disk.out_acc.y; q.a_add.z += q.disk.out_acc.z; }
         if (s.flat) { q.a_add.x += q.flat.out_acc.x; q.a_add.y += q.flat.out_acc.y; q.a_add.z += q.flat.out_acc.z; }
         if (s.gr) { q.a_add.x += q.gr.out_acc.x; q.a_add.y += q.gr.out_acc.y; q.a_add.z += q.gr.out_acc.z; }
     }
@@ -1213,7 +1293,7 @@ static void calculate_additional_effects(Sim& s, real t, bool evolution, bool dl
     if (s.fatal()) return;
     if (dl && s.wind) calculate_wind_factor(s);
     if (s.tides || s.flat) {
-        if ((dl && (s.tides || s.flat)) || (acc && (s.tides || s.flat || s.gr))) {
+        if ((dl && (s.tides || s.flat)) || (acc && (s.tides || s.disk || s.flat || s.gr))) {
             pair_dependent_scaled_dissipation_factors(s);
             if (s.tides) tides_orthogonal(s);
             if (s.flat) flat_orthogonal(s);
@@ -1240,6 +1320,7 @@ static void calculate_additional_effects(Sim& s, real t, bool evolution, bool dl
             }
         }
     }
+    if (acc && s.disk) disk_interaction_acceleration(s, t);
     if (dl) {
         if (s.tides || s.flat || (s.gr && s.gr_impl == POSI_GR_KIDDER1995) || s.wind) calculate_dangular_momentum_dt(s);
     }
@@ -1800,7 +1881,8 @@ static void write_historic_snapshot(const Sim& s) {
         const real rec[20] = {s.t, s.dt, real((double)q.id), q.r.x, q.r.y, q.r.z, q.spin.x, q.spin.y, q.spin.z,
                               q.v.x, q.v.y, q.v.z, q.mass, q.radius, q.rg2,
                               q.tides.kind != POSI_EFFECT_DISABLED ? q.tides.love_number : real(0.),
-                              q.tides.scaled_dissipation_factor, q.tides.lag_angle, q.tides.denergy_dt, real(0.)};
+                              q.tides.scaled_dissipation_factor, q.tides.lag_angle, q.tides.denergy_dt,
+                              q.disk.migration_timescale};
         for (int k = 0; k < 20; ++k) R[k] = static_cast<double>(rec[k]);
         ++g_hist_len;
     }
@@ -1863,6 +1945,7 @@ static void load(Sim& s, int64_t nmax, const int64_t* si, const double* sf, cons
     s.gr = si[POSI_SI_GR] != 0;
     s.gr_impl = (int)si[POSI_SI_GR_IMPL];
     s.wind = si[POSI_SI_WIND] != 0;
+    s.disk = si[POSI_SI_DISK] != 0;
     s.evolution = si[POSI_SI_EVOLUTION] != 0;
     s.iteration = si[POSI_SI_ITERATION];
     s.n_hist = si[POSI_SI_N_HIST];
@@ -1919,6 +2002,14 @@ static void load(Sim& s, int64_t nmax, const int64_t* si, const double* sf, cons
         q.flat.love_number = F[POSI_BF_K2F];
         q.gr.kind = (int)I[POSI_BI_GR_KIND];
         q.wind_kind = (int)I[POSI_BI_WIND_KIND];
+        q.disk.kind = (int)I[POSI_BI_DISK_KIND];
+        q.disk.inner = F[POSI_BF_DISK_INNER];
+        q.disk.outer = F[POSI_BF_DISK_OUTER];
+        q.disk.lifetime = F[POSI_BF_DISK_LIFETIME];
+        q.disk.alpha = F[POSI_BF_DISK_ALPHA];
+        q.disk.sigma0 = F[POSI_BF_DISK_SIGMA0];
+        q.disk.mu = F[POSI_BF_DISK_MU];
+        q.disk.migration_timescale = F[POSI_BF_DISK_MTS];
         q.tides.diss_factor = F[POSI_BF_DISS_FACTOR];
         q.tides.diss_scale = F[POSI_BF_DISS_SCALE];
         q.wind_k = F[POSI_BF_WIND_K];
@@ -1970,6 +2061,7 @@ static void store(const Sim& s, int64_t nmax, int64_t* si, double* sf, int64_t* 
         F[POSI_BF_DLX] = dv(q.dLdt.x); F[POSI_BF_DLY] = dv(q.dLdt.y); F[POSI_BF_DLZ] = dv(q.dLdt.z);
         F[POSI_BF_DENERGY_DT] = dv(q.tides.denergy_dt);
         F[POSI_BF_LAG_ANGLE] = dv(q.tides.lag_angle);
+        F[POSI_BF_DISK_MTS] = dv(q.disk.migration_timescale);
         F[POSI_BF_TD_DIST] = dv(q.tides.distance);
         F[POSI_BF_TD_VR] = dv(q.tides.radial_velocity);
         F[POSI_BF_TD_ORTHO] = dv(q.tides.ortho_planet);

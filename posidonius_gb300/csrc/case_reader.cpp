@@ -125,7 +125,7 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
     const bool disk = boolean(c, ce, "disk");
     const bool wind = boolean(c, ce, "wind");
     const bool evo = boolean(c, ce, "evolution");
-    if (disk) c.fail(POSI_ERR_UNSUPPORTED, "the disk effect is outside this path");
+
     const json::Value* gri = req(c, u, "general_relativity_implementation");
     int gr_code = POSI_GR_KIDDER1995;
     std::string gr_name = gri && gri->is_string() ? gri->text : std::string();
@@ -140,6 +140,8 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
         c.fail(POSI_ERR_UNSUPPORTED, "flattening host is not the most massive body");
     if (gr && (int64_t)num(c, hidx, "general_relativity") != host)
         c.fail(POSI_ERR_UNSUPPORTED, "general-relativity host is not the most massive body");
+    if (disk && (int64_t)num(c, hidx, "disk") != host)
+        c.fail(POSI_ERR_UNSUPPORTED, "disk host is not the most massive body");
     if (c.code != POSI_OK) { err = c.err; return c.code; }
     if (host < 0 || host >= n) { err = "host index out of range"; return POSI_ERR_PARSE; }
 
@@ -167,6 +169,7 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
     out.si[POSI_SI_GR] = gr;
     out.si[POSI_SI_GR_IMPL] = gr_code;
     out.si[POSI_SI_WIND] = wind;
+    out.si[POSI_SI_DISK] = disk;
     out.si[POSI_SI_EVOLUTION] = evo;
     out.si[POSI_SI_ITERATION] = (int64_t)num(c, &doc, "current_iteration");
     out.si[POSI_SI_N_HIST] = (int64_t)num(c, &doc, "n_historic_snapshots");
@@ -236,6 +239,31 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
         if (!(wind && wk) && !zero_axes(c, req(c, wpar, "output")))
             c.fail(POSI_ERR_UNSUPPORTED, "stale wind torque output");
         I[POSI_BI_WIND_KIND] = wk;
+        // disk (src/effects/disk.rs:43-47): "Disabled", "OrbitingBody" or
+        // {"CentralBody": DiskProperties}
+        {
+            const json::Value* deff = req(c, req(c, &p, "disk"), "effect");
+            if (c.code != POSI_OK) { err = c.err; return c.code; }
+            int dk = POSI_EFFECT_DISABLED;
+            if (deff->is_string()) {
+                if (deff->text == "OrbitingBody") dk = POSI_EFFECT_ORBITING;
+                else if (deff->text != "Disabled") c.fail(POSI_ERR_PARSE, "unknown disk effect " + deff->text);
+            } else if (deff->is_object() && deff->members.size() == 1 && deff->members[0].first == "CentralBody") {
+                dk = POSI_EFFECT_CENTRAL;
+                const json::Value* dp = &deff->members[0].second;
+                F[POSI_BF_DISK_INNER] = num(c, dp, "inner_edge_distance");
+                F[POSI_BF_DISK_OUTER] = num(c, dp, "outer_edge_distance");
+                F[POSI_BF_DISK_LIFETIME] = num(c, dp, "lifetime");
+                F[POSI_BF_DISK_ALPHA] = num(c, dp, "alpha");
+                F[POSI_BF_DISK_SIGMA0] = num(c, dp, "surface_density_normalization");
+                F[POSI_BF_DISK_MU] = num(c, dp, "mean_molecular_weight");
+            } else {
+                c.fail(POSI_ERR_PARSE, "malformed disk effect");
+            }
+            if (disk && b == host && dk != POSI_EFFECT_CENTRAL) c.fail(POSI_ERR_UNSUPPORTED, "disk host is not a central body");
+            I[POSI_BI_DISK_KIND] = dk;
+            F[POSI_BF_DISK_MTS] = num(c, req(c, req(c, req(c, &p, "disk"), "parameters"), "internal"), "migration_timescale");
+        }
         F[POSI_BF_WIND_K] = num(c, req(c, wpar, "input"), "k_factor");
         F[POSI_BF_WIND_RSAT] = num(c, req(c, wpar, "input"), "rotation_saturation");
         F[POSI_BF_WIND_RSAT2] = num(c, req(c, wpar, "internal"), "rotation_saturation_2");

@@ -1177,7 +1177,8 @@ posi_adjoint* posi_adjoint_create(posi_batch* b, int64_t n_steps, int64_t checkp
             return fail(POSI_ERR_UNSUPPORTED, "the adjoint supports non-evolving bodies only", nullptr);
         if (x[POSI_SI_GR] != 0 && x[POSI_SI_GR_IMPL] != POSI_GR_KIDDER1995)
             return fail(POSI_ERR_UNSUPPORTED, "the adjoint supports Kidder1995 general relativity only", nullptr);
-        if (x[POSI_SI_WIND] != 0) return fail(POSI_ERR_UNSUPPORTED, "the adjoint does not support wind", nullptr);
+        if (x[POSI_SI_WIND] != 0 || x[POSI_SI_DISK] != 0)
+            return fail(POSI_ERR_UNSUPPORTED, "the adjoint does not support wind or disk", nullptr);
         const int G = posi::adjoint_group_size(x[POSI_SI_N]);
         if (G == 0) return fail(POSI_ERR_UNSUPPORTED, "the adjoint supports systems of up to 8 bodies", nullptr);
         by_g[G].push_back((int32_t)s);

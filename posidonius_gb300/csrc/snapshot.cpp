@@ -184,6 +184,13 @@ bool update_case_document(json::Value& doc, int64_t n, const int64_t* si, const 
             err = "tides coordinates";
             return false;
         }
+        // the disk's migration timescale of the last evaluation (read by the
+        // historic records)
+        {
+            json::Value* dint = member(member(member(p, "disk"), "parameters"), "internal");
+            json::Value* mts = dint ? member(dint, "migration_timescale") : nullptr;
+            if (mts) set_number(*mts, F[POSI_BF_DISK_MTS]);
+        }
         if (!set_axes(&verr->items[(size_t)b], F + POSI_BF_EVX) || !set_axes(&lerr->items[(size_t)b], F + POSI_BF_ELX)) {
             err = "Kahan error arrays";
             return false;

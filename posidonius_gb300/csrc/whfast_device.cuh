@@ -88,6 +88,85 @@ __device__ __forceinline__ double pow_m1p5(double y) {
     const double e = fma(-th, q, 1.) - tl * q;    // 1 - (th + tl) q
     return fma(q, e, q);
 }
+// Double-double helpers (Dekker / Knuth error-free transformations).
+struct DD {
+    double hi, lo;
+};
+__device__ __forceinline__ DD dd_two_sum(double a, double b) {
+    const double s = a + b;
+    const double bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DD dd_quick(double a, double b) {
+    const double s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ DD dd_add(DD a, DD b) {
+    DD s = dd_two_sum(a.hi, b.hi);
+    s.lo += a.lo + b.lo;
+    return dd_quick(s.hi, s.lo);
+}
+__device__ __forceinline__ DD dd_mul(DD a, DD b) {
+    const double p = a.hi * b.hi;
+    double e = fma(a.hi, b.hi, -p);
+    e += a.hi * b.lo + a.lo * b.hi;
+    return dd_quick(p, e);
+}
+__device__ __forceinline__ DD dd_mul_d(DD a, double b) {
+    const double p = a.hi * b;
+    double e = fma(a.hi, b, -p);
+    e += a.lo * b;
+    return dd_quick(p, e);
+}
+
+// ln 2 split in two doubles (the nearest double and the remainder)
+constexpr double kLN2_HI = 0x1.62e42fefa39efp-1;
+constexpr double kLN2_LO = 0x1.abc9e3b39803fp-56;
+
+// e^x for the disk model (the reference's f64::exp), carried to about 100
+// bits and rounded once: x = k ln 2 + r, r / 2^9 through the Taylor series of
+// expm1 (double-double to the cubic term), nine doublings
+// expm1(2y) = expm1(y) (2 + expm1(y)), then 2^k (1 + expm1(r)).
+__device__ __forceinline__ double exp_dd(double x) {
+    if (x != x) return x;
+    if (x < -745.2) return 0.;
+    if (x > 709.8) return __longlong_as_double(0x7ff0000000000000LL);
+    const double k = rint(x * 1.4426950408889634);
+    const double p = k * kLN2_HI;
+    const double pe = fma(k, kLN2_HI, -p);   // k ln2_hi = p + pe exactly
+    DD r = dd_two_sum(x, -p);
+    r.lo -= pe;
+    r.lo -= k * kLN2_LO;
+    r = dd_quick(r.hi, r.lo);
+    r.hi *= 1. / 512.;
+    r.lo *= 1. / 512.;
+    const double h = r.hi;
+    const double tail = 1. / 24. + h * (1. / 120. + h * (1. / 720. + h * (1. / 5040. + h * (1. / 40320.))));
+    const DD r2 = dd_mul(r, r);
+    const DD r3 = dd_mul(r2, r);
+    DD sm = dd_add(r, dd_mul_d(r2, 0.5));
+    sm = dd_add(sm, dd_mul_d(r3, 1. / 6.));
+    sm = dd_add(sm, DD{r3.hi * h * tail, 0.});
+#pragma unroll
+    for (int i = 0; i < 9; ++i) sm = dd_mul(sm, dd_add(DD{2., 0.}, sm));
+    const DD e = dd_add(DD{1., 0.}, sm);
+    return ldexp(e.hi + e.lo, (int)k);
+}
+
+// y^(-1/2) (the reference's powf(-0.5)): 1 / (sqrt(y) + its residual term),
+// rounded once.
+__device__ __forceinline__ double pow_m0p5(double y) {
+    const double s = sqrt(y);
+    const double sl = fma(-s, s, y) / (2. * s);
+    const double q = 1. / s;
+    const double e = fma(-s, q, 1.) - sl * q;
+    return fma(q, e, q);
+}
+
+// src/constants.rs:71-74
+constexpr double kBOLTZMANN = 1.380649e-23 / (kM_SUN * kAU * kAU) * kDAY * kDAY;
+constexpr double kMASS_HYDROGEN = 1.672162841e-27 / kM_SUN;
+
 constexpr int kNMAX_QUART = 64;
 constexpr int kNMAX_NEWT = 32;
 constexpr int kMIDPOINT_MIN = 3;
@@ -168,7 +247,8 @@ struct GroupSmem {
 // host card slots
 enum { HC_PX = 0, HC_PY, HC_PZ, HC_VX, HC_VY, HC_VZ, HC_SX, HC_SY, HC_SZ, HC_NSV2, HC_M, HC_MG, HC_R,
        HC_SIG, HC_K2, HC_K2F, HC_MOI, HC_AM, HC_SLX, HC_SLY, HC_SLZ,
-       HC_LAG, HC_DFAC, HC_DSCALE, HC_COUNT };
+       HC_LAG, HC_DFAC, HC_DSCALE,
+       HC_DINNER, HC_DOUTER, HC_DLIFE, HC_DALPHA, HC_DSIG0, HC_DMU, HC_COUNT };
 static_assert(HC_COUNT <= kCARD, "host card");
 
 struct Body {
@@ -182,6 +262,9 @@ struct Body {
     int wk;                              // wind: 1 Interaction
     double wind_k, wind_rsat, wind_rsat2;
     double diss_factor, diss_scale;      // ConstantTimeLag inputs (dynamical tide of a host)
+    int dk;                              // disk effect kind
+    double disk_p[6];                    // DiskProperties (a disk host)
+    double dmts;                         // disk migration timescale of the last evaluation
     int64_t eoff, elen, eleft;
     // alternative (Jacobi / democratic-heliocentric / WHDS) coordinates
     double am, amg, ap[3], av[3], aacc[3];
@@ -191,9 +274,10 @@ template <int G>
 struct Sys {
     // uniform per group
     int s, n, host, coords, lane;
-    bool tides, flat, gr, evo, spin_on, wind;
+    bool tides, flat, gr, evo, spin_on, wind, disk;
     int gr_impl;     // posi_gr_impl; grk(): Kidder1995, the per-planet formulation
     bool dyn_host;   // the tidal host's evolution has a dynamical tide
+    bool disk_on;    // disk effect with a disk host
     __device__ __forceinline__ bool grk() const { return gr && gr_impl == POSI_GR_KIDDER1995; }
     unsigned mask;
     double dt, half_dt, t, time_limit, last_hist, hist_period, last_rec, rec_period;
@@ -280,6 +364,7 @@ struct Sys {
         flat = D.si[POSI_SI_FLAT * ns + s] != 0;
         gr = D.si[POSI_SI_GR * ns + s] != 0;
         wind = D.si[POSI_SI_WIND * ns + s] != 0;
+        disk = D.si[POSI_SI_DISK * ns + s] != 0;
         evo = D.si[POSI_SI_EVOLUTION * ns + s] != 0;
         gr_impl = (int)D.si[POSI_SI_GR_IMPL * ns + s];
         // whfast.rs:270-274: GR adds a spin torque only in Kidder1995
@@ -348,15 +433,23 @@ struct Sys {
             b.wind_rsat2 = F[POSI_BF_WIND_RSAT2 * st];
             b.diss_factor = F[POSI_BF_DISS_FACTOR * st];
             b.diss_scale = F[POSI_BF_DISS_SCALE * st];
+            b.dk = (int)I[POSI_BI_DISK_KIND * st];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) b.disk_p[k] = F[(POSI_BF_DISK_INNER + k) * st];
+            b.dmts = F[POSI_BF_DISK_MTS * st];
             b.evo = (int)I[POSI_BI_EVO_TYPE * st];
             b.eoff = I[POSI_BI_EVO_OFFSET * st];
             b.elen = I[POSI_BI_EVO_LEN * st];
             b.eleft = I[POSI_BI_EVO_LEFT * st];
             if (b.elen <= 0) b.evo = POSI_EVO_NON_EVOLVING;
         }
-        if (is_host) isc[5] = (tides && dynamical_evo(b.evo)) ? 1 : 0;
+        if (is_host) {
+            isc[5] = (tides && dynamical_evo(b.evo)) ? 1 : 0;
+            isc[6] = (disk && b.dk == POSI_EFFECT_CENTRAL) ? 1 : 0;
+        }
         sync();
         dyn_host = isc[5] != 0;
+        disk_on = isc[6] != 0;
 #if !POSI_EXACT
         mass_constants();
         pc_valid = false;
@@ -400,6 +493,7 @@ struct Sys {
         F[POSI_BF_NSV2 * st] = b.nsv2;
         F[POSI_BF_DENERGY_DT * st] = b.denergy;
         F[POSI_BF_LAG_ANGLE * st] = b.lag;
+        F[POSI_BF_DISK_MTS * st] = b.dmts;
 #pragma unroll
         for (int k = 0; k < 13; ++k) F[(POSI_BF_TD_DIST + k) * st] = P(PC_TD_DIST + k);
         D.bi[POSI_BI_EVO_LEFT * st + o] = b.eleft;
@@ -538,6 +632,38 @@ struct Sys {
         }
     }
 
+    // src/effects/disk.rs:154-268: the disk's force on this planet
+    // (migration, eccentricity and inclination damping; Alibert et al. 2013)
+    // from its heliocentric position (x, y, z), velocity (u, v, w), distance d
+    // and squared speed nv2; the host's values and DiskProperties from the card
+    __device__ void disk_force(double x, double y, double z, double u, double v, double w, double d, double nv2,
+                               double F[3]) {
+        const double hm = card[HC_M], hmg = card[HC_MG];
+        const double sma = (b.mg + hmg) * d / (2.0 * (b.mg + hmg) - d * nv2);
+        // DiskProperties::calculate_migration_timescale
+        const double keplerian_frequency = sqrt(hmg / powi<3>(d));
+        const double disk_temperature = 280.0 * pow_m0p5(d) * hm;
+        const double speed_of_sound_squared = kBOLTZMANN * disk_temperature / (card[HC_DMU] * kMASS_HYDROGEN);
+        const double viscosity = card[HC_DALPHA] * speed_of_sound_squared / keplerian_frequency;
+        const double gas_radial_velocity = -3.0 * viscosity / (2.0 * sma);
+        const double initial_density = card[HC_DSIG0] * (1. / d) * exp_dd(-1.0 * d / card[HC_DOUTER]) *
+                                       (1.0 - sqrt(card[HC_DINNER] / d));
+        double density = 0.;
+        if (d > card[HC_DINNER]) density = initial_density * exp_dd(-t / card[HC_DLIFE]);
+        const double yy = 2.0 * density * powi<2>(sma) / b.m;
+        const double a_dot = gas_radial_velocity * (yy < 1.0 ? yy : 1.0);   // f64::min(1.0, yy)
+        const double migration_timescale = -sma / a_dot;
+        b.dmts = migration_timescale;
+        const double factor_migration = -b.m / migration_timescale;
+        const double ecc_timescale = 0.1 * migration_timescale;
+        const double factor_ecc = -b.m * 2.0 / ecc_timescale;
+        const double factor_inc = -b.m * 2.0 / ecc_timescale;
+        const double sp = 1.0 / (d * d) * (x * u + y * v + z * w);
+        F[0] = factor_migration * u + factor_ecc * sp * x + 0.0;
+        F[1] = factor_migration * v + factor_ecc * sp * y + 0.0;
+        F[2] = factor_migration * w + factor_ecc * sp * z + factor_inc * w;
+    }
+
     // src/effects/tides/constant_time_lag.rs:20-93 with src/tools.rs:251-285:
     // the host's dissipation factor for this planet when the host's dynamical
     // tide is excited, else its own (x: heliocentric position, v: heliocentric
@@ -606,7 +732,7 @@ struct Sys {
         R[HR_VX] = b.v[0]; R[HR_VY] = b.v[1]; R[HR_VZ] = b.v[2];
         R[HR_M] = b.m; R[HR_R] = b.R; R[HR_RG2] = b.rg2;
         R[HR_K2] = b.tk != POSI_EFFECT_DISABLED ? b.k2 : 0.;
-        R[HR_SIGMA] = b.sig; R[HR_LAG] = b.lag; R[HR_DENERGY] = b.denergy; R[HR_MIGRATION] = 0.;
+        R[HR_SIGMA] = b.sig; R[HR_LAG] = b.lag; R[HR_DENERGY] = b.denergy; R[HR_MIGRATION] = b.dmts;
     }
 
     // Heliocentric position of a planet, its distance and unit vector: fixed
@@ -1271,6 +1397,13 @@ struct Sys {
                 dg[2] = kFA * (q1z - q2z + q3z);
             }
         }
+        double ad[3] = {0., 0., 0.}, fdisk[3] = {0., 0., 0.};
+        if (disk_on && planet() && b.dk == POSI_EFFECT_ORBITING) {
+            disk_force(x, y, z, hv[0], hv[1], hv[2], d, nv2, fdisk);
+            const double factor1 = 1. / b.m;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) ad[k] = factor1 * fdisk[k];
+        }
         // host back-reactions: fold the contribution columns in body order
         if (ncol > 0) colfold(0, ncol, nullptr, true, false);
         if (is_host) {
@@ -1295,6 +1428,21 @@ struct Sys {
                 }
             }
         }
+        if (disk_on) {
+            // src/effects/disk.rs:205-268: the host's force is minus the sum
+            // of the planets' forces, in body order
+            sync();
+            if (has) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) X(k, lane) = fdisk[k];
+            }
+            colfold(0, 3, nullptr, true, false);
+            if (is_host) {
+                const double factor2 = 1. / card[HC_M];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) ad[k] = -1.0 * factor2 * sums[k];
+            }
+        }
         if (gr && !grk()) gr_nbody(ag);
         sync();
         if (has) {
@@ -1310,6 +1458,7 @@ struct Sys {
             for (int k = 0; k < 3; ++k) {
                 double acc = 0.;
                 if (tides) acc += at[k];
+                if (disk) acc += ad[k];
                 if (flat) acc += af[k];
                 if (gr) acc += ag[k];
                 b.aa[k] = acc;
@@ -1457,12 +1606,18 @@ struct Sys {
                 dl1 += kFA * (fm2 * (lo2 * pL0 - lo0 * pL2) + h2y + ss3 * (nn2 * pL0 - nn0 * pL2));
                 dl2 += kFA * (fm2 * (lo0 * pL1 - lo1 * pL0) + h2z + ss3 * (nn0 * pL1 - nn1 * pL0));
             }
+            if (disk_on && b.dk == POSI_EFFECT_ORBITING) {
+                // the host's share enters through the (m/M) a columns below
+                double F[3];
+                disk_force(x, y, z, hv0, hv1, hv2, P(PC_D), nv2, F);
+                aa0 += inv_m * F[0]; aa1 += inv_m * F[1]; aa2 += inv_m * F[2];
+            }
             const double mr = P(PC_MRATIO);
             X(0, lane) = mr * aa0; X(1, lane) = mr * aa1; X(2, lane) = mr * aa2;
             X(3, lane) = th0; X(4, lane) = th1; X(5, lane) = th2;
         }
-        if (tides || flat || grk()) colfold(0, 6, nullptr, true, false);
-        if (is_host && (tides || flat || grk())) {
+        if (tides || flat || grk() || disk_on) colfold(0, 6, nullptr, true, false);
+        if (is_host && (tides || flat || grk() || disk_on)) {
             aa0 = -sums[0]; aa1 = -sums[1]; aa2 = -sums[2];
             dl0 = sums[3]; dl1 = sums[4]; dl2 = sums[5];
         }
@@ -1492,7 +1647,8 @@ struct Sys {
         if (is_host) { card[HC_PX] = b.r[0]; card[HC_PY] = b.r[1]; card[HC_PZ] = b.r[2];
                        card[HC_M] = b.m; card[HC_MG] = b.mg; card[HC_R] = b.R; card[HC_SIG] = b.sig;
                        card[HC_K2] = b.k2; card[HC_K2F] = b.k2f;
-                       card[HC_DFAC] = b.diss_factor; card[HC_DSCALE] = b.diss_scale; }
+                       card[HC_DFAC] = b.diss_factor; card[HC_DSCALE] = b.diss_scale;
+                       for (int k = 0; k < 6; ++k) card[HC_DINNER + k] = b.dk == POSI_EFFECT_CENTRAL ? b.disk_p[k] : 0.; }
         sync();
 #if POSI_EXACT
         if (planet()) set_geometry(b.r[0] - card[HC_PX], b.r[1] - card[HC_PY], b.r[2] - card[HC_PZ]);
@@ -2391,7 +2547,8 @@ __global__ void __launch_bounds__(128) additional_effects_kernel(Dev D, double t
     if (S.is_host) { S.card[HC_PX] = S.b.r[0]; S.card[HC_PY] = S.b.r[1]; S.card[HC_PZ] = S.b.r[2];
                      S.card[HC_M] = S.b.m; S.card[HC_MG] = S.b.mg; S.card[HC_R] = S.b.R; S.card[HC_SIG] = S.b.sig;
                      S.card[HC_K2] = S.b.k2; S.card[HC_K2F] = S.b.k2f;
-                     S.card[HC_DFAC] = S.b.diss_factor; S.card[HC_DSCALE] = S.b.diss_scale; }
+                     S.card[HC_DFAC] = S.b.diss_factor; S.card[HC_DSCALE] = S.b.diss_scale;
+                     for (int k = 0; k < 6; ++k) S.card[HC_DINNER + k] = S.b.dk == POSI_EFFECT_CENTRAL ? S.b.disk_p[k] : 0.; }
     S.sync();
     if (S.planet()) S.set_geometry(S.b.r[0] - S.card[HC_PX], S.b.r[1] - S.card[HC_PY], S.b.r[2] - S.card[HC_PZ]);
     S.additional_effects(D, 0, evolution != 0);

@@ -10,7 +10,7 @@ tests/common/universe.rs:36-44; tests/data/<case>/particle_<i>.json = final
 inertial position/velocity/acceleration after integrating to the time limit,
 tests/common/universe.rs:18-34) it writes <case>/case.json.gz and
 <case>/particles.json (the particle files merged).  Cases outside the path
-(disk, IAS15, LeapFrog) are skipped.
+(IAS15, LeapFrog) are skipped.
 The Python-generated twins (posidonius/tests/data/<case>/case.json) of the three
 integrator cases, which the reference steps once and compares
 (tests/test_integrator.rs:58-70), are stored as <case>/python_case.json.gz.
@@ -49,6 +49,8 @@ IN_SCOPE = [
     # dynamical tides of the solar-like host
     "test_evolution-solar_like_bolmontmathis2016",
     "test_evolution-solar_like_galletbolmont2017",
+    # protoplanetary disk
+    "test_disk-enabled_disk",
 ]
 
 

@@ -53,7 +53,7 @@ def test_plain_path_exact_matches_golden_and_oracle(tmp_path, name):
                                   "test_integrator-whfast_whds", "test_evolution-brown_dwarf_non_evolving",
                                   "test_general_relativity-anderson1975", "test_general_relativity-newhall1983",
                                   "test_evolution-solar_like_non_evolving",
-                                  "test_evolution-solar_like_bolmontmathis2016"])
+                                  "test_evolution-solar_like_bolmontmathis2016", "test_disk-enabled_disk"])
 def test_plain_path_fast_within_tolerance(tmp_path, name):
     w = pg.restore_snapshot(_json(tmp_path, name), mode=pg.FAST)
     w.run()

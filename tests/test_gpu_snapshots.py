@@ -56,7 +56,8 @@ def read_history(path, n):
 
 
 @pytest.mark.parametrize("name", ["test_tides-enabled_tides", "test_evolution-m_dwarf_baraffe2015",
-                                  "test_integrator-whfast_democraticheliocentric"])
+                                  "test_integrator-whfast_democraticheliocentric",
+                                  "test_disk-enabled_disk", "test_evolution-solar_like_bolmontmathis2016"])
 def test_history_records_match_oracle(tmp_path, name):
     path, d = _case(tmp_path, name, hist_period=0.24)
     w = pg.restore_snapshot(path, mode=pg.EXACT)

@@ -44,3 +44,19 @@ def test_max_bodies():
     text = open(HEADER).read()
     m = re.search(r"#define\s+POSI_MAX_BODIES\s+(\d+)", text)
     assert int(m.group(1)) == L.MAX_BODIES
+
+
+def test_ln2_split_constants():
+    """The double-double ln 2 of the kernels' exp (kLN2_HI + kLN2_LO) equals
+    ln 2 to about 2^-106."""
+    import decimal
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(__file__), "..", "posidonius_gb300", "csrc", "whfast_device.cuh")).read()
+    hi = float.fromhex(re.search(r"kLN2_HI = (0x[0-9a-fp.+-]+);", src).group(1))
+    lo = float.fromhex(re.search(r"kLN2_LO = (0x[0-9a-fp.+-]+);", src).group(1))
+    decimal.getcontext().prec = 60
+    ln2 = decimal.Decimal(2).ln()
+    err = abs(decimal.Decimal(hi) + decimal.Decimal(lo) - ln2)
+    assert hi == float(ln2)
+    assert err < decimal.Decimal(2) ** -106
