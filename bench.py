@@ -42,7 +42,8 @@ def parse():
     p.add_argument("--steps", type=int, default=3000)
     p.add_argument("--warmup", type=int, default=300)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="ensemble8", choices=["ensemble8", "uneven", "single", "gradient", "large"])
+    p.add_argument("--workload", default="ensemble8",
+                   choices=["ensemble8", "uneven", "single", "gradient", "large", "ias15"])
     p.add_argument("--large-bodies", type=int, default=1024, help="large workload: bodies in the system")
     p.add_argument("--grad-steps", type=int, default=10000, help="gradient workload: WHFast steps")
     p.add_argument("--checkpoint-every", type=int, default=100, help="gradient workload: checkpoint interval")
@@ -65,11 +66,16 @@ EFFECTS = {
     "ensemble8": "CTL tides + oblate flattening + Kidder GR",
     "single": "CTL tides + oblate flattening + Kidder GR",
     "uneven": "each of CTL tides / oblate flattening / Kidder GR on with p = 0.7; 20% circumbinary binaries",
+    "ias15": "CTL tides + oblate flattening + Kidder GR",
 }
 
 
 def make_workload(name, n_systems, rank=0):
     from posidonius_gb300 import ensemble as E
+    if name == "ias15":
+        # the ensemble8 systems integrated by IAS15 from a 0.08 d first step
+        seed = E.SEED_BASE + E.WORKLOAD_IDS["ensemble8"] + 1000 * rank
+        return E.as_ias15(E.workload_ensemble8(n_systems or 4096, seed=seed), dt=0.08)
     seed = E.SEED_BASE + E.WORKLOAD_IDS[name] + 1000 * rank
     if name == "ensemble8":
         return E.workload_ensemble8(n_systems or 4096, seed=seed)
@@ -201,7 +207,9 @@ def newtonian_energy(state, s):
 def pinned_like(state):
     import torch
     out = {}
-    for k in ("sys_i64", "sys_f64", "body_i64", "body_f64"):
+    for k in ("sys_i64", "sys_f64", "body_i64", "body_f64", "body_ias"):
+        if k not in state:
+            continue
         t = torch.empty(state[k].shape, dtype=torch.int64 if k.endswith("i64") else torch.float64, pin_memory=True)
         a = t.numpy()
         a[...] = state[k]
@@ -237,7 +245,9 @@ def cpu_leg(ens, steps_hint, seconds, nthreads):
     _, _, _, cnt = oracle.run(flo_state, max_steps=20, flops=True)
     flops = cnt[0] / (nf * 20)
     return {"value": n_sys * steps / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{n_sys} systems x {steps} WHFast steps of the {ens.get('_name', 'ensemble')} workload, "
+            "sample": f"{n_sys} systems x {steps} "
+                      f"{'IAS15' if int(ens['sys_i64'][0, L.SI_INTEGRATOR]) == L.INTEGRATOR_IAS15 else 'WHFast'} "
+                      f"steps of the {ens.get('_name', 'ensemble')} workload, "
                       f"C++ restatement of the Rust FP64 path, {nthreads} threads, {dt:.1f} s",
             "flops_per_system_step": flops}
 
@@ -644,9 +654,10 @@ def main():
     # ---- end-to-end through the C ABI with host buffers -----------------------
     state = batch.get_state()
     host = pinned_like(state)
-    out = {k: host[k].copy() for k in ("sys_i64", "sys_f64", "body_i64", "body_f64")}
+    keys = ("sys_i64", "sys_f64", "body_i64", "body_f64") + (("body_ias",) if "body_ias" in host else ())
+    out = {k: host[k].copy() for k in keys}
     out_p = pinned_like(out)
-    h2d = sum(host[k].nbytes for k in ("sys_i64", "sys_f64", "body_i64", "body_f64"))
+    h2d = sum(host[k].nbytes for k in keys)
     d2h = h2d
     barrier(world)
     torch.cuda.synchronize()
@@ -671,8 +682,10 @@ def main():
         "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded; posidonius_gb300.ensemble)",
         "config": {"workload": args.workload, "n_systems": int(batch.n_sys), "bodies_per_system": int(batch.nmax),
-                   "dt_days": 0.08, "mode": args.mode, "steps_per_launch": spl, "timed_launches": R,
-                   "effects": EFFECTS[args.workload], "coordinates": "Jacobi",
+                   "dt_days": 0.08 if args.workload != "ias15" else "adaptive (IAS15, first trial 0.08)",
+                   "mode": args.mode, "steps_per_launch": spl, "timed_launches": R,
+                   "effects": EFFECTS[args.workload],
+                   "coordinates": "Jacobi" if args.workload != "ias15" else "inertial (IAS15)",
                    "lanes_per_system": {str(k): v for k, v in sorted(lanes.items())},
                    "mapping": "autotuned" if not args.no_autotune else "smallest group",
                    "l2": f"flushed ({L2_FLUSH_BYTES >> 20} MiB write) before every timed launch",

@@ -62,6 +62,11 @@ enum posi_system_status {
  * particle order (the host may sit at any index).
  */
 enum posi_coords { POSI_JACOBI = 0, POSI_DEMOCRATIC_HELIOCENTRIC = 1, POSI_WHDS = 2 };
+/* Integrator of a system (src/integrator/mod.rs): WHFast (src/integrator/whfast.rs)
+ * or IAS15 (src/integrator/ias15.rs).  A batch holds systems of one integrator.
+ * For IAS15, sys_f64[POSI_SF_DT] is the adaptive Ias15.time_step and
+ * POSI_SF_HALF_DT, POSI_SI_COORDS and the WHFast error fields are unused. */
+enum posi_integrator { POSI_INTEGRATOR_WHFAST = 0, POSI_INTEGRATOR_IAS15 = 1 };
 enum posi_effect_kind { POSI_EFFECT_DISABLED = 0, POSI_EFFECT_CENTRAL = 1, POSI_EFFECT_ORBITING = 2 };
 /* GeneralRelativityImplementation (src/effects/general_relativity.rs) */
 enum posi_gr_impl { POSI_GR_KIDDER1995 = 0, POSI_GR_ANDERSON1975 = 1, POSI_GR_NEWHALL1983 = 2 };
@@ -93,6 +98,8 @@ enum posi_sys_i64_field {
     POSI_SI_GR_IMPL,             /* Universe.general_relativity_implementation (posi_gr_impl) */
     POSI_SI_WIND,                /* ConsiderEffects.wind */
     POSI_SI_DISK,                /* ConsiderEffects.disk */
+    POSI_SI_INTEGRATOR,          /* posi_integrator: the case document's integrator */
+    POSI_SI_IAS_MAX_EXCEEDED,    /* Ias15.integrator_iterations_max_exceeded */
     POSI_SI_COUNT
 };
 
@@ -106,6 +113,7 @@ enum posi_sys_f64_field {
     POSI_SF_LAST_REC,            /* WHFast.last_recovery_snapshot_time */
     POSI_SF_REC_PERIOD,          /* WHFast.recovery_snapshot_period */
     POSI_SF_INITIAL_TIME,        /* Universe.initial_time */
+    POSI_SF_IAS_DT_LAST,         /* Ias15.time_step_last_success */
     POSI_SF_COUNT
 };
 
@@ -160,6 +168,20 @@ enum posi_body_f64_field {
     POSI_BF_COUNT
 };
 
+/* IAS15 per-body state (src/integrator/ias15.rs:28-224, the fields that carry
+ * over from one step to the next), body_ias[(s*nmax + b)*POSI_IAS_COUNT + f]:
+ * the Gauss-Radau coefficients b_0..b_6, their predictions e_0..e_6, the
+ * last accepted br_0..br_6 and er_0..er_6, the same four sets for the spin
+ * angular momentum (sb, se, sbr, ser), and the compensated-summation terms
+ * csx, csv, css.  Set k of a field block holds its three components at
+ * block + 3*k + {0, 1, 2}. */
+enum posi_ias15_field {
+    POSI_IAS_B = 0, POSI_IAS_E = 21, POSI_IAS_BR = 42, POSI_IAS_ER = 63,
+    POSI_IAS_SB = 84, POSI_IAS_SE = 105, POSI_IAS_SBR = 126, POSI_IAS_SER = 147,
+    POSI_IAS_CSX = 168, POSI_IAS_CSV = 171, POSI_IAS_CSS = 174,
+    POSI_IAS_COUNT = 177
+};
+
 /* Largest body count of the batched kernels. */
 #define POSI_MAX_BODIES 32
 
@@ -199,6 +221,10 @@ int posi_device_count(void);
 int posi_read_case(const char* path, int64_t* n, int64_t* n_tables, int64_t* sys_i64, double* sys_f64,
                    int64_t* body_i64, double* body_f64, double* tables, double* roche);
 
+/* IAS15 cases: the per-body Gauss-Radau state of the case (n*POSI_IAS_COUNT
+ * doubles, posi_ias15_field layout).  POSI_ERR_STATE for a WHFast case. */
+int posi_read_case_ias15(const char* path, double* body_ias);
+
 /* ---- single system (the drop-in path: one system, one launch per step) -- */
 
 /* src/integrator/output.rs:178-241 restore_snapshot + deserialize_json_snapshot:
@@ -231,8 +257,8 @@ int posi_set_snapshot_periods(posi_handle* h, double historic_period, double rec
  * (+ src/particles/universe.rs:177-196 calculate_roche_radiuses). */
 int posi_initialize_physical_values(posi_handle* h);
 
-/* src/integrator/whfast.rs:235-305 Integrator::iterate, n_steps times (one
- * kernel launch per step).  Returns POSI_COMPLETED after the step that makes
+/* src/integrator/whfast.rs:235-305 (src/integrator/ias15.rs:420-463 for an
+ * IAS15 case) Integrator::iterate, n_steps times (one kernel launch per step).  Returns POSI_COMPLETED after the step that makes
  * current_time + time_step exceed time_limit, like Err("Simulation completed").
  * *steps_done receives the steps performed; *recovery_trigger is set when the
  * last step reported a recovery-snapshot trigger (Ok(true)). */
@@ -253,6 +279,11 @@ int posi_get_state(const posi_handle* h, int64_t* sys_i64, double* sys_f64,
                    int64_t* body_i64, double* body_f64, double* roche);
 int posi_set_state(posi_handle* h, const int64_t* sys_i64, const double* sys_f64,
                    const int64_t* body_i64, const double* body_f64);
+
+/* IAS15 systems: copy the per-body Gauss-Radau state (n*POSI_IAS_COUNT) to or
+ * from the host; POSI_ERR_STATE for a WHFast system. */
+int posi_get_ias15(const posi_handle* h, double* body_ias);
+int posi_set_ias15(posi_handle* h, const double* body_ias);
 
 /* src/integrator/output.rs:63-89 get_universe_history_writer: open the
  * historic-snapshot file (created if absent), fail with POSI_ERR_STATE when it
@@ -302,6 +333,15 @@ int posi_batch_get_state(const posi_batch* b, int64_t* sys_i64, double* sys_f64,
 int posi_batch_set_state(posi_batch* b, const int64_t* sys_i64, const double* sys_f64,
                          const int64_t* body_i64, const double* body_f64);
 
+/* IAS15 batches: the per-body Gauss-Radau state, [n_systems][nmax]
+ * [POSI_IAS_COUNT] (zeros after posi_batch_create); POSI_ERR_STATE for a
+ * WHFast batch.  A batch holds systems of one integrator (sys_i64
+ * [POSI_SI_INTEGRATOR]); an IAS15 batch advances by IAS15 steps in
+ * posi_batch_iterate (adaptive per system, groups of 8, 16 or 32 lanes, no
+ * balanced schedules, no autotuning). */
+int posi_batch_get_ias15(const posi_batch* b, double* body_ias);
+int posi_batch_set_ias15(posi_batch* b, const double* body_ias);
+
 /* Size of the ensemble. */
 int posi_batch_size(const posi_batch* b, int64_t* n_systems, int64_t* nmax);
 
@@ -337,8 +377,11 @@ int posi_fp64_probe(int blocks, int threads, int iters, double* ms, double* tflo
  * body's tidal dissipation factor (scaled_dissipation_factor) and Love number.
  * Supported: Jacobi coordinates, non-evolving bodies, up to 8 bodies per system.
  * The forward run stores the batch state every checkpoint_every steps; the
- * backward run re-integrates each chunk (recording its steps) and sweeps it in
- * reverse.  Derivatives are those of the computed map (the midpoint loop is
+ * backward run re-integrates each chunk from a copy of its checkpoint
+ * (recording its steps) and sweeps it in reverse, the re-integration of one
+ * chunk overlapping the reverse sweep of the next on a second stream when a
+ * second tape fits (2 x checkpoint_every x 209 doubles per body slot); it
+ * leaves the batch state as the forward run ended it.  Derivatives are those of the computed map (the midpoint loop is
  * reversed with its iteration counts, the Kepler root is differentiated
  * implicitly). */
 typedef struct posi_adjoint posi_adjoint;
@@ -393,7 +436,9 @@ int posi_adjoint_vjp_static(int64_t n_systems, int64_t nmax, const int64_t* d_sy
                             double* d_grad, int32_t* d_flags, void* stream);
 
 /* CUDA-event times of the last forward and backward runs, and the backward
- * run's split into chunk re-integration (record) and reverse sweeps. */
+ * run's split into chunk re-integration (record) and reverse sweeps (sums
+ * over the chunks; the two overlap, so they may add up to more than the
+ * backward time). */
 int posi_adjoint_last_timing(const posi_adjoint* a, double* forward_ms, double* backward_ms, double* record_ms,
                              double* reverse_ms);
 

@@ -42,8 +42,8 @@ def _lib(flops=False):
         i64p = ctypes.POINTER(ctypes.c_int64)
         f64p = ctypes.POINTER(ctypes.c_double)
         lib.oracle_run.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64, i64p, f64p, i64p, f64p, f64p,
-                                   f64p, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
-                                   i64p, i64p]
+                                   f64p, f64p, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_int, i64p, i64p]
         lib.oracle_run.restype = ctypes.c_int
         lib.oracle_history.argtypes = [f64p, ctypes.c_int64, i64p]
         lib.oracle_history.restype = None
@@ -95,8 +95,11 @@ def run(ens, op=ITERATE, max_steps=0, init_physical=False, arg=0, t_arg=0.0, nth
     ens = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in as_ensemble(ens).items()}
     lib = _lib(flops)
     ns, nmax = ens["n_sys"], ens["nmax"]
+    if "body_ias" not in ens:
+        ens["body_ias"] = np.zeros((ns, nmax, L.IAS_COUNT))
     for k, dt in (("sys_i64", np.int64), ("sys_f64", np.float64), ("body_i64", np.int64),
-                  ("body_f64", np.float64), ("tables", np.float64), ("roche", np.float64)):
+                  ("body_f64", np.float64), ("tables", np.float64), ("roche", np.float64),
+                  ("body_ias", np.float64)):
         ens[k] = np.ascontiguousarray(ens[k], dtype=dt)
     steps = np.zeros(ns, dtype=np.int64)
     result = np.zeros(ns, dtype=np.int64)
@@ -105,7 +108,8 @@ def run(ens, op=ITERATE, max_steps=0, init_physical=False, arg=0, t_arg=0.0, nth
         lib.oracle_flops(_p(cnt, ctypes.c_int64), 1)
     lib.oracle_run(op, ns, nmax, _p(ens["sys_i64"], ctypes.c_int64), _p(ens["sys_f64"], ctypes.c_double),
                    _p(ens["body_i64"], ctypes.c_int64), _p(ens["body_f64"], ctypes.c_double),
-                   _p(ens["tables"], ctypes.c_double), _p(ens["roche"], ctypes.c_double), int(max_steps),
+                   _p(ens["tables"], ctypes.c_double), _p(ens["roche"], ctypes.c_double),
+                   _p(ens["body_ias"], ctypes.c_double), int(max_steps),
                    int(init_physical), int(arg), float(t_arg), 1 if flops else int(nthreads),
                    _p(steps, ctypes.c_int64), _p(result, ctypes.c_int64))
     if flops:

@@ -66,8 +66,9 @@ def load_case(path_or_dict):
     if not isinstance(d, dict):
         with open(d) as f:
             d = json.load(f)
-    if "alternative_coordinates_type" not in d:
-        raise Unsupported("not a WHFast case")
+    ias15 = "alternative_coordinates_type" not in d and "b_0" in d and "time_step_last_success" in d
+    if "alternative_coordinates_type" not in d and not ias15:
+        raise Unsupported("neither a WHFast nor an IAS15 case")
     u = d["universe"]
     n = int(u["n_particles"])
     ce = u["consider_effects"]
@@ -88,8 +89,13 @@ def load_case(path_or_dict):
     bf = np.zeros((n, L.BF_COUNT), dtype=np.float64)
     si[L.SI_N] = n
     si[L.SI_HOST] = host
-    si[L.SI_COORDS] = {"Jacobi": L.JACOBI, "DemocraticHeliocentric": L.DEMOCRATIC_HELIOCENTRIC,
-                       "WHDS": L.WHDS}[d["alternative_coordinates_type"]]
+    if ias15:
+        si[L.SI_INTEGRATOR] = L.INTEGRATOR_IAS15
+        si[L.SI_IAS_MAX_EXCEEDED] = int(d["integrator_iterations_max_exceeded"])
+        sf[L.SF_IAS_DT_LAST] = d["time_step_last_success"]
+    else:
+        si[L.SI_COORDS] = {"Jacobi": L.JACOBI, "DemocraticHeliocentric": L.DEMOCRATIC_HELIOCENTRIC,
+                           "WHDS": L.WHDS}[d["alternative_coordinates_type"]]
     si[L.SI_TIDES] = int(ce["tides"])
     si[L.SI_FLAT] = int(ce["rotational_flattening"])
     si[L.SI_GR] = int(ce["general_relativity"])
@@ -99,9 +105,9 @@ def load_case(path_or_dict):
     si[L.SI_EVOLUTION] = int(ce["evolution"])
     si[L.SI_ITERATION] = int(d["current_iteration"])
     si[L.SI_N_HIST] = int(d["n_historic_snapshots"])
-    si[L.SI_TIMESTEP_WARNING] = int(d["timestep_warning"])
+    si[L.SI_TIMESTEP_WARNING] = int(d.get("timestep_warning", 0))
     sf[L.SF_DT] = d["time_step"]
-    sf[L.SF_HALF_DT] = d["half_time_step"]
+    sf[L.SF_HALF_DT] = d.get("half_time_step", 0.0)
     sf[L.SF_TIME] = d["current_time"]
     sf[L.SF_TIME_LIMIT] = u["time_limit"]
     sf[L.SF_LAST_HIST] = d["last_historic_snapshot_time"]
@@ -208,8 +214,9 @@ def load_case(path_or_dict):
             F[L.BF_AX + k] = p["inertial_acceleration"][key]
             F[L.BF_LX + k] = p["angular_momentum"][key]
             F[L.BF_SX + k] = p["spin"][key]
-            F[L.BF_EVX + k] = d["inertial_velocity_errors"][b][key]
-            F[L.BF_ELX + k] = d["particle_angular_momentum_errors"][b][key]
+            if not ias15:
+                F[L.BF_EVX + k] = d["inertial_velocity_errors"][b][key]
+                F[L.BF_ELX + k] = d["particle_angular_momentum_errors"][b][key]
             F[L.BF_ADDAX + k] = p["inertial_additional_acceleration"][key]
             F[L.BF_DLX + k] = p["dangular_momentum_dt"][key]
         F[L.BF_NSV2] = p["norm_spin_vector_2"]
@@ -234,8 +241,19 @@ def load_case(path_or_dict):
     if len(rr) >= n * n:
         roche = np.array(rr[: n * n], dtype=np.float64).reshape(n, n)
     tab = np.concatenate(tables) if tables else np.zeros(1)
+    ias = np.zeros((n, L.IAS_COUNT), dtype=np.float64)
+    if ias15:
+        # the serde arrays b_0..b_6, e_*, br_*, er_*, sb_*, se_*, sbr_*, ser_*
+        # hold 3*MAX_PARTICLES values (body i component c at 3*i + c)
+        for base, name in ((L.IAS_B, "b"), (L.IAS_E, "e"), (L.IAS_BR, "br"), (L.IAS_ER, "er"),
+                           (L.IAS_SB, "sb"), (L.IAS_SE, "se"), (L.IAS_SBR, "sbr"), (L.IAS_SER, "ser")):
+            for j in range(7):
+                arr = np.asarray(d[f"{name}_{j}"], dtype=np.float64)[: 3 * n].reshape(n, 3)
+                ias[:, base + 3 * j: base + 3 * j + 3] = arr
+        for base, name in ((L.IAS_CSX, "csx"), (L.IAS_CSV, "csv"), (L.IAS_CSS, "css")):
+            ias[:, base: base + 3] = np.asarray(d[name], dtype=np.float64)[: 3 * n].reshape(n, 3)
     return {"sys_i64": si, "sys_f64": sf, "body_i64": bi, "body_f64": bf, "tables": tab,
-            "roche": roche, "n": n}
+            "roche": roche, "n": n, "body_ias": ias}
 
 
 def stack(cases, nmax=None):
@@ -247,6 +265,7 @@ def stack(cases, nmax=None):
     bi = np.zeros((ns, nmax, L.BI_COUNT), dtype=np.int64)
     bf = np.zeros((ns, nmax, L.BF_COUNT), dtype=np.float64)
     roche = np.zeros((ns, nmax, nmax), dtype=np.float64)
+    ias = np.zeros((ns, nmax, L.IAS_COUNT), dtype=np.float64)
     tabs = []
     off = 0
     for k, c in enumerate(cases):
@@ -256,9 +275,11 @@ def stack(cases, nmax=None):
         bi[k, :n] = c["body_i64"]
         bf[k, :n] = c["body_f64"]
         roche[k, :n, :n] = c["roche"]
+        if "body_ias" in c:
+            ias[k, :n] = c["body_ias"]
         evolving = bi[k, :n, L.BI_EVO_LEN] > 0
         bi[k, :n, L.BI_EVO_OFFSET] = np.where(evolving, bi[k, :n, L.BI_EVO_OFFSET] + off, 0)
         tabs.append(c["tables"])
         off += len(c["tables"])
     return {"sys_i64": si, "sys_f64": sf, "body_i64": bi, "body_f64": bf,
-            "tables": np.concatenate(tabs), "roche": roche, "nmax": nmax, "n_sys": ns}
+            "tables": np.concatenate(tabs), "roche": roche, "nmax": nmax, "n_sys": ns, "body_ias": ias}

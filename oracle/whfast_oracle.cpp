@@ -208,6 +208,13 @@ struct Sim {
     std::vector<AltCoords> alt;
     std::vector<V3> errv, errL;
     std::vector<real> roche;
+    // src/integrator/ias15.rs:28-224 (IAS15 systems): per body POSI_IAS_COUNT
+    // values (posi_ias15_field), the last accepted step and the count of
+    // predictor-corrector loops that hit the iteration limit
+    int integrator = POSI_INTEGRATOR_WHFAST;
+    std::vector<real> ias;
+    real ias_dt_last = 0.;
+    int64_t ias_max_exceeded = 0;
     bool fatal() const { return (status & POSI_SYS_FATAL_MASK) != 0; }
 };
 
@@ -1932,12 +1939,20 @@ static int iterate(Sim& s, bool* recovery_trigger) {
     return POSI_OK;
 }
 
+#include "ias15_oracle.inc"
+
 // ---------------------------------------------------------------------------
 // Flat layout <-> Sim
 // ---------------------------------------------------------------------------
 static void load(Sim& s, int64_t nmax, const int64_t* si, const double* sf, const int64_t* bi, const double* bf,
-                 const double* tables, const double* roche) {
+                 const double* tables, const double* roche, const double* ias) {
     s.n = (int)si[POSI_SI_N];
+    s.integrator = (int)si[POSI_SI_INTEGRATOR];
+    s.ias_max_exceeded = si[POSI_SI_IAS_MAX_EXCEEDED];
+    s.ias_dt_last = sf[POSI_SF_IAS_DT_LAST];
+    s.ias.assign((size_t)si[POSI_SI_N] * POSI_IAS_COUNT, real(0.));
+    if (ias)
+        for (size_t k = 0; k < s.ias.size(); ++k) s.ias[k] = ias[k];
     s.host = (int)si[POSI_SI_HOST];
     s.coords = (int)si[POSI_SI_COORDS];
     s.tides = si[POSI_SI_TIDES] != 0;
@@ -2033,7 +2048,13 @@ static void load(Sim& s, int64_t nmax, const int64_t* si, const double* sf, cons
     }
 }
 
-static void store(const Sim& s, int64_t nmax, int64_t* si, double* sf, int64_t* bi, double* bf, double* roche) {
+static void store(const Sim& s, int64_t nmax, int64_t* si, double* sf, int64_t* bi, double* bf, double* roche,
+                  double* ias) {
+    si[POSI_SI_IAS_MAX_EXCEEDED] = s.ias_max_exceeded;
+    sf[POSI_SF_IAS_DT_LAST] = dv(s.ias_dt_last);
+    sf[POSI_SF_DT] = dv(s.dt);
+    if (ias)
+        for (size_t k = 0; k < s.ias.size(); ++k) ias[k] = dv(s.ias[k]);
     si[POSI_SI_ITERATION] = s.iteration;
     si[POSI_SI_N_HIST] = s.n_hist;
     si[POSI_SI_TIMESTEP_WARNING] = s.timestep_warning;
@@ -2096,8 +2117,8 @@ extern "C" {
 // For ORACLE_ITERATE: steps_done[s] receives the steps performed and
 // result[s] the last iterate() code.  nthreads <= 0 uses the hardware count.
 int oracle_run(int op, int64_t n_sys, int64_t nmax, int64_t* sys_i64, double* sys_f64, int64_t* body_i64,
-               double* body_f64, const double* tables, double* roche, int64_t max_steps, int init_physical,
-               int arg, double t_arg, int nthreads, int64_t* steps_done, int64_t* result) {
+               double* body_f64, const double* tables, double* roche, double* body_ias, int64_t max_steps,
+               int init_physical, int arg, double t_arg, int nthreads, int64_t* steps_done, int64_t* result) {
     if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
     if (nthreads > n_sys) nthreads = (int)std::max<int64_t>(1, n_sys);
     std::atomic<int64_t> next{0};
@@ -2111,13 +2132,14 @@ int oracle_run(int op, int64_t n_sys, int64_t nmax, int64_t* sys_i64, double* sy
             int64_t* bi = body_i64 + k * nmax * POSI_BI_COUNT;
             double* bf = body_f64 + k * nmax * POSI_BF_COUNT;
             double* ro = roche ? roche + k * nmax * nmax : nullptr;
-            orc::load(s, nmax, si, sf, bi, bf, tables, ro);
+            double* ia = body_ias ? body_ias + k * nmax * POSI_IAS_COUNT : nullptr;
+            orc::load(s, nmax, si, sf, bi, bf, tables, ro, ia);
             int64_t done = 0, rc = POSI_OK;
             if (op == ORACLE_ITERATE) {
                 if (init_physical) rc = orc::initialize_physical_values(s);
                 while (rc == POSI_OK && done < max_steps && !s.fatal()) {
                     bool rec = false;
-                    rc = orc::iterate(s, &rec);
+                    rc = s.integrator == POSI_INTEGRATOR_IAS15 ? orc::ias15_iterate(s, &rec) : orc::iterate(s, &rec);
                     if (rc == POSI_OK || rc == POSI_COMPLETED) ++done;
                 }
                 if (rc == POSI_COMPLETED) s.status = (s.status & ~int64_t(POSI_SYS_FATAL_MASK)) | POSI_SYS_COMPLETED;
@@ -2130,7 +2152,7 @@ int oracle_run(int op, int64_t n_sys, int64_t nmax, int64_t* sys_i64, double* sy
             } else if (op == ORACLE_INITIALIZE) {
                 rc = orc::initialize_physical_values(s);
             }
-            orc::store(s, nmax, si, sf, bi, bf, ro);
+            orc::store(s, nmax, si, sf, bi, bf, ro, ia);
             if (steps_done) steps_done[k] = done;
             if (result) result[k] = rc;
         }

@@ -32,7 +32,8 @@ HISTORY_BYTES_PER_PARTICLE = 8 + 8 + 4 + 8 * (20 - 3)
 
 
 def read_case(path):
-    """Parse a WHFast JSON case into the flat layout (C++ reader, no GPU)."""
+    """Parse a WHFast or IAS15 JSON case into the flat layout (C++ reader, no
+    GPU); ``body_ias`` holds the IAS15 per-body state (zeros for WHFast)."""
     n = ctypes.c_int64()
     nt = ctypes.c_int64()
     check(lib().posi_read_case(str(path).encode(), ctypes.byref(n), ctypes.byref(nt), None, None, None, None, None,
@@ -52,11 +53,20 @@ def read_case(path):
                                ptr(out["roche"], "f")))
     if nt == 0:
         out["tables"] = np.zeros(1)
+    out["body_ias"] = np.zeros((n, L.IAS_COUNT), np.float64)
+    if out["sys_i64"][L.SI_INTEGRATOR] == L.INTEGRATOR_IAS15:
+        check(lib().posi_read_case_ias15(str(path).encode(), ptr(out["body_ias"], "f")))
     return out
 
 
+def _is_ias15(sys_i64):
+    return int(np.asarray(sys_i64).reshape(-1, L.SI_COUNT)[0, L.SI_INTEGRATOR]) == L.INTEGRATOR_IAS15
+
+
 class WHFast:
-    """One system on the GPU (src/integrator/whfast.rs:99-1157)."""
+    """One system on the GPU (src/integrator/whfast.rs:99-1157; a case
+    document of the IAS15 integrator, src/integrator/ias15.rs, steps by IAS15
+    behind the same methods)."""
 
     def __init__(self, handle):
         if not handle:
@@ -84,7 +94,11 @@ class WHFast:
                                             int(mode), ctypes.byref(st))
         if not h:
             check(st.value)
-        return cls(h)
+        w = cls(h)
+        if _is_ias15(arr["sys_i64"]) and case.get("body_ias") is not None:
+            ias = np.ascontiguousarray(case["body_ias"], dtype=np.float64)
+            check(lib().posi_set_ias15(w._h, ptr(ias, "f")))
+        return w
 
     def close(self):
         if self._h:
@@ -180,6 +194,9 @@ class WHFast:
         }
         check(lib().posi_get_state(self._h, ptr(out["sys_i64"], "i"), ptr(out["sys_f64"], "f"),
                                    ptr(out["body_i64"], "i"), ptr(out["body_f64"], "f"), ptr(out["roche"], "f")))
+        if _is_ias15(out["sys_i64"]):
+            out["body_ias"] = np.zeros((n, L.IAS_COUNT), np.float64)
+            check(lib().posi_get_ias15(self._h, ptr(out["body_ias"], "f")))
         return out
 
     def set_state(self, state):
@@ -187,6 +204,13 @@ class WHFast:
                for k in ("sys_i64", "sys_f64", "body_i64", "body_f64")}
         check(lib().posi_set_state(self._h, ptr(arr["sys_i64"], "i"), ptr(arr["sys_f64"], "f"),
                                    ptr(arr["body_i64"], "i"), ptr(arr["body_f64"], "f")))
+        if _is_ias15(arr["sys_i64"]) and state.get("body_ias") is not None:
+            ias = np.ascontiguousarray(state["body_ias"], dtype=np.float64)
+            check(lib().posi_set_ias15(self._h, ptr(ias, "f")))
+
+
+# a handle on an IAS15 case document
+Ias15 = WHFast
 
 
 def restore_snapshot(path, mode=EXACT):
@@ -216,6 +240,10 @@ class Batch:
         if not h:
             check(st.value)
         self._h = ctypes.c_void_p(h)
+        self.ias15 = _is_ias15(arr["sys_i64"])
+        if self.ias15 and ens.get("body_ias") is not None:
+            ias = np.ascontiguousarray(ens["body_ias"], dtype=np.float64)
+            check(lib().posi_batch_set_ias15(self._h, ptr(ias, "f")))
 
     def close(self):
         if self._h:
@@ -270,6 +298,10 @@ class Batch:
         check(lib().posi_batch_get_state(self._h, ptr(out["sys_i64"], "i"), ptr(out["sys_f64"], "f"),
                                          ptr(out["body_i64"], "i"), ptr(out["body_f64"], "f"),
                                          ptr(out.get("roche"), "f")))
+        if self.ias15:
+            if out.get("body_ias") is None:
+                out["body_ias"] = np.zeros((self.n_sys, self.nmax, L.IAS_COUNT), np.float64)
+            check(lib().posi_batch_get_ias15(self._h, ptr(out["body_ias"], "f")))
         return out
 
     def set_state(self, state):
@@ -277,6 +309,9 @@ class Batch:
                for k in ("sys_i64", "sys_f64", "body_i64", "body_f64")}
         check(lib().posi_batch_set_state(self._h, ptr(arr["sys_i64"], "i"), ptr(arr["sys_f64"], "f"),
                                          ptr(arr["body_i64"], "i"), ptr(arr["body_f64"], "f")))
+        if self.ias15 and state.get("body_ias") is not None:
+            ias = np.ascontiguousarray(state["body_ias"], dtype=np.float64)
+            check(lib().posi_batch_set_ias15(self._h, ptr(ias, "f")))
 
 
 class ManyBody:

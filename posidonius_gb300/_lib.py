@@ -24,6 +24,11 @@ SIGNATURES = {
     "posi_last_error": (ctypes.c_char_p, []),
     "posi_device_count": (ctypes.c_int, []),
     "posi_read_case": (ctypes.c_int, [ctypes.c_char_p, _i64p, _i64p, _i64p, _f64p, _i64p, _f64p, _f64p, _f64p]),
+    "posi_read_case_ias15": (ctypes.c_int, [ctypes.c_char_p, _f64p]),
+    "posi_get_ias15": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
+    "posi_set_ias15": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
+    "posi_batch_get_ias15": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
+    "posi_batch_set_ias15": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
     "posi_universe_from_json": (_vp, [ctypes.c_char_p, ctypes.c_int, _intp]),
     "posi_universe_from_arrays": (_vp, [_i64p, _f64p, _i64p, _f64p, _f64p, ctypes.c_int64, _f64p, ctypes.c_int,
                                         _intp]),

@@ -94,7 +94,8 @@ __global__ void static_list_and_check(int32_t* list, int32_t n_sys, int64_t nmax
                     si[(int64_t)POSI_SI_EVOLUTION * n_sys + s] == 0 && n >= 1 && n <= nmax &&
                     (si[(int64_t)POSI_SI_GR * n_sys + s] == 0 ||
                      si[(int64_t)POSI_SI_GR_IMPL * n_sys + s] == POSI_GR_KIDDER1995) &&
-                    si[(int64_t)POSI_SI_WIND * n_sys + s] == 0 && si[(int64_t)POSI_SI_DISK * n_sys + s] == 0;
+                    si[(int64_t)POSI_SI_WIND * n_sys + s] == 0 && si[(int64_t)POSI_SI_DISK * n_sys + s] == 0 &&
+                    si[(int64_t)POSI_SI_INTEGRATOR * n_sys + s] == POSI_INTEGRATOR_WHFAST;
     flags[s] = ok ? 0 : POSI_ADJ_UNSUPPORTED;
 }
 

@@ -110,8 +110,12 @@ bool zero_axes(Ctx& c, const json::Value* v) {
 int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
     Ctx c;
     if (!doc.is_object()) { err = "case is not a JSON object"; return POSI_ERR_PARSE; }
-    if (!doc.find("alternative_coordinates_type")) {
-        err = "not a WHFast case (IAS15 and LeapFrog are outside this path)";
+    // WHFast documents carry the alternative coordinates, Ias15 ones the
+    // Gauss-Radau coefficients (src/integrator/ias15.rs:28-224)
+    const bool ias15 = !doc.find("alternative_coordinates_type") && doc.find("b_0") &&
+                       doc.find("time_step_last_success");
+    if (!doc.find("alternative_coordinates_type") && !ias15) {
+        err = "neither a WHFast nor an IAS15 case (LeapFrog is outside this path)";
         return POSI_ERR_UNSUPPORTED;
     }
     const json::Value* u = req(c, &doc, "universe");
@@ -153,14 +157,47 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
     out.tables.clear();
     out.roche.assign((size_t)n * n, 0.);
 
-    const json::Value* act = req(c, &doc, "alternative_coordinates_type");
-    int coords = -1;
-    if (act && act->is_string()) {
-        if (act->text == "Jacobi") coords = POSI_JACOBI;
-        else if (act->text == "DemocraticHeliocentric") coords = POSI_DEMOCRATIC_HELIOCENTRIC;
-        else if (act->text == "WHDS") coords = POSI_WHDS;
+    int coords = POSI_JACOBI;
+    out.ias.assign((size_t)n * POSI_IAS_COUNT, 0.);
+    if (!ias15) {
+        const json::Value* act = req(c, &doc, "alternative_coordinates_type");
+        coords = -1;
+        if (act && act->is_string()) {
+            if (act->text == "Jacobi") coords = POSI_JACOBI;
+            else if (act->text == "DemocraticHeliocentric") coords = POSI_DEMOCRATIC_HELIOCENTRIC;
+            else if (act->text == "WHDS") coords = POSI_WHDS;
+        }
+        if (coords < 0) { err = "unknown alternative_coordinates_type"; return POSI_ERR_PARSE; }
+    } else {
+        // the serde arrays hold 3 * MAX_PARTICLES values, body i component c at 3i + c
+        struct Blk { int base; const char* name; };
+        static const Blk blocks[] = {{POSI_IAS_B, "b"}, {POSI_IAS_E, "e"}, {POSI_IAS_BR, "br"},
+                                     {POSI_IAS_ER, "er"}, {POSI_IAS_SB, "sb"}, {POSI_IAS_SE, "se"},
+                                     {POSI_IAS_SBR, "sbr"}, {POSI_IAS_SER, "ser"}};
+        auto arr3 = [&](const std::string& key, int base) {
+            const json::Value* a = req(c, &doc, key.c_str());
+            if (!a) return;
+            if (!a->is_array() || (int64_t)a->items.size() < 3 * n) {
+                c.fail(POSI_ERR_PARSE, "field '" + key + "' is shorter than 3 * n_particles");
+                return;
+            }
+            for (int64_t b = 0; b < n; ++b)
+                for (int k = 0; k < 3; ++k) {
+                    const json::Value& x = a->items[(size_t)(3 * b + k)];
+                    if (!x.is_number()) { c.fail(POSI_ERR_PARSE, "field '" + key + "' holds a non-number"); return; }
+                    out.ias[(size_t)b * POSI_IAS_COUNT + base + k] = x.num();
+                }
+        };
+        for (const Blk& bk : blocks)
+            for (int j = 0; j < 7; ++j) arr3(std::string(bk.name) + "_" + std::to_string(j), bk.base + 3 * j);
+        arr3("csx", POSI_IAS_CSX);
+        arr3("csv", POSI_IAS_CSV);
+        arr3("css", POSI_IAS_CSS);
+        out.si[POSI_SI_INTEGRATOR] = POSI_INTEGRATOR_IAS15;
+        out.si[POSI_SI_IAS_MAX_EXCEEDED] = (int64_t)num(c, &doc, "integrator_iterations_max_exceeded");
+        out.sf[POSI_SF_IAS_DT_LAST] = num(c, &doc, "time_step_last_success");
+        if (c.code != POSI_OK) { err = c.err; return c.code; }
     }
-    if (coords < 0) { err = "unknown alternative_coordinates_type"; return POSI_ERR_PARSE; }
     out.si[POSI_SI_N] = n;
     out.si[POSI_SI_HOST] = host;
     out.si[POSI_SI_COORDS] = coords;
@@ -173,9 +210,9 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
     out.si[POSI_SI_EVOLUTION] = evo;
     out.si[POSI_SI_ITERATION] = (int64_t)num(c, &doc, "current_iteration");
     out.si[POSI_SI_N_HIST] = (int64_t)num(c, &doc, "n_historic_snapshots");
-    out.si[POSI_SI_TIMESTEP_WARNING] = (int64_t)num(c, &doc, "timestep_warning");
+    if (!ias15) out.si[POSI_SI_TIMESTEP_WARNING] = (int64_t)num(c, &doc, "timestep_warning");
     out.sf[POSI_SF_DT] = num(c, &doc, "time_step");
-    out.sf[POSI_SF_HALF_DT] = num(c, &doc, "half_time_step");
+    if (!ias15) out.sf[POSI_SF_HALF_DT] = num(c, &doc, "half_time_step");
     out.sf[POSI_SF_TIME] = num(c, &doc, "current_time");
     out.sf[POSI_SF_TIME_LIMIT] = num(c, u, "time_limit");
     out.sf[POSI_SF_LAST_HIST] = num(c, &doc, "last_historic_snapshot_time");
@@ -186,12 +223,13 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
 
     const json::Value* parts = req(c, u, "particles");
     const json::Value* evols = req(c, u, "particles_evolvers");
-    const json::Value* verr = req(c, &doc, "inertial_velocity_errors");
-    const json::Value* lerr = req(c, &doc, "particle_angular_momentum_errors");
+    const json::Value* verr = ias15 ? nullptr : req(c, &doc, "inertial_velocity_errors");
+    const json::Value* lerr = ias15 ? nullptr : req(c, &doc, "particle_angular_momentum_errors");
     if (c.code != POSI_OK) { err = c.err; return c.code; }
     if (!parts->is_array() || (int64_t)parts->items.size() < n || !evols->is_array() ||
-        (int64_t)evols->items.size() < n || !verr->is_array() || (int64_t)verr->items.size() < n ||
-        !lerr->is_array() || (int64_t)lerr->items.size() < n) {
+        (int64_t)evols->items.size() < n ||
+        (!ias15 && (!verr->is_array() || (int64_t)verr->items.size() < n || !lerr->is_array() ||
+                    (int64_t)lerr->items.size() < n))) {
         err = "particle arrays shorter than n_particles";
         return POSI_ERR_PARSE;
     }
@@ -323,7 +361,7 @@ int read_case(const json::Value& doc, FlatSystem& out, std::string& err) {
         axes(c, &p, "angular_momentum", &F[POSI_BF_LX]);
         axes(c, &p, "spin", &F[POSI_BF_SX]);
         F[POSI_BF_NSV2] = num(c, &p, "norm_spin_vector_2");
-        {
+        if (!ias15) {
             const json::Value& ve = verr->items[b];
             const json::Value& le = lerr->items[b];
             F[POSI_BF_EVX] = num(c, &ve, "x"); F[POSI_BF_EVY] = num(c, &ve, "y"); F[POSI_BF_EVZ] = num(c, &ve, "z");

@@ -1,7 +1,8 @@
-// case_reader.hpp -- WHFast JSON case / recovery snapshot -> flat system layout.
+// case_reader.hpp -- WHFast / IAS15 JSON case or recovery snapshot -> flat
+// system layout.
 //
 // The case format is the serde form of `WHFast` (src/integrator/whfast.rs:99-120
-// of the reference) as written by src/integrator/output.rs:28-54 and read back
+// of the reference) or of `Ias15` (src/integrator/ias15.rs:28-224) as written by src/integrator/output.rs:28-54 and read back
 // by output.rs:205-241; enums are externally tagged
 // ("effect": {"CentralBody": {"ConstantTimeLag": {...}}}, "evolution":
 // "NonEvolving" or {"Leconte2011": 0.08}).
@@ -23,6 +24,7 @@ struct FlatSystem {
     std::vector<double> bf;      // n * POSI_BF_COUNT
     std::vector<double> tables;  // evolution tables (4 * rows per evolving body)
     std::vector<double> roche;   // n * n
+    std::vector<double> ias;     // n * POSI_IAS_COUNT (IAS15 cases; zeros otherwise)
 };
 
 // Returns POSI_OK, POSI_ERR_PARSE (missing/ill-typed field) or

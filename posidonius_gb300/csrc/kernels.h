@@ -21,12 +21,15 @@ struct DevView {
     int32_t* step_flags;
     double* hist;
     double* rec;
+    double* ias;
 };
 
 // OP_STEPS_REC: OP_STEPS writing the adjoint's step records to DevView::rec
 // (FAST build only).
 // OP_STEPS_SCHED: OP_STEPS under a balanced schedule (whfast_sched_kernel)
-enum KernelOp { OP_STEPS = 0, OP_INIT = 1, OP_GRAVITY = 2, OP_EFFECTS = 3, OP_STEPS_REC = 4, OP_STEPS_SCHED = 5 };
+// OP_IAS15_STEPS: n_steps IAS15 steps (G = 8, 16 or 32; DevView::ias set)
+enum KernelOp { OP_STEPS = 0, OP_INIT = 1, OP_GRAVITY = 2, OP_EFFECTS = 3, OP_STEPS_REC = 4, OP_STEPS_SCHED = 5,
+                OP_IAS15_STEPS = 6 };
 
 struct LaunchArgs {
     int op;

@@ -16,6 +16,7 @@ static cudaError_t launch_g(const posi::DevView& v, const posi::LaunchArgs& a, c
     d.step_flags = v.step_flags;
     d.hist = v.hist;
     d.rec = v.rec;
+    d.ias = v.ias;
     const int threads = posi::kBlockThreads;
     const int groups_per_block = threads / G;
     const int blocks = (int)((v.n_list + groups_per_block - 1) / groups_per_block);
@@ -37,6 +38,14 @@ static cudaError_t launch_g(const posi::DevView& v, const posi::LaunchArgs& a, c
                 const size_t ssmem = (size_t)(posi::kSchedBlockThreads / G) * GroupSmem<G>::bytes;
                 whfast_sched_kernel<G><<<a.sched_blocks, posi::kSchedBlockThreads, ssmem, stream>>>(d, a.slot_job,
                                                                                                    a.slot_steps);
+                break;
+            } else {
+                return cudaErrorInvalidValue;
+            }
+        case posi::OP_IAS15_STEPS:
+            if constexpr (G >= 8) {
+                if (!d.ias) return cudaErrorInvalidValue;
+                ias15_steps_kernel<G><<<blocks, threads, smem, stream>>>(d, a.n_steps);
                 break;
             } else {
                 return cudaErrorInvalidValue;
@@ -67,6 +76,11 @@ static cudaError_t prepare_g() {
     if constexpr (G >= 4) {
         const int ssmem = (posi::kSchedBlockThreads / G) * GroupSmem<G>::bytes;
         if ((e = cudaFuncSetAttribute(whfast_sched_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, ssmem)) !=
+            cudaSuccess)
+            return e;
+    }
+    if constexpr (G >= 8) {
+        if ((e = cudaFuncSetAttribute(ias15_steps_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
             cudaSuccess)
             return e;
     }

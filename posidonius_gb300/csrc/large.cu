@@ -81,6 +81,8 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
         return fail(POSI_ERR_UNSUPPORTED, "the many-body engine supports Kidder1995 general relativity only", nullptr);
     if (sys_i64[POSI_SI_WIND] != 0 || sys_i64[POSI_SI_DISK] != 0)
         return fail(POSI_ERR_UNSUPPORTED, "the many-body engine does not support wind or disk", nullptr);
+    if (sys_i64[POSI_SI_INTEGRATOR] != POSI_INTEGRATOR_WHFAST)
+        return fail(POSI_ERR_UNSUPPORTED, "the many-body engine integrates with WHFast only", nullptr);
     const int64_t host = sys_i64[POSI_SI_HOST];
     if (host < 0 || host >= n) return fail(POSI_ERR_ARG, "host index out of range", nullptr);
     for (int64_t i = 0; i < n; ++i)

@@ -91,6 +91,10 @@ struct posi_batch {
     int32_t* d_list = nullptr;
     int32_t* d_flags = nullptr;
     double* d_hist = nullptr;  // historic records (attached by the snapshot writer)
+    // IAS15 batches (every system integrated by IAS15): the per-body
+    // Gauss-Radau state [POSI_IAS_COUNT][stride]
+    bool ias15 = false;
+    double* d_ias = nullptr;
     void* d_stage = nullptr;  // AoS staging buffer
     size_t stage_bytes = 0;
     int64_t n_tables = 0;
@@ -125,11 +129,13 @@ struct posi_batch {
         v.step_flags = d_flags;
         v.hist = d_hist;
         v.rec = nullptr;
+        v.ias = d_ias;
         return v;
     }
     cudaError_t launch(const Bucket& bk, const LaunchArgs& a0, cudaStream_t on = nullptr) const {
         LaunchArgs a = a0;
         a.G = bk.G;
+        if (ias15 && a.op == posi::OP_STEPS) a.op = posi::OP_IAS15_STEPS;
         DevView v = view(bk.offset, bk.count);
         cudaStream_t st = on ? on : stream;
         return mode == POSI_MODE_EXACT ? posi::launch_exact(v, a, st) : posi::launch_fast(v, a, st);
@@ -160,6 +166,7 @@ void free_batch(posi_batch* b) {
     cudaFree(b->d_roche); cudaFree(b->d_tables); cudaFree(b->d_list); cudaFree(b->d_flags);
     cudaFree(b->d_stage);
     cudaFree(b->d_hist);
+    cudaFree(b->d_ias);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -172,6 +179,8 @@ int validate_system(const int64_t* si, int64_t nmax, std::string& err) {
     if (posi::group_size_for(n) == 0) { err = "too many bodies for the batched kernel"; return POSI_ERR_UNSUPPORTED; }
     if (host < 0 || host >= n) { err = "host index out of range"; return POSI_ERR_ARG; }
     if (coords < POSI_JACOBI || coords > POSI_WHDS) { err = "unknown coordinates type"; return POSI_ERR_ARG; }
+    const int64_t integ = si[POSI_SI_INTEGRATOR];
+    if (integ != POSI_INTEGRATOR_WHFAST && integ != POSI_INTEGRATOR_IAS15) { err = "unknown integrator"; return POSI_ERR_ARG; }
     return POSI_OK;
 }
 
@@ -216,6 +225,7 @@ int build_buckets(posi_batch* b, const int64_t* sys_i64, const std::map<int64_t,
         } else if (b->mapping >= POSI_MAP_LANES2 && b->mapping <= POSI_MAP_WARP && b->mapping >= G) {
             G = b->mapping;
         }
+        if (b->ias15 && G < 8) G = 8;   // the IAS15 kernel runs groups of 8, 16 or 32 lanes
         by_g[G].push_back((int32_t)s);
         b->mapping_of_n[n] = G;
     }
@@ -310,6 +320,10 @@ posi_batch* create_batch(int64_t n_sys, int64_t nmax, const int64_t* si, const d
         std::string err;
         int rc = validate_system(si + s * POSI_SI_COUNT, nmax, err);
         if (rc != POSI_OK) { g_last_error = err; return fail(rc, nullptr); }
+        if (si[s * POSI_SI_COUNT + POSI_SI_INTEGRATOR] != si[POSI_SI_INTEGRATOR]) {
+            g_last_error = "a batch holds systems of one integrator";
+            return fail(POSI_ERR_UNSUPPORTED, nullptr);
+        }
     }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
@@ -323,6 +337,7 @@ posi_batch* create_batch(int64_t n_sys, int64_t nmax, const int64_t* si, const d
     b->mode = mode;
     b->mapping = mapping;
     b->n_tables = std::max<int64_t>(1, n_tables);
+    b->ias15 = si[POSI_SI_INTEGRATOR] == POSI_INTEGRATOR_IAS15;
     auto ok = [&](cudaError_t e) {
         if (e != cudaSuccess) { g_last_error = cudaGetErrorString(e); return false; }
         return true;
@@ -338,6 +353,7 @@ posi_batch* create_batch(int64_t n_sys, int64_t nmax, const int64_t* si, const d
     }
     const size_t nb = (size_t)b->stride;
     b->stage_bytes = std::max({nb * POSI_BF_COUNT * sizeof(double), nb * POSI_BI_COUNT * sizeof(int64_t),
+                               b->ias15 ? nb * POSI_IAS_COUNT * sizeof(double) : (size_t)0,
                                (size_t)n_sys * POSI_SF_COUNT * sizeof(double),
                                (size_t)n_sys * POSI_SI_COUNT * sizeof(int64_t), nb * nmax * sizeof(double)});
     if (!ok(cudaMalloc(&b->d_bf, nb * POSI_BF_COUNT * sizeof(double))) ||
@@ -347,6 +363,9 @@ posi_batch* create_batch(int64_t n_sys, int64_t nmax, const int64_t* si, const d
         !ok(cudaMalloc(&b->d_roche, nb * nmax * sizeof(double))) ||
         !ok(cudaMalloc(&b->d_tables, (size_t)b->n_tables * sizeof(double))) ||
         !ok(cudaMalloc(&b->d_flags, (size_t)n_sys * sizeof(int32_t))) || !ok(cudaMalloc(&b->d_stage, b->stage_bytes)))
+        return fail(POSI_ERR_CUDA, b);
+    if (b->ias15 && (!ok(cudaMalloc(&b->d_ias, nb * POSI_IAS_COUNT * sizeof(double))) ||
+                     !ok(cudaMemsetAsync(b->d_ias, 0, nb * POSI_IAS_COUNT * sizeof(double), b->stream))))
         return fail(POSI_ERR_CUDA, b);
     int rc;
     if ((rc = upload_aos<int64_t>(b, si, b->d_si, n_sys, POSI_SI_COUNT)) != POSI_OK ||
@@ -521,6 +540,18 @@ int posi_read_case(const char* path, int64_t* n, int64_t* n_tables, int64_t* sys
     return POSI_OK;
 }
 
+int posi_read_case_ias15(const char* path, double* body_ias) {
+    posi::FlatSystem fs;
+    int rc = load_case_file(path, fs);
+    if (rc != POSI_OK) return rc;
+    if (fs.si[POSI_SI_INTEGRATOR] != POSI_INTEGRATOR_IAS15) {
+        g_last_error = "not an IAS15 case";
+        return POSI_ERR_STATE;
+    }
+    if (body_ias) std::memcpy(body_ias, fs.ias.data(), fs.ias.size() * sizeof(double));
+    return POSI_OK;
+}
+
 posi_handle* posi_universe_from_json(const char* path, int mode, int* status) {
     posi::FlatSystem fs;
     posi::json::Value doc;
@@ -533,6 +564,11 @@ posi_handle* posi_universe_from_json(const char* path, int mode, int* status) {
                                  fs.tables.empty() ? nullptr : fs.tables.data(), (int64_t)fs.tables.size(),
                                  fs.roche.data(), mode, POSI_MAP_AUTO, status);
     if (!b) return nullptr;
+    if (b->ias15 && (rc = posi_batch_set_ias15(b, fs.ias.data())) != POSI_OK) {
+        free_batch(b);
+        if (status) *status = rc;
+        return nullptr;
+    }
     posi_handle* h = make_handle(b, fs.si.data(), fs.sf.data());
     h->doc = std::make_shared<posi::json::Value>(std::move(doc));
     return h;
@@ -628,6 +664,55 @@ std::string fatal_message(const int64_t* si) {
 }
 }  // namespace
 
+namespace {
+// src/integrator/ias15.rs:420-463, n_steps times: the adaptive step makes the
+// triggers unpredictable on the host, so every step is one launch followed by
+// a read of its trigger flags, its historic record and the system status.
+int iterate_ias15(posi_handle* h, int64_t n_steps, int64_t* steps_done, int* recovery_trigger) {
+    posi_batch* b = h->b;
+    const int64_t n = h->si[POSI_SI_N];
+    std::vector<double> record;
+    std::vector<unsigned char> bytes;
+    if (h->hist) record.resize((size_t)n * posi::kHistoryFields);
+    LaunchArgs a{};
+    a.op = posi::OP_STEPS;
+    a.n_steps = 1;
+    const int64_t it0 = h->si[POSI_SI_ITERATION];
+    bool rec = false;
+    for (int64_t k = 0; k < n_steps && !rec; ++k) {
+        if (h->hist) CK(cudaMemsetAsync(b->d_hist, 0xff, record.size() * sizeof(double), b->stream));
+        CK(cudaMemsetAsync(b->d_flags, 0, sizeof(int32_t), b->stream));
+        for (const Bucket& bk : b->buckets) CK(b->launch(bk, a));
+        int32_t flags = 0;
+        CK(cudaMemcpyAsync(&flags, b->d_flags, sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream));
+        if (h->hist)
+            CK(cudaMemcpyAsync(record.data(), b->d_hist, record.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                               b->stream));
+        CK(cudaStreamSynchronize(b->stream));
+        if (h->hist && !std::isnan(record[0])) {
+            bytes.clear();
+            posi::encode_history_record(record.data(), n, bytes);
+            if (std::fwrite(bytes.data(), 1, bytes.size(), h->hist) != bytes.size()) {
+                g_last_error = "cannot write the history file";
+                return POSI_ERR_IO;
+            }
+        }
+        int rc = refresh_mirror(h);
+        if (rc != POSI_OK) return rc;
+        if (steps_done) *steps_done = h->si[POSI_SI_ITERATION] - it0;
+        const int64_t fatal = h->si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK;
+        if (fatal == POSI_SYS_COMPLETED) return POSI_COMPLETED;
+        if (fatal) {
+            g_last_error = fatal_message(h->si.data());
+            return POSI_ERR_PHYSICS;
+        }
+        rec = (flags & 1) != 0;
+    }
+    if (recovery_trigger) *recovery_trigger = rec ? 1 : 0;
+    return POSI_OK;
+}
+}  // namespace
+
 int posi_iterate(posi_handle* h, int64_t n_steps, int64_t* steps_done, int* recovery_trigger) {
     if (!h || n_steps < 0) return POSI_ERR_ARG;
     if (steps_done) *steps_done = 0;
@@ -637,6 +722,7 @@ int posi_iterate(posi_handle* h, int64_t n_steps, int64_t* steps_done, int* reco
         g_last_error = fatal_message(h->si.data());
         return POSI_ERR_PHYSICS;
     }
+    if (h->b->ias15) return iterate_ias15(h, n_steps, steps_done, recovery_trigger);
     // Predict, with the kernel's own time arithmetic, how many steps run before
     // a step reports a recovery trigger or completes the simulation; the plain
     // path then runs exactly that many steps.
@@ -826,8 +912,14 @@ int posi_write_recovery_snapshot(posi_handle* h, const char* path) {
     std::vector<double> sf(POSI_SF_COUNT), bf((size_t)n * POSI_BF_COUNT), roche((size_t)n * n);
     rc = batch_get(h->b, si.data(), sf.data(), bi.data(), bf.data(), roche.data());
     if (rc != POSI_OK) return rc;
+    std::vector<double> ias;
+    if (h->b->ias15) {
+        ias.resize((size_t)n * POSI_IAS_COUNT);
+        if ((rc = posi_batch_get_ias15(h->b, ias.data())) != POSI_OK) return rc;
+    }
     std::string err;
-    if (!posi::update_case_document(*h->doc, n, si.data(), sf.data(), bi.data(), bf.data(), roche.data(), err)) {
+    if (!posi::update_case_document(*h->doc, n, si.data(), sf.data(), bi.data(), bf.data(), roche.data(),
+                                    ias.empty() ? nullptr : ias.data(), err)) {
         g_last_error = err;
         return POSI_ERR_PARSE;
     }
@@ -895,7 +987,7 @@ int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch)
             const int64_t len = std::min(steps_per_launch, n_steps - c * steps_per_launch);
             for (size_t k = 0; k < b->buckets.size(); ++k) {
                 const Bucket& bk = b->buckets[k];
-                if (!b->balanced || bk.G < 4 || plan.count({len, k})) continue;
+                if (!b->balanced || b->ias15 || bk.G < 4 || plan.count({len, k})) continue;
                 const int jobs = (int)((bk.count + (32 / bk.G) - 1) / (32 / bk.G));
                 std::vector<int32_t> t;
                 int launches = 0;
@@ -1000,6 +1092,40 @@ int posi_batch_set_state(posi_batch* b, const int64_t* sys_i64, const double* sy
     return batch_set(b, sys_i64, sys_f64, body_i64, body_f64);
 }
 
+int posi_batch_get_ias15(const posi_batch* b, double* body_ias) {
+    if (!b || !body_ias) return POSI_ERR_ARG;
+    if (!b->ias15) {
+        g_last_error = "not an IAS15 batch";
+        return POSI_ERR_STATE;
+    }
+    int rc = download_aos<double>(b, body_ias, b->d_ias, b->stride, POSI_IAS_COUNT);
+    if (rc != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    return POSI_OK;
+}
+
+int posi_batch_set_ias15(posi_batch* b, const double* body_ias) {
+    if (!b || !body_ias) return POSI_ERR_ARG;
+    if (!b->ias15) {
+        g_last_error = "not an IAS15 batch";
+        return POSI_ERR_STATE;
+    }
+    int rc = upload_aos<double>(b, body_ias, b->d_ias, b->stride, POSI_IAS_COUNT);
+    if (rc != POSI_OK) return rc;
+    CK(cudaStreamSynchronize(b->stream));
+    return POSI_OK;
+}
+
+int posi_get_ias15(const posi_handle* h, double* body_ias) {
+    if (!h) return POSI_ERR_ARG;
+    return posi_batch_get_ias15(h->b, body_ias);
+}
+
+int posi_set_ias15(posi_handle* h, const double* body_ias) {
+    if (!h) return POSI_ERR_ARG;
+    return posi_batch_set_ias15(h->b, body_ias);
+}
+
 // Autotuner: for every body count present, run each admissible lane mapping
 // (2..32 lanes per system, at least one lane per body) on the systems of that
 // count for probe_steps steps -- once to warm up, once timed with CUDA events
@@ -1007,6 +1133,13 @@ int posi_batch_set_state(posi_batch* b, const int64_t* sys_i64, const double* sy
 // buckets are then rebuilt with the chosen mappings.
 int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n) {
     if (!b || probe_steps < 1) return POSI_ERR_ARG;
+    if (b->ias15) {
+        // the IAS15 kernel's lane groups are fixed (8, 16 or 32 lanes)
+        if (lanes_by_n)
+            for (int k = 0; k <= POSI_MAX_BODIES; ++k)
+                lanes_by_n[k] = b->mapping_of_n.count(k) ? b->mapping_of_n.at(k) : 0;
+        return POSI_OK;
+    }
     const size_t nb = (size_t)b->stride;
     const size_t bytes_bf = nb * POSI_BF_COUNT * sizeof(double), bytes_bi = nb * POSI_BI_COUNT * sizeof(int64_t);
     const size_t bytes_sf = (size_t)b->n_sys * POSI_SF_COUNT * sizeof(double);
@@ -1113,8 +1246,16 @@ struct posi_adjoint {
     int64_t n_steps = 0, every = 0, n_chunks = 0;
     bool have_forward = false;
     size_t bytes_bf = 0, bytes_sf = 0, bytes_si = 0, bytes_ck = 0;
-    char* d_ckpt = nullptr;   // n_chunks + 1 states: chunk starts, then the final state
-    double* d_tape = nullptr;  // step records of one chunk
+    char* d_ckpt = nullptr;   // n_chunks states: the chunks' starts
+    // Backward pass: chunk c is re-integrated from a copy of its checkpoint in
+    // work slot c % n_buf, writing tape c % n_buf on rec_stream, while the
+    // reverse sweep of chunk c + 1 runs on the batch stream (two buffers; one
+    // when the second tape does not fit, and then the two alternate).
+    int n_buf = 0;
+    char* d_work = nullptr;    // n_buf states
+    double* d_tape[2] = {nullptr, nullptr};
+    cudaStream_t rec_stream = nullptr;
+    cudaEvent_t rec_done[2] = {nullptr, nullptr}, rev_done[2] = {nullptr, nullptr}, ready = nullptr;
     double* d_lam = nullptr;
     double* d_grad = nullptr;
     int32_t* d_err = nullptr;
@@ -1126,34 +1267,46 @@ struct posi_adjoint {
 namespace {
 void free_adjoint(posi_adjoint* a) {
     if (!a) return;
-    cudaFree(a->d_ckpt); cudaFree(a->d_tape); cudaFree(a->d_lam); cudaFree(a->d_grad);
-    cudaFree(a->d_err); cudaFree(a->d_list);
+    cudaFree(a->d_ckpt); cudaFree(a->d_work); cudaFree(a->d_tape[0]); cudaFree(a->d_tape[1]);
+    cudaFree(a->d_lam); cudaFree(a->d_grad); cudaFree(a->d_err); cudaFree(a->d_list);
+    for (int k = 0; k < 2; ++k) {
+        if (a->rec_done[k]) cudaEventDestroy(a->rec_done[k]);
+        if (a->rev_done[k]) cudaEventDestroy(a->rev_done[k]);
+    }
+    if (a->ready) cudaEventDestroy(a->ready);
+    if (a->rec_stream) cudaStreamDestroy(a->rec_stream);
     delete a;
 }
 
-int adj_copy_state(posi_adjoint* a, int64_t slot, bool save) {
+// Saves the batch state into checkpoint slot `slot`.
+int adj_save_state(posi_adjoint* a, int64_t slot) {
     posi_batch* b = a->b;
     char* base = a->d_ckpt + (size_t)slot * a->bytes_ck;
     auto cp = [&](void* dst, const void* src, size_t n) { return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToDevice, b->stream); };
-    if (save) {
-        CK(cp(base, b->d_bf, a->bytes_bf));
-        CK(cp(base + a->bytes_bf, b->d_sf, a->bytes_sf));
-        CK(cp(base + a->bytes_bf + a->bytes_sf, b->d_si, a->bytes_si));
-    } else {
-        CK(cp(b->d_bf, base, a->bytes_bf));
-        CK(cp(b->d_sf, base + a->bytes_bf, a->bytes_sf));
-        CK(cp(b->d_si, base + a->bytes_bf + a->bytes_sf, a->bytes_si));
-    }
+    CK(cp(base, b->d_bf, a->bytes_bf));
+    CK(cp(base + a->bytes_bf, b->d_sf, a->bytes_sf));
+    CK(cp(base + a->bytes_bf + a->bytes_sf, b->d_si, a->bytes_si));
     return POSI_OK;
 }
 
-posi::AdjView adj_view(const posi_adjoint* a, const Bucket& bk) {
+// A state (body fields, system scalars and integers) laid out as a checkpoint.
+struct StateRef {
+    double* bf;
+    double* sf;
+    int64_t* si;
+};
+
+StateRef state_at(const posi_adjoint* a, char* base) {
+    return {(double*)base, (double*)(base + a->bytes_bf), (int64_t*)(base + a->bytes_bf + a->bytes_sf)};
+}
+
+posi::AdjView adj_view(const posi_adjoint* a, const Bucket& bk, const StateRef& x, double* tape) {
     const posi_batch* b = a->b;
     posi::AdjView v;
     v.n_sys = b->n_sys; v.nmax = b->nmax; v.stride = b->stride;
-    v.bf = b->d_bf; v.bi = b->d_bi; v.sf = b->d_sf; v.si = b->d_si;
+    v.bf = x.bf; v.bi = b->d_bi; v.sf = x.sf; v.si = x.si;
     v.list = a->d_list + bk.offset; v.n_list = bk.count;
-    v.tape = a->d_tape; v.lam = a->d_lam; v.grad = a->d_grad; v.err = a->d_err;
+    v.tape = tape; v.lam = a->d_lam; v.grad = a->d_grad; v.err = a->d_err;
     return v;
 }
 }  // namespace
@@ -1179,6 +1332,8 @@ posi_adjoint* posi_adjoint_create(posi_batch* b, int64_t n_steps, int64_t checkp
             return fail(POSI_ERR_UNSUPPORTED, "the adjoint supports Kidder1995 general relativity only", nullptr);
         if (x[POSI_SI_WIND] != 0 || x[POSI_SI_DISK] != 0)
             return fail(POSI_ERR_UNSUPPORTED, "the adjoint does not support wind or disk", nullptr);
+        if (x[POSI_SI_INTEGRATOR] != POSI_INTEGRATOR_WHFAST)
+            return fail(POSI_ERR_UNSUPPORTED, "the adjoint differentiates the WHFast step only", nullptr);
         const int G = posi::adjoint_group_size(x[POSI_SI_N]);
         if (G == 0) return fail(POSI_ERR_UNSUPPORTED, "the adjoint supports systems of up to 8 bodies", nullptr);
         by_g[G].push_back((int32_t)s);
@@ -1206,15 +1361,28 @@ posi_adjoint* posi_adjoint_create(posi_batch* b, int64_t n_steps, int64_t checkp
         if (e != cudaSuccess) { g_last_error = cudaGetErrorString(e); return false; }
         return true;
     };
+    const size_t bytes_tape = (size_t)checkpoint_every * posi::kAdjTapeFields * nb * sizeof(double);
     if (!ok(posi::prepare_adjoint()) ||
-        !ok(cudaMalloc(&a->d_ckpt, a->bytes_ck * (size_t)(a->n_chunks + 1))) ||
-        !ok(cudaMalloc(&a->d_tape, (size_t)checkpoint_every * posi::kAdjTapeFields * nb * sizeof(double))) ||
+        !ok(cudaMalloc(&a->d_ckpt, a->bytes_ck * (size_t)a->n_chunks)) ||
+        !ok(cudaMalloc(&a->d_tape[0], bytes_tape)) ||
         !ok(cudaMalloc(&a->d_lam, nb * 12 * sizeof(double))) || !ok(cudaMalloc(&a->d_grad, nb * 2 * sizeof(double))) ||
         !ok(cudaMalloc(&a->d_err, (size_t)b->n_sys * sizeof(int32_t))) ||
         !ok(cudaMalloc(&a->d_list, list.size() * sizeof(int32_t))) ||
         !ok(cudaMemcpyAsync(a->d_list, list.data(), list.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream)) ||
         !ok(cudaStreamSynchronize(b->stream)))
         return fail(POSI_ERR_CUDA, g_last_error, a);
+    // the second tape and work slot are optional
+    a->n_buf = 1;
+    if (a->n_chunks > 1 && cudaMalloc(&a->d_tape[1], bytes_tape) == cudaSuccess) a->n_buf = 2;
+    cudaGetLastError();
+    if (!ok(cudaMalloc(&a->d_work, a->bytes_ck * (size_t)a->n_buf)) ||
+        !ok(cudaStreamCreateWithFlags(&a->rec_stream, cudaStreamNonBlocking)) ||
+        !ok(cudaEventCreateWithFlags(&a->ready, cudaEventDisableTiming)))
+        return fail(POSI_ERR_CUDA, g_last_error, a);
+    for (int k = 0; k < 2; ++k)
+        if (!ok(cudaEventCreateWithFlags(&a->rec_done[k], cudaEventDisableTiming)) ||
+            !ok(cudaEventCreateWithFlags(&a->rev_done[k], cudaEventDisableTiming)))
+            return fail(POSI_ERR_CUDA, g_last_error, a);
     if (status) *status = POSI_OK;
     return a;
 }
@@ -1230,11 +1398,10 @@ int posi_adjoint_forward(posi_adjoint* a) {
     CK(cudaEventRecord(e0, b->stream));
     int rc = POSI_OK;
     for (int64_t c = 0; c < a->n_chunks && rc == POSI_OK; ++c) {
-        if ((rc = adj_copy_state(a, c, true)) != POSI_OK) break;
+        if ((rc = adj_save_state(a, c)) != POSI_OK) break;
         const int64_t len = std::min(a->every, a->n_steps - c * a->every);
         rc = posi_batch_iterate(b, len, len);
     }
-    if (rc == POSI_OK) rc = adj_copy_state(a, a->n_chunks, true);
     CK(cudaEventRecord(e1, b->stream));
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -1265,14 +1432,26 @@ int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_
     CK(cudaGetLastError());
     CK(cudaMemsetAsync(a->d_grad, 0, (size_t)nb * 2 * sizeof(double), b->stream));
     CK(cudaMemsetAsync(a->d_err, 0, (size_t)b->n_sys * sizeof(int32_t), b->stream));
-    int rc = POSI_OK;
-    // per chunk: [restore + record | reverse] marks, for the time split
-    std::vector<cudaEvent_t> marks((size_t)a->n_chunks * 3);
+    // The chunks' re-integrations are independent (each starts from its
+    // checkpoint), so chunk c - 1 is re-integrated on rec_stream while the
+    // reverse sweep of chunk c runs; the batch's own state is not touched.
+    CK(cudaEventRecord(a->ready, b->stream));
+    CK(cudaStreamWaitEvent(a->rec_stream, a->ready, 0));
+    // per chunk: record start / end (rec_stream), reverse start / end
+    std::vector<cudaEvent_t> marks((size_t)a->n_chunks * 4);
     for (auto& e : marks) CK(cudaEventCreate(&e));
-    for (int64_t c = a->n_chunks - 1; c >= 0 && rc == POSI_OK; --c) {
-        CK(cudaEventRecord(marks[(size_t)c * 3], b->stream));
-        if ((rc = adj_copy_state(a, c, false)) != POSI_OK) break;
+    for (int64_t c = a->n_chunks - 1; c >= 0; --c) {
+        const int buf = (int)(c % a->n_buf);
         const int64_t len = std::min(a->every, a->n_steps - c * a->every);
+        char* work = a->d_work + (size_t)buf * a->bytes_ck;
+        const StateRef x = state_at(a, work);
+        double* tape = a->d_tape[buf];
+        cudaEvent_t* mk = marks.data() + (size_t)c * 4;
+        // the buffers' previous reader is the reverse sweep of chunk c + n_buf
+        if (c + a->n_buf < a->n_chunks) CK(cudaStreamWaitEvent(a->rec_stream, a->rev_done[buf], 0));
+        CK(cudaEventRecord(mk[0], a->rec_stream));
+        CK(cudaMemcpyAsync(work, a->d_ckpt + (size_t)c * a->bytes_ck, a->bytes_ck, cudaMemcpyDeviceToDevice,
+                           a->rec_stream));
         if (b->mode == POSI_MODE_FAST) {
             // re-integrate the chunk with the forward kernel itself, writing
             // the step records as it goes
@@ -1282,23 +1461,29 @@ int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_
             for (const Bucket& bk : b->buckets) {
                 la.G = bk.G;
                 DevView v = b->view(bk.offset, bk.count);
-                v.rec = a->d_tape;
-                CK(posi::launch_fast(v, la, b->stream));
+                v.bf = x.bf; v.sf = x.sf; v.si = x.si;
+                v.rec = tape;
+                CK(posi::launch_fast(v, la, a->rec_stream));
             }
         } else {
-            for (const Bucket& bk : a->buckets) CK(posi::launch_adjoint(adj_view(a, bk), 0, len, bk.G, b->stream));
+            for (const Bucket& bk : a->buckets)
+                CK(posi::launch_adjoint(adj_view(a, bk, x, tape), 0, len, bk.G, a->rec_stream));
         }
-        CK(cudaEventRecord(marks[(size_t)c * 3 + 1], b->stream));
-        for (const Bucket& bk : a->buckets) CK(posi::launch_adjoint(adj_view(a, bk), 1, len, bk.G, b->stream));
-        CK(cudaEventRecord(marks[(size_t)c * 3 + 2], b->stream));
+        CK(cudaEventRecord(mk[1], a->rec_stream));
+        CK(cudaEventRecord(a->rec_done[buf], a->rec_stream));
+        CK(cudaStreamWaitEvent(b->stream, a->rec_done[buf], 0));
+        CK(cudaEventRecord(mk[2], b->stream));
+        for (const Bucket& bk : a->buckets)
+            CK(posi::launch_adjoint(adj_view(a, bk, x, tape), 1, len, bk.G, b->stream));
+        CK(cudaEventRecord(mk[3], b->stream));
+        CK(cudaEventRecord(a->rev_done[buf], b->stream));
     }
-    if (rc != POSI_OK) return rc;
     CK(cudaStreamSynchronize(b->stream));
     a->record_ms = a->reverse_ms = 0.;
     for (int64_t c = 0; c < a->n_chunks; ++c) {
         float m1 = 0.f, m2 = 0.f;
-        cudaEventElapsedTime(&m1, marks[(size_t)c * 3], marks[(size_t)c * 3 + 1]);
-        cudaEventElapsedTime(&m2, marks[(size_t)c * 3 + 1], marks[(size_t)c * 3 + 2]);
+        cudaEventElapsedTime(&m1, marks[(size_t)c * 4], marks[(size_t)c * 4 + 1]);
+        cudaEventElapsedTime(&m2, marks[(size_t)c * 4 + 2], marks[(size_t)c * 4 + 3]);
         a->record_ms += m1;
         a->reverse_ms += m2;
     }
@@ -1319,8 +1504,6 @@ int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_
     }
     std::vector<int32_t> err((size_t)b->n_sys);
     CK(cudaMemcpyAsync(err.data(), a->d_err, err.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream));
-    // leave the batch at the end of the forward run
-    if ((rc = adj_copy_state(a, a->n_chunks, false)) != POSI_OK) return rc;
     CK(cudaStreamSynchronize(b->stream));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
@@ -1330,6 +1513,7 @@ int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_
     if (system_flags) {
         // systems the forward run froze (collision, Roche limit, ejection...)
         std::vector<int64_t> si((size_t)b->n_sys * POSI_SI_COUNT);
+        int rc;
         if ((rc = batch_get(b, si.data(), nullptr, nullptr, nullptr, nullptr)) != POSI_OK) return rc;
         for (int64_t s = 0; s < b->n_sys; ++s) {
             const int64_t st = si[(size_t)s * POSI_SI_COUNT + POSI_SI_STATUS] & POSI_SYS_FATAL_MASK;

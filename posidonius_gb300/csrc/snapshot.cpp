@@ -108,7 +108,7 @@ void write_json(const json::Value& v, std::string& out, int indent) {
 }
 
 bool update_case_document(json::Value& doc, int64_t n, const int64_t* si, const double* sf, const int64_t* bi,
-                          const double* bf, const double* roche, std::string& err) {
+                          const double* bf, const double* roche, const double* ias, std::string& err) {
     auto need = [&](json::Value* v, const char* what) {
         if (!v) err = std::string("case document lacks ") + what;
         return v != nullptr;
@@ -126,25 +126,60 @@ bool update_case_document(json::Value& doc, int64_t n, const int64_t* si, const 
         if (!need(v, f.key)) return false;
         set_number(*v, f.v);
     }
+    const bool ias15 = si[POSI_SI_INTEGRATOR] == POSI_INTEGRATOR_IAS15;
     struct I { const char* key; int64_t v; };
     const I i64s[] = {{"current_iteration", si[POSI_SI_ITERATION]},
                       {"n_historic_snapshots", si[POSI_SI_N_HIST]},
-                      {"timestep_warning", si[POSI_SI_TIMESTEP_WARNING]},
+                      {ias15 ? "integrator_iterations_max_exceeded" : "timestep_warning",
+                       ias15 ? si[POSI_SI_IAS_MAX_EXCEEDED] : si[POSI_SI_TIMESTEP_WARNING]},
                       {"hash", 0}};
     for (const I& f : i64s) {
         json::Value* v = member(&doc, f.key);
         if (!need(v, f.key)) return false;
         set_integer(*v, f.v);
     }
+    if (ias15) {
+        // src/integrator/ias15.rs:28-224: the adaptive step and the per-body
+        // Gauss-Radau state that carries over to the next step (the arrays
+        // hold 3 * MAX_PARTICLES values, body i component c at 3i + c; the
+        // scratch arrays g, at, x0, v0, a0, ... are rewritten by every step
+        // and keep the values the document had)
+        const F fs[] = {{"time_step", sf[POSI_SF_DT]}, {"time_step_last_success", sf[POSI_SF_IAS_DT_LAST]}};
+        for (const F& f : fs) {
+            json::Value* v = member(&doc, f.key);
+            if (!need(v, f.key)) return false;
+            set_number(*v, f.v);
+        }
+        if (!ias) { err = "IAS15 state missing"; return false; }
+        struct Blk { int base; const char* name; };
+        static const Blk blocks[] = {{POSI_IAS_B, "b"}, {POSI_IAS_E, "e"}, {POSI_IAS_BR, "br"},
+                                     {POSI_IAS_ER, "er"}, {POSI_IAS_SB, "sb"}, {POSI_IAS_SE, "se"},
+                                     {POSI_IAS_SBR, "sbr"}, {POSI_IAS_SER, "ser"}};
+        auto put = [&](const std::string& key, int base) {
+            json::Value* a = member(&doc, key.c_str());
+            if (!a || a->kind != json::Value::Array || (int64_t)a->items.size() < 3 * n) {
+                err = "case document lacks " + key;
+                return false;
+            }
+            for (int64_t b = 0; b < n; ++b)
+                for (int k = 0; k < 3; ++k)
+                    set_number(a->items[(size_t)(3 * b + k)], ias[(size_t)b * POSI_IAS_COUNT + base + k]);
+            return true;
+        };
+        for (const Blk& bk : blocks)
+            for (int j = 0; j < 7; ++j)
+                if (!put(std::string(bk.name) + "_" + std::to_string(j), bk.base + 3 * j)) return false;
+        if (!put("csx", POSI_IAS_CSX) || !put("csv", POSI_IAS_CSV) || !put("css", POSI_IAS_CSS)) return false;
+    }
     json::Value* tl = member(u, "time_limit");
     if (!need(tl, "time_limit")) return false;
     set_number(*tl, sf[POSI_SF_TIME_LIMIT]);
     json::Value* parts = member(u, "particles");
     json::Value* evols = member(u, "particles_evolvers");
-    json::Value* verr = member(&doc, "inertial_velocity_errors");
-    json::Value* lerr = member(&doc, "particle_angular_momentum_errors");
-    if (!need(parts, "particles") || !need(evols, "particles_evolvers") || !need(verr, "inertial_velocity_errors") ||
-        !need(lerr, "particle_angular_momentum_errors"))
+    json::Value* verr = ias15 ? nullptr : member(&doc, "inertial_velocity_errors");
+    json::Value* lerr = ias15 ? nullptr : member(&doc, "particle_angular_momentum_errors");
+    if (!need(parts, "particles") || !need(evols, "particles_evolvers") ||
+        (!ias15 && (!need(verr, "inertial_velocity_errors") || !need(lerr, "particle_angular_momentum_errors"))))
         return false;
     for (int64_t b = 0; b < n; ++b) {
         const double* F = bf + (size_t)b * POSI_BF_COUNT;
@@ -191,7 +226,8 @@ bool update_case_document(json::Value& doc, int64_t n, const int64_t* si, const 
             json::Value* mts = dint ? member(dint, "migration_timescale") : nullptr;
             if (mts) set_number(*mts, F[POSI_BF_DISK_MTS]);
         }
-        if (!set_axes(&verr->items[(size_t)b], F + POSI_BF_EVX) || !set_axes(&lerr->items[(size_t)b], F + POSI_BF_ELX)) {
+        if (!ias15 &&
+            (!set_axes(&verr->items[(size_t)b], F + POSI_BF_EVX) || !set_axes(&lerr->items[(size_t)b], F + POSI_BF_ELX))) {
             err = "Kahan error arrays";
             return false;
         }

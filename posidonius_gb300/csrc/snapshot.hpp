@@ -1,6 +1,6 @@
 // snapshot.hpp -- recovery snapshots and historic records of the drop-in path.
 //
-// Recovery snapshot (src/integrator/output.rs:28-54): the WHFast case document
+// Recovery snapshot (src/integrator/output.rs:28-54): the WHFast or IAS15 case document
 // the run started from, with every field the integration changes replaced by
 // the device state, written back as pretty-printed JSON (2-space indentation,
 // as serde_json::to_string_pretty).  Fields the integrator recomputes before
@@ -30,10 +30,13 @@ std::string format_double(double v);
 // Serialise with serde_json's pretty layout.
 void write_json(const json::Value& v, std::string& out, int indent = 0);
 
-// Replace the dynamic fields of a WHFast case document by the flat state of
-// its system (n bodies).  Returns false if the document lacks a field.
+// Replace the dynamic fields of a WHFast or IAS15 case document by the flat
+// state of its system (n bodies; ias: the IAS15 per-body state, n x
+// POSI_IAS_COUNT, for an IAS15 document).  Returns false if the document
+// lacks a field.
 bool update_case_document(json::Value& doc, int64_t n, const int64_t* sys_i64, const double* sys_f64,
-                          const int64_t* body_i64, const double* body_f64, const double* roche, std::string& err);
+                          const int64_t* body_i64, const double* body_f64, const double* roche, const double* ias,
+                          std::string& err);
 
 // Append the bincode bytes of one historic record of n bodies
 // (records: n x kHistoryFields doubles, id stored as a double).

@@ -211,6 +211,7 @@ struct Dev {
     int32_t* step_flags;           // per system: bit0 recovery trigger, bit1 historic trigger
     double* hist;                  // optional: [n_sys][nmax][HR_COUNT], last historic record
     double* rec;                   // optional: adjoint step records [step][POSI_REC_COUNT][stride]
+    double* ias;                   // IAS15 systems: [POSI_IAS_COUNT][stride]
 };
 
 // Per-planet constants of one half kick, slot k of lane j at P[k * G + j].
@@ -276,6 +277,7 @@ struct Sys {
     int s, n, host, coords, lane;
     bool tides, flat, gr, evo, spin_on, wind, disk;
     int gr_impl;     // posi_gr_impl; grk(): Kidder1995, the per-planet formulation
+    int gr_ignore;   // gravity terms the integrator leaves out (0 None, 1 WHFastOne, 2 WHFastTwo)
     bool dyn_host;   // the tidal host's evolution has a dynamical tide
     bool disk_on;    // disk effect with a disk host
     __device__ __forceinline__ bool grk() const { return gr && gr_impl == POSI_GR_KIDDER1995; }
@@ -367,6 +369,7 @@ struct Sys {
         disk = D.si[POSI_SI_DISK * ns + s] != 0;
         evo = D.si[POSI_SI_EVOLUTION * ns + s] != 0;
         gr_impl = (int)D.si[POSI_SI_GR_IMPL * ns + s];
+        gr_ignore = coords == POSI_JACOBI ? 1 : 2;
         // whfast.rs:270-274: GR adds a spin torque only in Kidder1995
         spin_on = tides || flat || evo || grk();
         iteration = D.si[POSI_SI_ITERATION * ns + s];
@@ -932,7 +935,7 @@ struct Sys {
     static_assert(GX_END <= kXS, "exchange slots");
 
     __device__ void gr_nbody(double g[3]) {
-        const int ignore = coords == POSI_JACOBI ? 1 : 2;   // WHFastOne / WHFastTwo
+        const int ignore = gr_ignore;
         sync();
         if (has) {
 #pragma unroll
@@ -943,7 +946,7 @@ struct Sys {
         // :661-697 the gravity accelerations plus the host terms the
         // integrator ignored: host inertial position minus the body's
         // heliocentric (GR) position
-        const int np = ignore == 1 ? 1 : n - 1;
+        const int np = ignore == 1 ? 1 : (ignore == 2 ? n - 1 : 0);
         const int rank = lane < host ? lane : lane - 1;   // position among the other bodies
         double na[3] = {b.a[0], b.a[1], b.a[2]};
         if (planet() && rank < np) {
@@ -2554,5 +2557,7 @@ __global__ void __launch_bounds__(128) additional_effects_kernel(Dev D, double t
     S.additional_effects(D, 0, evolution != 0);
     S.store(D);
 }
+
+#include "ias15_device.cuh"
 
 }  // namespace POSI_NS

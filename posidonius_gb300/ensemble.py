@@ -329,3 +329,19 @@ def workload_large(n_small=1021, seed=None, dt=0.1, coords=L.DEMOCRATIC_HELIOCEN
     star.flat = None
     star.gr = L.EFFECT_DISABLED
     return make_system(bodies, dt=dt, coords=coords, tides=True, flat=False, gr=False, **kw)
+
+
+def as_ias15(ens, dt=None):
+    """The same systems integrated by IAS15 (src/integrator/ias15.rs): a copy
+    of the ensemble with the integrator set, a fresh Gauss-Radau state
+    (``body_ias`` zeros, no accepted step yet) and, if given, the first trial
+    step ``dt`` in days (IAS15 adapts it from there)."""
+    out = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in ens.items()}
+    out["sys_i64"][:, L.SI_INTEGRATOR] = L.INTEGRATOR_IAS15
+    out["sys_i64"][:, L.SI_IAS_MAX_EXCEEDED] = 0
+    out["sys_f64"][:, L.SF_IAS_DT_LAST] = 0.0
+    if dt is not None:
+        out["sys_f64"][:, L.SF_DT] = dt
+        out["sys_f64"][:, L.SF_HALF_DT] = 0.5 * dt
+    out["body_ias"] = np.zeros(out["body_f64"].shape[:2] + (L.IAS_COUNT,), np.float64)
+    return out

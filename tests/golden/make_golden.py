@@ -1,4 +1,4 @@
-"""Copy the reference's golden WHFast cases into tests/golden/ (gzip-compressed).
+"""Copy the reference's golden WHFast and IAS15 cases into tests/golden/ (gzip-compressed).
 
 Run once in a checkout that has the Posidonius reference mounted:
 
@@ -9,8 +9,8 @@ For every in-scope case of the reference's Rust integration tests
 tests/common/universe.rs:36-44; tests/data/<case>/particle_<i>.json = final
 inertial position/velocity/acceleration after integrating to the time limit,
 tests/common/universe.rs:18-34) it writes <case>/case.json.gz and
-<case>/particles.json (the particle files merged).  Cases outside the path
-(IAS15, LeapFrog) are skipped.
+<case>/particles.json (the particle files merged).  LeapFrog cases, and the
+order cases whose case document the reference does not store, are skipped.
 The Python-generated twins (posidonius/tests/data/<case>/case.json) of the three
 integrator cases, which the reference steps once and compares
 (tests/test_integrator.rs:58-70), are stored as <case>/python_case.json.gz.
@@ -51,6 +51,8 @@ IN_SCOPE = [
     "test_evolution-solar_like_galletbolmont2017",
     # protoplanetary disk
     "test_disk-enabled_disk",
+    # the IAS15 integrator (tests/test_integrator.rs:266-312)
+    "test_integrator-ias15",
 ]
 
 

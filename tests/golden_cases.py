@@ -10,8 +10,12 @@ from posidonius_gb300 import layout as L
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def names():
-    return sorted(d for d in os.listdir(GOLDEN) if os.path.isdir(os.path.join(GOLDEN, d)))
+def names(integrator="whfast"):
+    """Golden cases of one integrator ("whfast", "ias15") or of all (None)."""
+    out = sorted(d for d in os.listdir(GOLDEN) if os.path.isdir(os.path.join(GOLDEN, d)))
+    if integrator is None:
+        return out
+    return [d for d in out if ("-ias15" in d) == (integrator == "ias15")]
 
 
 def case_path(name, python_twin=False):

@@ -7,8 +7,9 @@ from posidonius_gb300 import layout as L
 # at historic-snapshot steps and is NaN after the first one, 0/0)
 STATE_FIELDS = list(range(L.BF_COUNT))
 SYS_I64_FIELDS = [L.SI_ITERATION, L.SI_N_HIST, L.SI_TIMESTEP_WARNING, L.SI_STATUS, L.SI_FAIL_STEP, L.SI_FAIL_PAIR,
-                  L.SI_LAST_MIDPOINT_ITERS]
-SYS_F64_FIELDS = [L.SF_TIME, L.SF_LAST_HIST, L.SF_LAST_REC]
+                  L.SI_LAST_MIDPOINT_ITERS, L.SI_IAS_MAX_EXCEEDED]
+# the IAS15 step size adapts (constant for WHFast)
+SYS_F64_FIELDS = [L.SF_TIME, L.SF_LAST_HIST, L.SF_LAST_REC, L.SF_DT, L.SF_IAS_DT_LAST]
 
 
 def nbodies(ens, s):
@@ -49,6 +50,10 @@ def bitwise_diffs(a, b):
         for f in SYS_F64_FIELDS:
             if not same_bits(a["sys_f64"][s, f], b["sys_f64"][s, f]):
                 out.append((s, "sys_f64", f))
+        if a.get("body_ias") is not None and b.get("body_ias") is not None:
+            same = same_bits(a["body_ias"][s, :n], b["body_ias"][s, :n])
+            if not same.all():
+                out.append((s, "body_ias", list(np.nonzero((~same).any(axis=0))[0])))
     return out
 
 

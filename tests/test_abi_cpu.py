@@ -52,12 +52,12 @@ def _unzip(tmp_path, name, twin=False):
     return p
 
 
-@pytest.mark.parametrize("name", names())
+@pytest.mark.parametrize("name", names(None))
 def test_cpp_reader_matches_oracle_reader(built, tmp_path, name):
     ref = load_case(case_dict(name))
     got = pg.read_case(_unzip(tmp_path, name))
     assert got["n"] == ref["n"]
-    for k in ("sys_i64", "sys_f64", "body_i64", "body_f64", "roche"):
+    for k in ("sys_i64", "sys_f64", "body_i64", "body_f64", "roche", "body_ias"):
         assert np.array_equal(np.asarray(got[k]).view(np.int64) if got[k].dtype == np.float64 else got[k],
                               np.asarray(ref[k]).view(np.int64) if ref[k].dtype == np.float64 else ref[k]), k
     assert np.array_equal(got["tables"][: ref["tables"].size], ref["tables"])

@@ -27,6 +27,39 @@ def test_oracle_matches_reference_golden(name):
     assert err == 0.0, "restatement should be bit-exact against the Rust FP64 path"
 
 
+@pytest.mark.parametrize("name", names("ias15"))
+def test_oracle_ias15_matches_reference_golden(name):
+    """tests/test_integrator.rs:303-312 (ias15_rust): the IAS15 restatement
+    integrates the brown-dwarf case to the same bits.  The adaptive step
+    starts at 0.08 d and grows by the safety factor's limit of 4 per step
+    (0.32, 1.28, 5.12 d), so the run stops after 4 steps at t = 6.8 d with a
+    next step of 20.48 d beyond the 16 d limit."""
+    case = load_case(case_dict(name))
+    assert case["sys_i64"][L.SI_INTEGRATOR] == L.INTEGRATOR_IAS15
+    ens, steps, res = oracle.run(case, max_steps=10**6, init_physical=True)
+    assert steps[0] == 4
+    assert ens["sys_i64"][0, L.SI_STATUS] & L.SYS_FATAL_MASK == L.SYS_COMPLETED
+    assert ens["sys_f64"][0, L.SF_TIME] == 0.08 + 0.32 + 1.28 + 5.12
+    assert ens["sys_f64"][0, L.SF_DT] == 20.48
+    assert max_abs_error(ens["body_f64"][0], expected(name)) == 0.0
+
+
+def test_oracle_ias15_rejects_and_retries():
+    """A first step far too long for the system (100 d against an estimate
+    near 16 d) does not converge within 12 predictor-corrector iterations,
+    is rejected and redone with the estimated step (ias15.rs:1187-1217)."""
+    name = names("ias15")[0]
+    case = load_case(case_dict(name))
+    big = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in case.items()}
+    big["sys_f64"][L.SF_DT] = 100.0
+    big["sys_f64"][L.SF_TIME_LIMIT] = 1000.0
+    ens, steps, _ = oracle.run(big, max_steps=1, init_physical=True)
+    assert steps[0] == 1
+    assert ens["sys_i64"][0, L.SI_IAS_MAX_EXCEEDED] == 1
+    t1 = ens["sys_f64"][0, L.SF_TIME]
+    assert 10.0 < t1 < 25.0 and ens["sys_f64"][0, L.SF_IAS_DT_LAST] == t1
+
+
 @pytest.mark.parametrize("name", ["test_integrator-whfast_jacobi",
                                   "test_integrator-whfast_democraticheliocentric",
                                   "test_integrator-whfast_whds"])
