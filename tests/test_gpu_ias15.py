@@ -188,3 +188,55 @@ def test_history_records_match_oracle(tmp_path):
     from parity import same_bits
     assert same_bits(got, ref).all()
     assert bitwise_diffs(w.get_state(), ens) == []
+
+
+def test_batched_uneven_exact_matches_oracle():
+    """Systems of 2 to 10 bodies (circumbinary binaries included) by IAS15:
+    lane groups of 8 and 16, every system adapting its own step."""
+    ens = E.as_ias15(E.workload_uneven(96, seed=5), dt=0.1)
+    ref, steps, _ = oracle.run(ens, max_steps=15, init_physical=True, nthreads=8)
+    b = pg.Batch(ens, mode=pg.EXACT)
+    assert b.mapping_for(10) == 16 and b.mapping_for(3) == 8
+    b.initialize_physical_values()
+    b.iterate(15, 6)
+    st = b.get_state()
+    assert np.array_equal(st["sys_i64"][:, L.SI_ITERATION], steps)
+    assert bitwise_diffs(st, ref) == []
+
+
+def test_cli_start_resume_matches_uninterrupted_run(tmp_path):
+    """`posidonius start` / `resume` on an IAS15 case: the resumed run
+    continues bit for bit, history file included."""
+    import json
+    import subprocess
+    from posidonius_gb300 import build as B
+
+    def cli(*args):
+        return subprocess.run([B.CLI] + [str(a) for a in args], capture_output=True, text=True, timeout=300)
+
+    def case(limit, fname):
+        d = case_dict(GOLDEN[0])
+        d["historic_snapshot_period"] = 10.0
+        d["recovery_snapshot_period"] = 20.0
+        d["universe"]["time_limit"] = limit
+        p = tmp_path / fname
+        p.write_text(json.dumps(d))
+        return p
+
+    full = case(200.0, "full.json")
+    r = cli("start", full, tmp_path / "full_rec.json", tmp_path / "full_hist.bin", "-s")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Simulation completed" in r.stdout
+    part = case(100.0, "part.json")
+    r = cli("start", part, tmp_path / "rec.json", tmp_path / "hist.bin", "-s")
+    assert r.returncode == 0, r.stdout + r.stderr
+    snap = json.loads((tmp_path / "rec.json").read_text())
+    assert 0 < snap["current_time"] < 100.0 and snap["time_step_last_success"] > 0
+    r = cli("resume", tmp_path / "rec.json", tmp_path / "hist.bin", "--time-limit", 200, "-s")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert (tmp_path / "hist.bin").read_bytes() == (tmp_path / "full_hist.bin").read_bytes()
+    a = json.loads((tmp_path / "rec.json").read_text())
+    b = json.loads((tmp_path / "full_rec.json").read_text())
+    assert a["current_iteration"] == b["current_iteration"]
+    assert a["universe"]["particles"] == b["universe"]["particles"]
+    assert a["b_6"] == b["b_6"] and a["time_step"] == b["time_step"]
