@@ -107,9 +107,16 @@ def max_over_ranks(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(world, n_sys, steps, max_ms):
+    """Whole-job system-steps/s of `world` independent replicas of n_sys
+    systems each, from the slowest rank's time."""
+    return world * n_sys * steps / (max_ms * 1e-3)
 
 
 class ClockSampler:
@@ -648,7 +655,7 @@ def main():
     barrier(world)
     clock_info = clocks.stop()
     total_ms = max_over_ranks(total_ms, world)
-    value = world * batch.n_sys * K / (total_ms * 1e-3)
+    value = replica_value(world, batch.n_sys, K, total_ms)
     per_launch_ms = total_ms / R
 
     # ---- end-to-end through the C ABI with host buffers -----------------------
