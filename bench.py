@@ -45,6 +45,8 @@ def parse():
     p.add_argument("--workload", default="ensemble8",
                    choices=["ensemble8", "uneven", "single", "gradient", "large", "ias15"])
     p.add_argument("--large-bodies", type=int, default=1024, help="large workload: bodies in the system")
+    p.add_argument("--large-coords", default="dh", choices=["dh", "jacobi"],
+                   help="large workload: democratic heliocentric or Jacobi coordinates")
     p.add_argument("--grad-steps", type=int, default=10000, help="gradient workload: WHFast steps")
     p.add_argument("--checkpoint-every", type=int, default=100, help="gradient workload: checkpoint interval")
     p.add_argument("--fd-systems", type=int, default=32, help="gradient workload: systems checked by differences")
@@ -520,7 +522,8 @@ def run_large(args):
 
     N = args.large_bodies
     K = args.steps
-    case = E.workload_large(N - 3)
+    jacobi = args.large_coords == "jacobi"
+    case = E.workload_large(N - 3, coords=L.JACOBI if jacobi else L.DEMOCRATIC_HELIOCENTRIC)
     mb = pg.ManyBody(case)
     mb.initialize_physical_values()
     init = mb.get_state()
@@ -549,7 +552,8 @@ def run_large(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": done, "warmup": W,
         "ms_per_step": ms / max(done, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded; posidonius_gb300.ensemble.workload_large)",
-        "config": {"workload": "large", "bodies": N, "dt_days": 0.1, "coordinates": "democratic heliocentric",
+        "config": {"workload": "large", "bodies": N, "dt_days": 0.1,
+                   "coordinates": "Jacobi" if jacobi else "democratic heliocentric",
                    "effects": "CTL tides (every body an orbiting tidal body of the star; the small bodies with "
                               "zero dissipation and Love number)", "mode": "fast",
                    "l2": "flushed (512 MiB write) before the timed launch",
@@ -559,7 +563,7 @@ def run_large(args):
                 "d2h_bytes_per_step": bytes_io / max(done, 1), "note": "posi_large_set_state, iterate, get_state"},
         "gpu_launches": 1, "status": int(final["sys_i64"][L.SI_STATUS]), "clocks": clock_info,
     }
-    if not args.no_derivative:
+    if not args.no_derivative and not jacobi:
         result["derivative"] = large_derivative(mb, init, K, ms, flush, args.derivative_dirs)
     if not args.no_cpu_baseline:
         import oracle

@@ -10,6 +10,7 @@
 
 struct posi_large {
     int64_t n = 0;
+    int coords = POSI_DEMOCRATIC_HELIOCENTRIC;
     int grid = 0, nchunk = 0, per_block = 0;
     double *d_bf = nullptr, *d_sf = nullptr, *d_roche = nullptr, *d_pos = nullptr, *d_gpart = nullptr,
            *d_bpart = nullptr, *d_tot = nullptr, *d_tan = nullptr, *d_dpos = nullptr;
@@ -72,9 +73,9 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
     };
     if (n < 2 || !sys_i64 || !sys_f64 || !body_i64 || !body_f64) return fail(POSI_ERR_ARG, "bad arguments", nullptr);
     if (sys_i64[POSI_SI_N] != n) return fail(POSI_ERR_ARG, "sys_i64[POSI_SI_N] differs from n", nullptr);
-    if (sys_i64[POSI_SI_COORDS] != POSI_DEMOCRATIC_HELIOCENTRIC)
-        return fail(POSI_ERR_UNSUPPORTED, "the many-body engine integrates in democratic-heliocentric coordinates",
-                    nullptr);
+    if (sys_i64[POSI_SI_COORDS] != POSI_DEMOCRATIC_HELIOCENTRIC && sys_i64[POSI_SI_COORDS] != POSI_JACOBI)
+        return fail(POSI_ERR_UNSUPPORTED,
+                    "the many-body engine integrates in democratic-heliocentric or Jacobi coordinates", nullptr);
     if (sys_i64[POSI_SI_EVOLUTION] != 0)
         return fail(POSI_ERR_UNSUPPORTED, "the many-body engine supports non-evolving bodies only", nullptr);
     if (sys_i64[POSI_SI_GR] != 0 && sys_i64[POSI_SI_GR_IMPL] != POSI_GR_KIDDER1995)
@@ -96,6 +97,7 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
         return fail(POSI_ERR_CUDA, "occupancy query failed", nullptr);
     posi_large* L = new posi_large();
     L->n = n;
+    L->coords = (int)sys_i64[POSI_SI_COORDS];
     L->grid = sms;  // one block per SM: every block resident
     if ((int64_t)L->grid * posi_many::kBlock < n)
         return fail(POSI_ERR_UNSUPPORTED, "too many bodies for one resident grid (" +
@@ -211,10 +213,11 @@ namespace {
 
 // One cooperative launch of the engine (NT tangent directions) and its
 // error report.
-template <int NT>
+template <int NT, bool JAC = false>
 int run_large(posi_large* L, int64_t n_steps, const int32_t* seed_body, const int32_t* seed_param) {
     int per_sm = 0;
-    LCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, posi_many::large_steps_kernel<NT>, posi_many::kBlock, 0));
+    LCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, posi_many::large_steps_kernel<NT, JAC>,
+                                                      posi_many::kBlock, 0));
     if (per_sm < 1) {
         posi::set_last_error("the engine's blocks do not fit one per SM");
         return POSI_ERR_CUDA;
@@ -236,7 +239,7 @@ int run_large(posi_large* L, int64_t n_steps, const int32_t* seed_body, const in
     LCK(cudaMemsetAsync(L->d_bad, 0xff, sizeof(unsigned long long), L->stream));
     void* args[] = {&d, &n_steps};
     LCK(cudaEventRecord(L->e0, L->stream));
-    LCK(cudaLaunchCooperativeKernel((const void*)posi_many::large_steps_kernel<NT>, dim3(L->grid),
+    LCK(cudaLaunchCooperativeKernel((const void*)posi_many::large_steps_kernel<NT, JAC>, dim3(L->grid),
                                     dim3(posi_many::kBlock), args, 0, L->stream));
     LCK(cudaEventRecord(L->e1, L->stream));
     LCK(cudaEventSynchronize(L->e1));
@@ -275,6 +278,7 @@ extern "C" {
 int posi_large_iterate(posi_large* L, int64_t n_steps) {
     if (!L || n_steps < 0) return POSI_ERR_ARG;
     if (n_steps == 0) return POSI_OK;
+    if (L->coords == POSI_JACOBI) return run_large<0, true>(L, n_steps, nullptr, nullptr);
     return run_large<0>(L, n_steps, nullptr, nullptr);
 }
 
@@ -283,6 +287,10 @@ int posi_large_iterate_tangent(posi_large* L, int64_t n_steps, int32_t n_dirs, c
     if (!L || n_steps < 0 || n_dirs < 1 || n_dirs > posi_many::kMaxTangents || !seed_body || !seed_param || !tangents) {
         posi::set_last_error("bad arguments (1 to 4 directions, seeds and tangents required)");
         return POSI_ERR_ARG;
+    }
+    if (L->coords != POSI_DEMOCRATIC_HELIOCENTRIC) {
+        posi::set_last_error("the tangent runs integrate in democratic-heliocentric coordinates");
+        return POSI_ERR_UNSUPPORTED;
     }
     const int64_t n = L->n;
     for (int d = 0; d < n_dirs; ++d) {

@@ -201,6 +201,65 @@ __device__ bool grid_reduce(const LDev& D, const double (&vals)[NS], int nslots,
     return r;
 }
 
+// Grid-wide exclusive prefix over the bodies in index order (body i is thread
+// i % per_block of block i / per_block; only the one-role engine calls it):
+// excl[k] = sum of vals[k] over the bodies before this thread's, tot[k] over
+// all bodies, for nslots <= 8.  Warp shuffle scans, then the warps' totals in
+// shared memory, then one grid barrier after which every block sums the
+// partial rows of the blocks before it (one warp per slot, fixed butterfly).
+template <int NS>
+__device__ bool grid_scan(const LDev& D, const double (&vals)[NS], int nslots, double* excl, double* tot, double* shm,
+                          unsigned rows) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NW = kBlock / 32;
+    double wex[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        wex[k] = 0.;
+        if (k < nslots) {
+            double x = vals[k];
+            for (int o = 1; o < 32; o <<= 1) {
+                const double y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            const double ex = __shfl_up_sync(0xffffffffu, x, 1);
+            wex[k] = lane == 0 ? 0. : ex;
+            if (lane == 31) shm[warp * BP_ROW + k] = x;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NS; ++k)
+        if (k < nslots)
+            for (int w = 0; w < warp; ++w) wex[k] += shm[w * BP_ROW + k];
+    if (threadIdx.x < nslots) {
+        double bt = 0.;
+        for (int w = 0; w < NW; ++w) bt += shm[w * BP_ROW + threadIdx.x];
+        D.bpart[(size_t)blockIdx.x * BP_ROW + threadIdx.x] = bt;
+    }
+    if (!grid_barrier(D)) return false;
+    for (int k = warp; k < nslots; k += NW) {
+        double pre = 0., all = 0.;
+        for (unsigned b = lane; b < rows; b += 32) {
+            const double x = __ldcg(D.bpart + (size_t)b * BP_ROW + k);
+            all += x;
+            if (b < blockIdx.x) pre += x;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            pre += __shfl_xor_sync(0xffffffffu, pre, o);
+            all += __shfl_xor_sync(0xffffffffu, all, o);
+        }
+        if (lane == 0) { shm[NW * BP_ROW + k] = pre; shm[NW * BP_ROW + 8 + k] = all; }
+    }
+    __syncthreads();
+    for (int k = 0; k < nslots; ++k) {
+        excl[k] = shm[NW * BP_ROW + k] + wex[k];
+        tot[k] = shm[NW * BP_ROW + 8 + k];
+    }
+    __syncthreads();
+    return true;
+}
+
 struct BodyConst {
     double m, mg, R, moi, sig, k2, k2f;
     int tk, fk, gk;
@@ -275,6 +334,14 @@ struct Large {
     double da[3];           // tangent of the gravity acceleration
     double* shm;
     double Mtot, inv_M, inv_hm;
+    double kgm;             // GM of this body's Kepler drift
+    // Jacobi coordinates (the one-role engine): masses before this body and
+    // including it (host first, then index order), the first planet, and the
+    // barycentre (the host's Jacobi coordinates)
+    bool jac;
+    double eta_ex, eta_in;
+    int64_t p1;
+    double Rb[3], Vb[3];
     bool warp_bodies;       // this thread's warp owns at least one body
     unsigned body_rows;     // blocks that own bodies (the partial rows that can be nonzero)
 
@@ -521,7 +588,9 @@ struct Large {
     // ---- gravity over all ordered pairs, with the pair checks ----
     // pos[] holds heliocentric positions published before the preceding
     // barrier (differences of heliocentric and of inertial positions agree);
-    // the host sits at -shift (the jump moved every planet by +shift).  The
+    // the host sits at -shift (the jump moved every planet by +shift).  In
+    // Jacobi coordinates pos[] holds every body's inertial position and the
+    // pair of the host and the first planet is left out (WHFastOne).  The
     // pair loop, spread over every thread of the grid, carries all NT
     // tangent directions (positions published in dpos[]); the tangent of the
     // pair term -G m_j d / |d|^3 along dd is
@@ -536,7 +605,7 @@ struct Large {
         if (chunk < D.nchunk) {
             const int64_t j0 = chunk * nn / D.nchunk, j1 = (chunk + 1) * nn / D.nchunk;
             double xi, yi, zi;
-            if (gi == host) { xi = -shift[0]; yi = -shift[1]; zi = -shift[2]; }
+            if (gi == host && !jac) { xi = -shift[0]; yi = -shift[1]; zi = -shift[2]; }
             else { xi = __ldcg(&D.pos[gi]); yi = __ldcg(&D.pos[nn + gi]); zi = __ldcg(&D.pos[2 * nn + gi]); }
             double txi[3][AN], tax[3][AN];
             if constexpr (NT > 0)
@@ -551,7 +620,7 @@ struct Large {
             for (int64_t j = j0; j < j1; ++j) {
                 if (j == gi) continue;
                 double xj, yj, zj;
-                if (j == host) { xj = -shift[0]; yj = -shift[1]; zj = -shift[2]; }
+                if (j == host && !jac) { xj = -shift[0]; yj = -shift[1]; zj = -shift[2]; }
                 else { xj = __ldcg(&D.pos[j]); yj = __ldcg(&D.pos[nn + j]); zj = __ldcg(&D.pos[2 * nn + j]); }
                 const double dx = xi - xj, dy = yi - yj, dz = zi - zj;
                 const double d2 = dx * dx + dy * dy + dz * dz;
@@ -563,7 +632,9 @@ struct Large {
                     else if (d2 <= Rs * Rs) bad = key + POSI_SYS_COLLISION;
                     else if (gi == host && d2 > kMAX_DISTANCE_2) bad = key + POSI_SYS_EJECTED;
                 }
-                if (gi == host || j == host) continue;  // WHFastTwo
+                if (jac ? ((gi == host && j == p1) || (j == host && gi == p1))   // WHFastOne
+                        : (gi == host || j == host))                                // WHFastTwo
+                    continue;
                 const double inv_d = rsqrt(d2);
                 const double p = -kG * D.bf[POSI_BF_MASS * nn + j] * (inv_d * inv_d * inv_d);
                 ax += p * dx; ay += p * dy; az += p * dz;
@@ -609,15 +680,15 @@ struct Large {
     // derivative at the converged root).
     __device__ void kepler(double x[3], double u[3], double tx[3], double tu[3]) {
         if (planet) {
-            const KeplerScalars ks = kepler_scalars(hc.mg, x, u);
+            const KeplerScalars ks = kepler_scalars(kgm, x, u);
             bool ok = false;
             const double X = kepler_solve(ks, half_dt, &ok);
             if (!ok) atomicOr(D.err, LE_KEPLER);
             double r1[3], v1[3];
-            kepler_apply(hc.mg, half_dt, x, u, ks, X, r1, v1);
+            kepler_apply(kgm, half_dt, x, u, ks, X, r1, v1);
             if (tan_on()) {
                 double e1[3], f1[3];
-                kepler_jvp(hc.mg, half_dt, x, u, X, tx, tu, e1, f1);
+                kepler_jvp(kgm, half_dt, x, u, X, tx, tu, e1, f1);
                 for (int q = 0; q < 3; ++q) { tx[q] = e1[q]; tu[q] = f1[q]; }
             }
             for (int q = 0; q < 3; ++q) { x[q] = r1[q]; u[q] = v1[q]; }
@@ -687,6 +758,96 @@ struct Large {
     // planets' total momentum from the first: the interaction kick adds
     // dt sum_p m_p a_p, which is zero (the planets' mutual forces cancel and
     // the host's are left out of the kick).
+    // Jacobi -> inertial (src/integrator/whfast.rs:1034-1080): the reference's
+    // backward recurrence is R_(k-1) = R - sum over body k and the later ones
+    // of (m / eta_incl) x, R the barycentre; one grid scan of those terms
+    __device__ bool from_jacobi(const double x[3], const double u[3]) {
+        double vals[NS] = {}, ex[NS], tot[NS];
+        if (planet) {
+            const double w = c.m / eta_in;
+            for (int q = 0; q < 3; ++q) { vals[q] = w * x[q]; vals[3 + q] = w * u[q]; }
+        }
+        if (!grid_scan(D, vals, 6, ex, tot, shm, body_rows)) return false;
+        for (int q = 0; q < 3; ++q) { h.r[q] = Rb[q] - tot[q]; h.v[q] = Vb[q] - tot[3 + q]; }
+        if (planet)
+            for (int q = 0; q < 3; ++q) {
+                b.r[q] = x[q] + (Rb[q] - (tot[q] - ex[q]));
+                b.v[q] = u[q] + (Vb[q] - (tot[3 + q] - ex[3 + q]));
+            }
+        if (is_host)
+            for (int q = 0; q < 3; ++q) { b.r[q] = h.r[q]; b.v[q] = h.v[q]; }
+        return true;
+    }
+
+    // ---- one step in Jacobi coordinates (the one-role engine) ----
+    // The reference's sequential recurrences over the bodies (host first,
+    // then index order) become grid scans: inertial -> Jacobi subtracts the
+    // centre of mass of the bodies before (:889-933), the Jacobi
+    // accelerations likewise (:935-963), the Kepler drift of body k uses the
+    // cumulative GM of the bodies up to k (:640-645), the kick adds the
+    // indirect term for every planet but the first (:558-592), and there is
+    // no jump.  Summation order differs from the reference's (FAST).
+    __device__ bool step_jacobi() {
+        const bool first = last_hist < 0.;
+        if (first || last_hist + hist_period <= t) {
+            spin_of(c, b.L, b.S);
+            spin_of(hc, h.L, h.S);
+            last_hist = first ? 0. : last_hist + hist_period;
+        }
+        double cm[6], tcm[6] = {0., 0., 0., 0., 0., 0.};
+        if (!midpoint(half_dt, cm, tcm)) return false;
+        for (int q = 0; q < 3; ++q) { Rb[q] = cm[q] * inv_M; Vb[q] = cm[3 + q] * inv_M; }
+        double x[3] = {0., 0., 0.}, u[3] = {0., 0., 0.}, tx[3] = {0., 0., 0.}, tu[3] = {0., 0., 0.};
+        {
+            double vals[NS] = {}, ex[NS], tot[NS];
+            if (planet)
+                for (int q = 0; q < 3; ++q) { vals[q] = c.m * b.r[q]; vals[3 + q] = c.m * b.v[q]; }
+            if (!grid_scan(D, vals, 6, ex, tot, shm, body_rows)) return false;
+            if (planet) {
+                const double ie = 1. / eta_ex;
+                for (int q = 0; q < 3; ++q) {
+                    x[q] = b.r[q] - (hc.m * h.r[q] + ex[q]) * ie;
+                    u[q] = b.v[q] - (hc.m * h.v[q] + ex[3 + q]) * ie;
+                }
+            }
+        }
+        kepler(x, u, tx, tu);
+        for (int q = 0; q < 3; ++q) Rb[q] += half_dt * Vb[q];
+        if (!from_jacobi(x, u)) return false;
+        if (has && primal_role())
+            for (int q = 0; q < 3; ++q) D.pos[q * n + i] = b.r[q];
+        if (!grid_barrier(D)) return false;
+        const double zero[3] = {0., 0., 0.};
+        double tzero[NT > 0 ? NT : 1][3] = {};
+        if (!gravity(zero, tzero)) return false;
+        if (__ldcg(D.bad) != ~0ull) return false;  // frozen at the first failing pair
+        {
+            // Jacobi accelerations: planets' m a before this body, plus the host's
+            double vals[NS] = {}, ex[NS], tot[NS];
+            if (planet)
+                for (int q = 0; q < 3; ++q) vals[q] = c.m * a[q];
+            if (is_host)
+                for (int q = 0; q < 3; ++q) vals[3 + q] = hc.m * a[q];
+            if (!grid_scan(D, vals, 6, ex, tot, shm, body_rows)) return false;
+            if (planet) {
+                const double ie = 1. / eta_ex;
+                for (int q = 0; q < 3; ++q) u[q] += dt * (a[q] - (tot[3 + q] + ex[q]) * ie);
+                if (i != p1) {
+                    const double rj2i = 1. / (x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + 1e-12);
+                    const double rji = sqrt(rj2i);
+                    const double prefac = dt * (rji * rj2i * kG * eta_in);
+                    for (int q = 0; q < 3; ++q) u[q] += prefac * x[q];
+                }
+            }
+        }
+        kepler(x, u, tx, tu);
+        for (int q = 0; q < 3; ++q) Rb[q] += half_dt * Vb[q];
+        if (!from_jacobi(x, u)) return false;
+        if (!midpoint(half_dt, nullptr, nullptr)) return false;
+        t += dt;
+        return true;
+    }
+
     __device__ __forceinline__ bool step() {
         constexpr int AN = NT > 0 ? NT : 1;
         const bool tn = tan_on();
@@ -774,8 +935,11 @@ struct Large {
 
 // Thread roles: block b holds bodies [b per_block, (b + 1) per_block); thread
 // r per_block + l of the block is role r of body b per_block + l (r = 0..NT).
-template <int NT>
+// JAC: Jacobi coordinates (NT = 0 only), a kernel of its own so that the
+// democratic-heliocentric one carries none of its code.
+template <int NT, bool JAC = false>
 __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t n_steps) {
+    static_assert(!JAC || NT == 0, "Jacobi coordinates carry no tangents");
     __shared__ double shm[(kBlock / 32 + 1) * BP_ROW];
     Large<NT> S(D, shm);
     S.n = D.n;
@@ -841,12 +1005,27 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
         S.inv_M = 1. / S.Mtot;
         S.inv_hm = 1. / S.hc.m;
     }
+    S.jac = JAC;
+    S.kgm = S.hc.mg;
+    S.p1 = S.host == 0 ? 1 : 0;
+    S.eta_ex = S.eta_in = S.hc.m;
+    for (int q = 0; q < 3; ++q) S.Rb[q] = S.Vb[q] = 0.;
+    if constexpr (JAC) {
+        // the masses before each body and its cumulative GM (host first)
+        double vals[Large<NT>::NS] = {}, ex[Large<NT>::NS], tot[Large<NT>::NS];
+        if (S.planet) { vals[0] = S.c.m; vals[1] = S.c.mg; }
+        if (!grid_scan(D, vals, 2, ex, tot, shm, S.body_rows)) return;
+        S.eta_ex = S.hc.m + ex[0];
+        S.eta_in = S.eta_ex + S.c.m;
+        S.kgm = S.hc.mg + ex[1] + (S.planet ? S.c.mg : 0.);
+    }
     const bool live = (D.si[POSI_SI_STATUS] & POSI_SYS_FATAL_MASK) == 0;
     int64_t done = 0;
     bool ok = true;
     if (live) {
         for (int64_t k = 0; k < n_steps; ++k) {
-            ok = S.step();
+            if constexpr (JAC) ok = S.step_jacobi();
+            else ok = S.step();
             if (!ok) break;
             ++done;
             if (S.t + S.dt > S.time_limit) break;

@@ -2300,10 +2300,10 @@ struct Sys {
         if (lane == 0) isc[0] = 0x7fffffff;
         sync();
         int code = 0, ev_pair = 0x7fffffff;
+        double acc0 = 0., acc1 = 0., acc2 = 0.;
         if (has) {
             const int i = lane, mm = host;
             const double* ro = D.roche + (int64_t)s * D.nmax * D.nmax + (int64_t)i * D.nmax;
-            double acc0 = 0., acc1 = 0., acc2 = 0.;
             for (int j = 0; j < n; ++j) {
                 if (i == j) continue;
                 const double dx = b.r[0] - X(2, j);
@@ -2331,16 +2331,18 @@ struct Sys {
                 acc1 += prefact * dy;
                 acc2 += prefact * dz;
             }
-            b.a[0] = acc0; b.a[1] = acc1; b.a[2] = acc2;
             if (code) atomicMin(&isc[0], ev_pair);
         }
         sync();
         const int first = isc[0];
         if (first != 0x7fffffff) {
-            // the reference panics at the first offending pair in (i, j) order
+            // the reference panics at the first offending pair in (i, j) order,
+            // before it stores any acceleration
             if (has && lane == first / 1024) isc[4] = code;
             sync();
             set_fatal(isc[4], first / 1024, first % 1024);
+        } else if (has) {
+            b.a[0] = acc0; b.a[1] = acc1; b.a[2] = acc2;
         }
         sync();
     }

@@ -240,3 +240,23 @@ def test_cli_start_resume_matches_uninterrupted_run(tmp_path):
     assert a["current_iteration"] == b["current_iteration"]
     assert a["universe"]["particles"] == b["universe"]["particles"]
     assert a["b_6"] == b["b_6"] and a["time_step"] == b["time_step"]
+
+
+def test_close_encounter_in_a_substep_freezes_like_the_oracle():
+    """A planet thrown at another (0.03 AU apart, closing at 0.5 AU/d) passes
+    the Roche limit at a substep of the first step: the system freezes there
+    (the reference panics) with the substep's predicted state and the step's
+    start time, next to a system that integrates on."""
+    base = load_case(case_dict(GOLDEN[0]))
+    bad = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in base.items()}
+    bad["body_f64"][2, L.POS] = bad["body_f64"][1, L.POS] + np.array([0.03, 0.0, 0.0])
+    bad["body_f64"][2, L.VEL] = bad["body_f64"][1, L.VEL] + np.array([-0.5, 0.0, 0.0])
+    ens = stack([bad, base])
+    ref, steps, _ = oracle.run(ens, max_steps=3, init_physical=True, nthreads=2)
+    assert ref["sys_i64"][0, L.SI_STATUS] & L.SYS_FATAL_MASK == L.SYS_ROCHE
+    assert ref["sys_f64"][0, L.SF_TIME] == 0.0
+    assert np.abs(ref["body_f64"][0, :5, L.POS] - bad["body_f64"][:5, L.POS]).max() > 0   # mid-step state
+    b = pg.Batch(ens, mode=pg.EXACT)
+    b.initialize_physical_values()
+    b.iterate(3, 3)
+    assert bitwise_diffs(b.get_state(), ref) == []
