@@ -260,3 +260,22 @@ def test_close_encounter_in_a_substep_freezes_like_the_oracle():
     b.initialize_physical_values()
     b.iterate(3, 3)
     assert bitwise_diffs(b.get_state(), ref) == []
+
+
+@pytest.mark.parametrize("name", ["test_general_relativity-anderson1975", "test_general_relativity-newhall1983",
+                                  "test_disk-enabled_disk", "test_evolution-solar_like_bolmontmathis2016",
+                                  "test_evolution-solar_like_baraffe2015", "test_star_types-m_dwarf"])
+def test_every_effect_under_ias15_exact(name):
+    """The reference's WHFast goldens integrated by IAS15 instead: the
+    N-body GR forms (their Newtonian accelerations without ignored terms),
+    the disk, the wind, the dynamical tide and the evolving stars, 20
+    adaptive steps, bit for bit against the oracle."""
+    case = load_case(case_dict(name))
+    case["sys_f64"][L.SF_TIME_LIMIT] = 400.0
+    ens = E.as_ias15(stack([case]))
+    ref, steps, _ = oracle.run(ens, max_steps=20, init_physical=True)
+    assert steps[0] == 20
+    b = pg.Batch(ens, mode=pg.EXACT)
+    b.initialize_physical_values()
+    b.iterate(20, 10)
+    assert bitwise_diffs(b.get_state(), ref) == []
