@@ -447,9 +447,9 @@ int posi_adjoint_last_timing(const posi_adjoint* a, double* forward_ms, double* 
  * single system beyond the batched kernels' 32 bodies (a star, tidally active
  * planets and hundreds or thousands of small massive bodies): one cooperative
  * grid, thread per body, the O(N^2) pair loop spread over the whole GPU.
- * Democratic-heliocentric or Jacobi coordinates (the reference's sequential
- * Jacobi recurrences run as grid-wide prefix scans), non-evolving bodies, the
- * host the most massive body; FAST arithmetic.  State arrays as posi_universe_from_arrays
+ * Democratic-heliocentric, Jacobi or WHDS coordinates (the reference's
+ * sequential Jacobi recurrences run as grid-wide prefix scans), non-evolving
+ * bodies, the host the most massive body; FAST arithmetic.  State arrays as posi_universe_from_arrays
  * (one system of n bodies, row-major).  A physical event freezes the system
  * (posi_large_iterate returns POSI_ERR_PHYSICS; sys_i64[POSI_SI_FAIL_PAIR] =
  * i * n + j of the first failing pair). */
@@ -474,7 +474,7 @@ int posi_large_iterate(posi_large* L, int64_t n_steps);
  * seed_body[d]: POSI_SEED_SIGMA (dissipation factor) or POSI_SEED_K2 (Love
  * number k2); seed_body[d] = -1 perturbs no parameter.  The primal state
  * advances exactly as posi_large_iterate advances it.  Democratic-heliocentric
- * systems only (POSI_ERR_UNSUPPORTED for Jacobi). */
+ * systems only (POSI_ERR_UNSUPPORTED for Jacobi and WHDS). */
 enum posi_seed_param { POSI_SEED_SIGMA = 0, POSI_SEED_K2 = 1 };
 int posi_large_iterate_tangent(posi_large* L, int64_t n_steps, int32_t n_dirs, const int32_t* seed_body,
                                const int32_t* seed_param, double* tangents);

@@ -73,9 +73,8 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
     };
     if (n < 2 || !sys_i64 || !sys_f64 || !body_i64 || !body_f64) return fail(POSI_ERR_ARG, "bad arguments", nullptr);
     if (sys_i64[POSI_SI_N] != n) return fail(POSI_ERR_ARG, "sys_i64[POSI_SI_N] differs from n", nullptr);
-    if (sys_i64[POSI_SI_COORDS] != POSI_DEMOCRATIC_HELIOCENTRIC && sys_i64[POSI_SI_COORDS] != POSI_JACOBI)
-        return fail(POSI_ERR_UNSUPPORTED,
-                    "the many-body engine integrates in democratic-heliocentric or Jacobi coordinates", nullptr);
+    if (sys_i64[POSI_SI_COORDS] < POSI_JACOBI || sys_i64[POSI_SI_COORDS] > POSI_WHDS)
+        return fail(POSI_ERR_ARG, "unknown coordinates type", nullptr);
     if (sys_i64[POSI_SI_EVOLUTION] != 0)
         return fail(POSI_ERR_UNSUPPORTED, "the many-body engine supports non-evolving bodies only", nullptr);
     if (sys_i64[POSI_SI_GR] != 0 && sys_i64[POSI_SI_GR_IMPL] != POSI_GR_KIDDER1995)
@@ -213,10 +212,10 @@ namespace {
 
 // One cooperative launch of the engine (NT tangent directions) and its
 // error report.
-template <int NT, bool JAC = false>
+template <int NT, int CO = POSI_DEMOCRATIC_HELIOCENTRIC>
 int run_large(posi_large* L, int64_t n_steps, const int32_t* seed_body, const int32_t* seed_param) {
     int per_sm = 0;
-    LCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, posi_many::large_steps_kernel<NT, JAC>,
+    LCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, posi_many::large_steps_kernel<NT, CO>,
                                                       posi_many::kBlock, 0));
     if (per_sm < 1) {
         posi::set_last_error("the engine's blocks do not fit one per SM");
@@ -239,7 +238,7 @@ int run_large(posi_large* L, int64_t n_steps, const int32_t* seed_body, const in
     LCK(cudaMemsetAsync(L->d_bad, 0xff, sizeof(unsigned long long), L->stream));
     void* args[] = {&d, &n_steps};
     LCK(cudaEventRecord(L->e0, L->stream));
-    LCK(cudaLaunchCooperativeKernel((const void*)posi_many::large_steps_kernel<NT, JAC>, dim3(L->grid),
+    LCK(cudaLaunchCooperativeKernel((const void*)posi_many::large_steps_kernel<NT, CO>, dim3(L->grid),
                                     dim3(posi_many::kBlock), args, 0, L->stream));
     LCK(cudaEventRecord(L->e1, L->stream));
     LCK(cudaEventSynchronize(L->e1));
@@ -278,7 +277,8 @@ extern "C" {
 int posi_large_iterate(posi_large* L, int64_t n_steps) {
     if (!L || n_steps < 0) return POSI_ERR_ARG;
     if (n_steps == 0) return POSI_OK;
-    if (L->coords == POSI_JACOBI) return run_large<0, true>(L, n_steps, nullptr, nullptr);
+    if (L->coords == POSI_JACOBI) return run_large<0, POSI_JACOBI>(L, n_steps, nullptr, nullptr);
+    if (L->coords == POSI_WHDS) return run_large<0, POSI_WHDS>(L, n_steps, nullptr, nullptr);
     return run_large<0>(L, n_steps, nullptr, nullptr);
 }
 

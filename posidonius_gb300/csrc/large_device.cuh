@@ -848,6 +848,92 @@ struct Large {
         return true;
     }
 
+    // ---- one step in WHDS coordinates (the one-role engine) ----
+    // Heliocentric positions, barycentric velocities scaled by
+    // (m0 + m) / m0 (src/integrator/whfast.rs:973-1023), the Kepler drift
+    // with GM = G (m0 + m) (:648-652), a jump by dt/2 (p - m u / (m0 + m))
+    // with p = sum m u / (m0 + m) (:521-556), the kick scaled by
+    // (m0 + m) / m0 (:605-625) and the back-transform of :1090-1155.  The
+    // second jump reuses p: the kick adds dt sum m a / m0 to it, zero
+    // because the planets' mutual forces cancel and the host's are left out.
+    // sums: S[0..2] = sum m x, S[3..5] = sum (m / (m0 + m)) u, S[6..8] =
+    // sum m (m / (m0 + m)) u over the planets
+    __device__ bool whds_sums(const double x[3], const double u[3], double wv, double S[9]) {
+        double vals[NS] = {}, tot[NS];
+        if (planet)
+            for (int q = 0; q < 3; ++q) {
+                vals[q] = c.m * x[q];
+                vals[3 + q] = wv * u[q];
+                vals[6 + q] = c.m * wv * u[q];
+            }
+        if (!grid_reduce(D, vals, 9, tot, shm, warp_bodies, body_rows)) return false;
+        for (int q = 0; q < 9; ++q) S[q] = tot[q];
+        return true;
+    }
+
+    __device__ void whds_to_inertial(const double x[3], const double u[3], const double Rc[3], const double Vc[3],
+                                     const double Smx[3], const double P[3], double fac) {
+        for (int q = 0; q < 3; ++q) {
+            h.r[q] = Rc[q] - Smx[q] * inv_M;
+            h.v[q] = Vc[q] - P[q];
+        }
+        if (planet)
+            for (int q = 0; q < 3; ++q) { b.r[q] = x[q] + h.r[q]; b.v[q] = u[q] / fac + Vc[q]; }
+        if (is_host)
+            for (int q = 0; q < 3; ++q) { b.r[q] = h.r[q]; b.v[q] = h.v[q]; }
+    }
+
+    __device__ bool step_whds() {
+        const bool first = last_hist < 0.;
+        if (first || last_hist + hist_period <= t) {
+            spin_of(c, b.L, b.S);
+            spin_of(hc, h.L, h.S);
+            last_hist = first ? 0. : last_hist + hist_period;
+        }
+        double cm[6], tcm[6] = {0., 0., 0., 0., 0., 0.};
+        if (!midpoint(half_dt, cm, tcm)) return false;
+        double Rc[3], Vc[3], x[3] = {0., 0., 0.}, u[3] = {0., 0., 0.}, tx[3] = {0., 0., 0.}, tu[3] = {0., 0., 0.};
+        for (int q = 0; q < 3; ++q) { Rc[q] = cm[q] * inv_M; Vc[q] = cm[3 + q] * inv_M; }
+        const double fac = planet ? (hc.m + c.m) * inv_hm : 1.;   // (m0 + m) / m0
+        const double wv = planet ? c.m / (hc.m + c.m) : 0.;       // m / (m0 + m)
+        if (planet)
+            for (int q = 0; q < 3; ++q) { x[q] = b.r[q] - h.r[q]; u[q] = (b.v[q] - Vc[q]) * fac; }
+        // part 1: Kepler drift (and the barycentre's), jump, back to inertial
+        kepler(x, u, tx, tu);
+        for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
+        double S[9];
+        if (!whds_sums(x, u, wv, S)) return false;
+        const double P[3] = {S[3], S[4], S[5]};
+        double Smx[3];
+        for (int q = 0; q < 3; ++q) Smx[q] = S[q] + half_dt * (P[q] * (Mtot - hc.m) - S[6 + q]);
+        if (planet)
+            for (int q = 0; q < 3; ++q) x[q] += half_dt * (P[q] - wv * u[q]);
+        whds_to_inertial(x, u, Rc, Vc, Smx, P, fac);
+        // heliocentric positions after the jump for the pair loop (the host
+        // at the origin)
+        if (planet && primal_role())
+            for (int q = 0; q < 3; ++q) D.pos[q * n + i] = x[q];
+        if (!grid_barrier(D)) return false;
+        const double zero[3] = {0., 0., 0.};
+        double tzero[NT > 0 ? NT : 1][3] = {};
+        if (!gravity(zero, tzero)) return false;
+        if (__ldcg(D.bad) != ~0ull) return false;  // frozen at the first failing pair
+        // part 2: kick, jump, Kepler drift, back to inertial
+        if (planet)
+            for (int q = 0; q < 3; ++q) {
+                u[q] += dt * fac * a[q];
+                x[q] += half_dt * (P[q] - wv * u[q]);
+            }
+        kepler(x, u, tx, tu);
+        for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
+        if (!whds_sums(x, u, wv, S)) return false;
+        const double P2[3] = {S[3], S[4], S[5]};
+        whds_to_inertial(x, u, Rc, Vc, S, P2, fac);
+        if (!midpoint(half_dt, nullptr, nullptr)) return false;
+        t += dt;
+        return true;
+    }
+
     __device__ __forceinline__ bool step() {
         constexpr int AN = NT > 0 ? NT : 1;
         const bool tn = tan_on();
@@ -935,11 +1021,13 @@ struct Large {
 
 // Thread roles: block b holds bodies [b per_block, (b + 1) per_block); thread
 // r per_block + l of the block is role r of body b per_block + l (r = 0..NT).
-// JAC: Jacobi coordinates (NT = 0 only), a kernel of its own so that the
-// democratic-heliocentric one carries none of its code.
-template <int NT, bool JAC = false>
+// CO: the coordinates (posi_coords); Jacobi and WHDS (NT = 0 only) are
+// kernels of their own, so that the democratic-heliocentric one carries none
+// of their code.
+template <int NT, int CO = POSI_DEMOCRATIC_HELIOCENTRIC>
 __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t n_steps) {
-    static_assert(!JAC || NT == 0, "Jacobi coordinates carry no tangents");
+    constexpr bool JAC = CO == POSI_JACOBI;
+    static_assert(CO == POSI_DEMOCRATIC_HELIOCENTRIC || NT == 0, "Jacobi and WHDS carry no tangents");
     __shared__ double shm[(kBlock / 32 + 1) * BP_ROW];
     Large<NT> S(D, shm);
     S.n = D.n;
@@ -1006,7 +1094,7 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
         S.inv_hm = 1. / S.hc.m;
     }
     S.jac = JAC;
-    S.kgm = S.hc.mg;
+    S.kgm = CO == POSI_WHDS ? S.hc.mg + (S.planet ? S.c.mg : 0.) : S.hc.mg;
     S.p1 = S.host == 0 ? 1 : 0;
     S.eta_ex = S.eta_in = S.hc.m;
     for (int q = 0; q < 3; ++q) S.Rb[q] = S.Vb[q] = 0.;
@@ -1025,6 +1113,7 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
     if (live) {
         for (int64_t k = 0; k < n_steps; ++k) {
             if constexpr (JAC) ok = S.step_jacobi();
+            else if constexpr (CO == POSI_WHDS) ok = S.step_whds();
             else ok = S.step();
             if (!ok) break;
             ++done;

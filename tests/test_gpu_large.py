@@ -150,3 +150,29 @@ def test_large_jacobi_host_not_first():
     assert steps[0] == 100
     assert max_rel_error(got, {k: (v[0] if isinstance(v, np.ndarray) and k != "tables" else v)
                                for k, v in ref.items()}) <= TOL_100
+
+
+@pytest.mark.parametrize("n_small", [29, 125])
+def test_large_whds_matches_oracle(n_small):
+    """WHDS coordinates: within 1e-10 of the oracle after 100 steps."""
+    case = E.workload_large(n_small, seed=3, coords=L.WHDS)
+    st, got = _run_large(case, 100)
+    assert st == L.OK
+    ref, steps, _ = oracle.run(stack([case]), max_steps=100, init_physical=True)
+    assert steps[0] == 100
+    assert max_rel_error(got, {k: (v[0] if isinstance(v, np.ndarray) and k != "tables" else v)
+                               for k, v in ref.items()}) <= TOL_100
+
+
+def test_large_whds_matches_batched_kernel():
+    ens = E.workload_single(seed=2, coords=L.WHDS)
+    case = {k: (v[0] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
+    case["n"] = int(case["sys_i64"][L.SI_N])
+    b = pg.Batch(ens, mode=pg.FAST)
+    b.initialize_physical_values()
+    b.iterate(200, 200)
+    ref = b.get_state()
+    st, got = _run_large(case, 200)
+    assert st == L.OK
+    one = {k: (v[0] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ref.items()}
+    assert max_rel_error(got, one) <= TOL_100
