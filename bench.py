@@ -64,6 +64,13 @@ def parse():
     return p.parse_args()
 
 
+# DRAM bytes per system and kernel launch, from one ncu capture of the kernel
+# on 1024 systems (dram__bytes_read.sum + dram__bytes_write.sum over the
+# systems; the state is read and written once per launch whatever its step
+# count): profiles/whfast_steps_kernel_ensemble8_small.md (5.03 MB + 0 MB) and
+# profiles/ias15_steps_kernel_ensemble8_small.md (12.24 MB + 1.12 MB)
+DRAM_BYTES_PER_SYSTEM_LAUNCH = {"ensemble8": 5.03e6 / 1024, "ias15": 13.36e6 / 1024}
+
 EFFECTS = {
     "ensemble8": "CTL tides + oblate flattening + Kidder GR",
     "single": "CTL tides + oblate flattening + Kidder GR",
@@ -730,8 +737,15 @@ def main():
         result["accuracy_note"] = (f"relative deviation of the barycentric Newtonian energy from the oracle's own "
                                    f"trajectory after {W + 2 * K} steps, max over {len(sample)} sampled systems")
         achieved = flops * batch.n_sys * spl / (per_launch_ms * 1e-3) / 1e12
+        per_sys = DRAM_BYTES_PER_SYSTEM_LAUNCH.get(args.workload)
+        # a timed launch of the balanced schedule is several kernel launches,
+        # each reading and writing every system's state once
+        traffic = None if per_sys is None else per_sys * batch.n_sys * (launches / R)
         result["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                              "frac": achieved / peak, "traffic": None,
+                              "frac": achieved / peak, "traffic": traffic,
+                              "traffic_note": "DRAM bytes per timed launch: the per-system bytes of one ncu capture "
+                                              "on 1024 systems (profiles/) x systems x kernel launches per timed "
+                                              "launch; FP64-bound, the state stays on chip between steps",
                               "flops_per_system_step": flops,
                               "peak_source": "measured in-run: posi_fp64_probe (DFMA chains; MEASURED_PEAKS.json "
                                              "has no FP64 entry)",
