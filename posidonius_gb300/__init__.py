@@ -315,9 +315,11 @@ class Batch:
 
 
 class ManyBody:
-    """One system of many bodies on the whole GPU (posi_large_*): democratic
-    heliocentric WHFast, thread per body, the O(N^2) pair loop spread over
-    every SM.  ``case`` is a single-system dict of the flat layout."""
+    """One system of many bodies on the whole GPU (posi_large_*): WHFast in
+    the case's coordinates (democratic heliocentric, Jacobi or WHDS), thread
+    per body, the O(N^2) pair loop spread over every SM.  ``case`` is a
+    single-system dict of the flat layout.  Tangents (``iterate_tangent``):
+    democratic heliocentric only."""
 
     def __init__(self, case):
         st = ctypes.c_int(0)

@@ -26,7 +26,9 @@
 //   dissipation factors and Love numbers); NT = 0 is the plain integration.
 //
 // Coordinates: democratic heliocentric (src/integrator/whfast.rs:495-530,
-// 965-1024, 1082-1155).  Effects: constant-time-lag tides, oblate
+// 965-1024, 1082-1155); Jacobi (:889-963, 1034-1080: the sequential
+// recurrences as grid prefix scans) and WHDS (the scaled velocities, per-body
+// jump and kick) in kernels of their own, without tangents.  Effects: constant-time-lag tides, oblate
 // flattening, Kidder GR for orbiting bodies of a central host, in the FAST
 // formulation (the generated blocks of adjoint_effects.cuh); non-evolving
 // bodies.  Kepler drift: universal variables (adjoint_blocks.cuh).
