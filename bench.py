@@ -463,6 +463,21 @@ def run_gradient(args):
         "gradient_checks": checks, "clocks": clock_info,
         "gpu_launches": int(2 * ((K + every - 1) // every) * 2),
     }
+    # HBM traffic of the checkpoints and step records (the integration itself
+    # keeps every system on chip): one state copy per chunk in the forward
+    # run; in the backward run one state copy per chunk and the step records,
+    # written by the re-integration and read by the reverse sweep (2.69 MB per
+    # step for 1024 systems, dram__bytes_read.sum of the reverse kernel,
+    # profiles/adj_reverse_kernel_gradient_small.md, scaled by systems)
+    from posidonius_gb300 import layout as L
+    n_chunks = (K + every - 1) // every
+    state_bytes = S * 4 * L.BF_COUNT * 8 + S * (L.SF_COUNT + L.SI_COUNT) * 8
+    tape_bytes = 2.69e6 * (S / 1024) * K
+    result["hbm"] = {"checkpoint_bytes": n_chunks * state_bytes,
+                     "forward_gb_s": n_chunks * state_bytes / (fwd_ms * 1e-3) / 1e9,
+                     "step_record_bytes_written_and_read": 2 * tape_bytes,
+                     "backward_gb_s": (n_chunks * state_bytes + 2 * tape_bytes) / (bwd_ms * 1e-3) / 1e9,
+                     "note": "far below the HBM roof: the forward and reverse kernels are FP64-bound"}
     print(json.dumps(result), flush=True)
 
 
