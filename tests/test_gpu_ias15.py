@@ -279,3 +279,27 @@ def test_every_effect_under_ias15_exact(name):
     b.initialize_physical_values()
     b.iterate(20, 10)
     assert bitwise_diffs(b.get_state(), ref) == []
+
+
+def test_mixed_batches_and_other_engines_refuse_ias15():
+    """A batch holds systems of one integrator; the adjoint and the
+    many-body engine take WHFast systems only."""
+    from posidonius_gb300 import adjoint as A
+    whf = E.workload_single(seed=1)
+    ias = E.as_ias15(whf)
+    both = stack([{k: (v[0] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in e.items()}
+                  | {"n": int(e["sys_i64"][0, L.SI_N])} for e in (whf, ias)])
+    both["body_ias"] = np.concatenate([np.zeros_like(ias["body_ias"]), ias["body_ias"]])
+    with pytest.raises(pg.PosiError) as e:
+        pg.Batch(both, mode=pg.EXACT)
+    assert e.value.status == L.ERR_UNSUPPORTED
+    b = pg.Batch(ias, mode=pg.FAST)
+    b.initialize_physical_values()
+    with pytest.raises(pg.PosiError) as e:
+        A.Adjoint(b, 10, 5)
+    assert e.value.status == L.ERR_UNSUPPORTED
+    b.close()
+    one = {k: (v[0] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ias.items()}
+    with pytest.raises(pg.PosiError) as e:
+        pg.ManyBody(one)
+    assert e.value.status == L.ERR_UNSUPPORTED
