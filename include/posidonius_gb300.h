@@ -337,8 +337,8 @@ int posi_batch_set_state(posi_batch* b, const int64_t* sys_i64, const double* sy
  * [POSI_IAS_COUNT] (zeros after posi_batch_create); POSI_ERR_STATE for a
  * WHFast batch.  A batch holds systems of one integrator (sys_i64
  * [POSI_SI_INTEGRATOR]); an IAS15 batch advances by IAS15 steps in
- * posi_batch_iterate (adaptive per system, groups of 8, 16 or 32 lanes, no
- * balanced schedules, no autotuning). */
+ * posi_batch_iterate (adaptive per system, the smallest lane group that holds
+ * the system, no balanced schedules, no autotuning). */
 int posi_batch_get_ias15(const posi_batch* b, double* body_ias);
 int posi_batch_set_ias15(posi_batch* b, const double* body_ias);
 

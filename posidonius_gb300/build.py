@@ -23,6 +23,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = [
     ("kernels_exact.cu", ["-fmad=false"]),
     ("kernels_fast.cu", ["-fmad=true"]),
+    ("ias15_exact.cu", ["-fmad=false"]),
+    ("ias15_fast.cu", ["-fmad=true"]),
     ("posi_host.cu", ["-fmad=false"]),
     ("case_reader.cpp", ["-x", "cu", "-fmad=false"]),
     ("diagnostics.cu", ["-fmad=true"]),

@@ -1,10 +1,11 @@
 // ias15_device.cuh -- FP64 device code of the IAS15 integrator
-// (src/integrator/ias15.rs), included by whfast_device.cuh inside its
-// namespace and compiled in both arithmetic modes.
+// (src/integrator/ias15.rs), included by ias15_impl.cuh inside the namespace
+// of whfast_device.cuh and compiled in both arithmetic modes.
 //
-// Mapping: the WHFast kernel's lane groups (G = 8, 16 or 32 lanes, lane j owns
-// body j).  A lane keeps its body's Gauss-Radau coefficients b and g (7 sets
-// of 3 components, and the same for the spin angular momentum), their
+// Mapping: the WHFast kernel's lane groups (G = 2 to 32 lanes, the smallest
+// that holds the system; lane j owns body j).  A lane keeps its body's
+// Gauss-Radau coefficients b and g (7 sets of 3 components, and the same for
+// the spin angular momentum), their
 // compensated-summation terms and the step's initial state in local arrays;
 // the predictions e, the last accepted br / er (and their spin forms) and
 // csx / csv / css stay in the per-body IAS15 array in HBM ([POSI_IAS_COUNT]

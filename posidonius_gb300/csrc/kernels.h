@@ -27,7 +27,7 @@ struct DevView {
 // OP_STEPS_REC: OP_STEPS writing the adjoint's step records to DevView::rec
 // (FAST build only).
 // OP_STEPS_SCHED: OP_STEPS under a balanced schedule (whfast_sched_kernel)
-// OP_IAS15_STEPS: n_steps IAS15 steps (G = 8, 16 or 32; DevView::ias set)
+// OP_IAS15_STEPS: n_steps IAS15 steps (DevView::ias set)
 enum KernelOp { OP_STEPS = 0, OP_INIT = 1, OP_GRAVITY = 2, OP_EFFECTS = 3, OP_STEPS_REC = 4, OP_STEPS_SCHED = 5,
                 OP_IAS15_STEPS = 6 };
 
@@ -50,6 +50,12 @@ cudaError_t launch_fast(const DevView& d, const LaunchArgs& a, cudaStream_t stre
 // Kernel attributes (dynamic shared memory); call before the first launch.
 cudaError_t prepare_exact();
 cudaError_t prepare_fast();
+// The IAS15 kernels (their own translation units; launch_exact / launch_fast
+// forward OP_IAS15_STEPS to them).
+cudaError_t launch_ias15_exact(const DevView& d, const LaunchArgs& a, cudaStream_t stream);
+cudaError_t launch_ias15_fast(const DevView& d, const LaunchArgs& a, cudaStream_t stream);
+cudaError_t prepare_ias15_exact();
+cudaError_t prepare_ias15_fast();
 
 // Lanes per system used for a system of n bodies (0 when n is out of range).
 inline int group_size_for(int64_t n) {

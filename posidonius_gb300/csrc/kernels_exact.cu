@@ -4,7 +4,11 @@
 
 namespace posi {
 cudaError_t launch_exact(const DevView& d, const LaunchArgs& a, cudaStream_t stream) {
+    if (a.op == OP_IAS15_STEPS) return launch_ias15_exact(d, a, stream);
     return posi_exact::launch_any(d, a, stream);
 }
-cudaError_t prepare_exact() { return posi_exact::prepare_all(); }
+cudaError_t prepare_exact() {
+    cudaError_t e = posi_exact::prepare_all();
+    return e != cudaSuccess ? e : prepare_ias15_exact();
+}
 }  // namespace posi

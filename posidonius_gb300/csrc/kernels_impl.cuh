@@ -42,14 +42,6 @@ static cudaError_t launch_g(const posi::DevView& v, const posi::LaunchArgs& a, c
             } else {
                 return cudaErrorInvalidValue;
             }
-        case posi::OP_IAS15_STEPS:
-            if constexpr (G >= 8) {
-                if (!d.ias) return cudaErrorInvalidValue;
-                ias15_steps_kernel<G><<<blocks, threads, smem, stream>>>(d, a.n_steps);
-                break;
-            } else {
-                return cudaErrorInvalidValue;
-            }
         case posi::OP_INIT:
             init_physical_kernel<G><<<blocks, threads, smem, stream>>>(d);
             break;
@@ -76,11 +68,6 @@ static cudaError_t prepare_g() {
     if constexpr (G >= 4) {
         const int ssmem = (posi::kSchedBlockThreads / G) * GroupSmem<G>::bytes;
         if ((e = cudaFuncSetAttribute(whfast_sched_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, ssmem)) !=
-            cudaSuccess)
-            return e;
-    }
-    if constexpr (G >= 8) {
-        if ((e = cudaFuncSetAttribute(ias15_steps_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
             cudaSuccess)
             return e;
     }

@@ -225,7 +225,6 @@ int build_buckets(posi_batch* b, const int64_t* sys_i64, const std::map<int64_t,
         } else if (b->mapping >= POSI_MAP_LANES2 && b->mapping <= POSI_MAP_WARP && b->mapping >= G) {
             G = b->mapping;
         }
-        if (b->ias15 && G < 8) G = 8;   // the IAS15 kernel runs groups of 8, 16 or 32 lanes
         by_g[G].push_back((int32_t)s);
         b->mapping_of_n[n] = G;
     }
@@ -1134,7 +1133,7 @@ int posi_set_ias15(posi_handle* h, const double* body_ias) {
 int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n) {
     if (!b || probe_steps < 1) return POSI_ERR_ARG;
     if (b->ias15) {
-        // the IAS15 kernel's lane groups are fixed (8, 16 or 32 lanes)
+        // the IAS15 kernel takes the smallest lane group that holds a system
         if (lanes_by_n)
             for (int k = 0; k <= POSI_MAX_BODIES; ++k)
                 lanes_by_n[k] = b->mapping_of_n.count(k) ? b->mapping_of_n.at(k) : 0;

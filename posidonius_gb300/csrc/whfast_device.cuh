@@ -2560,6 +2560,4 @@ __global__ void __launch_bounds__(128) additional_effects_kernel(Dev D, double t
     S.store(D);
 }
 
-#include "ias15_device.cuh"
-
 }  // namespace POSI_NS
