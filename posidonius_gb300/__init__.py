@@ -386,3 +386,7 @@ class ManyBody:
                for k in ("sys_i64", "sys_f64", "body_i64", "body_f64")}
         check(lib().posi_large_set_state(self._h, ptr(arr["sys_i64"], "i"), ptr(arr["sys_f64"], "f"),
                                          ptr(arr["body_i64"], "i"), ptr(arr["body_f64"], "f")))
+
+
+# the pure-Python parts: seeded systems and ensembles, case documents
+from . import case_writer, ensemble  # noqa: E402,F401
