@@ -167,3 +167,22 @@ def test_cli_start_resume_matches_uninterrupted_run(tmp_path):
     b = json.loads((tmp_path / "full_rec.json").read_text())
     assert a["current_iteration"] == b["current_iteration"]
     assert a["universe"]["particles"] == b["universe"]["particles"]
+
+
+def test_generated_case_document_drives_the_cli_and_the_oracle(tmp_path):
+    """A seeded system written by the case writer: `posidonius start` runs
+    it to its time limit, and the library and the oracle integrate the
+    document to the same bits."""
+    from posidonius_gb300 import case_writer as W, ensemble as E
+    ens = E.workload_single(seed=4, time_limit=4.0)
+    path = tmp_path / "generated.json"
+    W.write_case(path, ens)
+    r = _cli("start", path, tmp_path / "rec.json", tmp_path / "hist.bin", "-s")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Simulation completed" in r.stdout
+    w = pg.restore_snapshot(path, mode=pg.EXACT)
+    steps = w.run()
+    assert steps == 49   # t + dt > 4.0 after 49 steps of 0.08 d
+    ref, rsteps, _ = oracle.run(load_case(str(path)), max_steps=10**6, init_physical=True)
+    assert rsteps[0] == steps
+    assert bitwise_diffs(w.get_state(), ref) == []
