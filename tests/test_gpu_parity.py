@@ -189,3 +189,28 @@ def test_collision_freezes_only_that_system():
     assert all(st["sys_i64"][s, L.SI_ITERATION] == 5 for s in (0, 2, 3))
     assert bitwise_diffs({k: (v[[0, 2, 3]] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in st.items()},
                          {k: (v[[0, 2, 3]] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ref.items()}) == []
+
+
+def test_batched_maximum_body_count_exact():
+    """The largest systems of the batched kernels (POSI_MAX_BODIES = 32
+    bodies, one warp per system) in all three coordinate systems and by
+    IAS15, with 17- and 20-body systems in the same lane groups: bit for
+    bit against the oracle."""
+    cases = []
+    for coords, n_small in ((L.JACOBI, 29), (L.DEMOCRATIC_HELIOCENTRIC, 29), (L.WHDS, 29), (L.JACOBI, 14),
+                            (L.WHDS, 17)):
+        cases.append(E.workload_large(n_small, seed=7 + n_small, coords=coords))
+    ens = stack(cases, nmax=L.MAX_BODIES)
+    ref, steps, _ = oracle.run(ens, max_steps=30, init_physical=True, nthreads=5)
+    b = pg.Batch(ens, mode=pg.EXACT)
+    assert b.mapping_for(32) == 32 and b.mapping_for(17) == 32
+    b.initialize_physical_values()
+    b.iterate(30, 10)
+    assert np.all(b.get_state()["sys_i64"][:, L.SI_ITERATION] == 30)
+    assert bitwise_diffs(b.get_state(), ref) == []
+    ias = E.as_ias15(stack(cases[:2], nmax=L.MAX_BODIES), dt=0.1)
+    ref, _, _ = oracle.run(ias, max_steps=5, init_physical=True, nthreads=2)
+    bi = pg.Batch(ias, mode=pg.EXACT)
+    bi.initialize_physical_values()
+    bi.iterate(5, 5)
+    assert bitwise_diffs(bi.get_state(), ref) == []
