@@ -214,3 +214,29 @@ def test_batched_maximum_body_count_exact():
     bi.initialize_physical_values()
     bi.iterate(5, 5)
     assert bitwise_diffs(bi.get_state(), ref) == []
+
+
+def test_empty_and_zero_step_requests():
+    """An ensemble of no systems is refused; zero steps change no bit; a
+    completed system stays frozen under further steps."""
+    ens = E.workload_ensemble8(4, seed=2)
+    empty = {k: (v[:0] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
+    empty["n_sys"] = 0
+    with pytest.raises(pg.PosiError) as e:
+        pg.Batch(empty, mode=pg.EXACT)
+    assert e.value.status == L.ERR_ARG
+    b = pg.Batch(ens, mode=pg.EXACT)
+    b.initialize_physical_values()
+    before = b.get_state()
+    b.iterate(0)
+    assert bitwise_diffs(b.get_state(), before) == []
+    short = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in ens.items()}
+    short["sys_f64"][:, L.SF_TIME_LIMIT] = 0.5   # completes after 6 steps of 0.08 d
+    c = pg.Batch(short, mode=pg.EXACT)
+    c.initialize_physical_values()
+    c.iterate(10, 10)
+    done = c.get_state()
+    assert np.all(done["sys_i64"][:, L.SI_STATUS] & L.SYS_FATAL_MASK == L.SYS_COMPLETED)
+    assert np.all(done["sys_i64"][:, L.SI_ITERATION] == 6)
+    c.iterate(5, 5)
+    assert bitwise_diffs(c.get_state(), done) == []
