@@ -1,6 +1,6 @@
 // whfast_device.cuh -- FP64 device code of the WHFast + tidal-effects step.
 //
-// Mapping: one group of G lanes (G = 4, 8, 16 or 32; G >= n) integrates one
+// Mapping: one group of G lanes (G = 2, 4, 8, 16 or 32; G >= n) integrates one
 // independent system; lane j owns body j (reference particle order, the host
 // at any index).  Each lane keeps its body's state in registers for the whole
 // launch; the per-planet constants of a half kick live in shared memory.
