@@ -95,3 +95,26 @@ def test_star_order_permutation():
     f1 = e1["body_f64"][0][[1, 0, 2, 3, 4]]
     for sl in (L.POS, L.VEL, L.ACC):
         assert np.abs(f0[:, sl] - f1[:, sl]).max() <= 1e-16
+
+
+def test_ias15_star_order_permutation():
+    """tests/test_order.rs (the IAS15 order cases): swapping the star and the
+    first planet of the IAS15 case gives the same trajectory; IAS15 has no
+    coordinate recurrence over the body order, so only the pair-sum order of
+    the accelerations changes (1e-15 absolute after the adaptive run)."""
+    name = names("ias15")[0]
+    d = case_dict(name)
+    u = d["universe"]
+    u["particles"][0], u["particles"][1] = u["particles"][1], u["particles"][0]
+    u["particles_evolvers"][0], u["particles_evolvers"][1] = u["particles_evolvers"][1], u["particles_evolvers"][0]
+    for k in ("most_massive", "tides", "rotational_flattening", "general_relativity"):
+        u["hosts"]["index"][k] = 1
+    base = load_case(case_dict(name))
+    swapped = load_case(d)
+    e0, s0, _ = oracle.run(base, max_steps=10**6, init_physical=True)
+    e1, s1, _ = oracle.run(swapped, max_steps=10**6, init_physical=True)
+    assert s0[0] == s1[0] == 4
+    f0 = e0["body_f64"][0]
+    f1 = e1["body_f64"][0][[1, 0, 2, 3, 4]]
+    for sl in (L.POS, L.VEL):
+        assert np.abs(f0[:, sl] - f1[:, sl]).max() <= 1e-15
