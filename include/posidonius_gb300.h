@@ -193,7 +193,7 @@ enum posi_mode { POSI_MODE_EXACT = 0, POSI_MODE_FAST = 1 };
 /* Thread mappings of the batched kernel (bodies per lane group). */
 enum posi_mapping {
     POSI_MAP_AUTO = 0,           /* autotuned per body-count bucket */
-    POSI_MAP_THREAD = 1,         /* one thread per system */
+    POSI_MAP_THREAD = 1,         /* one thread per system: not built, refused with POSI_ERR_UNSUPPORTED */
     POSI_MAP_LANES2 = 2,         /* 2 lanes per system (one body per lane) */
     POSI_MAP_LANES4 = 4,         /* 4 lanes per system */
     POSI_MAP_LANES8 = 8,
@@ -414,7 +414,8 @@ int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_
  * file-scope device array of 48 MiB, enough for 48 MiB / (209 * 8 bytes) =
  * 30,102 body-steps (n_steps * n_systems * nmax, less 4 bytes per system for
  * the system list); larger requests fail with POSI_ERR_ARG and a message
- * giving the limit.
+ * giving the limit (the bound is checked by division, so that no request
+ * size can wrap it).
  * Same computation as one chunk of posi_adjoint_backward: from the state in
  * the device arrays (the library's field-major layout: sys_i64
  * [POSI_SI_COUNT][n_systems], sys_f64 [POSI_SF_COUNT][n_systems], body_i64
@@ -423,12 +424,17 @@ int posi_adjoint_backward(posi_adjoint* a, const double* lam_final, double* lam_
  * reverse.  d_lam [12][n_systems * nmax] holds the adjoints of the final
  * (r, v, L, S) on entry and those of the initial state on return; d_grad
  * [2][n_systems * nmax] (d/d sigma, d/d k2) is added to; d_flags
- * [n_systems] receives posi_adjoint_flag bits (cleared first).  All pointers
+ * [n_systems] receives posi_adjoint_flag bits (cleared first).  A system
+ * the adjoint does not support (POSI_ADJ_UNSUPPORTED: not Jacobi, evolving
+ * bodies, Anderson / Newhall GR, wind, disk, IAS15, or a body count outside
+ * 1..nmax) is left out of the run: its d_lam and d_grad entries are not
+ * touched.  All pointers
  * are device pointers; the work is queued on `stream` (a cudaStream_t, or
  * NULL) and the outputs are ready when the stream reaches it.
  * The first call on a device takes the array's address
- * (cudaGetSymbolAddress) and sets the kernels' shared-memory attributes:
- * make that first call before any stream capture.  Every call on a device
+ * (cudaGetSymbolAddress) and sets the kernels' shared-memory attributes
+ * (under a lock, so host threads making their first calls at once are
+ * safe): make that first call before any stream capture.  Every call on a device
  * shares the one array: calls whose work overlaps on the GPU (other streams,
  * other host threads) race on it and must be serialised by the caller. */
 int posi_adjoint_vjp_static(int64_t n_systems, int64_t nmax, const int64_t* d_sys_i64, const double* d_sys_f64,

@@ -1,5 +1,6 @@
 // adjoint.cu -- launchers of the adjoint kernels (adjoint_device.cuh).
 #include <climits>
+#include <mutex>
 #include <string>
 
 #include "adjoint_device.cuh"
@@ -83,12 +84,12 @@ __device__ __align__(256) unsigned char g_adj_scratch[kStaticScratchBytes];
 
 constexpr int kMaxDevices = 64;
 void* g_scratch_ptr[kMaxDevices] = {};
+std::mutex g_scratch_setup;  // guards the once-per-device set-up below
 
 __global__ void static_list_and_check(int32_t* list, int32_t n_sys, int64_t nmax, const int64_t* si,
                                       int32_t* flags) {
     const int32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n_sys) return;
-    list[s] = s;
     const int64_t n = si[(int64_t)POSI_SI_N * n_sys + s];
     const bool ok = si[(int64_t)POSI_SI_COORDS * n_sys + s] == POSI_JACOBI &&
                     si[(int64_t)POSI_SI_EVOLUTION * n_sys + s] == 0 && n >= 1 && n <= nmax &&
@@ -97,6 +98,9 @@ __global__ void static_list_and_check(int32_t* list, int32_t n_sys, int64_t nmax
                     si[(int64_t)POSI_SI_WIND * n_sys + s] == 0 && si[(int64_t)POSI_SI_DISK * n_sys + s] == 0 &&
                     si[(int64_t)POSI_SI_INTEGRATOR * n_sys + s] == POSI_INTEGRATOR_WHFAST;
     flags[s] = ok ? 0 : POSI_ADJ_UNSUPPORTED;
+    // a refused system stays out of the record and reverse kernels: its body
+    // count may exceed nmax, and its lanes would then index the next system
+    list[s] = ok ? s : -1;
 }
 
 }  // namespace
@@ -118,38 +122,48 @@ extern "C" int posi_adjoint_vjp_static(int64_t n_systems, int64_t nmax, const in
         return POSI_ERR_UNSUPPORTED;
     }
     const int64_t stride = n_systems * nmax;
-    const size_t tape_bytes = ((size_t)n_steps * posi_adj::SV_COUNT * (size_t)stride * sizeof(double) + 255) / 256 * 256;
-    const size_t list_bytes = (size_t)n_systems * sizeof(int32_t);
-    if (tape_bytes + list_bytes > kStaticScratchBytes) {
-        set_last_error("posi_adjoint_vjp_static: n_steps x systems x bodies needs " +
-                       std::to_string(tape_bytes + list_bytes) + " bytes of step records, above the " +
-                       std::to_string(kStaticScratchBytes) + "-byte static scratch (at most " +
+    const size_t list_bytes = ((size_t)n_systems * sizeof(int32_t) + 255) / 256 * 256;
+    const size_t step_bytes = (size_t)posi_adj::SV_COUNT * sizeof(double) * (size_t)stride;
+    // bounded by division first, so that no product below can wrap
+    if ((uint64_t)nmax > kStaticScratchBytes || (uint64_t)stride > kStaticScratchBytes / sizeof(double) ||
+        list_bytes > kStaticScratchBytes || (uint64_t)n_steps > (kStaticScratchBytes - list_bytes) / step_bytes) {
+        set_last_error("posi_adjoint_vjp_static: " + std::to_string(n_steps) + " steps x " +
+                       std::to_string(n_systems) + " systems x " + std::to_string(nmax) +
+                       " bodies of step records do not fit the " + std::to_string(kStaticScratchBytes) +
+                       "-byte static scratch (at most " +
                        std::to_string(kStaticScratchBytes / (posi_adj::SV_COUNT * sizeof(double))) +
                        " body-steps)");
         return POSI_ERR_ARG;
     }
+    const size_t tape_bytes = (size_t)n_steps * step_bytes;  // a multiple of 8; the list follows it
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         set_last_error("posi_adjoint_vjp_static: no usable current device");
         return POSI_ERR_CUDA;
     }
     // set-up, once per device (the first call on a device must come before
-    // any stream capture)
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_adj_scratch);
-        if (e != cudaSuccess || !p) {
-            set_last_error(std::string("posi_adjoint_vjp_static: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            return POSI_ERR_CUDA;
+    // any stream capture); host threads making their first calls together
+    // wait for one another
+    char* base = nullptr;
+    {
+        std::lock_guard<std::mutex> setup_lock(g_scratch_setup);
+        if (!g_scratch_ptr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_adj_scratch);
+            if (e != cudaSuccess || !p) {
+                set_last_error(std::string("posi_adjoint_vjp_static: cudaGetSymbolAddress: ") +
+                               cudaGetErrorString(e));
+                return POSI_ERR_CUDA;
+            }
+            e = prepare_adjoint();
+            if (e != cudaSuccess) {
+                set_last_error(std::string("posi_adjoint_vjp_static: ") + cudaGetErrorString(e));
+                return POSI_ERR_CUDA;
+            }
+            g_scratch_ptr[dev] = p;
         }
-        e = prepare_adjoint();
-        if (e != cudaSuccess) {
-            set_last_error(std::string("posi_adjoint_vjp_static: ") + cudaGetErrorString(e));
-            return POSI_ERR_CUDA;
-        }
-        g_scratch_ptr[dev] = p;
+        base = (char*)g_scratch_ptr[dev];
     }
-    char* base = (char*)g_scratch_ptr[dev];
     AdjView v;
     v.n_sys = n_systems;
     v.nmax = nmax;

@@ -46,7 +46,7 @@ struct AdjDev {
     const int64_t* bi;      // [POSI_BI_COUNT][stride]
     const double* sf;       // [POSI_SF_COUNT][n_sys]
     const int64_t* si;      // [POSI_SI_COUNT][n_sys]
-    const int32_t* list;
+    const int32_t* list;    // systems to run; a negative entry is skipped
     int32_t n_list;
     double* tape;           // [k][SV_COUNT][stride] step records
     double* lam;            // [LM_COUNT][stride]
@@ -760,7 +760,7 @@ __device__ __forceinline__ bool adj_group_setup(const AdjDev& D, int& sys, int& 
     smem = shm + (size_t)gib * (AdjSmem<G>::bytes / 8);
     if (gid >= D.n_list) return false;
     sys = D.list[gid];
-    return true;
+    return sys >= 0;  // a negative entry is a system left out of the run
 }
 
 // Forward K steps from the chunk's start state, writing every step's record.

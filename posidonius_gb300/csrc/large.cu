@@ -12,7 +12,8 @@ struct posi_large {
     int64_t n = 0;
     int coords = POSI_DEMOCRATIC_HELIOCENTRIC;
     int grid = 0, nchunk = 0, per_block = 0;
-    double *d_bf = nullptr, *d_sf = nullptr, *d_roche = nullptr, *d_pos = nullptr, *d_gpart = nullptr,
+    double *d_bf = nullptr, *d_sf = nullptr, *d_roche = nullptr, *d_near2 = nullptr, *d_pos = nullptr,
+           *d_gpart = nullptr,
            *d_bpart = nullptr, *d_tot = nullptr, *d_tan = nullptr, *d_dpos = nullptr;
     int64_t *d_bi = nullptr, *d_si = nullptr;
     unsigned* d_bar = nullptr;
@@ -27,7 +28,8 @@ namespace {
 
 void free_large(posi_large* L) {
     if (!L) return;
-    cudaFree(L->d_bf); cudaFree(L->d_sf); cudaFree(L->d_roche); cudaFree(L->d_pos); cudaFree(L->d_gpart);
+    cudaFree(L->d_bf); cudaFree(L->d_sf); cudaFree(L->d_roche); cudaFree(L->d_near2); cudaFree(L->d_pos);
+    cudaFree(L->d_gpart);
     cudaFree(L->d_bpart); cudaFree(L->d_tot); cudaFree(L->d_bi); cudaFree(L->d_si); cudaFree(L->d_bar); cudaFree(L->d_err);
     cudaFree(L->d_bad); cudaFree(L->d_tan); cudaFree(L->d_dpos);
     if (L->e0) cudaEventDestroy(L->e0);
@@ -119,6 +121,7 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
         !ok(cudaMalloc(&L->d_sf, POSI_SF_COUNT * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_si, POSI_SI_COUNT * sizeof(int64_t))) ||
         !ok(cudaMalloc(&L->d_roche, (size_t)n * n * sizeof(double))) ||
+        !ok(cudaMalloc(&L->d_near2, (size_t)n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_pos, (size_t)3 * n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_gpart, (size_t)L->nchunk * 3 * (1 + posi_many::kMaxTangents) * n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_bpart, (size_t)L->grid * posi_many::BP_ROW * sizeof(double))) ||
@@ -145,16 +148,25 @@ int posi_large_set_state(posi_large* L, const int64_t* sys_i64, const double* sy
         auto bf = to_field_major(body_f64, n, POSI_BF_COUNT);
         LCK(cudaMemcpy(L->d_bf, bf.data(), bf.size() * sizeof(double), cudaMemcpyHostToDevice));
         // src/particles/universe.rs:177-196, libm pow like Rust's powf
-        std::vector<double> roche((size_t)n * n, 0.);
+        // near2[i]: the largest squared threshold of body i's checks (Roche
+        // radius of row i, sum of radii), so that the kernel reads the table
+        // only for pairs that are that close
+        std::vector<double> roche((size_t)n * n, 0.), near2((size_t)n, 0.);
         for (int64_t i = 0; i < n; ++i)
             for (int64_t j = 0; j < n; ++j) {
                 if (i == j) continue;
                 const double mi = body_f64[i * POSI_BF_COUNT + POSI_BF_MASS], mj = body_f64[j * POSI_BF_COUNT + POSI_BF_MASS];
                 const double ri = body_f64[i * POSI_BF_COUNT + POSI_BF_RADIUS], rj = body_f64[j * POSI_BF_COUNT + POSI_BF_RADIUS];
-                roche[(size_t)i * n + j] = mi > mj ? (rj / 0.462) * std::pow(mi / mj, 1. / 3.)
-                                                   : (ri / 0.462) * std::pow(mj / mi, 1. / 3.);
+                const double rr = mi > mj ? (rj / 0.462) * std::pow(mi / mj, 1. / 3.)
+                                          : (ri / 0.462) * std::pow(mj / mi, 1. / 3.);
+                roche[(size_t)i * n + j] = rr;
+                near2[i] = std::max(near2[i], std::max(rr * rr, (ri + rj) * (ri + rj)));
             }
+        // a margin of 1e-12 relative covers the rounding of the kernel's own
+        // products against the host's
+        for (auto& x : near2) x *= 1. + 1e-12;
         LCK(cudaMemcpy(L->d_roche, roche.data(), roche.size() * sizeof(double), cudaMemcpyHostToDevice));
+        LCK(cudaMemcpy(L->d_near2, near2.data(), near2.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
     if (body_i64) {
         auto bi = to_field_major(body_i64, n, POSI_BI_COUNT);
@@ -224,6 +236,7 @@ int run_large(posi_large* L, int64_t n_steps, const int32_t* seed_body, const in
     posi_many::LDev d{};
     d.n = L->n;
     d.bf = L->d_bf; d.bi = L->d_bi; d.sf = L->d_sf; d.si = L->d_si; d.roche = L->d_roche;
+    d.near2 = L->d_near2;
     d.pos = L->d_pos; d.gpart = L->d_gpart; d.bpart = L->d_bpart; d.tot = L->d_tot; d.bar = L->d_bar;
     d.err = L->d_err;
     d.bad = L->d_bad;

@@ -64,7 +64,8 @@ struct LDev {
     const int64_t* bi;      // [POSI_BI_COUNT][n]
     double* sf;             // [POSI_SF_COUNT]
     int64_t* si;            // [POSI_SI_COUNT]
-    const double* roche;    // [n][n] (symmetric)
+    const double* roche;    // [n][n] Roche radii, row i for the pairs (i, j > i)
+    const double* near2;    // [n] squared distance below which body i's pair checks can fire
     double* pos;            // [3][n] positions for the pair loop
     double* gpart;          // [nchunk][3 (1 + NT)][n] partial accelerations (and their tangents)
     double* bpart;          // [gridDim.x][BP_ROW]
@@ -617,6 +618,10 @@ struct Large {
                         tax[q][d] = 0.;
                     }
             const double Ri = D.bf[POSI_BF_RADIUS * nn + gi];
+            // no pair check of body gi fires beyond this distance: the rare
+            // pairs inside it read the table's row gi (the reference's
+            // roche_radiuses[i][j], not symmetric for equal masses)
+            const double near2 = D.near2[gi];
             double ax = 0., ay = 0., az = 0.;
             unsigned long long bad = ~0ull;
             for (int64_t j = j0; j < j1; ++j) {
@@ -626,8 +631,8 @@ struct Large {
                 else { xj = __ldcg(&D.pos[j]); yj = __ldcg(&D.pos[nn + j]); zj = __ldcg(&D.pos[2 * nn + j]); }
                 const double dx = xi - xj, dy = yi - yj, dz = zi - zj;
                 const double d2 = dx * dx + dy * dy + dz * dz;
-                if (gi < j && bad == ~0ull) {
-                    const double rr = D.roche[j * nn + gi];  // symmetric: coalesced across the warp
+                if (gi < j && bad == ~0ull && (d2 <= near2 || gi == host)) {
+                    const double rr = D.roche[gi * nn + j];
                     const double Rs = Ri + D.bf[POSI_BF_RADIUS * nn + j];
                     const unsigned long long key = (unsigned long long)(gi * nn + j) * 4ull;
                     if (d2 <= rr * rr) bad = key + POSI_SYS_ROCHE;

@@ -315,6 +315,16 @@ posi_batch* create_batch(int64_t n_sys, int64_t nmax, const int64_t* si, const d
         return fail(POSI_ERR_ARG, nullptr);
     }
     if (mode != POSI_MODE_EXACT && mode != POSI_MODE_FAST) { g_last_error = "unknown mode"; return fail(POSI_ERR_ARG, nullptr); }
+    if (mapping == POSI_MAP_THREAD) {
+        g_last_error = "POSI_MAP_THREAD (one thread per system) is not built; the batched kernels map a system "
+                       "onto a lane group (POSI_MAP_AUTO, POSI_MAP_LANES2..POSI_MAP_WARP)";
+        return fail(POSI_ERR_UNSUPPORTED, nullptr);
+    }
+    if (mapping != POSI_MAP_AUTO && mapping != POSI_MAP_LANES2 && mapping != POSI_MAP_LANES4 &&
+        mapping != POSI_MAP_LANES8 && mapping != POSI_MAP_LANES16 && mapping != POSI_MAP_WARP) {
+        g_last_error = "unknown mapping";
+        return fail(POSI_ERR_ARG, nullptr);
+    }
     for (int64_t s = 0; s < n_sys; ++s) {
         std::string err;
         int rc = validate_system(si + s * POSI_SI_COUNT, nmax, err);

@@ -111,3 +111,18 @@ def test_cli_usage_without_gpu():
     assert r.returncode == 2
     r = subprocess.run([B.CLI, "resume", "a.json", "b.bin", "--bogus"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 2
+
+
+def test_unbuilt_and_unknown_mappings_are_refused(built):
+    """POSI_MAP_THREAD is declared but not built: the batch refuses it (no
+    silent fallback to a lane group), before any device work; an unknown
+    mapping is an argument error."""
+    from posidonius_gb300 import ensemble as E
+    ens = E.workload_ensemble8(2, seed=1)
+    with pytest.raises(pg.PosiError) as e:
+        pg.Batch(ens, mapping=L.MAP_THREAD)
+    assert e.value.status == L.ERR_UNSUPPORTED
+    assert b"POSI_MAP_THREAD" in _lib.lib().posi_last_error()
+    with pytest.raises(pg.PosiError) as e:
+        pg.Batch(ens, mapping=3)
+    assert e.value.status == L.ERR_ARG
