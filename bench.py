@@ -6,9 +6,10 @@ radii apart), constant-time-lag tides + oblate flattening + Kidder GR, WHFast
 Jacobi, dt = 0.08 d, FP64, seeded synthetic inputs (posidonius_gb300.ensemble).
 One bench step = one WHFast step of every system.  Metric: system-steps/s.
 
-Timed region: K steps in R launches of the persistent kernel (CUDA graph
-replay); L2 is flushed before each launch and only the launches are timed,
-with CUDA events on the batch's stream.  ``e2e`` times the public C ABI with
+Timed region: one launch of the persistent kernel for K steps (CUDA graph
+replay), repeated at least five times and until the timed launches add up
+to 100 ms; L2 is flushed before each launch and only the launches are timed,
+with CUDA events on the batch's stream; the median launch is reported.  ``e2e`` times the public C ABI with
 host buffers: upload of the whole ensemble from pinned memory, K steps,
 download of the whole state.
 
@@ -34,6 +35,9 @@ sys.path.insert(0, ROOT)
 METRIC = "system-steps/s"
 UNIT = "system-steps/s"
 L2_FLUSH_BYTES = 512 << 20
+MIN_REPEATS = 5         # timed launches of K steps, at least
+MIN_TIMED_MS = 100.0    # and at least this much timed work in all
+MAX_REPEATS = 1000
 
 
 def parse():
@@ -61,6 +65,13 @@ def parse():
                    help="large workload: tangent directions of the derivative run (the two planets' "
                         "dissipation factors, then their Love numbers)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--horizon-steps", type=int, default=100000,
+                   help="default line: steps of the energy check at the workload's configured horizon")
+    p.add_argument("--horizon-systems", type=int, default=64, help="default line: systems of that check")
+    p.add_argument("--adjoint-steps", type=int, default=1000,
+                   help="default line: steps of the adjoint / forward timing on the differentiation shape")
+    p.add_argument("--no-extras", action="store_true",
+                   help="default line: leave out the energy-horizon check and the adjoint / forward timing")
     return p.parse_args()
 
 
@@ -288,6 +299,84 @@ def plain_path(mode, steps=400):
     w.close()
     return {"value": done / dt, "unit": UNIT, "workload": "single (star + 3 planets)", "steps": done,
             "note": "posi_iterate(h, 1) per WHFast step (one kernel launch + state readback each), wall clock"}
+
+
+def energy_horizon(workload, n_sys, steps, mode):
+    """The whole metric's accuracy half: n_sys systems of the workload
+    integrated for `steps` steps (its configured horizon) by the benchmarked
+    build, and the relative deviation of every system's barycentric
+    Newtonian energy from the oracle's own trajectory at the same step
+    (definition 1).  The oracle's sensitivity -- its own trajectory started
+    1e-15 (relative) away in position -- is reported beside it: a chaotic
+    system's trajectories part whatever the arithmetic.  Definition 3: the
+    same systems with every effect off (pure WHFast), the relative drift of
+    the Newtonian energy over the run, on the GPU."""
+    import oracle
+    import posidonius_gb300 as pg
+    from posidonius_gb300 import layout as L
+    from posidonius_gb300 import ensemble as E
+    seed = E.SEED_BASE + E.WORKLOAD_IDS[workload] + 500
+    ens = E.workload_ensemble8(n_sys, seed=seed) if workload != "uneven" else E.workload_uneven(n_sys, seed=seed)
+    nthreads = os.cpu_count() or 1
+    b = pg.Batch(ens, mode=mode)
+    b.initialize_physical_values()
+    t0 = time.perf_counter()
+    b.iterate(steps, min(steps, 25000))
+    gpu_s = time.perf_counter() - t0
+    got = b.get_state()
+    b.close()
+    ref, _, _ = oracle.run(ens, max_steps=steps, init_physical=True, nthreads=nthreads)
+    nud = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in ens.items()}
+    nud["body_f64"][:, :, L.POS] *= 1.0 + 1e-15
+    ref2, _, _ = oracle.run(nud, max_steps=steps, init_physical=True, nthreads=nthreads)
+    e_ref = np.array([newtonian_energy(ref, s) for s in range(n_sys)])
+    d1 = np.abs(np.array([newtonian_energy(got, s) for s in range(n_sys)]) - e_ref) / np.abs(e_ref)
+    sens = np.abs(np.array([newtonian_energy(ref2, s) for s in range(n_sys)]) - e_ref) / np.abs(e_ref)
+    off = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in ens.items()}
+    for f in (L.SI_TIDES, L.SI_FLAT, L.SI_GR):
+        off["sys_i64"][:, f] = 0
+    for f in (L.BI_TIDES_KIND, L.BI_FLAT_KIND, L.BI_GR_KIND):
+        off["body_i64"][:, :, f] = L.EFFECT_DISABLED
+    b = pg.Batch(off, mode=mode)
+    b.initialize_physical_values()
+    e0 = np.array([newtonian_energy(b.get_state(), s) for s in range(n_sys)])
+    b.iterate(steps, min(steps, 25000))
+    fin = b.get_state()
+    b.close()
+    d3 = np.abs(np.array([newtonian_energy(fin, s) for s in range(n_sys)]) - e0) / np.abs(e0)
+    q = lambda x: {"median": float(np.median(x)), "max": float(x.max())}
+    return {
+        "workload": workload, "systems": n_sys, "steps": steps, "days": steps * 0.08,
+        "def1_vs_oracle_trajectory": q(d1) | {"systems_within_1e-10": int((d1 <= 1e-10).sum())},
+        "oracle_self_sensitivity_1e-15_nudge": q(sens) | {"systems_within_1e-10": int((sens <= 1e-10).sum())},
+        "def3_pure_whfast_drift": q(d3),
+        "gpu_s": gpu_s,
+        "note": "relative deviation of the barycentric Newtonian energy: def 1 from the oracle's own trajectory at "
+                "the same step; beside it the oracle against itself started 1e-15 away (systems that part from "
+                "themselves part from any other arithmetic too); def 3 the pure-WHFast drift (effects off) "
+                "from the start",
+    }
+
+
+def adjoint_over_forward(steps, every=100, n_sys=1024):
+    """The metric's second half on the differentiation shape (1024 systems
+    of a star and 3 planets, checkpoints every `every` steps): backward
+    (adjoint) time over forward time of one loss gradient over `steps`
+    steps, CUDA events of the library's own forward and backward runs."""
+    from posidonius_gb300 import adjoint as A
+    from posidonius_gb300 import layout as L
+    ens, el, ms, moi, ss = A.gradient_workload(n_sys)
+    sig = ens["body_f64"][:, :, L.BF_SIGMA].copy()
+    k2 = ens["body_f64"][:, :, L.BF_K2].copy()
+    A.adjoint_gradient(ens, el, sig, k2, ms, moi, ss, min(steps, 2 * every), every)  # warm-up
+    _, _, _, _, (fwd_ms, bwd_ms, rec_ms, rev_ms), flags = A.adjoint_gradient(ens, el, sig, k2, ms, moi, ss, steps,
+                                                                              every)
+    return {"value": bwd_ms / fwd_ms, "forward_ms": fwd_ms, "backward_ms": bwd_ms, "steps": steps,
+            "checkpoint_every": every, "systems": n_sys, "bodies_per_system": 4,
+            "systems_flagged": int((flags != 0).sum()),
+            "note": "the gradient workload's shape (bench.py --workload gradient runs it at 1e4 steps with the "
+                    "gradient checks); forward = FAST integration with checkpoints, backward = chunk "
+                    "re-integration + reverse sweeps"}
 
 
 def run_reference(args):
@@ -644,45 +733,37 @@ def main():
     lanes = batch.autotune(probe_steps=20) if not args.no_autotune else {
         int(n): batch.mapping_for(int(n)) for n in np.unique(ens["sys_i64"][:, L.SI_N])}
     K = args.steps
-    R = max(1, min(args.launches, K))
-    spl = (K + R - 1) // R
-    K = spl * R
     W = max(3, args.warmup)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     clocks = ClockSampler(local)
     clocks.start()
-    # warm-up in launches of the timed shape, so the timed launches replay an
-    # already instantiated graph
-    done = 0
-    while done < W:
-        batch.iterate(spl, spl)
-        done += spl
-    W = done
+    # warm-up: exactly W steps, in one launch
+    batch.iterate(W, W)
     torch.cuda.synchronize()
     clocks.discard()
 
     # ---- device-timed region -------------------------------------------------
+    # one launch of K steps (one CUDA graph replay), L2 flushed before it,
+    # CUDA events on the batch's stream; repeated until the timed launches
+    # add up to at least MIN_TIMED_MS (and at least MIN_REPEATS times), the
+    # median launch reported.  Each repeat continues the integration.
     barrier(world)
     torch.cuda.synchronize()
-    total_ms = 0.0
+    times = []
     launches = 0
-    done = 0
-    done = 0
-    while done < K:
-        n = spl
-        flush.fill_(float(done))
+    while len(times) < MIN_REPEATS or (sum(times) < MIN_TIMED_MS and len(times) < MAX_REPEATS):
+        flush.fill_(float(len(times)))
         torch.cuda.synchronize()
-        batch.iterate(n, n)
+        batch.iterate(K, K)
         ms, nl = batch.last_timing()
-        total_ms += ms
-        launches += nl
-        done += n
+        times.append(ms)
+        launches = nl
     torch.cuda.synchronize()
     barrier(world)
     clock_info = clocks.stop()
-    total_ms = max_over_ranks(total_ms, world)
-    value = replica_value(world, batch.n_sys, K, total_ms)
-    per_launch_ms = total_ms / R
+    med_ms = max_over_ranks(statistics.median(times), world)
+    value = replica_value(world, batch.n_sys, K, med_ms)
+    total_ms = med_ms
 
     # ---- end-to-end through the C ABI with host buffers -----------------------
     state = batch.get_state()
@@ -694,13 +775,15 @@ def main():
     d2h = h2d
     barrier(world)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    batch.set_state(host)
-    batch.iterate(K, spl)
-    batch.get_state(out_p | {"roche": None})
-    e2e_s = time.perf_counter() - t0
+    e2e_times = []
+    while len(e2e_times) < MIN_REPEATS or (sum(e2e_times) < MIN_TIMED_MS * 1e-3 and len(e2e_times) < MAX_REPEATS):
+        t0 = time.perf_counter()
+        batch.set_state(host)
+        batch.iterate(K, K)
+        batch.get_state(out_p | {"roche": None})
+        e2e_times.append(time.perf_counter() - t0)
     barrier(world)
-    e2e_s = max_over_ranks(e2e_s, world)
+    e2e_s = max_over_ranks(statistics.median(e2e_times), world)
     e2e_value = world * batch.n_sys * K / e2e_s
 
     # ---- the plain path: one system (star + 3 planets), one launch per step ----
@@ -716,7 +799,11 @@ def main():
         "dtype": "f64", "data": "synthetic (seeded; posidonius_gb300.ensemble)",
         "config": {"workload": args.workload, "n_systems": int(batch.n_sys), "bodies_per_system": int(batch.nmax),
                    "dt_days": 0.08 if args.workload != "ias15" else "adaptive (IAS15, first trial 0.08)",
-                   "mode": args.mode, "steps_per_launch": spl, "timed_launches": R,
+                   "mode": args.mode, "steps_per_launch": K, "timed_launches": len(times),
+                   "timed_region": f"one launch of {K} steps (one CUDA graph replay), repeated {len(times)} times "
+                                   f"(at least {MIN_REPEATS}, at least {MIN_TIMED_MS:.0f} ms of timed launches in "
+                                   f"all), median launch; each repeat continues the integration",
+                   "timed_launch_ms": {"median": med_ms, "min": min(times), "max": max(times)},
                    "effects": EFFECTS[args.workload],
                    "coordinates": "Jacobi" if args.workload != "ias15" else "inertial (IAS15)",
                    "lanes_per_system": {str(k): v for k, v in sorted(lanes.items())},
@@ -724,8 +811,11 @@ def main():
                    "l2": f"flushed ({L2_FLUSH_BYTES >> 20} MiB write) before every timed launch",
                    "parallelism": f"replicas x{world} (independent ensembles per GPU)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
-                "note": f"one C-ABI call chain: upload {h2d} B, {K} steps, download {d2h} B"},
-        "gpu_launches": int(launches),
+                "note": f"one C-ABI call chain: upload {h2d} B, {K} steps, download {d2h} B; wall clock, median of "
+                        f"{len(e2e_times)} repeats"},
+        "gpu_launches": int(launches * len(times)),
+        "gpu_launches_note": f"{int(launches)} kernel launches per timed launch of {K} steps, {len(times)} timed "
+                             "launches",
         "plain_path": plain,
         "batched_over_plain": value / world / plain["value"],
         "clocks": clock_info,
@@ -741,21 +831,27 @@ def main():
         flops = cpu.pop("flops_per_system_step")
         result["cpu_baseline"] = cpu
         # accuracy: relative Newtonian-energy deviation from the oracle's own
-        # trajectory on a sample of systems, after W + 2K steps from the start
+        # trajectory on a sample of the benchmarked systems, at the step the
+        # bench left them
         sample = list(range(0, batch.n_sys, max(1, batch.n_sys // 8)))[:8]
         sub = {k: (v[sample] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
         sub["n_sys"] = len(sample)
-        ref, _, _ = oracle.run(sub, max_steps=W + 2 * K, init_physical=True, nthreads=len(sample))
+        it = int(final["sys_i64"][sample[0], L.SI_ITERATION])
+        ref, _, _ = oracle.run(sub, max_steps=it, init_physical=True, nthreads=len(sample))
         errs = [abs(newtonian_energy(final, s) - newtonian_energy(ref, i)) / abs(newtonian_energy(ref, i))
                 for i, s in enumerate(sample)]
         result["energy_rel_err_vs_oracle"] = max(errs)
         result["accuracy_note"] = (f"relative deviation of the barycentric Newtonian energy from the oracle's own "
-                                   f"trajectory after {W + 2 * K} steps, max over {len(sample)} sampled systems")
-        achieved = flops * batch.n_sys * spl / (per_launch_ms * 1e-3) / 1e12
+                                   f"trajectory after the {it} steps the bench ran, max over {len(sample)} sampled "
+                                   f"systems; energy_at_horizon gives the configured horizon")
+        if not args.no_extras and args.workload in ("ensemble8", "uneven"):
+            result["energy_at_horizon"] = energy_horizon(args.workload, args.horizon_systems, args.horizon_steps, mode)
+            result["adjoint_over_forward"] = adjoint_over_forward(args.adjoint_steps)
+        achieved = flops * batch.n_sys * K / (med_ms * 1e-3) / 1e12
         per_sys = DRAM_BYTES_PER_SYSTEM_LAUNCH.get(args.workload)
         # a timed launch of the balanced schedule is several kernel launches,
         # each reading and writing every system's state once
-        traffic = None if per_sys is None else per_sys * batch.n_sys * (launches / R)
+        traffic = None if per_sys is None else per_sys * batch.n_sys * launches
         result["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                               "frac": achieved / peak, "traffic": traffic,
                               "traffic_note": "DRAM bytes per timed launch: the per-system bytes of one ncu capture "

@@ -1,0 +1,186 @@
+"""GPU: the FAST build -- the arithmetic every benchmark line times -- pinned
+against the oracle on each benchmarked workload shape at its own size.
+
+* uneven ensembles (2-10 bodies, 20 % circumbinary binaries whose host may
+  sit at index 1, each effect on with p = 0.7, the autotuned lane mapping):
+  <= 1e-12 relative after one step, <= 1e-9 after 1e4 steps in r, v and L;
+* the 8-body ensemble at its configured horizon of 1e5 steps: relative
+  deviation of the barycentric Newtonian energy from the oracle's own
+  trajectory <= 1e-10, states <= 1e-9;
+* the many-body engine at 1024 bodies for 1e3 steps: <= 1e-9;
+* the many-body engine's Roche check on a pair of equal masses and unequal
+  radii, where the reference's table is not symmetric
+  (src/particles/universe.rs:176-196).
+
+A trajectory whose own sensitivity makes 1e-9 unreachable -- chaotic
+systems, where the oracle moved by 1e-15 of its initial positions ends more
+than 1e-11 away from itself -- is held to 1e3 times that sensitivity
+instead, and the number of such systems is bounded; the energy bound holds
+for every system.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import posidonius_gb300 as pg
+from oracle.case_json import stack
+from posidonius_gb300 import ensemble as E, layout as L
+
+from parity import max_rel_error
+
+pytestmark = pytest.mark.gpu
+
+TOL_STEP = 1e-12
+TOL_LONG = 1e-9
+TOL_ENERGY = 1e-10
+CHAOTIC = 1e-11      # the oracle's own divergence from a 1e-15 nudge above which a system counts as chaotic
+CHAOS_FACTOR = 1e3   # a chaotic system's FAST deviation in units of that divergence
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from posidonius_gb300 import build
+    build.build()
+    oracle.build()
+
+
+def _sub(st, s):
+    return {k: (v[s:s + 1] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in st.items()}
+
+
+def _per_system_errors(a, b):
+    return np.array([max_rel_error(_sub(a, s), _sub(b, s)) for s in range(a["sys_i64"].shape[0])])
+
+
+def _nudged(ens, rel=1e-15):
+    p = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in ens.items()}
+    p["body_f64"][:, :, L.POS] *= 1.0 + rel
+    return p
+
+
+def newtonian_energy(state, s):
+    """Barycentric Newtonian energy of system s: kinetic + pairwise potential."""
+    n = int(state["sys_i64"][s, L.SI_N])
+    bf = state["body_f64"][s, :n]
+    m, r, v = bf[:, L.BF_MASS], bf[:, L.POS], bf[:, L.VEL]
+    ek = 0.5 * np.sum(m * np.sum(v * v, axis=1))
+    ep = 0.0
+    for i in range(n):
+        d = np.linalg.norm(r[i + 1:] - r[i], axis=1)
+        ep -= E.G * m[i] * np.sum(m[i + 1:] / d)
+    return ek + ep
+
+
+def _check_long(got, ref, sens, label):
+    err = _per_system_errors(got, ref)
+    chaotic = sens > CHAOTIC
+    bound = np.where(chaotic, np.maximum(TOL_LONG, CHAOS_FACTOR * sens), TOL_LONG)
+    bad = np.nonzero(err > bound)[0]
+    assert len(bad) == 0, (label, bad[:8], err[bad][:8], sens[bad][:8])
+    # chaos is the exception, not the rule
+    assert chaotic.mean() <= 0.05, (label, chaotic.sum())
+    return err, chaotic
+
+
+def test_uneven_fast_one_step_autotuned():
+    ens = E.workload_uneven(512, seed=41)
+    hosts = ens["sys_i64"][:, L.SI_HOST]
+    assert (hosts != 0).any()                      # binaries whose host is not body 0
+    assert len(np.unique(ens["sys_i64"][:, L.SI_N])) == 9
+    b = pg.Batch(ens, mode=pg.FAST)
+    b.initialize_physical_values()
+    choice = b.autotune(probe_steps=5)
+    assert set(choice) == set(int(n) for n in ens["sys_i64"][:, L.SI_N])
+    b.iterate(1)
+    ref, _, _ = oracle.run(ens, max_steps=1, init_physical=True, nthreads=8)
+    err = _per_system_errors(b.get_state(), ref)
+    assert err.max() <= TOL_STEP, (np.argmax(err), err.max())
+
+
+def test_uneven_fast_1e4_steps_autotuned():
+    ens = E.workload_uneven(256, seed=23)
+    b = pg.Batch(ens, mode=pg.FAST)
+    b.initialize_physical_values()
+    b.autotune(probe_steps=5)
+    b.iterate(10000, 2500)
+    got = b.get_state()
+    ref, steps, _ = oracle.run(ens, max_steps=10000, init_physical=True, nthreads=16)
+    ref2, _, _ = oracle.run(_nudged(ens), max_steps=10000, init_physical=True, nthreads=16)
+    for f in (L.SI_STATUS, L.SI_ITERATION):
+        assert np.array_equal(got["sys_i64"][:, f], ref["sys_i64"][:, f]), f
+    sens = _per_system_errors(ref2, ref)
+    _check_long(got, ref, sens, "uneven 1e4")
+    live = (ref["sys_i64"][:, L.SI_STATUS] & L.SYS_FATAL_MASK) == 0
+    de = [abs(newtonian_energy(got, s) - newtonian_energy(ref, s)) / abs(newtonian_energy(ref, s))
+          for s in np.nonzero(live)[0]]
+    assert max(de) <= TOL_ENERGY, max(de)
+
+
+def test_ensemble8_fast_at_its_1e5_step_horizon():
+    """The 8-body ensemble over the 1e5 steps it is configured for (800 d)."""
+    ens = E.workload_ensemble8(64, seed=31)
+    b = pg.Batch(ens, mode=pg.FAST)
+    b.initialize_physical_values()
+    b.iterate(100000, 25000)
+    got = b.get_state()
+    assert np.all(got["sys_i64"][:, L.SI_ITERATION] == 100000)
+    ref, _, _ = oracle.run(ens, max_steps=100000, init_physical=True, nthreads=16)
+    de = np.array([abs(newtonian_energy(got, s) - newtonian_energy(ref, s)) / abs(newtonian_energy(ref, s))
+                   for s in range(64)])
+    assert de.max() <= TOL_ENERGY, (np.argmax(de), de.max())
+    ref2, _, _ = oracle.run(_nudged(ens), max_steps=100000, init_physical=True, nthreads=16)
+    sens = _per_system_errors(ref2, ref)
+    _check_long(got, ref, sens, "ensemble8 1e5")
+
+
+def test_many_body_engine_1024_bodies_1e3_steps():
+    case = E.workload_large(1021, seed=3)
+    mb = pg.ManyBody(case)
+    mb.initialize_physical_values()
+    assert mb.iterate(1000) == L.OK
+    got = mb.get_state()
+    mb.close()
+    ref, steps, _ = oracle.run(stack([case]), max_steps=1000, init_physical=True)
+    assert steps[0] == 1000
+    one = {k: (v[0] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ref.items()}
+    assert got["sys_i64"][L.SI_ITERATION] == 1000
+    assert max_rel_error(got, one) <= TOL_LONG
+
+
+def _equal_mass_close_pair(case, i, j, sep_in_ri):
+    """Bodies i < j get equal masses, body j a tenth of body i's radius, and
+    body j sits sep_in_ri radii of body i away, moving with it: inside the
+    Roche radius of row i (R_i / 0.462), outside that of row j and outside
+    the sum of the radii."""
+    bf = case["body_f64"]
+    bf[j, L.BF_MASS] = bf[i, L.BF_MASS]
+    bf[j, L.BF_MASS_G] = bf[i, L.BF_MASS_G]
+    bf[j, L.BF_RADIUS] = 0.1 * bf[i, L.BF_RADIUS]
+    ri = bf[i, L.BF_RADIUS]
+    bf[j, L.POS] = bf[i, L.POS] + np.array([sep_in_ri * ri, 0.0, 0.0])
+    bf[j, L.VEL] = bf[i, L.VEL]
+    return case
+
+
+def test_many_body_engine_roche_row_of_the_lower_index():
+    case = E.workload_large(29, seed=5)
+    n = case["n"]
+    i, j = 7, 11
+    # 1.5 R_i: beyond R_i + R_j = 1.1 R_i, inside R_i / 0.462 = 2.16 R_i,
+    # outside R_j / 0.462 = 0.22 R_i
+    _equal_mass_close_pair(case, i, j, 1.5)
+    ref, _, _ = oracle.run(stack([case]), max_steps=5, init_physical=True)
+    assert int(ref["sys_i64"][0, L.SI_STATUS]) & L.SYS_FATAL_MASK == L.SYS_ROCHE
+    rp = int(ref["sys_i64"][0, L.SI_FAIL_PAIR])
+    assert (rp // 1024, rp % 1024) == (i, j)
+    mb = pg.ManyBody(case)
+    mb.initialize_physical_values()
+    with pytest.raises(pg.PosiError) as e:
+        mb.iterate(5)
+    assert e.value.status == L.ERR_PHYSICS
+    st = mb.get_state()
+    mb.close()
+    assert int(st["sys_i64"][L.SI_STATUS]) & L.SYS_FATAL_MASK == L.SYS_ROCHE
+    pair = int(st["sys_i64"][L.SI_FAIL_PAIR])
+    assert (pair // n, pair % n) == (i, j)
+    assert int(st["sys_i64"][L.SI_FAIL_STEP]) == int(ref["sys_i64"][0, L.SI_FAIL_STEP])
