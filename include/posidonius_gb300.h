@@ -227,8 +227,10 @@ int posi_read_case_ias15(const char* path, double* body_ias);
 
 /* ---- single system (the drop-in path: one system, one launch per step) -- */
 
-/* src/integrator/output.rs:178-241 restore_snapshot + deserialize_json_snapshot:
- * read a WHFast JSON case (or JSON recovery snapshot). */
+/* src/integrator/output.rs:178-279 restore_snapshot + deserialize_json_snapshot
+ * / deserialize_bin_snapshot: read a WHFast or Ias15 case or recovery
+ * snapshot -- JSON when the path's extension is "json", bincode otherwise
+ * (WHFast tried first, then Ias15), as the reference decides. */
 posi_handle* posi_universe_from_json(const char* path, int mode, int* status);
 
 /* src/particles/universe.rs:73-175 Universe::new + src/integrator/whfast.rs:143-165
@@ -297,9 +299,15 @@ int posi_close_history(posi_handle* h);
 /* src/integrator/whfast.rs:307-316 + src/integrator/output.rs:28-54
  * write_recovery_snapshot: set last_recovery_snapshot_time, flush the history,
  * rename an existing file to <stem>.<YYYYMMDD>T<AM|PM>.bin and write the
- * WHFast case document with the current state (JSON paths; the handle must
- * come from posi_universe_from_json). */
+ * case document with the current state: pretty JSON for a ".json" path,
+ * bincode (bincode 1.3 layout of the WHFast / Ias15 struct) for any other
+ * (the handle must come from posi_universe_from_json). */
 int posi_write_recovery_snapshot(posi_handle* h, const char* path);
+
+/* src/integrator/output.rs:43-51, 186-191: convert a case or recovery
+ * snapshot between its JSON and bincode forms, each path's form chosen by
+ * its extension as the reference chooses it (no device needed). */
+int posi_convert_snapshot(const char* src, const char* dst);
 
 /* ---- batched ensembles (many independent systems, one persistent kernel) -- */
 

@@ -61,6 +61,7 @@ SIGNATURES = {
     "posi_open_history": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int64]),
     "posi_close_history": (ctypes.c_int, [_vp]),
     "posi_write_recovery_snapshot": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "posi_convert_snapshot": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p]),
     "posi_adjoint_create": (_vp, [_vp, ctypes.c_int64, ctypes.c_int64, _intp]),
     "posi_adjoint_destroy": (None, [_vp]),
     "posi_adjoint_forward": (ctypes.c_int, [_vp]),

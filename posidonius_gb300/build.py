@@ -29,6 +29,7 @@ UNITS = [
     ("case_reader.cpp", ["-x", "cu", "-fmad=false"]),
     ("diagnostics.cu", ["-fmad=true"]),
     ("snapshot.cpp", ["-x", "cu", "-fmad=false"]),
+    ("bincode.cpp", ["-x", "cu", "-fmad=false"]),
     ("adjoint.cu", ["-fmad=true"]),
     ("large.cu", ["-fmad=true"]),
 ]

@@ -1,10 +1,12 @@
 // posi_cli.cpp -- the `posidonius` command (src/main.rs), over the C ABI.
 //
-//   posidonius start <case.json> <recovery_snapshot.json> <history.bin> [-l seconds] [-s]
-//   posidonius resume <recovery_snapshot.json> <history.bin> [-l seconds] [-s]
+//   posidonius start <case.json> <recovery_snapshot.bin|.json> <history.bin> [-l seconds] [-s]
+//   posidonius resume <recovery_snapshot.bin|.json> <history.bin> [-l seconds] [-s]
 //              [--historic-snapshot-period days] [--recovery-snapshot-period days] [--time-limit days]
 //
-// Both take `--mode exact|fast` (default exact: results bit-identical to the
+// A snapshot path ending in ".json" is JSON, any other bincode, as in the
+// reference (src/integrator/output.rs:43-51, 186-191).  Both take
+// `--mode exact|fast` (default exact: results bit-identical to the
 // reference; fast: contracted arithmetic, see posi_mode) and `--device k`.
 // Messages, the refusal to overwrite files on start, the history truncation
 // on resume and the snapshot schedule follow src/main.rs:10-202: without an

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/posidonius_gb300.h"
+#include "bincode.hpp"
 #include "case_reader.hpp"
 #include "json.hpp"
 #include "kernels.h"
@@ -264,7 +265,13 @@ int build_buckets(posi_batch* b, const int64_t* sys_i64, const std::map<int64_t,
 // Returns false when the bucket needs no schedule.
 bool build_schedule(int sms, int jobs, int64_t steps, std::vector<int32_t>& table, int& launches) {
     constexpr double kLoneSpeed = 1.75;
-    constexpr int64_t kSubLaunches = 12;   // about this many per launch of `steps` steps
+    // about this many sub-launches per launch of `steps` steps, at least 50
+    // steps each: a sub-launch costs tens of microseconds (state load and
+    // store, launch, the tail of its slowest slot), which a short launch
+    // does not win back -- 20 steps in 17 sub-launches took 230 us per step
+    // on the 8-body ensemble against 213 us for one plain launch
+    const int64_t kSubLaunches = std::min<int64_t>(12, steps / 50);
+    if (kSubLaunches < 2) return false;
     const int per = posi::kSchedBlockThreads / 32;
     const int slots = sms * per;
     if (sms <= 0 || jobs <= slots / 2 || jobs >= slots) return false;
@@ -519,10 +526,19 @@ int load_case_file(const char* path, posi::FlatSystem& fs, posi::json::Value* do
     const std::string text = ss.str();
     posi::json::Value doc;
     std::string err;
-    posi::json::Parser parser(text.data(), text.size());
-    if (!parser.parse(doc, err)) {
-        g_last_error = "JSON: " + err;
-        return POSI_ERR_PARSE;
+    // src/integrator/output.rs:178-191: a path whose extension is not
+    // "json" holds a bincode snapshot
+    if (posi::is_bincode_path(path)) {
+        if (!posi::bincode_to_json(text, doc, err)) {
+            g_last_error = err;
+            return POSI_ERR_PARSE;
+        }
+    } else {
+        posi::json::Parser parser(text.data(), text.size());
+        if (!parser.parse(doc, err)) {
+            g_last_error = "JSON: " + err;
+            return POSI_ERR_PARSE;
+        }
     }
     int rc = posi::read_case(doc, fs, err);
     if (rc != POSI_OK) g_last_error = err;
@@ -907,11 +923,7 @@ int posi_write_recovery_snapshot(posi_handle* h, const char* path) {
     const size_t dot = p.find_last_of('.');
     const size_t slash = p.find_last_of('/');
     const bool has_ext = dot != std::string::npos && (slash == std::string::npos || dot > slash);
-    const std::string ext = has_ext ? p.substr(dot + 1) : "";
-    if (ext != "json") {
-        g_last_error = "only JSON recovery snapshots are written (bincode snapshots are not supported)";
-        return POSI_ERR_UNSUPPORTED;
-    }
+    const bool binary = posi::is_bincode_path(p);
     h->sf[POSI_SF_LAST_REC] = h->sf[POSI_SF_TIME];
     int rc = batch_set(h->b, nullptr, h->sf.data(), nullptr, nullptr);
     if (rc != POSI_OK) return rc;
@@ -944,13 +956,55 @@ int posi_write_recovery_snapshot(posi_handle* h, const char* path) {
         const std::string backup = (has_ext ? p.substr(0, dot) : p) + "." + stamp + (g.tm_hour < 12 ? "AM" : "PM") + ".bin";
         std::rename(path, backup.c_str());
     }
+    // src/integrator/output.rs:43-51: pretty JSON for a ".json" path,
+    // bincode otherwise
     std::string text;
-    posi::write_json(*h->doc, text);
+    if (binary) {
+        if (!posi::json_to_bincode(*h->doc, text, err)) {
+            g_last_error = err;
+            return POSI_ERR_PARSE;
+        }
+    } else {
+        posi::write_json(*h->doc, text);
+    }
     std::FILE* f = std::fopen(path, "wb");
     if (!f) { g_last_error = std::string("cannot write ") + path; return POSI_ERR_IO; }
     const size_t w = std::fwrite(text.data(), 1, text.size(), f);
     std::fclose(f);
     return w == text.size() ? POSI_OK : POSI_ERR_IO;
+}
+
+// Recovery snapshot conversion between the JSON and bincode forms (each
+// path's form by its extension, as the reference picks it).
+int posi_convert_snapshot(const char* src, const char* dst) {
+    if (!src || !dst) return POSI_ERR_ARG;
+    std::ifstream f(src, std::ios::binary);
+    if (!f) {
+        g_last_error = std::string("cannot open ") + src;
+        return POSI_ERR_IO;
+    }
+    std::stringstream ss;
+    ss << f.rdbuf();
+    const std::string text = ss.str();
+    posi::json::Value doc;
+    std::string err;
+    if (posi::is_bincode_path(src)) {
+        if (!posi::bincode_to_json(text, doc, err)) { g_last_error = err; return POSI_ERR_PARSE; }
+    } else {
+        posi::json::Parser parser(text.data(), text.size());
+        if (!parser.parse(doc, err)) { g_last_error = "JSON: " + err; return POSI_ERR_PARSE; }
+    }
+    std::string out;
+    if (posi::is_bincode_path(dst)) {
+        if (!posi::json_to_bincode(doc, out, err)) { g_last_error = err; return POSI_ERR_PARSE; }
+    } else {
+        posi::write_json(doc, out);
+    }
+    std::FILE* o = std::fopen(dst, "wb");
+    if (!o) { g_last_error = std::string("cannot write ") + dst; return POSI_ERR_IO; }
+    const size_t w = std::fwrite(out.data(), 1, out.size(), o);
+    std::fclose(o);
+    return w == out.size() ? POSI_OK : POSI_ERR_IO;
 }
 
 // ---- batched --------------------------------------------------------------

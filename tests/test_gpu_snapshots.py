@@ -19,7 +19,7 @@ import pytest
 import oracle
 import posidonius_gb300 as pg
 from oracle.case_json import load_case
-from posidonius_gb300 import build as B, layout as L
+from posidonius_gb300 import _lib, build as B, layout as L
 
 from golden_cases import case_dict
 from parity import bitwise_diffs, same_bits
@@ -186,3 +186,56 @@ def test_generated_case_document_drives_the_cli_and_the_oracle(tmp_path):
     ref, rsteps, _ = oracle.run(load_case(str(path)), max_steps=10**6, init_physical=True)
     assert rsteps[0] == steps
     assert bitwise_diffs(w.get_state(), ref) == []
+
+
+def test_cli_bincode_start_resume_as_documented(tmp_path):
+    """The reference's documented command lines (`posidonius start case.json
+    case.bin case_history.bin`, then `posidonius resume case.bin
+    case_history.bin`): bincode recovery snapshots, a resumed run that ends
+    with the same history bytes and the same final snapshot bytes as an
+    uninterrupted one, and a dated backup of the previous snapshot."""
+    name = "test_tides-enabled_tides"
+    full, _ = _case(tmp_path, name, hist_period=0.8, rec_period=4.0, time_limit=16.0, fname="full.json")
+    r = _cli("start", full, tmp_path / "full.bin", tmp_path / "full_history.bin", "-s")
+    assert r.returncode == 0, r.stdout + r.stderr
+    part, _ = _case(tmp_path, name, hist_period=0.8, rec_period=4.0, time_limit=8.0, fname="case.json")
+    r = _cli("start", part, tmp_path / "case.bin", tmp_path / "case_history.bin", "-s")
+    assert r.returncode == 0, r.stdout + r.stderr
+    backups = [f for f in os.listdir(tmp_path) if f.startswith("case.") and f.endswith(".bin") and "T" in f]
+    assert len(backups) == 1, backups
+    # the bincode snapshot reads back as the JSON document of the same state
+    lib = _lib.lib()
+    assert lib.posi_convert_snapshot(str(tmp_path / "case.bin").encode(), str(tmp_path / "case_rec.json").encode()) == L.OK
+    snap = json.loads((tmp_path / "case_rec.json").read_text())
+    assert 0 < snap["current_time"] < 8.0
+    r = _cli("resume", tmp_path / "case.bin", tmp_path / "case_history.bin", "--time-limit", 16, "-s")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Restored previous simulation" in r.stdout
+    assert (tmp_path / "case_history.bin").read_bytes() == (tmp_path / "full_history.bin").read_bytes()
+    # both runs wrote their last recovery snapshot at the same step, with the same state
+    for src, dst in (("case.bin", "a.json"), ("full.bin", "b.json")):
+        assert lib.posi_convert_snapshot(str(tmp_path / src).encode(), str(tmp_path / dst).encode()) == L.OK
+    a = json.loads((tmp_path / "a.json").read_text())
+    b = json.loads((tmp_path / "b.json").read_text())
+    assert a["current_iteration"] == b["current_iteration"]
+    assert a["universe"]["particles"] == b["universe"]["particles"]
+
+
+@pytest.mark.parametrize("mode", [pg.EXACT, pg.FAST])
+def test_bincode_resume_continues_bit_for_bit(tmp_path, mode):
+    """Through the library: a bincode recovery snapshot, restored, continues
+    bit for bit -- WHFast and IAS15 documents alike."""
+    for name in ("test_evolution-m_dwarf_baraffe2015", "test_integrator-ias15"):
+        path, _ = _case(tmp_path, name, hist_period=0.8, fname=name + ".json")
+        straight = pg.restore_snapshot(path, mode=mode)
+        straight.run(12)
+        w = pg.restore_snapshot(path, mode=mode)
+        w.run(5)
+        snap = tmp_path / (name + ".bin")
+        w.write_recovery_snapshot(snap)
+        w.close()
+        resumed = pg.restore_snapshot(snap, mode=mode)
+        resumed.run(7)
+        a, b = resumed.get_state(), straight.get_state()
+        b["sys_f64"][L.SF_LAST_REC] = a["sys_f64"][L.SF_LAST_REC]
+        assert bitwise_diffs(a, b) == [], name
