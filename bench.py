@@ -53,7 +53,7 @@ def parse():
                    help="large workload: democratic heliocentric or Jacobi coordinates")
     p.add_argument("--grad-steps", type=int, default=10000, help="gradient workload: WHFast steps")
     p.add_argument("--checkpoint-every", type=int, default=100, help="gradient workload: checkpoint interval")
-    p.add_argument("--fd-systems", type=int, default=32, help="gradient workload: systems checked by differences")
+    p.add_argument("--fd-systems", type=int, default=32, help="gradient workload: systems checked against the exact derivatives of the oracle")
     p.add_argument("--no-autotune", action="store_true", help="smallest lane group per system, no tuning")
     p.add_argument("--n-systems", type=int, default=None)
     p.add_argument("--launches", type=int, default=10, help="timed launches (L2 flushed before each)")
@@ -478,63 +478,72 @@ def run_gradient(args):
     plain_fwd_ms, _ = b.last_timing()
     b.close()
     value = S * K / ((fwd_ms + bwd_ms) * 1e-3)
-    # checks on a sample of systems
-    idx = np.linspace(0, S - 1, min(args.fd_systems, S)).astype(np.int64)
-    sub = {k: (v[idx] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
-    sub["n_sys"] = len(idx)
-    args_fd = (sub, el[idx], sig[idx], k2[idx], ms[idx], moi[idx], ss[idx], K)
-    _, _, fe1 = A.finite_difference_gradient(*args_fd, rel_step=1e-6)
-    _, _, fe2 = A.finite_difference_gradient(*args_fd, rel_step=1e-5)
-    keep = flags[idx] == 0
-    checks = {"elements_vs_gpu_differences": _fd_agreement(g_el[idx][keep], fe1[keep], fe2[keep])}
-    # a horizon short of the systems' sensitivity growth, where the
-    # difference quotients are themselves accurate
-    ks = min(K, 1000)
-    _, _, _, gs_el, _, fls = A.adjoint_gradient(sub, el[idx], sig[idx], k2[idx], ms[idx], moi[idx], ss[idx], ks,
-                                                every)
-    args_s = (sub, el[idx], sig[idx], k2[idx], ms[idx], moi[idx], ss[idx], ks)
-    _, _, fs_e1 = A.finite_difference_gradient(*args_s, rel_step=1e-6)
-    _, _, fs_e2 = A.finite_difference_gradient(*args_s, rel_step=1e-5)
-    ks_keep = fls == 0
-    checks[f"elements_vs_gpu_differences_{ks}_steps"] = _fd_agreement(gs_el[ks_keep], fs_e1[ks_keep],
-                                                                      fs_e2[ks_keep])
-    # the CPU restatement of the reference as the difference engine
+    # checks on a sample of systems: the adjoint against the exact
+    # derivatives of the oracle (its dual-number build), per system, in the
+    # max norm of each parameter group; chaotic systems (the oracle's own
+    # loss moved by more than 1e-9 by a 1e-13 nudge of the mean anomalies)
+    # are also checked at 1e3 steps, inside their predictability horizon
     import oracle
     oracle.build()
+    idx = np.linspace(0, S - 1, min(args.fd_systems, S)).astype(np.int64)
+
+    def sub_of(ix):
+        d = {k: (v[ix] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
+        d["n_sys"] = len(ix)
+        return d
+
+    def per_system(a, b):
+        a, b = (np.asarray(x).reshape(len(x), -1) for x in (a, b))
+        return np.abs(a - b).max(axis=1) / np.maximum(np.abs(b).max(axis=1), 1e-300)
 
     def oracle_runner(e, n):
         out, _, _ = oracle.run(e, max_steps=n, init_physical=True, nthreads=os.cpu_count() or 1)
         return out["body_f64"]
 
-    _, _, fo1 = A.finite_difference_gradient(*args_fd, rel_step=1e-6, runner=oracle_runner)
-    _, _, fo2 = A.finite_difference_gradient(*args_fd, rel_step=1e-5, runner=oracle_runner)
-    checks["elements_vs_cpu_restatement_differences"] = _fd_agreement(g_el[idx][keep], fo1[keep], fo2[keep])
-    # tidal parameters: amplified (same code path) so that differences resolve them
-    amp = dict(ens)
-    amp["body_f64"] = ens["body_f64"].copy()
-    amp["body_f64"][:, :, L.BF_SIGMA] *= 5e7
-    amp["body_f64"][:, :, L.BF_K2] *= 1e6
-    sig_a, k2_a = amp["body_f64"][:, :, L.BF_SIGMA].copy(), amp["body_f64"][:, :, L.BF_K2].copy()
-    sub_a = {k: (v[idx] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in amp.items()}
-    sub_a["n_sys"] = len(idx)
-    ka = min(K, 300)
-    _, ga_sig, ga_k2, _, _, fla = A.adjoint_gradient(sub_a, el[idx], sig_a[idx], k2_a[idx], ms[idx], moi[idx],
-                                                     ss[idx], ka, every)
-    args_a = (sub_a, el[idx], sig_a[idx], k2_a[idx], ms[idx], moi[idx], ss[idx], ka)
-    fs1, fk1, _ = A.finite_difference_gradient(*args_a, rel_step_tidal=1e-2)
-    fs2, fk2, _ = A.finite_difference_gradient(*args_a, rel_step_tidal=1e-3)
-    ka_keep = fla == 0
-    # as d loss / d ln(parameter): the bodies' dissipation factors span orders of magnitude
-    sa, kk = sig_a[idx][ka_keep], k2_a[idx][ka_keep]
-    checks["sigma_amplified_vs_gpu_differences"] = _fd_agreement(ga_sig[ka_keep] * sa, fs1[ka_keep] * sa,
-                                                                 fs2[ka_keep] * sa)
-    checks["k2_amplified_vs_gpu_differences"] = _fd_agreement(ga_k2[ka_keep] * kk, fk1[ka_keep] * kk,
-                                                              fk2[ka_keep] * kk)
-    checks["note"] = ("errors per system, in the max norm of its gradient, and per component where the two "
-                      "difference quotients agree to 1 %; elements: relative steps 1e-6 / 1e-5 at "
-                      f"physical parameters over {K} and over {ks} steps; sigma x 5e7 and k2 x 1e6 over {ka} steps, relative "
-                      "steps 1e-2 / 1e-3 (at physical values their effect on the loss is below its rounding level); "
-                      "fd noise = change of the difference quotient between the two steps")
+    def vs_dual(ix, ksteps, adj=None):
+        sub = sub_of(ix)
+        args_ = (sub, el[ix], sig[ix], k2[ix], ms[ix], moi[ix], ss[ix], ksteps)
+        if adj is None:
+            _, a_sig, a_k2, a_el, _, a_fl = A.adjoint_gradient(*args_, every)
+        else:
+            a_sig, a_k2, a_el, a_fl = adj
+        t0 = time.perf_counter()
+        _, d_sig, d_k2, d_el = A.oracle_dual_gradient(*args_)
+        dual_s = time.perf_counter() - t0
+        l1 = A.loss_of_parameters(*args_, runner=oracle_runner)
+        el2 = el[ix].copy()
+        el2[..., 5] += 1e-13
+        l2 = A.loss_of_parameters(sub, el2, sig[ix], k2[ix], ms[ix], moi[ix], ss[ix], ksteps, runner=oracle_runner)
+        sens = np.abs(l2 - l1) / np.abs(l1)
+        err = np.maximum.reduce([per_system(a_el, d_el), per_system(a_sig * sig[ix], d_sig * sig[ix]),
+                                 per_system(a_k2 * k2[ix], d_k2 * k2[ix])])
+        regular = (sens <= 1e-9) & (a_fl == 0)
+        return err, regular, a_fl, dual_s, sens
+
+    err, regular, fl, dual_s, sens = vs_dual(idx, K, (g_sig[idx], g_k2[idx], g_el[idx], flags[idx]))
+    checks = {f"vs_oracle_dual_{K}_steps": {
+        "systems": int(len(idx)), "median_rel_err": float(np.median(err)),
+        "frac_within_1e-6": float(np.mean(err <= 1e-6)),
+        "predictable_systems": int(regular.sum()),
+        "predictable_frac_within_1e-6": float(np.mean(err[regular] <= 1e-6)) if regular.any() else None,
+        "predictable_max_rel_err": float(err[regular].max()) if regular.any() else None,
+        "chaotic_systems": int((~regular).sum()), "systems_flagged": int((fl != 0).sum()),
+        "dual_oracle_s": dual_s}}
+    rest = idx[~regular]
+    if len(rest):
+        ks = min(K, 1000)
+        err2, reg2, fl2, _, sens2 = vs_dual(rest, ks)
+        ok2 = fl2 == 0
+        checks[f"chaotic_systems_at_{ks}_steps"] = {
+            "systems": int(len(rest)), "flagged": int((~ok2).sum()),
+            "max_rel_err": float(err2[ok2].max()) if ok2.any() else None,
+            "frac_within_1e-6": float(np.mean(err2[ok2] <= 1e-6)) if ok2.any() else None,
+            "max_oracle_sensitivity": float(sens2.max())}
+    checks["note"] = ("relative error per system in the max norm of each parameter group (6 elements per planet; "
+                      "sigma and k2 as d loss / d ln p), every parameter at its physical value, against forward-mode "
+                      "dual-number derivatives of the oracle's reference-order arithmetic (no step size, no "
+                      "difference noise); predictable = the oracle's own loss moves by <= 1e-9 under a 1e-13 "
+                      "nudge of the mean anomalies over the run")
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": min(K, 2 * every),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",

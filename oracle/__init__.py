@@ -18,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 LIB_FLOPS = os.path.join(BUILD, "liboracle_flops.so")
+LIB_DUAL = os.path.join(BUILD, "liboracle_dual.so")
 
 ITERATE, GRAVITY, ADDITIONAL_EFFECTS, INITIALIZE = 0, 1, 2, 3
 
@@ -33,8 +34,8 @@ def build(force=False):
 _libs = {}
 
 
-def _lib(flops=False):
-    path = LIB_FLOPS if flops else LIB
+def _lib(flops=False, dual=False):
+    path = LIB_FLOPS if flops else LIB_DUAL if dual else LIB
     if path not in _libs:
         if not os.path.exists(path):
             build()
@@ -51,6 +52,9 @@ def _lib(flops=False):
         lib.oracle_constant.restype = ctypes.c_double
         if flops:
             lib.oracle_flops.argtypes = [i64p, ctypes.c_int]
+        if dual:
+            lib.oracle_dual_io.argtypes = [f64p, f64p]
+            lib.oracle_dual_io.restype = ctypes.c_int
         _libs[path] = lib
     return _libs[path]
 
@@ -90,10 +94,11 @@ def run_with_history(case, max_steps, init_physical=False, max_records=100000):
     return out + (buf[:k].reshape(k // n, n, 20),)
 
 
-def run(ens, op=ITERATE, max_steps=0, init_physical=False, arg=0, t_arg=0.0, nthreads=1, flops=False):
+def run(ens, op=ITERATE, max_steps=0, init_physical=False, arg=0, t_arg=0.0, nthreads=1, flops=False,
+        _dual_lib=None):
     """Run `op` in place on a copy of the ensemble; returns (ensemble, steps_done, result[, flops])."""
     ens = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in as_ensemble(ens).items()}
-    lib = _lib(flops)
+    lib = _dual_lib or _lib(flops)
     ns, nmax = ens["n_sys"], ens["nmax"]
     if "body_ias" not in ens:
         ens["body_ias"] = np.zeros((ns, nmax, L.IAS_COUNT))
@@ -120,3 +125,31 @@ def run(ens, op=ITERATE, max_steps=0, init_physical=False, arg=0, t_arg=0.0, nth
 
 def constant(which):
     return _lib().oracle_constant(which)
+
+
+def dual_directions():
+    """Directional derivatives every value of the dual build carries."""
+    return _lib(dual=True).oracle_dual_io(None, None)
+
+
+def run_dual(ens, seed, max_steps, init_physical=False, nthreads=1):
+    """ITERATE with forward-mode dual numbers: the exact derivatives of the
+    oracle's computed map (its operation order, its branches) along the
+    seeded directions.  seed [n_sys, nmax, BF_COUNT, ND]: derivatives of the
+    inputs (position, velocity, spin angular momentum, spin, dissipation
+    factor, Love number of each body) along each direction.  Returns
+    (ensemble, steps_done, result, tangents [n_sys, nmax, BF_COUNT, ND]) --
+    tangents of the final position, velocity, spin angular momentum and
+    spin (other fields zero)."""
+    lib = _lib(dual=True)
+    ens = as_ensemble(ens)
+    nd = lib.oracle_dual_io(None, None)
+    shape = (int(ens["n_sys"]), int(ens["nmax"]), L.BF_COUNT, nd)
+    seed = np.ascontiguousarray(np.broadcast_to(seed, shape), dtype=np.float64)
+    out = np.zeros(shape, dtype=np.float64)
+    lib.oracle_dual_io(_p(seed, ctypes.c_double), _p(out, ctypes.c_double))
+    try:
+        res = run(ens, max_steps=max_steps, init_physical=init_physical, nthreads=nthreads, _dual_lib=lib)
+    finally:
+        lib.oracle_dual_io(None, None)
+    return res + (out,)

@@ -22,6 +22,12 @@
 //
 // Built with -DORACLE_COUNT_FLOPS the same code counts every FP64 operation
 // (+ - * / sqrt each count 1), which gives the algorithmic flops per step.
+// Built with -DORACLE_DUAL every value carries ORACLE_ND directional
+// derivatives (forward-mode dual numbers): the exact derivatives of the
+// computed map -- the same operation order, branches taken on the values --
+// with respect to the seeded inputs (oracle_dual_io), with no step size and
+// no difference noise.  Terms the reference evaluates through powf / exp
+// (Roche radii, the dynamical tide, the disk) carry no derivative there.
 
 #include <algorithm>
 #include <atomic>
@@ -67,6 +73,64 @@ static inline real rabs(real a) { return real(std::fabs(a.v)); }
 static inline real rfloor(real a) { return real(std::floor(a.v)); }
 static inline bool risnan(real a) { return std::isnan(a.v); }
 static inline double dv(real a) { return a.v; }
+#elif defined(ORACLE_DUAL)
+#ifndef ORACLE_ND
+#define ORACLE_ND 26
+#endif
+constexpr int ND = ORACLE_ND;
+struct real {
+    double v;
+    double d[ND];
+    real() : v(0.) { for (int k = 0; k < ND; ++k) d[k] = 0.; }
+    real(double x) : v(x) { for (int k = 0; k < ND; ++k) d[k] = 0.; }
+    explicit operator double() const { return v; }
+};
+static inline real operator+(const real& a, const real& b) {
+    real r(a.v + b.v);
+    for (int k = 0; k < ND; ++k) r.d[k] = a.d[k] + b.d[k];
+    return r;
+}
+static inline real operator-(const real& a, const real& b) {
+    real r(a.v - b.v);
+    for (int k = 0; k < ND; ++k) r.d[k] = a.d[k] - b.d[k];
+    return r;
+}
+static inline real operator*(const real& a, const real& b) {
+    real r(a.v * b.v);
+    for (int k = 0; k < ND; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+    return r;
+}
+static inline real operator/(const real& a, const real& b) {
+    real r(a.v / b.v);
+    const double ib = 1. / b.v;
+    for (int k = 0; k < ND; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) * ib;
+    return r;
+}
+static inline real operator-(const real& a) {
+    real r(-a.v);
+    for (int k = 0; k < ND; ++k) r.d[k] = -a.d[k];
+    return r;
+}
+static inline real& operator+=(real& a, const real& b) { a = a + b; return a; }
+static inline real& operator-=(real& a, const real& b) { a = a - b; return a; }
+static inline real& operator*=(real& a, const real& b) { a = a * b; return a; }
+static inline real& operator/=(real& a, const real& b) { a = a / b; return a; }
+static inline bool operator<(const real& a, const real& b) { return a.v < b.v; }
+static inline bool operator>(const real& a, const real& b) { return a.v > b.v; }
+static inline bool operator<=(const real& a, const real& b) { return a.v <= b.v; }
+static inline bool operator>=(const real& a, const real& b) { return a.v >= b.v; }
+static inline bool operator==(const real& a, const real& b) { return a.v == b.v; }
+static inline bool operator!=(const real& a, const real& b) { return a.v != b.v; }
+static inline real rsqrt_(const real& a) {
+    real r(std::sqrt(a.v));
+    const double h = r.v > 0. ? 0.5 / r.v : 0.;
+    for (int k = 0; k < ND; ++k) r.d[k] = a.d[k] * h;
+    return r;
+}
+static inline real rabs(const real& a) { return a.v < 0. ? -a : a; }
+static inline real rfloor(const real& a) { return real(std::floor(a.v)); }
+static inline bool risnan(const real& a) { return std::isnan(a.v); }
+static inline double dv(const real& a) { return a.v; }
 #else
 typedef double real;
 static inline real rsqrt_(real a) { return std::sqrt(a); }
@@ -2098,6 +2162,55 @@ static void store(const Sim& s, int64_t nmax, int64_t* si, double* sf, int64_t* 
     }
 }
 
+#ifdef ORACLE_DUAL
+// Seeds and tangents of the dual build, [n_sys][nmax][POSI_BF_COUNT][ND]:
+// the derivatives of a body's inputs along each direction (position,
+// velocity, spin angular momentum and spin, dissipation factor, Love
+// number), and on return those of its final position, velocity, spin
+// angular momentum and spin.
+static const double* g_dual_seed = nullptr;
+static double* g_dual_out = nullptr;
+
+static void seed3(V3& x, const double* S, int f) {
+    for (int k = 0; k < ND; ++k) {
+        x.x.d[k] = S[(f + 0) * ND + k];
+        x.y.d[k] = S[(f + 1) * ND + k];
+        x.z.d[k] = S[(f + 2) * ND + k];
+    }
+}
+static void out3(const V3& x, double* T, int f) {
+    for (int k = 0; k < ND; ++k) {
+        T[(f + 0) * ND + k] = x.x.d[k];
+        T[(f + 1) * ND + k] = x.y.d[k];
+        T[(f + 2) * ND + k] = x.z.d[k];
+    }
+}
+static void dual_seed(Sim& s, const double* S) {
+    for (int b = 0; b < s.n; ++b) {
+        const double* B = S + (size_t)b * POSI_BF_COUNT * ND;
+        Particle& q = s.p[b];
+        seed3(q.r, B, POSI_BF_PX);
+        seed3(q.v, B, POSI_BF_VX);
+        seed3(q.L, B, POSI_BF_LX);
+        seed3(q.spin, B, POSI_BF_SX);
+        for (int k = 0; k < ND; ++k) {
+            q.tides.scaled_dissipation_factor.d[k] = B[POSI_BF_SIGMA * ND + k];
+            q.tides.love_number.d[k] = B[POSI_BF_K2 * ND + k];
+        }
+    }
+}
+static void dual_tangents(const Sim& s, double* T) {
+    for (int b = 0; b < s.n; ++b) {
+        double* B = T + (size_t)b * POSI_BF_COUNT * ND;
+        const Particle& q = s.p[b];
+        out3(q.r, B, POSI_BF_PX);
+        out3(q.v, B, POSI_BF_VX);
+        out3(q.L, B, POSI_BF_LX);
+        out3(q.spin, B, POSI_BF_SX);
+    }
+}
+#endif
+
 }  // namespace orc
 
 // ---------------------------------------------------------------------------
@@ -2134,6 +2247,9 @@ int oracle_run(int op, int64_t n_sys, int64_t nmax, int64_t* sys_i64, double* sy
             double* ro = roche ? roche + k * nmax * nmax : nullptr;
             double* ia = body_ias ? body_ias + k * nmax * POSI_IAS_COUNT : nullptr;
             orc::load(s, nmax, si, sf, bi, bf, tables, ro, ia);
+#ifdef ORACLE_DUAL
+            if (orc::g_dual_seed) orc::dual_seed(s, orc::g_dual_seed + (size_t)k * nmax * POSI_BF_COUNT * orc::ND);
+#endif
             int64_t done = 0, rc = POSI_OK;
             if (op == ORACLE_ITERATE) {
                 if (init_physical) rc = orc::initialize_physical_values(s);
@@ -2153,6 +2269,9 @@ int oracle_run(int op, int64_t n_sys, int64_t nmax, int64_t* sys_i64, double* sy
                 rc = orc::initialize_physical_values(s);
             }
             orc::store(s, nmax, si, sf, bi, bf, ro, ia);
+#ifdef ORACLE_DUAL
+            if (orc::g_dual_out) orc::dual_tangents(s, orc::g_dual_out + (size_t)k * nmax * POSI_BF_COUNT * orc::ND);
+#endif
             if (steps_done) steps_done[k] = done;
             if (result) result[k] = rc;
         }
@@ -2178,6 +2297,17 @@ void oracle_history(double* buf, int64_t capacity, int64_t* len) {
         orc::g_hist_len = 0;
     }
 }
+
+#ifdef ORACLE_DUAL
+// Seeds (inputs) and tangents (outputs) of the next oracle_run calls, both
+// [n_sys][nmax][POSI_BF_COUNT][directions] or NULL; returns the directions
+// every value carries.
+int oracle_dual_io(const double* seed, double* out) {
+    orc::g_dual_seed = seed;
+    orc::g_dual_out = out;
+    return orc::ND;
+}
+#endif
 
 #ifdef ORACLE_COUNT_FLOPS
 // Flop counters of the calling thread since the last reset: {all, divisions, square roots}.

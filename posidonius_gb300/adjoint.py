@@ -420,6 +420,65 @@ def finite_difference_gradient(ens, elements, sigma, k2, masses, moi, star_spin,
     return g[:, :nb], g[:, nb:2 * nb], g[:, 2 * nb:].reshape(S, npl, 6)
 
 
+def oracle_dual_gradient(ens, elements, sigma, k2, masses, moi, star_spin, n_steps, nthreads=None):
+    """The same per-system loss gradient with respect to (sigma, k2,
+    elements) from the oracle's dual-number build: the initial state's
+    derivatives with respect to the elements (torch Jacobian of
+    elements_to_state) and unit rates of every body's sigma and k2 seed
+    forward-mode derivatives through n_steps of the oracle's reference-order
+    arithmetic; the loss gradient at the final state (torch) then contracts
+    them.  Exact derivatives of the computed map, no step size: the
+    reference the adjoint is checked against.  Returns (loss [S], d/dsigma
+    [S, nb], d/dk2 [S, nb], d/delements [S, np, 6])."""
+    import os
+
+    import oracle
+    torch = _torch()
+    elements = np.asarray(elements, float)
+    masses, moi = np.asarray(masses, float), np.asarray(moi, float)
+    S, npl = elements.shape[0], elements.shape[1]
+    nb = npl + 1
+    nd = oracle.dual_directions()
+    if 2 * nb + 6 * npl > nd:
+        raise ValueError(f"{2 * nb + 6 * npl} directions needed, the dual build carries {nd}")
+    e0 = initial_ensemble(ens, elements, sigma, k2, masses, moi, star_spin)
+    nmax = int(e0["nmax"])
+    seed = np.zeros((S, nmax, L.BF_COUNT, nd))
+    for b in range(nb):
+        seed[:, b, L.BF_SIGMA, b] = 1.0
+        seed[:, b, L.BF_K2, nb + b] = 1.0
+    t = lambda x: torch.as_tensor(np.asarray(x), dtype=torch.float64)
+    for s in range(S):
+        ms, mi, ss = t(masses[s:s + 1]), t(moi[s:s + 1]), t(star_spin[s:s + 1])
+
+        def state_of(el):
+            r0, v0, L0 = elements_to_state(el[None], ms, mi, ss)
+            return torch.cat([r0[0], v0[0], L0[0]], dim=-1)   # [nb, 9]
+
+        J = torch.autograd.functional.jacobian(state_of, t(elements[s])).numpy()  # [nb, 9, npl, 6]
+        J = J.reshape(nb, 9, npl * 6)
+        cols = slice(2 * nb, 2 * nb + 6 * npl)
+        seed[s, :nb, L.POS, cols] = J[:, 0:3]
+        seed[s, :nb, L.VEL, cols] = J[:, 3:6]
+        seed[s, :nb, L.ANG, cols] = J[:, 6:9]
+        inv = np.where(moi[s] != 0, 1.0 / np.where(moi[s] != 0, moi[s], 1.0), 0.0)
+        seed[s, :nb, L.SPIN, cols] = J[:, 6:9] * inv[:, None, None]
+    res = oracle.run_dual(e0, seed, n_steps, init_physical=True, nthreads=nthreads or os.cpu_count() or 1)
+    fin, T = res[0]["body_f64"][:, :nb], res[3][:, :nb]
+    r, v, Ls = (t(fin[..., sl]).requires_grad_(True) for sl in (L.POS, L.VEL, L.ANG))
+    el = t(elements).requires_grad_(True)
+    a0 = el[..., 0]
+    spin0 = torch.linalg.norm(pseudo_synchronous_spin(el[..., 0], el[..., 1], el[..., 2], el[..., 4],
+                                                      t(masses)[:, :1], t(masses)[:, 1:]), dim=-1)
+    loss = tidal_loss(r, v, Ls, t(masses), t(moi), a0, spin0)
+    loss.sum().backward()
+    g = np.einsum("sbq,sbqk->sk", r.grad.numpy(), T[:, :, L.POS, :]) + \
+        np.einsum("sbq,sbqk->sk", v.grad.numpy(), T[:, :, L.VEL, :]) + \
+        np.einsum("sbq,sbqk->sk", Ls.grad.numpy(), T[:, :, L.ANG, :])
+    g_el = g[:, 2 * nb:2 * nb + 6 * npl].reshape(S, npl, 6) + el.grad.numpy()
+    return loss.detach().numpy(), g[:, :nb], g[:, nb:2 * nb], g_el
+
+
 def adjoint_gradient(ens, elements, sigma, k2, masses, moi, star_spin, n_steps, checkpoint_every=100,
                      device="cuda", mode=None):
     """Per-system loss and its gradient with respect to (sigma, k2, elements)

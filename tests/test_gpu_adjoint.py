@@ -1,91 +1,128 @@
-"""GPU: the adjoint of the WHFast + tides step against finite differences.
+"""GPU: the adjoint of the WHFast + tides step against the exact derivatives
+of the oracle.
 
 Gradients of the differentiation workload's loss (squared final
 eccentricities, relative semi-major-axis drifts, relative planetary spin-rate
 changes) with respect to every body's dissipation factor and Love number and
 every planet's six initial orbital elements, by the checkpointed adjoint
-(torch autograd around posi_adjoint_*), against central finite differences of
-the same loss integrated by the forward kernel (relative step 1e-6 for the
-orbital elements).  At physical values the dissipation factors and Love
-numbers change the loss of a short run by less than its rounding level, so
-their gradients are checked with both amplified (same code path) and a
-1e-3 relative step, over which the loss is linear in them.
+(torch autograd around posi_adjoint_*), against the oracle's dual-number
+build: forward-mode derivatives through the reference-order arithmetic, with
+no step size and no difference noise (tests/test_oracle_dual.py checks them
+against central differences of the plain oracle).  Every parameter is at
+its physical value; the bound is 1e-6 relative per system and parameter
+group (the dissipation factors and Love numbers as d loss / d ln p, since
+they span orders of magnitude), with no allowance for noise.
+
+Over 1e4 steps a system whose planets pass close to one another is chaotic:
+a 1e-13 nudge of its mean anomalies moves the oracle's own loss by 1e-7 or
+more, and no two arithmetics share its trajectory.  Such systems are
+identified by that sensitivity of the oracle itself and checked at 1e3
+steps, inside their predictability horizon.
 """
 import numpy as np
 import pytest
 
+import oracle
 import posidonius_gb300 as pg
 from posidonius_gb300 import adjoint as A, ensemble as E, layout as L
 
 pytestmark = pytest.mark.gpu
 
-# relative agreement with central differences where they resolve the derivative
-ADJ_FD_TOL = 1e-5
+ADJ_TOL = 1e-6
+CHAOTIC = 1e-9   # relative loss change of the oracle under a 1e-13 nudge of the mean anomalies
 
 
 @pytest.fixture(scope="module", autouse=True)
 def built():
     from posidonius_gb300 import build
     build.build()
+    oracle.build()
 
 
-def _check(adj, fd, fd2):
-    """Worst ratio over systems of max |adj - fd| / (ADJ_FD_TOL max |fd| +
-    3 max |fd - fd2|), the maxima over the system's gradient components: the
-    adjoint must agree with the difference quotient fd to ADJ_FD_TOL of the
-    system's gradient, up to the quotient's own error, estimated by its
-    change between two step sizes (truncation where the loss bends over the
-    step, rounding noise of the loss where the step is small).  Norms per
-    system, not per component: a component whose two quotients agree by
-    chance would otherwise get a bound below the quotient's real error."""
-    adj, fd, fd2 = (x.reshape(x.shape[0], -1) for x in (adj, fd, fd2))
-    err = np.abs(adj - fd).max(axis=1)
-    bound = ADJ_FD_TOL * np.abs(fd).max(axis=1) + 3.0 * np.abs(fd - fd2).max(axis=1) + 1e-300
-    return float((err / bound).max())
+def _per_system(a, b):
+    a, b = (np.asarray(x).reshape(len(x), -1) for x in (a, b))
+    return np.abs(a - b).max(axis=1) / np.maximum(np.abs(b).max(axis=1), 1e-300)
+
+
+def _errors(ens, el, sig, k2, ms, moi, ss, n_steps, every):
+    """Per-system relative errors (elements, d/d ln sigma, d/d ln k2) of the
+    adjoint against the dual oracle, the adjoint's flags and the losses."""
+    loss, g_sig, g_k2, g_el, _, flags = A.adjoint_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, every)
+    d_loss, d_sig, d_k2, d_el = A.oracle_dual_gradient(ens, el, sig, k2, ms, moi, ss, n_steps)
+    err = np.stack([_per_system(g_el, d_el), _per_system(g_sig * sig, d_sig * sig),
+                    _per_system(g_k2 * k2, d_k2 * k2)], axis=1)
+    return err, flags, loss, d_loss
+
+
+def _oracle_sensitivity(ens, el, sig, k2, ms, moi, ss, n_steps):
+    def runner(e, n):
+        out, _, _ = oracle.run(e, max_steps=n, init_physical=True, nthreads=16)
+        return out["body_f64"]
+    l1 = A.loss_of_parameters(ens, el, sig, k2, ms, moi, ss, n_steps, runner=runner)
+    el2 = el.copy()
+    el2[..., 5] += 1e-13
+    l2 = A.loss_of_parameters(ens, el2, sig, k2, ms, moi, ss, n_steps, runner=runner)
+    return np.abs(l2 - l1) / np.abs(l1)
+
+
+def _params(ens):
+    return ens["body_f64"][:, :, L.BF_SIGMA].copy(), ens["body_f64"][:, :, L.BF_K2].copy()
 
 
 @pytest.mark.parametrize("n_steps,every", [(120, 50), (400, 100)])
-def test_adjoint_elements_match_finite_differences(n_steps, every):
-    """Physical parameters: the orbital-element gradients (relative steps 1e-6
-    and 1e-5)."""
-    ens, el, ms, moi, ss = A.gradient_workload(4, seed=7)
-    sig = ens["body_f64"][:, :, L.BF_SIGMA].copy()
-    k2 = ens["body_f64"][:, :, L.BF_K2].copy()
-    loss, g_sig, g_k2, g_el, _, flags = A.adjoint_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, every)
+def test_adjoint_matches_oracle_derivatives(n_steps, every):
+    """Every parameter at its physical value, every system."""
+    ens, el, ms, moi, ss = A.gradient_workload(8, seed=7)
+    sig, k2 = _params(ens)
+    err, flags, loss, d_loss = _errors(ens, el, sig, k2, ms, moi, ss, n_steps, every)
     assert not flags.any()
-    _, _, f_el = A.finite_difference_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, rel_step=1e-6)
-    _, _, f_el2 = A.finite_difference_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, rel_step=1e-5)
-    ref = A.loss_of_parameters(ens, el, sig, k2, ms, moi, ss, n_steps)
-    assert np.allclose(loss, ref, rtol=1e-10, atol=0)
-    err = _check(g_el, f_el, f_el2)
-    assert err <= 1.0, (err, g_el, f_el, f_el2)
+    assert np.allclose(loss, d_loss, rtol=1e-10, atol=0)
+    assert err.max() <= ADJ_TOL, err
 
 
-def test_adjoint_tidal_parameters_match_finite_differences():
-    """Dissipation factors x 5e7 and Love numbers x 1e6: their effect on the
-    loss becomes large enough for central differences (relative steps 1e-2
-    and 1e-3; the loss is linear in them over that range) to resolve it; the
-    code path is the one the physical parameters take.  A system the forward
-    run froze (Roche limit) is flagged and left out."""
+def _workload_sample(n):
+    """n systems spread over the differentiation workload (1024 systems of a
+    star and three planets)."""
+    ens, el, ms, moi, ss = A.gradient_workload(1024)
+    idx = np.linspace(0, 1023, n).astype(int)
+    ens = {k: (v[idx] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
+    ens["n_sys"] = n
+    return ens, el[idx], ms[idx], moi[idx], ss[idx]
+
+
+def test_adjoint_at_the_workloads_horizon():
+    """32 systems of the workload at its 1e4 steps (checkpoints every 100):
+    every system the oracle finds predictable over the run is within 1e-6,
+    and most are; the chaotic rest, at 1e3 steps, are within 1e-6 too."""
+    ens, el, ms, moi, ss = _workload_sample(32)
+    sig, k2 = _params(ens)
+    sens = _oracle_sensitivity(ens, el, sig, k2, ms, moi, ss, 10000)
+    regular = sens <= CHAOTIC
+    assert regular.mean() >= 0.6, regular.sum()
+    err, flags, _, _ = _errors(ens, el, sig, k2, ms, moi, ss, 10000, 100)
+    ok = regular & (flags == 0)
+    assert (err[ok] <= ADJ_TOL).all(), (np.nonzero(ok)[0], err[ok].max(axis=1))
+    rest = {k: (v[~ok] if isinstance(v, np.ndarray) and k != "tables" else v) for k, v in ens.items()}
+    rest["n_sys"] = int((~ok).sum())
+    if rest["n_sys"]:
+        short_sens = _oracle_sensitivity(rest, el[~ok], sig[~ok], k2[~ok], ms[~ok], moi[~ok], ss[~ok], 1000)
+        assert (short_sens <= CHAOTIC).all(), short_sens
+        err_s, flags_s, _, _ = _errors(rest, el[~ok], sig[~ok], k2[~ok], ms[~ok], moi[~ok], ss[~ok], 1000, 100)
+        assert flags_s.sum() <= A.FLAG_FROZEN      # at most one system frozen by a close encounter
+        assert err_s[flags_s == 0].max() <= ADJ_TOL, err_s
+
+
+def test_adjoint_flags_a_frozen_system():
+    """With dissipation factors x 5e7 and Love numbers x 1e6 one system of
+    this seed reaches its Roche limit: the forward run freezes it and the
+    adjoint flags it; the others match the oracle's derivatives."""
     ens, el, ms, moi, ss = A.gradient_workload(4, seed=11)
-    sig = ens["body_f64"][:, :, L.BF_SIGMA].copy() * 5e7
-    k2 = ens["body_f64"][:, :, L.BF_K2].copy() * 1e6
-    ens["body_f64"][:, :, L.BF_SIGMA] = sig
-    ens["body_f64"][:, :, L.BF_K2] = k2
-    n_steps, every = 300, 100
-    loss, g_sig, g_k2, g_el, _, flags = A.adjoint_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, every)
+    ens["body_f64"][:, :, L.BF_SIGMA] *= 5e7
+    ens["body_f64"][:, :, L.BF_K2] *= 1e6
+    sig, k2 = _params(ens)
+    err, flags, _, _ = _errors(ens, el, sig, k2, ms, moi, ss, 300, 100)
     assert flags[2] == A.FLAG_FROZEN and flags.sum() == A.FLAG_FROZEN
-    keep = flags == 0
-    f_sig, f_k2, _ = A.finite_difference_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, rel_step_tidal=1e-2)
-    f_sig2, f_k22, _ = A.finite_difference_gradient(ens, el, sig, k2, ms, moi, ss, n_steps, rel_step_tidal=1e-3)
-    # compared as d loss / d ln(parameter): the bodies' dissipation factors
-    # span five orders of magnitude, and a raw-unit norm would let the
-    # smallest one's (noise-dominated) component set every system's bound
-    s, k = sig[keep], k2[keep]
-    errs = {"sigma": _check(g_sig[keep] * s, f_sig[keep] * s, f_sig2[keep] * s),
-            "k2": _check(g_k2[keep] * k, f_k2[keep] * k, f_k22[keep] * k)}
-    assert max(errs.values()) <= 1.0, (errs, g_sig * sig, f_sig * sig, f_sig2 * sig, g_k2 * k2, f_k2 * k2,
-                                       f_k22 * k2)
+    assert err[flags == 0].max() <= ADJ_TOL, err
 
 
 def test_adjoint_of_identity_seed_is_consistent():
