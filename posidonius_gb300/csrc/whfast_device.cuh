@@ -2134,6 +2134,7 @@ struct Sys {
         double x, gs[4];
         double invperiod = 0., x_per_period = 0.;
         bool xpp_nan;
+#if POSI_EXACT
         if (beta > 0.) {
             const double sqrt_beta = sqrt(beta);
             invperiod = sqrt_beta * beta / (kTWO_PI * mass_g);
@@ -2149,13 +2150,48 @@ struct Sys {
             x = 0.;
             xpp_nan = true;
         }
+#else
+        // The period tests without their divisions (invperiod and
+        // x_per_period are formed only on the rare bisection path below):
+        // |dt| / P > 1 as |dt| sqrt(beta) beta > 2 pi GM, and the first
+        // Newton step's jump against 1 % of 2 pi / sqrt(beta) as
+        // |jump| sqrt(beta) > 0.02 pi.  The starting value is the series
+        // inversion of r0 X + eta0 G2(X) + zeta0 G3(X) = dt to fourth order
+        // in u = dt / r0 (G2 = X^2/2 - beta X^4/24, G3 = X^3/6 + ...): its
+        // error is O(u^5), about 1e-5 relative at 2 pi dt / P = 0.2, so the
+        // first Newton step already lands within 1e-8 and the loop stops
+        // after one more evaluation (the reference's second-order value
+        // needs three).
+        double sqrt_beta = 0.;
+        if (beta > 0.) {
+            sqrt_beta = sqrt(beta);
+            xpp_nan = false;
+            if (fabs(kdt) * sqrt_beta * beta > kTWO_PI * mass_g && tw == 0) {
+                status |= POSI_SYS_WARN_TIMESTEP;
+                isc[2] = 1;
+            }
+            const double u = kdt * r0i;
+            const double a2 = -0.5 * eta0 * r0i;
+            const double a3 = (0.5 * eta0 * eta0 * r0i - zeta0 * (1. / 6.)) * r0i;
+            const double a4 = -(eta0 * a3 + 0.5 * eta0 * a2 * a2 + 0.5 * zeta0 * a2 - eta0 * beta * (1. / 24.)) * r0i;
+            x = u * (1. + u * (a2 + u * (a3 + u * a4)));
+        } else {
+            x = 0.;
+            xpp_nan = true;
+        }
+#endif
         int converged = 0;
         double old_x = x;
         stiefel_gs3(beta, x, gs);
         double e = eta0 * gs[1] + zeta0 * gs[2];
         double ri = 1. / (r0 + e);
         x = ri * (x * e - eta0 * gs[2] - zeta0 * gs[3] + kdt);
-        if (!xpp_nan && fabs(x - old_x) > 0.01 * x_per_period) {
+#if POSI_EXACT
+        const bool jumped = !xpp_nan && fabs(x - old_x) > 0.01 * x_per_period;
+#else
+        const bool jumped = !xpp_nan && fabs(x - old_x) * sqrt_beta > 0.02 * kPI;
+#endif
+        if (jumped) {
             x = beta * kdt / mass_g;
             double prev_x[kNMAX_QUART + 1];
             for (int k = 0; k <= kNMAX_QUART; ++k) prev_x[k] = 0.;
@@ -2186,13 +2222,14 @@ struct Sys {
 #if POSI_EXACT
                 if (x == old_x || x == old_x2) { converged = 1; break; }
 #else
-                // quadratic convergence: a step below 1e-15 |x| leaves the
-                // next one below rounding, so stop one iteration earlier and
-                // move the G functions to the new root by their derivatives
-                // (dG_n/dx = G_(n-1), dG_0/dx = -beta G_1; second-order error
-                // about 1e-30): the drift stays a smooth function of x.
+                // quadratic convergence: after a step below 1e-10 |x| the
+                // root is off by the step's square times the contraction
+                // (below 1e-20 relative), so stop there and move the G
+                // functions to the new root by their derivatives (dG_n/dx =
+                // G_(n-1), dG_0/dx = -beta G_1; second-order error about the
+                // step's square): the drift stays a smooth function of x.
                 if (x == old_x || x == old_x2) { converged = 1; break; }
-                if (fabs(x - old_x) <= 1e-15 * fabs(x)) {
+                if (fabs(x - old_x) <= 1e-10 * fabs(x)) {
                     const double dx = x - old_x;
                     const double g0 = gs[0], g1 = gs[1], g2 = gs[2];
                     gs[0] = g0 - beta * g1 * dx;
@@ -2209,6 +2246,12 @@ struct Sys {
         }
         if (converged == 0) {
             double x_min, x_max;
+#if !POSI_EXACT
+            if (beta > 0.) {
+                invperiod = sqrt_beta * beta / (kTWO_PI * mass_g);
+                x_per_period = kTWO_PI / sqrt_beta;
+            }
+#endif
             if (beta > 0.) {
                 x_min = x_per_period * floor(kdt * invperiod);
                 x_max = x_min + x_per_period;
