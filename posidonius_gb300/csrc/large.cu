@@ -11,12 +11,13 @@
 struct posi_large {
     int64_t n = 0;
     int coords = POSI_DEMOCRATIC_HELIOCENTRIC;
-    int grid = 0, nchunk = 0, per_block = 0;
+    int grid = 0, ntile = 0, per_block = 0, per_block_tan = 32;
     double *d_bf = nullptr, *d_sf = nullptr, *d_roche = nullptr, *d_near2 = nullptr, *d_pos = nullptr,
            *d_gpart = nullptr,
            *d_bpart = nullptr, *d_tot = nullptr, *d_tan = nullptr, *d_dpos = nullptr;
     int64_t *d_bi = nullptr, *d_si = nullptr;
-    unsigned* d_bar = nullptr;
+    unsigned* d_bar = nullptr;   // [0..1] barrier of the grid, [2..3] of the body blocks
+    int* d_ctl = nullptr;
     int* d_err = nullptr;
     unsigned long long* d_bad = nullptr;
     cudaStream_t stream = nullptr;
@@ -30,7 +31,7 @@ void free_large(posi_large* L) {
     if (!L) return;
     cudaFree(L->d_bf); cudaFree(L->d_sf); cudaFree(L->d_roche); cudaFree(L->d_near2); cudaFree(L->d_pos);
     cudaFree(L->d_gpart);
-    cudaFree(L->d_bpart); cudaFree(L->d_tot); cudaFree(L->d_bi); cudaFree(L->d_si); cudaFree(L->d_bar); cudaFree(L->d_err);
+    cudaFree(L->d_bpart); cudaFree(L->d_tot); cudaFree(L->d_bi); cudaFree(L->d_si); cudaFree(L->d_bar); cudaFree(L->d_ctl); cudaFree(L->d_err);
     cudaFree(L->d_bad); cudaFree(L->d_tan); cudaFree(L->d_dpos);
     if (L->e0) cudaEventDestroy(L->e0);
     if (L->e1) cudaEventDestroy(L->e1);
@@ -103,9 +104,12 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
     if ((int64_t)L->grid * posi_many::kBlock < n)
         return fail(POSI_ERR_UNSUPPORTED, "too many bodies for one resident grid (" +
                                               std::to_string((int64_t)L->grid * posi_many::kBlock) + " at most)", L);
-    // slices of the pair loop: one thread per (body, slice), at least 16
-    // partners per slice
-    L->nchunk = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)L->grid * posi_many::kBlock) / n, n / 16));
+    // tiles of 32 bodies for the pair loop; bodies in the first blocks, 32
+    // per block (more only when the grid's blocks would not hold them): the
+    // tangent kernels need that layout (a warp per direction beside the
+    // primal warp), and the same one keeps the primal state of a tangent run
+    // the plain run's bit for bit (the reductions add block rows in order)
+    L->ntile = (int)((n + 31) / 32);
     {
         const int64_t need = (n + L->grid - 1) / L->grid;
         L->per_block = (int)std::min<int64_t>(posi_many::kBlock, std::max<int64_t>(32, (need + 31) / 32 * 32));
@@ -123,14 +127,14 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
         !ok(cudaMalloc(&L->d_roche, (size_t)n * n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_near2, (size_t)n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_pos, (size_t)3 * n * sizeof(double))) ||
-        !ok(cudaMalloc(&L->d_gpart, (size_t)L->nchunk * 3 * (1 + posi_many::kMaxTangents) * n * sizeof(double))) ||
-        !ok(cudaMalloc(&L->d_bpart, (size_t)L->grid * posi_many::BP_ROW * sizeof(double))) ||
+        !ok(cudaMalloc(&L->d_gpart, (size_t)L->ntile * 3 * (1 + posi_many::kMaxTangents) * n * sizeof(double))) ||
+        !ok(cudaMalloc(&L->d_bpart, (size_t)2 * L->grid * posi_many::BP_ROW * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_tot, posi_many::BP_ROW * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_tan, (size_t)posi_many::kMaxTangents * 12 * n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_dpos, (size_t)posi_many::kMaxTangents * 3 * n * sizeof(double))) ||
-        !ok(cudaMalloc(&L->d_bar, 2 * sizeof(unsigned))) || !ok(cudaMalloc(&L->d_err, sizeof(int))) ||
-        !ok(cudaMalloc(&L->d_bad, sizeof(unsigned long long))) ||
-        !ok(cudaMemset(L->d_bar, 0, 2 * sizeof(unsigned))) || !ok(cudaMemset(L->d_err, 0, sizeof(int))))
+        !ok(cudaMalloc(&L->d_bar, 4 * sizeof(unsigned))) || !ok(cudaMalloc(&L->d_err, sizeof(int))) ||
+        !ok(cudaMalloc(&L->d_ctl, sizeof(int))) || !ok(cudaMalloc(&L->d_bad, sizeof(unsigned long long))) ||
+        !ok(cudaMemset(L->d_bar, 0, 4 * sizeof(unsigned))) || !ok(cudaMemset(L->d_err, 0, sizeof(int))))
         return fail(POSI_ERR_CUDA, std::string("allocation failed"), L);
     int rc = posi_large_set_state(L, sys_i64, sys_f64, body_i64, body_f64);
     if (rc != POSI_OK) return fail(rc, "upload failed", L);
@@ -238,10 +242,17 @@ int run_large(posi_large* L, int64_t n_steps, const int32_t* seed_body, const in
     d.bf = L->d_bf; d.bi = L->d_bi; d.sf = L->d_sf; d.si = L->d_si; d.roche = L->d_roche;
     d.near2 = L->d_near2;
     d.pos = L->d_pos; d.gpart = L->d_gpart; d.bpart = L->d_bpart; d.tot = L->d_tot; d.bar = L->d_bar;
+    d.bbar = L->d_bar + 2;
+    d.ctl = L->d_ctl;
     d.err = L->d_err;
     d.bad = L->d_bad;
-    d.nchunk = L->nchunk;
-    d.per_block = L->per_block;
+    d.ntile = L->ntile;
+    d.per_block = NT > 0 ? L->per_block_tan : L->per_block;
+    d.nbb = (int)((L->n + d.per_block - 1) / d.per_block);
+    if (d.nbb > L->grid) {
+        posi::set_last_error("too many bodies for the resident grid");
+        return POSI_ERR_UNSUPPORTED;
+    }
     d.tan = L->d_tan;
     d.dpos = L->d_dpos;
     for (int k = 0; k < posi_many::kMaxTangents; ++k) {
@@ -249,6 +260,7 @@ int run_large(posi_large* L, int64_t n_steps, const int32_t* seed_body, const in
         d.seed_param[k] = seed_param ? seed_param[k] : 0;
     }
     LCK(cudaMemsetAsync(L->d_bad, 0xff, sizeof(unsigned long long), L->stream));
+    LCK(cudaMemsetAsync(L->d_ctl, 0, sizeof(int), L->stream));
     void* args[] = {&d, &n_steps};
     LCK(cudaEventRecord(L->e0, L->stream));
     LCK(cudaLaunchCooperativeKernel((const void*)posi_many::large_steps_kernel<NT, CO>, dim3(L->grid),
@@ -263,7 +275,7 @@ int run_large(posi_large* L, int64_t n_steps, const int32_t* seed_body, const in
     if (err & posi_many::LE_BARRIER) {
         posi::set_last_error("grid barrier wait ran out (the launch was abandoned; state unchanged)");
         cudaMemset(L->d_err, 0, sizeof(int));
-        cudaMemset(L->d_bar, 0, 2 * sizeof(unsigned));
+        cudaMemset(L->d_bar, 0, 4 * sizeof(unsigned));
         return POSI_ERR_CUDA;
     }
     if (err & posi_many::LE_KEPLER) {
@@ -316,7 +328,7 @@ int posi_large_iterate_tangent(posi_large* L, int64_t n_steps, int32_t n_dirs, c
     // the kernels carry 1, 2 or 4 directions; padding directions are zero
     const int nt = n_dirs == 1 ? 1 : n_dirs == 2 ? 2 : 4;
     // one warp per direction next to the primal warp of every 32 bodies
-    if (L->per_block != 32) {
+    if ((n + L->per_block_tan - 1) / L->per_block_tan > L->grid) {
         posi::set_last_error("tangents need at most 32 bodies per block (" +
                              std::to_string((int64_t)L->grid * 32) + " bodies on this device)");
         return POSI_ERR_UNSUPPORTED;

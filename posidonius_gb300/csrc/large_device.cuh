@@ -8,18 +8,28 @@
 // * Thread i owns body i for the whole launch (its state in registers).  The
 //   host body's state is kept, redundantly and identically, by every thread,
 //   so that the implicit-midpoint loop needs no broadcast.
-// * Reductions over bodies (host back-reactions, midpoint convergence,
-//   barycentre and momentum sums of the democratic-heliocentric transforms)
-//   are block sums written to a per-block slot and added in block order by
-//   every thread after a grid barrier: deterministic, run to run.
-// * Gravity (src/particles/universe.rs:198-303, all ordered pairs, WHFastTwo
-//   skip of the host) spreads the O(N^2) pair loop over every thread of the
-//   grid: thread t sums body (t mod N) over the t / N-th slice of the partner
-//   bodies; the slices are added in order.  The collision, Roche and
-//   ejection checks of the same loop report the first offending pair in the
-//   reference's (i, j) order.
-// * Grid barriers are counters in global memory with a bounded wait: a wait
-//   that runs out sets an error flag and every thread leaves the kernel.
+// * The bodies sit in the first blocks of the grid (the body blocks, 32
+//   bodies each while the grid has blocks enough).  Reductions over bodies
+//   (host back-reactions, midpoint convergence, barycentre and momentum sums
+//   of the transforms) are block sums written to a per-block row and added
+//   in block order after a barrier among the body blocks alone:
+//   deterministic run to run, and cheaper than a barrier of the whole grid
+//   (1.4 against 2.3 us on GB300).
+// * Gravity (src/particles/universe.rs:198-303) spreads the O(N^2) pair loop
+//   over every warp of the grid, over unordered pairs: the bodies form tiles
+//   of 32, and one warp takes a pair of tiles (I <= J), lane l holding body
+//   32 I + l while tile J's bodies rotate through the lanes by warp shuffles
+//   and carry their own sums with them, so each pair's 1 / r^3 serves both
+//   bodies.  Every body gets one partial sum per partner tile, added in tile
+//   order (deterministic).  Two grid barriers per step frame it: the
+//   positions published before, the partial sums after.  The blocks without
+//   bodies wait at the first and leave when the body blocks have finished.
+//   The collision, Roche and ejection checks of the same loop report the
+//   first offending pair in the reference's (i, j) order; a pair reads the
+//   Roche table's row i only when it is closer than the largest threshold of
+//   body i's checks.
+// * Barriers are counters in global memory with a bounded wait: a wait that
+//   runs out sets an error flag and every thread leaves the kernel.
 //
 // * large_steps_kernel<NT> with NT > 0 carries forward-mode tangents of the
 //   state along NT directions (derivatives with respect to initial state,
@@ -67,14 +77,17 @@ struct LDev {
     const double* roche;    // [n][n] Roche radii, row i for the pairs (i, j > i)
     const double* near2;    // [n] squared distance below which body i's pair checks can fire
     double* pos;            // [3][n] positions for the pair loop
-    double* gpart;          // [nchunk][3 (1 + NT)][n] partial accelerations (and their tangents)
-    double* bpart;          // [gridDim.x][BP_ROW]
+    double* gpart;          // [ntile][3 (1 + NT)][n] partial accelerations (and their tangents), per partner tile
+    double* bpart;          // [nbb][BP_ROW]
     double* tot;            // [BP_ROW] totals of the last reduction
-    unsigned* bar;          // [2] arrival count, generation
+    unsigned* bar;          // [2] arrival count, generation: barrier of the whole grid
+    unsigned* bbar;         // [2] the same among the body blocks
+    int* ctl;               // set to 1 by the body blocks when they have finished (the others then leave)
     int* err;               // error flags (LE_*)
     unsigned long long* bad;  // first failing pair: min over (i n + j) * 4 + code; all ones if none
-    int nchunk;
-    int per_block;          // bodies per block: body i is thread i % per_block of block i / per_block
+    int ntile;              // tiles of 32 bodies
+    int nbb;                // body blocks (the first nbb blocks of the grid)
+    int per_block;          // bodies per body block: body i is thread i % per_block of block i / per_block
     // tangent directions (the tangent kernels only)
     double* tan;            // [NT][12][n] tangents of r, v, L, S; read at launch, written back at the end
     double* dpos;           // [NT][3][n] position tangents for the pair loop
@@ -82,21 +95,39 @@ struct LDev {
     int seed_param[kMaxTangents];  // SEED_SIGMA (dissipation factor) or SEED_K2 (Love number)
 };
 
-// Sum of vals over the block into this block's partial row.  Only warps
-// that own bodies (active = the warp has a body) add: a warp's FP64 add holds
-// its SMSP's FP64 pipe 64 cycles, so the trees of empty warps would cost as
-// much as real ones; empty warps contribute zeros.
+// Sum of vals over the block into row blockIdx.x of bpart.  Only warps that
+// own bodies (warp_active) add: a warp's FP64 add holds its SMSP's FP64 pipe
+// 64 cycles whatever its active lanes, so the warps' sums are formed with
+// the lanes spread over the slots -- eight slots at a time, lane 4 s + p adds
+// the eight values 8p .. 8p + 7 of slot s in lane order, then the quarters
+// pair up, ((q0 + q1) + (q2 + q3)) -- 9 FP64 adds per eight slots instead
+// of 40 for shuffle trees.  The order of every slot's sum is fixed whatever
+// the number of slots, so a reduction carrying tangent slots beside the
+// primal ones gives the primal slots the same bits.
 template <int NS>
 __device__ __forceinline__ void block_partial(double* bpart, const double (&vals)[NS], int nslots, double* shm,
                                               bool warp_active) {
+    __shared__ double tw[kBlock / 32][8 * 33];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (warp_active) {
+        const int s = lane >> 2, p = lane & 3;
 #pragma unroll
-        for (int k = 0; k < NS; ++k) {
-            if (k < nslots) {
-                double x = vals[k];
-                for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-                if (lane == 0) shm[warp * BP_ROW + k] = x;
+        for (int c = 0; c < (NS + 7) / 8; ++c) {
+            if (c * 8 < nslots) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int k = c * 8 + q;
+                    if (k < NS) tw[warp][q * 33 + lane] = k < nslots ? vals[k] : 0.;
+                }
+                __syncwarp();
+                const double* t = &tw[warp][s * 33 + 8 * p];
+                double acc = t[0];
+#pragma unroll
+                for (int e = 1; e < 8; ++e) acc += t[e];
+                acc += __shfl_down_sync(0xffffffffu, acc, 1);
+                acc += __shfl_down_sync(0xffffffffu, acc, 2);
+                if (p == 0 && c * 8 + s < nslots) shm[warp * BP_ROW + c * 8 + s] = acc;
+                __syncwarp();
             }
         }
     }
@@ -116,15 +147,15 @@ __device__ __forceinline__ void block_partial(double* bpart, const double (&vals
 // releases the generation, the others poll it with acquire loads.  Returns
 // false (and flags the error) when the wait ran out; callers then leave the
 // kernel.
-__device__ bool grid_barrier(const LDev& D) {
+__device__ bool sync_blocks(const LDev& D, unsigned* ctr, unsigned parts) {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0) {
-        cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(D.bar[0]), gen(D.bar[1]);
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(ctr[0]), gen(ctr[1]);
         cuda::atomic_ref<int, cuda::thread_scope_device> err(*D.err);
         const unsigned g = gen.load(cuda::memory_order_relaxed);
         int ok = 1;
-        if (count.fetch_add(1u, cuda::memory_order_acq_rel) + 1u == gridDim.x) {
+        if (count.fetch_add(1u, cuda::memory_order_acq_rel) + 1u == parts) {
             count.store(0u, cuda::memory_order_relaxed);
             gen.fetch_add(1u, cuda::memory_order_release);
         } else {
@@ -145,74 +176,49 @@ __device__ bool grid_barrier(const LDev& D) {
     return ok_s != 0;
 }
 
-// Grid-wide sum: every block writes its partial row and arrives; the last
-// block to arrive adds the rows in block order (first warp, fixed butterfly),
-// publishes the totals and releases the others, which then read them once per
-// block.  One barrier, and only one block reads the partial rows.
+// Barrier of the whole grid (the pair loop's), and of the body blocks alone.
+__device__ __forceinline__ bool grid_barrier(const LDev& D) { return sync_blocks(D, D.bar, gridDim.x); }
+__device__ __forceinline__ bool body_barrier(const LDev& D) { return sync_blocks(D, D.bbar, (unsigned)D.nbb); }
+
+// Sum over the body blocks: every body block writes its partial row, the
+// body blocks meet, and every one of them adds the rows itself, in block
+// order (warp k mod 8 takes slot k; lane l rows l, l + 32, ...; then a fixed
+// butterfly): the same bits in every block, one barrier and no second round
+// trip through global memory.  The rows alternate between two buffers
+// (seq, counted by each caller): a block running ahead writes the next
+// reduction's row while a slower one may still read this one's.
 template <int NS>
 __device__ bool grid_reduce(const LDev& D, const double (&vals)[NS], int nslots, double* out, double* shm,
-                            bool warp_active, unsigned rows) {
-    __shared__ int last_s, ok_s;
-    __shared__ unsigned gen_s;
-    block_partial(D.bpart, vals, nslots, shm, warp_active);
-    if (threadIdx.x == 0) {
-        cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(D.bar[0]), gen(D.bar[1]);
-        gen_s = gen.load(cuda::memory_order_relaxed);
-        last_s = count.fetch_add(1u, cuda::memory_order_acq_rel) + 1u == gridDim.x;
-    }
-    __syncthreads();
-    int ok = 1;
-    if (last_s) {
-        // slot k is added by warp k mod 8 (the warps sit on different
-        // SMSPs); lane l takes rows l, l + 32, ... of the blocks that own
-        // bodies (the other rows are zero), then a fixed butterfly
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        for (int k = warp; k < nslots; k += kBlock / 32) {
-            double x = 0.;
-            for (unsigned b = lane; b < rows; b += 32) x += __ldcg(D.bpart + (size_t)b * BP_ROW + k);
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (lane == 0) D.tot[k] = x;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(D.bar[0]), gen(D.bar[1]);
-            count.store(0u, cuda::memory_order_relaxed);
-            gen.fetch_add(1u, cuda::memory_order_release);
-        }
-    } else if (threadIdx.x == 0) {
-        cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(D.bar[1]);
-        cuda::atomic_ref<int, cuda::thread_scope_device> err(*D.err);
-        const long long start = clock64();
-        while (gen.load(cuda::memory_order_relaxed) == gen_s) {
-            if (clock64() - start > kBarrierWaitCycles || (err.load(cuda::memory_order_relaxed) & LE_BARRIER)) {
-                ok = 0;
-                err.fetch_or(LE_BARRIER, cuda::memory_order_relaxed);
-                break;
-            }
-            __nanosleep(20);
-        }
-        cuda::atomic_thread_fence(cuda::memory_order_acquire, cuda::thread_scope_device);
-    }
-    if (threadIdx.x == 0) {
-        ok_s = ok;
-        for (int k = 0; k < nslots; ++k) shm[(kBlock / 32) * BP_ROW + k] = __ldcg(D.tot + k);
+                            bool warp_active, unsigned rows, unsigned& seq) {
+    double* buf = D.bpart + (size_t)(seq & 1u) * gridDim.x * BP_ROW;
+    ++seq;
+    block_partial(buf, vals, nslots, shm, warp_active);
+    if (!body_barrier(D)) return false;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = warp; k < nslots; k += kBlock / 32) {
+        double x = 0.;
+        for (unsigned b = lane; b < rows; b += 32) x += __ldcg(buf + (size_t)b * BP_ROW + k);
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) shm[(kBlock / 32) * BP_ROW + k] = x;
     }
     __syncthreads();
     for (int k = 0; k < nslots; ++k) out[k] = shm[(kBlock / 32) * BP_ROW + k];
-    const bool r = ok_s != 0;
     __syncthreads();
-    return r;
+    return true;
 }
 
-// Grid-wide exclusive prefix over the bodies in index order (body i is thread
+// Exclusive prefix over the bodies in index order, among the body blocks (body i is thread
 // i % per_block of block i / per_block; only the one-role engine calls it):
 // excl[k] = sum of vals[k] over the bodies before this thread's, tot[k] over
 // all bodies, for nslots <= 8.  Warp shuffle scans, then the warps' totals in
-// shared memory, then one grid barrier after which every block sums the
-// partial rows of the blocks before it (one warp per slot, fixed butterfly).
+// shared memory, then one barrier after which every block sums the partial
+// rows of the blocks before it (one warp per slot, fixed butterfly); rows in
+// alternating buffers, as grid_reduce's.
 template <int NS>
 __device__ bool grid_scan(const LDev& D, const double (&vals)[NS], int nslots, double* excl, double* tot, double* shm,
-                          unsigned rows) {
+                          unsigned rows, unsigned& seq) {
+    double* buf = D.bpart + (size_t)(seq & 1u) * gridDim.x * BP_ROW;
+    ++seq;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     constexpr int NW = kBlock / 32;
     double wex[NS];
@@ -238,13 +244,13 @@ __device__ bool grid_scan(const LDev& D, const double (&vals)[NS], int nslots, d
     if (threadIdx.x < nslots) {
         double bt = 0.;
         for (int w = 0; w < NW; ++w) bt += shm[w * BP_ROW + threadIdx.x];
-        D.bpart[(size_t)blockIdx.x * BP_ROW + threadIdx.x] = bt;
+        buf[(size_t)blockIdx.x * BP_ROW + threadIdx.x] = bt;
     }
-    if (!grid_barrier(D)) return false;
+    if (!body_barrier(D)) return false;
     for (int k = warp; k < nslots; k += NW) {
         double pre = 0., all = 0.;
         for (unsigned b = lane; b < rows; b += 32) {
-            const double x = __ldcg(D.bpart + (size_t)b * BP_ROW + k);
+            const double x = __ldcg(buf + (size_t)b * BP_ROW + k);
             all += x;
             if (b < blockIdx.x) pre += x;
         }
@@ -300,6 +306,151 @@ __device__ __forceinline__ void load_state(const LDev& D, int64_t i, BodyState& 
     }
 }
 
+// One lane of rotation of the partner tile's data and sums (lane l takes
+// lane l + 1's).
+template <int NT>
+__device__ __forceinline__ void rotate_partner(int lane, double& xj, double& yj, double& zj, double& gmj,
+                                               double& axj, double& ayj, double& azj,
+                                               double (&txj)[3][NT > 0 ? NT : 1], double (&taj)[3][NT > 0 ? NT : 1]) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int src = (lane + 1) & 31;
+    xj = __shfl_sync(FULL, xj, src); yj = __shfl_sync(FULL, yj, src); zj = __shfl_sync(FULL, zj, src);
+    gmj = __shfl_sync(FULL, gmj, src);
+    axj = __shfl_sync(FULL, axj, src); ayj = __shfl_sync(FULL, ayj, src); azj = __shfl_sync(FULL, azj, src);
+    if constexpr (NT > 0)
+        for (int q = 0; q < 3; ++q)
+            for (int d = 0; d < NT; ++d) {
+                txj[q][d] = __shfl_sync(FULL, txj[q][d], src);
+                taj[q][d] = __shfl_sync(FULL, taj[q][d], src);
+            }
+}
+
+// The pair loop of gravity (src/particles/universe.rs:198-303), run by every
+// warp of the grid after the positions are published.  Bodies form tiles of
+// 32; a warp takes one pair of tiles (I <= J), tile pairs spread over the
+// blocks first so that a block's warps (one per SMSP) take different pairs.
+// Lane l holds body i = 32 I + l; tile J's bodies start in lane order and
+// rotate one lane per step through 32 steps (warp shuffles), carrying their
+// own acceleration sums, so that each unordered pair (i < j) is evaluated
+// once: -G m_j d / |d|^3 for i, +G m_i d / |d|^3 for j, with d = x_i - x_j.
+// A diagonal tile (I = J) takes its 31 partners one-sided.  The pair skips of
+// the reference (WHFastOne: the host and the first planet in Jacobi
+// coordinates; WHFastTwo: every pair of the host otherwise) apply to the
+// forces only; the collision, Roche and ejection checks run on every pair
+// i < j -- the Roche table's row i (roche_radiuses[i][j], the reference's
+// entry for i < j) is read only when the pair is closer than body i's largest
+// threshold -- and the smallest (i n + j, check) key wins.  With NT tangent
+// directions the same rotation carries the tangents: the pair term's tangent
+// is -+ G m (dd - 3 (d . dd) d / |d|^2) / |d|^3, dd = dx_i - dx_j.  Partial
+// sums go to gpart[partner tile][row][body]: every body receives one per
+// tile.
+template <int NT>
+__device__ void pair_loop(const LDev& D, int host, int64_t p1, bool jac) {
+    constexpr int AN = NT > 0 ? NT : 1;
+    constexpr int rows = 3 * (1 + NT);
+    const int64_t n = D.n;
+    const int T = D.ntile;
+    const int64_t npairs = (int64_t)T * (T + 1) / 2;
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    for (int64_t tp = blockIdx.x + (int64_t)gridDim.x * wib; tp < npairs; tp += (int64_t)gridDim.x * wpb) {
+        int I = 0;
+        int64_t r = tp;
+        while (r >= T - I) { r -= T - I; ++I; }
+        const int J = I + (int)r;
+        const bool diag = I == J;
+        const int64_t i = (int64_t)I * 32 + lane;
+        const bool hi = i < n;
+        double xi = 0., yi = 0., zi = 0., gmi = 0., Ri = 0., nr2 = 0.;
+        double txi[3][AN] = {};
+        if (hi) {
+            xi = __ldcg(&D.pos[i]); yi = __ldcg(&D.pos[n + i]); zi = __ldcg(&D.pos[2 * n + i]);
+            gmi = kG * D.bf[POSI_BF_MASS * n + i];
+            Ri = D.bf[POSI_BF_RADIUS * n + i];
+            nr2 = D.near2[i];
+            if constexpr (NT > 0)
+                for (int q = 0; q < 3; ++q)
+                    for (int d = 0; d < NT; ++d) txi[q][d] = __ldcg(&D.dpos[(d * 3 + q) * n + i]);
+        }
+        // the partner tile: positions, masses and sums travel together (the
+        // partner's index follows from the step: lane l holds 32 J + (l + k) mod 32)
+        const int64_t j0 = (int64_t)J * 32 + lane;
+        double xj = 0., yj = 0., zj = 0., gmj = 0.;
+        double txj[3][AN] = {}, taj[3][AN] = {};
+        double axj = 0., ayj = 0., azj = 0.;
+        if (j0 < n) {
+            xj = __ldcg(&D.pos[j0]); yj = __ldcg(&D.pos[n + j0]); zj = __ldcg(&D.pos[2 * n + j0]);
+            gmj = kG * D.bf[POSI_BF_MASS * n + j0];
+            if constexpr (NT > 0)
+                for (int q = 0; q < 3; ++q)
+                    for (int d = 0; d < NT; ++d) txj[q][d] = __ldcg(&D.dpos[(d * 3 + q) * n + j0]);
+        }
+        // distances compared as the bit patterns of non-negative doubles
+        // (their order is the integers'), which keeps the gate off the FP64 pipe
+        const long long nr2_bits = __double_as_longlong(nr2);
+        double ax = 0., ay = 0., az = 0.;
+        double tai[3][AN] = {};
+        unsigned long long bad = ~0ull;
+        if (diag)
+            rotate_partner<NT>(lane, xj, yj, zj, gmj, axj, ayj, azj, txj, taj);
+        for (int k = diag ? 1 : 0; k < 32; ++k) {
+            const int64_t j = (int64_t)J * 32 + ((lane + k) & 31);
+            if (hi && j < n) {
+                const double dx = xi - xj, dy = yi - yj, dz = zi - zj;
+                const double d2 = dx * dx + dy * dy + dz * dz;
+                if (i < j && bad == ~0ull && (__double_as_longlong(d2) <= nr2_bits || i == host)) {
+                    const double rr = D.roche[i * n + j];
+                    const double Rs = Ri + D.bf[POSI_BF_RADIUS * n + j];
+                    const unsigned long long key = (unsigned long long)(i * n + j) * 4ull;
+                    if (d2 <= rr * rr) bad = key + POSI_SYS_ROCHE;
+                    else if (d2 <= Rs * Rs) bad = key + POSI_SYS_COLLISION;
+                    else if (i == host && d2 > kMAX_DISTANCE_2) bad = key + POSI_SYS_EJECTED;
+                }
+                const bool skip = jac ? ((i == host && j == p1) || (j == host && i == p1))  // WHFastOne
+                                      : (i == host || j == host);                          // WHFastTwo
+                if (!skip) {
+                    const double inv_d = rsqrt(d2);
+                    const double id3 = inv_d * inv_d * inv_d;
+                    const double pi = -gmj * id3, pj = gmi * id3;
+                    ax += pi * dx; ay += pi * dy; az += pi * dz;
+                    if (!diag) { axj += pj * dx; ayj += pj * dy; azj += pj * dz; }
+                    if constexpr (NT > 0) {
+                        const double i2 = inv_d * inv_d;
+                        for (int d = 0; d < NT; ++d) {
+                            const double ex = txi[0][d] - txj[0][d];
+                            const double ey = txi[1][d] - txj[1][d];
+                            const double ez = txi[2][d] - txj[2][d];
+                            const double s3 = 3. * (dx * ex + dy * ey + dz * ez) * i2;
+                            const double cx = ex - s3 * dx, cy = ey - s3 * dy, cz = ez - s3 * dz;
+                            tai[0][d] += pi * cx; tai[1][d] += pi * cy; tai[2][d] += pi * cz;
+                            if (!diag) { taj[0][d] += pj * cx; taj[1][d] += pj * cy; taj[2][d] += pj * cz; }
+                        }
+                    }
+                }
+            }
+            rotate_partner<NT>(lane, xj, yj, zj, gmj, axj, ayj, azj, txj, taj);
+        }
+        // 32 rotations: every partner is back in its own lane
+        if (hi) {
+            D.gpart[((int64_t)J * rows + 0) * n + i] = ax;
+            D.gpart[((int64_t)J * rows + 1) * n + i] = ay;
+            D.gpart[((int64_t)J * rows + 2) * n + i] = az;
+            if constexpr (NT > 0)
+                for (int q = 0; q < 3; ++q)
+                    for (int d = 0; d < NT; ++d) D.gpart[((int64_t)J * rows + 3 + q * NT + d) * n + i] = tai[q][d];
+        }
+        if (!diag && j0 < n) {
+            D.gpart[((int64_t)I * rows + 0) * n + j0] = axj;
+            D.gpart[((int64_t)I * rows + 1) * n + j0] = ayj;
+            D.gpart[((int64_t)I * rows + 2) * n + j0] = azj;
+            if constexpr (NT > 0)
+                for (int q = 0; q < 3; ++q)
+                    for (int d = 0; d < NT; ++d) D.gpart[((int64_t)I * rows + 3 + q * NT + d) * n + j0] = taj[q][d];
+        }
+        if (bad != ~0ull) atomicMin(D.bad, bad);
+    }
+}
+
 // Tangent of one body's state along one direction.
 struct Tangent {
     double r[3], v[3], L[3], S[3];
@@ -347,6 +498,7 @@ struct Large {
     double Rb[3], Vb[3];
     bool warp_bodies;       // this thread's warp owns at least one body
     unsigned body_rows;     // blocks that own bodies (the partial rows that can be nonzero)
+    unsigned rseq = 0;      // reductions and scans so far (their row buffer alternates)
 
     __device__ Large(const LDev& D_, double* shm_) : D(D_), shm(shm_) {}
 
@@ -504,7 +656,7 @@ struct Large {
                     vals[tslot(6, 3 + q)] = tth[q];
                 }
             double tot[NS];
-            if (!grid_reduce(D, vals, 6 + 6 * NT, tot, shm, warp_bodies, body_rows)) return false;
+            if (!grid_reduce(D, vals, 6 + 6 * NT, tot, shm, warp_bodies, body_rows, rseq)) return false;
             // the host's outputs, computed by every thread
             double haa[3], hdl[3];
             for (int q = 0; q < 3; ++q) { haa[q] = -tot[q]; hdl[q] = tot[3 + q]; }
@@ -549,7 +701,7 @@ struct Large {
                 }
                 const int ns = cm ? 10 + 6 * NT : 4;
                 double s4[NS];
-                if (!grid_reduce(D, cv, ns, s4, shm, warp_bodies, body_rows)) return false;
+                if (!grid_reduce(D, cv, ns, s4, shm, warp_bodies, body_rows, rseq)) return false;
                 if (cm) {
                     for (int q = 0; q < 6; ++q) cm[q] = s4[4 + q];
                     if (tn)
@@ -588,97 +740,84 @@ struct Large {
         return true;
     }
 
-    // ---- gravity over all ordered pairs, with the pair checks ----
-    // pos[] holds heliocentric positions published before the preceding
-    // barrier (differences of heliocentric and of inertial positions agree);
-    // the host sits at -shift (the jump moved every planet by +shift).  In
-    // Jacobi coordinates pos[] holds every body's inertial position and the
-    // pair of the host and the first planet is left out (WHFastOne).  The
-    // pair loop, spread over every thread of the grid, carries all NT
-    // tangent directions (positions published in dpos[]); the tangent of the
-    // pair term -G m_j d / |d|^3 along dd is
-    // -G m_j (dd - 3 (d . dd) d / |d|^2) / |d|^3.  tshift[d][q]: the
-    // tangents of the shift of every direction.
+    // ---- gravity: positions published, the pair loop over the whole grid,
+    // partial sums gathered ----
+    // pos[] holds the positions the pair loop reads: the planets' heliocentric
+    // positions (democratic heliocentric: published before the jump, the host
+    // then at -shift, since the jump moves every planet by +shift; WHDS:
+    // after the jump, the host at the origin) or every body's inertial
+    // position (Jacobi).  The host publishes its own entry here (and its
+    // tangents, -tshift[d], in dpos[]); then the grid meets, runs pair_loop,
+    // meets again, and each body adds its partial sums in tile order.
     __device__ bool gravity(const double shift[3], const double (&tshift)[NT > 0 ? NT : 1][3]) {
-        constexpr int AN = NT > 0 ? NT : 1;
-        const int64_t nn = n;
-        constexpr int rows = 3 * (1 + NT);  // rows of one slice in gpart
-        const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-        const int64_t gi = tid % nn, chunk = tid / nn;
-        if (chunk < D.nchunk) {
-            const int64_t j0 = chunk * nn / D.nchunk, j1 = (chunk + 1) * nn / D.nchunk;
-            double xi, yi, zi;
-            if (gi == host && !jac) { xi = -shift[0]; yi = -shift[1]; zi = -shift[2]; }
-            else { xi = __ldcg(&D.pos[gi]); yi = __ldcg(&D.pos[nn + gi]); zi = __ldcg(&D.pos[2 * nn + gi]); }
-            double txi[3][AN], tax[3][AN];
+        if (is_host && !jac) {
+            if (primal_role())
+                for (int q = 0; q < 3; ++q) D.pos[q * n + i] = -shift[q];
             if constexpr (NT > 0)
-                for (int q = 0; q < 3; ++q)
-                    for (int d = 0; d < NT; ++d) {
-                        txi[q][d] = gi == host ? -tshift[d][q] : __ldcg(&D.dpos[(d * 3 + q) * nn + gi]);
-                        tax[q][d] = 0.;
-                    }
-            const double Ri = D.bf[POSI_BF_RADIUS * nn + gi];
-            // no pair check of body gi fires beyond this distance: the rare
-            // pairs inside it read the table's row gi (the reference's
-            // roche_radiuses[i][j], not symmetric for equal masses)
-            const double near2 = D.near2[gi];
-            double ax = 0., ay = 0., az = 0.;
-            unsigned long long bad = ~0ull;
-            for (int64_t j = j0; j < j1; ++j) {
-                if (j == gi) continue;
-                double xj, yj, zj;
-                if (j == host && !jac) { xj = -shift[0]; yj = -shift[1]; zj = -shift[2]; }
-                else { xj = __ldcg(&D.pos[j]); yj = __ldcg(&D.pos[nn + j]); zj = __ldcg(&D.pos[2 * nn + j]); }
-                const double dx = xi - xj, dy = yi - yj, dz = zi - zj;
-                const double d2 = dx * dx + dy * dy + dz * dz;
-                if (gi < j && bad == ~0ull && (d2 <= near2 || gi == host)) {
-                    const double rr = D.roche[gi * nn + j];
-                    const double Rs = Ri + D.bf[POSI_BF_RADIUS * nn + j];
-                    const unsigned long long key = (unsigned long long)(gi * nn + j) * 4ull;
-                    if (d2 <= rr * rr) bad = key + POSI_SYS_ROCHE;
-                    else if (d2 <= Rs * Rs) bad = key + POSI_SYS_COLLISION;
-                    else if (gi == host && d2 > kMAX_DISTANCE_2) bad = key + POSI_SYS_EJECTED;
-                }
-                if (jac ? ((gi == host && j == p1) || (j == host && gi == p1))   // WHFastOne
-                        : (gi == host || j == host))                                // WHFastTwo
-                    continue;
-                const double inv_d = rsqrt(d2);
-                const double p = -kG * D.bf[POSI_BF_MASS * nn + j] * (inv_d * inv_d * inv_d);
-                ax += p * dx; ay += p * dy; az += p * dz;
-                if constexpr (NT > 0) {
-                    const double i2 = inv_d * inv_d;
-                    for (int d = 0; d < NT; ++d) {
-                        const double ex = txi[0][d] - __ldcg(&D.dpos[(d * 3 + 0) * nn + j]);
-                        const double ey = txi[1][d] - __ldcg(&D.dpos[(d * 3 + 1) * nn + j]);
-                        const double ez = txi[2][d] - __ldcg(&D.dpos[(d * 3 + 2) * nn + j]);
-                        const double s = 3. * (dx * ex + dy * ey + dz * ez) * i2;
-                        tax[0][d] += p * (ex - s * dx);
-                        tax[1][d] += p * (ey - s * dy);
-                        tax[2][d] += p * (ez - s * dz);
-                    }
-                }
-            }
-            D.gpart[(chunk * rows + 0) * nn + gi] = ax;
-            D.gpart[(chunk * rows + 1) * nn + gi] = ay;
-            D.gpart[(chunk * rows + 2) * nn + gi] = az;
-            if constexpr (NT > 0)
-                for (int q = 0; q < 3; ++q)
-                    for (int d = 0; d < NT; ++d) D.gpart[(chunk * rows + 3 + q * NT + d) * nn + gi] = tax[q][d];
-            if (bad != ~0ull) atomicMin(D.bad, bad);
+                if (tan_on())
+                    for (int q = 0; q < 3; ++q) D.dpos[(dir * 3 + q) * n + i] = -tshift[dir][q];
         }
         if (!grid_barrier(D)) return false;
-        if (has) {
-            for (int q = 0; q < 3; ++q) {
-                double acc = 0.;
-                for (int k = 0; k < D.nchunk; ++k) acc += __ldcg(&D.gpart[(k * rows + q) * nn + i]);
-                a[q] = acc;
-            }
-            if (tan_on())
-                for (int q = 0; q < 3; ++q) {
-                    double acc = 0.;
-                    for (int k = 0; k < D.nchunk; ++k) acc += __ldcg(&D.gpart[(k * rows + 3 + q * NT + dir) * nn + i]);
-                    da[q] = acc;
+        pair_loop<NT>(D, host, p1, jac);
+        if (!grid_barrier(D)) return false;
+        if (D.per_block == 32) {
+            // the body block's 32 bodies are tile blockIdx.x: its eight warps
+            // add the partial sums together -- warp w the partner tiles
+            // [w c, (w + 1) c), c = ceil(ntile / 8), in order -- and the
+            // chunk sums are added in warp order: a fixed order whatever the
+            // number of tangent rows, loads spread over the block instead of
+            // one latency-bound chain per body
+            __shared__ double gchunk[kBlock / 32][3][32];
+            __shared__ double gfinal[3 * (1 + kMaxTangents)][32];
+            constexpr int rows = 3 * (1 + NT);
+            const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+            const int c = (D.ntile + kBlock / 32 - 1) / (kBlock / 32);
+            const int64_t body = (int64_t)blockIdx.x * 32 + l, nn = n;
+            const int k0 = w * c, k1 = min(D.ntile, (w + 1) * c);
+            for (int rg = 0; rg < rows; rg += 3) {
+                double v[3] = {0., 0., 0.};
+                if (body < nn)
+                    for (int k = k0; k < k1; ++k)
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) v[q] += __ldcg(&D.gpart[((int64_t)k * rows + rg + q) * nn + body]);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) gchunk[w][q][l] = v[q];
+                __syncthreads();
+                if (threadIdx.x < 96) {
+                    const int q = threadIdx.x >> 5;
+                    double acc = gchunk[0][q][l];
+                    for (int ww = 1; ww < kBlock / 32; ++ww) acc += gchunk[ww][q][l];
+                    gfinal[rg + q][l] = acc;
                 }
+                __syncthreads();
+            }
+            if (has) {
+                for (int q = 0; q < 3; ++q) a[q] = gfinal[q][l];
+                if (tan_on())
+                    for (int q = 0; q < 3; ++q) da[q] = gfinal[3 + q * NT + dir][l];
+            }
+            __syncthreads();
+        } else if (has) {
+            // more than 32 bodies per block: each body adds its partial sums
+            // in tile order, loaded eight tiles at a time
+            constexpr int rows = 3 * (1 + NT);
+            const int64_t nn = n;
+            const int nq = tan_on() ? 6 : 3;
+            for (int qq = 0; qq < nq; ++qq) {
+                const int row = qq < 3 ? qq : 3 + (qq - 3) * NT + dir;
+                const double* src = D.gpart + (int64_t)row * nn + i;
+                const int64_t stride = (int64_t)rows * nn;
+                double acc = 0.;
+                for (int kk = 0; kk < D.ntile; kk += 8) {
+                    double v[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) v[e] = kk + e < D.ntile ? __ldcg(src + (int64_t)(kk + e) * stride) : 0.;
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        if (kk + e < D.ntile) acc += v[e];
+                }
+                if (qq < 3) a[qq] = acc; else da[qq - 3] = acc;
+            }
         }
         return true;
     }
@@ -749,7 +888,7 @@ struct Large {
                 }
         }
         double tot[NS];
-        if (!grid_reduce(D, vals, 6 + 6 * NT, tot, shm, warp_bodies, body_rows)) return false;
+        if (!grid_reduce(D, vals, 6 + 6 * NT, tot, shm, warp_bodies, body_rows, rseq)) return false;
         for (int q = 0; q < 6; ++q) S[q] = tot[q];
         if constexpr (NT > 0)
             for (int d = 0; d < NT; ++d)
@@ -774,7 +913,7 @@ struct Large {
             const double w = c.m / eta_in;
             for (int q = 0; q < 3; ++q) { vals[q] = w * x[q]; vals[3 + q] = w * u[q]; }
         }
-        if (!grid_scan(D, vals, 6, ex, tot, shm, body_rows)) return false;
+        if (!grid_scan(D, vals, 6, ex, tot, shm, body_rows, rseq)) return false;
         for (int q = 0; q < 3; ++q) { h.r[q] = Rb[q] - tot[q]; h.v[q] = Vb[q] - tot[3 + q]; }
         if (planet)
             for (int q = 0; q < 3; ++q) {
@@ -809,7 +948,7 @@ struct Large {
             double vals[NS] = {}, ex[NS], tot[NS];
             if (planet)
                 for (int q = 0; q < 3; ++q) { vals[q] = c.m * b.r[q]; vals[3 + q] = c.m * b.v[q]; }
-            if (!grid_scan(D, vals, 6, ex, tot, shm, body_rows)) return false;
+            if (!grid_scan(D, vals, 6, ex, tot, shm, body_rows, rseq)) return false;
             if (planet) {
                 const double ie = 1. / eta_ex;
                 for (int q = 0; q < 3; ++q) {
@@ -823,7 +962,6 @@ struct Large {
         if (!from_jacobi(x, u)) return false;
         if (has && primal_role())
             for (int q = 0; q < 3; ++q) D.pos[q * n + i] = b.r[q];
-        if (!grid_barrier(D)) return false;
         const double zero[3] = {0., 0., 0.};
         double tzero[NT > 0 ? NT : 1][3] = {};
         if (!gravity(zero, tzero)) return false;
@@ -835,7 +973,7 @@ struct Large {
                 for (int q = 0; q < 3; ++q) vals[q] = c.m * a[q];
             if (is_host)
                 for (int q = 0; q < 3; ++q) vals[3 + q] = hc.m * a[q];
-            if (!grid_scan(D, vals, 6, ex, tot, shm, body_rows)) return false;
+            if (!grid_scan(D, vals, 6, ex, tot, shm, body_rows, rseq)) return false;
             if (planet) {
                 const double ie = 1. / eta_ex;
                 for (int q = 0; q < 3; ++q) u[q] += dt * (a[q] - (tot[3 + q] + ex[q]) * ie);
@@ -873,7 +1011,7 @@ struct Large {
                 vals[3 + q] = wv * u[q];
                 vals[6 + q] = c.m * wv * u[q];
             }
-        if (!grid_reduce(D, vals, 9, tot, shm, warp_bodies, body_rows)) return false;
+        if (!grid_reduce(D, vals, 9, tot, shm, warp_bodies, body_rows, rseq)) return false;
         for (int q = 0; q < 9; ++q) S[q] = tot[q];
         return true;
     }
@@ -920,7 +1058,6 @@ struct Large {
         // at the origin)
         if (planet && primal_role())
             for (int q = 0; q < 3; ++q) D.pos[q * n + i] = x[q];
-        if (!grid_barrier(D)) return false;
         const double zero[3] = {0., 0., 0.};
         double tzero[NT > 0 ? NT : 1][3] = {};
         if (!gravity(zero, tzero)) return false;
@@ -1036,6 +1173,19 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
     constexpr bool JAC = CO == POSI_JACOBI;
     static_assert(CO == POSI_DEMOCRATIC_HELIOCENTRIC || NT == 0, "Jacobi and WHDS carry no tangents");
     __shared__ double shm[(kBlock / 32 + 1) * BP_ROW];
+    if ((int)blockIdx.x >= D.nbb) {
+        // a block without bodies joins the pair loop of every step and leaves
+        // once the body blocks have finished (ctl) or a pair has failed
+        const int host = (int)D.si[POSI_SI_HOST];
+        const int64_t p1 = host == 0 ? 1 : 0;
+        for (;;) {
+            if (!grid_barrier(D)) return;
+            if (__ldcg(D.ctl) != 0) return;
+            pair_loop<NT>(D, host, p1, JAC);
+            if (!grid_barrier(D)) return;
+            if (__ldcg(D.bad) != ~0ull) return;
+        }
+    }
     Large<NT> S(D, shm);
     S.n = D.n;
     const int roles = 1 + NT;
@@ -1095,7 +1245,7 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
         double vals[Large<NT>::NS] = {};
         vals[0] = S.has && S.primal_role() ? S.c.m : 0.;
         double tot[1];
-        if (!grid_reduce(D, vals, 1, tot, shm, S.warp_bodies, S.body_rows)) return;
+        if (!grid_reduce(D, vals, 1, tot, shm, S.warp_bodies, S.body_rows, S.rseq)) return;
         S.Mtot = tot[0];
         S.inv_M = 1. / S.Mtot;
         S.inv_hm = 1. / S.hc.m;
@@ -1109,7 +1259,7 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
         // the masses before each body and its cumulative GM (host first)
         double vals[Large<NT>::NS] = {}, ex[Large<NT>::NS], tot[Large<NT>::NS];
         if (S.planet) { vals[0] = S.c.m; vals[1] = S.c.mg; }
-        if (!grid_scan(D, vals, 2, ex, tot, shm, S.body_rows)) return;
+        if (!grid_scan(D, vals, 2, ex, tot, shm, S.body_rows, S.rseq)) return;
         S.eta_ex = S.hc.m + ex[0];
         S.eta_in = S.eta_ex + S.c.m;
         S.kgm = S.hc.mg + ex[1] + (S.planet ? S.c.mg : 0.);
@@ -1126,6 +1276,13 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
             ++done;
             if (S.t + S.dt > S.time_limit) break;
         }
+    }
+    // the blocks without bodies wait for another pair loop: release them,
+    // unless a failing pair (which every block reads after the last pair
+    // loop) or a failed barrier has sent them away already
+    if (!(__ldcg(D.err) & LE_BARRIER) && __ldcg(D.bad) == ~0ull) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(D.ctl, 1);
+        grid_barrier(D);
     }
     if (__ldcg(D.err) & LE_BARRIER) return;  // state left as it was: the launch failed
     if (S.has && S.primal_role()) {

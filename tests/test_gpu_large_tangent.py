@@ -85,10 +85,20 @@ def _check(tan, fd, fd2, label):
 
 
 def test_tangent_primal_matches_plain_run():
+    """The integrated state of a tangent run (positions, velocities, spin
+    angular momenta, spins and their compensation terms) is the plain run's
+    bit for bit: every primal sum is formed in the same order.  The stored
+    gravity acceleration of the last evaluation -- a diagnostic that enters
+    the state only through dt a, far below a velocity's last bit -- may
+    differ by a few ulps: the pair loop's instantiation with tangents is
+    compiled with other multiply-add contractions."""
     case = _case()
     plain = _final(case)
     prim, _ = _tangent(case, [(1, L.SEED_SIGMA), (2, L.SEED_SIGMA)])
-    np.testing.assert_array_equal(prim.view(np.int64), plain.view(np.int64))
+    acc = [L.BF_AX, L.BF_AY, L.BF_AZ]
+    state = [f for f in range(L.BF_COUNT) if f not in acc]
+    np.testing.assert_array_equal(prim[:, state].view(np.int64), plain[:, state].view(np.int64))
+    assert np.abs(prim[:, acc] - plain[:, acc]).max() <= 1e-14 * np.abs(plain[:, acc]).max()
 
 
 @pytest.mark.parametrize("body", [1, 2])
