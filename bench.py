@@ -344,17 +344,55 @@ def energy_horizon(workload, n_sys, steps, mode):
     fin = b.get_state()
     b.close()
     d3 = np.abs(np.array([newtonian_energy(fin, s) for s in range(n_sys)]) - e0) / np.abs(e0)
+    # definition 2: tides alone (flattening and GR off, their energies are
+    # not in the Newtonian sum), the Newtonian plus rotational energy plus
+    # the tidal dissipation dE/dt integrated over the run (trapezoid over
+    # historic snapshots every H steps, where the kernel refreshes dE/dt)
+    H = 50
+    tid = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in ens.items()}
+    for f in (L.SI_FLAT, L.SI_GR):
+        tid["sys_i64"][:, f] = 0
+    for f in (L.BI_FLAT_KIND, L.BI_GR_KIND):
+        tid["body_i64"][:, :, f] = L.EFFECT_DISABLED
+    tid["sys_f64"][:, L.SF_HIST_PERIOD] = H * tid["sys_f64"][:, L.SF_DT]
+
+    def budget(st):
+        e = np.array([newtonian_energy(st, s) for s in range(n_sys)])
+        bf = st["body_f64"]
+        moi = np.where(bf[..., L.BF_MOI] != 0, bf[..., L.BF_MOI], np.inf)
+        e += 0.5 * np.sum(np.sum(bf[..., L.ANG] ** 2, axis=-1) / moi, axis=1)
+        de = np.nansum(bf[..., L.BF_DENERGY_DT], axis=1)
+        return e, de
+
+    b = pg.Batch(tid, mode=mode)
+    b.initialize_physical_values()
+    e_first, de_prev = budget(b.get_state())
+    lost = np.zeros(n_sys)
+    dt_chunk = H * tid["sys_f64"][:, L.SF_DT]
+    for _ in range(steps // H):
+        b.iterate(H, H)
+        e_now, de_now = budget(b.get_state())
+        lost += 0.5 * (de_prev + de_now) * dt_chunk
+        de_prev = de_now
+    b.close()
+    d2 = np.abs(e_now + lost - e_first) / np.abs(e_first)
+    d2_no_loss = np.abs(e_now - e_first) / np.abs(e_first)
     q = lambda x: {"median": float(np.median(x)), "max": float(x.max())}
     return {
         "workload": workload, "systems": n_sys, "steps": steps, "days": steps * 0.08,
         "def1_vs_oracle_trajectory": q(d1) | {"systems_within_1e-10": int((d1 <= 1e-10).sum())},
         "oracle_self_sensitivity_1e-15_nudge": q(sens) | {"systems_within_1e-10": int((sens <= 1e-10).sum())},
+        "def2_tides_only_energy_budget_drift": q(d2) | {
+            "without_the_integrated_dissipation": q(d2_no_loss),
+            "integrated_dissipation_rel": q(np.abs(lost) / np.abs(e_first)),
+            "note": f"tides alone; Newtonian + rotational energy + the integral of the reference's tidal dE/dt "
+                    f"(trapezoid over historic snapshots every {H} steps), relative drift over the run"},
         "def3_pure_whfast_drift": q(d3),
         "gpu_s": gpu_s,
         "note": "relative deviation of the barycentric Newtonian energy: def 1 from the oracle's own trajectory at "
                 "the same step; beside it the oracle against itself started 1e-15 away (systems that part from "
                 "themselves part from any other arithmetic too); def 3 the pure-WHFast drift (effects off) "
-                "from the start",
+                "from the start; def 2 with tides alone (flattening and GR potentials are not in the Newtonian sum)",
     }
 
 
@@ -741,6 +779,10 @@ def main():
     # lane mapping per body count: picked by the autotuner (state unchanged)
     lanes = batch.autotune(probe_steps=20) if not args.no_autotune else {
         int(n): batch.mapping_for(int(n)) for n in np.unique(ens["sys_i64"][:, L.SI_N])}
+    tuning = None if args.no_autotune else {
+        str(n): {"systems": int(np.sum(ens["sys_i64"][:, L.SI_N] == n)), "chosen_lanes": int(g),
+                 "probe_ms_by_lanes": {str(k): v for k, v in batch.autotune_report(n).items()}}
+        for n, g in sorted(lanes.items())}
     K = args.steps
     W = max(3, args.warmup)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -822,6 +864,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
                 "note": f"one C-ABI call chain: upload {h2d} B, {K} steps, download {d2h} B; wall clock, median of "
                         f"{len(e2e_times)} repeats"},
+        "autotune": tuning,
         "gpu_launches": int(launches * len(times)),
         "gpu_launches_note": f"{int(launches)} kernel launches per timed launch of {K} steps, {len(times)} timed "
                              "launches",

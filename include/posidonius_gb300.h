@@ -366,6 +366,13 @@ int posi_batch_mapping_for(const posi_batch* b, int64_t n);
  * the mapping: every mapping computes the same bits. */
 int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n);
 
+/* The last autotune's probe times for systems of n bodies: ms_by_lanes[k]
+ * (6 entries) is the timed probe of 2^k lanes per system (k = 0: one thread
+ * per system, never probed since it is not built), -1 where that mapping was
+ * not admissible or not tried.  POSI_ERR_STATE when no system of n bodies
+ * was tuned. */
+int posi_batch_autotune_report(const posi_batch* b, int64_t n, double* ms_by_lanes);
+
 /* Device time of the last posi_batch_iterate in milliseconds (CUDA events on
  * the batch's stream) and the number of kernel launches it made. */
 int posi_batch_last_timing(const posi_batch* b, double* ms, int64_t* launches);

@@ -282,6 +282,13 @@ class Batch:
         check(lib().posi_batch_autotune(self._h, int(probe_steps), out))
         return {n: int(out[n]) for n in range(L.MAX_BODIES + 1) if out[n]}
 
+    def autotune_report(self, n):
+        """The last autotune's probe times (ms) for systems of n bodies, by
+        lanes per system: {lanes: ms} for the mappings it tried."""
+        ms = np.zeros(6, np.float64)
+        check(lib().posi_batch_autotune_report(self._h, int(n), ptr(ms, "f")))
+        return {1 << k: float(ms[k]) for k in range(6) if ms[k] >= 0}
+
     def empty_state(self):
         ns, nm = self.n_sys, self.nmax
         return {

@@ -56,6 +56,7 @@ SIGNATURES = {
     "posi_batch_set_state": (ctypes.c_int, [_vp, _i64p, _f64p, _i64p, _f64p]),
     "posi_batch_mapping_for": (ctypes.c_int, [_vp, ctypes.c_int64]),
     "posi_batch_autotune": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]),
+    "posi_batch_autotune_report": (ctypes.c_int, [_vp, ctypes.c_int64, _f64p]),
     "posi_batch_last_timing": (ctypes.c_int, [_vp, _f64p, _i64p]),
     "posi_fp64_probe": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p, _f64p]),
     "posi_open_history": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int64]),

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -107,6 +108,7 @@ struct posi_batch {
     std::vector<int32_t> host_list;
     std::map<int64_t, int> mapping_of_n;
     std::map<int64_t, double> tuned_ms_of_n;  // autotuner: best probe time per body count
+    std::map<int64_t, std::array<double, 6>> probe_ms_of_n;  // every probe, by log2 of the lanes
     double last_ms = 0.;
     int64_t last_launches = 0;
     cudaGraphExec_t graph = nullptr;
@@ -1245,6 +1247,7 @@ int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n)
     } lguard{d_probe};
     std::map<int64_t, int> chosen;
     b->tuned_ms_of_n.clear();
+    b->probe_ms_of_n.clear();
     LaunchArgs a{};
     a.op = posi::OP_STEPS;
     a.n_steps = probe_steps;
@@ -1254,6 +1257,8 @@ int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n)
         CK(cudaMemcpyAsync(d_probe, sys.data(), sys.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));
         double best = 1e300;
         int best_g = posi::group_size_for(n);
+        std::array<double, 6> probes;
+        probes.fill(-1.);
         for (int G = posi::group_size_for(n); G <= 32; G *= 2) {
             a.G = G;
             DevView v = b->view(0, (int32_t)sys.size());
@@ -1268,9 +1273,13 @@ int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n)
                 if ((rc = copy_all(false)) != POSI_OK) return rc;
             }
             if (ms < best) { best = ms; best_g = G; }
+            int k = 0;
+            while ((1 << k) < G) ++k;
+            probes[(size_t)k] = ms;
         }
         chosen[n] = best_g;
         b->tuned_ms_of_n[n] = best;
+        b->probe_ms_of_n[n] = probes;
     }
     CK(cudaStreamSynchronize(b->stream));
     std::vector<int64_t> si((size_t)b->n_sys * POSI_SI_COUNT);
@@ -1279,6 +1288,17 @@ int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n)
     if (lanes_by_n) {
         for (int k = 0; k <= POSI_MAX_BODIES; ++k) lanes_by_n[k] = chosen.count(k) ? chosen[k] : 0;
     }
+    return POSI_OK;
+}
+
+int posi_batch_autotune_report(const posi_batch* b, int64_t n, double* ms_by_lanes) {
+    if (!b || !ms_by_lanes) return POSI_ERR_ARG;
+    auto it = b->probe_ms_of_n.find(n);
+    if (it == b->probe_ms_of_n.end()) {
+        g_last_error = "no autotuned systems of " + std::to_string(n) + " bodies";
+        return POSI_ERR_STATE;
+    }
+    for (size_t k = 0; k < 6; ++k) ms_by_lanes[k] = it->second[k];
     return POSI_OK;
 }
 

@@ -140,6 +140,8 @@ def test_autotune_keeps_state_and_results(mode):
     assert set(choice) == ns
     for n, g in choice.items():
         assert g in (2, 4, 8, 16, 32) and g >= n and tuned.mapping_for(n) == g
+        probes = tuned.autotune_report(n)
+        assert g in probes and probes[g] == min(probes.values()) and 1 not in probes
     plain = pg.Batch(ens, mode=mode)
     plain.initialize_physical_values()
     tuned.iterate(30, 10)
