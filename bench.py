@@ -75,12 +75,13 @@ def parse():
     return p.parse_args()
 
 
-# DRAM bytes per system and kernel launch, from one ncu capture of the kernel
-# on 1024 systems (dram__bytes_read.sum + dram__bytes_write.sum over the
-# systems; the state is read and written once per launch whatever its step
-# count): profiles/whfast_steps_kernel_ensemble8_small.md (5.03 MB + 0 MB) and
-# profiles/ias15_steps_kernel_ensemble8_small.md (12.24 MB + 1.12 MB)
-DRAM_BYTES_PER_SYSTEM_LAUNCH = {"ensemble8": 5.03e6 / 1024, "ias15": 13.36e6 / 1024}
+# DRAM bytes per system and kernel launch, from one ncu capture of each kernel
+# (dram__bytes_read.sum + dram__bytes_write.sum over the systems; the state is
+# read and written once per launch whatever its step count):
+# profiles/whfast_steps_kernel_ensemble8_bench.md (4096 systems: 22.07 MB +
+# 0.02 MB) and profiles/ias15_steps_kernel_ensemble8_small.md (1024 systems:
+# 12.24 MB + 1.12 MB)
+DRAM_BYTES_PER_SYSTEM_LAUNCH = {"ensemble8": 22.09e6 / 4096, "ias15": 13.36e6 / 1024}
 
 EFFECTS = {
     "ensemble8": "CTL tides + oblate flattening + Kidder GR",
