@@ -908,7 +908,7 @@ def main():
         result["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                               "frac": achieved / peak, "traffic": traffic,
                               "traffic_note": "DRAM bytes per timed launch: the per-system bytes of one ncu capture "
-                                              "on 1024 systems (profiles/) x systems x kernel launches per timed "
+                                              "of the kernel (profiles/) x systems x kernel launches per timed "
                                               "launch; FP64-bound, the state stays on chip between steps",
                               "flops_per_system_step": flops,
                               "peak_source": "measured in-run: posi_fp64_probe (DFMA chains; MEASURED_PEAKS.json "

@@ -229,6 +229,14 @@ enum {
     PC_TD_L0, PC_TD_L1, PC_TD_L2,
     PC_COUNT
 };
+#if !POSI_EXACT
+// FAST keeps the Kidder GR constants in combined form (planet_constants):
+// these slots take the place of the reference-order ones.
+enum {
+    PC_GR0 = PC_B, PC_GR1 = PC_C, PC_GR2 = PC_DD, PC_GO0 = PC_E, PC_GO1 = PC_T1, PC_GO2 = PC_K5C,
+    PC_FMU = PC_FM, PC_FM2MU = PC_FM2
+};
+#endif
 
 // Fields of one historic-snapshot record (src/integrator/output.rs:91-135).
 enum { HR_T = 0, HR_DT, HR_ID, HR_PX, HR_PY, HR_PZ, HR_SX, HR_SY, HR_SZ, HR_VX, HR_VY, HR_VZ, HR_M, HR_R, HR_RG2,
@@ -802,27 +810,40 @@ struct Sys {
             const double f2 = f * f;
             const double gd2 = mgs * id2 * (1. / kC2);
             const double A = -gd2;
+            // The first- and second-order terms as one polynomial in |v|^2
+            // and v_r^2 (general_relativity.rs:187-298):
+            //   radial = A (GR0 + |v|^2 (GR1 + K2C |v|^2 - K4C v_r^2) + v_r^2 (GR2 + K3C v_r^2)),
+            //   ortho  = v_r (GO0 + GO1 |v|^2 + GO2 v_r^2)
+            // with GR0 = T1 - C, GR1 = B - K5C, GR2 = -(DD + K6C),
+            // GO0 = E - A05 Q, GO1 = A05 P, GO2 = -A05 R3 in the terms of the
+            // reference's two orders.
+            const double c_b = 1.0 + 3.0 * f, c_c = 2.0 * (2.0 + f) * mgd, c_dd = 1.5 * f;
+            const double c_e = gd2 * 2.0 * (2.0 - f);
+            const double c_t1 = (3.0 / 4.0) * (12.0 + 29.0 * f) * (mgd * mgd);
+            const double c_k5 = 0.5 * f * (13.0 - 4.0 * f) * mgd;
+            const double c_k6 = (2.0 + 25.0 * f + 2.0 * f2) * mgd;
+            const double a05 = A * (-0.5);
+            const double c_p = f * (15.0 + 4.0 * f);
+            const double c_q = (4.0 + 41.0 * f + 8.0 * f2) * mgd;
+            const double c_r3 = 3.0 * f * (3.0 + 2.0 * f);
             P(PC_A) = A;
-            P(PC_B) = 1.0 + 3.0 * f;
-            P(PC_C) = 2.0 * (2.0 + f) * mgd;
-            P(PC_DD) = 1.5 * f;
-            P(PC_E) = gd2 * 2.0 * (2.0 - f);
-            P(PC_T1) = (3.0 / 4.0) * (12.0 + 29.0 * f) * (mgd * mgd);
+            P(PC_GR0) = c_t1 - c_c;
+            P(PC_GR1) = c_b - c_k5;
+            P(PC_GR2) = -(c_dd + c_k6);
             P(PC_K2C) = f * (3.0 - 4.0 * f);
             P(PC_K3C) = (15.0 / 8.0) * f * (1.0 - 3.0 * f);
             P(PC_K4C) = (3.0 / 2.0) * f * (3.0 - 4.0 * f);
-            P(PC_K5C) = 0.5 * f * (13.0 - 4.0 * f) * mgd;
-            P(PC_K6C) = (2.0 + 25.0 * f + 2.0 * f2) * mgd;
-            P(PC_A05) = A * (-0.5);
-            P(PC_P) = f * (15.0 + 4.0 * f);
-            P(PC_Q) = (4.0 + 41.0 * f + 8.0 * f2) * mgd;
-            P(PC_R3) = 3.0 * f * (3.0 + 2.0 * f);
+            P(PC_GO0) = c_e - a05 * c_q;
+            P(PC_GO1) = a05 * c_p;
+            P(PC_GO2) = -a05 * c_r3;
             const double M = hm + b.m;
             const double iM = 1. / M;
+            const double mu = (hm * b.m) * iM;
             P(PC_MFM) = hm - b.m;                    // ((m_host - m) / M) M
-            P(PC_MU) = (hm * b.m) * iM;
-            P(PC_FM) = 2. + (3. / 2.) * b.m * inv_hm;
-            P(PC_FM2) = 2. + (3. / 2.) * hm * inv_m;
+            // Kidder 1995 eq. 2.4a / 2.4b: the orbital angular momentum
+            // mu (r x v) enters the torques scaled by these
+            P(PC_FMU) = (2. + (3. / 2.) * b.m * inv_hm) * mu;
+            P(PC_FM2MU) = (2. + (3. / 2.) * hm * inv_m) * mu;
             const double n0 = P(PC_XD), n1 = P(PC_YD), n2 = P(PC_ZD);
             P(PC_NN0) = n0;
             P(PC_NN1) = n1;
@@ -1486,7 +1507,7 @@ struct Sys {
             hv0 = b.v[0] - card[HC_VX];
             hv1 = b.v[1] - card[HC_VY];
             hv2 = b.v[2] - card[HC_VZ];
-            vr = (x * hv0 + y * hv1 + z * hv2) * P(PC_INV_D);
+            vr = P(PC_XD) * hv0 + P(PC_YD) * hv1 + P(PC_ZD) * hv2;
             nv2 = hv0 * hv0 + hv1 * hv1 + hv2 * hv2;
             rs_s = x * card[HC_SX] + y * card[HC_SY] + z * card[HC_SZ];
             rs_p = x * b.S[0] + y * b.S[1] + z * b.S[2];
@@ -1529,9 +1550,11 @@ struct Sys {
                 const double factor1 = vr * P(PC_C13);
                 const double radial = P(PC_CONS) + factor1 * t12;
                 const double factor3 = radial + ospd * vr;
-                const double F0 = factor3 * xd + osd * (hS1 * z - hS2 * y - hv0) + opd * (S1 * z - S2 * y - hv0);
-                const double F1 = factor3 * yd + osd * (hS2 * x - hS0 * z - hv1) + opd * (S2 * x - S0 * z - hv1);
-                const double F2 = factor3 * zd + osd * (hS0 * y - hS1 * x - hv2) + opd * (S0 * y - S1 * x - hv2);
+                // osd (S_h x r - v) + opd (S_p x r - v) = (osd S_h + opd S_p) x r - ospd v
+                const double w0 = osd * hS0 + opd * S0, w1 = osd * hS1 + opd * S1, w2 = osd * hS2 + opd * S2;
+                const double F0 = factor3 * xd + (w1 * z - w2 * y) - ospd * hv0;
+                const double F1 = factor3 * yd + (w2 * x - w0 * z) - ospd * hv1;
+                const double F2 = factor3 * zd + (w0 * y - w1 * x) - ospd * hv2;
                 aa0 += inv_m * F0; aa1 += inv_m * F1; aa2 += inv_m * F2;
                 const double qp = P(PC_OP) * rs_p, qs = os_ * rs_s;
                 const double opdd = P(PC_OPDD);
@@ -1562,16 +1585,10 @@ struct Sys {
             }
             if (grk() && b.gk == POSI_EFFECT_ORBITING) {
                 const double vr2 = vr * vr;
-                // first order: ortho / |v| = E v_r
-                const double radial1 = P(PC_A) * (P(PC_B) * nv2 - P(PC_C) - P(PC_DD) * vr2);
-                const double o1 = P(PC_E) * vr;
-                // second order
-                const double nv4 = nv2 * nv2;
-                const double vr4 = vr2 * vr2;
-                const double radial2 = P(PC_A) * (P(PC_T1) + P(PC_K2C) * nv4 + P(PC_K3C) * vr4 - P(PC_K4C) * vr2 * nv2 -
-                                                  P(PC_K5C) * nv2 - P(PC_K6C) * vr2);
-                const double ortho2 = P(PC_A05) * vr * (P(PC_P) * nv2 - P(PC_Q) - P(PC_R3) * vr2);
-                const double rad = radial1 + radial2, ort = o1 + ortho2;
+                // first + second order (the combined constants of planet_constants)
+                const double rad = P(PC_A) * (P(PC_GR0) + nv2 * (P(PC_GR1) + P(PC_K2C) * nv2 - P(PC_K4C) * vr2) +
+                                              vr2 * (P(PC_GR2) + P(PC_K3C) * vr2));
+                const double ort = vr * (P(PC_GO0) + P(PC_GO1) * nv2 + P(PC_GO2) * vr2);
                 double g0 = rad * xd + ort * hv0;
                 double g1 = rad * yd + ort * hv1;
                 double g2 = rad * zd + ort * hv2;
@@ -1594,20 +1611,26 @@ struct Sys {
                 g1 += kFA * (e1y - (hv2 * e7x - hv0 * e7z) + v3 * (nn2 * e3sx - nn0 * e3sz));
                 g2 += kFA * (e1z - (hv0 * e7y - hv1 * e7x) + v3 * (nn0 * e3sy - nn1 * e3sx));
                 aa0 += g0; aa1 += g1; aa2 += g2;
-                // Kidder 1995 eq. 2.4a / 2.4b
-                const double mu = P(PC_MU), fm = P(PC_FM), fm2 = P(PC_FM2);
-                const double lo0 = mu * h0, lo1 = mu * h1, lo2 = mu * h2;
-                const double h2x = pL1 * sL2 - pL2 * sL1;
-                const double h2y = pL2 * sL0 - pL0 * sL2;
-                const double h2z = pL0 * sL1 - pL1 * sL0;
+                // Kidder 1995 eq. 2.4a / 2.4b.  With L_o = mu (r x v) the
+                // torques are fm (L_o x S_h) - (L_p x S_h) + 3 (n.L_p) (n x S_h)
+                // on the host and fm2 (L_o x L_p) + (L_p x S_h) + 3 (n.S_h) (n x L_p)
+                // on the planet; the cross product is linear in its first
+                // argument, so each is one cross product of a combined vector.
                 const double sp3 = 3. * (nn0 * pL0 + nn1 * pL1 + nn2 * pL2);
                 const double ss3 = 3. * (nn0 * sL0 + nn1 * sL1 + nn2 * sL2);
-                th0 += kFA * (fm * (lo1 * sL2 - lo2 * sL1) - h2x + sp3 * (nn1 * sL2 - nn2 * sL1));
-                th1 += kFA * (fm * (lo2 * sL0 - lo0 * sL2) - h2y + sp3 * (nn2 * sL0 - nn0 * sL2));
-                th2 += kFA * (fm * (lo0 * sL1 - lo1 * sL0) - h2z + sp3 * (nn0 * sL1 - nn1 * sL0));
-                dl0 += kFA * (fm2 * (lo1 * pL2 - lo2 * pL1) + h2x + ss3 * (nn1 * pL2 - nn2 * pL1));
-                dl1 += kFA * (fm2 * (lo2 * pL0 - lo0 * pL2) + h2y + ss3 * (nn2 * pL0 - nn0 * pL2));
-                dl2 += kFA * (fm2 * (lo0 * pL1 - lo1 * pL0) + h2z + ss3 * (nn0 * pL1 - nn1 * pL0));
+                const double fmu = P(PC_FMU), fm2mu = P(PC_FM2MU);
+                const double ws0 = fmu * h0 - pL0 + sp3 * nn0;
+                const double ws1 = fmu * h1 - pL1 + sp3 * nn1;
+                const double ws2 = fmu * h2 - pL2 + sp3 * nn2;
+                const double wp0 = fm2mu * h0 - sL0 + ss3 * nn0;
+                const double wp1 = fm2mu * h1 - sL1 + ss3 * nn1;
+                const double wp2 = fm2mu * h2 - sL2 + ss3 * nn2;
+                th0 += kFA * (ws1 * sL2 - ws2 * sL1);
+                th1 += kFA * (ws2 * sL0 - ws0 * sL2);
+                th2 += kFA * (ws0 * sL1 - ws1 * sL0);
+                dl0 += kFA * (wp1 * pL2 - wp2 * pL1);
+                dl1 += kFA * (wp2 * pL0 - wp0 * pL2);
+                dl2 += kFA * (wp0 * pL1 - wp1 * pL0);
             }
             if (disk_on && b.dk == POSI_EFFECT_ORBITING) {
                 // the host's share enters through the (m/M) a columns below
