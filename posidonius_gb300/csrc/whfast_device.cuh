@@ -92,6 +92,22 @@ __device__ __forceinline__ double pow_m1p5(double y) {
 struct DD {
     double hi, lo;
 };
+// a <= b for a squared distance a and a squared threshold b (neither
+// negative), decided on the bit patterns: the order of non-negative doubles
+// is that of their bits read as integers.  A NaN on either side gives false,
+// as the floating-point comparison does.
+__device__ __forceinline__ bool sq_le(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long kInf = 0x7ff0000000000000LL;
+    return ia <= ib && ib <= kInf && ia <= kInf;
+}
+// a > b on the same terms
+__device__ __forceinline__ bool sq_gt(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long kInf = 0x7ff0000000000000LL;
+    return ia > ib && ia <= kInf && ib <= kInf;
+}
+
 __device__ __forceinline__ DD dd_two_sum(double a, double b) {
     const double s = a + b;
     const double bb = s - a;
@@ -235,6 +251,15 @@ enum {
 enum {
     PC_GR0 = PC_B, PC_GR1 = PC_C, PC_GR2 = PC_DD, PC_GO0 = PC_E, PC_GO1 = PC_T1, PC_GO2 = PC_K5C,
     PC_FMU = PC_FM, PC_FM2MU = PC_FM2
+};
+// Constants of a planet that hold for a whole launch when nothing evolves
+// (masses, radii, Love numbers and dissipation factors fixed): set at load,
+// or at each half kick of an evolving system (planet_launch_constants).
+enum {
+    PC_LT1 = PC_D8, PC_LT2 = PC_TERM1, PC_LCONS = PC_MHK2F,           // tides
+    PC_LMGS = PC_HMK2F, PC_LMGSC2 = PC_R5H, PC_LT1C = PC_R5P, PC_LCC = PC_D5, PC_LB = PC_K6C,
+    PC_LK5 = PC_A05, PC_LNDD = PC_P, PC_LK6 = PC_Q, PC_LQH = PC_R3, PC_LNEC = PC_MU,
+    PC_LNPH = PC_NN0, PC_LR3H = PC_NN1                                  // Kidder GR
 };
 #endif
 
@@ -463,6 +488,7 @@ struct Sys {
         disk_on = isc[6] != 0;
 #if !POSI_EXACT
         mass_constants();
+        if (!evo) launch_constants();
         pc_valid = false;
         pc_reuse = false;
 #endif
@@ -752,8 +778,14 @@ struct Sys {
         P(PC_X) = x;
         P(PC_Y) = y;
         P(PC_Z) = z;
+#if POSI_EXACT
         const double d = sqrt(powi<2>(x) + powi<2>(y) + powi<2>(z));
         const double inv_d = 1. / d;
+#else
+        const double d2 = powi<2>(x) + powi<2>(y) + powi<2>(z);
+        const double inv_d = rsqrt(d2);
+        const double d = d2 * inv_d;
+#endif
         P(PC_D) = d;
         P(PC_INV_D) = inv_d;
         P(PC_XD) = x * inv_d;
@@ -762,80 +794,56 @@ struct Sys {
     }
 
 #if !POSI_EXACT
-    // FAST: the same constants from powers of 1 / d and two reciprocals
-    // (1 / (m_host + m) and 1 / (mg_host + mg)) instead of a division each.
-    __device__ void planet_constants() {
-        const double hm = card[HC_M], hmg = card[HC_MG], hR = card[HC_R], hsig = card[HC_SIG];
-        const double hk2 = card[HC_K2], hk2f = card[HC_K2F];
-        const double id = P(PC_INV_D);
-        const double id2 = id * id, id5 = id2 * id2 * id, id7 = id5 * id2;
+    // FAST: the distance-free factors of the constants once per launch
+    // (planet_launch_constants), the powers of 1 / d once per half kick.
+    __device__ void planet_launch_constants(double hm, double hmg, double hR, double hsig, double hk2,
+                                            double hk2f) {
         if (tides && b.tk == POSI_EFFECT_ORBITING) {
             // src/effects/tides/constant_time_lag.rs:229-264, :266-307
             const double hm2 = hm * hm, m2 = b.m * b.m;
             const double term1 = m2 * powi<10>(hR) * hsig;
             const double term2 = hm2 * powi<10>(b.R) * b.sig;
-            const double o_s = 4.5 * term1 * id7;
-            const double o_p = 4.5 * term2 * id7;
-            P(PC_OS) = o_s;
-            P(PC_OP) = o_p;
-            P(PC_OSD) = o_s * id;
-            P(PC_OPD) = o_p * id;
-            P(PC_CONS) = kMINUS_3K2 * id7 * (m2 * powi<5>(hR) * hk2 + hm2 * powi<5>(b.R) * b.k2);
+            P(PC_LT1) = 4.5 * term1;
+            P(PC_LT2) = 4.5 * term2;
+            P(PC_LCONS) = kMINUS_3K2 * (m2 * powi<5>(hR) * hk2 + hm2 * powi<5>(b.R) * b.k2);
             P(PC_TERM2) = term2;
-            P(PC_OSPD) = (o_s + o_p) * id;
-            const double d = P(PC_D);
-            P(PC_OSDD) = o_s * d;
-            P(PC_OPDD) = o_p * d;
-            P(PC_C13) = -13.5 * (id7 * id);
             P(PC_T12) = term1 + term2;
         }
         if (flat && b.fk == POSI_EFFECT_ORBITING) {
             // src/effects/rotational_flattening/oblate_spheroid.rs:12-60
-            P(PC_N3D5) = -3. * id5;
-            P(PC_F15D7) = 15. * id7;
             // factor_star = cfs |Omega_host|^2, ortho_star = cofs (r . Omega_host(previous))
-            const double cfs = b.m * hk2f * powi<5>(hR) * (1. / 6.);
-            const double cfp = hm * b.k2f * powi<5>(b.R) * (1. / 6.);
-            P(PC_CFS) = cfs;
-            P(PC_CFP) = cfp;
-            P(PC_COFS) = -6. * cfs * id5;
-            P(PC_COFP) = -6. * cfp * id5;
+            P(PC_CFS) = b.m * hk2f * powi<5>(hR) * (1. / 6.);
+            P(PC_CFP) = hm * b.k2f * powi<5>(b.R) * (1. / 6.);
         }
         if (grk() && b.gk == POSI_EFFECT_ORBITING) {
-            // src/effects/general_relativity.rs:98, :187-298, :300-456
+            // src/effects/general_relativity.rs:98, :187-298, :300-456.
+            // The first- and second-order terms are one polynomial in |v|^2
+            // and v_r^2:
+            //   radial = A (GR0 + |v|^2 (GR1 + K2C |v|^2 - K4C v_r^2) + v_r^2 (GR2 + K3C v_r^2)),
+            //   ortho  = v_r (GO0 + GO1 |v|^2 + GO2 v_r^2),
+            // GR0 = T1 - C, GR1 = B - K5C, GR2 = -(DD + K6C), GO0 = E - A05 Q,
+            // GO1 = A05 P, GO2 = -A05 R3 in the terms of the reference's two
+            // orders; with mgd = (mg_host + mg) / d and A = -mgd / (c^2 d)
+            // every one is a launch constant times a power of mgd and A.
             const double mgs = hmg + b.mg;
             const double imgs = 1. / mgs;
             const double f = hmg * b.mg * (imgs * imgs);
-            const double mgd = mgs * id;
             const double f2 = f * f;
-            const double gd2 = mgs * id2 * (1. / kC2);
-            const double A = -gd2;
-            // The first- and second-order terms as one polynomial in |v|^2
-            // and v_r^2 (general_relativity.rs:187-298):
-            //   radial = A (GR0 + |v|^2 (GR1 + K2C |v|^2 - K4C v_r^2) + v_r^2 (GR2 + K3C v_r^2)),
-            //   ortho  = v_r (GO0 + GO1 |v|^2 + GO2 v_r^2)
-            // with GR0 = T1 - C, GR1 = B - K5C, GR2 = -(DD + K6C),
-            // GO0 = E - A05 Q, GO1 = A05 P, GO2 = -A05 R3 in the terms of the
-            // reference's two orders.
-            const double c_b = 1.0 + 3.0 * f, c_c = 2.0 * (2.0 + f) * mgd, c_dd = 1.5 * f;
-            const double c_e = gd2 * 2.0 * (2.0 - f);
-            const double c_t1 = (3.0 / 4.0) * (12.0 + 29.0 * f) * (mgd * mgd);
-            const double c_k5 = 0.5 * f * (13.0 - 4.0 * f) * mgd;
-            const double c_k6 = (2.0 + 25.0 * f + 2.0 * f2) * mgd;
-            const double a05 = A * (-0.5);
-            const double c_p = f * (15.0 + 4.0 * f);
-            const double c_q = (4.0 + 41.0 * f + 8.0 * f2) * mgd;
-            const double c_r3 = 3.0 * f * (3.0 + 2.0 * f);
-            P(PC_A) = A;
-            P(PC_GR0) = c_t1 - c_c;
-            P(PC_GR1) = c_b - c_k5;
-            P(PC_GR2) = -(c_dd + c_k6);
+            P(PC_LMGS) = mgs;
+            P(PC_LMGSC2) = -mgs * (1. / kC2);
+            P(PC_LT1C) = (3.0 / 4.0) * (12.0 + 29.0 * f);   // T1 / mgd^2
+            P(PC_LCC) = 2.0 * (2.0 + f);                     // C / mgd
+            P(PC_LB) = 1.0 + 3.0 * f;                        // B
+            P(PC_LK5) = 0.5 * f * (13.0 - 4.0 * f);          // K5C / mgd
+            P(PC_LNDD) = -1.5 * f;                           // -DD
+            P(PC_LK6) = 2.0 + 25.0 * f + 2.0 * f2;           // K6C / mgd
+            P(PC_LQH) = 0.5 * (4.0 + 41.0 * f + 8.0 * f2);   // Q / (2 mgd)
+            P(PC_LNEC) = -2.0 * (2.0 - f);                   // -E / (-A)
+            P(PC_LNPH) = -0.5 * (f * (15.0 + 4.0 * f));      // -P / 2
+            P(PC_LR3H) = 0.5 * (3.0 * f * (3.0 + 2.0 * f));  // R3 / 2
             P(PC_K2C) = f * (3.0 - 4.0 * f);
             P(PC_K3C) = (15.0 / 8.0) * f * (1.0 - 3.0 * f);
             P(PC_K4C) = (3.0 / 2.0) * f * (3.0 - 4.0 * f);
-            P(PC_GO0) = c_e - a05 * c_q;
-            P(PC_GO1) = a05 * c_p;
-            P(PC_GO2) = -a05 * c_r3;
             const double M = hm + b.m;
             const double iM = 1. / M;
             const double mu = (hm * b.m) * iM;
@@ -844,15 +852,58 @@ struct Sys {
             // mu (r x v) enters the torques scaled by these
             P(PC_FMU) = (2. + (3. / 2.) * b.m * inv_hm) * mu;
             P(PC_FM2MU) = (2. + (3. / 2.) * hm * inv_m) * mu;
-            const double n0 = P(PC_XD), n1 = P(PC_YD), n2 = P(PC_ZD);
-            P(PC_NN0) = n0;
-            P(PC_NN1) = n1;
-            P(PC_NN2) = n2;
-            P(PC_C6NN0) = 6. * n0;
-            P(PC_C6NN1) = 6. * n1;
-            P(PC_C6NN2) = 6. * n2;
         }
         P(PC_MRATIO) = b.m * hm == 0. ? 0. : b.m * inv_hm;
+    }
+
+    // the launch constants from the host's values, at load (every lane of
+    // the group takes part)
+    __device__ void launch_constants() {
+        const double hR = gbcast(has ? b.R : 0., host), hsig = gbcast(has ? b.sig : 0., host);
+        const double hk2 = gbcast(has ? b.k2 : 0., host), hk2f = gbcast(has ? b.k2f : 0., host);
+        const double hm = gbcast(has ? b.m : 0., host), hmg = gbcast(has ? b.mg : 0., host);
+        if (planet()) planet_launch_constants(hm, hmg, hR, hsig, hk2, hk2f);
+    }
+
+    __device__ void planet_constants() {
+        if (evo)
+            planet_launch_constants(card[HC_M], card[HC_MG], card[HC_R], card[HC_SIG], card[HC_K2], card[HC_K2F]);
+        const double id = P(PC_INV_D);
+        const double id2 = id * id, id5 = id2 * id2 * id, id7 = id5 * id2;
+        if (tides && b.tk == POSI_EFFECT_ORBITING) {
+            const double o_s = P(PC_LT1) * id7;
+            const double o_p = P(PC_LT2) * id7;
+            P(PC_OS) = o_s;
+            P(PC_OP) = o_p;
+            P(PC_OSD) = o_s * id;
+            P(PC_OPD) = o_p * id;
+            P(PC_CONS) = P(PC_LCONS) * id7;
+            P(PC_OSPD) = (o_s + o_p) * id;
+            const double d = P(PC_D);
+            P(PC_OSDD) = o_s * d;
+            P(PC_OPDD) = o_p * d;
+            P(PC_C13) = -13.5 * (id7 * id);
+        }
+        if (flat && b.fk == POSI_EFFECT_ORBITING) {
+            P(PC_N3D5) = -3. * id5;
+            P(PC_F15D7) = 15. * id7;
+            P(PC_COFS) = -6. * P(PC_CFS) * id5;
+            P(PC_COFP) = -6. * P(PC_CFP) * id5;
+        }
+        if (grk() && b.gk == POSI_EFFECT_ORBITING) {
+            const double mgd = P(PC_LMGS) * id;
+            const double A = P(PC_LMGSC2) * id2;
+            P(PC_A) = A;
+            P(PC_GR0) = mgd * (P(PC_LT1C) * mgd - P(PC_LCC));
+            P(PC_GR1) = P(PC_LB) - P(PC_LK5) * mgd;
+            P(PC_GR2) = P(PC_LNDD) - P(PC_LK6) * mgd;
+            P(PC_GO0) = A * (P(PC_LQH) * mgd + P(PC_LNEC));
+            P(PC_GO1) = A * P(PC_LNPH);
+            P(PC_GO2) = A * P(PC_LR3H);
+            P(PC_C6NN0) = 6. * P(PC_XD);
+            P(PC_C6NN1) = 6. * P(PC_YD);
+            P(PC_C6NN2) = 6. * P(PC_ZD);
+        }
     }
 #else
     __device__ void planet_constants() {
@@ -1595,7 +1646,7 @@ struct Sys {
                 // spin-orbit
                 const double sL0 = card[HC_SLX], sL1 = card[HC_SLY], sL2 = card[HC_SLZ];
                 const double pL0 = b.moi * S0, pL1 = b.moi * S1, pL2 = b.moi * S2;
-                const double nn0 = P(PC_NN0), nn1 = P(PC_NN1), nn2 = P(PC_NN2);
+                const double nn0 = xd, nn1 = yd, nn2 = zd;
                 const double mfM = P(PC_MFM);
                 const double msx = mfM * (pL0 * inv_m - sL0 * inv_hm);
                 const double msy = mfM * (pL1 * inv_m - sL1 * inv_hm);
@@ -2148,8 +2199,14 @@ struct Sys {
     __device__ void kepler_individual_step(double mass_g, double kdt) {
         const double p0 = b.ap[0], p1 = b.ap[1], p2 = b.ap[2];
         const double w0 = b.av[0], w1 = b.av[1], w2 = b.av[2];
+#if POSI_EXACT
         const double r0 = sqrt(powi<2>(p0) + powi<2>(p1) + powi<2>(p2));
         const double r0i = 1. / r0;
+#else
+        const double r02 = powi<2>(p0) + powi<2>(p1) + powi<2>(p2);
+        const double r0i = rsqrt(r02);
+        const double r0 = r02 * r0i;
+#endif
         const double v2 = powi<2>(w0) + powi<2>(w1) + powi<2>(w2);
         const double beta = 2. * mass_g * r0i - v2;
         const double eta0 = p0 * w0 + p1 * w1 + p2 * w2;
@@ -2377,9 +2434,16 @@ struct Sys {
                 const double dz = b.r[2] - X(4, j);
                 const double distance_2 = dx * dx + dy * dy + dz * dz;
                 if (i < j && code == 0) {
+#if POSI_EXACT
                     if (distance_2 <= powi<2>(ro[j])) { code = POSI_SYS_ROCHE; ev_pair = i * 1024 + j; }
                     else if (distance_2 <= powi<2>(b.R + X(5, j))) { code = POSI_SYS_COLLISION; ev_pair = i * 1024 + j; }
                     else if (kMAX_DISTANCE_2 > 0. && i == mm && distance_2 > kMAX_DISTANCE_2) { code = POSI_SYS_EJECTED; ev_pair = i * 1024 + j; }
+#else
+                    // the same tests on the bit patterns (sq_le), off the FP64 pipe
+                    if (sq_le(distance_2, powi<2>(ro[j]))) { code = POSI_SYS_ROCHE; ev_pair = i * 1024 + j; }
+                    else if (sq_le(distance_2, powi<2>(b.R + X(5, j)))) { code = POSI_SYS_COLLISION; ev_pair = i * 1024 + j; }
+                    else if (kMAX_DISTANCE_2 > 0. && i == mm && sq_gt(distance_2, kMAX_DISTANCE_2)) { code = POSI_SYS_EJECTED; ev_pair = i * 1024 + j; }
+#endif
                 }
                 if (ignore_terms == 1 &&
                     ((i == mm && mm == 0 && j == 1) || (i == mm && mm > 0 && j == 0) ||
