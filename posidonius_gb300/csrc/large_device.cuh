@@ -271,6 +271,7 @@ __device__ bool grid_scan(const LDev& D, const double (&vals)[NS], int nslots, d
 
 struct BodyConst {
     double m, mg, R, moi, sig, k2, k2f;
+    double inv_moi;  // 1 / moi (0 for a body without moment of inertia)
     int tk, fk, gk;
 };
 
@@ -284,6 +285,7 @@ __device__ __forceinline__ BodyConst load_const(const LDev& D, int64_t i) {
     c.sig = D.bf[POSI_BF_SIGMA * n + i];
     c.k2 = D.bf[POSI_BF_K2 * n + i];
     c.k2f = D.bf[POSI_BF_K2F * n + i];
+    c.inv_moi = c.moi != 0. ? 1. / c.moi : 0.;
     c.tk = (int)D.bi[POSI_BI_TIDES_KIND * n + i];
     c.fk = (int)D.bi[POSI_BI_FLAT_KIND * n + i];
     c.gk = (int)D.bi[POSI_BI_GR_KIND * n + i];
@@ -517,7 +519,7 @@ struct Large {
 
     __device__ static void spin_of(const BodyConst& k, const double L[3], double S[3]) {
         if (k.moi != 0.) {
-            const double im = 1. / k.moi;
+            const double im = k.inv_moi;
             for (int q = 0; q < 3; ++q) S[q] = L[q] * im;
         } else {
             for (int q = 0; q < 3; ++q) S[q] = 0.;
@@ -525,7 +527,7 @@ struct Large {
     }
 
     __device__ static void dspin_of(const BodyConst& k, const double dL[3], double dS[3]) {
-        const double im = k.moi != 0. ? 1. / k.moi : 0.;
+        const double im = k.inv_moi;
         for (int q = 0; q < 3; ++q) dS[q] = dL[q] * im;
     }
 
@@ -655,11 +657,44 @@ struct Large {
                     vals[tslot(6, q)] = mr * taa[q];
                     vals[tslot(6, 3 + q)] = tth[q];
                 }
+            // A planet's final values of this iteration need no reduction
+            // (only the host's do), so without tangents the convergence sums
+            // and the barycentre sums over the planets travel in the same
+            // reduction as the host's back-reactions (slots 6-15), and every
+            // thread adds the host's terms afterwards: one reduction per
+            // iteration.  The tangent engine reduces them separately, adding
+            // the host's terms the same way, so its primal state keeps the
+            // plain engine's bits.
+            const bool ctest = it >= kMIDPOINT_MIN - 1;
+            constexpr bool kMerged = NT == 0;
+            if (kMerged && ctest) {
+                if (planet) {
+                    double cvf[3], cLf[3];
+                    for (int q = 0; q < 3; ++q) {
+                        cvf[q] = v0[q] + (hdt * aa[q] - b.ev[q]);
+                        cLf[q] = L0[q] + (hdt * dl[q] - b.eL[q]);
+                        vals[6] += (cvf[q] - pv[q]) * (cvf[q] - pv[q]);
+                        vals[7] += cvf[q] * cvf[q];
+                        vals[8] += (cLf[q] - pL[q]) * (cLf[q] - pL[q]);
+                        vals[9] += cLf[q] * cLf[q];
+                        if (cm) vals[13 + q] = c.m * cvf[q];
+                    }
+                }
+                if (cm && has)
+                    for (int q = 0; q < 3; ++q) vals[10 + q] = c.m * b.r[q];
+            }
+            const int nred = kMerged && ctest ? (cm ? 16 : 10) : 6 + 6 * NT;
             double tot[NS];
-            if (!grid_reduce(D, vals, 6 + 6 * NT, tot, shm, warp_bodies, body_rows, rseq)) return false;
-            // the host's outputs, computed by every thread
+            if (!grid_reduce(D, vals, nred, tot, shm, warp_bodies, body_rows, rseq)) return false;
+            // the host's outputs and final values, computed by every thread
             double haa[3], hdl[3];
-            for (int q = 0; q < 3; ++q) { haa[q] = -tot[q]; hdl[q] = tot[3 + q]; }
+            for (int q = 0; q < 3; ++q) {
+                haa[q] = -tot[q]; hdl[q] = tot[3 + q];
+                hdvc[q] = hdt * haa[q] - h.ev[q];
+                hvf[q] = hv0[q] + hdvc[q];
+                hdLc[q] = hdt * hdl[q] - h.eL[q];
+                hLf[q] = hL0[q] + hdLc[q];
+            }
             if (is_host)
                 for (int q = 0; q < 3; ++q) { aa[q] = haa[q]; dl[q] = hdl[q]; }
             if (has) for (int q = 0; q < 3; ++q) {
@@ -667,10 +702,6 @@ struct Large {
                 vf[q] = v0[q] + dvc[q];
                 dLc[q] = hdt * dl[q] - b.eL[q];
                 Lf[q] = L0[q] + dLc[q];
-                hdvc[q] = hdt * haa[q] - h.ev[q];
-                hvf[q] = hv0[q] + hdvc[q];
-                hdLc[q] = hdt * hdl[q] - h.eL[q];
-                hLf[q] = hL0[q] + hdLc[q];
             }
             if (tn && has)
                 for (int q = 0; q < 3; ++q) {
@@ -681,32 +712,62 @@ struct Large {
                     thvf[q] = HT.v[q] + hdt * thaa;
                     thLf[q] = HT.L[q] + hdt * thdl;
                 }
-            if (it >= kMIDPOINT_MIN - 1) {
-                double cv[NS] = {};
-                if (has) {
-                    if (primal_role())
-                        for (int q = 0; q < 3; ++q) {
-                            cv[0] += (vf[q] - pv[q]) * (vf[q] - pv[q]);
-                            cv[1] += vf[q] * vf[q];
-                            cv[2] += (Lf[q] - pL[q]) * (Lf[q] - pL[q]);
-                            cv[3] += Lf[q] * Lf[q];
-                            cv[4 + q] = c.m * b.r[q];
-                            cv[7 + q] = c.m * vf[q];
-                        }
-                    if (tn && cm)
-                        for (int q = 0; q < 3; ++q) {
-                            cv[tslot(10, q)] = c.m * T.r[q];
-                            cv[tslot(10, 3 + q)] = c.m * tvf[q];
-                        }
-                }
-                const int ns = cm ? 10 + 6 * NT : 4;
+            if (ctest) {
+                // s4: the planets' convergence sums (0-3) and, with cm, the
+                // sums of m r (4-6, host included) and of the planets' m v (7-9)
                 double s4[NS];
-                if (!grid_reduce(D, cv, ns, s4, shm, warp_bodies, body_rows, rseq)) return false;
-                if (cm) {
-                    for (int q = 0; q < 6; ++q) cm[q] = s4[4 + q];
-                    if (tn)
+                if (kMerged) {
+                    for (int k = 0; k < 10; ++k) s4[k] = tot[6 + k];
+                } else {
+                    double cv[NS] = {};
+                    if (has) {
+                        if (primal_role())
+                            for (int q = 0; q < 3; ++q) {
+                                if (planet) {
+                                    cv[0] += (vf[q] - pv[q]) * (vf[q] - pv[q]);
+                                    cv[1] += vf[q] * vf[q];
+                                    cv[2] += (Lf[q] - pL[q]) * (Lf[q] - pL[q]);
+                                    cv[3] += Lf[q] * Lf[q];
+                                    cv[7 + q] = c.m * vf[q];
+                                }
+                                cv[4 + q] = c.m * b.r[q];
+                            }
+                        if (tn && cm)
+                            for (int q = 0; q < 3; ++q) {
+                                cv[tslot(10, q)] = c.m * T.r[q];
+                                cv[tslot(10, 3 + q)] = c.m * tvf[q];
+                            }
+                    }
+                    const int ns = cm ? 10 + 6 * NT : 4;
+                    if (!grid_reduce(D, cv, ns, s4, shm, warp_bodies, body_rows, rseq)) return false;
+                    if (tn && cm)
                         for (int q = 0; q < 6; ++q) tcm[q] = s4[tslot(10, q)];
                 }
+                // the host's terms, added by the block's first thread (a body:
+                // its copy of the host's state is current) and shared, so that
+                // every thread of the block takes the same branch
+                const int nsh = cm ? 10 : 4;
+                double* bc = shm + (kBlock / 32) * BP_ROW;
+                if (threadIdx.x == 0) {
+                    double hc4[4] = {0., 0., 0., 0.};
+                    for (int q = 0; q < 3; ++q) {
+                        hc4[0] += (hvf[q] - hpv[q]) * (hvf[q] - hpv[q]);
+                        hc4[1] += hvf[q] * hvf[q];
+                        hc4[2] += (hLf[q] - hpL[q]) * (hLf[q] - hpL[q]);
+                        hc4[3] += hLf[q] * hLf[q];
+                    }
+                    for (int k = 0; k < 4; ++k) bc[k] = s4[k] + hc4[k];
+                    if (cm)
+                        for (int q = 0; q < 3; ++q) {
+                            bc[4 + q] = s4[4 + q];
+                            bc[7 + q] = s4[7 + q] + hc.m * hvf[q];
+                        }
+                }
+                __syncthreads();
+                for (int k = 0; k < nsh; ++k) s4[k] = bc[k];
+                __syncthreads();
+                if (cm)
+                    for (int q = 0; q < 6; ++q) cm[q] = s4[4 + q];
                 if (s4[0] / s4[1] < kDBL_EPSILON_2 && (s4[3] == 0. || s4[2] / s4[3] < kDBL_EPSILON_2)) break;
             }
             if (has) for (int q = 0; q < 3; ++q) {
@@ -824,14 +885,69 @@ struct Large {
 
     // Kepler drift of a planet over half_dt, with the tangent (the implicit
     // derivative at the converged root).
+    // The universal-variable drift of kepler_solve / kepler_apply with fewer
+    // FP64 instructions on the body's chain: 1 / r0 from rsqrt, the
+    // G-functions of the root from the last Newton iterate's by a
+    // second-order Taylor step (the iterate is within 1e-8 of the root, so
+    // the neglected third order is below 1e-24 relative), one reciprocal of
+    // r instead of three divisions.
     __device__ void kepler(double x[3], double u[3], double tx[3], double tu[3]) {
         if (planet) {
-            const KeplerScalars ks = kepler_scalars(kgm, x, u);
+            const double mu = kgm, dt = half_dt;
+            const double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+            const double ir0 = rsqrt(r2);
+            const double r0 = r2 * ir0;
+            const double v2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+            const double beta = 2. * mu * ir0 - v2;
+            const double eta0 = x[0] * u[0] + x[1] * u[1] + x[2] * u[2];
+            const double zeta0 = mu - beta * r0;
+            double X = 0.;
+            if (beta > 0.) {
+                const double uu = dt * ir0;
+                const double a2 = -0.5 * eta0 * ir0;
+                const double a3 = (0.5 * eta0 * eta0 * ir0 - zeta0 * (1. / 6.)) * ir0;
+                const double a4 = -(eta0 * a3 + 0.5 * eta0 * a2 * a2 + 0.5 * zeta0 * a2 - eta0 * beta * (1. / 24.)) * ir0;
+                X = uu * (1. + uu * (a2 + uu * (a3 + uu * a4)));
+            }
             bool ok = false;
-            const double X = kepler_solve(ks, half_dt, &ok);
-            if (!ok) atomicOr(D.err, LE_KEPLER);
+            double G0 = 1., G1 = 0., G2 = 0., G3 = 0.;
+            for (int it = 0; it < kKEPLER_MAX_NEWTON; ++it) {
+                double c[4];
+                stumpff4(beta * X * X, c);
+                const double X2 = X * X;
+                G0 = c[0]; G1 = X * c[1]; G2 = X2 * c[2]; G3 = X2 * X * c[3];
+                const double F = r0 * X + eta0 * G2 + zeta0 * G3 - dt;
+                const double Fp = r0 + eta0 * G1 + zeta0 * G2;
+                const double dX = F / Fp;
+                X -= dX;
+                if (fabs(dX) <= 1e-8 * fabs(X) || dX == 0.) {
+                    // dG0 = -beta G1, dG1 = G0, dG2 = G1, dG3 = G2 per unit X
+                    const double e = -dX, e2h = 0.5 * e * e;
+                    const double n0 = G0 - beta * (G1 * e + G0 * e2h);
+                    const double n1 = G1 + G0 * e - beta * G1 * e2h;
+                    const double n2 = G2 + G1 * e + G0 * e2h;
+                    const double n3 = G3 + G2 * e + G1 * e2h;
+                    G0 = n0; G1 = n1; G2 = n2; G3 = n3;
+                    ok = true;
+                    break;
+                }
+            }
+            if (!ok) {
+                atomicOr(D.err, LE_KEPLER);
+                double c[4];
+                stumpff4(beta * X * X, c);
+                G0 = c[0]; G1 = X * c[1]; G2 = X * X * c[2]; G3 = X * X * X * c[3];
+            }
+            const double irr = 1. / (r0 + eta0 * G1 + zeta0 * G2);
+            const double f = -mu * G2 * ir0;
+            const double g = dt - mu * G3;
+            const double fd = -mu * G1 * ir0 * irr;
+            const double gd = -mu * G2 * irr;
             double r1[3], v1[3];
-            kepler_apply(kgm, half_dt, x, u, ks, X, r1, v1);
+            for (int k = 0; k < 3; ++k) {
+                r1[k] = x[k] + (f * x[k] + g * u[k]);
+                v1[k] = u[k] + (fd * x[k] + gd * u[k]);
+            }
             if (tan_on()) {
                 double e1[3], f1[3];
                 kepler_jvp(kgm, half_dt, x, u, X, tx, tu, e1, f1);

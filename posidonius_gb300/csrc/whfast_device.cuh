@@ -259,7 +259,7 @@ enum {
     PC_LT1 = PC_D8, PC_LT2 = PC_TERM1, PC_LCONS = PC_MHK2F,           // tides
     PC_LMGS = PC_HMK2F, PC_LMGSC2 = PC_R5H, PC_LT1C = PC_R5P, PC_LCC = PC_D5, PC_LB = PC_K6C,
     PC_LK5 = PC_A05, PC_LNDD = PC_P, PC_LK6 = PC_Q, PC_LQH = PC_R3, PC_LNEC = PC_MU,
-    PC_LNPH = PC_NN0, PC_LR3H = PC_NN1                                  // Kidder GR
+    PC_LNPH = PC_NN0, PC_LR3H = PC_NN1, PC_LMA = PC_NN2, PC_LMB = PC_MFM  // Kidder GR
 };
 #endif
 
@@ -847,7 +847,9 @@ struct Sys {
             const double M = hm + b.m;
             const double iM = 1. / M;
             const double mu = (hm * b.m) * iM;
-            P(PC_MFM) = hm - b.m;                    // ((m_host - m) / M) M
+            // ((m_host - m) / M) M (L_p / m - L_h / m_h) = LMA S_p - LMB L_h
+            P(PC_LMA) = (hm - b.m) * b.moi * inv_m;
+            P(PC_LMB) = (hm - b.m) * inv_hm;
             // Kidder 1995 eq. 2.4a / 2.4b: the orbital angular momentum
             // mu (r x v) enters the torques scaled by these
             P(PC_FMU) = (2. + (3. / 2.) * b.m * inv_hm) * mu;
@@ -900,9 +902,10 @@ struct Sys {
             P(PC_GO0) = A * (P(PC_LQH) * mgd + P(PC_LNEC));
             P(PC_GO1) = A * P(PC_LNPH);
             P(PC_GO2) = A * P(PC_LR3H);
-            P(PC_C6NN0) = 6. * P(PC_XD);
-            P(PC_C6NN1) = 6. * P(PC_YD);
-            P(PC_C6NN2) = 6. * P(PC_ZD);
+            const double id6 = 6. * id;
+            P(PC_C6NN0) = id6 * P(PC_XD);
+            P(PC_C6NN1) = id6 * P(PC_YD);
+            P(PC_C6NN2) = id6 * P(PC_ZD);
         }
     }
 #else
@@ -1584,6 +1587,12 @@ struct Sys {
             const double h0 = y * hv2 - z * hv1;
             const double h1 = z * hv0 - x * hv2;
             const double h2 = x * hv1 - y * hv0;
+            // S_p x r and S_h x r (tidal force, flattening torques)
+            double cS0 = 0., cS1 = 0., cS2 = 0., chS0 = 0., chS1 = 0., chS2 = 0.;
+            if ((tides && b.tk == POSI_EFFECT_ORBITING) || (flat && b.fk == POSI_EFFECT_ORBITING)) {
+                cS0 = S1 * z - S2 * y; cS1 = S2 * x - S0 * z; cS2 = S0 * y - S1 * x;
+                chS0 = hS1 * z - hS2 * y; chS1 = hS2 * x - hS0 * z; chS2 = hS0 * y - hS1 * x;
+            }
             if (tides && b.tk == POSI_EFFECT_ORBITING) {
                 double osd = P(PC_OSD), t12 = P(PC_T12), ospd = P(PC_OSPD), os_ = P(PC_OS), osdd = P(PC_OSDD);
                 const double opd = P(PC_OPD);
@@ -1601,11 +1610,10 @@ struct Sys {
                 const double factor1 = vr * P(PC_C13);
                 const double radial = P(PC_CONS) + factor1 * t12;
                 const double factor3 = radial + ospd * vr;
-                // osd (S_h x r - v) + opd (S_p x r - v) = (osd S_h + opd S_p) x r - ospd v
-                const double w0 = osd * hS0 + opd * S0, w1 = osd * hS1 + opd * S1, w2 = osd * hS2 + opd * S2;
-                const double F0 = factor3 * xd + (w1 * z - w2 * y) - ospd * hv0;
-                const double F1 = factor3 * yd + (w2 * x - w0 * z) - ospd * hv1;
-                const double F2 = factor3 * zd + (w0 * y - w1 * x) - ospd * hv2;
+                // osd (S_h x r - v) + opd (S_p x r - v)
+                const double F0 = factor3 * xd + (osd * chS0 + opd * cS0) - ospd * hv0;
+                const double F1 = factor3 * yd + (osd * chS1 + opd * cS1) - ospd * hv1;
+                const double F2 = factor3 * zd + (osd * chS2 + opd * cS2) - ospd * hv2;
                 aa0 += inv_m * F0; aa1 += inv_m * F1; aa2 += inv_m * F2;
                 const double qp = P(PC_OP) * rs_p, qs = os_ * rs_s;
                 const double opdd = P(PC_OPDD);
@@ -1627,12 +1635,9 @@ struct Sys {
                 const double F1 = radial * y + ofp * S1 + ofs * hS1;
                 const double F2 = radial * z + ofp * S2 + ofs * hS2;
                 aa0 += inv_m * F0; aa1 += inv_m * F1; aa2 += inv_m * F2;
-                dl0 -= ofp * (y * S2 - z * S1);
-                dl1 -= ofp * (z * S0 - x * S2);
-                dl2 -= ofp * (x * S1 - y * S0);
-                th0 -= ofs * (y * hS2 - z * hS1);
-                th1 -= ofs * (z * hS0 - x * hS2);
-                th2 -= ofs * (x * hS1 - y * hS0);
+                // -ofp (r x S_p), -ofs (r x S_h)
+                dl0 += ofp * cS0; dl1 += ofp * cS1; dl2 += ofp * cS2;
+                th0 += ofs * chS0; th1 += ofs * chS1; th2 += ofs * chS2;
             }
             if (grk() && b.gk == POSI_EFFECT_ORBITING) {
                 const double vr2 = vr * vr;
@@ -1647,20 +1652,22 @@ struct Sys {
                 const double sL0 = card[HC_SLX], sL1 = card[HC_SLY], sL2 = card[HC_SLZ];
                 const double pL0 = b.moi * S0, pL1 = b.moi * S1, pL2 = b.moi * S2;
                 const double nn0 = xd, nn1 = yd, nn2 = zd;
-                const double mfM = P(PC_MFM);
-                const double msx = mfM * (pL0 * inv_m - sL0 * inv_hm);
-                const double msy = mfM * (pL1 * inv_m - sL1 * inv_hm);
-                const double msz = mfM * (pL2 * inv_m - sL2 * inv_hm);
+                // ((m_h - m) / M) M (L_p / m - L_h / m_h) from the spins
+                const double ma = P(PC_LMA), mb = P(PC_LMB);
+                const double msx = ma * S0 - mb * sL0, msy = ma * S1 - mb * sL1, msz = ma * S2 - mb * sL2;
                 const double t0 = sL0 + pL0, t1 = sL1 + pL1, t2 = sL2 + pL2;
-                const double e1x = P(PC_C6NN0) * ((nn1 * hv2 - nn2 * hv1) * (2. * t0 + msx));
-                const double e1y = P(PC_C6NN1) * ((nn2 * hv0 - nn0 * hv2) * (2. * t1 + msy));
-                const double e1z = P(PC_C6NN2) * ((nn0 * hv1 - nn1 * hv0) * (2. * t2 + msz));
-                const double e7x = 7. * t0 + 3. * msx, e7y = 7. * t1 + 3. * msy, e7z = 7. * t2 + 3. * msz;
-                const double e3sx = 3. * t0 + msx, e3sy = 3. * t1 + msy, e3sz = 3. * t2 + msz;
-                const double v3 = 3. * vr;
-                g0 += kFA * (e1x - (hv1 * e7z - hv2 * e7y) + v3 * (nn1 * e3sz - nn2 * e3sy));
-                g1 += kFA * (e1y - (hv2 * e7x - hv0 * e7z) + v3 * (nn2 * e3sx - nn0 * e3sz));
-                g2 += kFA * (e1z - (hv0 * e7y - hv1 * e7x) + v3 * (nn0 * e3sy - nn1 * e3sx));
+                // (n x v)_k = (r x v)_k / d, the 6 n_k / d of planet_constants
+                const double e1x = P(PC_C6NN0) * (h0 * (2. * t0 + msx));
+                const double e1y = P(PC_C6NN1) * (h1 * (2. * t1 + msy));
+                const double e1z = P(PC_C6NN2) * (h2 * (2. * t2 + msz));
+                // -v x (7 t + 3 ms) + 3 v_r n x (3 t + ms) = a x t + 3 q x ms
+                // with q = v_r n - v and a = 7 q + 2 v_r n
+                const double q0 = vr * nn0 - hv0, q1 = vr * nn1 - hv1, q2 = vr * nn2 - hv2;
+                const double vr2x = 2. * vr;
+                const double a0 = 7. * q0 + vr2x * nn0, a1 = 7. * q1 + vr2x * nn1, a2 = 7. * q2 + vr2x * nn2;
+                g0 += kFA * (e1x + (a1 * t2 - a2 * t1) + 3. * (q1 * msz - q2 * msy));
+                g1 += kFA * (e1y + (a2 * t0 - a0 * t2) + 3. * (q2 * msx - q0 * msz));
+                g2 += kFA * (e1z + (a0 * t1 - a1 * t0) + 3. * (q0 * msy - q1 * msx));
                 aa0 += g0; aa1 += g1; aa2 += g2;
                 // Kidder 1995 eq. 2.4a / 2.4b.  With L_o = mu (r x v) the
                 // torques are fm (L_o x S_h) - (L_p x S_h) + 3 (n.L_p) (n x S_h)
@@ -1790,8 +1797,14 @@ struct Sys {
             if (has) {
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
+#if POSI_EXACT
                     b.v[k] = 0.5 * (ov[k] + fv[k]);
                     if (spin_on) b.L[k] = 0.5 * (oL[k] + fL[k]);
+#else
+                    // the midpoint as the start plus half the increment
+                    b.v[k] = ov[k] + 0.5 * dvc[k];
+                    if (spin_on) b.L[k] = oL[k] + 0.5 * dLc[k];
+#endif
                 }
             }
         }
