@@ -2277,14 +2277,40 @@ struct Sys {
         double old_x = x;
         stiefel_gs3(beta, x, gs);
         double e = eta0 * gs[1] + zeta0 * gs[2];
-        double ri = 1. / (r0 + e);
-        x = ri * (x * e - eta0 * gs[2] - zeta0 * gs[3] + kdt);
+        double ri;
 #if POSI_EXACT
+        ri = 1. / (r0 + e);
+        x = ri * (x * e - eta0 * gs[2] - zeta0 * gs[3] + kdt);
         const bool jumped = !xpp_nan && fabs(x - old_x) > 0.01 * x_per_period;
 #else
-        const bool jumped = !xpp_nan && fabs(x - old_x) * sqrt_beta > 0.02 * kPI;
+        // Halley's step from the series start (cubic: a start within 4e-6
+        // of the root lands within 1e-17 of it, below the rounding of x),
+        // then the G-functions at the new x by a second-order Taylor step
+        // (dG0 = -beta G1, dG1 = G0, dG2 = G1, dG3 = G2 per unit x).  Starts
+        // further off go on with the Newton iterations below.
+        {
+            const double fx = r0 * x + eta0 * gs[2] + zeta0 * gs[3] - kdt;
+            const double fp = r0 + e;
+            const double fpp = eta0 * gs[0] + zeta0 * gs[1];
+            const double dx = (2. * fx * fp) / (2. * fp * fp - fx * fpp);
+            x = x - dx;
+            if (fabs(dx) <= 4e-6 * fabs(x)) {
+                const double tt = -dx, th = 0.5 * tt * tt;
+                const double g0 = gs[0], g1 = gs[1], g2 = gs[2], g3 = gs[3];
+                gs[0] = g0 - beta * (g1 * tt + g0 * th);
+                gs[1] = g1 + g0 * tt - beta * g1 * th;
+                gs[2] = g2 + g1 * tt + g0 * th;
+                gs[3] = g3 + g2 * tt + g1 * th;
+                converged = 1;
+                e = eta0 * gs[1] + zeta0 * gs[2];
+                ri = 1. / (r0 + e);
+            }
+        }
+        const bool jumped = !converged && !xpp_nan && fabs(x - old_x) * sqrt_beta > 0.02 * kPI;
 #endif
-        if (jumped) {
+        if (converged) {
+            // Halley's step converged
+        } else if (jumped) {
             x = beta * kdt / mass_g;
             double prev_x[kNMAX_QUART + 1];
             for (int k = 0; k <= kNMAX_QUART; ++k) prev_x[k] = 0.;
@@ -2437,6 +2463,7 @@ struct Sys {
         sync();
         int code = 0, ev_pair = 0x7fffffff;
         double acc0 = 0., acc1 = 0., acc2 = 0.;
+#if POSI_EXACT
         if (has) {
             const int i = lane, mm = host;
             const double* ro = D.roche + (int64_t)s * D.nmax * D.nmax + (int64_t)i * D.nmax;
@@ -2447,41 +2474,97 @@ struct Sys {
                 const double dz = b.r[2] - X(4, j);
                 const double distance_2 = dx * dx + dy * dy + dz * dz;
                 if (i < j && code == 0) {
-#if POSI_EXACT
                     if (distance_2 <= powi<2>(ro[j])) { code = POSI_SYS_ROCHE; ev_pair = i * 1024 + j; }
                     else if (distance_2 <= powi<2>(b.R + X(5, j))) { code = POSI_SYS_COLLISION; ev_pair = i * 1024 + j; }
                     else if (kMAX_DISTANCE_2 > 0. && i == mm && distance_2 > kMAX_DISTANCE_2) { code = POSI_SYS_EJECTED; ev_pair = i * 1024 + j; }
-#else
-                    // the same tests on the bit patterns (sq_le), off the FP64 pipe
-                    if (sq_le(distance_2, powi<2>(ro[j]))) { code = POSI_SYS_ROCHE; ev_pair = i * 1024 + j; }
-                    else if (sq_le(distance_2, powi<2>(b.R + X(5, j)))) { code = POSI_SYS_COLLISION; ev_pair = i * 1024 + j; }
-                    else if (kMAX_DISTANCE_2 > 0. && i == mm && sq_gt(distance_2, kMAX_DISTANCE_2)) { code = POSI_SYS_EJECTED; ev_pair = i * 1024 + j; }
-#endif
                 }
                 if (ignore_terms == 1 &&
                     ((i == mm && mm == 0 && j == 1) || (i == mm && mm > 0 && j == 0) ||
                      (j == mm && mm == 0 && i == 1) || (j == mm && mm > 0 && i == 0)))
                     continue;
                 if (ignore_terms == 2 && (i == mm || j == mm)) continue;
-#if POSI_EXACT
                 const double distance = sqrt(distance_2);
                 const double prefact = -kG / (distance * distance * distance) * X(0, j);
-#else
-                const double ri = rsqrt(distance_2);
-                const double prefact = (ri * ri * ri) * X(0, j);
-#endif
                 acc0 += prefact * dx;
                 acc1 += prefact * dy;
                 acc2 += prefact * dz;
             }
             if (code) atomicMin(&isc[0], ev_pair);
         }
+#else
+        // Each unordered pair once: in round r lane k takes the pair
+        // (k, k + r mod n), adds its own term and hands the partner's to lane
+        // k + r by a shuffle; in the round r = n / 2 (n even) both lanes of
+        // a pair take their own term.  A lane checks the pairs it takes (the
+        // lower one in the round r = n / 2) and keeps its least (i, j).
+        {
+            const int mm = host;
+            const int64_t rbase = (int64_t)s * D.nmax * D.nmax;
+            for (int r = 1; 2 * r <= n; ++r) {
+                const bool hand = 2 * r < n;
+                double rx = 0., ry = 0., rz = 0.;
+                if (has) {
+                    int j = lane + r;
+                    if (j >= n) j -= n;
+                    const double dx = b.r[0] - X(2, j);
+                    const double dy = b.r[1] - X(3, j);
+                    const double dz = b.r[2] - X(4, j);
+                    const double distance_2 = dx * dx + dy * dy + dz * dz;
+                    if (hand || lane < j) {
+                        const int lo = lane < j ? lane : j, hi = lane < j ? j : lane;
+                        const int pair = lo * 1024 + hi;
+                        if (pair < ev_pair) {
+                            const double ro = D.roche[rbase + (int64_t)lo * D.nmax + hi];
+                            int c = 0;
+                            // the same tests on the bit patterns (sq_le), off the FP64 pipe
+                            if (sq_le(distance_2, powi<2>(ro))) c = POSI_SYS_ROCHE;
+                            else if (sq_le(distance_2, powi<2>(b.R + X(5, j)))) c = POSI_SYS_COLLISION;
+                            else if (kMAX_DISTANCE_2 > 0. && lo == mm && sq_gt(distance_2, kMAX_DISTANCE_2)) c = POSI_SYS_EJECTED;
+                            if (c) { code = c; ev_pair = pair; }
+                        }
+                    }
+                    const int i = lane;
+                    const bool skip =
+                        (ignore_terms == 1 &&
+                         ((i == mm && mm == 0 && j == 1) || (i == mm && mm > 0 && j == 0) ||
+                          (j == mm && mm == 0 && i == 1) || (j == mm && mm > 0 && i == 0))) ||
+                        (ignore_terms == 2 && (i == mm || j == mm));
+                    if (!skip) {
+                        const double ri = rsqrt(distance_2);
+                        const double ri3 = ri * ri * ri;
+                        const double prefact = ri3 * X(0, j);
+                        acc0 += prefact * dx;
+                        acc1 += prefact * dy;
+                        acc2 += prefact * dz;
+                        if (hand) {
+                            const double pk = -(ri3 * gm_neg);
+                            rx = pk * dx; ry = pk * dy; rz = pk * dz;
+                        }
+                    }
+                }
+                if (hand) {
+                    int src = lane - r;
+                    if (src < 0) src += n;
+                    if (!has) src = lane;
+                    const double gx = __shfl_sync(mask, rx, src, G);
+                    const double gy = __shfl_sync(mask, ry, src, G);
+                    const double gz = __shfl_sync(mask, rz, src, G);
+                    if (has) { acc0 += gx; acc1 += gy; acc2 += gz; }
+                }
+            }
+            if (code) atomicMin(&isc[0], ev_pair);
+        }
+#endif
         sync();
         const int first = isc[0];
         if (first != 0x7fffffff) {
             // the reference panics at the first offending pair in (i, j) order,
             // before it stores any acceleration
+#if POSI_EXACT
             if (has && lane == first / 1024) isc[4] = code;
+#else
+            if (has && code && ev_pair == first) isc[4] = code;
+#endif
             sync();
             set_fatal(isc[4], first / 1024, first % 1024);
         } else if (has) {
