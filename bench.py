@@ -780,9 +780,16 @@ def main():
     # lane mapping per body count: picked by the autotuner (state unchanged)
     lanes = batch.autotune(probe_steps=20) if not args.no_autotune else {
         int(n): batch.mapping_for(int(n)) for n in np.unique(ens["sys_i64"][:, L.SI_N])}
+    def probes(n):
+        # IAS15 batches take the smallest lane group without probing
+        try:
+            return {str(k): v for k, v in batch.autotune_report(n).items()}
+        except pg.PosiError:
+            return {}
+
     tuning = None if args.no_autotune else {
         str(n): {"systems": int(np.sum(ens["sys_i64"][:, L.SI_N] == n)), "chosen_lanes": int(g),
-                 "probe_ms_by_lanes": {str(k): v for k, v in batch.autotune_report(n).items()}}
+                 "probe_ms_by_lanes": probes(n)}
         for n, g in sorted(lanes.items())}
     K = args.steps
     W = max(3, args.warmup)
