@@ -190,8 +190,11 @@ def block_tides(g):
     factor1 = vr * (-13.5 / d8)
     radial = cons + factor1 * (term1 + term2)
     factor3 = radial + (o_s + o_p) * inv_d * vr
-    Hr, Sr = cross(H, r), cross(S, r)
-    F = [factor3 * rd[k] + osd * (Hr[k] - hv[k]) + opd * (Sr[k] - hv[k]) for k in range(3)]
+    # osd (H x r - v) + opd (S x r - v) = (osd H + opd S) x r - (osd + opd) v
+    w = [osd * H[k] + opd * S[k] for k in range(3)]
+    wr = cross(w, r)
+    ospd = (o_s + o_p) * inv_d
+    F = [factor3 * rd[k] + wr[k] - ospd * hv[k] for k in range(3)]
     inv_m = 1.0 / m
     a = [inv_m * F[k] for k in range(3)]
     opdd, osdd = o_p * d, o_s * d
@@ -255,43 +258,52 @@ def block_gr(g):
     Pc = f * (15.0 + 4.0 * f)
     Qc = (4.0 + 41.0 * f + 8.0 * f * f) * mgd
     R3 = 3.0 * f * (3.0 + 2.0 * f)
+    # the two orders as one polynomial in |v|^2 and v_r^2 (its coefficients
+    # depend on the position only)
+    GR0 = T1 - C
+    GR1 = B - K5C
+    GR2 = -(DD + K6C)
+    GO0 = E - A05 * Qc
+    GO1 = A05 * Pc
+    GO2 = -(A05 * R3)
     vr2 = vr * vr
-    radial1 = A * (B * nv2 - C - DD * vr2)
-    o1 = E * vr
-    nv4 = nv2 * nv2
-    vr4 = vr2 * vr2
-    radial2 = A * (T1 + K2C * nv4 + K3C * vr4 - K4C * vr2 * nv2 - K5C * nv2 - K6C * vr2)
-    ortho2 = A05 * vr * (Pc * nv2 - Qc - R3 * vr2)
-    rad = radial1 + radial2
-    ort = o1 + ortho2
+    rad = A * (GR0 + nv2 * (GR1 + K2C * nv2 - K4C * vr2) + vr2 * (GR2 + K3C * vr2))
+    ort = vr * (GO0 + GO1 * nv2 + GO2 * vr2)
     gacc = [rad * nn[k] + ort * hv[k] for k in range(3)]
-    # spin-orbit (general_relativity.rs:300-400, component-wise first term as written there)
+    # spin-orbit (general_relativity.rs:300-400, component-wise first term as
+    # written there): ms = ((m_h - m) / M) M (L_p / m - L_h / m_h)
     sL = [hmoi * H[k] for k in range(3)]
     pL = [moi * S[k] for k in range(3)]
     mfm = hm - m
-    ms = [mfm * (pL[k] / m - sL[k] / hm) for k in range(3)]
+    ma, mb = mfm * moi / m, mfm / hm
+    ms = [ma * S[k] - mb * sL[k] for k in range(3)]
     t = [sL[k] + pL[k] for k in range(3)]
-    nxv = cross(nn, hv)
-    e1 = [6.0 * nn[k] * (nxv[k] * (2.0 * t[k] + ms[k])) for k in range(3)]
-    e7 = [7.0 * t[k] + 3.0 * ms[k] for k in range(3)]
-    e3s = [3.0 * t[k] + ms[k] for k in range(3)]
-    v3 = 3.0 * vr
-    hxe7 = cross(hv, e7)
-    nxe3 = cross(nn, e3s)
-    a = [gacc[k] + fa * (e1[k] - hxe7[k] + v3 * nxe3[k]) for k in range(3)]
-    # Kidder 1995 eq. 2.4a / 2.4b (general_relativity.rs:400-456)
-    mu = hm * m / (hm + m)
-    fm = 2.0 + 1.5 * m / hm
-    fm2 = 2.0 + 1.5 * hm / m
+    # (n x v)_k = (r x v)_k / d
     h = cross(r, hv)
-    lo = [mu * h[k] for k in range(3)]
-    h2 = cross(pL, sL)
+    c6 = [6.0 * nn[k] * inv_d for k in range(3)]
+    e1 = [c6[k] * (h[k] * (2.0 * t[k] + ms[k])) for k in range(3)]
+    # -v x (7 t + 3 ms) + 3 v_r n x (3 t + ms) = aq x t + 3 q x ms with
+    # q = v_r n - v, aq = 7 q + 2 v_r n
+    q = [vr * nn[k] - hv[k] for k in range(3)]
+    vr2x = 2.0 * vr
+    aq = [7.0 * q[k] + vr2x * nn[k] for k in range(3)]
+    axt = cross(aq, t)
+    qxm = cross(q, ms)
+    a = [gacc[k] + fa * (e1[k] + axt[k] + 3.0 * qxm[k]) for k in range(3)]
+    # Kidder 1995 eq. 2.4a / 2.4b (general_relativity.rs:400-456): with
+    # L_o = mu (r x v) the torques fm (L_o x S_h) - (L_p x S_h) + 3 (n.L_p) (n x S_h)
+    # and fm2 (L_o x L_p) + (L_p x S_h) + 3 (n.S_h) (n x L_p), each one cross
+    # product of a combined vector
+    mu = hm * m / (hm + m)
+    fmu = (2.0 + 1.5 * m / hm) * mu
+    fm2mu = (2.0 + 1.5 * hm / m) * mu
     sp3 = 3.0 * dot(nn, pL)
     ss3 = 3.0 * dot(nn, sL)
-    loxs, loxp = cross(lo, sL), cross(lo, pL)
-    nxs, nxp = cross(nn, sL), cross(nn, pL)
-    th = [fa * (fm * loxs[k] - h2[k] + sp3 * nxs[k]) for k in range(3)]
-    dl = [fa * (fm2 * loxp[k] + h2[k] + ss3 * nxp[k]) for k in range(3)]
+    ws = [fmu * h[k] - pL[k] + sp3 * nn[k] for k in range(3)]
+    wp = [fm2mu * h[k] - sL[k] + ss3 * nn[k] for k in range(3)]
+    wsxs, wpxp = cross(ws, sL), cross(wp, pL)
+    th = [fa * wsxs[k] for k in range(3)]
+    dl = [fa * wpxp[k] for k in range(3)]
     return a + dl + th
 
 

@@ -69,9 +69,9 @@ __host__ __device__ __forceinline__ void adj_tides_pre(double in_x, double in_y,
     const double t103 = t74 + t80;
     const double t106 = t83 + t85;
     const double t107 = t33 * t106;
-    const double t149 = 1.0 / c_m;
-    const double t153 = t23 * t85;
-    const double t154 = t23 * t83;
+    const double t140 = 1.0 / c_m;
+    const double t144 = t23 * t85;
+    const double t145 = t23 * t83;
     pre[0] = in_x;
     pre[1] = in_y;
     pre[2] = in_z;
@@ -80,16 +80,16 @@ __host__ __device__ __forceinline__ void adj_tides_pre(double in_x, double in_y,
     pre[5] = t103;
     pre[6] = t97;
     pre[7] = t107;
-    pre[8] = t34;
-    pre[9] = t98;
-    pre[10] = t99;
+    pre[8] = t98;
+    pre[9] = t99;
+    pre[10] = t34;
     pre[11] = t35;
     pre[12] = t36;
-    pre[13] = t149;
+    pre[13] = t140;
     pre[14] = t85;
     pre[15] = t83;
-    pre[16] = t153;
-    pre[17] = t154;
+    pre[16] = t144;
+    pre[17] = t145;
 }
 
 // adj_tides: one midpoint iteration.  Outputs: a[3] (planet acceleration),
@@ -126,95 +126,86 @@ __host__ __device__ __forceinline__ void adj_tides_iter(const double* __restrict
     const double t105 = pre[6] + t104;
     const double t108 = t42 * pre[7];
     const double t109 = t105 + t108;
-    const double t110 = pre[2] * in_H1;
-    const double t111 = pre[1] * in_H2;
-    const double t112 = t110 - t111;
-    const double t113 = pre[0] * in_H2;
-    const double t114 = pre[2] * in_H0;
-    const double t115 = t113 - t114;
-    const double t116 = pre[1] * in_H0;
-    const double t117 = pre[0] * in_H1;
-    const double t118 = t116 - t117;
-    const double t119 = pre[2] * in_S1;
-    const double t120 = pre[1] * in_S2;
+    const double t110 = in_H0 * pre[8];
+    const double t111 = in_S0 * pre[9];
+    const double t112 = t110 + t111;
+    const double t113 = in_H1 * pre[8];
+    const double t114 = in_S1 * pre[9];
+    const double t115 = t113 + t114;
+    const double t116 = in_H2 * pre[8];
+    const double t117 = in_S2 * pre[9];
+    const double t118 = t116 + t117;
+    const double t119 = pre[2] * t115;
+    const double t120 = pre[1] * t118;
     const double t121 = t119 - t120;
-    const double t122 = pre[0] * in_S2;
-    const double t123 = pre[2] * in_S0;
+    const double t122 = pre[0] * t118;
+    const double t123 = pre[2] * t112;
     const double t124 = t122 - t123;
-    const double t125 = pre[1] * in_S0;
-    const double t126 = pre[0] * in_S1;
+    const double t125 = pre[1] * t112;
+    const double t126 = pre[0] * t115;
     const double t127 = t125 - t126;
-    const double t128 = pre[8] * t109;
-    const double t129 = t112 - in_hv0;
-    const double t130 = pre[9] * t129;
-    const double t131 = t128 + t130;
-    const double t132 = t121 - in_hv0;
-    const double t133 = pre[10] * t132;
-    const double t134 = t131 + t133;
-    const double t135 = pre[11] * t109;
-    const double t136 = t115 - in_hv1;
-    const double t137 = pre[9] * t136;
-    const double t138 = t135 + t137;
-    const double t139 = t124 - in_hv1;
-    const double t140 = pre[10] * t139;
-    const double t141 = t138 + t140;
-    const double t142 = pre[12] * t109;
-    const double t143 = t118 - in_hv2;
-    const double t144 = pre[9] * t143;
-    const double t145 = t142 + t144;
-    const double t146 = t127 - in_hv2;
-    const double t147 = pre[10] * t146;
-    const double t148 = t145 + t147;
-    const double t150 = t134 * pre[13];
-    const double t151 = t141 * pre[13];
-    const double t152 = t148 * pre[13];
-    const double t155 = t52 * pre[14];
-    const double t156 = t47 * pre[15];
-    const double t157 = in_S0 * pre[16];
-    const double t158 = pre[8] * t155;
-    const double t159 = t157 - t158;
-    const double t160 = t55 * pre[10];
-    const double t161 = t159 - t160;
-    const double t162 = -t161;
-    const double t163 = in_S1 * pre[16];
-    const double t164 = pre[11] * t155;
-    const double t165 = t163 - t164;
-    const double t166 = t58 * pre[10];
-    const double t167 = t165 - t166;
-    const double t168 = -t167;
-    const double t169 = in_S2 * pre[16];
-    const double t170 = pre[12] * t155;
-    const double t171 = t169 - t170;
-    const double t172 = t61 * pre[10];
-    const double t173 = t171 - t172;
-    const double t174 = -t173;
-    const double t175 = in_H0 * pre[17];
-    const double t176 = pre[8] * t156;
-    const double t177 = t175 - t176;
-    const double t178 = t55 * pre[9];
-    const double t179 = t177 - t178;
-    const double t180 = -t179;
-    const double t181 = in_H1 * pre[17];
-    const double t182 = pre[11] * t156;
-    const double t183 = t181 - t182;
-    const double t184 = t58 * pre[9];
-    const double t185 = t183 - t184;
-    const double t186 = -t185;
-    const double t187 = in_H2 * pre[17];
-    const double t188 = pre[12] * t156;
-    const double t189 = t187 - t188;
-    const double t190 = t61 * pre[9];
-    const double t191 = t189 - t190;
-    const double t192 = -t191;
-    out[0] = t150;
-    out[1] = t151;
-    out[2] = t152;
-    out[3] = t162;
-    out[4] = t168;
-    out[5] = t174;
-    out[6] = t180;
-    out[7] = t186;
-    out[8] = t192;
+    const double t128 = pre[10] * t109;
+    const double t129 = t121 + t128;
+    const double t130 = in_hv0 * pre[7];
+    const double t131 = t129 - t130;
+    const double t132 = pre[11] * t109;
+    const double t133 = t124 + t132;
+    const double t134 = in_hv1 * pre[7];
+    const double t135 = t133 - t134;
+    const double t136 = pre[12] * t109;
+    const double t137 = t127 + t136;
+    const double t138 = in_hv2 * pre[7];
+    const double t139 = t137 - t138;
+    const double t141 = t131 * pre[13];
+    const double t142 = t135 * pre[13];
+    const double t143 = t139 * pre[13];
+    const double t146 = t52 * pre[14];
+    const double t147 = t47 * pre[15];
+    const double t148 = in_S0 * pre[16];
+    const double t149 = pre[10] * t146;
+    const double t150 = t148 - t149;
+    const double t151 = t55 * pre[9];
+    const double t152 = t150 - t151;
+    const double t153 = -t152;
+    const double t154 = in_S1 * pre[16];
+    const double t155 = pre[11] * t146;
+    const double t156 = t154 - t155;
+    const double t157 = t58 * pre[9];
+    const double t158 = t156 - t157;
+    const double t159 = -t158;
+    const double t160 = in_S2 * pre[16];
+    const double t161 = pre[12] * t146;
+    const double t162 = t160 - t161;
+    const double t163 = t61 * pre[9];
+    const double t164 = t162 - t163;
+    const double t165 = -t164;
+    const double t166 = in_H0 * pre[17];
+    const double t167 = pre[10] * t147;
+    const double t168 = t166 - t167;
+    const double t169 = t55 * pre[8];
+    const double t170 = t168 - t169;
+    const double t171 = -t170;
+    const double t172 = in_H1 * pre[17];
+    const double t173 = pre[11] * t147;
+    const double t174 = t172 - t173;
+    const double t175 = t58 * pre[8];
+    const double t176 = t174 - t175;
+    const double t177 = -t176;
+    const double t178 = in_H2 * pre[17];
+    const double t179 = pre[12] * t147;
+    const double t180 = t178 - t179;
+    const double t181 = t61 * pre[8];
+    const double t182 = t180 - t181;
+    const double t183 = -t182;
+    out[0] = t141;
+    out[1] = t142;
+    out[2] = t143;
+    out[3] = t153;
+    out[4] = t159;
+    out[5] = t165;
+    out[6] = t171;
+    out[7] = t177;
+    out[8] = t183;
 }
 
 // adj_tides: VJP of one iteration.  bin[15] += adjoints of (hv0, hv1, hv2, S0, S1, S2, H0, H1, H2, P0, P1, P2, Q0, Q1, Q2);
@@ -251,246 +242,219 @@ __host__ __device__ __forceinline__ void adj_tides_iter_vjp(const double* __rest
     const double t105 = pre[6] + t104;
     const double t108 = t42 * pre[7];
     const double t109 = t105 + t108;
-    const double t110 = pre[2] * in_H1;
-    const double t111 = pre[1] * in_H2;
-    const double t112 = t110 - t111;
-    const double t113 = pre[0] * in_H2;
-    const double t114 = pre[2] * in_H0;
-    const double t115 = t113 - t114;
-    const double t116 = pre[1] * in_H0;
-    const double t117 = pre[0] * in_H1;
-    const double t118 = t116 - t117;
-    const double t119 = pre[2] * in_S1;
-    const double t120 = pre[1] * in_S2;
+    const double t110 = in_H0 * pre[8];
+    const double t111 = in_S0 * pre[9];
+    const double t112 = t110 + t111;
+    const double t113 = in_H1 * pre[8];
+    const double t114 = in_S1 * pre[9];
+    const double t115 = t113 + t114;
+    const double t116 = in_H2 * pre[8];
+    const double t117 = in_S2 * pre[9];
+    const double t118 = t116 + t117;
+    const double t119 = pre[2] * t115;
+    const double t120 = pre[1] * t118;
     const double t121 = t119 - t120;
-    const double t122 = pre[0] * in_S2;
-    const double t123 = pre[2] * in_S0;
+    const double t122 = pre[0] * t118;
+    const double t123 = pre[2] * t112;
     const double t124 = t122 - t123;
-    const double t125 = pre[1] * in_S0;
-    const double t126 = pre[0] * in_S1;
+    const double t125 = pre[1] * t112;
+    const double t126 = pre[0] * t115;
     const double t127 = t125 - t126;
-    const double t128 = pre[8] * t109;
-    const double t129 = t112 - in_hv0;
-    const double t130 = pre[9] * t129;
-    const double t131 = t128 + t130;
-    const double t132 = t121 - in_hv0;
-    const double t133 = pre[10] * t132;
-    const double t134 = t131 + t133;
-    const double t135 = pre[11] * t109;
-    const double t136 = t115 - in_hv1;
-    const double t137 = pre[9] * t136;
-    const double t138 = t135 + t137;
-    const double t139 = t124 - in_hv1;
-    const double t140 = pre[10] * t139;
-    const double t141 = t138 + t140;
-    const double t142 = pre[12] * t109;
-    const double t143 = t118 - in_hv2;
-    const double t144 = pre[9] * t143;
-    const double t145 = t142 + t144;
-    const double t146 = t127 - in_hv2;
-    const double t147 = pre[10] * t146;
-    const double t148 = t145 + t147;
-    const double t150 = t134 * pre[13];
-    const double t151 = t141 * pre[13];
-    const double t152 = t148 * pre[13];
-    const double t155 = t52 * pre[14];
-    const double t156 = t47 * pre[15];
-    const double t157 = in_S0 * pre[16];
-    const double t158 = pre[8] * t155;
-    const double t159 = t157 - t158;
-    const double t160 = t55 * pre[10];
-    const double t161 = t159 - t160;
-    const double t162 = -t161;
-    const double t163 = in_S1 * pre[16];
-    const double t164 = pre[11] * t155;
-    const double t165 = t163 - t164;
-    const double t166 = t58 * pre[10];
-    const double t167 = t165 - t166;
-    const double t168 = -t167;
-    const double t169 = in_S2 * pre[16];
-    const double t170 = pre[12] * t155;
-    const double t171 = t169 - t170;
-    const double t172 = t61 * pre[10];
-    const double t173 = t171 - t172;
-    const double t174 = -t173;
-    const double t175 = in_H0 * pre[17];
-    const double t176 = pre[8] * t156;
-    const double t177 = t175 - t176;
-    const double t178 = t55 * pre[9];
-    const double t179 = t177 - t178;
-    const double t180 = -t179;
-    const double t181 = in_H1 * pre[17];
-    const double t182 = pre[11] * t156;
-    const double t183 = t181 - t182;
-    const double t184 = t58 * pre[9];
-    const double t185 = t183 - t184;
-    const double t186 = -t185;
-    const double t187 = in_H2 * pre[17];
-    const double t188 = pre[12] * t156;
-    const double t189 = t187 - t188;
-    const double t190 = t61 * pre[9];
-    const double t191 = t189 - t190;
-    const double t192 = -t191;
-    double b150 = bout[0];
-    double b151 = bout[1];
-    double b152 = bout[2];
-    double b162 = bout[3];
-    double b168 = bout[4];
-    double b174 = bout[5];
-    double b180 = bout[6];
-    double b186 = bout[7];
-    double b192 = bout[8];
-    double b191 = -b192;
-    double b189 = b191;
-    double b190 = -b191;
-    double b61 = b190 * pre[9];
-    bpre[9] += b190 * t61;
-    double b187 = b189;
-    double b188 = -b189;
-    bpre[12] += b188 * t156;
-    double b156 = b188 * pre[12];
-    double b_H2 = b187 * pre[17];
-    bpre[17] += b187 * in_H2;
-    double b185 = -b186;
-    double b183 = b185;
-    double b184 = -b185;
-    double b58 = b184 * pre[9];
-    bpre[9] += b184 * t58;
-    double b181 = b183;
+    const double t128 = pre[10] * t109;
+    const double t129 = t121 + t128;
+    const double t130 = in_hv0 * pre[7];
+    const double t131 = t129 - t130;
+    const double t132 = pre[11] * t109;
+    const double t133 = t124 + t132;
+    const double t134 = in_hv1 * pre[7];
+    const double t135 = t133 - t134;
+    const double t136 = pre[12] * t109;
+    const double t137 = t127 + t136;
+    const double t138 = in_hv2 * pre[7];
+    const double t139 = t137 - t138;
+    const double t141 = t131 * pre[13];
+    const double t142 = t135 * pre[13];
+    const double t143 = t139 * pre[13];
+    const double t146 = t52 * pre[14];
+    const double t147 = t47 * pre[15];
+    const double t148 = in_S0 * pre[16];
+    const double t149 = pre[10] * t146;
+    const double t150 = t148 - t149;
+    const double t151 = t55 * pre[9];
+    const double t152 = t150 - t151;
+    const double t153 = -t152;
+    const double t154 = in_S1 * pre[16];
+    const double t155 = pre[11] * t146;
+    const double t156 = t154 - t155;
+    const double t157 = t58 * pre[9];
+    const double t158 = t156 - t157;
+    const double t159 = -t158;
+    const double t160 = in_S2 * pre[16];
+    const double t161 = pre[12] * t146;
+    const double t162 = t160 - t161;
+    const double t163 = t61 * pre[9];
+    const double t164 = t162 - t163;
+    const double t165 = -t164;
+    const double t166 = in_H0 * pre[17];
+    const double t167 = pre[10] * t147;
+    const double t168 = t166 - t167;
+    const double t169 = t55 * pre[8];
+    const double t170 = t168 - t169;
+    const double t171 = -t170;
+    const double t172 = in_H1 * pre[17];
+    const double t173 = pre[11] * t147;
+    const double t174 = t172 - t173;
+    const double t175 = t58 * pre[8];
+    const double t176 = t174 - t175;
+    const double t177 = -t176;
+    const double t178 = in_H2 * pre[17];
+    const double t179 = pre[12] * t147;
+    const double t180 = t178 - t179;
+    const double t181 = t61 * pre[8];
+    const double t182 = t180 - t181;
+    const double t183 = -t182;
+    double b141 = bout[0];
+    double b142 = bout[1];
+    double b143 = bout[2];
+    double b153 = bout[3];
+    double b159 = bout[4];
+    double b165 = bout[5];
+    double b171 = bout[6];
+    double b177 = bout[7];
+    double b183 = bout[8];
     double b182 = -b183;
-    bpre[11] += b182 * t156;
-    b156 += b182 * pre[11];
-    double b_H1 = b181 * pre[17];
-    bpre[17] += b181 * in_H1;
+    double b180 = b182;
+    double b181 = -b182;
+    double b61 = b181 * pre[8];
+    bpre[8] += b181 * t61;
+    double b178 = b180;
     double b179 = -b180;
-    double b177 = b179;
-    double b178 = -b179;
-    double b55 = b178 * pre[9];
-    bpre[9] += b178 * t55;
-    double b175 = b177;
+    bpre[12] += b179 * t147;
+    double b147 = b179 * pre[12];
+    double b_H2 = b178 * pre[17];
+    bpre[17] += b178 * in_H2;
     double b176 = -b177;
-    bpre[8] += b176 * t156;
-    b156 += b176 * pre[8];
-    double b_H0 = b175 * pre[17];
-    bpre[17] += b175 * in_H0;
+    double b174 = b176;
+    double b175 = -b176;
+    double b58 = b175 * pre[8];
+    bpre[8] += b175 * t58;
+    double b172 = b174;
     double b173 = -b174;
-    double b171 = b173;
-    double b172 = -b173;
-    b61 += b172 * pre[10];
-    bpre[10] += b172 * t61;
-    double b169 = b171;
+    bpre[11] += b173 * t147;
+    b147 += b173 * pre[11];
+    double b_H1 = b172 * pre[17];
+    bpre[17] += b172 * in_H1;
     double b170 = -b171;
-    bpre[12] += b170 * t155;
-    double b155 = b170 * pre[12];
-    double b_S2 = b169 * pre[16];
-    bpre[16] += b169 * in_S2;
+    double b168 = b170;
+    double b169 = -b170;
+    double b55 = b169 * pre[8];
+    bpre[8] += b169 * t55;
+    double b166 = b168;
     double b167 = -b168;
-    double b165 = b167;
-    double b166 = -b167;
-    b58 += b166 * pre[10];
-    bpre[10] += b166 * t58;
-    double b163 = b165;
+    bpre[10] += b167 * t147;
+    b147 += b167 * pre[10];
+    double b_H0 = b166 * pre[17];
+    bpre[17] += b166 * in_H0;
     double b164 = -b165;
-    bpre[11] += b164 * t155;
-    b155 += b164 * pre[11];
-    double b_S1 = b163 * pre[16];
-    bpre[16] += b163 * in_S1;
+    double b162 = b164;
+    double b163 = -b164;
+    b61 += b163 * pre[9];
+    bpre[9] += b163 * t61;
+    double b160 = b162;
     double b161 = -b162;
-    double b159 = b161;
-    double b160 = -b161;
-    b55 += b160 * pre[10];
-    bpre[10] += b160 * t55;
-    double b157 = b159;
+    bpre[12] += b161 * t146;
+    double b146 = b161 * pre[12];
+    double b_S2 = b160 * pre[16];
+    bpre[16] += b160 * in_S2;
     double b158 = -b159;
-    bpre[8] += b158 * t155;
-    b155 += b158 * pre[8];
-    double b_S0 = b157 * pre[16];
-    bpre[16] += b157 * in_S0;
-    double b47 = b156 * pre[15];
-    bpre[15] += b156 * t47;
-    double b52 = b155 * pre[14];
-    bpre[14] += b155 * t52;
-    double b148 = b152 * pre[13];
-    double b141 = b151 * pre[13];
-    double b134 = b150 * pre[13];
-    double b145 = b148;
-    double b147 = b148;
-    bpre[10] += b147 * t146;
-    double b146 = b147 * pre[10];
-    double b127 = b146;
-    double b_hv2 = -b146;
-    double b142 = b145;
-    double b144 = b145;
-    bpre[9] += b144 * t143;
-    double b143 = b144 * pre[9];
-    double b118 = b143;
-    b_hv2 += -b143;
-    bpre[12] += b142 * t109;
-    double b109 = b142 * pre[12];
-    double b138 = b141;
-    double b140 = b141;
-    bpre[10] += b140 * t139;
-    double b139 = b140 * pre[10];
-    double b124 = b139;
-    double b_hv1 = -b139;
-    double b135 = b138;
-    double b137 = b138;
-    bpre[9] += b137 * t136;
-    double b136 = b137 * pre[9];
-    double b115 = b136;
-    b_hv1 += -b136;
-    bpre[11] += b135 * t109;
-    b109 += b135 * pre[11];
-    double b131 = b134;
-    double b133 = b134;
-    bpre[10] += b133 * t132;
-    double b132 = b133 * pre[10];
-    double b121 = b132;
-    double b_hv0 = -b132;
-    double b128 = b131;
-    double b130 = b131;
-    bpre[9] += b130 * t129;
-    double b129 = b130 * pre[9];
-    double b112 = b129;
-    b_hv0 += -b129;
-    bpre[8] += b128 * t109;
-    b109 += b128 * pre[8];
+    double b156 = b158;
+    double b157 = -b158;
+    b58 += b157 * pre[9];
+    bpre[9] += b157 * t58;
+    double b154 = b156;
+    double b155 = -b156;
+    bpre[11] += b155 * t146;
+    b146 += b155 * pre[11];
+    double b_S1 = b154 * pre[16];
+    bpre[16] += b154 * in_S1;
+    double b152 = -b153;
+    double b150 = b152;
+    double b151 = -b152;
+    b55 += b151 * pre[9];
+    bpre[9] += b151 * t55;
+    double b148 = b150;
+    double b149 = -b150;
+    bpre[10] += b149 * t146;
+    b146 += b149 * pre[10];
+    double b_S0 = b148 * pre[16];
+    bpre[16] += b148 * in_S0;
+    double b47 = b147 * pre[15];
+    bpre[15] += b147 * t47;
+    double b52 = b146 * pre[14];
+    bpre[14] += b146 * t52;
+    double b139 = b143 * pre[13];
+    double b135 = b142 * pre[13];
+    double b131 = b141 * pre[13];
+    double b137 = b139;
+    double b138 = -b139;
+    double b_hv2 = b138 * pre[7];
+    bpre[7] += b138 * in_hv2;
+    double b127 = b137;
+    double b136 = b137;
+    bpre[12] += b136 * t109;
+    double b109 = b136 * pre[12];
+    double b133 = b135;
+    double b134 = -b135;
+    double b_hv1 = b134 * pre[7];
+    bpre[7] += b134 * in_hv1;
+    double b124 = b133;
+    double b132 = b133;
+    bpre[11] += b132 * t109;
+    b109 += b132 * pre[11];
+    double b129 = b131;
+    double b130 = -b131;
+    double b_hv0 = b130 * pre[7];
+    bpre[7] += b130 * in_hv0;
+    double b121 = b129;
+    double b128 = b129;
+    bpre[10] += b128 * t109;
+    b109 += b128 * pre[10];
     double b125 = b127;
     double b126 = -b127;
-    bpre[0] += b126 * in_S1;
-    b_S1 += b126 * pre[0];
-    bpre[1] += b125 * in_S0;
-    b_S0 += b125 * pre[1];
+    bpre[0] += b126 * t115;
+    double b115 = b126 * pre[0];
+    bpre[1] += b125 * t112;
+    double b112 = b125 * pre[1];
     double b122 = b124;
     double b123 = -b124;
-    bpre[2] += b123 * in_S0;
-    b_S0 += b123 * pre[2];
-    bpre[0] += b122 * in_S2;
-    b_S2 += b122 * pre[0];
+    bpre[2] += b123 * t112;
+    b112 += b123 * pre[2];
+    bpre[0] += b122 * t118;
+    double b118 = b122 * pre[0];
     double b119 = b121;
     double b120 = -b121;
-    bpre[1] += b120 * in_S2;
-    b_S2 += b120 * pre[1];
-    bpre[2] += b119 * in_S1;
-    b_S1 += b119 * pre[2];
+    bpre[1] += b120 * t118;
+    b118 += b120 * pre[1];
+    bpre[2] += b119 * t115;
+    b115 += b119 * pre[2];
     double b116 = b118;
-    double b117 = -b118;
-    bpre[0] += b117 * in_H1;
-    b_H1 += b117 * pre[0];
-    bpre[1] += b116 * in_H0;
-    b_H0 += b116 * pre[1];
+    double b117 = b118;
+    b_S2 += b117 * pre[9];
+    bpre[9] += b117 * in_S2;
+    b_H2 += b116 * pre[8];
+    bpre[8] += b116 * in_H2;
     double b113 = b115;
-    double b114 = -b115;
-    bpre[2] += b114 * in_H0;
-    b_H0 += b114 * pre[2];
-    bpre[0] += b113 * in_H2;
-    b_H2 += b113 * pre[0];
+    double b114 = b115;
+    b_S1 += b114 * pre[9];
+    bpre[9] += b114 * in_S1;
+    b_H1 += b113 * pre[8];
+    bpre[8] += b113 * in_H1;
     double b110 = b112;
-    double b111 = -b112;
-    bpre[1] += b111 * in_H2;
-    b_H2 += b111 * pre[1];
-    bpre[2] += b110 * in_H1;
-    b_H1 += b110 * pre[2];
+    double b111 = b112;
+    b_S0 += b111 * pre[9];
+    bpre[9] += b111 * in_S0;
+    b_H0 += b110 * pre[8];
+    bpre[8] += b110 * in_H0;
     double b105 = b109;
     double b108 = b109;
     double b42 = b108 * pre[7];
@@ -620,9 +584,9 @@ __host__ __device__ __forceinline__ void adj_tides_pre_vjp(double in_x, double i
     const double t103 = t74 + t80;
     const double t106 = t83 + t85;
     const double t107 = t33 * t106;
-    const double t149 = 1.0 / c_m;
-    const double t153 = t23 * t85;
-    const double t154 = t23 * t83;
+    const double t140 = 1.0 / c_m;
+    const double t144 = t23 * t85;
+    const double t145 = t23 * t83;
     double b_x = bpre[0];
     double b_y = bpre[1];
     double b_z = bpre[2];
@@ -631,19 +595,19 @@ __host__ __device__ __forceinline__ void adj_tides_pre_vjp(double in_x, double i
     double b103 = bpre[5];
     double b97 = bpre[6];
     double b107 = bpre[7];
-    double b34 = bpre[8];
-    double b98 = bpre[9];
-    double b99 = bpre[10];
+    double b98 = bpre[8];
+    double b99 = bpre[9];
+    double b34 = bpre[10];
     double b35 = bpre[11];
     double b36 = bpre[12];
     double b85 = bpre[14];
     double b83 = bpre[15];
-    double b153 = bpre[16];
-    double b154 = bpre[17];
-    double b23 = b154 * t83;
-    b83 += b154 * t23;
-    b23 += b153 * t85;
-    b85 += b153 * t23;
+    double b144 = bpre[16];
+    double b145 = bpre[17];
+    double b23 = b145 * t83;
+    b83 += b145 * t23;
+    b23 += b144 * t85;
+    b85 += b144 * t23;
     b33 += b107 * t106;
     double b106 = b107 * t33;
     b83 += b106;
@@ -756,9 +720,9 @@ __host__ __device__ __forceinline__ void adj_tides_pre_jvp(double in_x, double i
     const double t103 = t74 + t80;
     const double t106 = t83 + t85;
     const double t107 = t33 * t106;
-    const double t149 = 1.0 / c_m;
-    const double t153 = t23 * t85;
-    const double t154 = t23 * t83;
+    const double t140 = 1.0 / c_m;
+    const double t144 = t23 * t85;
+    const double t145 = t23 * t83;
     double d18[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d18[k] = 2.0 * in_x * din[0 * NT + k];
@@ -855,12 +819,12 @@ __host__ __device__ __forceinline__ void adj_tides_pre_jvp(double in_x, double i
     double d107[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d107[k] = d33[k] * t106 + t33 * d106[k];
-    double d153[NT];
+    double d144[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d153[k] = d23[k] * t85 + t23 * d85[k];
-    double d154[NT];
+    for (int k = 0; k < NT; ++k) d144[k] = d23[k] * t85 + t23 * d85[k];
+    double d145[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d154[k] = d23[k] * t83 + t23 * d83[k];
+    for (int k = 0; k < NT; ++k) d145[k] = d23[k] * t83 + t23 * d83[k];
     pre[0] = in_x;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[0 * NT + k] = din[0 * NT + k];
@@ -885,22 +849,22 @@ __host__ __device__ __forceinline__ void adj_tides_pre_jvp(double in_x, double i
     pre[7] = t107;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[7 * NT + k] = d107[k];
-    pre[8] = t34;
+    pre[8] = t98;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[8 * NT + k] = d34[k];
-    pre[9] = t98;
+    for (int k = 0; k < NT; ++k) dpre[8 * NT + k] = d98[k];
+    pre[9] = t99;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[9 * NT + k] = d98[k];
-    pre[10] = t99;
+    for (int k = 0; k < NT; ++k) dpre[9 * NT + k] = d99[k];
+    pre[10] = t34;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[10 * NT + k] = d99[k];
+    for (int k = 0; k < NT; ++k) dpre[10 * NT + k] = d34[k];
     pre[11] = t35;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[11 * NT + k] = d35[k];
     pre[12] = t36;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[12 * NT + k] = d36[k];
-    pre[13] = t149;
+    pre[13] = t140;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[13 * NT + k] = 0.0;
     pre[14] = t85;
@@ -909,12 +873,12 @@ __host__ __device__ __forceinline__ void adj_tides_pre_jvp(double in_x, double i
     pre[15] = t83;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[15 * NT + k] = d83[k];
-    pre[16] = t153;
+    pre[16] = t144;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[16 * NT + k] = d153[k];
-    pre[17] = t154;
+    for (int k = 0; k < NT; ++k) dpre[16 * NT + k] = d144[k];
+    pre[17] = t145;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[17 * NT + k] = d154[k];
+    for (int k = 0; k < NT; ++k) dpre[17 * NT + k] = d145[k];
 }
 
 // adj_tides: one iteration, outputs and their tangents (din[i * NT + k] for the
@@ -954,86 +918,77 @@ __host__ __device__ __forceinline__ void adj_tides_iter_jvp(const double* __rest
     const double t105 = pre[6] + t104;
     const double t108 = t42 * pre[7];
     const double t109 = t105 + t108;
-    const double t110 = pre[2] * in_H1;
-    const double t111 = pre[1] * in_H2;
-    const double t112 = t110 - t111;
-    const double t113 = pre[0] * in_H2;
-    const double t114 = pre[2] * in_H0;
-    const double t115 = t113 - t114;
-    const double t116 = pre[1] * in_H0;
-    const double t117 = pre[0] * in_H1;
-    const double t118 = t116 - t117;
-    const double t119 = pre[2] * in_S1;
-    const double t120 = pre[1] * in_S2;
+    const double t110 = in_H0 * pre[8];
+    const double t111 = in_S0 * pre[9];
+    const double t112 = t110 + t111;
+    const double t113 = in_H1 * pre[8];
+    const double t114 = in_S1 * pre[9];
+    const double t115 = t113 + t114;
+    const double t116 = in_H2 * pre[8];
+    const double t117 = in_S2 * pre[9];
+    const double t118 = t116 + t117;
+    const double t119 = pre[2] * t115;
+    const double t120 = pre[1] * t118;
     const double t121 = t119 - t120;
-    const double t122 = pre[0] * in_S2;
-    const double t123 = pre[2] * in_S0;
+    const double t122 = pre[0] * t118;
+    const double t123 = pre[2] * t112;
     const double t124 = t122 - t123;
-    const double t125 = pre[1] * in_S0;
-    const double t126 = pre[0] * in_S1;
+    const double t125 = pre[1] * t112;
+    const double t126 = pre[0] * t115;
     const double t127 = t125 - t126;
-    const double t128 = pre[8] * t109;
-    const double t129 = t112 - in_hv0;
-    const double t130 = pre[9] * t129;
-    const double t131 = t128 + t130;
-    const double t132 = t121 - in_hv0;
-    const double t133 = pre[10] * t132;
-    const double t134 = t131 + t133;
-    const double t135 = pre[11] * t109;
-    const double t136 = t115 - in_hv1;
-    const double t137 = pre[9] * t136;
-    const double t138 = t135 + t137;
-    const double t139 = t124 - in_hv1;
-    const double t140 = pre[10] * t139;
-    const double t141 = t138 + t140;
-    const double t142 = pre[12] * t109;
-    const double t143 = t118 - in_hv2;
-    const double t144 = pre[9] * t143;
-    const double t145 = t142 + t144;
-    const double t146 = t127 - in_hv2;
-    const double t147 = pre[10] * t146;
-    const double t148 = t145 + t147;
-    const double t150 = t134 * pre[13];
-    const double t151 = t141 * pre[13];
-    const double t152 = t148 * pre[13];
-    const double t155 = t52 * pre[14];
-    const double t156 = t47 * pre[15];
-    const double t157 = in_S0 * pre[16];
-    const double t158 = pre[8] * t155;
-    const double t159 = t157 - t158;
-    const double t160 = t55 * pre[10];
-    const double t161 = t159 - t160;
-    const double t162 = -t161;
-    const double t163 = in_S1 * pre[16];
-    const double t164 = pre[11] * t155;
-    const double t165 = t163 - t164;
-    const double t166 = t58 * pre[10];
-    const double t167 = t165 - t166;
-    const double t168 = -t167;
-    const double t169 = in_S2 * pre[16];
-    const double t170 = pre[12] * t155;
-    const double t171 = t169 - t170;
-    const double t172 = t61 * pre[10];
-    const double t173 = t171 - t172;
-    const double t174 = -t173;
-    const double t175 = in_H0 * pre[17];
-    const double t176 = pre[8] * t156;
-    const double t177 = t175 - t176;
-    const double t178 = t55 * pre[9];
-    const double t179 = t177 - t178;
-    const double t180 = -t179;
-    const double t181 = in_H1 * pre[17];
-    const double t182 = pre[11] * t156;
-    const double t183 = t181 - t182;
-    const double t184 = t58 * pre[9];
-    const double t185 = t183 - t184;
-    const double t186 = -t185;
-    const double t187 = in_H2 * pre[17];
-    const double t188 = pre[12] * t156;
-    const double t189 = t187 - t188;
-    const double t190 = t61 * pre[9];
-    const double t191 = t189 - t190;
-    const double t192 = -t191;
+    const double t128 = pre[10] * t109;
+    const double t129 = t121 + t128;
+    const double t130 = in_hv0 * pre[7];
+    const double t131 = t129 - t130;
+    const double t132 = pre[11] * t109;
+    const double t133 = t124 + t132;
+    const double t134 = in_hv1 * pre[7];
+    const double t135 = t133 - t134;
+    const double t136 = pre[12] * t109;
+    const double t137 = t127 + t136;
+    const double t138 = in_hv2 * pre[7];
+    const double t139 = t137 - t138;
+    const double t141 = t131 * pre[13];
+    const double t142 = t135 * pre[13];
+    const double t143 = t139 * pre[13];
+    const double t146 = t52 * pre[14];
+    const double t147 = t47 * pre[15];
+    const double t148 = in_S0 * pre[16];
+    const double t149 = pre[10] * t146;
+    const double t150 = t148 - t149;
+    const double t151 = t55 * pre[9];
+    const double t152 = t150 - t151;
+    const double t153 = -t152;
+    const double t154 = in_S1 * pre[16];
+    const double t155 = pre[11] * t146;
+    const double t156 = t154 - t155;
+    const double t157 = t58 * pre[9];
+    const double t158 = t156 - t157;
+    const double t159 = -t158;
+    const double t160 = in_S2 * pre[16];
+    const double t161 = pre[12] * t146;
+    const double t162 = t160 - t161;
+    const double t163 = t61 * pre[9];
+    const double t164 = t162 - t163;
+    const double t165 = -t164;
+    const double t166 = in_H0 * pre[17];
+    const double t167 = pre[10] * t147;
+    const double t168 = t166 - t167;
+    const double t169 = t55 * pre[8];
+    const double t170 = t168 - t169;
+    const double t171 = -t170;
+    const double t172 = in_H1 * pre[17];
+    const double t173 = pre[11] * t147;
+    const double t174 = t172 - t173;
+    const double t175 = t58 * pre[8];
+    const double t176 = t174 - t175;
+    const double t177 = -t176;
+    const double t178 = in_H2 * pre[17];
+    const double t179 = pre[12] * t147;
+    const double t180 = t178 - t179;
+    const double t181 = t61 * pre[8];
+    const double t182 = t180 - t181;
+    const double t183 = -t182;
     double d37[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d37[k] = dpre[0 * NT + k] * in_hv0 + pre[0] * din[0 * NT + k];
@@ -1126,271 +1081,244 @@ __host__ __device__ __forceinline__ void adj_tides_iter_jvp(const double* __rest
     for (int k = 0; k < NT; ++k) d109[k] = d105[k] + d108[k];
     double d110[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d110[k] = dpre[2 * NT + k] * in_H1 + pre[2] * din[7 * NT + k];
+    for (int k = 0; k < NT; ++k) d110[k] = din[6 * NT + k] * pre[8] + in_H0 * dpre[8 * NT + k];
     double d111[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d111[k] = dpre[1 * NT + k] * in_H2 + pre[1] * din[8 * NT + k];
+    for (int k = 0; k < NT; ++k) d111[k] = din[3 * NT + k] * pre[9] + in_S0 * dpre[9 * NT + k];
     double d112[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d112[k] = d110[k] - d111[k];
+    for (int k = 0; k < NT; ++k) d112[k] = d110[k] + d111[k];
     double d113[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d113[k] = dpre[0 * NT + k] * in_H2 + pre[0] * din[8 * NT + k];
+    for (int k = 0; k < NT; ++k) d113[k] = din[7 * NT + k] * pre[8] + in_H1 * dpre[8 * NT + k];
     double d114[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d114[k] = dpre[2 * NT + k] * in_H0 + pre[2] * din[6 * NT + k];
+    for (int k = 0; k < NT; ++k) d114[k] = din[4 * NT + k] * pre[9] + in_S1 * dpre[9 * NT + k];
     double d115[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d115[k] = d113[k] - d114[k];
+    for (int k = 0; k < NT; ++k) d115[k] = d113[k] + d114[k];
     double d116[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d116[k] = dpre[1 * NT + k] * in_H0 + pre[1] * din[6 * NT + k];
+    for (int k = 0; k < NT; ++k) d116[k] = din[8 * NT + k] * pre[8] + in_H2 * dpre[8 * NT + k];
     double d117[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d117[k] = dpre[0 * NT + k] * in_H1 + pre[0] * din[7 * NT + k];
+    for (int k = 0; k < NT; ++k) d117[k] = din[5 * NT + k] * pre[9] + in_S2 * dpre[9 * NT + k];
     double d118[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d118[k] = d116[k] - d117[k];
+    for (int k = 0; k < NT; ++k) d118[k] = d116[k] + d117[k];
     double d119[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d119[k] = dpre[2 * NT + k] * in_S1 + pre[2] * din[4 * NT + k];
+    for (int k = 0; k < NT; ++k) d119[k] = dpre[2 * NT + k] * t115 + pre[2] * d115[k];
     double d120[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d120[k] = dpre[1 * NT + k] * in_S2 + pre[1] * din[5 * NT + k];
+    for (int k = 0; k < NT; ++k) d120[k] = dpre[1 * NT + k] * t118 + pre[1] * d118[k];
     double d121[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d121[k] = d119[k] - d120[k];
     double d122[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d122[k] = dpre[0 * NT + k] * in_S2 + pre[0] * din[5 * NT + k];
+    for (int k = 0; k < NT; ++k) d122[k] = dpre[0 * NT + k] * t118 + pre[0] * d118[k];
     double d123[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d123[k] = dpre[2 * NT + k] * in_S0 + pre[2] * din[3 * NT + k];
+    for (int k = 0; k < NT; ++k) d123[k] = dpre[2 * NT + k] * t112 + pre[2] * d112[k];
     double d124[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d124[k] = d122[k] - d123[k];
     double d125[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d125[k] = dpre[1 * NT + k] * in_S0 + pre[1] * din[3 * NT + k];
+    for (int k = 0; k < NT; ++k) d125[k] = dpre[1 * NT + k] * t112 + pre[1] * d112[k];
     double d126[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d126[k] = dpre[0 * NT + k] * in_S1 + pre[0] * din[4 * NT + k];
+    for (int k = 0; k < NT; ++k) d126[k] = dpre[0 * NT + k] * t115 + pre[0] * d115[k];
     double d127[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d127[k] = d125[k] - d126[k];
     double d128[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d128[k] = dpre[8 * NT + k] * t109 + pre[8] * d109[k];
+    for (int k = 0; k < NT; ++k) d128[k] = dpre[10 * NT + k] * t109 + pre[10] * d109[k];
     double d129[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d129[k] = d112[k] - din[0 * NT + k];
+    for (int k = 0; k < NT; ++k) d129[k] = d121[k] + d128[k];
     double d130[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d130[k] = dpre[9 * NT + k] * t129 + pre[9] * d129[k];
+    for (int k = 0; k < NT; ++k) d130[k] = din[0 * NT + k] * pre[7] + in_hv0 * dpre[7 * NT + k];
     double d131[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d131[k] = d128[k] + d130[k];
+    for (int k = 0; k < NT; ++k) d131[k] = d129[k] - d130[k];
     double d132[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d132[k] = d121[k] - din[0 * NT + k];
+    for (int k = 0; k < NT; ++k) d132[k] = dpre[11 * NT + k] * t109 + pre[11] * d109[k];
     double d133[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d133[k] = dpre[10 * NT + k] * t132 + pre[10] * d132[k];
+    for (int k = 0; k < NT; ++k) d133[k] = d124[k] + d132[k];
     double d134[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d134[k] = d131[k] + d133[k];
+    for (int k = 0; k < NT; ++k) d134[k] = din[1 * NT + k] * pre[7] + in_hv1 * dpre[7 * NT + k];
     double d135[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d135[k] = dpre[11 * NT + k] * t109 + pre[11] * d109[k];
+    for (int k = 0; k < NT; ++k) d135[k] = d133[k] - d134[k];
     double d136[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d136[k] = d115[k] - din[1 * NT + k];
+    for (int k = 0; k < NT; ++k) d136[k] = dpre[12 * NT + k] * t109 + pre[12] * d109[k];
     double d137[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d137[k] = dpre[9 * NT + k] * t136 + pre[9] * d136[k];
+    for (int k = 0; k < NT; ++k) d137[k] = d127[k] + d136[k];
     double d138[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d138[k] = d135[k] + d137[k];
+    for (int k = 0; k < NT; ++k) d138[k] = din[2 * NT + k] * pre[7] + in_hv2 * dpre[7 * NT + k];
     double d139[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d139[k] = d124[k] - din[1 * NT + k];
-    double d140[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d140[k] = dpre[10 * NT + k] * t139 + pre[10] * d139[k];
+    for (int k = 0; k < NT; ++k) d139[k] = d137[k] - d138[k];
     double d141[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d141[k] = d138[k] + d140[k];
+    for (int k = 0; k < NT; ++k) d141[k] = d131[k] * pre[13];
     double d142[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d142[k] = dpre[12 * NT + k] * t109 + pre[12] * d109[k];
+    for (int k = 0; k < NT; ++k) d142[k] = d135[k] * pre[13];
     double d143[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d143[k] = d118[k] - din[2 * NT + k];
-    double d144[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d144[k] = dpre[9 * NT + k] * t143 + pre[9] * d143[k];
-    double d145[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d145[k] = d142[k] + d144[k];
+    for (int k = 0; k < NT; ++k) d143[k] = d139[k] * pre[13];
     double d146[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d146[k] = d127[k] - din[2 * NT + k];
+    for (int k = 0; k < NT; ++k) d146[k] = d52[k] * pre[14] + t52 * dpre[14 * NT + k];
     double d147[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d147[k] = dpre[10 * NT + k] * t146 + pre[10] * d146[k];
+    for (int k = 0; k < NT; ++k) d147[k] = d47[k] * pre[15] + t47 * dpre[15 * NT + k];
     double d148[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d148[k] = d145[k] + d147[k];
+    for (int k = 0; k < NT; ++k) d148[k] = din[3 * NT + k] * pre[16] + in_S0 * dpre[16 * NT + k];
+    double d149[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d149[k] = dpre[10 * NT + k] * t146 + pre[10] * d146[k];
     double d150[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d150[k] = d134[k] * pre[13];
+    for (int k = 0; k < NT; ++k) d150[k] = d148[k] - d149[k];
     double d151[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d151[k] = d141[k] * pre[13];
+    for (int k = 0; k < NT; ++k) d151[k] = d55[k] * pre[9] + t55 * dpre[9 * NT + k];
     double d152[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d152[k] = d148[k] * pre[13];
+    for (int k = 0; k < NT; ++k) d152[k] = d150[k] - d151[k];
+    double d153[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d153[k] = -d152[k];
+    double d154[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d154[k] = din[4 * NT + k] * pre[16] + in_S1 * dpre[16 * NT + k];
     double d155[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d155[k] = d52[k] * pre[14] + t52 * dpre[14 * NT + k];
+    for (int k = 0; k < NT; ++k) d155[k] = dpre[11 * NT + k] * t146 + pre[11] * d146[k];
     double d156[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d156[k] = d47[k] * pre[15] + t47 * dpre[15 * NT + k];
+    for (int k = 0; k < NT; ++k) d156[k] = d154[k] - d155[k];
     double d157[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d157[k] = din[3 * NT + k] * pre[16] + in_S0 * dpre[16 * NT + k];
+    for (int k = 0; k < NT; ++k) d157[k] = d58[k] * pre[9] + t58 * dpre[9 * NT + k];
     double d158[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d158[k] = dpre[8 * NT + k] * t155 + pre[8] * d155[k];
+    for (int k = 0; k < NT; ++k) d158[k] = d156[k] - d157[k];
     double d159[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d159[k] = d157[k] - d158[k];
+    for (int k = 0; k < NT; ++k) d159[k] = -d158[k];
     double d160[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d160[k] = d55[k] * pre[10] + t55 * dpre[10 * NT + k];
+    for (int k = 0; k < NT; ++k) d160[k] = din[5 * NT + k] * pre[16] + in_S2 * dpre[16 * NT + k];
     double d161[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d161[k] = d159[k] - d160[k];
+    for (int k = 0; k < NT; ++k) d161[k] = dpre[12 * NT + k] * t146 + pre[12] * d146[k];
     double d162[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d162[k] = -d161[k];
+    for (int k = 0; k < NT; ++k) d162[k] = d160[k] - d161[k];
     double d163[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d163[k] = din[4 * NT + k] * pre[16] + in_S1 * dpre[16 * NT + k];
+    for (int k = 0; k < NT; ++k) d163[k] = d61[k] * pre[9] + t61 * dpre[9 * NT + k];
     double d164[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d164[k] = dpre[11 * NT + k] * t155 + pre[11] * d155[k];
+    for (int k = 0; k < NT; ++k) d164[k] = d162[k] - d163[k];
     double d165[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d165[k] = d163[k] - d164[k];
+    for (int k = 0; k < NT; ++k) d165[k] = -d164[k];
     double d166[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d166[k] = d58[k] * pre[10] + t58 * dpre[10 * NT + k];
+    for (int k = 0; k < NT; ++k) d166[k] = din[6 * NT + k] * pre[17] + in_H0 * dpre[17 * NT + k];
     double d167[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d167[k] = d165[k] - d166[k];
+    for (int k = 0; k < NT; ++k) d167[k] = dpre[10 * NT + k] * t147 + pre[10] * d147[k];
     double d168[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d168[k] = -d167[k];
+    for (int k = 0; k < NT; ++k) d168[k] = d166[k] - d167[k];
     double d169[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d169[k] = din[5 * NT + k] * pre[16] + in_S2 * dpre[16 * NT + k];
+    for (int k = 0; k < NT; ++k) d169[k] = d55[k] * pre[8] + t55 * dpre[8 * NT + k];
     double d170[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d170[k] = dpre[12 * NT + k] * t155 + pre[12] * d155[k];
+    for (int k = 0; k < NT; ++k) d170[k] = d168[k] - d169[k];
     double d171[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d171[k] = d169[k] - d170[k];
+    for (int k = 0; k < NT; ++k) d171[k] = -d170[k];
     double d172[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d172[k] = d61[k] * pre[10] + t61 * dpre[10 * NT + k];
+    for (int k = 0; k < NT; ++k) d172[k] = din[7 * NT + k] * pre[17] + in_H1 * dpre[17 * NT + k];
     double d173[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d173[k] = d171[k] - d172[k];
+    for (int k = 0; k < NT; ++k) d173[k] = dpre[11 * NT + k] * t147 + pre[11] * d147[k];
     double d174[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d174[k] = -d173[k];
+    for (int k = 0; k < NT; ++k) d174[k] = d172[k] - d173[k];
     double d175[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d175[k] = din[6 * NT + k] * pre[17] + in_H0 * dpre[17 * NT + k];
+    for (int k = 0; k < NT; ++k) d175[k] = d58[k] * pre[8] + t58 * dpre[8 * NT + k];
     double d176[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d176[k] = dpre[8 * NT + k] * t156 + pre[8] * d156[k];
+    for (int k = 0; k < NT; ++k) d176[k] = d174[k] - d175[k];
     double d177[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d177[k] = d175[k] - d176[k];
+    for (int k = 0; k < NT; ++k) d177[k] = -d176[k];
     double d178[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d178[k] = d55[k] * pre[9] + t55 * dpre[9 * NT + k];
+    for (int k = 0; k < NT; ++k) d178[k] = din[8 * NT + k] * pre[17] + in_H2 * dpre[17 * NT + k];
     double d179[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d179[k] = d177[k] - d178[k];
+    for (int k = 0; k < NT; ++k) d179[k] = dpre[12 * NT + k] * t147 + pre[12] * d147[k];
     double d180[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d180[k] = -d179[k];
+    for (int k = 0; k < NT; ++k) d180[k] = d178[k] - d179[k];
     double d181[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d181[k] = din[7 * NT + k] * pre[17] + in_H1 * dpre[17 * NT + k];
+    for (int k = 0; k < NT; ++k) d181[k] = d61[k] * pre[8] + t61 * dpre[8 * NT + k];
     double d182[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d182[k] = dpre[11 * NT + k] * t156 + pre[11] * d156[k];
+    for (int k = 0; k < NT; ++k) d182[k] = d180[k] - d181[k];
     double d183[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d183[k] = d181[k] - d182[k];
-    double d184[NT];
+    for (int k = 0; k < NT; ++k) d183[k] = -d182[k];
+    out[0] = t141;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d184[k] = d58[k] * pre[9] + t58 * dpre[9 * NT + k];
-    double d185[NT];
+    for (int k = 0; k < NT; ++k) dout[0 * NT + k] = d141[k];
+    out[1] = t142;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d185[k] = d183[k] - d184[k];
-    double d186[NT];
+    for (int k = 0; k < NT; ++k) dout[1 * NT + k] = d142[k];
+    out[2] = t143;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d186[k] = -d185[k];
-    double d187[NT];
+    for (int k = 0; k < NT; ++k) dout[2 * NT + k] = d143[k];
+    out[3] = t153;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d187[k] = din[8 * NT + k] * pre[17] + in_H2 * dpre[17 * NT + k];
-    double d188[NT];
+    for (int k = 0; k < NT; ++k) dout[3 * NT + k] = d153[k];
+    out[4] = t159;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d188[k] = dpre[12 * NT + k] * t156 + pre[12] * d156[k];
-    double d189[NT];
+    for (int k = 0; k < NT; ++k) dout[4 * NT + k] = d159[k];
+    out[5] = t165;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d189[k] = d187[k] - d188[k];
-    double d190[NT];
+    for (int k = 0; k < NT; ++k) dout[5 * NT + k] = d165[k];
+    out[6] = t171;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d190[k] = d61[k] * pre[9] + t61 * dpre[9 * NT + k];
-    double d191[NT];
+    for (int k = 0; k < NT; ++k) dout[6 * NT + k] = d171[k];
+    out[7] = t177;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d191[k] = d189[k] - d190[k];
-    double d192[NT];
+    for (int k = 0; k < NT; ++k) dout[7 * NT + k] = d177[k];
+    out[8] = t183;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d192[k] = -d191[k];
-    out[0] = t150;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dout[0 * NT + k] = d150[k];
-    out[1] = t151;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dout[1 * NT + k] = d151[k];
-    out[2] = t152;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dout[2 * NT + k] = d152[k];
-    out[3] = t162;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dout[3 * NT + k] = d162[k];
-    out[4] = t168;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dout[4 * NT + k] = d168[k];
-    out[5] = t174;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dout[5 * NT + k] = d174[k];
-    out[6] = t180;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dout[6 * NT + k] = d180[k];
-    out[7] = t186;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dout[7 * NT + k] = d186[k];
-    out[8] = t192;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dout[8 * NT + k] = d192[k];
+    for (int k = 0; k < NT; ++k) dout[8 * NT + k] = d183[k];
 }
 
 // adj_flat: pre inputs (x, y, z); iteration inputs (hv0, hv1, hv2, S0, S1, S2, H0, H1, H2, P0, P1, P2, Q0, Q1, Q2);
@@ -2335,7 +2263,7 @@ __host__ __device__ __forceinline__ void adj_flat_iter_jvp(const double* __restr
 
 // adj_gr: pre inputs (x, y, z); iteration inputs (hv0, hv1, hv2, S0, S1, S2, H0, H1, H2, P0, P1, P2, Q0, Q1, Q2);
 // constants (hm, hmg, hmoi, m, mg, moi)
-constexpr int adj_gr_NPRE = 29;
+constexpr int adj_gr_NPRE = 24;
 
 // adj_gr: values fixed during a half kick (position, tidal parameters).
 __host__ __device__ __forceinline__ void adj_gr_pre(double in_x, double in_y, double in_z,
@@ -2402,48 +2330,60 @@ __host__ __device__ __forceinline__ void adj_gr_pre(double in_x, double in_y, do
     const double t112 = t53 * t111;
     const double t113 = 3.0 + t96;
     const double t114 = t58 * t113;
-    const double t159 = c_hm - c_m;
-    const double t185 = t34 * 6.0;
-    const double t190 = t35 * 6.0;
-    const double t195 = t36 * 6.0;
+    const double t115 = t77 - t63;
+    const double t116 = t59 - t92;
+    const double t117 = t65 + t99;
+    const double t118 = -t117;
+    const double t119 = t101 * t112;
+    const double t120 = t69 - t119;
+    const double t121 = t101 * t104;
+    const double t122 = t101 * t114;
+    const double t123 = -t122;
+    const double t156 = c_hm - c_m;
+    const double t157 = c_moi * t156;
+    const double t158 = t157 / c_m;
+    const double t159 = t156 / c_hm;
+    const double t182 = t34 * 6.0;
+    const double t183 = t33 * t182;
+    const double t184 = t35 * 6.0;
+    const double t185 = t33 * t184;
+    const double t186 = t36 * 6.0;
+    const double t187 = t33 * t186;
     const double t250 = c_m * c_hm;
     const double t251 = c_m + c_hm;
     const double t252 = t250 / t251;
     const double t253 = c_m * 1.5;
     const double t254 = t253 / c_hm;
     const double t255 = 2.0 + t254;
-    const double t256 = c_hm * 1.5;
-    const double t257 = t256 / c_m;
-    const double t258 = 2.0 + t257;
+    const double t256 = t252 * t255;
+    const double t257 = c_hm * 1.5;
+    const double t258 = t257 / c_m;
+    const double t259 = 2.0 + t258;
+    const double t260 = t252 * t259;
     pre[0] = in_x;
     pre[1] = in_y;
     pre[2] = in_z;
     pre[3] = t33;
-    pre[4] = t59;
-    pre[5] = t63;
-    pre[6] = t65;
-    pre[7] = t56;
-    pre[8] = t69;
-    pre[9] = t81;
-    pre[10] = t77;
-    pre[11] = t85;
-    pre[12] = t86;
-    pre[13] = t92;
-    pre[14] = t99;
-    pre[15] = t101;
-    pre[16] = t104;
-    pre[17] = t112;
-    pre[18] = t114;
-    pre[19] = t34;
-    pre[20] = t35;
-    pre[21] = t36;
-    pre[22] = t159;
-    pre[23] = t185;
-    pre[24] = t190;
-    pre[25] = t195;
-    pre[26] = t252;
-    pre[27] = t255;
-    pre[28] = t258;
+    pre[4] = t81;
+    pre[5] = t116;
+    pre[6] = t86;
+    pre[7] = t115;
+    pre[8] = t85;
+    pre[9] = t118;
+    pre[10] = t56;
+    pre[11] = t121;
+    pre[12] = t120;
+    pre[13] = t123;
+    pre[14] = t34;
+    pre[15] = t35;
+    pre[16] = t36;
+    pre[17] = t158;
+    pre[18] = t159;
+    pre[19] = t183;
+    pre[20] = t185;
+    pre[21] = t187;
+    pre[22] = t256;
+    pre[23] = t260;
 }
 
 // adj_gr: one midpoint iteration.  Outputs: a[3] (planet acceleration),
@@ -2461,243 +2401,189 @@ __host__ __device__ __forceinline__ void adj_gr_iter(const double* __restrict__ 
     const double t45 = t43 + t44;
     const double t46 = in_hv2 * in_hv2;
     const double t47 = t45 + t46;
-    const double t115 = t42 * t42;
-    const double t116 = t47 * pre[4];
-    const double t117 = t116 - pre[5];
-    const double t118 = pre[6] * t115;
-    const double t119 = t117 - t118;
-    const double t120 = pre[7] * t119;
-    const double t121 = t42 * pre[8];
-    const double t122 = t47 * t47;
-    const double t123 = t115 * t115;
-    const double t124 = pre[9] * t122;
-    const double t125 = pre[10] + t124;
-    const double t126 = pre[11] * t123;
-    const double t127 = t125 + t126;
-    const double t128 = pre[12] * t115;
+    const double t124 = t42 * t42;
+    const double t125 = t47 * pre[4];
+    const double t126 = pre[5] + t125;
+    const double t127 = pre[6] * t124;
+    const double t128 = t126 - t127;
     const double t129 = t47 * t128;
-    const double t130 = t127 - t129;
-    const double t131 = t47 * pre[13];
-    const double t132 = t130 - t131;
-    const double t133 = pre[14] * t115;
-    const double t134 = t132 - t133;
-    const double t135 = pre[7] * t134;
-    const double t136 = t42 * pre[15];
-    const double t137 = t47 * pre[16];
-    const double t138 = t137 - pre[17];
-    const double t139 = pre[18] * t115;
-    const double t140 = t138 - t139;
-    const double t141 = t136 * t140;
-    const double t142 = t120 + t135;
-    const double t143 = t121 + t141;
-    const double t144 = pre[19] * t142;
-    const double t145 = in_hv0 * t143;
+    const double t130 = pre[7] + t129;
+    const double t131 = pre[8] * t124;
+    const double t132 = pre[9] + t131;
+    const double t133 = t124 * t132;
+    const double t134 = t130 + t133;
+    const double t135 = pre[10] * t134;
+    const double t136 = t47 * pre[11];
+    const double t137 = pre[12] + t136;
+    const double t138 = pre[13] * t124;
+    const double t139 = t137 + t138;
+    const double t140 = t42 * t139;
+    const double t141 = pre[14] * t135;
+    const double t142 = in_hv0 * t140;
+    const double t143 = t141 + t142;
+    const double t144 = pre[15] * t135;
+    const double t145 = in_hv1 * t140;
     const double t146 = t144 + t145;
-    const double t147 = pre[20] * t142;
-    const double t148 = in_hv1 * t143;
+    const double t147 = pre[16] * t135;
+    const double t148 = in_hv2 * t140;
     const double t149 = t147 + t148;
-    const double t150 = pre[21] * t142;
-    const double t151 = in_hv2 * t143;
-    const double t152 = t150 + t151;
-    const double t153 = in_H0 * c_hmoi;
-    const double t154 = in_H1 * c_hmoi;
-    const double t155 = in_H2 * c_hmoi;
-    const double t156 = in_S0 * c_moi;
-    const double t157 = in_S1 * c_moi;
-    const double t158 = in_S2 * c_moi;
-    const double t160 = t156 / c_m;
-    const double t161 = t153 / c_hm;
+    const double t150 = in_H0 * c_hmoi;
+    const double t151 = in_H1 * c_hmoi;
+    const double t152 = in_H2 * c_hmoi;
+    const double t153 = in_S0 * c_moi;
+    const double t154 = in_S1 * c_moi;
+    const double t155 = in_S2 * c_moi;
+    const double t160 = in_S0 * pre[17];
+    const double t161 = t150 * pre[18];
     const double t162 = t160 - t161;
-    const double t163 = pre[22] * t162;
-    const double t164 = t157 / c_m;
-    const double t165 = t154 / c_hm;
-    const double t166 = t164 - t165;
-    const double t167 = pre[22] * t166;
-    const double t168 = t158 / c_m;
-    const double t169 = t155 / c_hm;
-    const double t170 = t168 - t169;
-    const double t171 = pre[22] * t170;
-    const double t172 = t153 + t156;
-    const double t173 = t154 + t157;
-    const double t174 = t155 + t158;
-    const double t175 = in_hv2 * pre[20];
-    const double t176 = in_hv1 * pre[21];
+    const double t163 = in_S1 * pre[17];
+    const double t164 = t151 * pre[18];
+    const double t165 = t163 - t164;
+    const double t166 = in_S2 * pre[17];
+    const double t167 = t152 * pre[18];
+    const double t168 = t166 - t167;
+    const double t169 = t150 + t153;
+    const double t170 = t151 + t154;
+    const double t171 = t152 + t155;
+    const double t172 = pre[1] * in_hv2;
+    const double t173 = pre[2] * in_hv1;
+    const double t174 = t172 - t173;
+    const double t175 = pre[2] * in_hv0;
+    const double t176 = pre[0] * in_hv2;
     const double t177 = t175 - t176;
-    const double t178 = in_hv0 * pre[21];
-    const double t179 = in_hv2 * pre[19];
+    const double t178 = pre[0] * in_hv1;
+    const double t179 = pre[1] * in_hv0;
     const double t180 = t178 - t179;
-    const double t181 = in_hv1 * pre[19];
-    const double t182 = in_hv0 * pre[20];
-    const double t183 = t181 - t182;
-    const double t186 = 2.0 * t172;
-    const double t187 = t163 + t186;
-    const double t188 = t177 * t187;
-    const double t189 = pre[23] * t188;
-    const double t191 = 2.0 * t173;
-    const double t192 = t167 + t191;
-    const double t193 = t180 * t192;
-    const double t194 = pre[24] * t193;
-    const double t196 = 2.0 * t174;
-    const double t197 = t171 + t196;
-    const double t198 = t183 * t197;
-    const double t199 = pre[25] * t198;
-    const double t201 = t172 * 7.0;
-    const double t202 = 3.0 * t163;
-    const double t203 = t201 + t202;
-    const double t204 = t173 * 7.0;
-    const double t205 = 3.0 * t167;
-    const double t206 = t204 + t205;
-    const double t207 = t174 * 7.0;
-    const double t208 = 3.0 * t171;
-    const double t209 = t207 + t208;
-    const double t210 = 3.0 * t172;
-    const double t211 = t163 + t210;
-    const double t212 = 3.0 * t173;
-    const double t213 = t167 + t212;
-    const double t214 = 3.0 * t174;
-    const double t215 = t171 + t214;
-    const double t216 = t42 * 3.0;
-    const double t217 = in_hv1 * t209;
-    const double t218 = in_hv2 * t206;
+    const double t188 = 2.0 * t169;
+    const double t189 = t162 + t188;
+    const double t190 = t174 * t189;
+    const double t191 = pre[19] * t190;
+    const double t192 = 2.0 * t170;
+    const double t193 = t165 + t192;
+    const double t194 = t177 * t193;
+    const double t195 = pre[20] * t194;
+    const double t196 = 2.0 * t171;
+    const double t197 = t168 + t196;
+    const double t198 = t180 * t197;
+    const double t199 = pre[21] * t198;
+    const double t200 = pre[14] * t42;
+    const double t201 = t200 - in_hv0;
+    const double t202 = pre[15] * t42;
+    const double t203 = t202 - in_hv1;
+    const double t204 = pre[16] * t42;
+    const double t205 = t204 - in_hv2;
+    const double t206 = t42 * 2.0;
+    const double t208 = t201 * 7.0;
+    const double t209 = pre[14] * t206;
+    const double t210 = t208 + t209;
+    const double t211 = t203 * 7.0;
+    const double t212 = pre[15] * t206;
+    const double t213 = t211 + t212;
+    const double t214 = t205 * 7.0;
+    const double t215 = pre[16] * t206;
+    const double t216 = t214 + t215;
+    const double t217 = t171 * t213;
+    const double t218 = t170 * t216;
     const double t219 = t217 - t218;
-    const double t220 = in_hv2 * t203;
-    const double t221 = in_hv0 * t209;
+    const double t220 = t169 * t216;
+    const double t221 = t171 * t210;
     const double t222 = t220 - t221;
-    const double t223 = in_hv0 * t206;
-    const double t224 = in_hv1 * t203;
+    const double t223 = t170 * t210;
+    const double t224 = t169 * t213;
     const double t225 = t223 - t224;
-    const double t226 = pre[20] * t215;
-    const double t227 = pre[21] * t213;
+    const double t226 = t168 * t203;
+    const double t227 = t165 * t205;
     const double t228 = t226 - t227;
-    const double t229 = pre[21] * t211;
-    const double t230 = pre[19] * t215;
+    const double t229 = t162 * t205;
+    const double t230 = t168 * t201;
     const double t231 = t229 - t230;
-    const double t232 = pre[19] * t213;
-    const double t233 = pre[20] * t211;
+    const double t232 = t165 * t201;
+    const double t233 = t162 * t203;
     const double t234 = t232 - t233;
-    const double t235 = t189 - t219;
-    const double t236 = t216 * t228;
+    const double t235 = t191 + t219;
+    const double t236 = 3.0 * t228;
     const double t237 = t235 + t236;
     const double t238 = kFA * t237;
-    const double t239 = t146 + t238;
-    const double t240 = t194 - t222;
-    const double t241 = t216 * t231;
+    const double t239 = t143 + t238;
+    const double t240 = t195 + t222;
+    const double t241 = 3.0 * t231;
     const double t242 = t240 + t241;
     const double t243 = kFA * t242;
-    const double t244 = t149 + t243;
-    const double t245 = t199 - t225;
-    const double t246 = t216 * t234;
+    const double t244 = t146 + t243;
+    const double t245 = t199 + t225;
+    const double t246 = 3.0 * t234;
     const double t247 = t245 + t246;
     const double t248 = kFA * t247;
-    const double t249 = t152 + t248;
-    const double t259 = pre[1] * in_hv2;
-    const double t260 = pre[2] * in_hv1;
-    const double t261 = t259 - t260;
-    const double t262 = pre[2] * in_hv0;
-    const double t263 = pre[0] * in_hv2;
-    const double t264 = t262 - t263;
-    const double t265 = pre[0] * in_hv1;
-    const double t266 = pre[1] * in_hv0;
-    const double t267 = t265 - t266;
-    const double t268 = pre[26] * t261;
-    const double t269 = pre[26] * t264;
-    const double t270 = pre[26] * t267;
-    const double t271 = t155 * t157;
-    const double t272 = t154 * t158;
-    const double t273 = t271 - t272;
-    const double t274 = t153 * t158;
-    const double t275 = t155 * t156;
-    const double t276 = t274 - t275;
-    const double t277 = t154 * t156;
-    const double t278 = t153 * t157;
-    const double t279 = t277 - t278;
-    const double t280 = pre[19] * t156;
-    const double t281 = pre[20] * t157;
-    const double t282 = t280 + t281;
-    const double t283 = pre[21] * t158;
+    const double t249 = t149 + t248;
+    const double t261 = pre[14] * t153;
+    const double t262 = pre[15] * t154;
+    const double t263 = t261 + t262;
+    const double t264 = pre[16] * t155;
+    const double t265 = t263 + t264;
+    const double t266 = 3.0 * t265;
+    const double t267 = pre[14] * t150;
+    const double t268 = pre[15] * t151;
+    const double t269 = t267 + t268;
+    const double t270 = pre[16] * t152;
+    const double t271 = t269 + t270;
+    const double t272 = 3.0 * t271;
+    const double t273 = t174 * pre[22];
+    const double t274 = t273 - t153;
+    const double t275 = pre[14] * t266;
+    const double t276 = t274 + t275;
+    const double t277 = t177 * pre[22];
+    const double t278 = t277 - t154;
+    const double t279 = pre[15] * t266;
+    const double t280 = t278 + t279;
+    const double t281 = t180 * pre[22];
+    const double t282 = t281 - t155;
+    const double t283 = pre[16] * t266;
     const double t284 = t282 + t283;
-    const double t285 = 3.0 * t284;
-    const double t286 = pre[19] * t153;
-    const double t287 = pre[20] * t154;
+    const double t285 = t174 * pre[23];
+    const double t286 = t285 - t150;
+    const double t287 = pre[14] * t272;
     const double t288 = t286 + t287;
-    const double t289 = pre[21] * t155;
-    const double t290 = t288 + t289;
-    const double t291 = 3.0 * t290;
-    const double t292 = t155 * t269;
-    const double t293 = t154 * t270;
-    const double t294 = t292 - t293;
-    const double t295 = t153 * t270;
-    const double t296 = t155 * t268;
-    const double t297 = t295 - t296;
-    const double t298 = t154 * t268;
-    const double t299 = t153 * t269;
-    const double t300 = t298 - t299;
-    const double t301 = t158 * t269;
-    const double t302 = t157 * t270;
-    const double t303 = t301 - t302;
-    const double t304 = t156 * t270;
-    const double t305 = t158 * t268;
-    const double t306 = t304 - t305;
-    const double t307 = t157 * t268;
-    const double t308 = t156 * t269;
-    const double t309 = t307 - t308;
-    const double t310 = pre[20] * t155;
-    const double t311 = pre[21] * t154;
-    const double t312 = t310 - t311;
-    const double t313 = pre[21] * t153;
-    const double t314 = pre[19] * t155;
-    const double t315 = t313 - t314;
-    const double t316 = pre[19] * t154;
-    const double t317 = pre[20] * t153;
-    const double t318 = t316 - t317;
-    const double t319 = pre[20] * t158;
-    const double t320 = pre[21] * t157;
-    const double t321 = t319 - t320;
-    const double t322 = pre[21] * t156;
-    const double t323 = pre[19] * t158;
-    const double t324 = t322 - t323;
-    const double t325 = pre[19] * t157;
-    const double t326 = pre[20] * t156;
-    const double t327 = t325 - t326;
-    const double t328 = pre[27] * t294;
-    const double t329 = t328 - t273;
-    const double t330 = t285 * t312;
-    const double t331 = t329 + t330;
-    const double t332 = kFA * t331;
-    const double t333 = pre[27] * t297;
-    const double t334 = t333 - t276;
-    const double t335 = t285 * t315;
-    const double t336 = t334 + t335;
-    const double t337 = kFA * t336;
-    const double t338 = pre[27] * t300;
-    const double t339 = t338 - t279;
-    const double t340 = t285 * t318;
-    const double t341 = t339 + t340;
-    const double t342 = kFA * t341;
-    const double t343 = pre[28] * t303;
-    const double t344 = t273 + t343;
-    const double t345 = t291 * t321;
-    const double t346 = t344 + t345;
-    const double t347 = kFA * t346;
-    const double t348 = pre[28] * t306;
-    const double t349 = t276 + t348;
-    const double t350 = t291 * t324;
-    const double t351 = t349 + t350;
-    const double t352 = kFA * t351;
-    const double t353 = pre[28] * t309;
-    const double t354 = t279 + t353;
-    const double t355 = t291 * t327;
-    const double t356 = t354 + t355;
-    const double t357 = kFA * t356;
+    const double t289 = t177 * pre[23];
+    const double t290 = t289 - t151;
+    const double t291 = pre[15] * t272;
+    const double t292 = t290 + t291;
+    const double t293 = t180 * pre[23];
+    const double t294 = t293 - t152;
+    const double t295 = pre[16] * t272;
+    const double t296 = t294 + t295;
+    const double t297 = t152 * t280;
+    const double t298 = t151 * t284;
+    const double t299 = t297 - t298;
+    const double t300 = t150 * t284;
+    const double t301 = t152 * t276;
+    const double t302 = t300 - t301;
+    const double t303 = t151 * t276;
+    const double t304 = t150 * t280;
+    const double t305 = t303 - t304;
+    const double t306 = t155 * t292;
+    const double t307 = t154 * t296;
+    const double t308 = t306 - t307;
+    const double t309 = t153 * t296;
+    const double t310 = t155 * t288;
+    const double t311 = t309 - t310;
+    const double t312 = t154 * t288;
+    const double t313 = t153 * t292;
+    const double t314 = t312 - t313;
+    const double t315 = kFA * t299;
+    const double t316 = kFA * t302;
+    const double t317 = kFA * t305;
+    const double t318 = kFA * t308;
+    const double t319 = kFA * t311;
+    const double t320 = kFA * t314;
     out[0] = t239;
     out[1] = t244;
     out[2] = t249;
-    out[3] = t347;
-    out[4] = t352;
-    out[5] = t357;
-    out[6] = t332;
-    out[7] = t337;
-    out[8] = t342;
+    out[3] = t318;
+    out[4] = t319;
+    out[5] = t320;
+    out[6] = t315;
+    out[7] = t316;
+    out[8] = t317;
 }
 
 // adj_gr: VJP of one iteration.  bin[15] += adjoints of (hv0, hv1, hv2, S0, S1, S2, H0, H1, H2, P0, P1, P2, Q0, Q1, Q2);
@@ -2715,641 +2601,494 @@ __host__ __device__ __forceinline__ void adj_gr_iter_vjp(const double* __restric
     const double t45 = t43 + t44;
     const double t46 = in_hv2 * in_hv2;
     const double t47 = t45 + t46;
-    const double t115 = t42 * t42;
-    const double t116 = t47 * pre[4];
-    const double t117 = t116 - pre[5];
-    const double t118 = pre[6] * t115;
-    const double t119 = t117 - t118;
-    const double t120 = pre[7] * t119;
-    const double t121 = t42 * pre[8];
-    const double t122 = t47 * t47;
-    const double t123 = t115 * t115;
-    const double t124 = pre[9] * t122;
-    const double t125 = pre[10] + t124;
-    const double t126 = pre[11] * t123;
-    const double t127 = t125 + t126;
-    const double t128 = pre[12] * t115;
+    const double t124 = t42 * t42;
+    const double t125 = t47 * pre[4];
+    const double t126 = pre[5] + t125;
+    const double t127 = pre[6] * t124;
+    const double t128 = t126 - t127;
     const double t129 = t47 * t128;
-    const double t130 = t127 - t129;
-    const double t131 = t47 * pre[13];
-    const double t132 = t130 - t131;
-    const double t133 = pre[14] * t115;
-    const double t134 = t132 - t133;
-    const double t135 = pre[7] * t134;
-    const double t136 = t42 * pre[15];
-    const double t137 = t47 * pre[16];
-    const double t138 = t137 - pre[17];
-    const double t139 = pre[18] * t115;
-    const double t140 = t138 - t139;
-    const double t141 = t136 * t140;
-    const double t142 = t120 + t135;
-    const double t143 = t121 + t141;
-    const double t144 = pre[19] * t142;
-    const double t145 = in_hv0 * t143;
+    const double t130 = pre[7] + t129;
+    const double t131 = pre[8] * t124;
+    const double t132 = pre[9] + t131;
+    const double t133 = t124 * t132;
+    const double t134 = t130 + t133;
+    const double t135 = pre[10] * t134;
+    const double t136 = t47 * pre[11];
+    const double t137 = pre[12] + t136;
+    const double t138 = pre[13] * t124;
+    const double t139 = t137 + t138;
+    const double t140 = t42 * t139;
+    const double t141 = pre[14] * t135;
+    const double t142 = in_hv0 * t140;
+    const double t143 = t141 + t142;
+    const double t144 = pre[15] * t135;
+    const double t145 = in_hv1 * t140;
     const double t146 = t144 + t145;
-    const double t147 = pre[20] * t142;
-    const double t148 = in_hv1 * t143;
+    const double t147 = pre[16] * t135;
+    const double t148 = in_hv2 * t140;
     const double t149 = t147 + t148;
-    const double t150 = pre[21] * t142;
-    const double t151 = in_hv2 * t143;
-    const double t152 = t150 + t151;
-    const double t153 = in_H0 * c_hmoi;
-    const double t154 = in_H1 * c_hmoi;
-    const double t155 = in_H2 * c_hmoi;
-    const double t156 = in_S0 * c_moi;
-    const double t157 = in_S1 * c_moi;
-    const double t158 = in_S2 * c_moi;
-    const double t160 = t156 / c_m;
-    const double t161 = t153 / c_hm;
+    const double t150 = in_H0 * c_hmoi;
+    const double t151 = in_H1 * c_hmoi;
+    const double t152 = in_H2 * c_hmoi;
+    const double t153 = in_S0 * c_moi;
+    const double t154 = in_S1 * c_moi;
+    const double t155 = in_S2 * c_moi;
+    const double t160 = in_S0 * pre[17];
+    const double t161 = t150 * pre[18];
     const double t162 = t160 - t161;
-    const double t163 = pre[22] * t162;
-    const double t164 = t157 / c_m;
-    const double t165 = t154 / c_hm;
-    const double t166 = t164 - t165;
-    const double t167 = pre[22] * t166;
-    const double t168 = t158 / c_m;
-    const double t169 = t155 / c_hm;
-    const double t170 = t168 - t169;
-    const double t171 = pre[22] * t170;
-    const double t172 = t153 + t156;
-    const double t173 = t154 + t157;
-    const double t174 = t155 + t158;
-    const double t175 = in_hv2 * pre[20];
-    const double t176 = in_hv1 * pre[21];
+    const double t163 = in_S1 * pre[17];
+    const double t164 = t151 * pre[18];
+    const double t165 = t163 - t164;
+    const double t166 = in_S2 * pre[17];
+    const double t167 = t152 * pre[18];
+    const double t168 = t166 - t167;
+    const double t169 = t150 + t153;
+    const double t170 = t151 + t154;
+    const double t171 = t152 + t155;
+    const double t172 = pre[1] * in_hv2;
+    const double t173 = pre[2] * in_hv1;
+    const double t174 = t172 - t173;
+    const double t175 = pre[2] * in_hv0;
+    const double t176 = pre[0] * in_hv2;
     const double t177 = t175 - t176;
-    const double t178 = in_hv0 * pre[21];
-    const double t179 = in_hv2 * pre[19];
+    const double t178 = pre[0] * in_hv1;
+    const double t179 = pre[1] * in_hv0;
     const double t180 = t178 - t179;
-    const double t181 = in_hv1 * pre[19];
-    const double t182 = in_hv0 * pre[20];
-    const double t183 = t181 - t182;
-    const double t186 = 2.0 * t172;
-    const double t187 = t163 + t186;
-    const double t188 = t177 * t187;
-    const double t189 = pre[23] * t188;
-    const double t191 = 2.0 * t173;
-    const double t192 = t167 + t191;
-    const double t193 = t180 * t192;
-    const double t194 = pre[24] * t193;
-    const double t196 = 2.0 * t174;
-    const double t197 = t171 + t196;
-    const double t198 = t183 * t197;
-    const double t199 = pre[25] * t198;
-    const double t201 = t172 * 7.0;
-    const double t202 = 3.0 * t163;
-    const double t203 = t201 + t202;
-    const double t204 = t173 * 7.0;
-    const double t205 = 3.0 * t167;
-    const double t206 = t204 + t205;
-    const double t207 = t174 * 7.0;
-    const double t208 = 3.0 * t171;
-    const double t209 = t207 + t208;
-    const double t210 = 3.0 * t172;
-    const double t211 = t163 + t210;
-    const double t212 = 3.0 * t173;
-    const double t213 = t167 + t212;
-    const double t214 = 3.0 * t174;
-    const double t215 = t171 + t214;
-    const double t216 = t42 * 3.0;
-    const double t217 = in_hv1 * t209;
-    const double t218 = in_hv2 * t206;
+    const double t188 = 2.0 * t169;
+    const double t189 = t162 + t188;
+    const double t190 = t174 * t189;
+    const double t191 = pre[19] * t190;
+    const double t192 = 2.0 * t170;
+    const double t193 = t165 + t192;
+    const double t194 = t177 * t193;
+    const double t195 = pre[20] * t194;
+    const double t196 = 2.0 * t171;
+    const double t197 = t168 + t196;
+    const double t198 = t180 * t197;
+    const double t199 = pre[21] * t198;
+    const double t200 = pre[14] * t42;
+    const double t201 = t200 - in_hv0;
+    const double t202 = pre[15] * t42;
+    const double t203 = t202 - in_hv1;
+    const double t204 = pre[16] * t42;
+    const double t205 = t204 - in_hv2;
+    const double t206 = t42 * 2.0;
+    const double t208 = t201 * 7.0;
+    const double t209 = pre[14] * t206;
+    const double t210 = t208 + t209;
+    const double t211 = t203 * 7.0;
+    const double t212 = pre[15] * t206;
+    const double t213 = t211 + t212;
+    const double t214 = t205 * 7.0;
+    const double t215 = pre[16] * t206;
+    const double t216 = t214 + t215;
+    const double t217 = t171 * t213;
+    const double t218 = t170 * t216;
     const double t219 = t217 - t218;
-    const double t220 = in_hv2 * t203;
-    const double t221 = in_hv0 * t209;
+    const double t220 = t169 * t216;
+    const double t221 = t171 * t210;
     const double t222 = t220 - t221;
-    const double t223 = in_hv0 * t206;
-    const double t224 = in_hv1 * t203;
+    const double t223 = t170 * t210;
+    const double t224 = t169 * t213;
     const double t225 = t223 - t224;
-    const double t226 = pre[20] * t215;
-    const double t227 = pre[21] * t213;
+    const double t226 = t168 * t203;
+    const double t227 = t165 * t205;
     const double t228 = t226 - t227;
-    const double t229 = pre[21] * t211;
-    const double t230 = pre[19] * t215;
+    const double t229 = t162 * t205;
+    const double t230 = t168 * t201;
     const double t231 = t229 - t230;
-    const double t232 = pre[19] * t213;
-    const double t233 = pre[20] * t211;
+    const double t232 = t165 * t201;
+    const double t233 = t162 * t203;
     const double t234 = t232 - t233;
-    const double t235 = t189 - t219;
-    const double t236 = t216 * t228;
+    const double t235 = t191 + t219;
+    const double t236 = 3.0 * t228;
     const double t237 = t235 + t236;
     const double t238 = kFA * t237;
-    const double t239 = t146 + t238;
-    const double t240 = t194 - t222;
-    const double t241 = t216 * t231;
+    const double t239 = t143 + t238;
+    const double t240 = t195 + t222;
+    const double t241 = 3.0 * t231;
     const double t242 = t240 + t241;
     const double t243 = kFA * t242;
-    const double t244 = t149 + t243;
-    const double t245 = t199 - t225;
-    const double t246 = t216 * t234;
+    const double t244 = t146 + t243;
+    const double t245 = t199 + t225;
+    const double t246 = 3.0 * t234;
     const double t247 = t245 + t246;
     const double t248 = kFA * t247;
-    const double t249 = t152 + t248;
-    const double t259 = pre[1] * in_hv2;
-    const double t260 = pre[2] * in_hv1;
-    const double t261 = t259 - t260;
-    const double t262 = pre[2] * in_hv0;
-    const double t263 = pre[0] * in_hv2;
-    const double t264 = t262 - t263;
-    const double t265 = pre[0] * in_hv1;
-    const double t266 = pre[1] * in_hv0;
-    const double t267 = t265 - t266;
-    const double t268 = pre[26] * t261;
-    const double t269 = pre[26] * t264;
-    const double t270 = pre[26] * t267;
-    const double t271 = t155 * t157;
-    const double t272 = t154 * t158;
-    const double t273 = t271 - t272;
-    const double t274 = t153 * t158;
-    const double t275 = t155 * t156;
-    const double t276 = t274 - t275;
-    const double t277 = t154 * t156;
-    const double t278 = t153 * t157;
-    const double t279 = t277 - t278;
-    const double t280 = pre[19] * t156;
-    const double t281 = pre[20] * t157;
-    const double t282 = t280 + t281;
-    const double t283 = pre[21] * t158;
+    const double t249 = t149 + t248;
+    const double t261 = pre[14] * t153;
+    const double t262 = pre[15] * t154;
+    const double t263 = t261 + t262;
+    const double t264 = pre[16] * t155;
+    const double t265 = t263 + t264;
+    const double t266 = 3.0 * t265;
+    const double t267 = pre[14] * t150;
+    const double t268 = pre[15] * t151;
+    const double t269 = t267 + t268;
+    const double t270 = pre[16] * t152;
+    const double t271 = t269 + t270;
+    const double t272 = 3.0 * t271;
+    const double t273 = t174 * pre[22];
+    const double t274 = t273 - t153;
+    const double t275 = pre[14] * t266;
+    const double t276 = t274 + t275;
+    const double t277 = t177 * pre[22];
+    const double t278 = t277 - t154;
+    const double t279 = pre[15] * t266;
+    const double t280 = t278 + t279;
+    const double t281 = t180 * pre[22];
+    const double t282 = t281 - t155;
+    const double t283 = pre[16] * t266;
     const double t284 = t282 + t283;
-    const double t285 = 3.0 * t284;
-    const double t286 = pre[19] * t153;
-    const double t287 = pre[20] * t154;
+    const double t285 = t174 * pre[23];
+    const double t286 = t285 - t150;
+    const double t287 = pre[14] * t272;
     const double t288 = t286 + t287;
-    const double t289 = pre[21] * t155;
-    const double t290 = t288 + t289;
-    const double t291 = 3.0 * t290;
-    const double t292 = t155 * t269;
-    const double t293 = t154 * t270;
-    const double t294 = t292 - t293;
-    const double t295 = t153 * t270;
-    const double t296 = t155 * t268;
-    const double t297 = t295 - t296;
-    const double t298 = t154 * t268;
-    const double t299 = t153 * t269;
-    const double t300 = t298 - t299;
-    const double t301 = t158 * t269;
-    const double t302 = t157 * t270;
-    const double t303 = t301 - t302;
-    const double t304 = t156 * t270;
-    const double t305 = t158 * t268;
-    const double t306 = t304 - t305;
-    const double t307 = t157 * t268;
-    const double t308 = t156 * t269;
-    const double t309 = t307 - t308;
-    const double t310 = pre[20] * t155;
-    const double t311 = pre[21] * t154;
-    const double t312 = t310 - t311;
-    const double t313 = pre[21] * t153;
-    const double t314 = pre[19] * t155;
-    const double t315 = t313 - t314;
-    const double t316 = pre[19] * t154;
-    const double t317 = pre[20] * t153;
-    const double t318 = t316 - t317;
-    const double t319 = pre[20] * t158;
-    const double t320 = pre[21] * t157;
-    const double t321 = t319 - t320;
-    const double t322 = pre[21] * t156;
-    const double t323 = pre[19] * t158;
-    const double t324 = t322 - t323;
-    const double t325 = pre[19] * t157;
-    const double t326 = pre[20] * t156;
-    const double t327 = t325 - t326;
-    const double t328 = pre[27] * t294;
-    const double t329 = t328 - t273;
-    const double t330 = t285 * t312;
-    const double t331 = t329 + t330;
-    const double t332 = kFA * t331;
-    const double t333 = pre[27] * t297;
-    const double t334 = t333 - t276;
-    const double t335 = t285 * t315;
-    const double t336 = t334 + t335;
-    const double t337 = kFA * t336;
-    const double t338 = pre[27] * t300;
-    const double t339 = t338 - t279;
-    const double t340 = t285 * t318;
-    const double t341 = t339 + t340;
-    const double t342 = kFA * t341;
-    const double t343 = pre[28] * t303;
-    const double t344 = t273 + t343;
-    const double t345 = t291 * t321;
-    const double t346 = t344 + t345;
-    const double t347 = kFA * t346;
-    const double t348 = pre[28] * t306;
-    const double t349 = t276 + t348;
-    const double t350 = t291 * t324;
-    const double t351 = t349 + t350;
-    const double t352 = kFA * t351;
-    const double t353 = pre[28] * t309;
-    const double t354 = t279 + t353;
-    const double t355 = t291 * t327;
-    const double t356 = t354 + t355;
-    const double t357 = kFA * t356;
+    const double t289 = t177 * pre[23];
+    const double t290 = t289 - t151;
+    const double t291 = pre[15] * t272;
+    const double t292 = t290 + t291;
+    const double t293 = t180 * pre[23];
+    const double t294 = t293 - t152;
+    const double t295 = pre[16] * t272;
+    const double t296 = t294 + t295;
+    const double t297 = t152 * t280;
+    const double t298 = t151 * t284;
+    const double t299 = t297 - t298;
+    const double t300 = t150 * t284;
+    const double t301 = t152 * t276;
+    const double t302 = t300 - t301;
+    const double t303 = t151 * t276;
+    const double t304 = t150 * t280;
+    const double t305 = t303 - t304;
+    const double t306 = t155 * t292;
+    const double t307 = t154 * t296;
+    const double t308 = t306 - t307;
+    const double t309 = t153 * t296;
+    const double t310 = t155 * t288;
+    const double t311 = t309 - t310;
+    const double t312 = t154 * t288;
+    const double t313 = t153 * t292;
+    const double t314 = t312 - t313;
+    const double t315 = kFA * t299;
+    const double t316 = kFA * t302;
+    const double t317 = kFA * t305;
+    const double t318 = kFA * t308;
+    const double t319 = kFA * t311;
+    const double t320 = kFA * t314;
     double b239 = bout[0];
     double b244 = bout[1];
     double b249 = bout[2];
-    double b347 = bout[3];
-    double b352 = bout[4];
-    double b357 = bout[5];
-    double b332 = bout[6];
-    double b337 = bout[7];
-    double b342 = bout[8];
-    double b356 = b357 * kFA;
-    double b354 = b356;
-    double b355 = b356;
-    double b291 = b355 * t327;
-    double b327 = b355 * t291;
-    double b279 = b354;
-    double b353 = b354;
-    double b309 = b353 * pre[28];
-    double b351 = b352 * kFA;
-    double b349 = b351;
-    double b350 = b351;
-    b291 += b350 * t324;
-    double b324 = b350 * t291;
-    double b276 = b349;
-    double b348 = b349;
-    double b306 = b348 * pre[28];
-    double b346 = b347 * kFA;
-    double b344 = b346;
-    double b345 = b346;
-    b291 += b345 * t321;
-    double b321 = b345 * t291;
-    double b273 = b344;
-    double b343 = b344;
-    double b303 = b343 * pre[28];
-    double b341 = b342 * kFA;
-    double b339 = b341;
-    double b340 = b341;
-    double b285 = b340 * t318;
-    double b318 = b340 * t285;
-    double b338 = b339;
-    b279 += -b339;
-    double b300 = b338 * pre[27];
-    double b336 = b337 * kFA;
-    double b334 = b336;
-    double b335 = b336;
-    b285 += b335 * t315;
-    double b315 = b335 * t285;
-    double b333 = b334;
-    b276 += -b334;
-    double b297 = b333 * pre[27];
-    double b331 = b332 * kFA;
-    double b329 = b331;
-    double b330 = b331;
-    b285 += b330 * t312;
-    double b312 = b330 * t285;
-    double b328 = b329;
-    b273 += -b329;
-    double b294 = b328 * pre[27];
-    double b325 = b327;
-    double b326 = -b327;
-    bpre[20] += b326 * t156;
-    double b156 = b326 * pre[20];
-    bpre[19] += b325 * t157;
-    double b157 = b325 * pre[19];
-    double b322 = b324;
-    double b323 = -b324;
-    bpre[19] += b323 * t158;
-    double b158 = b323 * pre[19];
-    bpre[21] += b322 * t156;
-    b156 += b322 * pre[21];
-    double b319 = b321;
-    double b320 = -b321;
-    bpre[21] += b320 * t157;
-    b157 += b320 * pre[21];
-    bpre[20] += b319 * t158;
-    b158 += b319 * pre[20];
-    double b316 = b318;
-    double b317 = -b318;
-    bpre[20] += b317 * t153;
-    double b153 = b317 * pre[20];
-    bpre[19] += b316 * t154;
-    double b154 = b316 * pre[19];
-    double b313 = b315;
-    double b314 = -b315;
-    bpre[19] += b314 * t155;
-    double b155 = b314 * pre[19];
-    bpre[21] += b313 * t153;
-    b153 += b313 * pre[21];
-    double b310 = b312;
-    double b311 = -b312;
-    bpre[21] += b311 * t154;
-    b154 += b311 * pre[21];
-    bpre[20] += b310 * t155;
-    b155 += b310 * pre[20];
-    double b307 = b309;
-    double b308 = -b309;
-    b156 += b308 * t269;
-    double b269 = b308 * t156;
-    b157 += b307 * t268;
-    double b268 = b307 * t157;
-    double b304 = b306;
-    double b305 = -b306;
-    b158 += b305 * t268;
-    b268 += b305 * t158;
-    b156 += b304 * t270;
-    double b270 = b304 * t156;
-    double b301 = b303;
-    double b302 = -b303;
-    b157 += b302 * t270;
-    b270 += b302 * t157;
-    b158 += b301 * t269;
-    b269 += b301 * t158;
-    double b298 = b300;
-    double b299 = -b300;
-    b153 += b299 * t269;
-    b269 += b299 * t153;
-    b154 += b298 * t268;
-    b268 += b298 * t154;
-    double b295 = b297;
-    double b296 = -b297;
-    b155 += b296 * t268;
-    b268 += b296 * t155;
-    b153 += b295 * t270;
-    b270 += b295 * t153;
-    double b292 = b294;
-    double b293 = -b294;
-    b154 += b293 * t270;
-    b270 += b293 * t154;
-    b155 += b292 * t269;
-    b269 += b292 * t155;
-    double b290 = b291 * 3.0;
-    double b288 = b290;
+    double b318 = bout[3];
+    double b319 = bout[4];
+    double b320 = bout[5];
+    double b315 = bout[6];
+    double b316 = bout[7];
+    double b317 = bout[8];
+    double b314 = b320 * kFA;
+    double b311 = b319 * kFA;
+    double b308 = b318 * kFA;
+    double b305 = b317 * kFA;
+    double b302 = b316 * kFA;
+    double b299 = b315 * kFA;
+    double b312 = b314;
+    double b313 = -b314;
+    double b153 = b313 * t292;
+    double b292 = b313 * t153;
+    double b154 = b312 * t288;
+    double b288 = b312 * t154;
+    double b309 = b311;
+    double b310 = -b311;
+    double b155 = b310 * t288;
+    b288 += b310 * t155;
+    b153 += b309 * t296;
+    double b296 = b309 * t153;
+    double b306 = b308;
+    double b307 = -b308;
+    b154 += b307 * t296;
+    b296 += b307 * t154;
+    b155 += b306 * t292;
+    b292 += b306 * t155;
+    double b303 = b305;
+    double b304 = -b305;
+    double b150 = b304 * t280;
+    double b280 = b304 * t150;
+    double b151 = b303 * t276;
+    double b276 = b303 * t151;
+    double b300 = b302;
+    double b301 = -b302;
+    double b152 = b301 * t276;
+    b276 += b301 * t152;
+    b150 += b300 * t284;
+    double b284 = b300 * t150;
+    double b297 = b299;
+    double b298 = -b299;
+    b151 += b298 * t284;
+    b284 += b298 * t151;
+    b152 += b297 * t280;
+    b280 += b297 * t152;
+    double b294 = b296;
+    double b295 = b296;
+    bpre[16] += b295 * t272;
+    double b272 = b295 * pre[16];
+    double b293 = b294;
+    b152 += -b294;
+    double b180 = b293 * pre[23];
+    double b290 = b292;
+    double b291 = b292;
+    bpre[15] += b291 * t272;
+    b272 += b291 * pre[15];
     double b289 = b290;
-    bpre[21] += b289 * t155;
-    b155 += b289 * pre[21];
+    b151 += -b290;
+    double b177 = b289 * pre[23];
     double b286 = b288;
     double b287 = b288;
-    bpre[20] += b287 * t154;
-    b154 += b287 * pre[20];
-    bpre[19] += b286 * t153;
-    b153 += b286 * pre[19];
-    double b284 = b285 * 3.0;
+    bpre[14] += b287 * t272;
+    b272 += b287 * pre[14];
+    double b285 = b286;
+    b150 += -b286;
+    double b174 = b285 * pre[23];
     double b282 = b284;
     double b283 = b284;
-    bpre[21] += b283 * t158;
-    b158 += b283 * pre[21];
-    double b280 = b282;
+    bpre[16] += b283 * t266;
+    double b266 = b283 * pre[16];
     double b281 = b282;
-    bpre[20] += b281 * t157;
-    b157 += b281 * pre[20];
-    bpre[19] += b280 * t156;
-    b156 += b280 * pre[19];
-    double b277 = b279;
-    double b278 = -b279;
-    b153 += b278 * t157;
-    b157 += b278 * t153;
-    b154 += b277 * t156;
-    b156 += b277 * t154;
+    b155 += -b282;
+    b180 += b281 * pre[22];
+    double b278 = b280;
+    double b279 = b280;
+    bpre[15] += b279 * t266;
+    b266 += b279 * pre[15];
+    double b277 = b278;
+    b154 += -b278;
+    b177 += b277 * pre[22];
     double b274 = b276;
-    double b275 = -b276;
-    b155 += b275 * t156;
-    b156 += b275 * t155;
-    b153 += b274 * t158;
-    b158 += b274 * t153;
-    double b271 = b273;
-    double b272 = -b273;
-    b154 += b272 * t158;
-    b158 += b272 * t154;
-    b155 += b271 * t157;
-    b157 += b271 * t155;
-    double b267 = b270 * pre[26];
-    double b264 = b269 * pre[26];
-    double b261 = b268 * pre[26];
-    double b265 = b267;
-    double b266 = -b267;
-    bpre[1] += b266 * in_hv0;
-    double b_hv0 = b266 * pre[1];
-    bpre[0] += b265 * in_hv1;
-    double b_hv1 = b265 * pre[0];
-    double b262 = b264;
-    double b263 = -b264;
-    bpre[0] += b263 * in_hv2;
-    double b_hv2 = b263 * pre[0];
-    bpre[2] += b262 * in_hv0;
-    b_hv0 += b262 * pre[2];
-    double b259 = b261;
-    double b260 = -b261;
-    bpre[2] += b260 * in_hv1;
-    b_hv1 += b260 * pre[2];
-    bpre[1] += b259 * in_hv2;
-    b_hv2 += b259 * pre[1];
-    double b152 = b249;
+    double b275 = b276;
+    bpre[14] += b275 * t266;
+    b266 += b275 * pre[14];
+    double b273 = b274;
+    b153 += -b274;
+    b174 += b273 * pre[22];
+    double b271 = b272 * 3.0;
+    double b269 = b271;
+    double b270 = b271;
+    bpre[16] += b270 * t152;
+    b152 += b270 * pre[16];
+    double b267 = b269;
+    double b268 = b269;
+    bpre[15] += b268 * t151;
+    b151 += b268 * pre[15];
+    bpre[14] += b267 * t150;
+    b150 += b267 * pre[14];
+    double b265 = b266 * 3.0;
+    double b263 = b265;
+    double b264 = b265;
+    bpre[16] += b264 * t155;
+    b155 += b264 * pre[16];
+    double b261 = b263;
+    double b262 = b263;
+    bpre[15] += b262 * t154;
+    b154 += b262 * pre[15];
+    bpre[14] += b261 * t153;
+    b153 += b261 * pre[14];
+    double b149 = b249;
     double b248 = b249;
     double b247 = b248 * kFA;
     double b245 = b247;
     double b246 = b247;
-    double b216 = b246 * t234;
-    double b234 = b246 * t216;
+    double b234 = b246 * 3.0;
     double b199 = b245;
-    double b225 = -b245;
-    double b149 = b244;
+    double b225 = b245;
+    double b146 = b244;
     double b243 = b244;
     double b242 = b243 * kFA;
     double b240 = b242;
     double b241 = b242;
-    b216 += b241 * t231;
-    double b231 = b241 * t216;
-    double b194 = b240;
-    double b222 = -b240;
-    double b146 = b239;
+    double b231 = b241 * 3.0;
+    double b195 = b240;
+    double b222 = b240;
+    double b143 = b239;
     double b238 = b239;
     double b237 = b238 * kFA;
     double b235 = b237;
     double b236 = b237;
-    b216 += b236 * t228;
-    double b228 = b236 * t216;
-    double b189 = b235;
-    double b219 = -b235;
+    double b228 = b236 * 3.0;
+    double b191 = b235;
+    double b219 = b235;
     double b232 = b234;
     double b233 = -b234;
-    bpre[20] += b233 * t211;
-    double b211 = b233 * pre[20];
-    bpre[19] += b232 * t213;
-    double b213 = b232 * pre[19];
+    double b162 = b233 * t203;
+    double b203 = b233 * t162;
+    double b165 = b232 * t201;
+    double b201 = b232 * t165;
     double b229 = b231;
     double b230 = -b231;
-    bpre[19] += b230 * t215;
-    double b215 = b230 * pre[19];
-    bpre[21] += b229 * t211;
-    b211 += b229 * pre[21];
+    double b168 = b230 * t201;
+    b201 += b230 * t168;
+    b162 += b229 * t205;
+    double b205 = b229 * t162;
     double b226 = b228;
     double b227 = -b228;
-    bpre[21] += b227 * t213;
-    b213 += b227 * pre[21];
-    bpre[20] += b226 * t215;
-    b215 += b226 * pre[20];
+    b165 += b227 * t205;
+    b205 += b227 * t165;
+    b168 += b226 * t203;
+    b203 += b226 * t168;
     double b223 = b225;
     double b224 = -b225;
-    b_hv1 += b224 * t203;
-    double b203 = b224 * in_hv1;
-    b_hv0 += b223 * t206;
-    double b206 = b223 * in_hv0;
+    double b169 = b224 * t213;
+    double b213 = b224 * t169;
+    double b170 = b223 * t210;
+    double b210 = b223 * t170;
     double b220 = b222;
     double b221 = -b222;
-    b_hv0 += b221 * t209;
-    double b209 = b221 * in_hv0;
-    b_hv2 += b220 * t203;
-    b203 += b220 * in_hv2;
+    double b171 = b221 * t210;
+    b210 += b221 * t171;
+    b169 += b220 * t216;
+    double b216 = b220 * t169;
     double b217 = b219;
     double b218 = -b219;
-    b_hv2 += b218 * t206;
-    b206 += b218 * in_hv2;
-    b_hv1 += b217 * t209;
-    b209 += b217 * in_hv1;
-    double b42 = b216 * 3.0;
-    double b171 = b215;
-    double b214 = b215;
-    double b174 = b214 * 3.0;
-    double b167 = b213;
+    b170 += b218 * t216;
+    b216 += b218 * t170;
+    b171 += b217 * t213;
+    b213 += b217 * t171;
+    double b214 = b216;
+    double b215 = b216;
+    bpre[16] += b215 * t206;
+    double b206 = b215 * pre[16];
+    b205 += b214 * 7.0;
+    double b211 = b213;
     double b212 = b213;
-    double b173 = b212 * 3.0;
-    double b163 = b211;
-    double b210 = b211;
-    double b172 = b210 * 3.0;
-    double b207 = b209;
-    double b208 = b209;
-    b171 += b208 * 3.0;
-    b174 += b207 * 7.0;
-    double b204 = b206;
-    double b205 = b206;
-    b167 += b205 * 3.0;
-    b173 += b204 * 7.0;
-    double b201 = b203;
+    bpre[15] += b212 * t206;
+    b206 += b212 * pre[15];
+    b203 += b211 * 7.0;
+    double b208 = b210;
+    double b209 = b210;
+    bpre[14] += b209 * t206;
+    b206 += b209 * pre[14];
+    b201 += b208 * 7.0;
+    double b42 = b206 * 2.0;
+    double b204 = b205;
+    double b_hv2 = -b205;
+    bpre[16] += b204 * t42;
+    b42 += b204 * pre[16];
     double b202 = b203;
-    b163 += b202 * 3.0;
-    b172 += b201 * 7.0;
-    bpre[25] += b199 * t198;
-    double b198 = b199 * pre[25];
-    double b183 = b198 * t197;
-    double b197 = b198 * t183;
-    b171 += b197;
+    double b_hv1 = -b203;
+    bpre[15] += b202 * t42;
+    b42 += b202 * pre[15];
+    double b200 = b201;
+    double b_hv0 = -b201;
+    bpre[14] += b200 * t42;
+    b42 += b200 * pre[14];
+    bpre[21] += b199 * t198;
+    double b198 = b199 * pre[21];
+    b180 += b198 * t197;
+    double b197 = b198 * t180;
+    b168 += b197;
     double b196 = b197;
-    b174 += b196 * 2.0;
-    bpre[24] += b194 * t193;
-    double b193 = b194 * pre[24];
-    double b180 = b193 * t192;
-    double b192 = b193 * t180;
-    b167 += b192;
-    double b191 = b192;
-    b173 += b191 * 2.0;
-    bpre[23] += b189 * t188;
-    double b188 = b189 * pre[23];
-    double b177 = b188 * t187;
-    double b187 = b188 * t177;
-    b163 += b187;
-    double b186 = b187;
-    b172 += b186 * 2.0;
-    double b181 = b183;
-    double b182 = -b183;
-    b_hv0 += b182 * pre[20];
-    bpre[20] += b182 * in_hv0;
-    b_hv1 += b181 * pre[19];
-    bpre[19] += b181 * in_hv1;
+    b171 += b196 * 2.0;
+    bpre[20] += b195 * t194;
+    double b194 = b195 * pre[20];
+    b177 += b194 * t193;
+    double b193 = b194 * t177;
+    b165 += b193;
+    double b192 = b193;
+    b170 += b192 * 2.0;
+    bpre[19] += b191 * t190;
+    double b190 = b191 * pre[19];
+    b174 += b190 * t189;
+    double b189 = b190 * t174;
+    b162 += b189;
+    double b188 = b189;
+    b169 += b188 * 2.0;
     double b178 = b180;
     double b179 = -b180;
-    b_hv2 += b179 * pre[19];
-    bpre[19] += b179 * in_hv2;
-    b_hv0 += b178 * pre[21];
-    bpre[21] += b178 * in_hv0;
+    bpre[1] += b179 * in_hv0;
+    b_hv0 += b179 * pre[1];
+    bpre[0] += b178 * in_hv1;
+    b_hv1 += b178 * pre[0];
     double b175 = b177;
     double b176 = -b177;
-    b_hv1 += b176 * pre[21];
-    bpre[21] += b176 * in_hv1;
-    b_hv2 += b175 * pre[20];
-    bpre[20] += b175 * in_hv2;
-    b155 += b174;
-    b158 += b174;
-    b154 += b173;
-    b157 += b173;
-    b153 += b172;
-    b156 += b172;
-    double b170 = b171 * pre[22];
-    double b168 = b170;
-    double b169 = -b170;
-    b155 += b169 / c_hm;
-    b158 += b168 / c_m;
-    double b166 = b167 * pre[22];
-    double b164 = b166;
-    double b165 = -b166;
-    b154 += b165 / c_hm;
-    b157 += b164 / c_m;
-    double b162 = b163 * pre[22];
+    bpre[0] += b176 * in_hv2;
+    b_hv2 += b176 * pre[0];
+    bpre[2] += b175 * in_hv0;
+    b_hv0 += b175 * pre[2];
+    double b172 = b174;
+    double b173 = -b174;
+    bpre[2] += b173 * in_hv1;
+    b_hv1 += b173 * pre[2];
+    bpre[1] += b172 * in_hv2;
+    b_hv2 += b172 * pre[1];
+    b152 += b171;
+    b155 += b171;
+    b151 += b170;
+    b154 += b170;
+    b150 += b169;
+    b153 += b169;
+    double b166 = b168;
+    double b167 = -b168;
+    b152 += b167 * pre[18];
+    double b_S2 = b166 * pre[17];
+    double b163 = b165;
+    double b164 = -b165;
+    b151 += b164 * pre[18];
+    double b_S1 = b163 * pre[17];
     double b160 = b162;
     double b161 = -b162;
-    b153 += b161 / c_hm;
-    b156 += b160 / c_m;
-    double b_S2 = b158 * c_moi;
-    double b_S1 = b157 * c_moi;
-    double b_S0 = b156 * c_moi;
-    double b_H2 = b155 * c_hmoi;
-    double b_H1 = b154 * c_hmoi;
-    double b_H0 = b153 * c_hmoi;
-    double b150 = b152;
-    double b151 = b152;
-    b_hv2 += b151 * t143;
-    double b143 = b151 * in_hv2;
-    bpre[21] += b150 * t142;
-    double b142 = b150 * pre[21];
+    b150 += b161 * pre[18];
+    double b_S0 = b160 * pre[17];
+    b_S2 += b155 * c_moi;
+    b_S1 += b154 * c_moi;
+    b_S0 += b153 * c_moi;
+    double b_H2 = b152 * c_hmoi;
+    double b_H1 = b151 * c_hmoi;
+    double b_H0 = b150 * c_hmoi;
     double b147 = b149;
     double b148 = b149;
-    b_hv1 += b148 * t143;
-    b143 += b148 * in_hv1;
-    bpre[20] += b147 * t142;
-    b142 += b147 * pre[20];
+    b_hv2 += b148 * t140;
+    double b140 = b148 * in_hv2;
+    bpre[16] += b147 * t135;
+    double b135 = b147 * pre[16];
     double b144 = b146;
     double b145 = b146;
-    b_hv0 += b145 * t143;
-    b143 += b145 * in_hv0;
-    bpre[19] += b144 * t142;
-    b142 += b144 * pre[19];
-    double b121 = b143;
+    b_hv1 += b145 * t140;
+    b140 += b145 * in_hv1;
+    bpre[15] += b144 * t135;
+    b135 += b144 * pre[15];
     double b141 = b143;
-    double b120 = b142;
-    double b135 = b142;
-    double b136 = b141 * t140;
-    double b140 = b141 * t136;
-    double b138 = b140;
-    double b139 = -b140;
-    double b115 = b139 * pre[18];
-    double b137 = b138;
-    bpre[17] += -b138;
-    double b47 = b137 * pre[16];
-    b42 += b136 * pre[15];
-    bpre[15] += b136 * t42;
-    bpre[7] += b135 * t134;
-    double b134 = b135 * pre[7];
-    double b132 = b134;
-    double b133 = -b134;
-    bpre[14] += b133 * t115;
-    b115 += b133 * pre[14];
-    double b130 = b132;
-    double b131 = -b132;
-    b47 += b131 * pre[13];
-    bpre[13] += b131 * t47;
-    double b127 = b130;
-    double b129 = -b130;
+    double b142 = b143;
+    b_hv0 += b142 * t140;
+    b140 += b142 * in_hv0;
+    bpre[14] += b141 * t135;
+    b135 += b141 * pre[14];
+    b42 += b140 * t139;
+    double b139 = b140 * t42;
+    double b137 = b139;
+    double b138 = b139;
+    bpre[13] += b138 * t124;
+    double b124 = b138 * pre[13];
+    bpre[12] += b137;
+    double b136 = b137;
+    double b47 = b136 * pre[11];
+    bpre[11] += b136 * t47;
+    bpre[10] += b135 * t134;
+    double b134 = b135 * pre[10];
+    double b130 = b134;
+    double b133 = b134;
+    b124 += b133 * t132;
+    double b132 = b133 * t124;
+    bpre[9] += b132;
+    double b131 = b132;
+    b124 += b131 * pre[8];
+    bpre[7] += b130;
+    double b129 = b130;
     b47 += b129 * t128;
     double b128 = b129 * t47;
-    b115 += b128 * pre[12];
-    double b125 = b127;
-    double b126 = b127;
-    double b123 = b126 * pre[11];
-    bpre[10] += b125;
-    double b124 = b125;
-    double b122 = b124 * pre[9];
-    b115 += 2.0 * b123 * t115;
-    b47 += 2.0 * b122 * t47;
-    b42 += b121 * pre[8];
-    bpre[8] += b121 * t42;
-    bpre[7] += b120 * t119;
-    double b119 = b120 * pre[7];
-    double b117 = b119;
-    double b118 = -b119;
-    b115 += b118 * pre[6];
-    double b116 = b117;
-    bpre[5] += -b117;
-    b47 += b116 * pre[4];
-    b42 += 2.0 * b115 * t42;
+    double b126 = b128;
+    double b127 = -b128;
+    b124 += b127 * pre[6];
+    bpre[5] += b126;
+    double b125 = b126;
+    b47 += b125 * pre[4];
+    b42 += 2.0 * b124 * t42;
     double b45 = b47;
     double b46 = b47;
     b_hv2 += 2.0 * b46 * in_hv2;
@@ -3445,40 +3184,74 @@ __host__ __device__ __forceinline__ void adj_gr_pre_vjp(double in_x, double in_y
     const double t112 = t53 * t111;
     const double t113 = 3.0 + t96;
     const double t114 = t58 * t113;
-    const double t159 = c_hm - c_m;
-    const double t185 = t34 * 6.0;
-    const double t190 = t35 * 6.0;
-    const double t195 = t36 * 6.0;
+    const double t115 = t77 - t63;
+    const double t116 = t59 - t92;
+    const double t117 = t65 + t99;
+    const double t118 = -t117;
+    const double t119 = t101 * t112;
+    const double t120 = t69 - t119;
+    const double t121 = t101 * t104;
+    const double t122 = t101 * t114;
+    const double t123 = -t122;
+    const double t156 = c_hm - c_m;
+    const double t157 = c_moi * t156;
+    const double t158 = t157 / c_m;
+    const double t159 = t156 / c_hm;
+    const double t182 = t34 * 6.0;
+    const double t183 = t33 * t182;
+    const double t184 = t35 * 6.0;
+    const double t185 = t33 * t184;
+    const double t186 = t36 * 6.0;
+    const double t187 = t33 * t186;
     const double t250 = c_m * c_hm;
     const double t251 = c_m + c_hm;
     const double t252 = t250 / t251;
     const double t253 = c_m * 1.5;
     const double t254 = t253 / c_hm;
     const double t255 = 2.0 + t254;
-    const double t256 = c_hm * 1.5;
-    const double t257 = t256 / c_m;
-    const double t258 = 2.0 + t257;
+    const double t256 = t252 * t255;
+    const double t257 = c_hm * 1.5;
+    const double t258 = t257 / c_m;
+    const double t259 = 2.0 + t258;
+    const double t260 = t252 * t259;
     double b_x = bpre[0];
     double b_y = bpre[1];
     double b_z = bpre[2];
     double b33 = bpre[3];
-    double b63 = bpre[5];
-    double b56 = bpre[7];
-    double b69 = bpre[8];
-    double b77 = bpre[10];
-    double b92 = bpre[13];
-    double b99 = bpre[14];
-    double b101 = bpre[15];
-    double b112 = bpre[17];
-    double b34 = bpre[19];
-    double b35 = bpre[20];
-    double b36 = bpre[21];
-    double b185 = bpre[23];
-    double b190 = bpre[24];
-    double b195 = bpre[25];
-    b36 += b195 * 6.0;
-    b35 += b190 * 6.0;
-    b34 += b185 * 6.0;
+    double b116 = bpre[5];
+    double b115 = bpre[7];
+    double b118 = bpre[9];
+    double b56 = bpre[10];
+    double b121 = bpre[11];
+    double b120 = bpre[12];
+    double b123 = bpre[13];
+    double b34 = bpre[14];
+    double b35 = bpre[15];
+    double b36 = bpre[16];
+    double b183 = bpre[19];
+    double b185 = bpre[20];
+    double b187 = bpre[21];
+    b33 += b187 * t186;
+    double b186 = b187 * t33;
+    b36 += b186 * 6.0;
+    b33 += b185 * t184;
+    double b184 = b185 * t33;
+    b35 += b184 * 6.0;
+    b33 += b183 * t182;
+    double b182 = b183 * t33;
+    b34 += b182 * 6.0;
+    double b122 = -b123;
+    double b101 = b122 * t114;
+    b101 += b121 * t104;
+    double b69 = b120;
+    double b119 = -b120;
+    b101 += b119 * t112;
+    double b112 = b119 * t101;
+    double b117 = -b118;
+    double b99 = b117;
+    double b92 = -b116;
+    double b77 = b115;
+    double b63 = -b115;
     double b53 = b112 * t111;
     b56 += b101 * -0.5;
     b53 += b99 * t98;
@@ -3580,19 +3353,36 @@ __host__ __device__ __forceinline__ void adj_gr_pre_jvp(double in_x, double in_y
     const double t112 = t53 * t111;
     const double t113 = 3.0 + t96;
     const double t114 = t58 * t113;
-    const double t159 = c_hm - c_m;
-    const double t185 = t34 * 6.0;
-    const double t190 = t35 * 6.0;
-    const double t195 = t36 * 6.0;
+    const double t115 = t77 - t63;
+    const double t116 = t59 - t92;
+    const double t117 = t65 + t99;
+    const double t118 = -t117;
+    const double t119 = t101 * t112;
+    const double t120 = t69 - t119;
+    const double t121 = t101 * t104;
+    const double t122 = t101 * t114;
+    const double t123 = -t122;
+    const double t156 = c_hm - c_m;
+    const double t157 = c_moi * t156;
+    const double t158 = t157 / c_m;
+    const double t159 = t156 / c_hm;
+    const double t182 = t34 * 6.0;
+    const double t183 = t33 * t182;
+    const double t184 = t35 * 6.0;
+    const double t185 = t33 * t184;
+    const double t186 = t36 * 6.0;
+    const double t187 = t33 * t186;
     const double t250 = c_m * c_hm;
     const double t251 = c_m + c_hm;
     const double t252 = t250 / t251;
     const double t253 = c_m * 1.5;
     const double t254 = t253 / c_hm;
     const double t255 = 2.0 + t254;
-    const double t256 = c_hm * 1.5;
-    const double t257 = t256 / c_m;
-    const double t258 = 2.0 + t257;
+    const double t256 = t252 * t255;
+    const double t257 = c_hm * 1.5;
+    const double t258 = t257 / c_m;
+    const double t259 = 2.0 + t258;
+    const double t260 = t252 * t259;
     double d18[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d18[k] = 2.0 * in_x * din[0 * NT + k];
@@ -3665,15 +3455,51 @@ __host__ __device__ __forceinline__ void adj_gr_pre_jvp(double in_x, double in_y
     double d112[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d112[k] = d53[k] * t111;
+    double d115[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d115[k] = d77[k] - d63[k];
+    double d116[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d116[k] = -d92[k];
+    double d117[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d117[k] = d99[k];
+    double d118[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d118[k] = -d117[k];
+    double d119[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d119[k] = d101[k] * t112 + t101 * d112[k];
+    double d120[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d120[k] = d69[k] - d119[k];
+    double d121[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d121[k] = d101[k] * t104;
+    double d122[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d122[k] = d101[k] * t114;
+    double d123[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d123[k] = -d122[k];
+    double d182[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d182[k] = d34[k] * 6.0;
+    double d183[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d183[k] = d33[k] * t182 + t33 * d182[k];
+    double d184[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d184[k] = d35[k] * 6.0;
     double d185[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d185[k] = d34[k] * 6.0;
-    double d190[NT];
+    for (int k = 0; k < NT; ++k) d185[k] = d33[k] * t184 + t33 * d184[k];
+    double d186[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d190[k] = d35[k] * 6.0;
-    double d195[NT];
+    for (int k = 0; k < NT; ++k) d186[k] = d36[k] * 6.0;
+    double d187[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d195[k] = d36[k] * 6.0;
+    for (int k = 0; k < NT; ++k) d187[k] = d33[k] * t186 + t33 * d186[k];
     pre[0] = in_x;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[0 * NT + k] = din[0 * NT + k];
@@ -3686,81 +3512,66 @@ __host__ __device__ __forceinline__ void adj_gr_pre_jvp(double in_x, double in_y
     pre[3] = t33;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[3 * NT + k] = d33[k];
-    pre[4] = t59;
+    pre[4] = t81;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[4 * NT + k] = 0.0;
-    pre[5] = t63;
+    pre[5] = t116;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[5 * NT + k] = d63[k];
-    pre[6] = t65;
+    for (int k = 0; k < NT; ++k) dpre[5 * NT + k] = d116[k];
+    pre[6] = t86;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[6 * NT + k] = 0.0;
-    pre[7] = t56;
+    pre[7] = t115;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[7 * NT + k] = d56[k];
-    pre[8] = t69;
+    for (int k = 0; k < NT; ++k) dpre[7 * NT + k] = d115[k];
+    pre[8] = t85;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[8 * NT + k] = d69[k];
-    pre[9] = t81;
+    for (int k = 0; k < NT; ++k) dpre[8 * NT + k] = 0.0;
+    pre[9] = t118;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[9 * NT + k] = 0.0;
-    pre[10] = t77;
+    for (int k = 0; k < NT; ++k) dpre[9 * NT + k] = d118[k];
+    pre[10] = t56;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[10 * NT + k] = d77[k];
-    pre[11] = t85;
+    for (int k = 0; k < NT; ++k) dpre[10 * NT + k] = d56[k];
+    pre[11] = t121;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[11 * NT + k] = 0.0;
-    pre[12] = t86;
+    for (int k = 0; k < NT; ++k) dpre[11 * NT + k] = d121[k];
+    pre[12] = t120;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[12 * NT + k] = 0.0;
-    pre[13] = t92;
+    for (int k = 0; k < NT; ++k) dpre[12 * NT + k] = d120[k];
+    pre[13] = t123;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[13 * NT + k] = d92[k];
-    pre[14] = t99;
+    for (int k = 0; k < NT; ++k) dpre[13 * NT + k] = d123[k];
+    pre[14] = t34;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[14 * NT + k] = d99[k];
-    pre[15] = t101;
+    for (int k = 0; k < NT; ++k) dpre[14 * NT + k] = d34[k];
+    pre[15] = t35;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[15 * NT + k] = d101[k];
-    pre[16] = t104;
+    for (int k = 0; k < NT; ++k) dpre[15 * NT + k] = d35[k];
+    pre[16] = t36;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[16 * NT + k] = 0.0;
-    pre[17] = t112;
+    for (int k = 0; k < NT; ++k) dpre[16 * NT + k] = d36[k];
+    pre[17] = t158;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[17 * NT + k] = d112[k];
-    pre[18] = t114;
+    for (int k = 0; k < NT; ++k) dpre[17 * NT + k] = 0.0;
+    pre[18] = t159;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[18 * NT + k] = 0.0;
-    pre[19] = t34;
+    pre[19] = t183;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[19 * NT + k] = d34[k];
-    pre[20] = t35;
+    for (int k = 0; k < NT; ++k) dpre[19 * NT + k] = d183[k];
+    pre[20] = t185;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[20 * NT + k] = d35[k];
-    pre[21] = t36;
+    for (int k = 0; k < NT; ++k) dpre[20 * NT + k] = d185[k];
+    pre[21] = t187;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[21 * NT + k] = d36[k];
-    pre[22] = t159;
+    for (int k = 0; k < NT; ++k) dpre[21 * NT + k] = d187[k];
+    pre[22] = t256;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dpre[22 * NT + k] = 0.0;
-    pre[23] = t185;
+    pre[23] = t260;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[23 * NT + k] = d185[k];
-    pre[24] = t190;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[24 * NT + k] = d190[k];
-    pre[25] = t195;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[25 * NT + k] = d195[k];
-    pre[26] = t252;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[26 * NT + k] = 0.0;
-    pre[27] = t255;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[27 * NT + k] = 0.0;
-    pre[28] = t258;
-#pragma unroll
-    for (int k = 0; k < NT; ++k) dpre[28 * NT + k] = 0.0;
+    for (int k = 0; k < NT; ++k) dpre[23 * NT + k] = 0.0;
 }
 
 // adj_gr: one iteration, outputs and their tangents (din[i * NT + k] for the
@@ -3781,234 +3592,180 @@ __host__ __device__ __forceinline__ void adj_gr_iter_jvp(const double* __restric
     const double t45 = t43 + t44;
     const double t46 = in_hv2 * in_hv2;
     const double t47 = t45 + t46;
-    const double t115 = t42 * t42;
-    const double t116 = t47 * pre[4];
-    const double t117 = t116 - pre[5];
-    const double t118 = pre[6] * t115;
-    const double t119 = t117 - t118;
-    const double t120 = pre[7] * t119;
-    const double t121 = t42 * pre[8];
-    const double t122 = t47 * t47;
-    const double t123 = t115 * t115;
-    const double t124 = pre[9] * t122;
-    const double t125 = pre[10] + t124;
-    const double t126 = pre[11] * t123;
-    const double t127 = t125 + t126;
-    const double t128 = pre[12] * t115;
+    const double t124 = t42 * t42;
+    const double t125 = t47 * pre[4];
+    const double t126 = pre[5] + t125;
+    const double t127 = pre[6] * t124;
+    const double t128 = t126 - t127;
     const double t129 = t47 * t128;
-    const double t130 = t127 - t129;
-    const double t131 = t47 * pre[13];
-    const double t132 = t130 - t131;
-    const double t133 = pre[14] * t115;
-    const double t134 = t132 - t133;
-    const double t135 = pre[7] * t134;
-    const double t136 = t42 * pre[15];
-    const double t137 = t47 * pre[16];
-    const double t138 = t137 - pre[17];
-    const double t139 = pre[18] * t115;
-    const double t140 = t138 - t139;
-    const double t141 = t136 * t140;
-    const double t142 = t120 + t135;
-    const double t143 = t121 + t141;
-    const double t144 = pre[19] * t142;
-    const double t145 = in_hv0 * t143;
+    const double t130 = pre[7] + t129;
+    const double t131 = pre[8] * t124;
+    const double t132 = pre[9] + t131;
+    const double t133 = t124 * t132;
+    const double t134 = t130 + t133;
+    const double t135 = pre[10] * t134;
+    const double t136 = t47 * pre[11];
+    const double t137 = pre[12] + t136;
+    const double t138 = pre[13] * t124;
+    const double t139 = t137 + t138;
+    const double t140 = t42 * t139;
+    const double t141 = pre[14] * t135;
+    const double t142 = in_hv0 * t140;
+    const double t143 = t141 + t142;
+    const double t144 = pre[15] * t135;
+    const double t145 = in_hv1 * t140;
     const double t146 = t144 + t145;
-    const double t147 = pre[20] * t142;
-    const double t148 = in_hv1 * t143;
+    const double t147 = pre[16] * t135;
+    const double t148 = in_hv2 * t140;
     const double t149 = t147 + t148;
-    const double t150 = pre[21] * t142;
-    const double t151 = in_hv2 * t143;
-    const double t152 = t150 + t151;
-    const double t153 = in_H0 * c_hmoi;
-    const double t154 = in_H1 * c_hmoi;
-    const double t155 = in_H2 * c_hmoi;
-    const double t156 = in_S0 * c_moi;
-    const double t157 = in_S1 * c_moi;
-    const double t158 = in_S2 * c_moi;
-    const double t160 = t156 / c_m;
-    const double t161 = t153 / c_hm;
+    const double t150 = in_H0 * c_hmoi;
+    const double t151 = in_H1 * c_hmoi;
+    const double t152 = in_H2 * c_hmoi;
+    const double t153 = in_S0 * c_moi;
+    const double t154 = in_S1 * c_moi;
+    const double t155 = in_S2 * c_moi;
+    const double t160 = in_S0 * pre[17];
+    const double t161 = t150 * pre[18];
     const double t162 = t160 - t161;
-    const double t163 = pre[22] * t162;
-    const double t164 = t157 / c_m;
-    const double t165 = t154 / c_hm;
-    const double t166 = t164 - t165;
-    const double t167 = pre[22] * t166;
-    const double t168 = t158 / c_m;
-    const double t169 = t155 / c_hm;
-    const double t170 = t168 - t169;
-    const double t171 = pre[22] * t170;
-    const double t172 = t153 + t156;
-    const double t173 = t154 + t157;
-    const double t174 = t155 + t158;
-    const double t175 = in_hv2 * pre[20];
-    const double t176 = in_hv1 * pre[21];
+    const double t163 = in_S1 * pre[17];
+    const double t164 = t151 * pre[18];
+    const double t165 = t163 - t164;
+    const double t166 = in_S2 * pre[17];
+    const double t167 = t152 * pre[18];
+    const double t168 = t166 - t167;
+    const double t169 = t150 + t153;
+    const double t170 = t151 + t154;
+    const double t171 = t152 + t155;
+    const double t172 = pre[1] * in_hv2;
+    const double t173 = pre[2] * in_hv1;
+    const double t174 = t172 - t173;
+    const double t175 = pre[2] * in_hv0;
+    const double t176 = pre[0] * in_hv2;
     const double t177 = t175 - t176;
-    const double t178 = in_hv0 * pre[21];
-    const double t179 = in_hv2 * pre[19];
+    const double t178 = pre[0] * in_hv1;
+    const double t179 = pre[1] * in_hv0;
     const double t180 = t178 - t179;
-    const double t181 = in_hv1 * pre[19];
-    const double t182 = in_hv0 * pre[20];
-    const double t183 = t181 - t182;
-    const double t186 = 2.0 * t172;
-    const double t187 = t163 + t186;
-    const double t188 = t177 * t187;
-    const double t189 = pre[23] * t188;
-    const double t191 = 2.0 * t173;
-    const double t192 = t167 + t191;
-    const double t193 = t180 * t192;
-    const double t194 = pre[24] * t193;
-    const double t196 = 2.0 * t174;
-    const double t197 = t171 + t196;
-    const double t198 = t183 * t197;
-    const double t199 = pre[25] * t198;
-    const double t201 = t172 * 7.0;
-    const double t202 = 3.0 * t163;
-    const double t203 = t201 + t202;
-    const double t204 = t173 * 7.0;
-    const double t205 = 3.0 * t167;
-    const double t206 = t204 + t205;
-    const double t207 = t174 * 7.0;
-    const double t208 = 3.0 * t171;
-    const double t209 = t207 + t208;
-    const double t210 = 3.0 * t172;
-    const double t211 = t163 + t210;
-    const double t212 = 3.0 * t173;
-    const double t213 = t167 + t212;
-    const double t214 = 3.0 * t174;
-    const double t215 = t171 + t214;
-    const double t216 = t42 * 3.0;
-    const double t217 = in_hv1 * t209;
-    const double t218 = in_hv2 * t206;
+    const double t188 = 2.0 * t169;
+    const double t189 = t162 + t188;
+    const double t190 = t174 * t189;
+    const double t191 = pre[19] * t190;
+    const double t192 = 2.0 * t170;
+    const double t193 = t165 + t192;
+    const double t194 = t177 * t193;
+    const double t195 = pre[20] * t194;
+    const double t196 = 2.0 * t171;
+    const double t197 = t168 + t196;
+    const double t198 = t180 * t197;
+    const double t199 = pre[21] * t198;
+    const double t200 = pre[14] * t42;
+    const double t201 = t200 - in_hv0;
+    const double t202 = pre[15] * t42;
+    const double t203 = t202 - in_hv1;
+    const double t204 = pre[16] * t42;
+    const double t205 = t204 - in_hv2;
+    const double t206 = t42 * 2.0;
+    const double t208 = t201 * 7.0;
+    const double t209 = pre[14] * t206;
+    const double t210 = t208 + t209;
+    const double t211 = t203 * 7.0;
+    const double t212 = pre[15] * t206;
+    const double t213 = t211 + t212;
+    const double t214 = t205 * 7.0;
+    const double t215 = pre[16] * t206;
+    const double t216 = t214 + t215;
+    const double t217 = t171 * t213;
+    const double t218 = t170 * t216;
     const double t219 = t217 - t218;
-    const double t220 = in_hv2 * t203;
-    const double t221 = in_hv0 * t209;
+    const double t220 = t169 * t216;
+    const double t221 = t171 * t210;
     const double t222 = t220 - t221;
-    const double t223 = in_hv0 * t206;
-    const double t224 = in_hv1 * t203;
+    const double t223 = t170 * t210;
+    const double t224 = t169 * t213;
     const double t225 = t223 - t224;
-    const double t226 = pre[20] * t215;
-    const double t227 = pre[21] * t213;
+    const double t226 = t168 * t203;
+    const double t227 = t165 * t205;
     const double t228 = t226 - t227;
-    const double t229 = pre[21] * t211;
-    const double t230 = pre[19] * t215;
+    const double t229 = t162 * t205;
+    const double t230 = t168 * t201;
     const double t231 = t229 - t230;
-    const double t232 = pre[19] * t213;
-    const double t233 = pre[20] * t211;
+    const double t232 = t165 * t201;
+    const double t233 = t162 * t203;
     const double t234 = t232 - t233;
-    const double t235 = t189 - t219;
-    const double t236 = t216 * t228;
+    const double t235 = t191 + t219;
+    const double t236 = 3.0 * t228;
     const double t237 = t235 + t236;
     const double t238 = kFA * t237;
-    const double t239 = t146 + t238;
-    const double t240 = t194 - t222;
-    const double t241 = t216 * t231;
+    const double t239 = t143 + t238;
+    const double t240 = t195 + t222;
+    const double t241 = 3.0 * t231;
     const double t242 = t240 + t241;
     const double t243 = kFA * t242;
-    const double t244 = t149 + t243;
-    const double t245 = t199 - t225;
-    const double t246 = t216 * t234;
+    const double t244 = t146 + t243;
+    const double t245 = t199 + t225;
+    const double t246 = 3.0 * t234;
     const double t247 = t245 + t246;
     const double t248 = kFA * t247;
-    const double t249 = t152 + t248;
-    const double t259 = pre[1] * in_hv2;
-    const double t260 = pre[2] * in_hv1;
-    const double t261 = t259 - t260;
-    const double t262 = pre[2] * in_hv0;
-    const double t263 = pre[0] * in_hv2;
-    const double t264 = t262 - t263;
-    const double t265 = pre[0] * in_hv1;
-    const double t266 = pre[1] * in_hv0;
-    const double t267 = t265 - t266;
-    const double t268 = pre[26] * t261;
-    const double t269 = pre[26] * t264;
-    const double t270 = pre[26] * t267;
-    const double t271 = t155 * t157;
-    const double t272 = t154 * t158;
-    const double t273 = t271 - t272;
-    const double t274 = t153 * t158;
-    const double t275 = t155 * t156;
-    const double t276 = t274 - t275;
-    const double t277 = t154 * t156;
-    const double t278 = t153 * t157;
-    const double t279 = t277 - t278;
-    const double t280 = pre[19] * t156;
-    const double t281 = pre[20] * t157;
-    const double t282 = t280 + t281;
-    const double t283 = pre[21] * t158;
+    const double t249 = t149 + t248;
+    const double t261 = pre[14] * t153;
+    const double t262 = pre[15] * t154;
+    const double t263 = t261 + t262;
+    const double t264 = pre[16] * t155;
+    const double t265 = t263 + t264;
+    const double t266 = 3.0 * t265;
+    const double t267 = pre[14] * t150;
+    const double t268 = pre[15] * t151;
+    const double t269 = t267 + t268;
+    const double t270 = pre[16] * t152;
+    const double t271 = t269 + t270;
+    const double t272 = 3.0 * t271;
+    const double t273 = t174 * pre[22];
+    const double t274 = t273 - t153;
+    const double t275 = pre[14] * t266;
+    const double t276 = t274 + t275;
+    const double t277 = t177 * pre[22];
+    const double t278 = t277 - t154;
+    const double t279 = pre[15] * t266;
+    const double t280 = t278 + t279;
+    const double t281 = t180 * pre[22];
+    const double t282 = t281 - t155;
+    const double t283 = pre[16] * t266;
     const double t284 = t282 + t283;
-    const double t285 = 3.0 * t284;
-    const double t286 = pre[19] * t153;
-    const double t287 = pre[20] * t154;
+    const double t285 = t174 * pre[23];
+    const double t286 = t285 - t150;
+    const double t287 = pre[14] * t272;
     const double t288 = t286 + t287;
-    const double t289 = pre[21] * t155;
-    const double t290 = t288 + t289;
-    const double t291 = 3.0 * t290;
-    const double t292 = t155 * t269;
-    const double t293 = t154 * t270;
-    const double t294 = t292 - t293;
-    const double t295 = t153 * t270;
-    const double t296 = t155 * t268;
-    const double t297 = t295 - t296;
-    const double t298 = t154 * t268;
-    const double t299 = t153 * t269;
-    const double t300 = t298 - t299;
-    const double t301 = t158 * t269;
-    const double t302 = t157 * t270;
-    const double t303 = t301 - t302;
-    const double t304 = t156 * t270;
-    const double t305 = t158 * t268;
-    const double t306 = t304 - t305;
-    const double t307 = t157 * t268;
-    const double t308 = t156 * t269;
-    const double t309 = t307 - t308;
-    const double t310 = pre[20] * t155;
-    const double t311 = pre[21] * t154;
-    const double t312 = t310 - t311;
-    const double t313 = pre[21] * t153;
-    const double t314 = pre[19] * t155;
-    const double t315 = t313 - t314;
-    const double t316 = pre[19] * t154;
-    const double t317 = pre[20] * t153;
-    const double t318 = t316 - t317;
-    const double t319 = pre[20] * t158;
-    const double t320 = pre[21] * t157;
-    const double t321 = t319 - t320;
-    const double t322 = pre[21] * t156;
-    const double t323 = pre[19] * t158;
-    const double t324 = t322 - t323;
-    const double t325 = pre[19] * t157;
-    const double t326 = pre[20] * t156;
-    const double t327 = t325 - t326;
-    const double t328 = pre[27] * t294;
-    const double t329 = t328 - t273;
-    const double t330 = t285 * t312;
-    const double t331 = t329 + t330;
-    const double t332 = kFA * t331;
-    const double t333 = pre[27] * t297;
-    const double t334 = t333 - t276;
-    const double t335 = t285 * t315;
-    const double t336 = t334 + t335;
-    const double t337 = kFA * t336;
-    const double t338 = pre[27] * t300;
-    const double t339 = t338 - t279;
-    const double t340 = t285 * t318;
-    const double t341 = t339 + t340;
-    const double t342 = kFA * t341;
-    const double t343 = pre[28] * t303;
-    const double t344 = t273 + t343;
-    const double t345 = t291 * t321;
-    const double t346 = t344 + t345;
-    const double t347 = kFA * t346;
-    const double t348 = pre[28] * t306;
-    const double t349 = t276 + t348;
-    const double t350 = t291 * t324;
-    const double t351 = t349 + t350;
-    const double t352 = kFA * t351;
-    const double t353 = pre[28] * t309;
-    const double t354 = t279 + t353;
-    const double t355 = t291 * t327;
-    const double t356 = t354 + t355;
-    const double t357 = kFA * t356;
+    const double t289 = t177 * pre[23];
+    const double t290 = t289 - t151;
+    const double t291 = pre[15] * t272;
+    const double t292 = t290 + t291;
+    const double t293 = t180 * pre[23];
+    const double t294 = t293 - t152;
+    const double t295 = pre[16] * t272;
+    const double t296 = t294 + t295;
+    const double t297 = t152 * t280;
+    const double t298 = t151 * t284;
+    const double t299 = t297 - t298;
+    const double t300 = t150 * t284;
+    const double t301 = t152 * t276;
+    const double t302 = t300 - t301;
+    const double t303 = t151 * t276;
+    const double t304 = t150 * t280;
+    const double t305 = t303 - t304;
+    const double t306 = t155 * t292;
+    const double t307 = t154 * t296;
+    const double t308 = t306 - t307;
+    const double t309 = t153 * t296;
+    const double t310 = t155 * t288;
+    const double t311 = t309 - t310;
+    const double t312 = t154 * t288;
+    const double t313 = t153 * t292;
+    const double t314 = t312 - t313;
+    const double t315 = kFA * t299;
+    const double t316 = kFA * t302;
+    const double t317 = kFA * t305;
+    const double t318 = kFA * t308;
+    const double t319 = kFA * t311;
+    const double t320 = kFA * t314;
     double d37[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d37[k] = dpre[0 * NT + k] * in_hv0 + pre[0] * din[0 * NT + k];
@@ -4042,354 +3799,309 @@ __host__ __device__ __forceinline__ void adj_gr_iter_jvp(const double* __restric
     double d47[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d47[k] = d45[k] + d46[k];
-    double d115[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d115[k] = 2.0 * t42 * d42[k];
-    double d116[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d116[k] = d47[k] * pre[4];
-    double d117[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d117[k] = d116[k] - dpre[5 * NT + k];
-    double d118[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d118[k] = pre[6] * d115[k];
-    double d119[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d119[k] = d117[k] - d118[k];
-    double d120[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d120[k] = dpre[7 * NT + k] * t119 + pre[7] * d119[k];
-    double d121[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d121[k] = d42[k] * pre[8] + t42 * dpre[8 * NT + k];
-    double d122[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d122[k] = 2.0 * t47 * d47[k];
-    double d123[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d123[k] = 2.0 * t115 * d115[k];
     double d124[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d124[k] = pre[9] * d122[k];
+    for (int k = 0; k < NT; ++k) d124[k] = 2.0 * t42 * d42[k];
     double d125[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d125[k] = dpre[10 * NT + k] + d124[k];
+    for (int k = 0; k < NT; ++k) d125[k] = d47[k] * pre[4];
     double d126[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d126[k] = pre[11] * d123[k];
+    for (int k = 0; k < NT; ++k) d126[k] = dpre[5 * NT + k] + d125[k];
     double d127[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d127[k] = d125[k] + d126[k];
+    for (int k = 0; k < NT; ++k) d127[k] = pre[6] * d124[k];
     double d128[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d128[k] = pre[12] * d115[k];
+    for (int k = 0; k < NT; ++k) d128[k] = d126[k] - d127[k];
     double d129[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d129[k] = d47[k] * t128 + t47 * d128[k];
     double d130[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d130[k] = d127[k] - d129[k];
+    for (int k = 0; k < NT; ++k) d130[k] = dpre[7 * NT + k] + d129[k];
     double d131[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d131[k] = d47[k] * pre[13] + t47 * dpre[13 * NT + k];
+    for (int k = 0; k < NT; ++k) d131[k] = pre[8] * d124[k];
     double d132[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d132[k] = d130[k] - d131[k];
+    for (int k = 0; k < NT; ++k) d132[k] = dpre[9 * NT + k] + d131[k];
     double d133[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d133[k] = dpre[14 * NT + k] * t115 + pre[14] * d115[k];
+    for (int k = 0; k < NT; ++k) d133[k] = d124[k] * t132 + t124 * d132[k];
     double d134[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d134[k] = d132[k] - d133[k];
+    for (int k = 0; k < NT; ++k) d134[k] = d130[k] + d133[k];
     double d135[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d135[k] = dpre[7 * NT + k] * t134 + pre[7] * d134[k];
+    for (int k = 0; k < NT; ++k) d135[k] = dpre[10 * NT + k] * t134 + pre[10] * d134[k];
     double d136[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d136[k] = d42[k] * pre[15] + t42 * dpre[15 * NT + k];
+    for (int k = 0; k < NT; ++k) d136[k] = d47[k] * pre[11] + t47 * dpre[11 * NT + k];
     double d137[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d137[k] = d47[k] * pre[16];
+    for (int k = 0; k < NT; ++k) d137[k] = dpre[12 * NT + k] + d136[k];
     double d138[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d138[k] = d137[k] - dpre[17 * NT + k];
+    for (int k = 0; k < NT; ++k) d138[k] = dpre[13 * NT + k] * t124 + pre[13] * d124[k];
     double d139[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d139[k] = pre[18] * d115[k];
+    for (int k = 0; k < NT; ++k) d139[k] = d137[k] + d138[k];
     double d140[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d140[k] = d138[k] - d139[k];
+    for (int k = 0; k < NT; ++k) d140[k] = d42[k] * t139 + t42 * d139[k];
     double d141[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d141[k] = d136[k] * t140 + t136 * d140[k];
+    for (int k = 0; k < NT; ++k) d141[k] = dpre[14 * NT + k] * t135 + pre[14] * d135[k];
     double d142[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d142[k] = d120[k] + d135[k];
+    for (int k = 0; k < NT; ++k) d142[k] = din[0 * NT + k] * t140 + in_hv0 * d140[k];
     double d143[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d143[k] = d121[k] + d141[k];
+    for (int k = 0; k < NT; ++k) d143[k] = d141[k] + d142[k];
     double d144[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d144[k] = dpre[19 * NT + k] * t142 + pre[19] * d142[k];
+    for (int k = 0; k < NT; ++k) d144[k] = dpre[15 * NT + k] * t135 + pre[15] * d135[k];
     double d145[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d145[k] = din[0 * NT + k] * t143 + in_hv0 * d143[k];
+    for (int k = 0; k < NT; ++k) d145[k] = din[1 * NT + k] * t140 + in_hv1 * d140[k];
     double d146[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d146[k] = d144[k] + d145[k];
     double d147[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d147[k] = dpre[20 * NT + k] * t142 + pre[20] * d142[k];
+    for (int k = 0; k < NT; ++k) d147[k] = dpre[16 * NT + k] * t135 + pre[16] * d135[k];
     double d148[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d148[k] = din[1 * NT + k] * t143 + in_hv1 * d143[k];
+    for (int k = 0; k < NT; ++k) d148[k] = din[2 * NT + k] * t140 + in_hv2 * d140[k];
     double d149[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d149[k] = d147[k] + d148[k];
     double d150[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d150[k] = dpre[21 * NT + k] * t142 + pre[21] * d142[k];
+    for (int k = 0; k < NT; ++k) d150[k] = din[6 * NT + k] * c_hmoi;
     double d151[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d151[k] = din[2 * NT + k] * t143 + in_hv2 * d143[k];
+    for (int k = 0; k < NT; ++k) d151[k] = din[7 * NT + k] * c_hmoi;
     double d152[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d152[k] = d150[k] + d151[k];
+    for (int k = 0; k < NT; ++k) d152[k] = din[8 * NT + k] * c_hmoi;
     double d153[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d153[k] = din[6 * NT + k] * c_hmoi;
+    for (int k = 0; k < NT; ++k) d153[k] = din[3 * NT + k] * c_moi;
     double d154[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d154[k] = din[7 * NT + k] * c_hmoi;
+    for (int k = 0; k < NT; ++k) d154[k] = din[4 * NT + k] * c_moi;
     double d155[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d155[k] = din[8 * NT + k] * c_hmoi;
-    double d156[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d156[k] = din[3 * NT + k] * c_moi;
-    double d157[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d157[k] = din[4 * NT + k] * c_moi;
-    double d158[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d158[k] = din[5 * NT + k] * c_moi;
+    for (int k = 0; k < NT; ++k) d155[k] = din[5 * NT + k] * c_moi;
     double d160[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d160[k] = d156[k] / c_m;
+    for (int k = 0; k < NT; ++k) d160[k] = din[3 * NT + k] * pre[17];
     double d161[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d161[k] = d153[k] / c_hm;
+    for (int k = 0; k < NT; ++k) d161[k] = d150[k] * pre[18];
     double d162[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d162[k] = d160[k] - d161[k];
     double d163[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d163[k] = pre[22] * d162[k];
+    for (int k = 0; k < NT; ++k) d163[k] = din[4 * NT + k] * pre[17];
     double d164[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d164[k] = d157[k] / c_m;
+    for (int k = 0; k < NT; ++k) d164[k] = d151[k] * pre[18];
     double d165[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d165[k] = d154[k] / c_hm;
+    for (int k = 0; k < NT; ++k) d165[k] = d163[k] - d164[k];
     double d166[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d166[k] = d164[k] - d165[k];
+    for (int k = 0; k < NT; ++k) d166[k] = din[5 * NT + k] * pre[17];
     double d167[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d167[k] = pre[22] * d166[k];
+    for (int k = 0; k < NT; ++k) d167[k] = d152[k] * pre[18];
     double d168[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d168[k] = d158[k] / c_m;
+    for (int k = 0; k < NT; ++k) d168[k] = d166[k] - d167[k];
     double d169[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d169[k] = d155[k] / c_hm;
+    for (int k = 0; k < NT; ++k) d169[k] = d150[k] + d153[k];
     double d170[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d170[k] = d168[k] - d169[k];
+    for (int k = 0; k < NT; ++k) d170[k] = d151[k] + d154[k];
     double d171[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d171[k] = pre[22] * d170[k];
+    for (int k = 0; k < NT; ++k) d171[k] = d152[k] + d155[k];
     double d172[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d172[k] = d153[k] + d156[k];
+    for (int k = 0; k < NT; ++k) d172[k] = dpre[1 * NT + k] * in_hv2 + pre[1] * din[2 * NT + k];
     double d173[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d173[k] = d154[k] + d157[k];
+    for (int k = 0; k < NT; ++k) d173[k] = dpre[2 * NT + k] * in_hv1 + pre[2] * din[1 * NT + k];
     double d174[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d174[k] = d155[k] + d158[k];
+    for (int k = 0; k < NT; ++k) d174[k] = d172[k] - d173[k];
     double d175[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d175[k] = din[2 * NT + k] * pre[20] + in_hv2 * dpre[20 * NT + k];
+    for (int k = 0; k < NT; ++k) d175[k] = dpre[2 * NT + k] * in_hv0 + pre[2] * din[0 * NT + k];
     double d176[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d176[k] = din[1 * NT + k] * pre[21] + in_hv1 * dpre[21 * NT + k];
+    for (int k = 0; k < NT; ++k) d176[k] = dpre[0 * NT + k] * in_hv2 + pre[0] * din[2 * NT + k];
     double d177[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d177[k] = d175[k] - d176[k];
     double d178[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d178[k] = din[0 * NT + k] * pre[21] + in_hv0 * dpre[21 * NT + k];
+    for (int k = 0; k < NT; ++k) d178[k] = dpre[0 * NT + k] * in_hv1 + pre[0] * din[1 * NT + k];
     double d179[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d179[k] = din[2 * NT + k] * pre[19] + in_hv2 * dpre[19 * NT + k];
+    for (int k = 0; k < NT; ++k) d179[k] = dpre[1 * NT + k] * in_hv0 + pre[1] * din[0 * NT + k];
     double d180[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d180[k] = d178[k] - d179[k];
-    double d181[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d181[k] = din[1 * NT + k] * pre[19] + in_hv1 * dpre[19 * NT + k];
-    double d182[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d182[k] = din[0 * NT + k] * pre[20] + in_hv0 * dpre[20 * NT + k];
-    double d183[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d183[k] = d181[k] - d182[k];
-    double d186[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d186[k] = 2.0 * d172[k];
-    double d187[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d187[k] = d163[k] + d186[k];
     double d188[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d188[k] = d177[k] * t187 + t177 * d187[k];
+    for (int k = 0; k < NT; ++k) d188[k] = 2.0 * d169[k];
     double d189[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d189[k] = dpre[23 * NT + k] * t188 + pre[23] * d188[k];
+    for (int k = 0; k < NT; ++k) d189[k] = d162[k] + d188[k];
+    double d190[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d190[k] = d174[k] * t189 + t174 * d189[k];
     double d191[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d191[k] = 2.0 * d173[k];
+    for (int k = 0; k < NT; ++k) d191[k] = dpre[19 * NT + k] * t190 + pre[19] * d190[k];
     double d192[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d192[k] = d167[k] + d191[k];
+    for (int k = 0; k < NT; ++k) d192[k] = 2.0 * d170[k];
     double d193[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d193[k] = d180[k] * t192 + t180 * d192[k];
+    for (int k = 0; k < NT; ++k) d193[k] = d165[k] + d192[k];
     double d194[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d194[k] = dpre[24 * NT + k] * t193 + pre[24] * d193[k];
+    for (int k = 0; k < NT; ++k) d194[k] = d177[k] * t193 + t177 * d193[k];
+    double d195[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d195[k] = dpre[20 * NT + k] * t194 + pre[20] * d194[k];
     double d196[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d196[k] = 2.0 * d174[k];
+    for (int k = 0; k < NT; ++k) d196[k] = 2.0 * d171[k];
     double d197[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d197[k] = d171[k] + d196[k];
+    for (int k = 0; k < NT; ++k) d197[k] = d168[k] + d196[k];
     double d198[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d198[k] = d183[k] * t197 + t183 * d197[k];
+    for (int k = 0; k < NT; ++k) d198[k] = d180[k] * t197 + t180 * d197[k];
     double d199[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d199[k] = dpre[25 * NT + k] * t198 + pre[25] * d198[k];
+    for (int k = 0; k < NT; ++k) d199[k] = dpre[21 * NT + k] * t198 + pre[21] * d198[k];
+    double d200[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) d200[k] = dpre[14 * NT + k] * t42 + pre[14] * d42[k];
     double d201[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d201[k] = d172[k] * 7.0;
+    for (int k = 0; k < NT; ++k) d201[k] = d200[k] - din[0 * NT + k];
     double d202[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d202[k] = 3.0 * d163[k];
+    for (int k = 0; k < NT; ++k) d202[k] = dpre[15 * NT + k] * t42 + pre[15] * d42[k];
     double d203[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d203[k] = d201[k] + d202[k];
+    for (int k = 0; k < NT; ++k) d203[k] = d202[k] - din[1 * NT + k];
     double d204[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d204[k] = d173[k] * 7.0;
+    for (int k = 0; k < NT; ++k) d204[k] = dpre[16 * NT + k] * t42 + pre[16] * d42[k];
     double d205[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d205[k] = 3.0 * d167[k];
+    for (int k = 0; k < NT; ++k) d205[k] = d204[k] - din[2 * NT + k];
     double d206[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d206[k] = d204[k] + d205[k];
-    double d207[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d207[k] = d174[k] * 7.0;
+    for (int k = 0; k < NT; ++k) d206[k] = d42[k] * 2.0;
     double d208[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d208[k] = 3.0 * d171[k];
+    for (int k = 0; k < NT; ++k) d208[k] = d201[k] * 7.0;
     double d209[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d209[k] = d207[k] + d208[k];
+    for (int k = 0; k < NT; ++k) d209[k] = dpre[14 * NT + k] * t206 + pre[14] * d206[k];
     double d210[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d210[k] = 3.0 * d172[k];
+    for (int k = 0; k < NT; ++k) d210[k] = d208[k] + d209[k];
     double d211[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d211[k] = d163[k] + d210[k];
+    for (int k = 0; k < NT; ++k) d211[k] = d203[k] * 7.0;
     double d212[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d212[k] = 3.0 * d173[k];
+    for (int k = 0; k < NT; ++k) d212[k] = dpre[15 * NT + k] * t206 + pre[15] * d206[k];
     double d213[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d213[k] = d167[k] + d212[k];
+    for (int k = 0; k < NT; ++k) d213[k] = d211[k] + d212[k];
     double d214[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d214[k] = 3.0 * d174[k];
+    for (int k = 0; k < NT; ++k) d214[k] = d205[k] * 7.0;
     double d215[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d215[k] = d171[k] + d214[k];
+    for (int k = 0; k < NT; ++k) d215[k] = dpre[16 * NT + k] * t206 + pre[16] * d206[k];
     double d216[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d216[k] = d42[k] * 3.0;
+    for (int k = 0; k < NT; ++k) d216[k] = d214[k] + d215[k];
     double d217[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d217[k] = din[1 * NT + k] * t209 + in_hv1 * d209[k];
+    for (int k = 0; k < NT; ++k) d217[k] = d171[k] * t213 + t171 * d213[k];
     double d218[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d218[k] = din[2 * NT + k] * t206 + in_hv2 * d206[k];
+    for (int k = 0; k < NT; ++k) d218[k] = d170[k] * t216 + t170 * d216[k];
     double d219[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d219[k] = d217[k] - d218[k];
     double d220[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d220[k] = din[2 * NT + k] * t203 + in_hv2 * d203[k];
+    for (int k = 0; k < NT; ++k) d220[k] = d169[k] * t216 + t169 * d216[k];
     double d221[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d221[k] = din[0 * NT + k] * t209 + in_hv0 * d209[k];
+    for (int k = 0; k < NT; ++k) d221[k] = d171[k] * t210 + t171 * d210[k];
     double d222[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d222[k] = d220[k] - d221[k];
     double d223[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d223[k] = din[0 * NT + k] * t206 + in_hv0 * d206[k];
+    for (int k = 0; k < NT; ++k) d223[k] = d170[k] * t210 + t170 * d210[k];
     double d224[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d224[k] = din[1 * NT + k] * t203 + in_hv1 * d203[k];
+    for (int k = 0; k < NT; ++k) d224[k] = d169[k] * t213 + t169 * d213[k];
     double d225[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d225[k] = d223[k] - d224[k];
     double d226[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d226[k] = dpre[20 * NT + k] * t215 + pre[20] * d215[k];
+    for (int k = 0; k < NT; ++k) d226[k] = d168[k] * t203 + t168 * d203[k];
     double d227[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d227[k] = dpre[21 * NT + k] * t213 + pre[21] * d213[k];
+    for (int k = 0; k < NT; ++k) d227[k] = d165[k] * t205 + t165 * d205[k];
     double d228[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d228[k] = d226[k] - d227[k];
     double d229[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d229[k] = dpre[21 * NT + k] * t211 + pre[21] * d211[k];
+    for (int k = 0; k < NT; ++k) d229[k] = d162[k] * t205 + t162 * d205[k];
     double d230[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d230[k] = dpre[19 * NT + k] * t215 + pre[19] * d215[k];
+    for (int k = 0; k < NT; ++k) d230[k] = d168[k] * t201 + t168 * d201[k];
     double d231[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d231[k] = d229[k] - d230[k];
     double d232[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d232[k] = dpre[19 * NT + k] * t213 + pre[19] * d213[k];
+    for (int k = 0; k < NT; ++k) d232[k] = d165[k] * t201 + t165 * d201[k];
     double d233[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d233[k] = dpre[20 * NT + k] * t211 + pre[20] * d211[k];
+    for (int k = 0; k < NT; ++k) d233[k] = d162[k] * t203 + t162 * d203[k];
     double d234[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d234[k] = d232[k] - d233[k];
     double d235[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d235[k] = d189[k] - d219[k];
+    for (int k = 0; k < NT; ++k) d235[k] = d191[k] + d219[k];
     double d236[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d236[k] = d216[k] * t228 + t216 * d228[k];
+    for (int k = 0; k < NT; ++k) d236[k] = 3.0 * d228[k];
     double d237[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d237[k] = d235[k] + d236[k];
@@ -4398,13 +4110,13 @@ __host__ __device__ __forceinline__ void adj_gr_iter_jvp(const double* __restric
     for (int k = 0; k < NT; ++k) d238[k] = kFA * d237[k];
     double d239[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d239[k] = d146[k] + d238[k];
+    for (int k = 0; k < NT; ++k) d239[k] = d143[k] + d238[k];
     double d240[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d240[k] = d194[k] - d222[k];
+    for (int k = 0; k < NT; ++k) d240[k] = d195[k] + d222[k];
     double d241[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d241[k] = d216[k] * t231 + t216 * d231[k];
+    for (int k = 0; k < NT; ++k) d241[k] = 3.0 * d231[k];
     double d242[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d242[k] = d240[k] + d241[k];
@@ -4413,13 +4125,13 @@ __host__ __device__ __forceinline__ void adj_gr_iter_jvp(const double* __restric
     for (int k = 0; k < NT; ++k) d243[k] = kFA * d242[k];
     double d244[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d244[k] = d149[k] + d243[k];
+    for (int k = 0; k < NT; ++k) d244[k] = d146[k] + d243[k];
     double d245[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d245[k] = d199[k] - d225[k];
+    for (int k = 0; k < NT; ++k) d245[k] = d199[k] + d225[k];
     double d246[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d246[k] = d216[k] * t234 + t216 * d234[k];
+    for (int k = 0; k < NT; ++k) d246[k] = 3.0 * d234[k];
     double d247[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d247[k] = d245[k] + d246[k];
@@ -4428,304 +4140,187 @@ __host__ __device__ __forceinline__ void adj_gr_iter_jvp(const double* __restric
     for (int k = 0; k < NT; ++k) d248[k] = kFA * d247[k];
     double d249[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d249[k] = d152[k] + d248[k];
-    double d259[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d259[k] = dpre[1 * NT + k] * in_hv2 + pre[1] * din[2 * NT + k];
-    double d260[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d260[k] = dpre[2 * NT + k] * in_hv1 + pre[2] * din[1 * NT + k];
+    for (int k = 0; k < NT; ++k) d249[k] = d149[k] + d248[k];
     double d261[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d261[k] = d259[k] - d260[k];
+    for (int k = 0; k < NT; ++k) d261[k] = dpre[14 * NT + k] * t153 + pre[14] * d153[k];
     double d262[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d262[k] = dpre[2 * NT + k] * in_hv0 + pre[2] * din[0 * NT + k];
+    for (int k = 0; k < NT; ++k) d262[k] = dpre[15 * NT + k] * t154 + pre[15] * d154[k];
     double d263[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d263[k] = dpre[0 * NT + k] * in_hv2 + pre[0] * din[2 * NT + k];
+    for (int k = 0; k < NT; ++k) d263[k] = d261[k] + d262[k];
     double d264[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d264[k] = d262[k] - d263[k];
+    for (int k = 0; k < NT; ++k) d264[k] = dpre[16 * NT + k] * t155 + pre[16] * d155[k];
     double d265[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d265[k] = dpre[0 * NT + k] * in_hv1 + pre[0] * din[1 * NT + k];
+    for (int k = 0; k < NT; ++k) d265[k] = d263[k] + d264[k];
     double d266[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d266[k] = dpre[1 * NT + k] * in_hv0 + pre[1] * din[0 * NT + k];
+    for (int k = 0; k < NT; ++k) d266[k] = 3.0 * d265[k];
     double d267[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d267[k] = d265[k] - d266[k];
+    for (int k = 0; k < NT; ++k) d267[k] = dpre[14 * NT + k] * t150 + pre[14] * d150[k];
     double d268[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d268[k] = pre[26] * d261[k];
+    for (int k = 0; k < NT; ++k) d268[k] = dpre[15 * NT + k] * t151 + pre[15] * d151[k];
     double d269[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d269[k] = pre[26] * d264[k];
+    for (int k = 0; k < NT; ++k) d269[k] = d267[k] + d268[k];
     double d270[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d270[k] = pre[26] * d267[k];
+    for (int k = 0; k < NT; ++k) d270[k] = dpre[16 * NT + k] * t152 + pre[16] * d152[k];
     double d271[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d271[k] = d155[k] * t157 + t155 * d157[k];
+    for (int k = 0; k < NT; ++k) d271[k] = d269[k] + d270[k];
     double d272[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d272[k] = d154[k] * t158 + t154 * d158[k];
+    for (int k = 0; k < NT; ++k) d272[k] = 3.0 * d271[k];
     double d273[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d273[k] = d271[k] - d272[k];
+    for (int k = 0; k < NT; ++k) d273[k] = d174[k] * pre[22];
     double d274[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d274[k] = d153[k] * t158 + t153 * d158[k];
+    for (int k = 0; k < NT; ++k) d274[k] = d273[k] - d153[k];
     double d275[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d275[k] = d155[k] * t156 + t155 * d156[k];
+    for (int k = 0; k < NT; ++k) d275[k] = dpre[14 * NT + k] * t266 + pre[14] * d266[k];
     double d276[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d276[k] = d274[k] - d275[k];
+    for (int k = 0; k < NT; ++k) d276[k] = d274[k] + d275[k];
     double d277[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d277[k] = d154[k] * t156 + t154 * d156[k];
+    for (int k = 0; k < NT; ++k) d277[k] = d177[k] * pre[22];
     double d278[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d278[k] = d153[k] * t157 + t153 * d157[k];
+    for (int k = 0; k < NT; ++k) d278[k] = d277[k] - d154[k];
     double d279[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d279[k] = d277[k] - d278[k];
+    for (int k = 0; k < NT; ++k) d279[k] = dpre[15 * NT + k] * t266 + pre[15] * d266[k];
     double d280[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d280[k] = dpre[19 * NT + k] * t156 + pre[19] * d156[k];
+    for (int k = 0; k < NT; ++k) d280[k] = d278[k] + d279[k];
     double d281[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d281[k] = dpre[20 * NT + k] * t157 + pre[20] * d157[k];
+    for (int k = 0; k < NT; ++k) d281[k] = d180[k] * pre[22];
     double d282[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d282[k] = d280[k] + d281[k];
+    for (int k = 0; k < NT; ++k) d282[k] = d281[k] - d155[k];
     double d283[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d283[k] = dpre[21 * NT + k] * t158 + pre[21] * d158[k];
+    for (int k = 0; k < NT; ++k) d283[k] = dpre[16 * NT + k] * t266 + pre[16] * d266[k];
     double d284[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d284[k] = d282[k] + d283[k];
     double d285[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d285[k] = 3.0 * d284[k];
+    for (int k = 0; k < NT; ++k) d285[k] = d174[k] * pre[23];
     double d286[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d286[k] = dpre[19 * NT + k] * t153 + pre[19] * d153[k];
+    for (int k = 0; k < NT; ++k) d286[k] = d285[k] - d150[k];
     double d287[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d287[k] = dpre[20 * NT + k] * t154 + pre[20] * d154[k];
+    for (int k = 0; k < NT; ++k) d287[k] = dpre[14 * NT + k] * t272 + pre[14] * d272[k];
     double d288[NT];
 #pragma unroll
     for (int k = 0; k < NT; ++k) d288[k] = d286[k] + d287[k];
     double d289[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d289[k] = dpre[21 * NT + k] * t155 + pre[21] * d155[k];
+    for (int k = 0; k < NT; ++k) d289[k] = d177[k] * pre[23];
     double d290[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d290[k] = d288[k] + d289[k];
+    for (int k = 0; k < NT; ++k) d290[k] = d289[k] - d151[k];
     double d291[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d291[k] = 3.0 * d290[k];
+    for (int k = 0; k < NT; ++k) d291[k] = dpre[15 * NT + k] * t272 + pre[15] * d272[k];
     double d292[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d292[k] = d155[k] * t269 + t155 * d269[k];
+    for (int k = 0; k < NT; ++k) d292[k] = d290[k] + d291[k];
     double d293[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d293[k] = d154[k] * t270 + t154 * d270[k];
+    for (int k = 0; k < NT; ++k) d293[k] = d180[k] * pre[23];
     double d294[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d294[k] = d292[k] - d293[k];
+    for (int k = 0; k < NT; ++k) d294[k] = d293[k] - d152[k];
     double d295[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d295[k] = d153[k] * t270 + t153 * d270[k];
+    for (int k = 0; k < NT; ++k) d295[k] = dpre[16 * NT + k] * t272 + pre[16] * d272[k];
     double d296[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d296[k] = d155[k] * t268 + t155 * d268[k];
+    for (int k = 0; k < NT; ++k) d296[k] = d294[k] + d295[k];
     double d297[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d297[k] = d295[k] - d296[k];
+    for (int k = 0; k < NT; ++k) d297[k] = d152[k] * t280 + t152 * d280[k];
     double d298[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d298[k] = d154[k] * t268 + t154 * d268[k];
+    for (int k = 0; k < NT; ++k) d298[k] = d151[k] * t284 + t151 * d284[k];
     double d299[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d299[k] = d153[k] * t269 + t153 * d269[k];
+    for (int k = 0; k < NT; ++k) d299[k] = d297[k] - d298[k];
     double d300[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d300[k] = d298[k] - d299[k];
+    for (int k = 0; k < NT; ++k) d300[k] = d150[k] * t284 + t150 * d284[k];
     double d301[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d301[k] = d158[k] * t269 + t158 * d269[k];
+    for (int k = 0; k < NT; ++k) d301[k] = d152[k] * t276 + t152 * d276[k];
     double d302[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d302[k] = d157[k] * t270 + t157 * d270[k];
+    for (int k = 0; k < NT; ++k) d302[k] = d300[k] - d301[k];
     double d303[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d303[k] = d301[k] - d302[k];
+    for (int k = 0; k < NT; ++k) d303[k] = d151[k] * t276 + t151 * d276[k];
     double d304[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d304[k] = d156[k] * t270 + t156 * d270[k];
+    for (int k = 0; k < NT; ++k) d304[k] = d150[k] * t280 + t150 * d280[k];
     double d305[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d305[k] = d158[k] * t268 + t158 * d268[k];
+    for (int k = 0; k < NT; ++k) d305[k] = d303[k] - d304[k];
     double d306[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d306[k] = d304[k] - d305[k];
+    for (int k = 0; k < NT; ++k) d306[k] = d155[k] * t292 + t155 * d292[k];
     double d307[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d307[k] = d157[k] * t268 + t157 * d268[k];
+    for (int k = 0; k < NT; ++k) d307[k] = d154[k] * t296 + t154 * d296[k];
     double d308[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d308[k] = d156[k] * t269 + t156 * d269[k];
+    for (int k = 0; k < NT; ++k) d308[k] = d306[k] - d307[k];
     double d309[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d309[k] = d307[k] - d308[k];
+    for (int k = 0; k < NT; ++k) d309[k] = d153[k] * t296 + t153 * d296[k];
     double d310[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d310[k] = dpre[20 * NT + k] * t155 + pre[20] * d155[k];
+    for (int k = 0; k < NT; ++k) d310[k] = d155[k] * t288 + t155 * d288[k];
     double d311[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d311[k] = dpre[21 * NT + k] * t154 + pre[21] * d154[k];
+    for (int k = 0; k < NT; ++k) d311[k] = d309[k] - d310[k];
     double d312[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d312[k] = d310[k] - d311[k];
+    for (int k = 0; k < NT; ++k) d312[k] = d154[k] * t288 + t154 * d288[k];
     double d313[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d313[k] = dpre[21 * NT + k] * t153 + pre[21] * d153[k];
+    for (int k = 0; k < NT; ++k) d313[k] = d153[k] * t292 + t153 * d292[k];
     double d314[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d314[k] = dpre[19 * NT + k] * t155 + pre[19] * d155[k];
+    for (int k = 0; k < NT; ++k) d314[k] = d312[k] - d313[k];
     double d315[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d315[k] = d313[k] - d314[k];
+    for (int k = 0; k < NT; ++k) d315[k] = kFA * d299[k];
     double d316[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d316[k] = dpre[19 * NT + k] * t154 + pre[19] * d154[k];
+    for (int k = 0; k < NT; ++k) d316[k] = kFA * d302[k];
     double d317[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d317[k] = dpre[20 * NT + k] * t153 + pre[20] * d153[k];
+    for (int k = 0; k < NT; ++k) d317[k] = kFA * d305[k];
     double d318[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d318[k] = d316[k] - d317[k];
+    for (int k = 0; k < NT; ++k) d318[k] = kFA * d308[k];
     double d319[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d319[k] = dpre[20 * NT + k] * t158 + pre[20] * d158[k];
+    for (int k = 0; k < NT; ++k) d319[k] = kFA * d311[k];
     double d320[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) d320[k] = dpre[21 * NT + k] * t157 + pre[21] * d157[k];
-    double d321[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d321[k] = d319[k] - d320[k];
-    double d322[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d322[k] = dpre[21 * NT + k] * t156 + pre[21] * d156[k];
-    double d323[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d323[k] = dpre[19 * NT + k] * t158 + pre[19] * d158[k];
-    double d324[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d324[k] = d322[k] - d323[k];
-    double d325[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d325[k] = dpre[19 * NT + k] * t157 + pre[19] * d157[k];
-    double d326[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d326[k] = dpre[20 * NT + k] * t156 + pre[20] * d156[k];
-    double d327[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d327[k] = d325[k] - d326[k];
-    double d328[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d328[k] = pre[27] * d294[k];
-    double d329[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d329[k] = d328[k] - d273[k];
-    double d330[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d330[k] = d285[k] * t312 + t285 * d312[k];
-    double d331[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d331[k] = d329[k] + d330[k];
-    double d332[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d332[k] = kFA * d331[k];
-    double d333[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d333[k] = pre[27] * d297[k];
-    double d334[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d334[k] = d333[k] - d276[k];
-    double d335[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d335[k] = d285[k] * t315 + t285 * d315[k];
-    double d336[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d336[k] = d334[k] + d335[k];
-    double d337[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d337[k] = kFA * d336[k];
-    double d338[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d338[k] = pre[27] * d300[k];
-    double d339[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d339[k] = d338[k] - d279[k];
-    double d340[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d340[k] = d285[k] * t318 + t285 * d318[k];
-    double d341[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d341[k] = d339[k] + d340[k];
-    double d342[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d342[k] = kFA * d341[k];
-    double d343[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d343[k] = pre[28] * d303[k];
-    double d344[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d344[k] = d273[k] + d343[k];
-    double d345[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d345[k] = d291[k] * t321 + t291 * d321[k];
-    double d346[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d346[k] = d344[k] + d345[k];
-    double d347[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d347[k] = kFA * d346[k];
-    double d348[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d348[k] = pre[28] * d306[k];
-    double d349[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d349[k] = d276[k] + d348[k];
-    double d350[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d350[k] = d291[k] * t324 + t291 * d324[k];
-    double d351[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d351[k] = d349[k] + d350[k];
-    double d352[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d352[k] = kFA * d351[k];
-    double d353[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d353[k] = pre[28] * d309[k];
-    double d354[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d354[k] = d279[k] + d353[k];
-    double d355[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d355[k] = d291[k] * t327 + t291 * d327[k];
-    double d356[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d356[k] = d354[k] + d355[k];
-    double d357[NT];
-#pragma unroll
-    for (int k = 0; k < NT; ++k) d357[k] = kFA * d356[k];
+    for (int k = 0; k < NT; ++k) d320[k] = kFA * d314[k];
     out[0] = t239;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dout[0 * NT + k] = d239[k];
@@ -4735,24 +4330,24 @@ __host__ __device__ __forceinline__ void adj_gr_iter_jvp(const double* __restric
     out[2] = t249;
 #pragma unroll
     for (int k = 0; k < NT; ++k) dout[2 * NT + k] = d249[k];
-    out[3] = t347;
+    out[3] = t318;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dout[3 * NT + k] = d347[k];
-    out[4] = t352;
+    for (int k = 0; k < NT; ++k) dout[3 * NT + k] = d318[k];
+    out[4] = t319;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dout[4 * NT + k] = d352[k];
-    out[5] = t357;
+    for (int k = 0; k < NT; ++k) dout[4 * NT + k] = d319[k];
+    out[5] = t320;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dout[5 * NT + k] = d357[k];
-    out[6] = t332;
+    for (int k = 0; k < NT; ++k) dout[5 * NT + k] = d320[k];
+    out[6] = t315;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dout[6 * NT + k] = d332[k];
-    out[7] = t337;
+    for (int k = 0; k < NT; ++k) dout[6 * NT + k] = d315[k];
+    out[7] = t316;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dout[7 * NT + k] = d337[k];
-    out[8] = t342;
+    for (int k = 0; k < NT; ++k) dout[7 * NT + k] = d316[k];
+    out[8] = t317;
 #pragma unroll
-    for (int k = 0; k < NT; ++k) dout[8 * NT + k] = d342[k];
+    for (int k = 0; k < NT; ++k) dout[8 * NT + k] = d317[k];
 }
 
 }  // namespace posi_adj
