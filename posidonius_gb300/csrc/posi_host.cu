@@ -260,13 +260,14 @@ int build_buckets(posi_batch* b, const int64_t* sys_i64, const std::map<int64_t,
 // With `jobs` warps of systems between one and two per SMSP, the first
 // `light` blocks hold four jobs (one warp per SMSP) and the others eight (two
 // per SMSP).  A lone warp runs kLoneSpeed times as many steps per unit time as
-// one sharing its SMSP (measured on GB300: 121 against 213 us per step of the
-// 8-body ensemble), so in every sub-launch the jobs in lone slots get that
-// many more steps, and the jobs with the most steps left take the lone slots.
+// one sharing its SMSP (measured on GB300: 104.8 against 169.2 us per step of
+// the 8-body ensemble at 2432 and 4864 systems), so in every sub-launch the
+// jobs in lone slots get that many more steps, and the jobs with the most
+// steps left take the lone slots.
 // table: per sub-launch, the job of every slot (-1: idle) then its steps.
 // Returns false when the bucket needs no schedule.
 bool build_schedule(int sms, int jobs, int64_t steps, std::vector<int32_t>& table, int& launches) {
-    constexpr double kLoneSpeed = 1.75;
+    constexpr double kLoneSpeed = 1.6;
     // about this many sub-launches per launch of `steps` steps, at least 50
     // steps each: a sub-launch costs tens of microseconds (state load and
     // store, launch, the tail of its slowest slot), which a short launch

@@ -1645,9 +1645,9 @@ struct Sys {
                 const double rad = P(PC_A) * (P(PC_GR0) + nv2 * (P(PC_GR1) + P(PC_K2C) * nv2 - P(PC_K4C) * vr2) +
                                               vr2 * (P(PC_GR2) + P(PC_K3C) * vr2));
                 const double ort = vr * (P(PC_GO0) + P(PC_GO1) * nv2 + P(PC_GO2) * vr2);
-                double g0 = rad * xd + ort * hv0;
-                double g1 = rad * yd + ort * hv1;
-                double g2 = rad * zd + ort * hv2;
+                aa0 += rad * xd; aa0 += ort * hv0;
+                aa1 += rad * yd; aa1 += ort * hv1;
+                aa2 += rad * zd; aa2 += ort * hv2;
                 // spin-orbit
                 const double sL0 = card[HC_SLX], sL1 = card[HC_SLY], sL2 = card[HC_SLZ];
                 const double pL0 = b.moi * S0, pL1 = b.moi * S1, pL2 = b.moi * S2;
@@ -1665,10 +1665,9 @@ struct Sys {
                 const double q0 = vr * nn0 - hv0, q1 = vr * nn1 - hv1, q2 = vr * nn2 - hv2;
                 const double vr2x = 2. * vr;
                 const double a0 = 7. * q0 + vr2x * nn0, a1 = 7. * q1 + vr2x * nn1, a2 = 7. * q2 + vr2x * nn2;
-                g0 += kFA * (e1x + (a1 * t2 - a2 * t1) + 3. * (q1 * msz - q2 * msy));
-                g1 += kFA * (e1y + (a2 * t0 - a0 * t2) + 3. * (q2 * msx - q0 * msz));
-                g2 += kFA * (e1z + (a0 * t1 - a1 * t0) + 3. * (q0 * msy - q1 * msx));
-                aa0 += g0; aa1 += g1; aa2 += g2;
+                aa0 += kFA * (e1x + (a1 * t2 - a2 * t1) + 3. * (q1 * msz - q2 * msy));
+                aa1 += kFA * (e1y + (a2 * t0 - a0 * t2) + 3. * (q2 * msx - q0 * msz));
+                aa2 += kFA * (e1z + (a0 * t1 - a1 * t0) + 3. * (q0 * msy - q1 * msx));
                 // Kidder 1995 eq. 2.4a / 2.4b.  With L_o = mu (r x v) the
                 // torques are fm (L_o x S_h) - (L_p x S_h) + 3 (n.L_p) (n x S_h)
                 // on the host and fm2 (L_o x L_p) + (L_p x S_h) + 3 (n.S_h) (n x L_p)
@@ -2103,36 +2102,38 @@ struct Sys {
         }
     }
 
-    __device__ void alternative_to_inertial() {
+    // with_v = false: positions only (the pair loop needs nothing else;
+    // the velocities follow from the same alternative coordinates later)
+    __device__ void alternative_to_inertial(bool with_v = true) {
         if (coords == POSI_JACOBI) {
             // R_(k-1) = R_total - sum_(i >= k) (m_i / eta_i) r'_i
-            double res[6];
+            const int nk = with_v ? 6 : 3;
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
+                if (k >= nk) break;
                 const double a = k < 3 ? b.ap[k] : b.av[k - 3];
                 const double own = jac_c * a;
                 const double incl = gscan(own);
                 const double tot = gbcast(incl, G - 1);
                 const double R = gbcast(a, host);
-                res[k] = is_host ? R - tot : a + (R - (tot - incl + own));
+                const double res = is_host ? R - tot : a + (R - (tot - incl + own));
+                if (k < 3) b.r[k] = res; else b.v[k - 3] = res;
             }
-            b.r[0] = res[0]; b.r[1] = res[1]; b.r[2] = res[2];
-            b.v[0] = res[3]; b.v[1] = res[4]; b.v[2] = res[5];
         } else {
             const bool whds = coords == POSI_WHDS;
             const double w = whds ? whds_w : dh_w;
-            double res[6];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const double sp = gsum(planet() ? b.ap[k] * b.m : 0.) * inv_mtot;
-                const double sv = gsum(planet() ? b.av[k] * w : 0.);
-                const double R = gbcast(b.ap[k], host), V = gbcast(b.av[k], host);
+                const double R = gbcast(b.ap[k], host);
                 const double rh = R - sp;
-                res[k] = is_host ? rh : b.ap[k] + rh;
-                res[3 + k] = is_host ? V - sv : (whds ? b.av[k] / whds_f : b.av[k]) + V;
+                b.r[k] = is_host ? rh : b.ap[k] + rh;
+                if (with_v) {
+                    const double sv = gsum(planet() ? b.av[k] * w : 0.);
+                    const double V = gbcast(b.av[k], host);
+                    b.v[k] = is_host ? V - sv : (whds ? b.av[k] / whds_f : b.av[k]) + V;
+                }
             }
-            b.r[0] = res[0]; b.r[1] = res[1]; b.r[2] = res[2];
-            b.v[0] = res[3]; b.v[1] = res[4]; b.v[2] = res[5];
         }
     }
 
@@ -2611,13 +2612,27 @@ struct Sys {
         if (rp)
 #pragma unroll
             for (int k = 0; k < 3; ++k) { recw(posi_rec::SV_RJB + k, b.ap[k]); recw(posi_rec::SV_VJB + k, b.av[k]); }
+#if POSI_EXACT
         alternative_to_inertial();
+#else
+        // the velocities only where the step stops here (the state of a
+        // stopped system is the transformed one)
+        alternative_to_inertial(false);
+#endif
         if (rp)
 #pragma unroll
             for (int k = 0; k < 3; ++k) recw(posi_rec::SV_RG + k, b.r[k]);
+#if POSI_EXACT
         if (fatal()) return false;
         gravity(D, ignore);
         if (fatal()) return false;
+#else
+        if (!fatal()) gravity(D, ignore);
+        if (fatal()) {
+            alternative_to_inertial(true);
+            return false;
+        }
+#endif
         interaction_step(dt);
         jump_step(half_dt);
         if (rp)
