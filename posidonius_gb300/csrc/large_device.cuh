@@ -99,8 +99,8 @@ struct LDev {
 // own bodies (warp_active) add: a warp's FP64 add holds its SMSP's FP64 pipe
 // 64 cycles whatever its active lanes, so the warps' sums are formed with
 // the lanes spread over the slots -- eight slots at a time, lane 4 s + p adds
-// the eight values 8p .. 8p + 7 of slot s in lane order, then the quarters
-// pair up, ((q0 + q1) + (q2 + q3)) -- 9 FP64 adds per eight slots instead
+// the eight values 8p .. 8p + 7 of slot s as a pairwise tree, then the
+// quarters pair up, ((q0 + q1) + (q2 + q3)) -- 9 FP64 adds per eight slots instead
 // of 40 for shuffle trees.  The order of every slot's sum is fixed whatever
 // the number of slots, so a reduction carrying tangent slots beside the
 // primal ones gives the primal slots the same bits.
@@ -121,9 +121,8 @@ __device__ __forceinline__ void block_partial(double* bpart, const double (&vals
                 }
                 __syncwarp();
                 const double* t = &tw[warp][s * 33 + 8 * p];
-                double acc = t[0];
-#pragma unroll
-                for (int e = 1; e < 8; ++e) acc += t[e];
+                // a tree (depth 3, not a chain of 7): the adds wait on one another less
+                double acc = ((t[0] + t[1]) + (t[2] + t[3])) + ((t[4] + t[5]) + (t[6] + t[7]));
                 acc += __shfl_down_sync(0xffffffffu, acc, 1);
                 acc += __shfl_down_sync(0xffffffffu, acc, 2);
                 if (p == 0 && c * 8 + s < nslots) shm[warp * BP_ROW + c * 8 + s] = acc;

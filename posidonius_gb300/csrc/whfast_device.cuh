@@ -2183,7 +2183,8 @@ struct Sys {
         const double x2 = powi<2>(x);
         double z = beta * x2;
         int nq = 0;
-        while (fabs(z) > 0.1) { z = z / 4.; nq += 1; }
+        // |z| > 0.1 on the bit patterns (the same decision, off the FP64 pipe)
+        while (sq_gt(fabs(z), 0.1)) { z = z / 4.; nq += 1; }
         // 1/k!, k = 0..13
         const double if0 = 1., if1 = 1., if2 = 1. / 2., if3 = 1. / 6., if4 = 1. / 24., if5 = 1. / 120.,
                      if6 = 1. / 720., if7 = 1. / 5040., if8 = 1. / 40320., if9 = 1. / 362880.,
@@ -2256,11 +2257,12 @@ struct Sys {
         // first Newton step already lands within 1e-8 and the loop stops
         // after one more evaluation (the reference's second-order value
         // needs three).
-        double sqrt_beta = 0.;
         if (beta > 0.) {
-            sqrt_beta = sqrt(beta);
             xpp_nan = false;
-            if (fabs(kdt) * sqrt_beta * beta > kTWO_PI * mass_g && tw == 0) {
+            // |dt| sqrt(beta) beta > 2 pi GM squared (both sides positive):
+            // sqrt(beta) only where the iterations need the period
+            const double tpg = kTWO_PI * mass_g;
+            if (kdt * kdt * (beta * beta * beta) > tpg * tpg && tw == 0) {
                 status |= POSI_SYS_WARN_TIMESTEP;
                 isc[2] = 1;
             }
@@ -2307,7 +2309,7 @@ struct Sys {
                 ri = 1. / (r0 + e);
             }
         }
-        const bool jumped = !converged && !xpp_nan && fabs(x - old_x) * sqrt_beta > 0.02 * kPI;
+        const bool jumped = !converged && !xpp_nan && fabs(x - old_x) * sqrt(beta) > 0.02 * kPI;
 #endif
         if (converged) {
             // Halley's step converged
@@ -2368,6 +2370,7 @@ struct Sys {
             double x_min, x_max;
 #if !POSI_EXACT
             if (beta > 0.) {
+                const double sqrt_beta = sqrt(beta);
                 invperiod = sqrt_beta * beta / (kTWO_PI * mass_g);
                 x_per_period = kTWO_PI / sqrt_beta;
             }
