@@ -360,7 +360,13 @@ int posi_batch_mapping_for(const posi_batch* b, int64_t n);
  * integrates one system per process).  For every body count present, each
  * admissible lane mapping (2..32 lanes per system, one body per lane) runs
  * probe_steps steps on the systems of that count, timed with CUDA events; the
- * state is restored after every trial and the fastest mapping is kept.
+ * state is restored after every trial.  A batch of one body count keeps the
+ * fastest mapping.  When several counts together hold at least one warp per
+ * SMSP at their smallest lane groups (their launches share the GPU), each
+ * keeps the mapping of least SMSP time: probe time x min(warps, SMSPs) /
+ * SMSPs, since a bucket probed alone on fewer warps than SMSPs takes its
+ * longest lane's time whatever its lane group, while side by side its warps
+ * hold SMSPs the other buckets could use.
  * lanes_by_n (optional, POSI_MAX_BODIES + 1 entries) receives the choice per
  * body count (0 where no system has that count).  Results do not depend on
  * the mapping: every mapping computes the same bits. */

@@ -1045,7 +1045,10 @@ int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch)
     if (!b->graph || b->graph_steps != n_steps || b->graph_spl != steps_per_launch) {
         if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
         // balanced schedules of every (chunk length, bucket), made before the
-        // capture and kept with the graph
+        // capture and kept with the graph; a schedule assumes its bucket has
+        // the GPU to itself, so buckets launched side by side run plain
+        // (measured on the uneven ensemble: 594.7 us per step with schedules
+        // against 586.2 us without)
         const int slots = b->sms * (posi::kSchedBlockThreads / 32);
         std::vector<int32_t> tables;
         std::map<std::pair<int64_t, size_t>, std::pair<size_t, int>> plan;  // -> (offset, sub-launches)
@@ -1053,7 +1056,7 @@ int posi_batch_iterate(posi_batch* b, int64_t n_steps, int64_t steps_per_launch)
             const int64_t len = std::min(steps_per_launch, n_steps - c * steps_per_launch);
             for (size_t k = 0; k < b->buckets.size(); ++k) {
                 const Bucket& bk = b->buckets[k];
-                if (!b->balanced || b->ias15 || bk.G < 4 || plan.count({len, k})) continue;
+                if (!b->balanced || b->ias15 || bk.G < 4 || b->buckets.size() > 1 || plan.count({len, k})) continue;
                 const int jobs = (int)((bk.count + (32 / bk.G) - 1) / (32 / bk.G));
                 std::vector<int32_t> t;
                 int launches = 0;
@@ -1195,8 +1198,8 @@ int posi_set_ias15(posi_handle* h, const double* body_ias) {
 // Autotuner: for every body count present, run each admissible lane mapping
 // (2..32 lanes per system, at least one lane per body) on the systems of that
 // count for probe_steps steps -- once to warm up, once timed with CUDA events
-// -- restoring their state after every trial, and keep the fastest.  The
-// buckets are then rebuilt with the chosen mappings.
+// -- restoring their state after every trial, and keep the cheapest (below).
+// The buckets are then rebuilt with the chosen mappings.
 int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n) {
     if (!b || probe_steps < 1) return POSI_ERR_ARG;
     if (b->ias15) {
@@ -1252,11 +1255,25 @@ int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n)
     LaunchArgs a{};
     a.op = posi::OP_STEPS;
     a.n_steps = probe_steps;
+    // A bucket probed alone with fewer warps than the GPU has SMSPs times
+    // its longest lane's chain, whatever its lane group.  When the buckets
+    // run side by side and together fill the SMSPs, what a bucket costs the
+    // others is the SMSP time it holds: its probe time x min(warps, SMSPs) /
+    // SMSPs.  So with several buckets that together hold at least one warp
+    // per SMSP at their smallest groups, the mapping minimises that share;
+    // otherwise (one bucket, or a GPU the buckets do not fill) its time.
+    const int64_t smsps = 4 * (int64_t)b->sms;
+    int64_t min_warps = 0;
+    for (auto& kv : by_n) {
+        const int64_t per_warp = 32 / posi::group_size_for(kv.first);
+        min_warps += ((int64_t)kv.second.size() + per_warp - 1) / per_warp;
+    }
+    const bool shared_gpu = by_n.size() > 1 && min_warps >= smsps;
     for (auto& kv : by_n) {
         const int64_t n = kv.first;
         const std::vector<int32_t>& sys = kv.second;
         CK(cudaMemcpyAsync(d_probe, sys.data(), sys.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));
-        double best = 1e300;
+        double best = 1e300, best_ms = 0.;
         int best_g = posi::group_size_for(n);
         std::array<double, 6> probes;
         probes.fill(-1.);
@@ -1273,13 +1290,15 @@ int posi_batch_autotune(posi_batch* b, int64_t probe_steps, int32_t* lanes_by_n)
                 CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
                 if ((rc = copy_all(false)) != POSI_OK) return rc;
             }
-            if (ms < best) { best = ms; best_g = G; }
+            const int64_t warps = ((int64_t)sys.size() + (32 / G) - 1) / (32 / G);
+            const double cost = shared_gpu ? ms * (double)std::min(warps, smsps) / (double)smsps : ms;
+            if (cost < best) { best = cost; best_ms = ms; best_g = G; }
             int k = 0;
             while ((1 << k) < G) ++k;
             probes[(size_t)k] = ms;
         }
         chosen[n] = best_g;
-        b->tuned_ms_of_n[n] = best;
+        b->tuned_ms_of_n[n] = best_ms;
         b->probe_ms_of_n[n] = probes;
     }
     CK(cudaStreamSynchronize(b->stream));

@@ -54,3 +54,21 @@ def test_balanced_schedule_exact_mode():
     assert la > lb
     assert np.all(a["sys_i64"][:, L.SI_ITERATION] == 120)
     assert np.array_equal(a["body_f64"].view(np.int64), b["body_f64"].view(np.int64))
+
+
+def test_side_by_side_buckets_run_plain():
+    """A batch of several body counts launches its buckets side by side; a
+    schedule assumes its bucket has the GPU to itself, so none is made."""
+    ens = E.workload_uneven(4096, seed=7)
+    assert len(np.unique(ens["sys_i64"][:, L.SI_N])) > 1
+    runs = []
+    for balanced in (True, False):
+        b = pg.Batch(ens, mode=pg.FAST)
+        b.set_balanced(balanced)
+        b.initialize_physical_values()
+        b.iterate(200, 200)
+        runs.append((b.get_state(), b.last_timing()[1]))
+        b.close()
+    (a, la), (c, lc) = runs
+    assert la == lc
+    assert np.array_equal(a["body_f64"].view(np.int64), c["body_f64"].view(np.int64))
