@@ -443,16 +443,15 @@ int compute_roche(posi_batch* b) {
     return POSI_OK;
 }
 
+// The transposes and copies share one staging buffer; the stream orders them
+// (a copy into or out of the buffer waits for the kernel before it), so one
+// synchronisation at the end suffices.
 int batch_get(const posi_batch* b, int64_t* si, double* sf, int64_t* bi, double* bf, double* roche) {
     int rc;
     if (si && (rc = download_aos<int64_t>(b, si, b->d_si, b->n_sys, POSI_SI_COUNT)) != POSI_OK) return rc;
-    CK(cudaStreamSynchronize(b->stream));
     if (sf && (rc = download_aos<double>(b, sf, b->d_sf, b->n_sys, POSI_SF_COUNT)) != POSI_OK) return rc;
-    CK(cudaStreamSynchronize(b->stream));
     if (bi && (rc = download_aos<int64_t>(b, bi, b->d_bi, b->stride, POSI_BI_COUNT)) != POSI_OK) return rc;
-    CK(cudaStreamSynchronize(b->stream));
     if (bf && (rc = download_aos<double>(b, bf, b->d_bf, b->stride, POSI_BF_COUNT)) != POSI_OK) return rc;
-    CK(cudaStreamSynchronize(b->stream));
     if (roche)
         CK(cudaMemcpyAsync(roche, b->d_roche, (size_t)b->stride * b->nmax * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
@@ -462,11 +461,8 @@ int batch_get(const posi_batch* b, int64_t* si, double* sf, int64_t* bi, double*
 int batch_set(posi_batch* b, const int64_t* si, const double* sf, const int64_t* bi, const double* bf) {
     int rc;
     if (si && (rc = upload_aos<int64_t>(b, si, b->d_si, b->n_sys, POSI_SI_COUNT)) != POSI_OK) return rc;
-    CK(cudaStreamSynchronize(b->stream));
     if (sf && (rc = upload_aos<double>(b, sf, b->d_sf, b->n_sys, POSI_SF_COUNT)) != POSI_OK) return rc;
-    CK(cudaStreamSynchronize(b->stream));
     if (bi && (rc = upload_aos<int64_t>(b, bi, b->d_bi, b->stride, POSI_BI_COUNT)) != POSI_OK) return rc;
-    CK(cudaStreamSynchronize(b->stream));
     if (bf && (rc = upload_aos<double>(b, bf, b->d_bf, b->stride, POSI_BF_COUNT)) != POSI_OK) return rc;
     CK(cudaStreamSynchronize(b->stream));
     return POSI_OK;
