@@ -229,6 +229,51 @@ def test_batched_maximum_body_count_exact():
     assert bitwise_diffs(bi.get_state(), ref) == []
 
 
+def test_collision_first_pair_fast():
+    """FAST (the pair loop over unordered pairs in rounds, the lanes keeping
+    their least pair): with two overlapping pairs in one system the event
+    reported is the first in (i, j) order, as in the reference, and the
+    stopped system's state -- its velocities transformed at the stop --
+    matches the oracle's."""
+    ens = E.workload_ensemble8(4, seed=9)
+    # planet 6 on top of planet 5 and planet 3 on top of planet 2: the pair
+    # (2, 3) comes first in (i, j) order; the rounds meet (5, 6) as early
+    ens["body_f64"][1, 6, L.POS] = ens["body_f64"][1, 5, L.POS] + 1e-9
+    ens["body_f64"][1, 6, L.VEL] = ens["body_f64"][1, 5, L.VEL]
+    ens["body_f64"][1, 3, L.POS] = ens["body_f64"][1, 2, L.POS] + 1e-9
+    ens["body_f64"][1, 3, L.VEL] = ens["body_f64"][1, 2, L.VEL]
+    ref, _, _ = oracle.run(ens, max_steps=5, init_physical=True)
+    b = pg.Batch(ens, mode=pg.FAST)
+    b.initialize_physical_values()
+    b.iterate(5)
+    st = b.get_state()
+    for f in (L.SI_STATUS, L.SI_FAIL_PAIR, L.SI_FAIL_STEP, L.SI_ITERATION):
+        assert st["sys_i64"][1, f] == ref["sys_i64"][1, f], f
+    assert st["sys_i64"][1, L.SI_FAIL_PAIR] == 2 * 1024 + 3
+    assert max_rel_error(st, ref) <= 1e-11   # 5 steps of at most 1e-12 each
+
+
+def test_batched_maximum_body_count_fast():
+    """The same largest systems under FAST (pairwise gravity over unordered
+    pairs in rounds of shuffled terms, with odd and even body counts up to
+    32 in one warp): within 1e-12 of the oracle after one step and 1e-10
+    after 30."""
+    cases = []
+    for coords, n_small in ((L.JACOBI, 29), (L.DEMOCRATIC_HELIOCENTRIC, 29), (L.WHDS, 29), (L.JACOBI, 14),
+                            (L.WHDS, 17)):
+        cases.append(E.workload_large(n_small, seed=7 + n_small, coords=coords))
+    ens = stack(cases, nmax=L.MAX_BODIES)
+    for steps, tol in ((1, 1e-12), (30, 1e-10)):
+        ref, _, _ = oracle.run(ens, max_steps=steps, init_physical=True, nthreads=5)
+        b = pg.Batch(ens, mode=pg.FAST)
+        b.initialize_physical_values()
+        b.iterate(steps, steps)
+        got = b.get_state()
+        b.close()
+        assert np.all(got["sys_i64"][:, L.SI_ITERATION] == steps)
+        assert max_rel_error(got, ref) <= tol, (steps, max_rel_error(got, ref))
+
+
 def test_empty_and_zero_step_requests():
     """An ensemble of no systems is refused; zero steps change no bit; a
     completed system stays frozen under further steps."""
