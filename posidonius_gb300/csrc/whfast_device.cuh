@@ -2286,12 +2286,16 @@ struct Sys {
         x = ri * (x * e - eta0 * gs[2] - zeta0 * gs[3] + kdt);
         const bool jumped = !xpp_nan && fabs(x - old_x) > 0.01 * x_per_period;
 #else
-        // Halley's step from the series start (cubic: a start within 4e-6
-        // of the root lands within 1e-17 of it, below the rounding of x),
-        // then the G-functions at the new x by a second-order Taylor step
-        // (dG0 = -beta G1, dG1 = G0, dG2 = G1, dG3 = G2 per unit x).  Starts
-        // further off go on with the Newton iterations below.
-        {
+        // Halley's step from the series start of a bound orbit (cubic: a
+        // start within 4e-6 of the root lands within 1e-17 of it, below the
+        // rounding of x), then the G-functions at the new x by a second-order
+        // Taylor step (dG0 = -beta G1, dG1 = G0, dG2 = G1, dG3 = G2 per unit
+        // x).  Starts further off go on with the Newton iterations below; an
+        // unbound orbit (no series start) takes Newton's first step.
+        if (!(beta > 0.)) {
+            ri = 1. / (r0 + e);
+            x = ri * (x * e - eta0 * gs[2] - zeta0 * gs[3] + kdt);
+        } else {
             const double fx = r0 * x + eta0 * gs[2] + zeta0 * gs[3] - kdt;
             const double fp = r0 + e;
             const double fpp = eta0 * gs[0] + zeta0 * gs[1];
