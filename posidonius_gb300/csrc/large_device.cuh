@@ -538,11 +538,18 @@ struct Large {
     // With cm != nullptr the last convergence reduction also carries the sums
     // of m r and m v over all bodies at the final velocities (cm[0..5]), and
     // their tangents (tcm).
+    // The position terms of the effect blocks (and their tangents): the
+    // closing half kick of a step and the opening one of the next see the
+    // same positions, so the second reuses the first's; a drift clears them.
+    Pre prc, dprc;
+    bool prc_ok = false;
+
     __device__ bool midpoint(double hdt, double* cm, double* tcm) {
         double x[3] = {0., 0., 0.};
-        Pre pr, dpr;
+        Pre& pr = prc;
+        Pre& dpr = dprc;
         const bool tn = tan_on();
-        if (planet) {
+        if (planet && !prc_ok) {
             for (int q = 0; q < 3; ++q) x[q] = b.r[q] - h.r[q];
             if (tides_on()) adj_tides_pre(x[0], x[1], x[2], c.sig, hc.sig, c.k2, hc.k2, c.R, hc.R, hc.m, c.m, pr.t);
             if (flat_on()) adj_flat_pre(x[0], x[1], x[2], c.R, hc.R, hc.k2f, hc.m, c.k2f, c.m, pr.f);
@@ -564,6 +571,7 @@ struct Large {
                     adj_gr_pre_jvp<1>(x[0], x[1], x[2], hc.m, hc.mg, hc.moi, c.m, c.mg, c.moi, din, scratch, dpr.g);
             }
         }
+        prc_ok = true;
         const double mr = planet ? c.m / hc.m : 0.;
         // own and host: original, current, previous-final, previous spin
         double v0[3], L0[3], vc[3], Lc[3], vf[3], Lf[3], pv[3], pL[3], Sp[3], Sc[3], dvc[3], dLc[3];
@@ -891,6 +899,7 @@ struct Large {
     // the neglected third order is below 1e-24 relative), one reciprocal of
     // r instead of three divisions.
     __device__ void kepler(double x[3], double u[3], double tx[3], double tu[3]) {
+        prc_ok = false;  // the drift moves the positions
         if (planet) {
             const double mu = kgm, dt = half_dt;
             const double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
