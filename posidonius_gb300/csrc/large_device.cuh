@@ -354,7 +354,12 @@ __device__ void pair_loop(const LDev& D, int host, int64_t p1, bool jac) {
     const int64_t npairs = (int64_t)T * (T + 1) / 2;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    for (int64_t tp = blockIdx.x + (int64_t)gridDim.x * wib; tp < npairs; tp += (int64_t)gridDim.x * wpb) {
+    // a work item is half a tile pair: partner offsets [0, 16) or [16, 32)
+    // (the diagonal pair from 1), so that two items share an SMSP where one
+    // pair would leave a lone warp; each half writes its own partial slot
+    for (int64_t it = blockIdx.x + (int64_t)gridDim.x * wib; it < 2 * npairs; it += (int64_t)gridDim.x * wpb) {
+        const int h = it >= npairs ? 1 : 0;
+        const int64_t tp = it - h * npairs;
         int I = 0;
         int64_t r = tp;
         while (r >= T - I) { r -= T - I; ++I; }
@@ -375,7 +380,8 @@ __device__ void pair_loop(const LDev& D, int host, int64_t p1, bool jac) {
         }
         // the partner tile: positions, masses and sums travel together (the
         // partner's index follows from the step: lane l holds 32 J + (l + k) mod 32)
-        const int64_t j0 = (int64_t)J * 32 + lane;
+        const int kb = h ? 16 : (diag ? 1 : 0), ke = h ? 32 : 16;
+        const int64_t j0 = (int64_t)J * 32 + ((lane + kb) & 31);
         double xj = 0., yj = 0., zj = 0., gmj = 0.;
         double txj[3][AN] = {}, taj[3][AN] = {};
         double axj = 0., ayj = 0., azj = 0.;
@@ -392,9 +398,7 @@ __device__ void pair_loop(const LDev& D, int host, int64_t p1, bool jac) {
         double ax = 0., ay = 0., az = 0.;
         double tai[3][AN] = {};
         unsigned long long bad = ~0ull;
-        if (diag)
-            rotate_partner<NT>(lane, xj, yj, zj, gmj, axj, ayj, azj, txj, taj);
-        for (int k = diag ? 1 : 0; k < 32; ++k) {
+        for (int k = kb; k < ke; ++k) {
             const int64_t j = (int64_t)J * 32 + ((lane + k) & 31);
             if (hi && j < n) {
                 const double dx = xi - xj, dy = yi - yj, dz = zi - zj;
@@ -431,22 +435,25 @@ __device__ void pair_loop(const LDev& D, int host, int64_t p1, bool jac) {
             }
             rotate_partner<NT>(lane, xj, yj, zj, gmj, axj, ayj, azj, txj, taj);
         }
-        // 32 rotations: every partner is back in its own lane
+        // after the half's rotations lane l holds the partner 32 J + (l + ke) mod 32;
+        // partial slot 2 K + h holds the sums over partner tile K's half h
+        const int64_t sj = 2 * (int64_t)J + h, si = 2 * (int64_t)I + h;
         if (hi) {
-            D.gpart[((int64_t)J * rows + 0) * n + i] = ax;
-            D.gpart[((int64_t)J * rows + 1) * n + i] = ay;
-            D.gpart[((int64_t)J * rows + 2) * n + i] = az;
+            D.gpart[(sj * rows + 0) * n + i] = ax;
+            D.gpart[(sj * rows + 1) * n + i] = ay;
+            D.gpart[(sj * rows + 2) * n + i] = az;
             if constexpr (NT > 0)
                 for (int q = 0; q < 3; ++q)
-                    for (int d = 0; d < NT; ++d) D.gpart[((int64_t)J * rows + 3 + q * NT + d) * n + i] = tai[q][d];
+                    for (int d = 0; d < NT; ++d) D.gpart[(sj * rows + 3 + q * NT + d) * n + i] = tai[q][d];
         }
-        if (!diag && j0 < n) {
-            D.gpart[((int64_t)I * rows + 0) * n + j0] = axj;
-            D.gpart[((int64_t)I * rows + 1) * n + j0] = ayj;
-            D.gpart[((int64_t)I * rows + 2) * n + j0] = azj;
+        const int64_t jw = (int64_t)J * 32 + ((lane + ke) & 31);
+        if (!diag && jw < n) {
+            D.gpart[(si * rows + 0) * n + jw] = axj;
+            D.gpart[(si * rows + 1) * n + jw] = ayj;
+            D.gpart[(si * rows + 2) * n + jw] = azj;
             if constexpr (NT > 0)
                 for (int q = 0; q < 3; ++q)
-                    for (int d = 0; d < NT; ++d) D.gpart[((int64_t)I * rows + 3 + q * NT + d) * n + j0] = taj[q][d];
+                    for (int d = 0; d < NT; ++d) D.gpart[(si * rows + 3 + q * NT + d) * n + jw] = taj[q][d];
         }
         if (bad != ~0ull) atomicMin(D.bad, bad);
     }
@@ -830,8 +837,8 @@ struct Large {
         if (!grid_barrier(D)) return false;
         if (D.per_block == 32) {
             // the body block's 32 bodies are tile blockIdx.x: its eight warps
-            // add the partial sums together -- warp w the partner tiles
-            // [w c, (w + 1) c), c = ceil(ntile / 8), in order -- and the
+            // add the partial sums together -- warp w the half-tile slots
+            // [w c, (w + 1) c), c = ceil(2 ntile / 8), in order -- and the
             // chunk sums are added in warp order: a fixed order whatever the
             // number of tangent rows, loads spread over the block instead of
             // one latency-bound chain per body
@@ -839,9 +846,10 @@ struct Large {
             __shared__ double gfinal[3 * (1 + kMaxTangents)][32];
             constexpr int rows = 3 * (1 + NT);
             const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-            const int c = (D.ntile + kBlock / 32 - 1) / (kBlock / 32);
+            const int nslot = 2 * D.ntile;  // two half-tile partials per partner tile
+            const int c = (nslot + kBlock / 32 - 1) / (kBlock / 32);
             const int64_t body = (int64_t)blockIdx.x * 32 + l, nn = n;
-            const int k0 = w * c, k1 = min(D.ntile, (w + 1) * c);
+            const int k0 = w * c, k1 = min(nslot, (w + 1) * c);
             for (int rg = 0; rg < rows; rg += 3) {
                 double v[3] = {0., 0., 0.};
                 if (body < nn)
@@ -876,13 +884,14 @@ struct Large {
                 const double* src = D.gpart + (int64_t)row * nn + i;
                 const int64_t stride = (int64_t)rows * nn;
                 double acc = 0.;
-                for (int kk = 0; kk < D.ntile; kk += 8) {
+                const int nslot = 2 * D.ntile;
+                for (int kk = 0; kk < nslot; kk += 8) {
                     double v[8];
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) v[e] = kk + e < D.ntile ? __ldcg(src + (int64_t)(kk + e) * stride) : 0.;
+                    for (int e = 0; e < 8; ++e) v[e] = kk + e < nslot ? __ldcg(src + (int64_t)(kk + e) * stride) : 0.;
 #pragma unroll
                     for (int e = 0; e < 8; ++e)
-                        if (kk + e < D.ntile) acc += v[e];
+                        if (kk + e < nslot) acc += v[e];
                 }
                 if (qq < 3) a[qq] = acc; else da[qq - 3] = acc;
             }
