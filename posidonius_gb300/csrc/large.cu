@@ -127,7 +127,8 @@ posi_large* posi_large_create(int64_t n, const int64_t* sys_i64, const double* s
         !ok(cudaMalloc(&L->d_roche, (size_t)n * n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_near2, (size_t)n * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_pos, (size_t)3 * n * sizeof(double))) ||
-        !ok(cudaMalloc(&L->d_gpart, (size_t)2 * L->ntile * 3 * (1 + posi_many::kMaxTangents) * n * sizeof(double))) ||
+        !ok(cudaMalloc(&L->d_gpart, (size_t)posi_many::kPairSplit * L->ntile * 3 * (1 + posi_many::kMaxTangents) * n *
+                                        sizeof(double))) ||
         !ok(cudaMalloc(&L->d_bpart, (size_t)2 * L->grid * posi_many::BP_ROW * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_tot, posi_many::BP_ROW * sizeof(double))) ||
         !ok(cudaMalloc(&L->d_tan, (size_t)posi_many::kMaxTangents * 12 * n * sizeof(double))) ||

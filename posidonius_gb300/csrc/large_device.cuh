@@ -62,6 +62,10 @@ constexpr long long kBarrierWaitCycles = 4000000000LL;  // about 2 s at the maxi
 // directions a reduction carries 10 + 6 NT values.  Partial rows are BP_ROW
 // doubles apart whatever the count.
 enum { BP_SLOTS = 16, BP_ROW = 40 };
+// parts a tile pair of the pair loop is split into (a divisor of 32): halves
+// measured best at 1024 bodies (131.6 us per step; quarters 132.7, eighths
+// 138.0 -- more partial slots to gather -- and whole pairs 140.8)
+constexpr int kPairSplit = 2;
 constexpr int kMaxTangents = 4;
 constexpr int slots_for(int nt) { return nt == 0 ? BP_SLOTS : 10 + 6 * nt; }
 static_assert(slots_for(kMaxTangents) <= BP_ROW, "partial row too short");
@@ -354,11 +358,13 @@ __device__ void pair_loop(const LDev& D, int host, int64_t p1, bool jac) {
     const int64_t npairs = (int64_t)T * (T + 1) / 2;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    // a work item is half a tile pair: partner offsets [0, 16) or [16, 32)
-    // (the diagonal pair from 1), so that two items share an SMSP where one
-    // pair would leave a lone warp; each half writes its own partial slot
-    for (int64_t it = blockIdx.x + (int64_t)gridDim.x * wib; it < 2 * npairs; it += (int64_t)gridDim.x * wpb) {
-        const int h = it >= npairs ? 1 : 0;
+    // a work item is a part of a tile pair: partner offsets
+    // [32 h / kPairSplit, 32 (h + 1) / kPairSplit) (the diagonal pair from
+    // 1), so that several items share an SMSP where one pair would leave a
+    // lone warp; each part writes its own partial slot
+    for (int64_t it = blockIdx.x + (int64_t)gridDim.x * wib; it < kPairSplit * npairs;
+         it += (int64_t)gridDim.x * wpb) {
+        const int h = (int)(it / npairs);
         const int64_t tp = it - h * npairs;
         int I = 0;
         int64_t r = tp;
@@ -380,7 +386,7 @@ __device__ void pair_loop(const LDev& D, int host, int64_t p1, bool jac) {
         }
         // the partner tile: positions, masses and sums travel together (the
         // partner's index follows from the step: lane l holds 32 J + (l + k) mod 32)
-        const int kb = h ? 16 : (diag ? 1 : 0), ke = h ? 32 : 16;
+        const int kb = h ? h * (32 / kPairSplit) : (diag ? 1 : 0), ke = (h + 1) * (32 / kPairSplit);
         const int64_t j0 = (int64_t)J * 32 + ((lane + kb) & 31);
         double xj = 0., yj = 0., zj = 0., gmj = 0.;
         double txj[3][AN] = {}, taj[3][AN] = {};
@@ -435,9 +441,9 @@ __device__ void pair_loop(const LDev& D, int host, int64_t p1, bool jac) {
             }
             rotate_partner<NT>(lane, xj, yj, zj, gmj, axj, ayj, azj, txj, taj);
         }
-        // after the half's rotations lane l holds the partner 32 J + (l + ke) mod 32;
-        // partial slot 2 K + h holds the sums over partner tile K's half h
-        const int64_t sj = 2 * (int64_t)J + h, si = 2 * (int64_t)I + h;
+        // after the part's rotations lane l holds the partner 32 J + (l + ke) mod 32;
+        // partial slot kPairSplit K + h holds the sums over partner tile K's part h
+        const int64_t sj = kPairSplit * (int64_t)J + h, si = kPairSplit * (int64_t)I + h;
         if (hi) {
             D.gpart[(sj * rows + 0) * n + i] = ax;
             D.gpart[(sj * rows + 1) * n + i] = ay;
@@ -837,8 +843,8 @@ struct Large {
         if (!grid_barrier(D)) return false;
         if (D.per_block == 32) {
             // the body block's 32 bodies are tile blockIdx.x: its eight warps
-            // add the partial sums together -- warp w the half-tile slots
-            // [w c, (w + 1) c), c = ceil(2 ntile / 8), in order -- and the
+            // add the partial sums together -- warp w the partial slots
+            // [w c, (w + 1) c), c = ceil(kPairSplit ntile / 8), in order -- and the
             // chunk sums are added in warp order: a fixed order whatever the
             // number of tangent rows, loads spread over the block instead of
             // one latency-bound chain per body
@@ -846,7 +852,7 @@ struct Large {
             __shared__ double gfinal[3 * (1 + kMaxTangents)][32];
             constexpr int rows = 3 * (1 + NT);
             const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-            const int nslot = 2 * D.ntile;  // two half-tile partials per partner tile
+            const int nslot = kPairSplit * D.ntile;  // kPairSplit partials per partner tile
             const int c = (nslot + kBlock / 32 - 1) / (kBlock / 32);
             const int64_t body = (int64_t)blockIdx.x * 32 + l, nn = n;
             const int k0 = w * c, k1 = min(nslot, (w + 1) * c);
@@ -884,7 +890,7 @@ struct Large {
                 const double* src = D.gpart + (int64_t)row * nn + i;
                 const int64_t stride = (int64_t)rows * nn;
                 double acc = 0.;
-                const int nslot = 2 * D.ntile;
+                const int nslot = kPairSplit * D.ntile;
                 for (int kk = 0; kk < nslot; kk += 8) {
                     double v[8];
 #pragma unroll
