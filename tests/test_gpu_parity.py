@@ -229,6 +229,33 @@ def test_batched_maximum_body_count_exact():
     assert bitwise_diffs(bi.get_state(), ref) == []
 
 
+@pytest.mark.parametrize("mode", [pg.EXACT, pg.FAST])
+def test_smallest_and_widest_lane_groups_agree(mode):
+    """Every system on its smallest lane group (2 lanes for 2 bodies, 4 for
+    3-4, 8 for 5-8, 16 for 9-10 -- the groups the autotuner picks when the
+    body counts share the GPU) against every system on a whole warp: the
+    same bits after 50 steps, and FAST within 1e-12 of the oracle after one
+    step on the smallest groups."""
+    ens = E.workload_uneven(512, seed=37)
+    out = []
+    for mapping in (L.MAP_LANES2, L.MAP_WARP):
+        b = pg.Batch(ens, mode=mode, mapping=mapping)
+        b.initialize_physical_values()
+        if mapping == L.MAP_LANES2:
+            assert b.mapping_for(2) == 2 and b.mapping_for(3) == 4 and b.mapping_for(9) == 16
+        b.iterate(50, 25)
+        out.append(b.get_state())
+        b.close()
+    assert bitwise_diffs(out[0], out[1]) == []
+    if mode == pg.FAST:
+        ref, _, _ = oracle.run(ens, max_steps=1, init_physical=True, nthreads=8)
+        b = pg.Batch(ens, mode=mode, mapping=L.MAP_LANES2)
+        b.initialize_physical_values()
+        b.iterate(1)
+        assert max_rel_error(b.get_state(), ref) <= 1e-12
+        b.close()
+
+
 def test_collision_first_pair_fast():
     """FAST (the pair loop over unordered pairs in rounds, the lanes keeping
     their least pair): with two overlapping pairs in one system the event
