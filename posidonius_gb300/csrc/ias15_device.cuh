@@ -40,6 +40,20 @@ __constant__ double kIAS_R[28] = {
     0x1.3ff25add4c6cfp-1, 0x1.b8b21f9dbc761p-2, 0x1.f24cbdf70c5a2p-3,
     0x1.79a65b9461f2ap-4,
 };
+// FAST: the reciprocals of kIAS_R (a product instead of a division in the
+// substep updates; one rounding more than the reference's division)
+__constant__ double kIAS_RINV[28] = {
+    1. / 0x1.cce7242fd9812p-5, 1. / 0x1.7122082358d27p-3, 1. / 0x1.fbd07e2ec4e45p-4,
+    1. / 0x1.6916742f0c9c5p-2, 1. / 0x1.2f798fa9116c3p-2, 1. / 0x1.610ae03ac0664p-3,
+    1. / 0x1.18248525f4802p-1, 1. / 0x1.f6ac25c5edd01p-2, 1. / 0x1.77b8063a3c970p-2,
+    1. / 0x1.8e652c39b8c7cp-3, 1. / 0x1.77ea65770fa49p-1, 1. / 0x1.5b1bf334120c8p-1,
+    1. / 0x1.1ba1e36e39700p-1, 1. / 0x1.86be56bf12acdp-2, 1. / 0x1.7f1781446c91fp-3,
+    1. / 0x1.c548c982467cdp-1, 1. / 0x1.a87a573f48e4cp-1, 1. / 0x1.6900477970483p-1,
+    1. / 0x1.10bd8f6ac02eap-1, 1. / 0x1.5a4888b8a3f96p-2, 1. / 0x1.3579902cdb60ep-3,
+    1. / 0x1.f47d94f4d2bb2p-1, 1. / 0x1.d7af22b1d5231p-1, 1. / 0x1.983512ebfc868p-1,
+    1. / 0x1.3ff25add4c6cfp-1, 1. / 0x1.b8b21f9dbc761p-2, 1. / 0x1.f24cbdf70c5a2p-3,
+    1. / 0x1.79a65b9461f2ap-4,
+};
 __constant__ double kIAS_C[21] = {
     -0x1.cce7242fd9812p-5, 0x1.4c4b384151c1ep-7, -0x1.e45bd12f4f32cp-3,
     -0x1.d4b3379a1992dp-9, 0x1.7f2161e152586p-4, -0x1.2da22e635a1aep-1,
@@ -201,8 +215,13 @@ struct Ias15 {
         ias_add_cs(gk, cs, zero);
         const double old = g[3 * j + c];
         const int base = j * (j + 1) / 2;
+#if POSI_EXACT
         double v = gk / kIAS_R[base];
         for (int m = 0; m < j; ++m) v = (v - g[3 * m + c]) / kIAS_R[base + 1 + m];
+#else
+        double v = gk * kIAS_RINV[base];
+        for (int m = 0; m < j; ++m) v = (v - g[3 * m + c]) * kIAS_RINV[base + 1 + m];
+#endif
         g[3 * j + c] = v;
         const double tmp = v - old;
         const int cb = j * (j - 1) / 2;
@@ -271,6 +290,9 @@ struct Ias15 {
                     const double h = kIAS_H[sub];
                     double sp[9];
                     sp[0] = S.dt * h;
+                    double sv[8];
+                    sv[0] = S.dt * h;
+#if POSI_EXACT
                     sp[1] = sp[0] * sp[0] / 2.;
                     sp[2] = sp[1] * h / 3.;
                     sp[3] = sp[2] * h / 2.;
@@ -279,8 +301,6 @@ struct Ias15 {
                     sp[6] = 5. * sp[5] * h / 7.;
                     sp[7] = 3. * sp[6] * h / 4.;
                     sp[8] = 7. * sp[7] * h / 9.;
-                    double sv[8];
-                    sv[0] = S.dt * h;
                     sv[1] = sv[0] * h / 2.;
                     sv[2] = 2. * sv[1] * h / 3.;
                     sv[3] = 3. * sv[2] * h / 4.;
@@ -288,6 +308,24 @@ struct Ias15 {
                     sv[5] = 5. * sv[4] * h / 6.;
                     sv[6] = 6. * sv[5] * h / 7.;
                     sv[7] = 7. * sv[6] * h / 8.;
+#else
+                    // the same factors with products by the reciprocals
+                    sp[1] = sp[0] * sp[0] * 0.5;
+                    sp[2] = sp[1] * h * (1. / 3.);
+                    sp[3] = sp[2] * h * 0.5;
+                    sp[4] = sp[3] * h * (3. / 5.);
+                    sp[5] = sp[4] * h * (2. / 3.);
+                    sp[6] = sp[5] * h * (5. / 7.);
+                    sp[7] = sp[6] * h * 0.75;
+                    sp[8] = sp[7] * h * (7. / 9.);
+                    sv[1] = sv[0] * h * 0.5;
+                    sv[2] = sv[1] * h * (2. / 3.);
+                    sv[3] = sv[2] * h * 0.75;
+                    sv[4] = sv[3] * h * 0.8;
+                    sv[5] = sv[4] * h * (5. / 6.);
+                    sv[6] = sv[5] * h * (6. / 7.);
+                    sv[7] = sv[6] * h * 0.875;
+#endif
                     if (S.has) {
                         for (int c = 0; c < 3; ++c) {
                             // Everhart's eq. 9 (positions) and 10 (velocities, spins)
@@ -419,23 +457,41 @@ struct Ias15 {
             // Everhart's eqs. 11-12, compensated
             if (S.has) {
                 const double dt2 = dt_done * dt_done;
+#if POSI_EXACT
                 const double xdiv[7] = {6., 12., 20., 30., 42., 56., 72.};
                 const double vdiv[7] = {2., 3., 4., 5., 6., 7., 8.};
+#else
+                // products by the reciprocals
+                const double xmul[7] = {1. / 6., 1. / 12., 1. / 20., 1. / 30., 1. / 42., 1. / 56., 1. / 72.};
+                const double vmul[7] = {0.5, 1. / 3., 0.25, 0.2, 1. / 6., 1. / 7., 0.125};
+#endif
                 for (int c = 0; c < 3; ++c) {
                     double x = L.x0[c], cx = L.csx[c];
+#if POSI_EXACT
                     for (int j = 6; j >= 0; --j) ias_add_cs(x, cx, L.b[3 * j + c] / xdiv[j] * dt2);
+#else
+                    for (int j = 6; j >= 0; --j) ias_add_cs(x, cx, L.b[3 * j + c] * xmul[j] * dt2);
+#endif
                     ias_add_cs(x, cx, L.a0[c] / 2. * dt2);
                     ias_add_cs(x, cx, L.v0[c] * dt_done);
                     L.csx[c] = cx;
                     double v = L.v0[c], cv = L.csv[c];
+#if POSI_EXACT
                     for (int j = 6; j >= 0; --j) ias_add_cs(v, cv, L.b[3 * j + c] / vdiv[j] * dt_done);
+#else
+                    for (int j = 6; j >= 0; --j) ias_add_cs(v, cv, L.b[3 * j + c] * vmul[j] * dt_done);
+#endif
                     ias_add_cs(v, cv, L.a0[c] * dt_done);
                     L.csv[c] = cv;
                     bd.r[c] = x;
                     bd.v[c] = v;
                     if (ispin) {
                         double l = L.l0[c], cl = L.css[c];
+#if POSI_EXACT
                         for (int j = 6; j >= 0; --j) ias_add_cs(l, cl, L.sb[3 * j + c] / vdiv[j] * dt_done);
+#else
+                        for (int j = 6; j >= 0; --j) ias_add_cs(l, cl, L.sb[3 * j + c] * vmul[j] * dt_done);
+#endif
                         ias_add_cs(l, cl, L.dl0[c] * dt_done);
                         L.css[c] = cl;
                         bd.L[c] = l;
