@@ -97,8 +97,12 @@ class Graph:
         if a.op == "lit" and (b is None or b.op == "lit"):
             x, y = a.val, (b.val if b is not None else None)
             v = {"add": lambda: x + y, "sub": lambda: x - y, "mul": lambda: x * y, "div": lambda: x / y,
-                 "neg": lambda: -x, "sqrt": lambda: x ** 0.5}[op]()
+                 "neg": lambda: -x, "sqrt": lambda: x ** 0.5, "rcp": lambda: 1.0 / x}[op]()
             return self.lit(v)
+        # a / b as a (1 / b): one division per divisor, shared by every
+        # quotient and by the sweeps' derivatives (d(1/b) = -(1/b)^2 db)
+        if op == "div":
+            return self.op("mul", a, self.op("rcp", b))
         if op == "mul" and b is not None:
             if a.op == "lit" and a.val == 1.0:
                 return b
@@ -328,6 +332,8 @@ def _expr(n, names):
         return f"{a[0]} * {a[1]}"
     if n.op == "div":
         return f"{a[0]} / {a[1]}"
+    if n.op == "rcp":
+        return f"1.0 / {a[0]}"
     if n.op == "neg":
         return f"-{a[0]}"
     if n.op == "sqrt":
@@ -487,6 +493,8 @@ def emit(name, builder):
             elif n.op == "div":
                 contrib(a[0], f"{bn} / {an[1]}")
                 contrib(a[1], f"-{bn} * {nmap[n.id]} / {an[1]}")
+            elif n.op == "rcp":
+                contrib(a[0], f"-{bn} * {nmap[n.id]} * {nmap[n.id]}")
             elif n.op == "sqrt":
                 contrib(a[0], f"0.5 * {bn} / {nmap[n.id]}")
         return body, adj
@@ -607,6 +615,8 @@ def emit_jvp(name, builder):
                     e = f"{da[0]} / {an[1]}"
                 else:
                     e = f"-{nm[n.id]} * {da[1]} / {an[1]}"
+            elif n.op == "rcp":
+                e = f"-{nm[n.id]} * {nm[n.id]} * {da[0]}"
             elif n.op == "sqrt":
                 e = f"0.5 * {da[0]} / {nm[n.id]}"
             L.append(f"    double d{n.id}[NT];")
