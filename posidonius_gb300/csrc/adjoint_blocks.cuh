@@ -189,10 +189,12 @@ __host__ __device__ __forceinline__ void kepler_vjp(double mu, double dt, const 
     gfun6(s.beta, X, G);
     const double r0 = s.r0;
     const double rr = r0 + s.eta0 * G[1] + s.zeta0 * G[2];
-    const double f = -mu * G[2] / r0;
+    // the two reciprocals every quotient below needs
+    const double ir0 = 1. / r0, irr = 1. / rr;
+    const double f = -mu * G[2] * ir0;
     const double g = dt - mu * G[3];
-    const double fd = -mu * G[1] / (r0 * rr);
-    const double gd = -mu * G[2] / rr;
+    const double fd = -mu * G[1] * (ir0 * irr);
+    const double gd = -mu * G[2] * irr;
     double lf = 0., lg = 0., lfd = 0., lgd = 0.;
     for (int k = 0; k < 3; ++k) {
         lr0[k] = lr1[k] * (1. + f) + fd * lv1[k];
@@ -204,17 +206,17 @@ __host__ __device__ __forceinline__ void kepler_vjp(double mu, double dt, const 
     }
     double lG1 = 0., lG2 = 0., lG3 = 0., lr0s = 0., lrr = 0., leta = 0., lzeta = 0., lbeta = 0.;
     // f = -mu G2 / r0
-    lG2 += -mu / r0 * lf;
-    lr0s += mu * G[2] / (r0 * r0) * lf;
+    lG2 += -mu * ir0 * lf;
+    lr0s += mu * G[2] * (ir0 * ir0) * lf;
     // g = dt - mu G3
     lG3 += -mu * lg;
     // fd = -mu G1 / (r0 rr)
-    lG1 += -mu / (r0 * rr) * lfd;
-    lr0s += mu * G[1] / (r0 * r0 * rr) * lfd;
-    lrr += mu * G[1] / (r0 * rr * rr) * lfd;
+    lG1 += -mu * (ir0 * irr) * lfd;
+    lr0s += mu * G[1] * (ir0 * ir0 * irr) * lfd;
+    lrr += mu * G[1] * (ir0 * irr * irr) * lfd;
     // gd = -mu G2 / rr
-    lG2 += -mu / rr * lgd;
-    lrr += mu * G[2] / (rr * rr) * lgd;
+    lG2 += -mu * irr * lgd;
+    lrr += mu * G[2] * (irr * irr) * lgd;
     // rr = r0 + eta0 G1 + zeta0 G2
     lr0s += lrr;
     leta += G[1] * lrr;
@@ -228,7 +230,7 @@ __host__ __device__ __forceinline__ void kepler_vjp(double mu, double dt, const 
     const double lX = G[0] * lG1 + G[1] * lG2 + G[2] * lG3;
     lbeta += dG1b * lG1 + dG2b * lG2 + dG3b * lG3;
     // implicit root: F(X; r0, eta0, zeta0, beta) = 0, F_X = rr
-    const double w = lX / rr;
+    const double w = lX * irr;
     const double Fb = s.eta0 * dG2b + s.zeta0 * dG3b;
     lr0s += -X * w;
     leta += -G[2] * w;
@@ -238,10 +240,11 @@ __host__ __device__ __forceinline__ void kepler_vjp(double mu, double dt, const 
     lbeta += -r0 * lzeta;
     lr0s += -s.beta * lzeta;
     // beta = 2 mu / r0 - v2
-    lr0s += -2. * mu / (r0 * r0) * lbeta;
+    lr0s += -2. * mu * (ir0 * ir0) * lbeta;
     const double lv2 = -lbeta;
+    const double lr0i = lr0s * ir0;
     for (int k = 0; k < 3; ++k) {
-        lr0[k] += v[k] * leta + r[k] / r0 * lr0s;
+        lr0[k] += v[k] * leta + r[k] * lr0i;
         lv0[k] += r[k] * leta + 2. * v[k] * lv2;
     }
 }
@@ -257,29 +260,30 @@ __host__ __device__ __forceinline__ void kepler_jvp(double mu, double dt, const 
     gfun6(s.beta, X, G);
     const double r0 = s.r0;
     const double rr = r0 + s.eta0 * G[1] + s.zeta0 * G[2];
-    const double f = -mu * G[2] / r0;
+    const double ir0 = 1. / r0, irr = 1. / rr;
+    const double f = -mu * G[2] * ir0;
     const double g = dt - mu * G[3];
-    const double fd = -mu * G[1] / (r0 * rr);
-    const double gd = -mu * G[2] / rr;
-    const double dr0s = (r[0] * dr[0] + r[1] * dr[1] + r[2] * dr[2]) / r0;
+    const double fd = -mu * G[1] * (ir0 * irr);
+    const double gd = -mu * G[2] * irr;
+    const double dr0s = (r[0] * dr[0] + r[1] * dr[1] + r[2] * dr[2]) * ir0;
     const double dv2 = 2. * (v[0] * dv[0] + v[1] * dv[1] + v[2] * dv[2]);
-    const double dbeta = -2. * mu / (r0 * r0) * dr0s - dv2;
+    const double dbeta = -2. * mu * (ir0 * ir0) * dr0s - dv2;
     const double deta = dr[0] * v[0] + dr[1] * v[1] + dr[2] * v[2] + r[0] * dv[0] + r[1] * dv[1] + r[2] * dv[2];
     const double dzeta = -s.beta * dr0s - r0 * dbeta;
     const double dG1b = 0.5 * (G[3] - X * G[2]);
     const double dG2b = 0.5 * (2. * G[4] - X * G[3]);
     const double dG3b = 0.5 * (3. * G[5] - X * G[4]);
     const double Fb = s.eta0 * dG2b + s.zeta0 * dG3b;
-    const double dX = -(X * dr0s + G[2] * deta + G[3] * dzeta + Fb * dbeta) / rr;
+    const double dX = -(X * dr0s + G[2] * deta + G[3] * dzeta + Fb * dbeta) * irr;
     const double dG1 = G[0] * dX + dG1b * dbeta;
     const double dG2 = G[1] * dX + dG2b * dbeta;
     const double dG3 = G[2] * dX + dG3b * dbeta;
     const double drr = dr0s + deta * G[1] + s.eta0 * dG1 + dzeta * G[2] + s.zeta0 * dG2;
-    const double df = -mu * (dG2 * r0 - G[2] * dr0s) / (r0 * r0);
+    const double df = -mu * (dG2 * r0 - G[2] * dr0s) * (ir0 * ir0);
     const double dg = -mu * dG3;
-    const double den = r0 * rr;
-    const double dfd = -mu * (dG1 * den - G[1] * (dr0s * rr + r0 * drr)) / (den * den);
-    const double dgd = -mu * (dG2 * rr - G[2] * drr) / (rr * rr);
+    const double den = r0 * rr, iden = ir0 * irr;
+    const double dfd = -mu * (dG1 * den - G[1] * (dr0s * rr + r0 * drr)) * (iden * iden);
+    const double dgd = -mu * (dG2 * rr - G[2] * drr) * (irr * irr);
     for (int k = 0; k < 3; ++k) {
         dr1[k] = dr[k] + df * r[k] + f * dr[k] + dg * v[k] + g * dv[k];
         dv1[k] = dv[k] + dfd * r[k] + fd * dr[k] + dgd * v[k] + gd * dv[k];
