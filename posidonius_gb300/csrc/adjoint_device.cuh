@@ -59,8 +59,9 @@ constexpr int kACARD = 48;  // host card
 constexpr int kASUMS = 16;
 template <int G>
 struct AdjSmem {
-    // exchange, card, sums, masses, inclusive eta by order position, body by order position
-    static constexpr int doubles = kAXS * G + kACARD + kASUMS + 3 * G;
+    // exchange, card, sums, masses, inclusive eta by order position, body by
+    // order position, 1 / eta and eta_(p-1) / eta_p by order position
+    static constexpr int doubles = kAXS * G + kACARD + kASUMS + 5 * G;
     static constexpr int bytes = doubles * 8;
 };
 
@@ -85,9 +86,10 @@ struct AdjSys {
     unsigned mask;
     bool tides, flat, gr, has, is_host;
     double dt, half_dt, t, last_hist, hist_period;
-    double *xs, *card, *sums, *gm, *geta, *gord;
+    double *xs, *card, *sums, *gm, *geta, *gord, *gieta, *gci;
     // own body constants
     double m, mg, R, moi, sig, k2, k2f, mr, kep_gm, eta_q, eta_prev, M, inv_moi;
+    double iM, i_eta_prev, i_m, i_gmh;  // reciprocals of the Jacobi transforms' divisors
     int tk, fk, gk;
     // state
     double r[3], v[3], L[3], S[3], ev[3], eL[3];
@@ -120,6 +122,8 @@ struct AdjSys {
         gm = sums + kASUMS;
         geta = gm + G;
         gord = geta + G;
+        gieta = gord + G;
+        gci = gieta + G;
         const int64_t ns = D.n_sys;
         n = (int)D.si[(int64_t)POSI_SI_N * ns + s];
         host = (int)D.si[(int64_t)POSI_SI_HOST * ns + s];
@@ -169,6 +173,14 @@ struct AdjSys {
         M = geta[n - 1];
         eta_q = has ? geta[q] : 0.;
         eta_prev = (has && q > 0) ? geta[q - 1] : 0.;
+        if (lane < n) {
+            gieta[lane] = 1. / geta[lane];
+            gci[lane] = lane > 0 ? geta[lane - 1] / geta[lane] : 0.;
+        }
+        iM = 1. / M;
+        i_eta_prev = eta_prev != 0. ? 1. / eta_prev : 0.;
+        i_m = has ? 1. / m : 0.;
+        i_gmh = 1. / gm[host];
         // Kepler GM: host mass_g plus the mass_g of the bodies up to this one in Jacobi order
         sync();
         X(0, lane) = mg;
@@ -510,7 +522,7 @@ struct AdjSys {
                 const int j = ord(p);
                 for (int c = 0; c < 3; ++c) Rs[c] += gm[j] * X(base + c, j);
             }
-            for (int c = 0; c < 3; ++c) wj[c] = is_host ? Rs[c] / M : w[c] - Rs[c] / eta_prev;
+            for (int c = 0; c < 3; ++c) wj[c] = is_host ? Rs[c] * iM : w[c] - Rs[c] * i_eta_prev;
         }
         sync();
     }
@@ -521,11 +533,11 @@ struct AdjSys {
         sync();
         if (has) {
             double acc[3];
-            for (int c = 0; c < 3; ++c) acc[c] = X(base + c, host) / M;
+            for (int c = 0; c < 3; ++c) acc[c] = X(base + c, host) * iM;
             for (int p = n - 1; p >= 1; --p) {
                 if (p <= q && !is_host) break;
                 const int j = ord(p);
-                for (int c = 0; c < 3; ++c) acc[c] -= X(base + c, j) / geta[p - 1];
+                for (int c = 0; c < 3; ++c) acc[c] -= X(base + c, j) * gieta[p - 1];
             }
             for (int c = 0; c < 3; ++c) lw[c] = (is_host ? 0. : lwj[c]) + m * acc[c];
         }
@@ -542,10 +554,10 @@ struct AdjSys {
             const int low = is_host ? 1 : q;
             for (int p = n - 1; p >= low; --p) {
                 const int j = ord(p);
-                const double ci = geta[p - 1] / geta[p];
+                const double ci = gci[p];
                 for (int c = 0; c < 3; ++c) Rs[c] = (Rs[c] - gm[j] * X(base + c, j)) * ci;
             }
-            for (int c = 0; c < 3; ++c) w[c] = is_host ? Rs[c] / m : wj[c] + Rs[c] / eta_prev;
+            for (int c = 0; c < 3; ++c) w[c] = is_host ? Rs[c] * i_m : wj[c] + Rs[c] * i_eta_prev;
         }
         sync();
     }
@@ -556,13 +568,13 @@ struct AdjSys {
         sync();
         if (has) {
             double A[3];
-            for (int c = 0; c < 3; ++c) A[c] = X(base + c, host) / gm[host];
+            for (int c = 0; c < 3; ++c) A[c] = X(base + c, host) * i_gmh;
             const int upto = is_host ? n - 1 : q;
             for (int p = 1; p <= upto; ++p) {
                 const int j = ord(p);
-                const double ci = geta[p - 1] / geta[p];
+                const double ci = gci[p];
                 for (int c = 0; c < 3; ++c) {
-                    A[c] += X(base + c, j) / geta[p - 1];
+                    A[c] += X(base + c, j) * gieta[p - 1];
                     if (p == q) lwj[c] = lw[c] - gm[j] * ci * A[c];
                     A[c] *= ci;
                 }
