@@ -434,7 +434,8 @@ struct AdjSys {
                 double s0 = 0., s1 = 0., s2 = 0., s3 = 0.;
                 for (int j = 0; j < n; ++j) { s0 += X(0, j); s1 += X(1, j); s2 += X(2, j); s3 += X(3, j); }
                 sync();
-                if (s0 / s1 < kDBL_EPSILON_2 && (s3 == 0. || s2 / s3 < kDBL_EPSILON_2)) { K = i + 1; break; }
+                // a / b < eps^2 as a < eps^2 b, the FAST kernel's form of the test
+                if (s0 < kDBL_EPSILON_2 * s1 && (s3 == 0. || s2 < kDBL_EPSILON_2 * s3)) { K = i + 1; break; }
             }
             for (int c = 0; c < 3; ++c) {
                 vc[c] = 0.5 * (v0[c] + vf[c]);

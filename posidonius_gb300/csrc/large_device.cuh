@@ -585,7 +585,7 @@ struct Large {
             }
         }
         prc_ok = true;
-        const double mr = planet ? c.m / hc.m : 0.;
+        const double mr = planet ? c.m * inv_hm : 0.;
         // own and host: original, current, previous-final, previous spin
         double v0[3], L0[3], vc[3], Lc[3], vf[3], Lf[3], pv[3], pL[3], Sp[3], Sc[3], dvc[3], dLc[3];
         double hv0[3], hL0[3], hvc[3], hLc[3], hvf[3], hLf[3], hpv[3], hpL[3], hSp[3], hSc[3], hdvc[3], hdLc[3];
