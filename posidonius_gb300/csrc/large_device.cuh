@@ -669,10 +669,13 @@ struct Large {
                     }
                 }
             }
+            // threads without a body leave their slots at zero and run no FP64
+            // work of their own here: in a body block, a warp without bodies
+            // shares its SMSP's FP64 pipe with a warp of bodies
             double vals[NS] = {};
-            if (primal_role())
+            if (primal_role() && has)
                 for (int q = 0; q < 3; ++q) { vals[q] = mr * aa[q]; vals[3 + q] = th[q]; }
-            if (tn)
+            if (tn && has)
                 for (int q = 0; q < 3; ++q) {
                     vals[tslot(6, q)] = mr * taa[q];
                     vals[tslot(6, 3 + q)] = tth[q];
@@ -707,14 +710,16 @@ struct Large {
             double tot[NS];
             if (!grid_reduce(D, vals, nred, tot, shm, warp_bodies, body_rows, rseq)) return false;
             // the host's outputs and final values, computed by every thread
-            double haa[3], hdl[3];
-            for (int q = 0; q < 3; ++q) {
-                haa[q] = -tot[q]; hdl[q] = tot[3 + q];
-                hdvc[q] = hdt * haa[q] - h.ev[q];
-                hvf[q] = hv0[q] + hdvc[q];
-                hdLc[q] = hdt * hdl[q] - h.eL[q];
-                hLf[q] = hL0[q] + hdLc[q];
-            }
+            // that holds a body (the block's first thread among them)
+            double haa[3] = {0., 0., 0.}, hdl[3] = {0., 0., 0.};
+            if (has)
+                for (int q = 0; q < 3; ++q) {
+                    haa[q] = -tot[q]; hdl[q] = tot[3 + q];
+                    hdvc[q] = hdt * haa[q] - h.ev[q];
+                    hvf[q] = hv0[q] + hdvc[q];
+                    hdLc[q] = hdt * hdl[q] - h.eL[q];
+                    hLf[q] = hL0[q] + hdLc[q];
+                }
             if (is_host)
                 for (int q = 0; q < 3; ++q) { aa[q] = haa[q]; dl[q] = hdl[q]; }
             if (has) for (int q = 0; q < 3; ++q) {
@@ -764,10 +769,13 @@ struct Large {
                         for (int q = 0; q < 6; ++q) tcm[q] = s4[tslot(10, q)];
                 }
                 // the host's terms, added by the block's first thread (a body:
-                // its copy of the host's state is current) and shared, so that
-                // every thread of the block takes the same branch
+                // its copy of the host's state is current) and shared with the
+                // convergence decision, so that every thread of the block takes
+                // the same branch; the test compares a < eps b instead of
+                // dividing (the sums of squares are not negative)
                 const int nsh = cm ? 10 : 4;
                 double* bc = shm + (kBlock / 32) * BP_ROW;
+                __shared__ int converged_s;
                 if (threadIdx.x == 0) {
                     double hc4[4] = {0., 0., 0., 0.};
                     for (int q = 0; q < 3; ++q) {
@@ -782,13 +790,16 @@ struct Large {
                             bc[4 + q] = s4[4 + q];
                             bc[7 + q] = s4[7 + q] + hc.m * hvf[q];
                         }
+                    converged_s = bc[0] < kDBL_EPSILON_2 * bc[1] && (bc[3] == 0. || bc[2] < kDBL_EPSILON_2 * bc[3]);
                 }
                 __syncthreads();
-                for (int k = 0; k < nsh; ++k) s4[k] = bc[k];
+                const bool converged = converged_s != 0;
+                if (cm)
+                    for (int k = 0; k < nsh; ++k) s4[k] = bc[k];
                 __syncthreads();
                 if (cm)
                     for (int q = 0; q < 6; ++q) cm[q] = s4[4 + q];
-                if (s4[0] / s4[1] < kDBL_EPSILON_2 && (s4[3] == 0. || s4[2] / s4[3] < kDBL_EPSILON_2)) break;
+                if (converged) break;
             }
             if (has) for (int q = 0; q < 3; ++q) {
                 vc[q] = 0.5 * (v0[q] + vf[q]);
