@@ -1243,10 +1243,13 @@ struct Large {
         }
         double cm[6], tcm[6] = {0., 0., 0., 0., 0., 0.};
         if (!midpoint(half_dt, cm, tcm)) return false;
-        // inertial -> democratic heliocentric
-        double Rc[3], Vc[3], x[3] = {0., 0., 0.}, u[3] = {0., 0., 0.};
+        // inertial -> democratic heliocentric (the barycentre's terms and the
+        // jump's shift only in threads that hold a body: a warp without
+        // bodies shares a body warp's SMSP and its FP64 pipe)
+        double Rc[3] = {0., 0., 0.}, Vc[3] = {0., 0., 0.}, x[3] = {0., 0., 0.}, u[3] = {0., 0., 0.};
         double tRc[3] = {0., 0., 0.}, tVc[3] = {0., 0., 0.}, tx[3] = {0., 0., 0.}, tu[3] = {0., 0., 0.};
-        for (int q = 0; q < 3; ++q) { Rc[q] = cm[q] * inv_M; Vc[q] = cm[3 + q] * inv_M; }
+        if (has)
+            for (int q = 0; q < 3; ++q) { Rc[q] = cm[q] * inv_M; Vc[q] = cm[3 + q] * inv_M; }
         if (planet)
             for (int q = 0; q < 3; ++q) { x[q] = b.r[q] - h.r[q]; u[q] = b.v[q] - Vc[q]; }
         if (tn)
@@ -1258,16 +1261,18 @@ struct Large {
             }
         // part 1: Kepler drift (and the barycentre's), jump, back to inertial
         kepler(x, u, tx, tu);
-        for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
+        if (has)
+            for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
         if (tn)
             for (int q = 0; q < 3; ++q) tRc[q] += half_dt * tVc[q];
         double S[6], tS_all[AN][6];
         if (!planet_sums(x, u, tx, tu, true, S, tS_all)) return false;
-        double shift[3], tshift[AN][3];
-        for (int q = 0; q < 3; ++q) {
-            shift[q] = half_dt * S[3 + q] * inv_hm;        // jump: dt/2 P / m_host
-            S[q] += shift[q] * (Mtot - hc.m);              // sum_p m_p (x_p + shift)
-        }
+        double shift[3] = {0., 0., 0.}, tshift[AN][3];
+        if (has)
+            for (int q = 0; q < 3; ++q) {
+                shift[q] = half_dt * S[3 + q] * inv_hm;        // jump: dt/2 P / m_host
+                S[q] += shift[q] * (Mtot - hc.m);              // sum_p m_p (x_p + shift)
+            }
         const double P[3] = {S[3], S[4], S[5]};
         if (planet)
             for (int q = 0; q < 3; ++q) x[q] += shift[q];
@@ -1300,7 +1305,8 @@ struct Large {
                 tx[q] += half_dt * tP[q] * inv_hm;
             }
         kepler(x, u, tx, tu);
-        for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
+        if (has)
+            for (int q = 0; q < 3; ++q) Rc[q] += half_dt * Vc[q];
         if (tn)
             for (int q = 0; q < 3; ++q) tRc[q] += half_dt * tVc[q];
         if (!planet_sums(x, u, tx, tu, false, S, tS_all)) return false;
