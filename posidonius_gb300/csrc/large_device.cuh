@@ -801,12 +801,14 @@ struct Large {
                     for (int q = 0; q < 6; ++q) cm[q] = s4[4 + q];
                 if (converged) break;
             }
+            // the midpoints (v0 + vf) / 2 as v0 + dvc / 2 (vf = v0 + dvc): one
+            // FMA instead of an add and a multiply, as in the batched FAST kernel
             if (has) for (int q = 0; q < 3; ++q) {
-                vc[q] = 0.5 * (v0[q] + vf[q]);
-                Lc[q] = 0.5 * (L0[q] + Lf[q]);
+                vc[q] = v0[q] + 0.5 * dvc[q];
+                Lc[q] = L0[q] + 0.5 * dLc[q];
                 Sp[q] = Sc[q];
-                hvc[q] = 0.5 * (hv0[q] + hvf[q]);
-                hLc[q] = 0.5 * (hL0[q] + hLf[q]);
+                hvc[q] = hv0[q] + 0.5 * hdvc[q];
+                hLc[q] = hL0[q] + 0.5 * hdLc[q];
                 hSp[q] = hSc[q];
             }
             if (tn && has)
