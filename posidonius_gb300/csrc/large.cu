@@ -16,7 +16,7 @@ struct posi_large {
            *d_gpart = nullptr,
            *d_bpart = nullptr, *d_tot = nullptr, *d_tan = nullptr, *d_dpos = nullptr;
     int64_t *d_bi = nullptr, *d_si = nullptr;
-    unsigned* d_bar = nullptr;   // [0..1] barrier of the grid, [2..3] of the body blocks
+    unsigned* d_bar = nullptr;   // [0] arrival count of the grid's barriers, [2] of the body blocks'; zeroed per launch
     int* d_ctl = nullptr;
     int* d_err = nullptr;
     unsigned long long* d_bad = nullptr;
@@ -262,6 +262,7 @@ int run_large(posi_large* L, int64_t n_steps, const int32_t* seed_body, const in
     }
     LCK(cudaMemsetAsync(L->d_bad, 0xff, sizeof(unsigned long long), L->stream));
     LCK(cudaMemsetAsync(L->d_ctl, 0, sizeof(int), L->stream));
+    LCK(cudaMemsetAsync(L->d_bar, 0, 4 * sizeof(unsigned), L->stream));  // the barriers' arrival counts
     void* args[] = {&d, &n_steps};
     LCK(cudaEventRecord(L->e0, L->stream));
     LCK(cudaLaunchCooperativeKernel((const void*)posi_many::large_steps_kernel<NT, CO>, dim3(L->grid),

@@ -84,8 +84,8 @@ struct LDev {
     double* gpart;          // [ntile][3 (1 + NT)][n] partial accelerations (and their tangents), per partner tile
     double* bpart;          // [nbb][BP_ROW]
     double* tot;            // [BP_ROW] totals of the last reduction
-    unsigned* bar;          // [2] arrival count, generation: barrier of the whole grid
-    unsigned* bbar;         // [2] the same among the body blocks
+    unsigned* bar;          // arrival count of the whole grid's barriers (zeroed before each launch)
+    unsigned* bbar;         // the same among the body blocks
     int* ctl;               // set to 1 by the body blocks when they have finished (the others then leave)
     int* err;               // error flags (LE_*)
     unsigned long long* bad;  // first failing pair: min over (i n + j) * 4 + code; all ones if none
@@ -145,33 +145,41 @@ __device__ __forceinline__ void block_partial(double* bpart, const double (&vals
     __syncthreads();
 }
 
-// Grid-wide barrier with a bounded wait: thread 0 of each block arrives with
-// a release-acquire add on the arrival count; the last block resets it and
-// releases the generation, the others poll it with acquire loads.  Returns
-// false (and flags the error) when the wait ran out; callers then leave the
-// kernel.
-__device__ bool sync_blocks(const LDev& D, unsigned* ctr, unsigned parts) {
+// Per-block counts of the barriers passed (0: the whole grid's, 1: the body
+// blocks'), zeroed by thread 0 at launch; only thread 0 touches them.
+__device__ __forceinline__ unsigned& barrier_count(int which) {
+    __shared__ unsigned counts[2];
+    return counts[which];
+}
+
+// Barrier among `parts` blocks with a bounded wait.  The arrival count only
+// grows during a launch (the host zeroes it before each): thread 0 of each
+// block adds its arrival with a release reduction, whose result it does not
+// wait for, then polls the count with acquire loads until the k-th barrier's
+// k x parts arrivals are in (a signed difference, so the count may wrap).
+// One trip to L2 and back on the critical path, where an arrive / reset /
+// release-a-generation barrier takes three.  Returns false (and flags the
+// error) when the wait ran out; callers then leave the kernel.
+__device__ bool sync_blocks(const LDev& D, unsigned* ctr, unsigned parts, int which) {
     __shared__ int ok_s;
     __syncthreads();
     if (threadIdx.x == 0) {
-        cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(ctr[0]), gen(ctr[1]);
+        unsigned& k = barrier_count(which);
+        const unsigned target = (++k) * parts;
         cuda::atomic_ref<int, cuda::thread_scope_device> err(*D.err);
-        const unsigned g = gen.load(cuda::memory_order_relaxed);
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
         int ok = 1;
-        if (count.fetch_add(1u, cuda::memory_order_acq_rel) + 1u == parts) {
-            count.store(0u, cuda::memory_order_relaxed);
-            gen.fetch_add(1u, cuda::memory_order_release);
-        } else {
-            const long long start = clock64();
-            while (gen.load(cuda::memory_order_relaxed) == g) {
-                if (clock64() - start > kBarrierWaitCycles || (err.load(cuda::memory_order_relaxed) & LE_BARRIER)) {
-                    ok = 0;
-                    err.fetch_or(LE_BARRIER, cuda::memory_order_relaxed);
-                    break;
-                }
-                __nanosleep(20);
+        const long long start = clock64();
+        for (;;) {
+            unsigned v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+            if ((int)(v - target) >= 0) break;
+            if (clock64() - start > kBarrierWaitCycles || (err.load(cuda::memory_order_relaxed) & LE_BARRIER)) {
+                ok = 0;
+                err.fetch_or(LE_BARRIER, cuda::memory_order_relaxed);
+                break;
             }
-            cuda::atomic_thread_fence(cuda::memory_order_acquire, cuda::thread_scope_device);
+            __nanosleep(20);
         }
         ok_s = ok;
     }
@@ -180,8 +188,8 @@ __device__ bool sync_blocks(const LDev& D, unsigned* ctr, unsigned parts) {
 }
 
 // Barrier of the whole grid (the pair loop's), and of the body blocks alone.
-__device__ __forceinline__ bool grid_barrier(const LDev& D) { return sync_blocks(D, D.bar, gridDim.x); }
-__device__ __forceinline__ bool body_barrier(const LDev& D) { return sync_blocks(D, D.bbar, (unsigned)D.nbb); }
+__device__ __forceinline__ bool grid_barrier(const LDev& D) { return sync_blocks(D, D.bar, gridDim.x, 0); }
+__device__ __forceinline__ bool body_barrier(const LDev& D) { return sync_blocks(D, D.bbar, (unsigned)D.nbb, 1); }
 
 // Sum over the body blocks: every body block writes its partial row, the
 // body blocks meet, and every one of them adds the rows itself, in block
@@ -1331,6 +1339,7 @@ __global__ void __launch_bounds__(kBlock, 1) large_steps_kernel(LDev D, int64_t 
     constexpr bool JAC = CO == POSI_JACOBI;
     static_assert(CO == POSI_DEMOCRATIC_HELIOCENTRIC || NT == 0, "Jacobi and WHDS carry no tangents");
     __shared__ double shm[(kBlock / 32 + 1) * BP_ROW];
+    if (threadIdx.x == 0) barrier_count(0) = barrier_count(1) = 0;
     if ((int)blockIdx.x >= D.nbb) {
         // a block without bodies joins the pair loop of every step and leaves
         // once the body blocks have finished (ctl) or a pair has failed
