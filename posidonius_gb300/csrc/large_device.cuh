@@ -192,10 +192,11 @@ __device__ __forceinline__ bool grid_barrier(const LDev& D) { return sync_blocks
 __device__ __forceinline__ bool body_barrier(const LDev& D) { return sync_blocks(D, D.bbar, (unsigned)D.nbb, 1); }
 
 // Sum over the body blocks: every body block writes its partial row, the
-// body blocks meet, and every one of them adds the rows itself, in block
-// order (warp k mod 8 takes slot k; lane l rows l, l + 32, ...; then a fixed
-// butterfly): the same bits in every block, one barrier and no second round
-// trip through global memory.  The rows alternate between two buffers
+// body blocks meet, and every one of them adds the rows itself in a fixed
+// order (a tree per chunk of eight slots for up to 32 rows; beyond, warp
+// k mod 8 takes slot k, lane l rows l, l + 32, ..., then a butterfly): the
+// same bits in every block, one barrier and no second round trip through
+// global memory.  The rows alternate between two buffers
 // (seq, counted by each caller): a block running ahead writes the next
 // reduction's row while a slower one may still read this one's.
 template <int NS>
@@ -206,11 +207,33 @@ __device__ bool grid_reduce(const LDev& D, const double (&vals)[NS], int nslots,
     block_partial(buf, vals, nslots, shm, warp_active);
     if (!body_barrier(D)) return false;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = warp; k < nslots; k += kBlock / 32) {
-        double x = 0.;
-        for (unsigned b = lane; b < rows; b += 32) x += __ldcg(buf + (size_t)b * BP_ROW + k);
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        if (lane == 0) shm[(kBlock / 32) * BP_ROW + k] = x;
+    if (rows <= 32) {
+        // up to 32 rows: lane 4 s + p of a warp adds rows p, p + 4, ..., p + 28
+        // of slot 8 c + s as a pairwise tree, then the four parts pair up,
+        // ((0 + 1) + (2 + 3)) -- nine FP64 adds per chunk of eight slots, one
+        // chunk per warp, where a shuffle tree takes five per slot; the order
+        // of a slot's sum depends on the rows alone
+        const int s8 = lane >> 2, p = lane & 3;
+        for (int c = warp; c * 8 < nslots; c += kBlock / 32) {
+            const int k = c * 8 + s8;
+            double t[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const unsigned b = (unsigned)(4 * e + p);
+                t[e] = (k < nslots && b < rows) ? __ldcg(buf + (size_t)b * BP_ROW + k) : 0.;
+            }
+            double x = ((t[0] + t[1]) + (t[2] + t[3])) + ((t[4] + t[5]) + (t[6] + t[7]));
+            x += __shfl_down_sync(0xffffffffu, x, 1);
+            x += __shfl_down_sync(0xffffffffu, x, 2);
+            if (p == 0 && k < nslots) shm[(kBlock / 32) * BP_ROW + k] = x;
+        }
+    } else {
+        for (int k = warp; k < nslots; k += kBlock / 32) {
+            double x = 0.;
+            for (unsigned b = lane; b < rows; b += 32) x += __ldcg(buf + (size_t)b * BP_ROW + k);
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) shm[(kBlock / 32) * BP_ROW + k] = x;
+        }
     }
     __syncthreads();
     for (int k = 0; k < nslots; ++k) out[k] = shm[(kBlock / 32) * BP_ROW + k];
